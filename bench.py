@@ -1,0 +1,326 @@
+#!/usr/bin/env python
+"""Benchmark: agent-steps/s of the plain FP64 per-step update.
+
+Workload (default): 300 m x 300 m field, 600 random wall segments, 100,000
+ThreeCircle agents at ~1.1 agents/m^2, cell 3.6 m; one step = the standard
+node tree (orientation, adjusting, agent-agent, agent-wall, adaptive
+velocity Verlet, reset) -- one MultiAgentSimulation.update().  Synthetic,
+seeded inputs (no dataset exists for this path).
+
+Arms:
+  ours       device path through the C ABI.  `value`: state resident in HBM,
+             each timed step one CUDA-graph launch bracketed by CUDA events on
+             the library stream, L2 flushed (256 MiB write) between steps.
+             `e2e`: same steps through the C ABI with pinned host records
+             copied in and out every step, wall clock.
+  reference  the reference algorithm's CPU implementation on the host cores:
+             the C restatement of the reference's numba path (the reference
+             itself is Python + numba, with nothing compiled to run here),
+             agent-parallel over all host threads.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun each rank advances its own replica of the workload (no data
+exchange between ranks); rank 0 prints one JSON line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'agent-steps/s at 100k agents on 1 GB300: plain vs batched; adjoint/forward cost'
+UNIT = 'agent-steps/s'
+
+# Algorithmic float64 operations per unit of work (add, sub, mul, div, sqrt,
+# compare = 1; an elementary function counts the float64 operations of its
+# cd_math.h implementation: hypot 4, exp 31).  Units: unordered candidate
+# pair (bound check), near pair (distance), interacting pair (h < 3: social
+# force, both sides), contact pair (h < 0: contact, both sides), near wall
+# (distance), wall contact, agent (adjusting, timestep, Verlet, shoulders).
+WEIGHTS = {
+    'three_circle': dict(cand=6, near=104, inter=311, contact=48, wall_near=81, wall_contact=30,
+                         agent=64),
+    'circular': dict(cand=6, near=11, inter=139, contact=48, wall_near=27, wall_contact=24,
+                     agent=30),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=5)
+    ap.add_argument('--impl', default='ours', choices=('ours', 'reference'))
+    ap.add_argument('--agents', type=int, default=100_000)
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return ws, rank, local
+
+
+def workload(n_agents):
+    from crowddynamics_gb300 import scenarios as S
+    if n_agents == 100_000:
+        return S.large_field()
+    size = 300.0 * (n_agents / 100_000) ** 0.5
+    return S.large_field(n=n_agents, size=size, n_walls=max(1, int(600 * n_agents / 100_000)))
+
+
+def config_of(scen, nodes_desc):
+    return {'workload': 'large_field_threecircle_100k' if len(scen.agents) == 100_000 else scen.name,
+            'agents': len(scen.agents), 'walls': len(scen.walls), 'body': scen.body,
+            'domain_m': [scen.bounds[2] - scen.bounds[0], scen.bounds[3] - scen.bounds[1]],
+            'cell_size_m': scen.cell_size, 'grid': list(scen.grid[3:]),
+            'nodes': nodes_desc, 'dt_min': scen.dt_min, 'dt_max': scen.dt_max,
+            'l2': 'flushed (256 MiB write) between timed steps',
+            'parallelism': 'replicas (one independent workload per GPU)'}
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix='.csv')
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.Q,
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        out = {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': [], 'samples': 0}
+        if not self.path or not os.path.exists(self.path):
+            return out
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(',')]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), f[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return out
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[k] for _, _, r in rows for k in range(4)
+                          if r[k].lower() in ('active', '1', 'yes')})
+        return {'sm_mhz': statistics.median(r[0] for r in rows), 'sm_max_mhz': max(r[1] for r in rows),
+                'reasons': reasons, 'samples': len(rows)}
+
+
+def algorithmic_flops(scen, counts):
+    """Algorithmic float64 operations of one step of the reference algorithm
+    on this state (pair columns count each unordered pair twice)."""
+    w = WEIGHTS[scen.body]
+    tot = counts.sum(axis=0)
+    return (w['cand'] * tot[0] / 2 + w['near'] * tot[1] / 2 + w['inter'] * tot[2] / 2 +
+            w['contact'] * tot[3] / 2 + w['wall_near'] * tot[4] + w['wall_contact'] * tot[5] +
+            w['agent'] * len(scen.agents))
+
+
+def cpu_sample(scen, nodes_orc, steps, nthreads):
+    """Time `steps` oracle steps of the workload with `nthreads` threads."""
+    from oracle import oracle as O
+    a = scen.agents.copy()
+    grid = O.make_grid(*scen.grid)
+    O.step(a, grid, scen.walls, flags=nodes_orc, dt_min=scen.dt_min, dt_max=scen.dt_max,
+           nthreads=nthreads)                      # warm-up
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        O.step(a, grid, scen.walls, flags=nodes_orc, dt_min=scen.dt_min, dt_max=scen.dt_max,
+               nthreads=nthreads)
+    return time.perf_counter() - t0
+
+
+ORC_NODES = 2 | 4 | 8 | 16 | 32 | 64    # orientation .. reset, no fluctuation
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    from oracle import build as ob
+    ob.build()
+    scen = workload(args.agents)
+    nthreads = os.cpu_count() or 1
+    from oracle import oracle as O
+    a = scen.agents.copy()
+    grid = O.make_grid(*scen.grid)
+    for _ in range(args.warmup):
+        O.step(a, grid, scen.walls, flags=ORC_NODES, dt_min=scen.dt_min, dt_max=scen.dt_max,
+               nthreads=nthreads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.step(a, grid, scen.walls, flags=ORC_NODES, dt_min=scen.dt_min, dt_max=scen.dt_max,
+               nthreads=nthreads)
+    el = time.perf_counter() - t0
+    value = len(scen.agents) * args.steps / el
+    sample = ('%d full steps of the %d-agent workload, C restatement of the reference '
+              'algorithm, agent-parallel OpenMP' % (args.steps, len(scen.agents)))
+    line = {'metric': METRIC, 'value': value, 'unit': UNIT, 'impl': 'reference',
+            'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': el / args.steps * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic (seeded)',
+            'config': config_of(scen, 'orientation+adjusting+agent_agent+agent_obstacle+integrate+reset'),
+            'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': nthreads, 'kind': 'port',
+                             'sample': sample},
+            'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0,
+                    'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, ws, rank, local):
+    import numpy as np
+    import torch
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl')
+    torch.cuda.set_device(local)
+    from crowddynamics_gb300 import build as B
+    B.build()
+    from crowddynamics_gb300 import _native as N
+    from crowddynamics_gb300.engine import batch_from_scenarios
+
+    scen = workload(args.agents)
+    n = len(scen.agents)
+    nodes = N.NODE_ALL & ~N.NODE_FLUCTUATION
+    b, agents, _ = batch_from_scenarios([scen])
+    counts0 = b.pair_counts()
+    peak_gflops = N.measure_fp64_peak()
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device='cuda')
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    # warm-up (graph capture happens here)
+    b.run(max(args.warmup, 3), nodes)
+    barrier()
+    b.set_timing(True)
+    with Clocks(local) as clk:
+        for k in range(args.steps):
+            flush.fill_(k & 0xff)
+            torch.cuda.synchronize()
+            b.run(1, nodes)
+    barrier()
+    kt = b.kernel_time()
+    b.set_timing(False)
+    run_ms = kt['run_ms']
+    if dist is not None:
+        t = torch.tensor([run_ms], device='cuda', dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        run_ms = float(t.item())
+    value = ws * n * args.steps / (run_ms / 1e3)
+    force_ms = kt['force_ms'] / max(kt['force_launches'], 1)
+    counts1 = b.pair_counts()
+    flops = 0.5 * (algorithmic_flops(scen, counts0) + algorithmic_flops(scen, counts1))
+    achieved = flops / (force_ms / 1e3) / 1e12
+    peak = peak_gflops / 1e3
+
+    # end to end through the C ABI with pinned host records
+    host = torch.empty(n * agents.dtype.itemsize, dtype=torch.uint8, pin_memory=True)
+    rec = host.numpy().view(agents.dtype)
+    b.download(rec)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        b.upload(rec)
+        b.run(1, nodes)
+        b.download(rec)
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device='cuda', dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = ws * n * args.steps / e2e_s
+
+    traffic = None
+    tpath = os.path.join(ROOT, 'profiles', 'roofline_inputs.json')
+    if os.path.exists(tpath):
+        try:
+            tr = json.load(open(tpath))
+            if tr.get('workload') == config_of(scen, '')['workload']:
+                traffic = tr.get('k_forces_dram_bytes_per_launch')
+        except (OSError, ValueError):
+            traffic = None
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    line = {'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': run_ms / args.steps, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic (seeded)',
+            'config': config_of(scen, 'orientation+adjusting+agent_agent+agent_obstacle+integrate+reset'),
+            'e2e': {'value': e2e, 'unit': UNIT,
+                    'h2d_bytes_per_step': n * agents.dtype.itemsize,
+                    'd2h_bytes_per_step': n * agents.dtype.itemsize},
+            'gpu_launches': b.kernels_per_step(nodes) * args.steps,
+            'roofline': {'bound': 'fp64', 'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s',
+                         'frac': achieved / peak, 'traffic': traffic,
+                         'kernel': 'k_forces', 'kernel_ms': force_ms,
+                         'flops_per_launch': flops,
+                         'peak_source': 'measured live: FP64 FMA chain kernel (2 flops per FMA)'},
+            'clocks': clk.summary()}
+    if ws == 1 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        steps = 2
+        el = cpu_sample(scen, ORC_NODES, steps, nthreads)
+        line['cpu_baseline'] = {'value': n * steps / el, 'unit': UNIT, 'cores': nthreads,
+                                'kind': 'port',
+                                'sample': '%d steps of the full %d-agent workload, C restatement '
+                                          'of the reference algorithm, OpenMP over %d threads'
+                                          % (steps, n, nthreads)}
+    print(json.dumps(line), flush=True)
+    b.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    if args.impl == 'reference':
+        run_reference(args, ws, rank)
+    else:
+        run_ours(args, ws, rank, local)
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,137 @@
+"""ctypes binding of ``libcdgpu.so`` (the C ABI in ``include/cdgpu.h``).
+
+The library is built in-tree by ``crowddynamics_gb300.build``.  There is no
+fallback: if the library cannot be loaded, or no CUDA device is usable, every
+entry point raises ``DeviceError``.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from crowddynamics_gb300.exceptions import (
+    CellOverflow, CrowdDynamicsException, DeviceError, InvalidType, InvalidValue)
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'libcdgpu.so')
+
+CD_OK = 0
+CD_ERR_INVALID_TYPE = 1
+CD_ERR_INVALID_VALUE = 2
+CD_ERR_CUDA = 3
+CD_ERR_NOT_FINITE = 4
+CD_ERR_CAPACITY = 5
+
+NODE_FLUCTUATION = 1
+NODE_ORIENTATION = 2
+NODE_ADJUSTING = 4
+NODE_AGENT_AGENT = 8
+NODE_AGENT_OBSTACLE = 16
+NODE_INTEGRATE = 32
+NODE_RESET = 64
+NODE_ALL = 127
+
+#: Exported entry points (every function declared in include/cdgpu.h).
+SYMBOLS = (
+    'cd_last_error', 'cd_create', 'cd_destroy', 'cd_upload_agents',
+    'cd_download_agents', 'cd_set_walls', 'cd_set_noise', 'cd_step', 'cd_run',
+    'cd_synchronize', 'cd_get_time', 'cd_get_cell_list', 'cd_pair_counts',
+    'cd_sizes', 'cd_set_timing', 'cd_kernel_time', 'cd_kernels_per_step',
+    'cd_measure_fp64_peak',
+)
+
+#: Columns of cd_pair_counts.
+COUNT_COLS = ('candidates', 'near', 'interacting', 'contact', 'walls_near', 'walls_contact')
+
+
+class Scenario(ctypes.Structure):
+    """``cd_scenario`` of include/cdgpu.h."""
+    _fields_ = [
+        ('agent_begin', ctypes.c_int64), ('agent_count', ctypes.c_int64),
+        ('wall_begin', ctypes.c_int64), ('wall_count', ctypes.c_int64),
+        ('x0', ctypes.c_double), ('y0', ctypes.c_double), ('cell_size', ctypes.c_double),
+        ('nx', ctypes.c_int64), ('ny', ctypes.c_int64),
+        ('dt_min', ctypes.c_double), ('dt_max', ctypes.c_double),
+    ]
+
+
+_lib = None
+
+
+def load(path=None):
+    """Load the library (once) and declare the signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise DeviceError('libcdgpu.so not found at %s; run crowddynamics_gb300.build.build()'
+                          % path)
+    try:
+        L = ctypes.CDLL(path)
+    except OSError as e:
+        raise DeviceError('cannot load libcdgpu.so: %s' % e)
+    P = ctypes.c_void_p
+    i64 = ctypes.c_int64
+    pi64 = ctypes.POINTER(ctypes.c_int64)
+    pd = ctypes.POINTER(ctypes.c_double)
+    sig = {
+        'cd_last_error': (ctypes.c_char_p, [P]),
+        'cd_create': (ctypes.c_int, [ctypes.POINTER(P), ctypes.c_int, i64, ctypes.POINTER(Scenario)]),
+        'cd_destroy': (None, [P]),
+        'cd_upload_agents': (ctypes.c_int, [P, P, i64, i64, pi64]),
+        'cd_download_agents': (ctypes.c_int, [P, P, i64, i64, pi64]),
+        'cd_set_walls': (ctypes.c_int, [P, P, i64]),
+        'cd_set_noise': (ctypes.c_int, [P, P, P]),
+        'cd_step': (ctypes.c_int, [P, ctypes.c_int, pd]),
+        'cd_run': (ctypes.c_int, [P, ctypes.c_int, i64]),
+        'cd_synchronize': (ctypes.c_int, [P]),
+        'cd_get_time': (ctypes.c_int, [P, pd, pd]),
+        'cd_get_cell_list': (ctypes.c_int, [P, pi64, pi64, pi64, pi64]),
+        'cd_pair_counts': (ctypes.c_int, [P, pi64]),
+        'cd_sizes': (ctypes.c_int, [P, pi64, pi64, pi64]),
+        'cd_set_timing': (ctypes.c_int, [P, ctypes.c_int]),
+        'cd_kernel_time': (ctypes.c_int, [P, pd, pi64, pd, pd, pi64]),
+        'cd_kernels_per_step': (ctypes.c_int, [P, ctypes.c_int, pi64]),
+        'cd_measure_fp64_peak': (ctypes.c_int, [pd]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def check(rc, ctx=None):
+    """Map a CD_* status to the reference's exception hierarchy."""
+    if rc == CD_OK:
+        return
+    msg = load().cd_last_error(ctx).decode(errors='replace')
+    if rc == CD_ERR_INVALID_TYPE:
+        raise InvalidType(msg)
+    if rc in (CD_ERR_INVALID_VALUE, CD_ERR_NOT_FINITE):
+        raise InvalidValue(msg)
+    if rc == CD_ERR_CAPACITY:
+        raise CellOverflow(msg)
+    if rc == CD_ERR_CUDA:
+        raise DeviceError(msg)
+    raise CrowdDynamicsException('cdgpu status %d: %s' % (rc, msg))
+
+
+def ptr(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def i64ptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+
+
+def dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def measure_fp64_peak():
+    """FP64 FMA throughput of the current device, GFLOP/s."""
+    g = ctypes.c_double()
+    check(load().cd_measure_fp64_peak(ctypes.byref(g)))
+    return g.value

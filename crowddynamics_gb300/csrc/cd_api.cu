@@ -1,0 +1,687 @@
+// cd_api.cu -- host side of the C ABI declared in include/cdgpu.h.
+//
+// A context owns every device buffer of one batch of scenarios; nothing is
+// allocated per step, so a step (or a captured CUDA graph of one step) only
+// launches kernels and memsets on the context's stream.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cd_internal.cuh"
+#include "../../include/cdgpu.h"
+
+using cdk::StepArgs;
+using cdk::ScenDev;
+
+static thread_local std::string g_create_error;
+
+struct cd_ctx {
+    int body = 0;
+    int64_t n = 0, nw = 0, ncells = 0;
+    int nscen = 0;
+    std::vector<cd_scenario> scen_host;
+    std::vector<ScenDev> scen_dev;
+    std::vector<int> scen_of_host;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+
+    double *colbuf = nullptr;
+    double *col[cdk::NCOL] = {};
+    int *scen_of = nullptr;
+    ScenDev *scen = nullptr;
+    int *key = nullptr, *count = nullptr, *fill = nullptr, *start = nullptr;
+    int *perm_unsorted = nullptr, *perm = nullptr, *scan_scratch = nullptr;
+    double2 *stage = nullptr;
+    float4 *cull = nullptr;
+    double *walls_raw = nullptr, *walls = nullptr;
+    float4 *walls_f = nullptr;
+    int *wall_start = nullptr, *wall_idx = nullptr;
+    int64_t wall_idx_cap = 0;
+    double *noise_f = nullptr, *noise_m = nullptr;
+    bool noise_pending = false;
+    unsigned long long *vmax = nullptr;
+    double *v0max = nullptr, *dt = nullptr, *time_tot = nullptr;
+    int *err = nullptr;
+    int *diag = nullptr;
+
+    char *aos = nullptr;
+    int64_t aos_bytes = 0, itemsize = 0;
+    int64_t off[CD_F_COUNT];
+    bool have_records = false;
+
+    std::vector<double> walls_host;
+    std::vector<double> extent_max;     // per scenario, from the last upload
+    bool walls_dirty = true;
+
+    cudaGraphExec_t graph = nullptr;
+    int graph_nodes = -1;
+
+    bool timing = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs0 = nullptr, evs1 = nullptr;
+    cudaEvent_t evr0 = nullptr, evr1 = nullptr;
+    double force_ms = 0, step_ms = 0, run_ms = 0;
+    int64_t launches = 0, run_steps = 0;
+
+    std::string msg;
+};
+
+namespace {
+
+int fail(cd_ctx *c, int code, const std::string &m) {
+    if (c) c->msg = m;
+    else g_create_error = m;
+    return code;
+}
+
+#define CUDA_OR_FAIL(ctx, call)                                                       \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess)                                                        \
+            return fail((ctx), CD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+StepArgs args_of(cd_ctx *c, int nodes) {
+    StepArgs a;
+    a.n = (int)c->n;
+    a.n_scen = c->nscen;
+    a.n_cells = (int)c->ncells;
+    a.body = c->body;
+    a.nodes = nodes;
+    for (int k = 0; k < cdk::NCOL; ++k) a.col[k] = c->col[k];
+    a.scen_of = c->scen_of;
+    a.scen = c->scen;
+    a.key = c->key;
+    a.count = c->count;
+    a.fill = c->fill;
+    a.start = c->start;
+    a.perm_unsorted = c->perm_unsorted;
+    a.perm = c->perm;
+    a.stage = c->stage;
+    a.cull = c->cull;
+    a.walls = c->walls;
+    a.walls_f = c->walls_f;
+    a.wall_start = c->wall_start;
+    a.wall_idx = c->wall_idx;
+    a.noise_f = c->noise_f;
+    a.noise_m = c->noise_m;
+    a.vmax = c->vmax;
+    a.v0max = c->v0max;
+    a.dt = c->dt;
+    a.time_tot = c->time_tot;
+    a.err = c->err;
+    return a;
+}
+
+template <typename T>
+int dalloc(cd_ctx *c, T **p, int64_t count) {
+    size_t bytes = sizeof(T) * (size_t)std::max<int64_t>(count, 1);
+    cudaError_t e = cudaMalloc((void **)p, bytes);
+    if (e != cudaSuccess)
+        return fail(c, CD_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return CD_OK;
+}
+
+void release(cd_ctx *c) {
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    void *ptrs[] = {c->colbuf, c->scen_of, c->scen, c->key, c->count, c->fill, c->start,
+                    c->perm_unsorted, c->perm, c->scan_scratch, c->stage, c->cull,
+                    c->walls_raw, c->walls, c->walls_f, c->wall_start, c->wall_idx,
+                    c->noise_f, c->noise_m, c->vmax, c->v0max, c->dt, c->time_tot,
+                    c->err, c->diag, c->aos};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->evs0) cudaEventDestroy(c->evs0);
+    if (c->evs1) cudaEventDestroy(c->evs1);
+    if (c->evr0) cudaEventDestroy(c->evr0);
+    if (c->evr1) cudaEventDestroy(c->evr1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+}
+
+// Flat cell range of a coordinate interval along one axis (clamped).
+inline void axis_range(double lo, double hi, double v0, double cell, int64_t n, int64_t &a,
+                       int64_t &b) {
+    auto f = [&](double v) -> int64_t {
+        double q = std::floor((v - v0) / cell);
+        if (q < 0) return 0;
+        if (q > (double)(n - 1)) return n - 1;
+        return (int64_t)q;
+    };
+    a = f(lo);
+    b = f(hi);
+}
+
+// Bin every wall into the cells whose square overlaps the wall's bounding
+// box grown by the scenario's agent extent (+ a margin); per-cell lists stay
+// in ascending wall order, the reference's loop order.
+int bin_walls(cd_ctx *c) {
+    std::vector<int> cnt((size_t)c->ncells + 1, 0);
+    std::vector<std::pair<int, int>> items;
+    for (int s = 0; s < c->nscen; ++s) {
+        const cd_scenario &sc = c->scen_host[s];
+        double ext = c->extent_max.empty() ? 0.0 : c->extent_max[s];
+        double reach = ext + 0.05;
+        c->scen_dev[s].wall_reach = ext + 0.04;
+        int64_t base = c->scen_dev[s].cell_base;
+        for (int64_t w = sc.wall_begin; w < sc.wall_begin + sc.wall_count; ++w) {
+            const double *p = &c->walls_host[4 * w];
+            bool ok = true;
+            for (int k = 0; k < 4; ++k) ok &= std::isfinite(p[k]);
+            if (!ok) continue;     // the reference's distance is NaN: no contact
+            int64_t x0, x1, y0, y1;
+            axis_range(std::min(p[0], p[2]) - reach, std::max(p[0], p[2]) + reach, sc.x0,
+                       sc.cell_size, sc.nx, x0, x1);
+            axis_range(std::min(p[1], p[3]) - reach, std::max(p[1], p[3]) + reach, sc.y0,
+                       sc.cell_size, sc.ny, y0, y1);
+            for (int64_t ix = x0; ix <= x1; ++ix)
+                for (int64_t iy = y0; iy <= y1; ++iy) {
+                    int cell = (int)(base + ix * sc.ny + iy);
+                    items.emplace_back(cell, (int)w);
+                    cnt[cell]++;
+                }
+        }
+    }
+    std::vector<int> startv((size_t)c->ncells + 1, 0);
+    for (int64_t k = 0; k < c->ncells; ++k) startv[k + 1] = startv[k] + cnt[k];
+    std::vector<int> idx(items.size());
+    std::vector<int> fillv((size_t)c->ncells, 0);
+    for (auto &it : items) idx[startv[it.first] + fillv[it.first]++] = it.second;
+    if ((int64_t)idx.size() > c->wall_idx_cap) {
+        if (c->wall_idx) cudaFree(c->wall_idx);
+        c->wall_idx = nullptr;
+        if (int rc = dalloc(c, &c->wall_idx, (int64_t)idx.size())) return rc;
+        c->wall_idx_cap = (int64_t)idx.size();
+        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; c->graph_nodes = -1; }
+    }
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(c->wall_start, startv.data(), sizeof(int) * startv.size(),
+                                    cudaMemcpyHostToDevice, c->stream));
+    if (!idx.empty())
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(c->wall_idx, idx.data(), sizeof(int) * idx.size(),
+                                        cudaMemcpyHostToDevice, c->stream));
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(c->scen, c->scen_dev.data(), sizeof(ScenDev) * c->nscen,
+                                    cudaMemcpyHostToDevice, c->stream));
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    c->walls_dirty = false;
+    return CD_OK;
+}
+
+// Cell list + staging for the current state (no forces).
+void enqueue_cells(cd_ctx *c, const StepArgs &a) {
+    cudaMemsetAsync(c->count, 0, sizeof(int) * c->ncells, c->stream);
+    cudaMemsetAsync(c->fill, 0, sizeof(int) * c->ncells, c->stream);
+    cudaMemsetAsync(c->vmax, 0, sizeof(unsigned long long) * c->nscen, c->stream);
+    cdk::launch_prepare(a, c->stream);
+    if (a.nodes & cdk::N_INTEG) cdk::launch_dt(a, c->stream);
+    cdk::launch_scan(c->count, c->start, (int)c->ncells, c->scan_scratch, c->stream);
+    cdk::launch_scatter(a, c->stream);
+    cdk::launch_gather(a, c->stream);
+}
+
+void enqueue_step(cd_ctx *c, int nodes, bool timed) {
+    StepArgs a = args_of(c, nodes);
+    if (timed) cudaEventRecord(c->evs0, c->stream);
+    enqueue_cells(c, a);
+    if (timed) cudaEventRecord(c->ev0, c->stream);
+    cdk::launch_forces(a, c->stream);
+    if (timed) cudaEventRecord(c->ev1, c->stream);
+    if (timed) cudaEventRecord(c->evs1, c->stream);
+}
+
+int64_t kernels_per_step(const cd_ctx *c, int nodes) {
+    if (c->n == 0) return (nodes & CD_NODE_INTEGRATE) ? 1 : 0;
+    int64_t k = 5;                                      // prepare scatter rank gather forces
+    k += (nodes & CD_NODE_INTEGRATE) ? 1 : 0;           // dt
+    k += cdk::scan_scratch_ints((int)c->ncells) > 1 ? 3 : 1;
+    return k;
+}
+
+int check_device_error(cd_ctx *c) {
+    int h = 0;
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(&h, c->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    if (h) {
+        cudaMemsetAsync(c->err, 0, sizeof(int), c->stream);
+        cudaStreamSynchronize(c->stream);
+        if (h & cdk::ERR_NOT_FINITE)
+            return fail(c, CD_ERR_NOT_FINITE, "an agent position is not finite");
+        return fail(c, CD_ERR_INVALID_VALUE, "device reported error bits " + std::to_string(h));
+    }
+    return CD_OK;
+}
+
+int prepare_step(cd_ctx *c, int nodes) {
+    if (nodes & ~CD_NODE_ALL) return fail(c, CD_ERR_INVALID_VALUE, "unknown node flags");
+    if (!c->have_records) return fail(c, CD_ERR_INVALID_VALUE, "no agents uploaded");
+    if ((nodes & CD_NODE_AGENT_OBSTACLE) && c->walls_dirty && c->nw > 0) {
+        if (c->walls_host.empty())
+            return fail(c, CD_ERR_INVALID_VALUE, "walls declared but cd_set_walls not called");
+        if (int rc = bin_walls(c)) return rc;
+    }
+    return CD_OK;
+}
+
+bool aligned_field(int64_t off, int64_t itemsize, int width) {
+    return off >= 0 && (off % 4) == 0 && off + 8 * width <= itemsize;
+}
+
+// Largest torso-to-skin extent per scenario, from packed records.
+void host_extents(cd_ctx *c, const char *rec, int64_t itemsize, const int64_t *off) {
+    c->extent_max.assign(c->nscen, 0.0);
+    auto rd = [&](int64_t i, int f, int comp) {
+        double v;
+        std::memcpy(&v, rec + i * itemsize + off[f] + 8 * comp, 8);
+        return v;
+    };
+    for (int s = 0; s < c->nscen; ++s) {
+        const cd_scenario &sc = c->scen_host[s];
+        double m = 0.0;
+        for (int64_t i = sc.agent_begin; i < sc.agent_begin + sc.agent_count; ++i) {
+            double e;
+            if (c->body == CD_BODY_CIRCULAR) {
+                e = rd(i, CD_F_RADIUS, 0);
+            } else {
+                double x = rd(i, CD_F_POSITION, 0), y = rd(i, CD_F_POSITION, 1);
+                double rs = rd(i, CD_F_R_S, 0);
+                double l = std::hypot(rd(i, CD_F_POSITION_LS, 0) - x, rd(i, CD_F_POSITION_LS, 1) - y) + rs;
+                double r = std::hypot(rd(i, CD_F_POSITION_RS, 0) - x, rd(i, CD_F_POSITION_RS, 1) - y) + rs;
+                e = std::max(std::max(rd(i, CD_F_R_T, 0), rd(i, CD_F_R_TS, 0) + rs), std::max(l, r));
+            }
+            if (std::isfinite(e)) m = std::max(m, e);
+        }
+        if (m > c->extent_max[s]) c->extent_max[s] = m;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *cd_last_error(const cd_ctx *ctx) {
+    return ctx ? ctx->msg.c_str() : g_create_error.c_str();
+}
+
+int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenario *scen) {
+    if (!out) return fail(nullptr, CD_ERR_INVALID_VALUE, "out is NULL");
+    *out = nullptr;
+    if (body_type != CD_BODY_CIRCULAR && body_type != CD_BODY_THREE_CIRCLE)
+        return fail(nullptr, CD_ERR_INVALID_TYPE, "unknown body type");
+    if (n_scenarios < 1 || !scen) return fail(nullptr, CD_ERR_INVALID_VALUE, "need >= 1 scenario");
+    int64_t n = 0, nw = 0, ncells = 0;
+    for (int64_t s = 0; s < n_scenarios; ++s) {
+        const cd_scenario &sc = scen[s];
+        if (sc.agent_begin != n || sc.agent_count < 0 || sc.wall_begin != nw || sc.wall_count < 0)
+            return fail(nullptr, CD_ERR_INVALID_VALUE, "agent/wall ranges must tile in order");
+        if (!(sc.cell_size > 0) || !std::isfinite(sc.cell_size) || !std::isfinite(sc.x0) ||
+            !std::isfinite(sc.y0) || sc.nx < 1 || sc.ny < 1)
+            return fail(nullptr, CD_ERR_INVALID_VALUE, "bad cell grid");
+        if (!(sc.dt_min >= 0) || !(sc.dt_max >= 0) || !std::isfinite(sc.dt_max))
+            return fail(nullptr, CD_ERR_INVALID_VALUE, "bad timestep bounds");
+        n += sc.agent_count;
+        nw += sc.wall_count;
+        ncells += sc.nx * sc.ny;
+        if (sc.nx > (1 << 30) || sc.ny > (1 << 30) || ncells > (int64_t)INT32_MAX - 1)
+            return fail(nullptr, CD_ERR_CAPACITY, "too many cells");
+    }
+    if (n > (int64_t)INT32_MAX / 16 || nw > (int64_t)INT32_MAX / 16)
+        return fail(nullptr, CD_ERR_CAPACITY, "too many agents or walls");
+
+    cd_ctx *c = new cd_ctx();
+    c->body = body_type;
+    c->n = n;
+    c->nw = nw;
+    c->ncells = ncells;
+    c->nscen = (int)n_scenarios;
+    c->scen_host.assign(scen, scen + n_scenarios);
+    c->scen_dev.resize(n_scenarios);
+    c->scen_of_host.resize(std::max<int64_t>(n, 1));
+    std::fill(c->off, c->off + CD_F_COUNT, -1);
+    int64_t base = 0;
+    for (int64_t s = 0; s < n_scenarios; ++s) {
+        const cd_scenario &sc = scen[s];
+        ScenDev &d = c->scen_dev[s];
+        d.x0 = sc.x0; d.y0 = sc.y0; d.cell = sc.cell_size;
+        d.dt_min = sc.dt_min; d.dt_max = sc.dt_max;
+        d.wall_reach = 0.0;
+        d.nx = (int)sc.nx; d.ny = (int)sc.ny;
+        d.cell_base = (int)base;
+        d.agent_begin = (int)sc.agent_begin; d.agent_count = (int)sc.agent_count;
+        d.wall_begin = (int)sc.wall_begin; d.wall_count = (int)sc.wall_count;
+        base += sc.nx * sc.ny;
+        for (int64_t i = sc.agent_begin; i < sc.agent_begin + sc.agent_count; ++i)
+            c->scen_of_host[i] = (int)s;
+    }
+    int rc = CD_OK;
+    auto step = [&](int r) { if (r && !rc) rc = r; return rc == CD_OK; };
+    cudaGetDevice(&c->device);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+        rc = fail(c, CD_ERR_CUDA, "cudaStreamCreate failed");
+    const int64_t npad = std::max<int64_t>(n, 1);
+    if (rc == CD_OK && step(dalloc(c, &c->colbuf, npad * cdk::NCOL)))
+        for (int k = 0; k < cdk::NCOL; ++k) c->col[k] = c->colbuf + k * npad;
+    const int sq = body_type == CD_BODY_CIRCULAR ? cdk::STAGE_Q_CIRC : cdk::STAGE_Q_TC;
+    step(dalloc(c, &c->scen_of, n));
+    step(dalloc(c, &c->scen, n_scenarios));
+    step(dalloc(c, &c->key, n));
+    step(dalloc(c, &c->count, ncells));
+    step(dalloc(c, &c->fill, ncells));
+    step(dalloc(c, &c->start, ncells + 1));
+    step(dalloc(c, &c->perm_unsorted, n));
+    step(dalloc(c, &c->perm, n));
+    step(dalloc(c, &c->scan_scratch, cdk::scan_scratch_ints((int)ncells)));
+    step(dalloc(c, &c->stage, n * sq));
+    step(dalloc(c, &c->cull, n));
+    step(dalloc(c, &c->walls_raw, nw * 4));
+    step(dalloc(c, &c->walls, nw * cdk::WALL_D));
+    step(dalloc(c, &c->walls_f, nw));
+    step(dalloc(c, &c->wall_start, ncells + 1));
+    step(dalloc(c, &c->noise_f, 2 * n));
+    step(dalloc(c, &c->noise_m, n));
+    step(dalloc(c, &c->vmax, n_scenarios));
+    step(dalloc(c, &c->v0max, n_scenarios));
+    step(dalloc(c, &c->dt, n_scenarios));
+    step(dalloc(c, &c->time_tot, n_scenarios));
+    step(dalloc(c, &c->err, 1));
+    step(dalloc(c, &c->diag, (int64_t)CD_COUNT_COLS * n));
+    if (rc == CD_OK) {
+        cudaMemcpy(c->scen_of, c->scen_of_host.data(), sizeof(int) * npad, cudaMemcpyHostToDevice);
+        cudaMemcpy(c->scen, c->scen_dev.data(), sizeof(ScenDev) * n_scenarios, cudaMemcpyHostToDevice);
+        cudaMemset(c->colbuf, 0, sizeof(double) * npad * cdk::NCOL);
+        cudaMemset(c->time_tot, 0, sizeof(double) * n_scenarios);
+        cudaMemset(c->dt, 0, sizeof(double) * n_scenarios);
+        cudaMemset(c->err, 0, sizeof(int));
+        cudaMemset(c->wall_start, 0, sizeof(int) * (ncells + 1));
+        cudaEventCreate(&c->ev0);
+        cudaEventCreate(&c->ev1);
+        cudaEventCreate(&c->evs0);
+        cudaEventCreate(&c->evs1);
+        cudaEventCreate(&c->evr0);
+        cudaEventCreate(&c->evr1);
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) rc = fail(c, CD_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (rc != CD_OK) {
+        g_create_error = c->msg;
+        release(c);
+        delete c;
+        return rc;
+    }
+    c->walls_dirty = nw > 0;
+    *out = c;
+    return CD_OK;
+}
+
+void cd_destroy(cd_ctx *ctx) {
+    if (!ctx) return;
+    cudaStreamSynchronize(ctx->stream);
+    release(ctx);
+    delete ctx;
+}
+
+int cd_upload_agents(cd_ctx *c, const void *records, int64_t n, int64_t itemsize,
+                     const int64_t *off) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (n != c->n) return fail(c, CD_ERR_INVALID_VALUE, "agent count differs from the context");
+    if (itemsize <= 0 || !off || (n > 0 && !records))
+        return fail(c, CD_ERR_INVALID_VALUE, "bad records");
+    static const int need_circ[] = {CD_F_POSITION, CD_F_VELOCITY, CD_F_TARGET_DIRECTION, CD_F_FORCE,
+                                    CD_F_FORCE_PREV, CD_F_RADIUS, CD_F_MASS, CD_F_TARGET_VELOCITY,
+                                    CD_F_TAU_ADJ, CD_F_K_SOC, CD_F_TAU_0, CD_F_MU, CD_F_KAPPA,
+                                    CD_F_DAMPING};
+    static const int need_tc[] = {CD_F_R_T, CD_F_R_S, CD_F_R_TS, CD_F_INERTIA_ROT,
+                                  CD_F_TARGET_ANGULAR_VELOCITY, CD_F_POSITION_LS, CD_F_POSITION_RS,
+                                  CD_F_ORIENTATION, CD_F_ANGULAR_VELOCITY, CD_F_TARGET_ORIENTATION,
+                                  CD_F_TORQUE, CD_F_TORQUE_PREV, CD_F_TAU_ROT};
+    for (int f : need_circ) {
+        int width = (f <= CD_F_FORCE_PREV) ? 2 : 1;
+        if (!aligned_field(off[f], itemsize, width))
+            return fail(c, CD_ERR_INVALID_TYPE, "record lacks a required, 4-byte aligned field");
+    }
+    if (c->body == CD_BODY_THREE_CIRCLE)
+        for (int f : need_tc) {
+            int width = (f == CD_F_POSITION_LS || f == CD_F_POSITION_RS) ? 2 : 1;
+            if (!aligned_field(off[f], itemsize, width))
+                return fail(c, CD_ERR_INVALID_TYPE, "record lacks a ThreeCircle field");
+        }
+    if (itemsize % 4) return fail(c, CD_ERR_INVALID_TYPE, "record size must be a multiple of 4");
+    int64_t bytes = n * itemsize;
+    if (bytes > c->aos_bytes) {
+        if (c->aos) cudaFree(c->aos);
+        c->aos = nullptr;
+        if (int rc = dalloc(c, &c->aos, bytes)) return rc;
+        c->aos_bytes = bytes;
+    }
+    c->itemsize = itemsize;
+    std::memcpy(c->off, off, sizeof(int64_t) * CD_F_COUNT);
+    if (n > 0) {
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(c->aos, records, bytes, cudaMemcpyHostToDevice, c->stream));
+        long long offl[CD_F_COUNT];
+        for (int k = 0; k < CD_F_COUNT; ++k) offl[k] = off[k];
+        cdk::launch_aos_to_soa(c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
+    }
+    StepArgs a = args_of(c, 0);
+    cdk::launch_v0max(a, c->v0max, c->stream);
+    // Wall bins depend on the agents' extent.
+    std::vector<double> prev = c->extent_max;
+    host_extents(c, static_cast<const char *>(records), itemsize, off);
+    for (int s = 0; s < c->nscen; ++s)
+        if (prev.empty() || c->extent_max[s] > prev[s]) c->walls_dirty = true;
+    if (!c->walls_dirty && !prev.empty()) c->extent_max = prev;
+    c->have_records = true;
+    CUDA_OR_FAIL(c, cudaGetLastError());
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    return CD_OK;
+}
+
+int cd_download_agents(cd_ctx *c, void *records, int64_t n, int64_t itemsize, const int64_t *off) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (!c->have_records) return fail(c, CD_ERR_INVALID_VALUE, "no agents uploaded");
+    if (n != c->n || itemsize != c->itemsize || !off ||
+        std::memcmp(off, c->off, sizeof(int64_t) * CD_F_COUNT) != 0)
+        return fail(c, CD_ERR_INVALID_VALUE, "record layout differs from the upload");
+    if (n == 0) return CD_OK;
+    long long offl[CD_F_COUNT];
+    for (int k = 0; k < CD_F_COUNT; ++k) offl[k] = off[k];
+    cdk::launch_soa_to_aos(c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(records, c->aos, n * itemsize, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_OR_FAIL(c, cudaGetLastError());
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    return check_device_error(c);
+}
+
+int cd_set_walls(cd_ctx *c, const double *walls, int64_t n_walls) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (n_walls != c->nw) return fail(c, CD_ERR_INVALID_VALUE, "wall count differs from the context");
+    if (n_walls > 0 && !walls) return fail(c, CD_ERR_INVALID_VALUE, "walls is NULL");
+    c->walls_host.assign(walls, walls + 4 * n_walls);
+    if (n_walls > 0) {
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(c->walls_raw, walls, sizeof(double) * 4 * n_walls,
+                                        cudaMemcpyHostToDevice, c->stream));
+        cdk::launch_wall_prep(c->walls_raw, c->walls, c->walls_f, (int)n_walls, c->stream);
+    }
+    c->walls_dirty = true;
+    CUDA_OR_FAIL(c, cudaGetLastError());
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    return CD_OK;
+}
+
+int cd_set_noise(cd_ctx *c, const double *force, const double *torque) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (c->n > 0 && !force) return fail(c, CD_ERR_INVALID_VALUE, "force noise is NULL");
+    if (c->n > 0) {
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(c->noise_f, force, sizeof(double) * 2 * c->n,
+                                        cudaMemcpyHostToDevice, c->stream));
+        if (torque)
+            CUDA_OR_FAIL(c, cudaMemcpyAsync(c->noise_m, torque, sizeof(double) * c->n,
+                                            cudaMemcpyHostToDevice, c->stream));
+        else
+            CUDA_OR_FAIL(c, cudaMemsetAsync(c->noise_m, 0, sizeof(double) * c->n, c->stream));
+    }
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    c->noise_pending = true;
+    return CD_OK;
+}
+
+int cd_step(cd_ctx *c, int nodes, double *dt) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (int rc = prepare_step(c, nodes)) return rc;
+    if ((nodes & CD_NODE_FLUCTUATION) && !c->noise_pending)
+        return fail(c, CD_ERR_INVALID_VALUE, "cd_set_noise must precede a step with fluctuation");
+    enqueue_step(c, nodes, c->timing);
+    if (nodes & CD_NODE_FLUCTUATION) c->noise_pending = false;
+    CUDA_OR_FAIL(c, cudaGetLastError());
+    if (c->timing) {
+        CUDA_OR_FAIL(c, cudaEventSynchronize(c->evs1));
+        float ms = 0, sms = 0;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        cudaEventElapsedTime(&sms, c->evs0, c->evs1);
+        c->force_ms += ms;
+        c->step_ms += sms;
+        c->launches += 1;
+    }
+    if (dt) {
+        if (int rc = check_device_error(c)) return rc;
+        CUDA_OR_FAIL(c, cudaMemcpy(dt, c->dt, sizeof(double) * c->nscen, cudaMemcpyDeviceToHost));
+    }
+    return CD_OK;
+}
+
+int cd_run(cd_ctx *c, int nodes, int64_t steps) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (nodes & CD_NODE_FLUCTUATION)
+        return fail(c, CD_ERR_INVALID_VALUE, "cd_run cannot consume per-step host noise");
+    if (steps < 0) return fail(c, CD_ERR_INVALID_VALUE, "negative step count");
+    if (int rc = prepare_step(c, nodes)) return rc;
+    if (!c->graph || c->graph_nodes != nodes) {
+        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+        cudaGraph_t g;
+        CUDA_OR_FAIL(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_step(c, nodes, true);     // event records become graph nodes
+        cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        if (e != cudaSuccess) return fail(c, CD_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&c->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(c, CD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        c->graph_nodes = nodes;
+    }
+    if (c->timing) cudaEventRecord(c->evr0, c->stream);
+    for (int64_t k = 0; k < steps; ++k) CUDA_OR_FAIL(c, cudaGraphLaunch(c->graph, c->stream));
+    if (c->timing) {
+        cudaEventRecord(c->evr1, c->stream);
+        CUDA_OR_FAIL(c, cudaEventSynchronize(c->evr1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c->evr0, c->evr1);
+        c->run_ms += ms;
+        c->run_steps += steps;
+        if (steps == 1) {      // the graph's own events bracket its force kernel
+            float fms = 0;
+            cudaEventElapsedTime(&fms, c->ev0, c->ev1);
+            c->force_ms += fms;
+            c->launches += 1;
+        }
+    }
+    return check_device_error(c);
+}
+
+int cd_synchronize(cd_ctx *c) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    return check_device_error(c);
+}
+
+int cd_get_time(cd_ctx *c, double *dt, double *time_tot) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    if (dt) CUDA_OR_FAIL(c, cudaMemcpy(dt, c->dt, sizeof(double) * c->nscen, cudaMemcpyDeviceToHost));
+    if (time_tot)
+        CUDA_OR_FAIL(c, cudaMemcpy(time_tot, c->time_tot, sizeof(double) * c->nscen, cudaMemcpyDeviceToHost));
+    return CD_OK;
+}
+
+int cd_get_cell_list(cd_ctx *c, int64_t *keys, int64_t *order, int64_t *cells_count,
+                     int64_t *cells_offset) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    std::vector<int> k(std::max<int64_t>(c->n, 1)), p(std::max<int64_t>(c->n, 1)),
+        st((size_t)c->ncells + 1);
+    CUDA_OR_FAIL(c, cudaMemcpy(k.data(), c->key, sizeof(int) * c->n, cudaMemcpyDeviceToHost));
+    CUDA_OR_FAIL(c, cudaMemcpy(p.data(), c->perm, sizeof(int) * c->n, cudaMemcpyDeviceToHost));
+    CUDA_OR_FAIL(c, cudaMemcpy(st.data(), c->start, sizeof(int) * (c->ncells + 1), cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < c->n; ++i) {
+        int s = c->scen_of_host[i];
+        if (keys) keys[i] = k[i] - c->scen_dev[s].cell_base;
+        if (order) order[i] = p[i];
+    }
+    for (int64_t q = 0; q < c->ncells; ++q) {
+        if (cells_count) cells_count[q] = st[q + 1] - st[q];
+        if (cells_offset) cells_offset[q] = st[q];
+    }
+    return CD_OK;
+}
+
+int cd_pair_counts(cd_ctx *c, int64_t *counts) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (!c->have_records) return fail(c, CD_ERR_INVALID_VALUE, "no agents uploaded");
+    if (c->walls_dirty && c->nw > 0) {
+        if (c->walls_host.empty())
+            return fail(c, CD_ERR_INVALID_VALUE, "walls declared but cd_set_walls not called");
+        if (int rc = bin_walls(c)) return rc;
+    }
+    StepArgs a = args_of(c, CD_NODE_AGENT_AGENT | CD_NODE_AGENT_OBSTACLE);
+    enqueue_cells(c, a);
+    cdk::launch_pair_counts(a, c->diag, c->stream);
+    CUDA_OR_FAIL(c, cudaGetLastError());
+    if (int rc = check_device_error(c)) return rc;
+    std::vector<int> h((size_t)CD_COUNT_COLS * std::max<int64_t>(c->n, 1));
+    CUDA_OR_FAIL(c, cudaMemcpy(h.data(), c->diag, sizeof(int) * CD_COUNT_COLS * c->n,
+                               cudaMemcpyDeviceToHost));
+    if (counts)
+        for (int64_t k = 0; k < (int64_t)CD_COUNT_COLS * c->n; ++k) counts[k] = h[k];
+    return CD_OK;
+}
+
+int cd_sizes(const cd_ctx *c, int64_t *n_agents, int64_t *n_walls, int64_t *n_cells) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (n_agents) *n_agents = c->n;
+    if (n_walls) *n_walls = c->nw;
+    if (n_cells) *n_cells = c->ncells;
+    return CD_OK;
+}
+
+int cd_set_timing(cd_ctx *c, int enable) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    c->timing = enable != 0;
+    c->force_ms = c->step_ms = c->run_ms = 0;
+    c->launches = c->run_steps = 0;
+    return CD_OK;
+}
+
+int cd_kernel_time(cd_ctx *c, double *force_ms, int64_t *force_launches, double *step_ms,
+                   double *run_ms, int64_t *run_steps) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (force_ms) *force_ms = c->force_ms;
+    if (force_launches) *force_launches = c->launches;
+    if (step_ms) *step_ms = c->step_ms;
+    if (run_ms) *run_ms = c->run_ms;
+    if (run_steps) *run_steps = c->run_steps;
+    return CD_OK;
+}
+
+int cd_kernels_per_step(const cd_ctx *c, int nodes, int64_t *kernels) {
+    if (!c || !kernels) return fail(nullptr, CD_ERR_INVALID_VALUE, "NULL argument");
+    *kernels = kernels_per_step(c, nodes);
+    return CD_OK;
+}
+
+int cd_measure_fp64_peak(double *gflops) {
+    if (!gflops) return fail(nullptr, CD_ERR_INVALID_VALUE, "gflops is NULL");
+    double g = cdk::fp64_peak_gflops();
+    if (g <= 0) return fail(nullptr, CD_ERR_CUDA, "FP64 peak measurement failed");
+    *gflops = g;
+    return CD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,83 @@
+// cd_internal.cuh -- shared device-side types of libcdgpu (not part of the ABI).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace cdk {
+
+// Primary agent state: one float64 column per field, agents in batch order.
+enum Col {
+    X, Y, VX, VY, FX, FY, FPX, FPY, E0X, E0Y, R, MASS, TAU_ADJ, K_SOC, TAU0,
+    MU, KAPPA, DAMP, V0,
+    XLS, YLS, XRS, YRS, RT, RS, RTS, INERTIA, W0, PHI, OMEGA, PHI0, TORQUE,
+    TORQUE_PREV, TAU_ROT,
+    NCOL
+};
+
+// Staged neighbour records (cell-sorted order), in double2 units.
+constexpr int STAGE_Q_CIRC = 6;    // (x,y)(vx,vy)(r,m)(k,tau0)(mu,kappa)(damp,-)
+constexpr int STAGE_Q_TC = 10;     // (x,y)(xls,yls)(xrs,yrs)(vx,vy)(rt,rs)
+                                   // (rts,m)(k,tau0)(mu,kappa)(damp,sin)(cos,-)
+constexpr int WALL_D = 8;          // p0x p0y p1x p1y tx ty lw -
+
+// Device error bits (StepArgs::err).
+constexpr int ERR_NOT_FINITE = 1;
+
+// Node flags (mirror CD_NODE_* of include/cdgpu.h).
+constexpr int N_FLUCT = 1, N_ORIENT = 2, N_ADJUST = 4, N_AGENT = 8,
+              N_WALL = 16, N_INTEG = 32, N_RESET = 64;
+
+struct ScenDev {
+    double x0, y0, cell;
+    double dt_min, dt_max;
+    double wall_reach;          // agent extent the wall bins were built for
+    int nx, ny;
+    int cell_base;              // first flat cell of this scenario
+    int agent_begin, agent_count;
+    int wall_begin, wall_count;
+};
+
+struct StepArgs {
+    int n, n_scen, n_cells, body, nodes;
+    double *col[NCOL];
+    const int *scen_of;          // scenario of every agent
+    const ScenDev *scen;
+    // cell list
+    int *key;                    // flat cell (batch-global) per agent
+    int *count, *fill, *start;   // per cell; start has n_cells + 1 entries
+    int *perm_unsorted, *perm;   // slot -> agent
+    // staging (cell-sorted)
+    double2 *stage;
+    float4 *cull;                // (x, y, extent, -) as float
+    // walls
+    const double *walls;         // WALL_D doubles per wall
+    const float4 *walls_f;       // (p0x, p0y, p1x, p1y) as float
+    const int *wall_start, *wall_idx;   // per-cell CSR of wall ids
+    // fluctuation (host-drawn)
+    const double *noise_f, *noise_m;
+    // timestep
+    unsigned long long *vmax;    // per scenario, ordered bits of max |v|
+    const double *v0max;         // per scenario max target_velocity
+    double *dt, *time_tot;       // per scenario
+    int *err;
+};
+
+// Launchers (cd_kernels.cu)
+void launch_prepare(const StepArgs &a, cudaStream_t s);
+void launch_dt(const StepArgs &a, cudaStream_t s);
+int scan_scratch_ints(int n);
+void launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s);
+void launch_scatter(const StepArgs &a, cudaStream_t s);
+void launch_gather(const StepArgs &a, cudaStream_t s);
+void launch_forces(const StepArgs &a, cudaStream_t s);
+void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s);
+void launch_v0max(const StepArgs &a, double *v0max_out, cudaStream_t s);
+void launch_wall_prep(const double *raw, double *walls, float4 *walls_f, int nw,
+                      cudaStream_t s);
+void launch_aos_to_soa(const char *aos, long long itemsize, const long long *off,
+                       int n, int body, double *const *col, cudaStream_t s);
+void launch_soa_to_aos(char *aos, long long itemsize, const long long *off,
+                       int n, int body, const double *const *col, cudaStream_t s);
+double fp64_peak_gflops();
+
+}  // namespace cdk

@@ -1,0 +1,1017 @@
+// cd_kernels.cu -- device kernels of libcdgpu (sm_103a, float64 arithmetic).
+//
+// One step of the reference's MultiAgentSimulation.update()
+// (crowddynamics/simulation/multiagent.py:51-55) runs as:
+//   prepare  : cell key + per-cell count of every agent, per-scenario max |v|
+//   dt       : adaptive timestep per scenario (core/integrator.py:29-97)
+//   scan     : exclusive prefix sum of cell counts -> cell start offsets
+//   scatter  : agents into cells (atomic), then a stable per-cell rank so that
+//              each cell lists its agents in ascending index order
+//   gather   : cell-sorted staging copy of the fields the pair loop reads, plus
+//              a float32 (x, y, extent) record for the conservative pre-check
+//   forces   : per agent: noise + orientation + adjusting + agent-agent +
+//              agent-wall, then velocity Verlet, shoulders and reset
+//
+// The library is compiled without fused multiply-add contraction and uses the
+// elementary functions of cd_math.h, so every float64 result rounds exactly
+// as the oracle's does; agent-agent contributions are summed per agent in the
+// reference's visiting order (3 x 3 cells in (dx, dy) lexicographic order,
+// each cell in ascending agent order), so a step is bit-identical to the
+// oracle's and multi-step rollouts stay identical.
+//
+// Float64 is the only arithmetic that reaches a result.  Float32 is used for
+// one thing: skipping agent pairs (and wall segments) whose centre distance
+// exceeds the social cut-off plus both extents by a margin far above float32
+// rounding, i.e. pairs the reference evaluates to exactly no contribution.
+#include <cstdint>
+#include <cmath>
+#include "cd_internal.cuh"
+#include "cd_math.h"
+
+namespace cdk {
+
+namespace {
+
+constexpr double SIGTH_SOC = 3.0;      // core/interactions.py:45
+constexpr double F_SOC_MAX = 2e3;      // core/motion/power_law.py:52
+constexpr double TAU_MAX = 30.0;       // core/motion/power_law.py:243
+constexpr double PI_D = 3.141592653589793;
+constexpr float CULL_MARGIN = 0.01f;   // metres, >> float32 error at 1e4 m
+constexpr int NT_FORCES = 128;
+constexpr int LIST_CAP = 64;           // survivors staged per thread per pass
+
+// ---- float64 helpers restating core/vector2D.py ------------------------
+
+// Python float modulo (numba follows CPython's float_rem).
+__device__ __forceinline__ double py_mod(double x, double y) {
+    double m = fmod(x, y);
+    if (m != 0.0) {
+        if ((y < 0) != (m < 0)) m += y;
+    } else {
+        m = copysign(0.0, y);
+    }
+    return m;
+}
+
+// wrap_to_pi, core/vector2D.py:8-36
+__device__ __forceinline__ double wrap_to_pi(double rad) {
+    double r = py_mod(rad, 2 * PI_D);
+    if (rad < 0 && r == PI_D) return -PI_D;
+    if (r > PI_D) return r - (2 * PI_D);
+    return r;
+}
+
+__device__ __forceinline__ double np_sign(double x) {
+    return x > 0 ? 1.0 : (x < 0 ? -1.0 : x);
+}
+
+// truncate, core/vector2D.py:166-187
+__device__ __forceinline__ void truncate2(double &vx, double &vy, double l) {
+    double vlen = cdm_hypot(vx, vy);
+    if (vlen > l) {
+        double s = l / vlen;
+        vx = vx * s;
+        vy = vy * s;
+    }
+}
+
+// magnitude, core/motion/power_law.py:83-102
+__device__ __forceinline__ double magnitude(double tau, double tau_0) {
+    return (2.0 / tau + 1.0 / tau_0) * cdm_exp(-tau / tau_0) / (tau * tau);
+}
+
+// force_contact, core/motion/contact.py:12-48; t = rotate270(n) = (n.y, -n.x)
+__device__ __forceinline__ void force_contact(double h, double nx, double ny,
+                                              double vx, double vy, double mu,
+                                              double kappa, double damping,
+                                              double &cx, double &cy) {
+    double tx = ny, ty = -nx;
+    double vt = vx * tx + vy * ty;
+    double vn = vx * nx + vy * ny;
+    cx = (-h) * (mu * nx - (kappa * vt) * tx) + (damping * vn) * nx;
+    cy = (-h) * (mu * ny - (kappa * vt) * ty) + (damping * vn) * ny;
+}
+
+// Ordered-bits encoding of a non-negative double for atomicMax.
+__device__ __forceinline__ unsigned long long ord_bits(double v) {
+    return (unsigned long long)__double_as_longlong(v);
+}
+
+__device__ __forceinline__ int axis_cell(double v, double v0, double cell, int n) {
+    double q = floor((v - v0) / cell);
+    if (q < 0.0) return 0;
+    if (q > (double)(n - 1)) return n - 1;
+    return (int)q;
+}
+
+// ---- staged agent records ----------------------------------------------
+
+struct Circ {
+    double x, y, vx, vy, r, m, k, tau0, mu, kappa, damp;
+};
+
+struct TC {
+    double x[3], y[3];          // torso, left shoulder, right shoulder
+    double vx, vy, rt, rs, rts, m, k, tau0, mu, kappa, damp, sn, cs;
+};
+
+// Register-friendly selection of part k (0 torso, 1 left, 2 right).
+__device__ __forceinline__ double sel3(const double v[3], int k) {
+    return k == 0 ? v[0] : (k == 1 ? v[1] : v[2]);
+}
+
+__device__ __forceinline__ Circ load_circ(const double2 *__restrict__ st, int slot) {
+    const double2 *p = st + (size_t)slot * STAGE_Q_CIRC;
+    double2 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2), q3 = __ldg(p + 3),
+            q4 = __ldg(p + 4), q5 = __ldg(p + 5);
+    Circ a;
+    a.x = q0.x; a.y = q0.y; a.vx = q1.x; a.vy = q1.y; a.r = q2.x; a.m = q2.y;
+    a.k = q3.x; a.tau0 = q3.y; a.mu = q4.x; a.kappa = q4.y; a.damp = q5.x;
+    return a;
+}
+
+__device__ __forceinline__ TC load_tc(const double2 *__restrict__ st, int slot) {
+    const double2 *p = st + (size_t)slot * STAGE_Q_TC;
+    double2 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2), q3 = __ldg(p + 3),
+            q4 = __ldg(p + 4), q5 = __ldg(p + 5), q6 = __ldg(p + 6), q7 = __ldg(p + 7),
+            q8 = __ldg(p + 8), q9 = __ldg(p + 9);
+    TC a;
+    a.x[0] = q0.x; a.y[0] = q0.y; a.x[1] = q1.x; a.y[1] = q1.y; a.x[2] = q2.x; a.y[2] = q2.y;
+    a.vx = q3.x; a.vy = q3.y; a.rt = q4.x; a.rs = q4.y; a.rts = q5.x; a.m = q5.y;
+    a.k = q6.x; a.tau0 = q6.y; a.mu = q7.x; a.kappa = q7.y; a.damp = q8.x; a.sn = q8.y;
+    a.cs = q9.x;
+    return a;
+}
+
+// ---- pair interactions: the contribution to ONE side -------------------
+//
+// The reference evaluates each unordered pair once as (i, j), i being the
+// agent of the owner cell (core/interactions.py:152-166), and adds force_i to
+// i and force_j to j.  Here every agent sums its own side: P is the pair's
+// first agent, Q the second, and me_P says whether the calling agent is P.
+// Quantities shared by both sides (h, tau, gradient) are computed from (P, Q)
+// exactly as the reference does, so each side gets the reference's value.
+
+// interaction_agent_agent_circular, core/interactions.py:51-70, with
+// distance_circles (core/distance.py:16-47) and force_social_circular
+// (core/motion/power_law.py:213-259).
+__device__ __forceinline__ void pair_circular(const Circ &P, const Circ &Q, bool me_P,
+                                              double &fx, double &fy) {
+    double xx = P.x - Q.x, xy = P.y - Q.y;
+    double d = cdm_hypot(xx, xy);
+    double r_tot = P.r + Q.r;
+    double h = d - r_tot;
+    if (!(h < SIGTH_SOC)) return;
+    const Circ &M = me_P ? P : Q;
+    double vrx = P.vx - Q.vx, vry = P.vy - Q.vy;
+    double a = vrx * vrx + vry * vry;
+    double b = -(xx * vrx + xy * vry);
+    double c = (xx * xx + xy * xy) - r_tot * r_tot;
+    double disc = b * b - a * c;
+    double Fx = 0.0, Fy = 0.0;
+    // isnan(d) || d == 0 || a == 0  <=>  !(disc > 0) || a == 0
+    if (disc > 0 && a != 0) {
+        double dd = sqrt(disc);
+        double tau = (b - dd) / a;
+        if (!(tau <= 0 || tau > TAU_MAX)) {
+            double gx = (vrx - (vrx * b + xx * a) / dd) / a;
+            double gy = (vry - (vry * b + xy * a) / dd) / a;
+            double cm = (-M.m) * M.k;
+            double mag = magnitude(tau, M.tau0);
+            Fx = (cm * gx) * mag;
+            Fy = (cm * gy) * mag;
+            if (!me_P) { Fx = -Fx; Fy = -Fy; }     // force_j = 0 - (...)
+            truncate2(Fx, Fy, F_SOC_MAX);
+        }
+    }
+    if (h < 0) {
+        double nx = 0.0, ny = 0.0;
+        if (d != 0.0) { nx = xx / d; ny = xy / d; }
+        double cx, cy;
+        force_contact(h, nx, ny, vrx, vry, M.mu, M.kappa, M.damp, cx, cy);
+        if (me_P) { Fx = Fx + cx; Fy = Fy + cy; }
+        else { Fx = Fx - cx; Fy = Fy - cy; }
+    }
+    fx += Fx;
+    fy += Fy;
+}
+
+// interaction_agent_agent_three_circle, core/interactions.py:73-104, with
+// distance_three_circles (core/distance.py:50-105, incl. r_moment1 taken from
+// x0[j_min], :103) and force_social_three_circle (power_law.py:262-363: the
+// first defined root is accepted even if negative, no tau_max cut-off).
+__device__ __forceinline__ void pair_three_circle(const TC &P, const TC &Q, bool me_P,
+                                                  double &fx, double &fy, double &tq) {
+    // distance_three_circles: minimum over 3 x 3 sub-circles, first wins
+    double h_min = __longlong_as_double(0x7ff8000000000000LL);
+    double sdx = 0.0, sdy = 0.0, sd = 0.0;
+    int i_min = 0, j_min = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        double ri = (i == 0) ? P.rt : P.rs;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            double rj = (j == 0) ? Q.rt : Q.rs;
+            double dx = P.x[i] - Q.x[j], dy = P.y[i] - Q.y[j];
+            double d = cdm_hypot(dx, dy);
+            double h = d - (ri + rj);
+            if (h < h_min || isnan(h_min)) {
+                h_min = h; sdx = dx; sdy = dy; sd = d; i_min = i; j_min = j;
+            }
+        }
+    }
+    if (!(h_min < SIGTH_SOC)) return;
+    double nx = 0.0, ny = 0.0;
+    if (sd != 0.0) { nx = sdx / sd; ny = sdy / sd; }
+    // moment arm of the calling side
+    double rmx, rmy;
+    if (me_P) {
+        double r = (i_min == 0) ? P.rt : P.rs;
+        rmx = (sel3(P.x, i_min) + r * nx) - P.x[0];
+        rmy = (sel3(P.y, i_min) + r * ny) - P.y[0];
+    } else {
+        double r = (j_min == 0) ? Q.rt : Q.rs;
+        rmx = (sel3(P.x, j_min) - r * nx) - Q.x[0];
+        rmy = (sel3(P.y, j_min) - r * ny) - Q.y[0];
+    }
+    const TC &M = me_P ? P : Q;
+    double vrx = P.vx - Q.vx, vry = P.vy - Q.vy;
+    double a = vrx * vrx + vry * vry;
+    double Fx = 0.0, Fy = 0.0;
+    if (a != 0) {
+        double tau = __longlong_as_double(0x7ff8000000000000LL);
+        double b_min = 0.0, d_min = 0.0;
+        int ci = 0, cj = 0;
+#pragma unroll
+        for (int pi = 0; pi < 3; ++pi) {
+            double ri = (pi == 0) ? P.rt : P.rs;
+#pragma unroll
+            for (int pj = 0; pj < 3; ++pj) {
+                double rj = (pj == 0) ? Q.rt : Q.rs;
+                double xr = P.x[pi] - Q.x[pj], yr = P.y[pi] - Q.y[pj];
+                double r_tot = ri + rj;
+                double b = -(xr * vrx + yr * vry);
+                double c = (xr * xr + yr * yr) - r_tot * r_tot;
+                double disc = b * b - a * c;
+                if (!(disc > 0)) continue;           // isnan(d) or d == 0
+                double d = sqrt(disc);
+                double tau_new = (b - d) / a;
+                if (isnan(tau) || (0 < tau_new && tau_new < tau)) {
+                    ci = pi; cj = pj; tau = tau_new; b_min = b; d_min = d;
+                }
+            }
+        }
+        if (!(isnan(tau) || tau <= 0)) {
+            // r_off = r_off_i - r_off_j; r_off_k = +/- r_ts (sin phi, -cos phi)
+            // for a left/right shoulder contact part, 0 for the torso
+            double ox = 0.0, oy = 0.0;
+            if (ci != 0) {
+                double ex = P.rts * P.sn, ey = P.rts * (-P.cs);
+                ox = (ci == 1) ? (0.0 + ex) : (0.0 - ex);
+                oy = (ci == 1) ? (0.0 + ey) : (0.0 - ey);
+            }
+            if (cj != 0) {
+                double ex = Q.rts * Q.sn, ey = Q.rts * (-Q.cs);
+                ox = ox - ((cj == 1) ? (0.0 + ex) : (0.0 - ex));
+                oy = oy - ((cj == 1) ? (0.0 + ey) : (0.0 - ey));
+            }
+            double xr = P.x[0] - Q.x[0], yr = P.y[0] - Q.y[0];
+            double gx = (vrx - (a * (xr + 2 * ox) + b_min * vrx) / d_min) / a;
+            double gy = (vry - (a * (yr + 2 * oy) + b_min * vry) / d_min) / a;
+            double cm = (-M.m) * M.k;
+            double mag = magnitude(tau, M.tau0);
+            Fx = (cm * gx) * mag;
+            Fy = (cm * gy) * mag;
+            if (!me_P) { Fx = -Fx; Fy = -Fy; }
+            truncate2(Fx, Fy, F_SOC_MAX);
+        }
+    }
+    if (h_min < 0) {
+        double cx, cy;
+        force_contact(h_min, nx, ny, vrx, vry, M.mu, M.kappa, M.damp, cx, cy);
+        if (me_P) { Fx = Fx + cx; Fy = Fy + cy; }
+        else { Fx = Fx - cx; Fy = Fy - cy; }
+    }
+    fx += Fx;
+    fy += Fy;
+    tq += rmx * Fy - rmy * Fx;      // cross(r_moment, force)
+}
+
+// ---- walls -------------------------------------------------------------
+
+// distance_circle_line, core/distance.py:108-146 (wall tangent precomputed)
+__device__ __forceinline__ double dist_circle_line(double x, double y, double r,
+                                                   const double *w, double &nx,
+                                                   double &ny) {
+    double p0x = w[0], p0y = w[1], p1x = w[2], p1y = w[3];
+    double tx = w[4], ty = w[5], l_w = w[6];
+    double nwx = -ty, nwy = tx;                 // rotate90(t_w)
+    double q0x = x - p0x, q0y = y - p0y;
+    double q1x = x - p1x, q1y = y - p1y;
+    double l_t = -(tx * q1x + ty * q1y) - (tx * q0x + ty * q0y);
+    double d_iw;
+    if (l_t > l_w) {
+        d_iw = cdm_hypot(q0x, q0y);
+        nx = q0x / d_iw; ny = q0y / d_iw;
+    } else if (l_t < -l_w) {
+        d_iw = cdm_hypot(q1x, q1y);
+        nx = q1x / d_iw; ny = q1y / d_iw;
+    } else {
+        double l_n = nwx * q0x + nwy * q0y;
+        d_iw = fabs(l_n);
+        double s = np_sign(l_n);
+        nx = s * nwx; ny = s * nwy;
+    }
+    return d_iw - r;
+}
+
+// Float32 pre-check: centre-to-segment distance clearly above `reach`.
+__device__ __forceinline__ bool wall_far(float x, float y, float reach, float4 w) {
+    float dx = w.z - w.x, dy = w.w - w.y;
+    float qx = x - w.x, qy = y - w.y;
+    float dd = dx * dx + dy * dy;
+    float t = dd > 0.f ? fminf(fmaxf((qx * dx + qy * dy) / dd, 0.f), 1.f) : 0.f;
+    float rx = qx - t * dx, ry = qy - t * dy;
+    float lim = reach + CULL_MARGIN;
+    return rx * rx + ry * ry > lim * lim;       // false for NaN
+}
+
+__device__ __forceinline__ void wall_circular(const Circ &A, const double *w,
+                                              double &fx, double &fy) {
+    double nx, ny;
+    double h = dist_circle_line(A.x, A.y, A.r, w, nx, ny);
+    if (h < 0) {
+        double cx, cy;
+        force_contact(h, nx, ny, A.vx, A.vy, A.mu, A.kappa, A.damp, cx, cy);
+        fx += cx; fy += cy;
+    }
+}
+
+// interaction_agent_three_circle_obstacle, core/interactions.py:123-141, with
+// distance_three_circle_line, core/distance.py:149-180
+__device__ __forceinline__ void wall_three_circle(const TC &A, const double *w,
+                                                  double &fx, double &fy, double &tq) {
+    double h_min = __longlong_as_double(0x7ff8000000000000LL);
+    double nx = 0.0, ny = 0.0;
+    int i_min = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        double r = (i == 0) ? A.rt : A.rs;
+        double mx, my;
+        double h = dist_circle_line(A.x[i], A.y[i], r, w, mx, my);
+        if (h < h_min || isnan(h_min)) { h_min = h; nx = mx; ny = my; i_min = i; }
+    }
+    if (h_min < 0) {
+        double r = (i_min == 0) ? A.rt : A.rs;
+        double rmx = (sel3(A.x, i_min) - r * nx) - A.x[0];
+        double rmy = (sel3(A.y, i_min) - r * ny) - A.y[0];
+        double cx, cy;
+        force_contact(h_min, nx, ny, A.vx, A.vy, A.mu, A.kappa, A.damp, cx, cy);
+        fx += cx; fy += cy;
+        tq += rmx * cy - rmy * cx;
+    }
+}
+
+// ---- kernels ------------------------------------------------------------
+
+__global__ void k_prepare(StepArgs a) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = -1;
+    double l = 0.0;
+    if (i < a.n) {
+        s = a.scen_of[i];
+        const ScenDev sc = a.scen[s];
+        double x = a.col[X][i], y = a.col[Y][i];
+        int key = sc.cell_base;
+        if (isfinite(x) && isfinite(y)) {
+            key += axis_cell(x, sc.x0, sc.cell, sc.nx) * sc.ny + axis_cell(y, sc.y0, sc.cell, sc.ny);
+        } else {
+            atomicOr(a.err, ERR_NOT_FINITE);
+        }
+        a.key[i] = key;
+        atomicAdd(&a.count[key], 1);
+        l = cdm_hypot(a.col[VX][i], a.col[VY][i]);      // length(velocity)
+    }
+    // per-scenario max |v| (NaN and 0 ignored, like `if l > v_max`)
+    unsigned mask = __activemask();
+    int s0 = __shfl_sync(mask, s, 0);
+    bool uniform = __all_sync(mask, s == s0);
+    if (uniform) {
+        double m = (l > 0) ? l : 0.0;
+        for (int o = 16; o > 0; o >>= 1) {
+            double t = __shfl_xor_sync(mask, m, o);
+            m = (t > m) ? t : m;
+        }
+        if ((threadIdx.x & 31) == 0 && s0 >= 0 && m > 0)
+            atomicMax(&a.vmax[s0], ord_bits(m));
+    } else if (s >= 0 && l > 0) {
+        atomicMax(&a.vmax[s], ord_bits(l));
+    }
+}
+
+// adaptive_timestep, core/integrator.py:29-97; accumulates time_tot.
+__global__ void k_dt(StepArgs a) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.n_scen) return;
+    const ScenDev sc = a.scen[s];
+    double v_max = __longlong_as_double((long long)a.vmax[s]);
+    double dt;
+    if (v_max == 0.0) {
+        dt = sc.dt_max;
+    } else {
+        double c = 1.1;
+        double dx_max = c * a.v0max[s] * sc.dt_max;
+        double t = dx_max / v_max;
+        if (t > sc.dt_max) dt = sc.dt_max;
+        else if (t < sc.dt_min) dt = sc.dt_min;
+        else dt = t;
+    }
+    a.dt[s] = dt;
+    a.time_tot[s] += dt;
+}
+
+// Per-scenario max of target_velocity (np.max propagates NaN).
+__global__ void k_v0max(StepArgs a, double *out) {
+    int s = blockIdx.x;
+    if (s >= a.n_scen) return;
+    const ScenDev sc = a.scen[s];
+    __shared__ double red[256];
+    __shared__ int any_nan;
+    if (threadIdx.x == 0) any_nan = 0;
+    __syncthreads();
+    double m = -INFINITY;
+    for (int k = threadIdx.x; k < sc.agent_count; k += blockDim.x) {
+        double v = a.col[V0][sc.agent_begin + k];
+        if (isnan(v)) any_nan = 1;
+        else m = fmax(m, v);
+    }
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[s] = any_nan ? __longlong_as_double(0x7ff8000000000000LL) : red[0];
+}
+
+// -- exclusive scan (block-local, then block totals) --
+
+constexpr int SCAN_NT = 1024, SCAN_IPT = 4, SCAN_TILE = SCAN_NT * SCAN_IPT;
+
+__global__ void __launch_bounds__(SCAN_NT) k_scan_local(const int *in, int *out, int *blocksums, int n) {
+    __shared__ int wtot[SCAN_NT / 32];
+    int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_IPT;
+    int v[SCAN_IPT];
+    int sum = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_IPT; ++k) {
+        v[k] = (base + k < n) ? in[base + k] : 0;
+        sum += v[k];
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) wtot[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int x = wtot[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += t;
+        }
+        wtot[lane] = x;
+    }
+    __syncthreads();
+    int excl = incl - sum + (w > 0 ? wtot[w - 1] : 0);
+#pragma unroll
+    for (int k = 0; k < SCAN_IPT; ++k) {
+        if (base + k < n) out[base + k] = excl;
+        excl += v[k];
+    }
+    if (threadIdx.x == SCAN_NT - 1) {
+        if (blocksums) blocksums[blockIdx.x] = excl;
+        else out[n] = excl;           // single tile: total at out[n]
+    }
+}
+
+__global__ void k_scan_add(int *out, const int *offs, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] += offs[i / SCAN_TILE];
+}
+
+__global__ void k_scatter(StepArgs a) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    int c = a.key[i];
+    int p = a.start[c] + atomicAdd(&a.fill[c], 1);
+    a.perm_unsorted[p] = i;
+}
+
+// Stable order inside a cell: rank = number of agents of the cell with a
+// smaller index.
+__global__ void k_rank(StepArgs a) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.n) return;
+    int i = a.perm_unsorted[p];
+    int c = a.key[i];
+    int b = a.start[c], e = a.start[c + 1];
+    int r = 0;
+    for (int q = b; q < e; ++q) r += (a.perm_unsorted[q] < i);
+    a.perm[b + r] = i;
+}
+
+// Extent: distance from the torso centre to the farthest skin point.
+__device__ __forceinline__ double extent_tc(double x, double y, double xl, double yl,
+                                            double xr, double yr, double rt, double rs) {
+    double e = rt;
+    double l = cdm_hypot(xl - x, yl - y) + rs;
+    double r = cdm_hypot(xr - x, yr - y) + rs;
+    e = (l > e) ? l : e;
+    e = (r > e) ? r : e;
+    return e;
+}
+
+__device__ __forceinline__ float up_f(double v) {
+    float f = (float)v;
+    return f + fabsf(f) * 1e-6f + 1e-6f;
+}
+
+__global__ void k_gather(StepArgs a) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.n) return;
+    int i = a.perm[s];
+    double *const *c = a.col;
+    if (a.body == 0) {
+        double2 *p = a.stage + (size_t)s * STAGE_Q_CIRC;
+        p[0] = make_double2(c[X][i], c[Y][i]);
+        p[1] = make_double2(c[VX][i], c[VY][i]);
+        p[2] = make_double2(c[R][i], c[MASS][i]);
+        p[3] = make_double2(c[K_SOC][i], c[TAU0][i]);
+        p[4] = make_double2(c[MU][i], c[KAPPA][i]);
+        p[5] = make_double2(c[DAMP][i], 0.0);
+        double e = c[R][i];
+        a.cull[s] = make_float4((float)c[X][i], (float)c[Y][i], up_f(e), 0.f);
+    } else {
+        double2 *p = a.stage + (size_t)s * STAGE_Q_TC;
+        double x = c[X][i], y = c[Y][i];
+        double phi = c[PHI][i];
+        p[0] = make_double2(x, y);
+        p[1] = make_double2(c[XLS][i], c[YLS][i]);
+        p[2] = make_double2(c[XRS][i], c[YRS][i]);
+        p[3] = make_double2(c[VX][i], c[VY][i]);
+        p[4] = make_double2(c[RT][i], c[RS][i]);
+        p[5] = make_double2(c[RTS][i], c[MASS][i]);
+        p[6] = make_double2(c[K_SOC][i], c[TAU0][i]);
+        p[7] = make_double2(c[MU][i], c[KAPPA][i]);
+        double sn, cs;
+        cdm_sincos(phi, &sn, &cs);
+        p[8] = make_double2(c[DAMP][i], sn);
+        p[9] = make_double2(cs, 0.0);
+        double e = extent_tc(x, y, c[XLS][i], c[YLS][i], c[XRS][i], c[YRS][i], c[RT][i], c[RS][i]);
+        a.cull[s] = make_float4((float)x, (float)y, up_f(e), 0.f);
+    }
+}
+
+// Float32 conservative pre-check: true if the pair certainly has h >= 3.
+__device__ __forceinline__ bool pair_far(float4 me, float4 o) {
+    float dx = me.x - o.x, dy = me.y - o.y;
+    float lim = (float)SIGTH_SOC + me.z + o.z + CULL_MARGIN;
+    return dx * dx + dy * dy > lim * lim;       // false for NaN
+}
+
+// Candidate enumeration over the 3 x 3 cell neighbourhood of slot s.  The
+// pair (s, t) is oriented with s first iff t is later in the same cell or t's
+// cell is in the forward half of the stencil (flat offset dx*ny + dy > 0).
+// Calls fn(t, s_is_first) for every candidate that survives the pre-check;
+// counts all candidates in *cand.
+template <typename Fn>
+__device__ __forceinline__ void for_candidates(const StepArgs &a, const ScenDev &sc, int s,
+                                               int my_cell, float4 me, Fn fn, int *cand) {
+    int local = my_cell - sc.cell_base;
+    int ix = local / sc.ny, iy = local - ix * sc.ny;
+    for (int dx = -1; dx <= 1; ++dx) {
+        int jx = ix + dx;
+        if (jx < 0 || jx >= sc.nx) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            int jy = iy + dy;
+            if (jy < 0 || jy >= sc.ny) continue;
+            int c2 = sc.cell_base + jx * sc.ny + jy;
+            int b = __ldg(&a.start[c2]), e = __ldg(&a.start[c2 + 1]);
+            bool fwd = (dx > 0) || (dx == 0 && dy > 0);
+            bool same = (dx == 0 && dy == 0);
+            for (int t = b; t < e; ++t) {
+                if (t == s) continue;
+                if (cand) ++*cand;
+                float4 o = __ldg(&a.cull[t]);
+                if (pair_far(me, o)) continue;
+                fn(t, same ? (s < t) : fwd);
+            }
+        }
+    }
+}
+
+template <int BODY>
+__global__ void __launch_bounds__(NT_FORCES) k_forces(StepArgs a) {
+    __shared__ int list[LIST_CAP * NT_FORCES];
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.n) return;
+    const int i = a.perm[s];
+    const int sid = a.scen_of[i];
+    const ScenDev sc = a.scen[sid];
+    double *const *col = a.col;
+    const float4 me = a.cull[s];
+    const int my_cell = a.key[i];
+    const int nodes = a.nodes;
+
+    double fx = col[FX][i], fy = col[FY][i];
+    double tq = (BODY == 1) ? col[TORQUE][i] : 0.0;
+
+    // Fluctuation (simulation/logic.py:78-86), noise drawn on the host
+    if ((nodes & N_FLUCT) && a.noise_f) {
+        fx = fx + a.noise_f[2 * i];
+        fy = fy + a.noise_f[2 * i + 1];
+        if (BODY == 1 && a.noise_m) tq = tq + a.noise_m[i];
+    }
+    double phi0 = (BODY == 1) ? col[PHI0][i] : 0.0;
+    // Orientation (core/steering/orientation.py:17-21)
+    if (BODY == 1 && (nodes & N_ORIENT)) phi0 = cdm_atan2(col[E0Y][i], col[E0X][i]);
+    // Adjusting (core/motion/adjusting.py:16-121)
+    if (nodes & N_ADJUST) {
+        double k = col[MASS][i] / col[TAU_ADJ][i];
+        double v0 = col[V0][i];
+        fx = fx + k * (v0 * col[E0X][i] - col[VX][i]);
+        fy = fy + k * (v0 * col[E0Y][i] - col[VY][i]);
+        if (BODY == 1) {
+            tq = tq + col[INERTIA][i] / col[TAU_ROT][i] *
+                          (wrap_to_pi(phi0 - col[PHI][i]) / PI_D * col[W0][i] - col[OMEGA][i]);
+        }
+    }
+
+    // Agent-agent (core/interactions.py:147-166)
+    if (nodes & N_AGENT) {
+        int *mylist = list + threadIdx.x;
+        if (BODY == 0) {
+            const Circ A = load_circ(a.stage, s);
+            int nl = 0;
+            auto flush = [&]() {
+                for (int k = 0; k < nl; ++k) {
+                    int v = mylist[k * NT_FORCES];
+                    bool first = v < 0;
+                    const Circ B = load_circ(a.stage, first ? ~v : v);
+                    if (first) pair_circular(A, B, true, fx, fy);
+                    else pair_circular(B, A, false, fx, fy);
+                }
+                nl = 0;
+            };
+            for_candidates(a, sc, s, my_cell, me, [&](int t, bool first) {
+                mylist[nl * NT_FORCES] = first ? ~t : t;
+                if (++nl == LIST_CAP) flush();
+            }, (int *)nullptr);
+            flush();
+        } else {
+            const TC A = load_tc(a.stage, s);
+            int nl = 0;
+            auto flush = [&]() {
+                for (int k = 0; k < nl; ++k) {
+                    int v = mylist[k * NT_FORCES];
+                    bool first = v < 0;
+                    const TC B = load_tc(a.stage, first ? ~v : v);
+                    if (first) pair_three_circle(A, B, true, fx, fy, tq);
+                    else pair_three_circle(B, A, false, fx, fy, tq);
+                }
+                nl = 0;
+            };
+            for_candidates(a, sc, s, my_cell, me, [&](int t, bool first) {
+                mylist[nl * NT_FORCES] = first ? ~t : t;
+                if (++nl == LIST_CAP) flush();
+            }, (int *)nullptr);
+            flush();
+        }
+    }
+
+    // Agent-wall (core/interactions.py:107-141,169-186), walls in index order
+    if ((nodes & N_WALL) && sc.wall_count > 0) {
+        const bool all_walls = me.z > (float)sc.wall_reach;
+        int wb, we;
+        if (all_walls) { wb = sc.wall_begin; we = sc.wall_begin + sc.wall_count; }
+        else { wb = __ldg(&a.wall_start[my_cell]); we = __ldg(&a.wall_start[my_cell + 1]); }
+        if (BODY == 0) {
+            Circ A;
+            bool loaded = false;
+            for (int q = wb; q < we; ++q) {
+                int w = all_walls ? q : __ldg(&a.wall_idx[q]);
+                if (wall_far(me.x, me.y, me.z, __ldg(&a.walls_f[w]))) continue;
+                if (!loaded) { A = load_circ(a.stage, s); loaded = true; }
+                wall_circular(A, a.walls + (size_t)w * WALL_D, fx, fy);
+            }
+        } else {
+            TC A;
+            bool loaded = false;
+            for (int q = wb; q < we; ++q) {
+                int w = all_walls ? q : __ldg(&a.wall_idx[q]);
+                if (wall_far(me.x, me.y, me.z, __ldg(&a.walls_f[w]))) continue;
+                if (!loaded) { A = load_tc(a.stage, s); loaded = true; }
+                wall_three_circle(A, a.walls + (size_t)w * WALL_D, fx, fy, tq);
+            }
+        }
+    }
+
+    if (BODY == 1 && (nodes & N_ORIENT)) col[PHI0][i] = phi0;
+
+    if (nodes & N_INTEG) {
+        // velocity_verlet_integrator, core/integrator.py:164-193,209-256
+        const double dt = a.dt[sid];
+        const double dt2 = dt * dt;
+        double m = col[MASS][i];
+        double oax = col[FPX][i] / m, oay = col[FPY][i] / m;
+        double nax = fx / m, nay = fy / m;
+        double vx = col[VX][i] + (oax + nax) / 2 * dt;
+        double vy = col[VY][i] + (oay + nay) / 2 * dt;
+        double x = col[X][i] + (vx * dt + nax / 2 * dt2);
+        double y = col[Y][i] + (vy * dt + nay / 2 * dt2);
+        col[FPX][i] = fx; col[FPY][i] = fy;
+        col[VX][i] = vx; col[VY][i] = vy;
+        col[X][i] = x; col[Y][i] = y;
+        if (BODY == 1) {
+            double I = col[INERTIA][i];
+            double oaa = col[TORQUE_PREV][i] / I, naa = tq / I;
+            col[TORQUE_PREV][i] = tq;
+            double w = col[OMEGA][i] + (oaa + naa) / 2 * dt;
+            double phi = wrap_to_pi(col[PHI][i] + (w * dt + naa / 2 * dt2));
+            col[OMEGA][i] = w;
+            col[PHI][i] = phi;
+            // shoulders, simulation/agents.py:473-486
+            double rts = col[RTS][i];
+            double sn, cs;
+            cdm_sincos(phi, &sn, &cs);
+            double ox = sn * rts, oy = (-cs) * rts;
+            col[XLS][i] = x - ox; col[YLS][i] = y - oy;
+            col[XRS][i] = x + ox; col[YRS][i] = y + oy;
+        }
+    }
+    if (nodes & N_RESET) {
+        // Reset.update, simulation/logic.py:59-64 (runs last)
+        col[FX][i] = 0.0; col[FY][i] = 0.0;
+        if (BODY == 1) col[TORQUE][i] = 0.0;
+    } else {
+        col[FX][i] = fx; col[FY][i] = fy;
+        if (BODY == 1) col[TORQUE][i] = tq;
+    }
+}
+
+// Skin distance of a pair (same value whichever side is first).
+__device__ __forceinline__ double pair_h(const StepArgs &a, int s, int t) {
+    if (a.body == 0) {
+        const Circ A = load_circ(a.stage, s), B = load_circ(a.stage, t);
+        return cdm_hypot(A.x - B.x, A.y - B.y) - (A.r + B.r);
+    }
+    const TC A = load_tc(a.stage, s), B = load_tc(a.stage, t);
+    double h_min = __longlong_as_double(0x7ff8000000000000LL);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double h = cdm_hypot(A.x[i] - B.x[j], A.y[i] - B.y[j]) -
+                       ((i == 0 ? A.rt : A.rs) + (j == 0 ? B.rt : B.rs));
+            if (h < h_min || isnan(h_min)) h_min = h;
+        }
+    return h_min;
+}
+
+// Per-agent interaction counts (diagnostics / algorithmic work accounting):
+// candidates, pre-check survivors, h < 3, h < 0, walls past the pre-check,
+// walls in contact.
+__global__ void k_pair_counts(StepArgs a, int *out) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.n) return;
+    int i = a.perm[s];
+    const ScenDev sc = a.scen[a.scen_of[i]];
+    const float4 me = a.cull[s];
+    int nc = 0, nn = 0, ni = 0, nt = 0, wn = 0, wc = 0;
+    for_candidates(a, sc, s, a.key[i], me, [&](int t, bool) {
+        ++nn;
+        double h = pair_h(a, s, t);
+        ni += (h < SIGTH_SOC);
+        nt += (h < 0);
+    }, &nc);
+    if (sc.wall_count > 0) {
+        const bool all_walls = me.z > (float)sc.wall_reach;
+        int my_cell = a.key[i];
+        int wb = all_walls ? sc.wall_begin : a.wall_start[my_cell];
+        int we = all_walls ? sc.wall_begin + sc.wall_count : a.wall_start[my_cell + 1];
+        for (int q = wb; q < we; ++q) {
+            int w = all_walls ? q : a.wall_idx[q];
+            if (wall_far(me.x, me.y, me.z, a.walls_f[w])) continue;
+            ++wn;
+            double fx = 0, fy = 0, tq = 0;
+            if (a.body == 0) {
+                const Circ A = load_circ(a.stage, s);
+                double nx, ny;
+                wc += dist_circle_line(A.x, A.y, A.r, a.walls + (size_t)w * WALL_D, nx, ny) < 0;
+            } else {
+                const TC A = load_tc(a.stage, s);
+                double h_min = __longlong_as_double(0x7ff8000000000000LL);
+                for (int k = 0; k < 3; ++k) {
+                    double nx, ny;
+                    double h = dist_circle_line(A.x[k], A.y[k], k == 0 ? A.rt : A.rs,
+                                                a.walls + (size_t)w * WALL_D, nx, ny);
+                    if (h < h_min || isnan(h_min)) h_min = h;
+                }
+                wc += h_min < 0;
+            }
+            (void)fx; (void)fy; (void)tq;
+        }
+    }
+    int *o = out + (size_t)i * 6;
+    o[0] = nc; o[1] = nn; o[2] = ni; o[3] = nt; o[4] = wn; o[5] = wc;
+}
+
+__global__ void k_wall_prep(const double *raw, double *walls, float4 *wf, int nw) {
+    int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nw) return;
+    double p0x = raw[4 * w], p0y = raw[4 * w + 1], p1x = raw[4 * w + 2], p1y = raw[4 * w + 3];
+    double dx = p1x - p0x, dy = p1y - p0y;
+    double l_w = cdm_hypot(dx, dy);
+    double *o = walls + (size_t)w * WALL_D;
+    o[0] = p0x; o[1] = p0y; o[2] = p1x; o[3] = p1y;
+    o[4] = dx / l_w; o[5] = dy / l_w; o[6] = l_w; o[7] = 0.0;
+    wf[w] = make_float4((float)p0x, (float)p0y, (float)p1x, (float)p1y);
+}
+
+// -- packed host records <-> columns -------------------------------------
+// Record fields are 4-byte aligned (packed numpy dtypes), so every float64 is
+// moved as two 32-bit words.
+
+struct FieldMap { int field, comp, col; };
+// (CD_F_* field, vector component, column)
+__constant__ FieldMap kMapCirc[19] = {
+    {0, 0, X}, {0, 1, Y}, {1, 0, VX}, {1, 1, VY}, {2, 0, E0X}, {2, 1, E0Y},
+    {3, 0, FX}, {3, 1, FY}, {4, 0, FPX}, {4, 1, FPY}, {5, 0, R}, {9, 0, MASS},
+    {11, 0, V0}, {13, 0, TAU_ADJ}, {14, 0, K_SOC}, {15, 0, TAU0}, {16, 0, MU},
+    {17, 0, KAPPA}, {18, 0, DAMP}};
+__constant__ FieldMap kMapTC[34] = {
+    {0, 0, X}, {0, 1, Y}, {1, 0, VX}, {1, 1, VY}, {2, 0, E0X}, {2, 1, E0Y},
+    {3, 0, FX}, {3, 1, FY}, {4, 0, FPX}, {4, 1, FPY}, {5, 0, R}, {9, 0, MASS},
+    {11, 0, V0}, {13, 0, TAU_ADJ}, {14, 0, K_SOC}, {15, 0, TAU0}, {16, 0, MU},
+    {17, 0, KAPPA}, {18, 0, DAMP},
+    {20, 0, XLS}, {20, 1, YLS}, {21, 0, XRS}, {21, 1, YRS}, {6, 0, RT}, {7, 0, RS},
+    {8, 0, RTS}, {10, 0, INERTIA}, {12, 0, W0}, {22, 0, PHI}, {23, 0, OMEGA},
+    {24, 0, PHI0}, {25, 0, TORQUE}, {26, 0, TORQUE_PREV}, {27, 0, TAU_ROT}};
+// Columns the step writes (downloaded back into the records).
+__constant__ int kOutCirc[8] = {X, Y, VX, VY, FX, FY, FPX, FPY};
+__constant__ int kOutTC[17] = {X, Y, VX, VY, FX, FY, FPX, FPY, XLS, YLS, XRS, YRS,
+                               PHI, OMEGA, PHI0, TORQUE, TORQUE_PREV};
+
+struct OffTable { long long off[32]; };
+struct ColPtrs { double *p[NCOL]; };
+
+__device__ __forceinline__ double ld_rec(const char *rec, long long off) {
+    const unsigned *p = reinterpret_cast<const unsigned *>(rec + off);
+    return __hiloint2double((int)p[1], (int)p[0]);
+}
+__device__ __forceinline__ void st_rec(char *rec, long long off, double v) {
+    unsigned *p = reinterpret_cast<unsigned *>(rec + off);
+    p[0] = (unsigned)__double2loint(v);
+    p[1] = (unsigned)__double2hiint(v);
+}
+
+__global__ void k_aos_to_soa(const char *aos, long long itemsize, OffTable off, int n,
+                             int body, ColPtrs cols) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const char *rec = aos + (size_t)i * itemsize;
+    const FieldMap *map = body == 0 ? kMapCirc : kMapTC;
+    int nm = body == 0 ? 19 : 34;
+    for (int k = 0; k < nm; ++k) {
+        long long o = off.off[map[k].field];
+        if (o < 0) continue;
+        cols.p[map[k].col][i] = ld_rec(rec, o + 8 * map[k].comp);
+    }
+}
+
+__global__ void k_soa_to_aos(char *aos, long long itemsize, OffTable off, int n, int body,
+                             ColPtrs cols) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    char *rec = aos + (size_t)i * itemsize;
+    const FieldMap *map = body == 0 ? kMapCirc : kMapTC;
+    const int *outs = body == 0 ? kOutCirc : kOutTC;
+    int nm = body == 0 ? 19 : 34, no = body == 0 ? 8 : 17;
+    for (int k = 0; k < nm; ++k) {
+        bool written = false;
+        for (int q = 0; q < no; ++q) written |= (outs[q] == map[k].col);
+        long long o = off.off[map[k].field];
+        if (!written || o < 0) continue;
+        st_rec(rec, o + 8 * map[k].comp, cols.p[map[k].col][i]);
+    }
+}
+
+__global__ void k_fp64_fma(double *out, int iters, double b, double c) {
+    double a0 = threadIdx.x * 1e-3, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3,
+           a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+    for (int i = 0; i < iters; ++i) {
+        a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+        a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+inline int nblk(long long n, int nt) { return (int)((n + nt - 1) / nt); }
+
+}  // namespace
+
+void launch_prepare(const StepArgs &a, cudaStream_t s) {
+    if (a.n > 0) k_prepare<<<nblk(a.n, 256), 256, 0, s>>>(a);
+}
+void launch_dt(const StepArgs &a, cudaStream_t s) {
+    if (a.n_scen > 0) k_dt<<<nblk(a.n_scen, 128), 128, 0, s>>>(a);
+}
+int scan_scratch_ints(int n) {
+    int nb = nblk(n, SCAN_TILE);
+    return nb > 1 ? 2 * (nb + 1) : 1;
+}
+void launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s) {
+    int nb = nblk(n, SCAN_TILE);
+    if (nb <= 1) {
+        k_scan_local<<<1, SCAN_NT, 0, s>>>(in, out, nullptr, n);
+        return;
+    }
+    int *sums = scratch, *offs = scratch + nb + 1;
+    k_scan_local<<<nb, SCAN_NT, 0, s>>>(in, out, sums, n);
+    k_scan_local<<<1, SCAN_NT, 0, s>>>(sums, offs, nullptr, nb);   // offs[nb] = total
+    k_scan_add<<<nblk(n, 256), 256, 0, s>>>(out, offs, n);
+    cudaMemcpyAsync(out + n, offs + nb, sizeof(int), cudaMemcpyDeviceToDevice, s);
+}
+void launch_scatter(const StepArgs &a, cudaStream_t s) {
+    if (a.n <= 0) return;
+    k_scatter<<<nblk(a.n, 256), 256, 0, s>>>(a);
+    k_rank<<<nblk(a.n, 256), 256, 0, s>>>(a);
+}
+void launch_gather(const StepArgs &a, cudaStream_t s) {
+    if (a.n > 0) k_gather<<<nblk(a.n, 128), 128, 0, s>>>(a);
+}
+void launch_forces(const StepArgs &a, cudaStream_t s) {
+    if (a.n <= 0) return;
+    if (a.body == 0) k_forces<0><<<nblk(a.n, NT_FORCES), NT_FORCES, 0, s>>>(a);
+    else k_forces<1><<<nblk(a.n, NT_FORCES), NT_FORCES, 0, s>>>(a);
+}
+void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s) {
+    if (a.n > 0) k_pair_counts<<<nblk(a.n, 128), 128, 0, s>>>(a, counts);
+}
+void launch_v0max(const StepArgs &a, double *out, cudaStream_t s) {
+    if (a.n_scen > 0) k_v0max<<<a.n_scen, 256, 0, s>>>(a, out);
+}
+void launch_wall_prep(const double *raw, double *walls, float4 *wf, int nw, cudaStream_t s) {
+    if (nw > 0) k_wall_prep<<<nblk(nw, 128), 128, 0, s>>>(raw, walls, wf, nw);
+}
+void launch_aos_to_soa(const char *aos, long long itemsize, const long long *off, int n,
+                       int body, double *const *col, cudaStream_t s) {
+    if (n <= 0) return;
+    OffTable t;
+    for (int k = 0; k < 32; ++k) t.off[k] = k < 29 ? off[k] : -1;
+    ColPtrs c;
+    for (int k = 0; k < NCOL; ++k) c.p[k] = col[k];
+    k_aos_to_soa<<<nblk(n, 128), 128, 0, s>>>(aos, itemsize, t, n, body, c);
+}
+void launch_soa_to_aos(char *aos, long long itemsize, const long long *off, int n, int body,
+                       const double *const *col, cudaStream_t s) {
+    if (n <= 0) return;
+    OffTable t;
+    for (int k = 0; k < 32; ++k) t.off[k] = k < 29 ? off[k] : -1;
+    ColPtrs c;
+    for (int k = 0; k < NCOL; ++k) c.p[k] = const_cast<double *>(col[k]);
+    k_soa_to_aos<<<nblk(n, 128), 128, 0, s>>>(aos, itemsize, t, n, body, c);
+}
+
+double fp64_peak_gflops() {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    double *out = nullptr;
+    if (cudaMalloc(&out, sizeof(double) * blocks * threads) != cudaSuccess) return -1;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(e0);
+        k_fp64_fma<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (cudaGetLastError() != cudaSuccess) return -1;
+    double flops = 2.0 * 8 * iters * (double)blocks * threads;
+    return flops / (best * 1e-3) / 1e9;
+}
+
+}  // namespace cdk

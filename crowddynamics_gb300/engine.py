@@ -1,0 +1,205 @@
+"""Python handle on one device context (a batch of scenarios).
+
+``DeviceBatch`` is a thin owner of a ``cd_ctx``: every method is one C-ABI
+call.  A plain simulation is a batch of one scenario; the batched form packs
+many independent scenarios (their agents and walls concatenated) into one
+context so that one launch advances all of them.
+"""
+import ctypes
+import math
+
+import numpy as np
+
+from crowddynamics_gb300 import _native as N
+from crowddynamics_gb300.exceptions import InvalidType, InvalidValue
+from crowddynamics_gb300.simulation.agents import (
+    BODY_CIRCULAR, BODY_THREE_CIRCLE, body_type_of, field_offsets)
+
+
+def walls_as_rows(walls):
+    """obstacle_type_linear array / (W, 4) array / sequence of ((x0, y0),
+    (x1, y1)) -> contiguous (W, 4) float64 rows (p0x, p0y, p1x, p1y)."""
+    if walls is None:
+        return np.zeros((0, 4))
+    a = np.asarray(walls)
+    if a.dtype.names is not None:
+        out = np.empty((len(a), 4))
+        if len(a):
+            out[:, 0:2] = a['p0']
+            out[:, 2:4] = a['p1']
+        return out
+    a = np.asarray(a, dtype=np.float64)
+    if a.size == 0:
+        return np.zeros((0, 4))
+    return np.ascontiguousarray(a.reshape(-1, 4))
+
+
+def grid_for_bounds(bounds, cell_size):
+    """(x0, y0, cell, nx, ny) covering bounds = (xmin, ymin, xmax, ymax)."""
+    xmin, ymin, xmax, ymax = (float(v) for v in bounds)
+    if not all(math.isfinite(v) for v in (xmin, ymin, xmax, ymax)):
+        raise InvalidValue('grid bounds must be finite')
+    nx = max(1, int(math.floor((xmax - xmin) / cell_size)) + 1)
+    ny = max(1, int(math.floor((ymax - ymin) / cell_size)) + 1)
+    return xmin, ymin, float(cell_size), nx, ny
+
+
+class DeviceBatch:
+    """One ``cd_ctx``: ``body`` is 'circular' or 'three_circle'; ``specs`` is
+    a list of dicts with keys n_agents, n_walls, grid=(x0, y0, cell, nx, ny),
+    dt_min, dt_max."""
+
+    def __init__(self, body, specs):
+        self._lib = N.load()
+        self.body = body
+        self.body_code = BODY_CIRCULAR if body == 'circular' else BODY_THREE_CIRCLE
+        if body not in ('circular', 'three_circle'):
+            raise InvalidType('body must be circular or three_circle')
+        arr = (N.Scenario * len(specs))()
+        a0 = w0 = 0
+        for k, sp in enumerate(specs):
+            x0, y0, cell, nx, ny = sp['grid']
+            arr[k] = N.Scenario(a0, int(sp['n_agents']), w0, int(sp['n_walls']),
+                                float(x0), float(y0), float(cell), int(nx), int(ny),
+                                float(sp.get('dt_min', 0.001)), float(sp.get('dt_max', 0.01)))
+            a0 += int(sp['n_agents'])
+            w0 += int(sp['n_walls'])
+        self.n_agents, self.n_walls, self.n_scenarios = a0, w0, len(specs)
+        self.specs = list(specs)
+        ctx = ctypes.c_void_p()
+        N.check(self._lib.cd_create(ctypes.byref(ctx), self.body_code, len(specs), arr))
+        self._ctx = ctx
+        self._offsets = None
+        ncell = ctypes.c_int64()
+        N.check(self._lib.cd_sizes(ctx, None, None, ctypes.byref(ncell)), ctx)
+        self.n_cells = ncell.value
+
+    # -- lifetime --
+    def close(self):
+        if getattr(self, '_ctx', None):
+            self._lib.cd_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _chk(self, rc):
+        N.check(rc, self._ctx)
+
+    # -- data --
+    def upload(self, records):
+        if body_type_of(records) != self.body_code:
+            raise InvalidType('agent dtype does not match the context body type')
+        if not records.flags.c_contiguous:
+            raise InvalidValue('agent array must be C-contiguous')
+        off = field_offsets(records.dtype)
+        self._offsets = off
+        self._chk(self._lib.cd_upload_agents(self._ctx, N.ptr(records), len(records),
+                                             records.dtype.itemsize, N.i64ptr(off)))
+
+    def download(self, records):
+        if not records.flags.c_contiguous or not records.flags.writeable:
+            raise InvalidValue('agent array must be C-contiguous and writeable')
+        off = field_offsets(records.dtype)
+        self._chk(self._lib.cd_download_agents(self._ctx, N.ptr(records), len(records),
+                                               records.dtype.itemsize, N.i64ptr(off)))
+
+    def set_walls(self, walls):
+        rows = walls_as_rows(walls)
+        self._chk(self._lib.cd_set_walls(self._ctx, N.ptr(rows), len(rows)))
+
+    def set_noise(self, force, torque=None):
+        f = np.ascontiguousarray(force, dtype=np.float64)
+        if f.shape != (self.n_agents, 2):
+            raise InvalidValue('force noise must have shape (n, 2)')
+        m = None
+        if torque is not None:
+            m = np.ascontiguousarray(torque, dtype=np.float64)
+            if m.shape != (self.n_agents,):
+                raise InvalidValue('torque noise must have shape (n,)')
+        self._chk(self._lib.cd_set_noise(self._ctx, N.ptr(f), N.ptr(m)))
+
+    # -- stepping --
+    def step(self, nodes=N.NODE_ALL, want_dt=False):
+        """One update with the given node flags; returns per-scenario dt when
+        ``want_dt`` (waits for the step), else None."""
+        if want_dt:
+            dt = np.zeros(self.n_scenarios)
+            self._chk(self._lib.cd_step(self._ctx, int(nodes), N.dptr(dt)))
+            return dt
+        self._chk(self._lib.cd_step(self._ctx, int(nodes), None))
+        return None
+
+    def run(self, steps, nodes=N.NODE_ALL & ~N.NODE_FLUCTUATION):
+        """``steps`` updates as CUDA-graph launches; waits and checks status."""
+        self._chk(self._lib.cd_run(self._ctx, int(nodes), int(steps)))
+
+    def synchronize(self):
+        self._chk(self._lib.cd_synchronize(self._ctx))
+
+    def time(self):
+        dt = np.zeros(self.n_scenarios)
+        tt = np.zeros(self.n_scenarios)
+        self._chk(self._lib.cd_get_time(self._ctx, N.dptr(dt), N.dptr(tt)))
+        return dt, tt
+
+    # -- diagnostics --
+    def cell_list(self):
+        keys = np.zeros(self.n_agents, np.int64)
+        order = np.zeros(self.n_agents, np.int64)
+        cnt = np.zeros(self.n_cells, np.int64)
+        off = np.zeros(self.n_cells, np.int64)
+        self._chk(self._lib.cd_get_cell_list(self._ctx, N.i64ptr(keys), N.i64ptr(order),
+                                             N.i64ptr(cnt), N.i64ptr(off)))
+        return keys, order, cnt, off
+
+    def pair_counts(self):
+        """Per-agent counts (n, 6): candidates, near, interacting (h < 3),
+        contact (h < 0), walls near, walls in contact."""
+        c = np.zeros((self.n_agents, len(N.COUNT_COLS)), np.int64)
+        self._chk(self._lib.cd_pair_counts(self._ctx, N.i64ptr(c)))
+        return c
+
+    def set_timing(self, enable=True):
+        self._chk(self._lib.cd_set_timing(self._ctx, int(bool(enable))))
+
+    def kernel_time(self):
+        """dict(force_ms, force_launches, step_ms, run_ms, run_steps) since
+        the last set_timing."""
+        f, s, r = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        n, rn = ctypes.c_int64(), ctypes.c_int64()
+        self._chk(self._lib.cd_kernel_time(self._ctx, ctypes.byref(f), ctypes.byref(n),
+                                           ctypes.byref(s), ctypes.byref(r), ctypes.byref(rn)))
+        return dict(force_ms=f.value, force_launches=n.value, step_ms=s.value,
+                    run_ms=r.value, run_steps=rn.value)
+
+    def kernels_per_step(self, nodes=N.NODE_ALL):
+        k = ctypes.c_int64()
+        self._chk(self._lib.cd_kernels_per_step(self._ctx, int(nodes), ctypes.byref(k)))
+        return k.value
+
+
+def batch_from_scenarios(scenarios):
+    """DeviceBatch holding every scenario of ``scenarios`` (same body type),
+    with the concatenated agent array and walls uploaded.  Returns
+    (batch, agents, walls_rows)."""
+    bodies = {s.body for s in scenarios}
+    if len(bodies) != 1:
+        raise InvalidType('a batch holds one body type')
+    specs = [dict(n_agents=len(s.agents), n_walls=len(s.walls), grid=s.grid,
+                  dt_min=s.dt_min, dt_max=s.dt_max) for s in scenarios]
+    b = DeviceBatch(bodies.pop(), specs)
+    agents = np.ascontiguousarray(np.concatenate([s.agents for s in scenarios]))
+    walls = np.concatenate([walls_as_rows(s.walls) for s in scenarios]) if scenarios else np.zeros((0, 4))
+    b.upload(agents)
+    b.set_walls(walls)
+    return b, agents, walls

@@ -1,0 +1,178 @@
+/*
+ * cdgpu.h -- C ABI of the GB300-native per-step agent update (libcdgpu.so).
+ *
+ * The library advances crowds of Circular or ThreeCircle agents by the
+ * reference's per-step update: fluctuation (host-drawn noise), orientation,
+ * adjusting force/torque, agent-agent power-law social + contact forces over
+ * a uniform cell list, agent-wall contact forces, adaptive-timestep velocity
+ * Verlet and reset.  All arithmetic is IEEE float64.  Plain pointers and
+ * sizes only; every entry point returns CD_OK (0) or a CD_ERR_* code and
+ * keeps a message for cd_last_error().
+ *
+ * A context owns one batch of independent scenarios (a plain simulation is
+ * a batch of one).  Scenarios share a body type; each has its own agent
+ * range, wall range, cell grid and timestep bounds.  Calls on one context
+ * are not reentrant; one context runs on one CUDA stream of the device that
+ * was current at cd_create.
+ *
+ * Reference interfaces each entry point replaces (paths inside the
+ * crowddynamics project):
+ *   cd_step / cd_run ...... MultiAgentSimulation.update()
+ *                           crowddynamics/simulation/multiagent.py:51-55 with
+ *                           the nodes of crowddynamics/simulation/logic.py:59-130,258-261
+ *   CD_NODE_AGENT_AGENT ... agent_agent_block_list, core/interactions.py:191-205
+ *   CD_NODE_AGENT_OBSTACLE  agent_obstacle, core/interactions.py:208-214
+ *   CD_NODE_ADJUSTING ..... force_adjust_agents / torque_adjust_agents,
+ *                           core/motion/adjusting.py:98-121
+ *   CD_NODE_ORIENTATION ... orient_towards_target_direction,
+ *                           core/steering/orientation.py:17-21
+ *   CD_NODE_INTEGRATE ..... velocity_verlet_integrator, core/integrator.py:209-256
+ *   CD_NODE_RESET ......... Reset.update, simulation/logic.py:59-64
+ *   CD_NODE_FLUCTUATION ... Fluctuation.update, simulation/logic.py:78-86
+ *                           (noise drawn on the host, passed by cd_set_noise)
+ *   cd_upload_agents /
+ *   cd_download_agents .... the in-place numpy structured agent arrays the
+ *                           nodes read and write (simulation/agents.py:447-448)
+ *   cd_set_walls .......... geom_to_linear_obstacles' obstacle_type_linear
+ *                           array, core/geometry.py:99-102, core/structures.py:6-9
+ */
+#ifndef CDGPU_H
+#define CDGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define CD_OK 0
+#define CD_ERR_INVALID_TYPE 1   /* body type / record layout not recognised  */
+#define CD_ERR_INVALID_VALUE 2  /* bad size, range or non-finite input       */
+#define CD_ERR_CUDA 3           /* a CUDA runtime call failed                 */
+#define CD_ERR_NOT_FINITE 4     /* a kernel saw a non-finite agent position   */
+#define CD_ERR_CAPACITY 5       /* an input exceeded a fixed capacity         */
+
+/* ---- body types -------------------------------------------------------- */
+#define CD_BODY_CIRCULAR 0
+#define CD_BODY_THREE_CIRCLE 1
+
+/* ---- logic nodes run by cd_step / cd_run (bit flags, post-order) ------- */
+#define CD_NODE_FLUCTUATION 1
+#define CD_NODE_ORIENTATION 2
+#define CD_NODE_ADJUSTING 4
+#define CD_NODE_AGENT_AGENT 8
+#define CD_NODE_AGENT_OBSTACLE 16
+#define CD_NODE_INTEGRATE 32
+#define CD_NODE_RESET 64
+#define CD_NODE_ALL 127
+
+/* ---- float64 fields of an agent record (offset-table order) ------------ */
+enum {
+    CD_F_POSITION = 0, CD_F_VELOCITY, CD_F_TARGET_DIRECTION, CD_F_FORCE,
+    CD_F_FORCE_PREV, CD_F_RADIUS, CD_F_R_T, CD_F_R_S, CD_F_R_TS, CD_F_MASS,
+    CD_F_INERTIA_ROT, CD_F_TARGET_VELOCITY, CD_F_TARGET_ANGULAR_VELOCITY,
+    CD_F_TAU_ADJ, CD_F_K_SOC, CD_F_TAU_0, CD_F_MU, CD_F_KAPPA, CD_F_DAMPING,
+    CD_F_STD_RAND_FORCE, CD_F_POSITION_LS, CD_F_POSITION_RS, CD_F_ORIENTATION,
+    CD_F_ANGULAR_VELOCITY, CD_F_TARGET_ORIENTATION, CD_F_TORQUE,
+    CD_F_TORQUE_PREV, CD_F_TAU_ROT, CD_F_STD_RAND_TORQUE, CD_F_COUNT
+};
+
+/* One scenario of a batch.  The cell grid covers [x0, x0 + nx*cell_size) x
+ * [y0, y0 + ny*cell_size); an agent outside it is binned into the nearest
+ * border cell, which keeps every interacting pair in adjacent cells.  The
+ * reference's default cell size is sight_soc + 2 * max_agent_radius
+ * (simulation/logic.py:97-116). */
+typedef struct {
+    int64_t agent_begin, agent_count;   /* range in the batch's agent array */
+    int64_t wall_begin, wall_count;     /* range in the batch's wall array  */
+    double x0, y0, cell_size;           /* grid origin and cell size (m)    */
+    int64_t nx, ny;                     /* grid shape (cells)               */
+    double dt_min, dt_max;              /* Integrator.dt_min / dt_max (s)   */
+} cd_scenario;
+
+typedef struct cd_ctx cd_ctx;
+
+/* Message of the last failed call on `ctx` (or of the last failed
+ * cd_create when ctx is NULL). */
+const char *cd_last_error(const cd_ctx *ctx);
+
+/* Create a context for `n_scenarios` scenarios of `body_type`.  Agent and
+ * wall ranges must tile [0, total) in scenario order.  Allocates all device
+ * memory the step needs. */
+int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios,
+              const cd_scenario *scenarios);
+void cd_destroy(cd_ctx *ctx);
+
+/* Copy `n` (= total agents) packed host records of `itemsize` bytes into the
+ * device.  `field_offsets` holds CD_F_COUNT byte offsets (-1 = absent);
+ * float64 fields must be 4-byte aligned.  Recomputes timestep maxima. */
+int cd_upload_agents(cd_ctx *ctx, const void *records, int64_t n,
+                     int64_t itemsize, const int64_t *field_offsets);
+/* Write the device state back into `n` packed host records.  Whole records
+ * are written: fields the device does not update keep the values of the
+ * last cd_upload_agents. */
+int cd_download_agents(cd_ctx *ctx, void *records, int64_t n, int64_t itemsize,
+                       const int64_t *field_offsets);
+
+/* Replace all walls: `n_walls` rows of (p0x, p0y, p1x, p1y) float64, split
+ * among scenarios by their wall ranges.  Walls are binned into the cells of
+ * their scenario's grid. */
+int cd_set_walls(cd_ctx *ctx, const double *walls, int64_t n_walls);
+
+/* Host-drawn fluctuation added by the next step that runs
+ * CD_NODE_FLUCTUATION: force (n x 2) and torque (n; ignored for Circular,
+ * may be NULL). */
+int cd_set_noise(cd_ctx *ctx, const double *force, const double *torque);
+
+/* Run one update with the selected nodes (CD_NODE_* flags).  If `dt` is not
+ * NULL the call waits for the step and writes each scenario's timestep. */
+int cd_step(cd_ctx *ctx, int nodes, double *dt);
+/* Run `steps` updates with the selected nodes as one CUDA-graph launch per
+ * step (captured on first use).  CD_NODE_FLUCTUATION is not allowed.
+ * Waits for completion and checks the device status. */
+int cd_run(cd_ctx *ctx, int nodes, int64_t steps);
+/* Wait for all work of the context and report device-side errors. */
+int cd_synchronize(cd_ctx *ctx);
+/* Per-scenario last timestep and accumulated time (simulation.data['dt'],
+ * simulation.data['time_tot']). */
+int cd_get_time(cd_ctx *ctx, double *dt, double *time_tot);
+
+/* Diagnostics: the cell list of the last step that ran CD_NODE_AGENT_AGENT
+ * (keys: flat cell index per agent within its scenario's grid; order: agent
+ * indices grouped by cell, ascending inside a cell; count/offset per cell of
+ * all scenarios, scenarios concatenated). */
+int cd_get_cell_list(cd_ctx *ctx, int64_t *keys, int64_t *order,
+                     int64_t *cells_count, int64_t *cells_offset);
+/* Diagnostics for the current state, per agent, CD_COUNT_COLS int64 each
+ * (row-major n x CD_COUNT_COLS): candidate partners (same or adjacent cell),
+ * partners that survive the conservative distance pre-check, partners with
+ * skin distance h < 3 (interacting), partners with h < 0 (contact), wall
+ * segments that survive the pre-check, walls in contact.  Summing a pair
+ * column over agents counts every unordered pair twice. */
+#define CD_COUNT_COLS 6
+int cd_pair_counts(cd_ctx *ctx, int64_t *counts);
+
+/* Total cells over all scenarios and agents/walls of the context. */
+int cd_sizes(const cd_ctx *ctx, int64_t *n_agents, int64_t *n_walls,
+             int64_t *n_cells);
+
+/* Timing: when enabled, cd_step records CUDA events on the context stream
+ * around the whole step and around the agent-force kernel, and cd_run
+ * around its graph launches; cd_kernel_time returns the accumulated
+ * milliseconds since the last cd_set_timing: force kernel (and its launch
+ * count), whole cd_step steps, and cd_run steps (and their count). */
+int cd_set_timing(cd_ctx *ctx, int enable);
+int cd_kernel_time(cd_ctx *ctx, double *force_ms, int64_t *force_launches,
+                   double *step_ms, double *run_ms, int64_t *run_steps);
+/* Number of kernels one step with `nodes` launches (memsets excluded). */
+int cd_kernels_per_step(const cd_ctx *ctx, int nodes, int64_t *kernels);
+
+/* Measured FP64 FMA throughput of the current device in GFLOP/s (2 flops
+ * per FMA), used as the roofline denominator. */
+int cd_measure_fp64_peak(double *gflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CDGPU_H */

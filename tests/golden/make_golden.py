@@ -1,0 +1,171 @@
+"""Generate the golden fixtures from the reference's own hot-path code.
+
+Run in a container that has the reference source tree (path from the
+CROWDDYNAMICS_REFERENCE environment variable, default /root/reference):
+
+    python tests/golden/make_golden.py
+
+It executes the reference's numba-decorated functions as plain Python via
+``oracle/ref_loader.py`` (numba, cell_lists and the agents module stubbed)
+on seeded inputs and stores inputs and outputs in ``tests/golden/*.npz``.
+Each case records the grid of the restated cell list it used.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import ref_loader as RL  # noqa: E402
+from crowddynamics_gb300 import scenarios as S  # noqa: E402
+from crowddynamics_gb300.simulation.agents import new_agents, shoulders  # noqa: E402
+
+NODES_ALL = ('fluctuation', 'orientation', 'adjusting', 'agent_agent', 'agent_obstacle',
+             'integrate', 'reset')
+
+
+def save(name, **arrays):
+    path = os.path.join(HERE, name + '.npz')
+    np.savez_compressed(path, **arrays)
+    print('wrote', path, os.path.getsize(path), 'bytes')
+
+
+def scenario_case(name, scen, steps, seed):
+    """Per-node outputs from the initial state, then `steps` full updates
+    with host-drawn noise."""
+    RL.configure_grid(*scen.grid)
+    init = scen.agents.copy()
+    out = dict(init=init, walls=scen.walls, grid=np.array(scen.grid, dtype=np.float64),
+               cell_size=np.float64(scen.cell_size), dt_min=np.float64(scen.dt_min),
+               dt_max=np.float64(scen.dt_max))
+    for node in ('agent_agent', 'agent_obstacle', 'adjusting', 'orientation'):
+        a = init.copy()
+        nodes = (node, 'orientation') if node == 'adjusting' else (node,)
+        RL.step(a, scen.cell_size, scen.walls, nodes=nodes)
+        out['node_' + node] = a
+    rng = np.random.default_rng(seed)
+    a = init.copy()
+    nf_all, nm_all, dts, states = [], [], [], []
+    for k in range(steps):
+        nf, nm = S.draw_noise(a, rng)
+        dt = RL.step(a, scen.cell_size, scen.walls, nf, nm, scen.dt_min, scen.dt_max,
+                     nodes=NODES_ALL)
+        nf_all.append(nf)
+        nm_all.append(nm if nm is not None else np.zeros(len(a)))
+        dts.append(dt)
+        states.append(a.copy())
+    out['noise_f'] = np.array(nf_all)
+    out['noise_m'] = np.array(nm_all)
+    out['dt'] = np.array(dts)
+    out['states'] = np.array(states)
+    save(name, **out)
+
+
+def pair_cases():
+    """Two-agent configurations covering the branches of the pair kernels:
+    co-moving (a == 0), head-on, contact (h < 0), coincident centres (d == 0),
+    tangential miss, tau > 30 cut-off, and a truncated (|F| > 2000 N) case."""
+    R = RL.load()
+    cases = []
+    for model in ('circular', 'three_circle'):
+        base = new_agents(2, model)
+        base['radius'] = 0.255
+        base['mass'] = 73.5
+        base['target_velocity'] = 1.0
+        if model == 'three_circle':
+            base['r_t'] = 0.5882 * 0.255
+            base['r_s'] = 0.3725 * 0.255
+            base['r_ts'] = 0.6275 * 0.255
+            base['inertia_rot'] = 4.0
+            base['target_angular_velocity'] = 4 * np.pi
+        configs = [
+            ((0, 0), (2, 0), (1, 0), (1, 0), 0.0, 0.0),          # co-moving
+            ((0, 0), (2, 0), (1, 0), (-1, 0), 0.0, np.pi),       # head-on
+            ((0, 0), (0.4, 0.05), (0.3, 0), (-0.2, 0.1), 0.3, 2.0),  # contact
+            ((1, 1), (1, 1), (0.5, 0), (0, 0.5), 0.0, 1.0),      # coincident
+            ((0, 0), (2, 2), (1, 0), (0, 0), 0.0, 0.0),          # miss
+            ((0, 0), (2.9, 0), (0.01, 0), (0, 0), 0.0, 0.0),     # slow approach, tau > 30
+            ((0, 0), (0.56, 0), (2, 0), (-2, 0), 0.0, np.pi),    # near contact, large force
+            ((0, 0), (1.1, 0.3), (0.2, -0.4), (-0.7, 0.1), -2.5, 0.7),
+            ((3, 3), (3.3, 3.6), (-0.4, 0.2), (0.9, -1.0), 3.0, -1.2),
+        ]
+        for xi, xj, vi, vj, phi_i, phi_j in configs:
+            a = base.copy()
+            a['position'] = [xi, xj]
+            a['velocity'] = [vi, vj]
+            if model == 'three_circle':
+                a['orientation'] = [phi_i, phi_j]
+                shoulders(a)
+            cases.append(a)
+    out = {}
+    for k, a in enumerate(cases):
+        out['in_%d' % k] = a
+        b = a.copy()
+        if 'position_ls' in a.dtype.fields:
+            R.interactions.interaction_agent_agent_three_circle(0, 1, b)
+            fi, fj = R.power_law.force_social_three_circle(a, 0, 1)
+        else:
+            R.interactions.interaction_agent_agent_circular(0, 1, b)
+            fi, fj = R.power_law.force_social_circular(a, 0, 1)
+        out['pair_%d' % k] = b
+        out['social_%d' % k] = np.array([fi, fj])
+    out['count'] = np.int64(len(cases))
+    save('pairs', **out)
+
+
+def wall_cases():
+    """Agent-wall branches: both endpoints, the interior, a zero-length wall,
+    an agent centred on the line."""
+    R = RL.load()
+    walls = S.walls_array([((0, 0), (4, 0)), ((5, -1), (5, 3)), ((2, 2), (2, 2)),
+                           ((-1, 2), (1, 4))])
+    out = {'walls': walls}
+    for model in ('circular', 'three_circle'):
+        pos = np.array([(-0.1, 0.1), (2.0, 0.2), (4.1, -0.1), (4.85, 1.0), (2.0, 0.0),
+                        (0.1, 2.95), (2.0, 2.1), (5.0, 3.2)])
+        a = new_agents(len(pos), model)
+        a['position'] = pos
+        a['radius'] = 0.27
+        a['velocity'] = [(0.3, -0.2)] * len(pos)
+        if model == 'three_circle':
+            a['r_t'], a['r_s'], a['r_ts'] = 0.16, 0.1, 0.1
+            a['orientation'] = np.linspace(-3, 3, len(pos))
+            shoulders(a)
+        out['in_' + model] = a
+        b = a.copy()
+        R.interactions.agent_obstacle(b, walls)
+        out['out_' + model] = b
+    save('walls', **out)
+
+
+def misc_cases():
+    """wrap_to_pi at odd multiples of pi and adaptive_timestep bounds."""
+    R = RL.load()
+    x = np.array([0.0, np.pi, -np.pi, 3 * np.pi, -3 * np.pi, 7.0, -7.0, 1e-300, -1e-300,
+                  100.0, -100.0, 2 * np.pi, -2 * np.pi, 0.5, -0.5])
+    w = np.array([R.vector2D.wrap_to_pi(float(v)) for v in x])
+    a = new_agents(5, 'circular')
+    a['velocity'] = [(0.1, 0), (0, 0.9), (1.3, 0.4), (0, 0), (0.2, 0.2)]
+    a['target_velocity'] = [1.0, 1.2, 0.8, 1.5, 0.9]
+    dts = np.array([R.integrator.adaptive_timestep(a, lo, hi)
+                    for lo, hi in ((0.001, 0.01), (0.01, 0.01), (0.0001, 0.002), (0.02, 0.5))])
+    z = new_agents(3, 'circular')
+    dt_zero = R.integrator.adaptive_timestep(z, 0.001, 0.01)
+    save('misc', wrap_x=x, wrap_y=w, dt_agents=a, dts=dts, dt_zero=np.float64(dt_zero))
+
+
+def main():
+    if not RL.available():
+        sys.exit('reference source tree not found; set CROWDDYNAMICS_REFERENCE')
+    scenario_case('hallway_small', S.hallway(n=120, width=20.0, height=6.0, seed=3), 3, 21)
+    scenario_case('room_small', S.room(n=150, size=12.0, seed=4), 3, 22)
+    pair_cases()
+    wall_cases()
+    misc_cases()
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,228 @@
+"""Device path vs the C oracle on seeded inputs, through the C ABI.
+
+Two levels:
+* against the oracle in exact-math mode (the device's elementary functions,
+  no fused multiply-add on either side) every float64 result must be
+  bit-identical, for single nodes, full steps and 50-step rollouts;
+* against the plain oracle (C library functions) per-step forces and
+  torques must agree within 1e-9 relative with a 1e-12 N (N m) floor.
+Integer work (cell keys, cell order, candidate counts) must match bit for
+bit.
+"""
+import numpy as np
+import pytest
+
+from conftest import assert_vec_close
+from crowddynamics_gb300 import _native as N
+from crowddynamics_gb300 import scenarios as S
+from crowddynamics_gb300.engine import DeviceBatch, batch_from_scenarios
+
+pytestmark = pytest.mark.gpu
+
+RTOL, ATOL = 1e-9, 1e-12
+
+
+def oracle_grid(O, scen):
+    return O.make_grid(*scen.grid)
+
+
+def device_step(scen, nodes, noise=None):
+    b, agents, _ = batch_from_scenarios([scen])
+    if noise is not None:
+        b.set_noise(*noise)
+    dt = b.step(nodes, want_dt=True)
+    out = agents.copy()
+    b.download(out)
+    b.close()
+    return out, dt[0]
+
+
+ORC = {N.NODE_FLUCTUATION: 1, N.NODE_ORIENTATION: 2, N.NODE_ADJUSTING: 4,
+       N.NODE_AGENT_AGENT: 8, N.NODE_AGENT_OBSTACLE: 16, N.NODE_INTEGRATE: 32,
+       N.NODE_RESET: 64}
+
+
+def orc_flags(nodes):
+    return sum(v for k, v in ORC.items() if nodes & k)
+
+
+def oracle_step(O, scen, nodes, noise=None, nthreads=1, exact=False):
+    a = scen.agents.copy()
+    nf, nm = noise if noise is not None else (None, None)
+    O.set_exact_math(exact)
+    try:
+        dt = O.step(a, oracle_grid(O, scen), scen.walls, nf, nm, flags=orc_flags(nodes),
+                    dt_min=scen.dt_min, dt_max=scen.dt_max, nthreads=nthreads)
+    finally:
+        O.set_exact_math(False)
+    return a, dt
+
+
+STATE = ('position', 'velocity', 'force', 'force_prev', 'torque', 'torque_prev',
+         'orientation', 'angular_velocity', 'target_orientation', 'position_ls',
+         'position_rs')
+
+
+def assert_identical(got, ref, what=''):
+    for f in STATE:
+        if f in ref.dtype.fields:
+            g, r = got[f], ref[f]
+            same = (g == r) | (np.isnan(g) & np.isnan(r))
+            if not same.all():
+                k = np.argwhere(~same)[0]
+                raise AssertionError('%s %s differs at %s: %r vs %r (%d values)' % (
+                    what, f, k, g[tuple(k)], r[tuple(k)], int((~same).sum())))
+
+
+SCENARIOS = {
+    'hallway': lambda: S.hallway(),
+    'room': lambda: S.room(),
+}
+
+
+@pytest.mark.parametrize('name', sorted(SCENARIOS))
+@pytest.mark.parametrize('nodes', [N.NODE_AGENT_AGENT, N.NODE_AGENT_OBSTACLE,
+                                   N.NODE_ADJUSTING | N.NODE_ORIENTATION])
+def test_node_forces(oracle, native, name, nodes):
+    scen = SCENARIOS[name]()
+    got, _ = device_step(scen, nodes)
+    assert_identical(got, oracle_step(oracle, scen, nodes, exact=True)[0], 'exact')
+    ref, _ = oracle_step(oracle, scen, nodes)
+    assert_vec_close(got['force'], ref['force'], RTOL, ATOL, 'force')
+    if scen.body == 'three_circle':
+        assert_vec_close(got['torque'], ref['torque'], RTOL, ATOL, 'torque')
+        assert_vec_close(got['target_orientation'], ref['target_orientation'], 1e-15, 1e-15,
+                         'target_orientation')
+
+
+@pytest.mark.parametrize('name', sorted(SCENARIOS))
+def test_full_step(oracle, native, name):
+    scen = SCENARIOS[name]()
+    rng = np.random.default_rng(11)
+    noise = S.draw_noise(scen.agents, rng)
+    got, dt_g = device_step(scen, N.NODE_ALL, noise)
+    exact, dt_e = oracle_step(oracle, scen, N.NODE_ALL, noise, exact=True)
+    assert dt_g == dt_e
+    assert_identical(got, exact, 'exact')
+    ref, dt_r = oracle_step(oracle, scen, N.NODE_ALL, noise)
+    assert abs(dt_g - dt_r) <= 1e-15 * dt_r
+    for f in ('force_prev', 'velocity', 'position'):
+        assert_vec_close(got[f], ref[f], RTOL, ATOL, f)
+    assert np.all(got['force'] == 0)
+    if scen.body == 'three_circle':
+        for f in ('torque_prev', 'angular_velocity', 'orientation'):
+            assert_vec_close(got[f], ref[f], RTOL, ATOL, f)
+        assert_vec_close(got['position_ls'], ref['position_ls'], RTOL, ATOL, 'position_ls')
+
+
+@pytest.mark.parametrize('name', sorted(SCENARIOS))
+def test_rollout_50_steps(oracle, native, name):
+    scen = SCENARIOS[name]()
+    rng = np.random.default_rng(5)
+    b, agents, _ = batch_from_scenarios([scen])
+    ref = scen.agents.copy()
+    grid = oracle_grid(oracle, scen)
+    t_ref = 0.0
+    with oracle.exact_math():
+        for k in range(50):
+            nf, nm = S.draw_noise(ref, rng)
+            b.set_noise(nf, nm)
+            b.step(N.NODE_ALL)
+            t_ref += oracle.step(ref, grid, scen.walls, nf, nm, dt_min=scen.dt_min,
+                                 dt_max=scen.dt_max)
+    got = agents.copy()
+    b.download(got)
+    dt, tt = b.time()
+    b.close()
+    assert_identical(got, ref, 'rollout')
+    assert tt[0] == t_ref
+    d = np.hypot(*(got['position'] - ref['position']).T)
+    assert d.max() <= 1e-6, d.max()
+
+
+def test_cell_list_bit_exact(oracle, native):
+    for scen in (S.hallway(), S.room(), S.large_field(n=20000, size=140.0, n_walls=100, seed=9)):
+        b, agents, _ = batch_from_scenarios([scen])
+        b.step(N.NODE_AGENT_AGENT)
+        keys, order, cnt, off = b.cell_list()
+        b.close()
+        x = np.ascontiguousarray(scen.agents['position'][:, 0])
+        y = np.ascontiguousarray(scen.agents['position'][:, 1])
+        k_ref, p_ref, c_ref, o_ref = oracle.cell_list(x, y, oracle_grid(oracle, scen))
+        assert np.array_equal(keys, k_ref)
+        assert np.array_equal(order, p_ref)
+        assert np.array_equal(cnt, c_ref)
+        assert np.array_equal(off, o_ref)
+
+
+def test_candidate_pairs_bit_exact(oracle, native):
+    """Per-agent number of candidate partners equals the restated cell_lists
+    pair set, and every partner the pre-check keeps is a candidate."""
+    for scen in (S.hallway(), S.room()):
+        b, agents, _ = batch_from_scenarios([scen])
+        counts = b.pair_counts()
+        cand, near = counts[:, 0], counts[:, 1]
+        b.close()
+        x = np.ascontiguousarray(scen.agents['position'][:, 0])
+        y = np.ascontiguousarray(scen.agents['position'][:, 1])
+        pairs = oracle.candidate_pairs(x, y, oracle_grid(oracle, scen))
+        ref = np.bincount(pairs.ravel(), minlength=len(x))
+        assert np.array_equal(cand, ref)
+        assert np.all(near <= cand)
+        # every pair within the social range must survive the pre-check
+        d = np.hypot(*(scen.agents['position'][pairs[:, 0]] - scen.agents['position'][pairs[:, 1]]).T)
+        close = pairs[d < 3.0]
+        need = np.bincount(close.ravel(), minlength=len(x))
+        assert np.all(near >= need)
+
+
+def test_large_field_forces(oracle, native):
+    """Full-size 100k ThreeCircle step: agent-agent + walls + adjusting vs the
+    oracle's agent-parallel restatement."""
+    scen = S.large_field()
+    nodes = N.NODE_ORIENTATION | N.NODE_ADJUSTING | N.NODE_AGENT_AGENT | N.NODE_AGENT_OBSTACLE
+    got, _ = device_step(scen, nodes)
+    assert_identical(got, oracle_step(oracle, scen, nodes, nthreads=16, exact=True)[0], 'exact')
+    ref, _ = oracle_step(oracle, scen, nodes, nthreads=16)
+    assert_vec_close(got['force'], ref['force'], RTOL, ATOL, 'force')
+    assert_vec_close(got['torque'], ref['torque'], RTOL, ATOL, 'torque')
+
+
+def test_deterministic(native):
+    scen = S.room()
+    outs = []
+    for _ in range(2):
+        b, agents, _ = batch_from_scenarios([scen])
+        b.run(20)
+        o = agents.copy()
+        b.download(o)
+        b.close()
+        outs.append(o)
+    assert outs[0].tobytes() == outs[1].tobytes()
+
+
+def test_graph_run_matches_steps(native):
+    scen = S.hallway()
+    b1, a1, _ = batch_from_scenarios([scen])
+    b2, a2, _ = batch_from_scenarios([scen])
+    nodes = N.NODE_ALL & ~N.NODE_FLUCTUATION
+    b1.run(10, nodes)
+    for _ in range(10):
+        b2.step(nodes)
+    o1, o2 = a1.copy(), a2.copy()
+    b1.download(o1)
+    b2.download(o2)
+    assert o1.tobytes() == o2.tobytes()
+    assert np.array_equal(b1.time()[1], b2.time()[1])
+    b1.close()
+    b2.close()
+
+
+def test_non_finite_position_raises(native):
+    from crowddynamics_gb300.exceptions import InvalidValue
+    scen = S.hallway()
+    scen.agents['position'][3] = (np.nan, 1.0)
+    b, agents, _ = batch_from_scenarios([scen])
+    with pytest.raises(InvalidValue):
+        b.step(N.NODE_AGENT_AGENT, want_dt=True)
+    b.close()
