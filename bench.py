@@ -231,6 +231,7 @@ def run_ours(args, ws, rank, local):
 
     # warm-up (graph capture happens here)
     b.run(max(args.warmup, 3), nodes)
+    b.synchronize()
     barrier()
     b.set_timing(True)
     with Clocks(local) as clk:

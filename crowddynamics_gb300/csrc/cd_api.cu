@@ -221,13 +221,19 @@ void enqueue_cells(cd_ctx *c, const StepArgs &a) {
     cdk::launch_gather(a, c->stream);
 }
 
-void enqueue_step(cd_ctx *c, int nodes, bool timed) {
+// One step on the context stream.  `timed`: record the step and force-kernel
+// events (cd_step).  `captured`: the sequence is being captured into a graph;
+// the force-kernel events are then recorded as external event-record nodes
+// (a plain cudaEventRecord under capture only marks a capture dependency).
+void enqueue_step(cd_ctx *c, int nodes, bool timed, bool captured = false) {
     StepArgs a = args_of(c, nodes);
     if (timed) cudaEventRecord(c->evs0, c->stream);
     enqueue_cells(c, a);
     if (timed) cudaEventRecord(c->ev0, c->stream);
+    if (captured) cudaEventRecordWithFlags(c->ev0, c->stream, cudaEventRecordExternal);
     cdk::launch_forces(a, c->stream);
     if (timed) cudaEventRecord(c->ev1, c->stream);
+    if (captured) cudaEventRecordWithFlags(c->ev1, c->stream, cudaEventRecordExternal);
     if (timed) cudaEventRecord(c->evs1, c->stream);
 }
 
@@ -240,6 +246,7 @@ int64_t kernels_per_step(const cd_ctx *c, int nodes) {
 }
 
 int check_device_error(cd_ctx *c) {
+    CUDA_OR_FAIL(c, cudaGetLastError());
     int h = 0;
     CUDA_OR_FAIL(c, cudaMemcpyAsync(&h, c->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
@@ -558,9 +565,11 @@ int cd_run(cd_ctx *c, int nodes, int64_t steps) {
     if (!c->graph || c->graph_nodes != nodes) {
         if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
         cudaGraph_t g;
+        CUDA_OR_FAIL(c, cudaGetLastError());
         CUDA_OR_FAIL(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-        enqueue_step(c, nodes, true);     // event records become graph nodes
+        enqueue_step(c, nodes, false, true);
         cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        if (e == cudaSuccess) e = cudaGetLastError();
         if (e != cudaSuccess) return fail(c, CD_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
         e = cudaGraphInstantiate(&c->graph, g, 0);
         cudaGraphDestroy(g);
@@ -569,6 +578,7 @@ int cd_run(cd_ctx *c, int nodes, int64_t steps) {
     }
     if (c->timing) cudaEventRecord(c->evr0, c->stream);
     for (int64_t k = 0; k < steps; ++k) CUDA_OR_FAIL(c, cudaGraphLaunch(c->graph, c->stream));
+    CUDA_OR_FAIL(c, cudaGetLastError());
     if (c->timing) {
         cudaEventRecord(c->evr1, c->stream);
         CUDA_OR_FAIL(c, cudaEventSynchronize(c->evr1));

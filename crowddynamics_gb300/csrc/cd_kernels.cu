@@ -499,9 +499,10 @@ __global__ void __launch_bounds__(SCAN_NT) k_scan_local(const int *in, int *out,
     }
 }
 
-__global__ void k_scan_add(int *out, const int *offs, int n) {
+__global__ void k_scan_add(int *out, const int *offs, int n, int nb) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] += offs[i / SCAN_TILE];
+    else if (i == n) out[n] = offs[nb];          // total
 }
 
 __global__ void k_scatter(StepArgs a) {
@@ -942,8 +943,7 @@ void launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s) {
     int *sums = scratch, *offs = scratch + nb + 1;
     k_scan_local<<<nb, SCAN_NT, 0, s>>>(in, out, sums, n);
     k_scan_local<<<1, SCAN_NT, 0, s>>>(sums, offs, nullptr, nb);   // offs[nb] = total
-    k_scan_add<<<nblk(n, 256), 256, 0, s>>>(out, offs, n);
-    cudaMemcpyAsync(out + n, offs + nb, sizeof(int), cudaMemcpyDeviceToDevice, s);
+    k_scan_add<<<nblk(n + 1, 256), 256, 0, s>>>(out, offs, n, nb);
 }
 void launch_scatter(const StepArgs &a, cudaStream_t s) {
     if (a.n <= 0) return;

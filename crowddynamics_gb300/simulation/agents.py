@@ -193,6 +193,9 @@ class Agents:
     """
 
     def __init__(self, agent_type='circular', array=None, size=0):
+        if array is not None:
+            agent_type = 'circular' if body_type_of(np.asarray(array)) == BODY_CIRCULAR \
+                else 'three_circle'
         if isinstance(agent_type, str):
             model = agent_type
         elif isinstance(agent_type, np.dtype):

@@ -813,3 +813,16 @@ double orc_step(char *base, int64_t n, int64_t itemsize, const int64_t *off, int
     if (flags & ORC_RESET) orc_reset(base, n, itemsize, off, body);
     return dt;
 }
+
+/* The shared elementary functions, exported for accuracy tests:
+ * which = 0 hypot(a, b), 1 exp(a), 2 sin(a), 3 cos(a), 4 atan2(a, b). */
+double orc_cdm(int which, double a, double b) {
+    switch (which) {
+    case 0: return cdm_hypot(a, b);
+    case 1: return cdm_exp(a);
+    case 2: return cdm_sin(a);
+    case 3: return cdm_cos(a);
+    case 4: return cdm_atan2(a, b);
+    default: return NAN;
+    }
+}

@@ -79,6 +79,8 @@ def lib():
         L.orc_candidate_pairs.restype = i64
         L.orc_set_exact_math.argtypes = [ctypes.c_int]
         L.orc_set_exact_math.restype = None
+        L.orc_cdm.argtypes = [ctypes.c_int, d, d]
+        L.orc_cdm.restype = d
         L.orc_wrap_to_pi.argtypes = [d]
         L.orc_wrap_to_pi.restype = d
         _lib = L
@@ -184,6 +186,12 @@ def reset(agents):
     """simulation/logic.py:59-64"""
     off = _offsets(agents)
     lib().orc_reset(_ptr(agents), len(agents), agents.dtype.itemsize, _ptr(off), _body(agents))
+
+
+def cdm(name, a, b=0.0):
+    """One of the shared elementary functions: hypot, exp, sin, cos, atan2."""
+    which = ('hypot', 'exp', 'sin', 'cos', 'atan2').index(name)
+    return lib().orc_cdm(which, float(a), float(b))
 
 
 def wrap_to_pi(x):
