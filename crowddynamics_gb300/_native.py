@@ -36,8 +36,14 @@ SYMBOLS = (
     'cd_download_agents', 'cd_set_walls', 'cd_set_noise', 'cd_step', 'cd_run',
     'cd_synchronize', 'cd_get_time', 'cd_get_cell_list', 'cd_pair_counts',
     'cd_sizes', 'cd_set_timing', 'cd_kernel_time', 'cd_kernels_per_step',
-    'cd_measure_fp64_peak',
+    'cd_measure_fp64_peak', 'cd_agent_agent_noalloc',
 )
+
+#: Limits and column order of cd_agent_agent_noalloc.
+NOALLOC_MAX_AGENTS = 16384
+NOALLOC_MAX_CELLS = 16384
+NA_COLS = ('x', 'y', 'vx', 'vy', 'mass', 'k_soc', 'tau_0', 'mu', 'kappa', 'damping', 'radius',
+           'r_t', 'r_s', 'r_ts', 'x_ls', 'y_ls', 'x_rs', 'y_rs', 'orientation')
 
 #: Columns of cd_pair_counts.
 COUNT_COLS = ('candidates', 'near', 'interacting', 'contact', 'walls_near', 'walls_contact')
@@ -93,6 +99,8 @@ def load(path=None):
         'cd_kernel_time': (ctypes.c_int, [P, pd, pi64, pd, pd, pi64]),
         'cd_kernels_per_step': (ctypes.c_int, [P, ctypes.c_int, pi64]),
         'cd_measure_fp64_peak': (ctypes.c_int, [pd]),
+        'cd_agent_agent_noalloc': (ctypes.c_int, [ctypes.c_int, i64, P, P, P, P, ctypes.c_double,
+                                                  ctypes.c_double, ctypes.c_double, i64, i64, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

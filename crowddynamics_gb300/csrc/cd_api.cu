@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <mutex>
 #include <vector>
 
 #include "cd_internal.cuh"
@@ -695,3 +696,149 @@ int cd_measure_fp64_peak(double *gflops) {
 }
 
 }  // extern "C"
+
+// ---- agent-agent forces without device allocation -------------------------
+//
+// The cell list and staging buffers of one agent-agent pass live in the
+// file-scope array below, carved at fixed 256-byte-aligned offsets.  Host code
+// never uses the array's name as an address: its device address comes from
+// cudaGetSymbolAddress, looked up once per device.
+
+namespace {
+
+constexpr size_t na_align(size_t b) { return (b + 255) & ~size_t(255); }
+constexpr int NA_N = CD_NOALLOC_MAX_AGENTS, NA_C = CD_NOALLOC_MAX_CELLS;
+constexpr size_t NA_OFF_SCEN = 0;
+constexpr size_t NA_OFF_SCEN_OF = NA_OFF_SCEN + na_align(sizeof(ScenDev));
+constexpr size_t NA_OFF_KEY = NA_OFF_SCEN_OF + na_align(sizeof(int) * NA_N);
+constexpr size_t NA_OFF_COUNT = NA_OFF_KEY + na_align(sizeof(int) * NA_N);
+constexpr size_t NA_OFF_FILL = NA_OFF_COUNT + na_align(sizeof(int) * NA_C);
+constexpr size_t NA_OFF_START = NA_OFF_FILL + na_align(sizeof(int) * NA_C);
+constexpr size_t NA_OFF_PERM_U = NA_OFF_START + na_align(sizeof(int) * (NA_C + 1));
+constexpr size_t NA_OFF_PERM = NA_OFF_PERM_U + na_align(sizeof(int) * NA_N);
+constexpr size_t NA_OFF_SCAN = NA_OFF_PERM + na_align(sizeof(int) * NA_N);
+constexpr size_t NA_SCAN_INTS = 2 * (NA_C / 4096 + 2);
+constexpr size_t NA_OFF_STAGE = NA_OFF_SCAN + na_align(sizeof(int) * NA_SCAN_INTS);
+constexpr size_t NA_OFF_CULL = NA_OFF_STAGE + na_align(sizeof(double2) * NA_N * cdk::STAGE_Q_TC);
+constexpr size_t NA_OFF_VMAX = NA_OFF_CULL + na_align(sizeof(float4) * NA_N);
+constexpr size_t NA_OFF_ERR = NA_OFF_VMAX + na_align(sizeof(unsigned long long));
+constexpr size_t NA_BYTES = NA_OFF_ERR + na_align(sizeof(int));
+
+__device__ __align__(256) static unsigned char g_noalloc_scratch[NA_BYTES];
+
+std::mutex g_na_mutex;
+unsigned char *g_na_base[256] = {};
+
+// Scenario record and per-agent scenario ids (all zero) for one call.
+__global__ void k_na_init(ScenDev *scen, int *scen_of, int n, double x0, double y0, double cell,
+                          int nx, int ny) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        ScenDev d;
+        d.x0 = x0; d.y0 = y0; d.cell = cell;
+        d.dt_min = 0.0; d.dt_max = 0.0; d.wall_reach = 0.0;
+        d.nx = nx; d.ny = ny; d.cell_base = 0;
+        d.agent_begin = 0; d.agent_count = n; d.wall_begin = 0; d.wall_count = 0;
+        *scen = d;
+    }
+    if (i < n) scen_of[i] = 0;
+}
+
+}  // namespace
+
+extern "C" int cd_agent_agent_noalloc(int body_type, int64_t n, const double *cols,
+                                      double *force_x, double *force_y, double *torque,
+                                      double x0, double y0, double cell_size, int64_t nx,
+                                      int64_t ny, void *stream_ptr) {
+    if (body_type != CD_BODY_CIRCULAR && body_type != CD_BODY_THREE_CIRCLE)
+        return fail(nullptr, CD_ERR_INVALID_TYPE, "unknown body type");
+    if (n < 0) return fail(nullptr, CD_ERR_INVALID_VALUE, "negative agent count");
+    if (n > CD_NOALLOC_MAX_AGENTS)
+        return fail(nullptr, CD_ERR_CAPACITY, "cd_agent_agent_noalloc: " + std::to_string(n) +
+                                                  " agents exceed CD_NOALLOC_MAX_AGENTS (" +
+                                                  std::to_string(CD_NOALLOC_MAX_AGENTS) + ")");
+    if (nx < 1 || ny < 1 || !(cell_size > 0) || !std::isfinite(cell_size) || !std::isfinite(x0) ||
+        !std::isfinite(y0))
+        return fail(nullptr, CD_ERR_INVALID_VALUE, "bad cell grid");
+    if (nx > CD_NOALLOC_MAX_CELLS || ny > CD_NOALLOC_MAX_CELLS || nx * ny > CD_NOALLOC_MAX_CELLS)
+        return fail(nullptr, CD_ERR_CAPACITY, "cd_agent_agent_noalloc: " + std::to_string(nx * ny) +
+                                                  " cells exceed CD_NOALLOC_MAX_CELLS (" +
+                                                  std::to_string(CD_NOALLOC_MAX_CELLS) + ")");
+    if (n == 0) return CD_OK;
+    if (!cols || !force_x || !force_y || (body_type == CD_BODY_THREE_CIRCLE && !torque))
+        return fail(nullptr, CD_ERR_INVALID_VALUE, "NULL column or output pointer");
+    cudaStream_t st = static_cast<cudaStream_t>(stream_ptr);
+    int dev = 0;
+    CUDA_OR_FAIL(nullptr, cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return fail(nullptr, CD_ERR_INVALID_VALUE, "device ordinal out of range");
+    unsigned char *base;
+    {
+        std::lock_guard<std::mutex> lock(g_na_mutex);
+        if (!g_na_base[dev]) {
+            void *p = nullptr;
+            CUDA_OR_FAIL(nullptr, cudaGetSymbolAddress(&p, g_noalloc_scratch));
+            g_na_base[dev] = static_cast<unsigned char *>(p);
+        }
+        base = g_na_base[dev];
+    }
+    const int ncells = (int)(nx * ny);
+    StepArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.n = (int)n;
+    a.n_scen = 1;
+    a.n_cells = ncells;
+    a.body = body_type;
+    a.nodes = cdk::N_AGENT;
+    const double *c = cols;
+    auto col = [&](int k) { return const_cast<double *>(c + (size_t)k * n); };
+    a.col[cdk::X] = col(CD_NA_X); a.col[cdk::Y] = col(CD_NA_Y);
+    a.col[cdk::VX] = col(CD_NA_VX); a.col[cdk::VY] = col(CD_NA_VY);
+    a.col[cdk::MASS] = col(CD_NA_MASS); a.col[cdk::K_SOC] = col(CD_NA_K_SOC);
+    a.col[cdk::TAU0] = col(CD_NA_TAU_0); a.col[cdk::MU] = col(CD_NA_MU);
+    a.col[cdk::KAPPA] = col(CD_NA_KAPPA); a.col[cdk::DAMP] = col(CD_NA_DAMPING);
+    a.col[cdk::FX] = force_x; a.col[cdk::FY] = force_y;
+    if (body_type == CD_BODY_CIRCULAR) {
+        a.col[cdk::R] = col(CD_NA_RADIUS);
+    } else {
+        a.col[cdk::RT] = col(CD_NA_R_T); a.col[cdk::RS] = col(CD_NA_R_S);
+        a.col[cdk::RTS] = col(CD_NA_R_TS);
+        a.col[cdk::XLS] = col(CD_NA_X_LS); a.col[cdk::YLS] = col(CD_NA_Y_LS);
+        a.col[cdk::XRS] = col(CD_NA_X_RS); a.col[cdk::YRS] = col(CD_NA_Y_RS);
+        a.col[cdk::PHI] = col(CD_NA_ORIENTATION);
+        a.col[cdk::PHI0] = col(CD_NA_ORIENTATION);     // read, never written (no orientation node)
+        a.col[cdk::TORQUE] = torque;
+    }
+    ScenDev *scen = reinterpret_cast<ScenDev *>(base + NA_OFF_SCEN);
+    int *scen_of = reinterpret_cast<int *>(base + NA_OFF_SCEN_OF);
+    a.scen = scen;
+    a.scen_of = scen_of;
+    a.key = reinterpret_cast<int *>(base + NA_OFF_KEY);
+    a.count = reinterpret_cast<int *>(base + NA_OFF_COUNT);
+    a.fill = reinterpret_cast<int *>(base + NA_OFF_FILL);
+    a.start = reinterpret_cast<int *>(base + NA_OFF_START);
+    a.perm_unsorted = reinterpret_cast<int *>(base + NA_OFF_PERM_U);
+    a.perm = reinterpret_cast<int *>(base + NA_OFF_PERM);
+    a.stage = reinterpret_cast<double2 *>(base + NA_OFF_STAGE);
+    a.cull = reinterpret_cast<float4 *>(base + NA_OFF_CULL);
+    a.vmax = reinterpret_cast<unsigned long long *>(base + NA_OFF_VMAX);
+    a.err = reinterpret_cast<int *>(base + NA_OFF_ERR);
+    int *scan = reinterpret_cast<int *>(base + NA_OFF_SCAN);
+    // the array keeps the previous call's contents: zero what must start at 0
+    CUDA_OR_FAIL(nullptr, cudaMemsetAsync(a.count, 0, sizeof(int) * ncells, st));
+    CUDA_OR_FAIL(nullptr, cudaMemsetAsync(a.fill, 0, sizeof(int) * ncells, st));
+    CUDA_OR_FAIL(nullptr, cudaMemsetAsync(a.vmax, 0, sizeof(unsigned long long), st));
+    CUDA_OR_FAIL(nullptr, cudaMemsetAsync(a.err, 0, sizeof(int), st));
+    k_na_init<<<(int)((n + 255) / 256), 256, 0, st>>>(scen, scen_of, (int)n, x0, y0, cell_size,
+                                                       (int)nx, (int)ny);
+    cdk::launch_prepare(a, st);
+    cdk::launch_scan(a.count, a.start, ncells, scan, st);
+    cdk::launch_scatter(a, st);
+    cdk::launch_gather(a, st);
+    cdk::launch_forces(a, st);
+    CUDA_OR_FAIL(nullptr, cudaGetLastError());
+    int h = 0;
+    CUDA_OR_FAIL(nullptr, cudaMemcpyAsync(&h, a.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_OR_FAIL(nullptr, cudaStreamSynchronize(st));
+    if (h & cdk::ERR_NOT_FINITE) return fail(nullptr, CD_ERR_NOT_FINITE, "an agent position is not finite");
+    return CD_OK;
+}

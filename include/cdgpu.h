@@ -172,6 +172,43 @@ int cd_kernels_per_step(const cd_ctx *ctx, int nodes, int64_t *kernels);
  * per FMA), used as the roofline denominator. */
 int cd_measure_fp64_peak(double *gflops);
 
+/* ---- agent-agent forces without any device allocation ------------------
+ * No counterpart in the reference: an extra entry point for callers that
+ * cannot allocate device memory while they run -- for example a host
+ * application that owns all device memory through its own pool, or code
+ * running where cudaMalloc is not allowed.  It computes the same
+ * agent-agent forces as CD_NODE_AGENT_AGENT for one scenario, but keeps its
+ * cell list and staging buffers in a fixed array that the library holds on
+ * every device that loads it, for the life of the process
+ * (about 3.4 MB).  It calls no cudaMalloc,
+ * cudaFree or allocating library routine.
+ *
+ * Limits: n <= CD_NOALLOC_MAX_AGENTS and nx * ny <= CD_NOALLOC_MAX_CELLS;
+ * larger inputs are rejected with CD_ERR_CAPACITY before any device work.
+ * `cols` is a device array of column-major float64 columns of length n,
+ * column k at cols + k * n, in CD_NA_* order (Circular reads columns 0-10,
+ * ThreeCircle reads 0-9 and 11-18).  Forces are added to the device arrays
+ * force_x / force_y (and the torque to `torque`, ThreeCircle only), as the
+ * reference adds to agents['force'] in place.  Work runs on `stream` (a
+ * cudaStream_t; NULL = default stream) and the call returns after it ends.
+ *
+ * The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any stream
+ * capture.  All calls share the one array: calls whose work overlaps on the
+ * GPU (other host threads, or other streams) race and must not be issued. */
+#define CD_NOALLOC_MAX_AGENTS 16384
+#define CD_NOALLOC_MAX_CELLS 16384
+enum {
+    CD_NA_X = 0, CD_NA_Y, CD_NA_VX, CD_NA_VY, CD_NA_MASS, CD_NA_K_SOC, CD_NA_TAU_0,
+    CD_NA_MU, CD_NA_KAPPA, CD_NA_DAMPING, CD_NA_RADIUS, CD_NA_R_T, CD_NA_R_S,
+    CD_NA_R_TS, CD_NA_X_LS, CD_NA_Y_LS, CD_NA_X_RS, CD_NA_Y_RS, CD_NA_ORIENTATION,
+    CD_NA_NCOLS
+};
+int cd_agent_agent_noalloc(int body_type, int64_t n, const double *cols,
+                           double *force_x, double *force_y, double *torque,
+                           double x0, double y0, double cell_size, int64_t nx,
+                           int64_t ny, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
