@@ -36,7 +36,7 @@ struct cd_ctx {
     int *key = nullptr, *count = nullptr, *fill = nullptr, *start = nullptr;
     int *perm_unsorted = nullptr, *perm = nullptr, *scan_scratch = nullptr;
     double2 *stage = nullptr;
-    float4 *cull = nullptr;
+    float4 *cull = nullptr, *stage_f = nullptr;
     double *walls_raw = nullptr, *walls = nullptr;
     float4 *walls_f = nullptr;
     int *wall_start = nullptr, *wall_idx = nullptr;
@@ -102,6 +102,7 @@ StepArgs args_of(cd_ctx *c, int nodes) {
     a.perm = c->perm;
     a.stage = c->stage;
     a.cull = c->cull;
+    a.stage_f = c->stage_f;
     a.walls = c->walls;
     a.walls_f = c->walls_f;
     a.wall_start = c->wall_start;
@@ -128,7 +129,7 @@ int dalloc(cd_ctx *c, T **p, int64_t count) {
 void release(cd_ctx *c) {
     if (c->graph) cudaGraphExecDestroy(c->graph);
     void *ptrs[] = {c->colbuf, c->scen_of, c->scen, c->key, c->count, c->fill, c->start,
-                    c->perm_unsorted, c->perm, c->scan_scratch, c->stage, c->cull,
+                    c->perm_unsorted, c->perm, c->scan_scratch, c->stage, c->cull, c->stage_f,
                     c->walls_raw, c->walls, c->walls_f, c->wall_start, c->wall_idx,
                     c->noise_f, c->noise_m, c->vmax, c->v0max, c->dt, c->time_tot,
                     c->err, c->diag, c->aos};
@@ -365,6 +366,9 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     int rc = CD_OK;
     auto step = [&](int r) { if (r && !rc) rc = r; return rc == CD_OK; };
     cudaGetDevice(&c->device);
+    if (int e = cdk::init_kernels())
+        rc = fail(c, CD_ERR_CUDA, std::string("kernel attributes: ") +
+                                     cudaGetErrorString((cudaError_t)e));
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
         rc = fail(c, CD_ERR_CUDA, "cudaStreamCreate failed");
     const int64_t npad = std::max<int64_t>(n, 1);
@@ -382,6 +386,7 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->scan_scratch, cdk::scan_scratch_ints((int)ncells)));
     step(dalloc(c, &c->stage, n * sq));
     step(dalloc(c, &c->cull, n));
+    step(dalloc(c, &c->stage_f, 2 * n));
     step(dalloc(c, &c->walls_raw, nw * 4));
     step(dalloc(c, &c->walls, nw * cdk::WALL_D));
     step(dalloc(c, &c->walls_f, nw));
@@ -720,9 +725,11 @@ constexpr size_t NA_OFF_SCAN = NA_OFF_PERM + na_align(sizeof(int) * NA_N);
 constexpr size_t NA_SCAN_INTS = 2 * (NA_C / 4096 + 2);
 constexpr size_t NA_OFF_STAGE = NA_OFF_SCAN + na_align(sizeof(int) * NA_SCAN_INTS);
 constexpr size_t NA_OFF_CULL = NA_OFF_STAGE + na_align(sizeof(double2) * NA_N * cdk::STAGE_Q_TC);
-constexpr size_t NA_OFF_VMAX = NA_OFF_CULL + na_align(sizeof(float4) * NA_N);
+constexpr size_t NA_OFF_STAGEF = NA_OFF_CULL + na_align(sizeof(float4) * NA_N);
+constexpr size_t NA_OFF_VMAX = NA_OFF_STAGEF + na_align(sizeof(float4) * 2 * NA_N);
 constexpr size_t NA_OFF_ERR = NA_OFF_VMAX + na_align(sizeof(unsigned long long));
 constexpr size_t NA_BYTES = NA_OFF_ERR + na_align(sizeof(int));
+static_assert(NA_BYTES < (4u << 20), "allocation-free scratch stays below 4 MiB");
 
 __device__ __align__(256) static unsigned char g_noalloc_scratch[NA_BYTES];
 
@@ -777,6 +784,9 @@ extern "C" int cd_agent_agent_noalloc(int body_type, int64_t n, const double *co
         if (!g_na_base[dev]) {
             void *p = nullptr;
             CUDA_OR_FAIL(nullptr, cudaGetSymbolAddress(&p, g_noalloc_scratch));
+            if (int e = cdk::init_kernels())
+                return fail(nullptr, CD_ERR_CUDA, std::string("kernel attributes: ") +
+                                                      cudaGetErrorString((cudaError_t)e));
             g_na_base[dev] = static_cast<unsigned char *>(p);
         }
         base = g_na_base[dev];
@@ -820,6 +830,7 @@ extern "C" int cd_agent_agent_noalloc(int body_type, int64_t n, const double *co
     a.perm = reinterpret_cast<int *>(base + NA_OFF_PERM);
     a.stage = reinterpret_cast<double2 *>(base + NA_OFF_STAGE);
     a.cull = reinterpret_cast<float4 *>(base + NA_OFF_CULL);
+    a.stage_f = reinterpret_cast<float4 *>(base + NA_OFF_STAGEF);
     a.vmax = reinterpret_cast<unsigned long long *>(base + NA_OFF_VMAX);
     a.err = reinterpret_cast<int *>(base + NA_OFF_ERR);
     int *scan = reinterpret_cast<int *>(base + NA_OFF_SCAN);

@@ -49,6 +49,8 @@ struct StepArgs {
     // staging (cell-sorted)
     double2 *stage;
     float4 *cull;                // (x, y, extent, -) as float
+    float4 *stage_f;             // ThreeCircle: 2 per slot, float32 geometry for
+                                 // the sub-circle pre-selection (see k_gather)
     // walls
     const double *walls;         // WALL_D doubles per wall
     const float4 *walls_f;       // (p0x, p0y, p1x, p1y) as float
@@ -79,5 +81,8 @@ void launch_aos_to_soa(const char *aos, long long itemsize, const long long *off
 void launch_soa_to_aos(char *aos, long long itemsize, const long long *off,
                        int n, int body, const double *const *col, cudaStream_t s);
 double fp64_peak_gflops();
+// Shared-memory bytes of the force kernel (dynamic) and one-time attributes.
+size_t forces_smem_bytes(int body);
+int init_kernels();
 
 }  // namespace cdk

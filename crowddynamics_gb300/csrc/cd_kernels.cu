@@ -143,160 +143,6 @@ __device__ __forceinline__ TC load_tc(const double2 *__restrict__ st, int slot) 
     return a;
 }
 
-// ---- pair interactions: the contribution to ONE side -------------------
-//
-// The reference evaluates each unordered pair once as (i, j), i being the
-// agent of the owner cell (core/interactions.py:152-166), and adds force_i to
-// i and force_j to j.  Here every agent sums its own side: P is the pair's
-// first agent, Q the second, and me_P says whether the calling agent is P.
-// Quantities shared by both sides (h, tau, gradient) are computed from (P, Q)
-// exactly as the reference does, so each side gets the reference's value.
-
-// interaction_agent_agent_circular, core/interactions.py:51-70, with
-// distance_circles (core/distance.py:16-47) and force_social_circular
-// (core/motion/power_law.py:213-259).
-__device__ __forceinline__ void pair_circular(const Circ &P, const Circ &Q, bool me_P,
-                                              double &fx, double &fy) {
-    double xx = P.x - Q.x, xy = P.y - Q.y;
-    double d = cdm_hypot(xx, xy);
-    double r_tot = P.r + Q.r;
-    double h = d - r_tot;
-    if (!(h < SIGTH_SOC)) return;
-    const Circ &M = me_P ? P : Q;
-    double vrx = P.vx - Q.vx, vry = P.vy - Q.vy;
-    double a = vrx * vrx + vry * vry;
-    double b = -(xx * vrx + xy * vry);
-    double c = (xx * xx + xy * xy) - r_tot * r_tot;
-    double disc = b * b - a * c;
-    double Fx = 0.0, Fy = 0.0;
-    // isnan(d) || d == 0 || a == 0  <=>  !(disc > 0) || a == 0
-    if (disc > 0 && a != 0) {
-        double dd = sqrt(disc);
-        double tau = (b - dd) / a;
-        if (!(tau <= 0 || tau > TAU_MAX)) {
-            double gx = (vrx - (vrx * b + xx * a) / dd) / a;
-            double gy = (vry - (vry * b + xy * a) / dd) / a;
-            double cm = (-M.m) * M.k;
-            double mag = magnitude(tau, M.tau0);
-            Fx = (cm * gx) * mag;
-            Fy = (cm * gy) * mag;
-            if (!me_P) { Fx = -Fx; Fy = -Fy; }     // force_j = 0 - (...)
-            truncate2(Fx, Fy, F_SOC_MAX);
-        }
-    }
-    if (h < 0) {
-        double nx = 0.0, ny = 0.0;
-        if (d != 0.0) { nx = xx / d; ny = xy / d; }
-        double cx, cy;
-        force_contact(h, nx, ny, vrx, vry, M.mu, M.kappa, M.damp, cx, cy);
-        if (me_P) { Fx = Fx + cx; Fy = Fy + cy; }
-        else { Fx = Fx - cx; Fy = Fy - cy; }
-    }
-    fx += Fx;
-    fy += Fy;
-}
-
-// interaction_agent_agent_three_circle, core/interactions.py:73-104, with
-// distance_three_circles (core/distance.py:50-105, incl. r_moment1 taken from
-// x0[j_min], :103) and force_social_three_circle (power_law.py:262-363: the
-// first defined root is accepted even if negative, no tau_max cut-off).
-__device__ __forceinline__ void pair_three_circle(const TC &P, const TC &Q, bool me_P,
-                                                  double &fx, double &fy, double &tq) {
-    // distance_three_circles: minimum over 3 x 3 sub-circles, first wins
-    double h_min = __longlong_as_double(0x7ff8000000000000LL);
-    double sdx = 0.0, sdy = 0.0, sd = 0.0;
-    int i_min = 0, j_min = 0;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        double ri = (i == 0) ? P.rt : P.rs;
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            double rj = (j == 0) ? Q.rt : Q.rs;
-            double dx = P.x[i] - Q.x[j], dy = P.y[i] - Q.y[j];
-            double d = cdm_hypot(dx, dy);
-            double h = d - (ri + rj);
-            if (h < h_min || isnan(h_min)) {
-                h_min = h; sdx = dx; sdy = dy; sd = d; i_min = i; j_min = j;
-            }
-        }
-    }
-    if (!(h_min < SIGTH_SOC)) return;
-    double nx = 0.0, ny = 0.0;
-    if (sd != 0.0) { nx = sdx / sd; ny = sdy / sd; }
-    // moment arm of the calling side
-    double rmx, rmy;
-    if (me_P) {
-        double r = (i_min == 0) ? P.rt : P.rs;
-        rmx = (sel3(P.x, i_min) + r * nx) - P.x[0];
-        rmy = (sel3(P.y, i_min) + r * ny) - P.y[0];
-    } else {
-        double r = (j_min == 0) ? Q.rt : Q.rs;
-        rmx = (sel3(P.x, j_min) - r * nx) - Q.x[0];
-        rmy = (sel3(P.y, j_min) - r * ny) - Q.y[0];
-    }
-    const TC &M = me_P ? P : Q;
-    double vrx = P.vx - Q.vx, vry = P.vy - Q.vy;
-    double a = vrx * vrx + vry * vry;
-    double Fx = 0.0, Fy = 0.0;
-    if (a != 0) {
-        double tau = __longlong_as_double(0x7ff8000000000000LL);
-        double b_min = 0.0, d_min = 0.0;
-        int ci = 0, cj = 0;
-#pragma unroll
-        for (int pi = 0; pi < 3; ++pi) {
-            double ri = (pi == 0) ? P.rt : P.rs;
-#pragma unroll
-            for (int pj = 0; pj < 3; ++pj) {
-                double rj = (pj == 0) ? Q.rt : Q.rs;
-                double xr = P.x[pi] - Q.x[pj], yr = P.y[pi] - Q.y[pj];
-                double r_tot = ri + rj;
-                double b = -(xr * vrx + yr * vry);
-                double c = (xr * xr + yr * yr) - r_tot * r_tot;
-                double disc = b * b - a * c;
-                if (!(disc > 0)) continue;           // isnan(d) or d == 0
-                double d = sqrt(disc);
-                double tau_new = (b - d) / a;
-                if (isnan(tau) || (0 < tau_new && tau_new < tau)) {
-                    ci = pi; cj = pj; tau = tau_new; b_min = b; d_min = d;
-                }
-            }
-        }
-        if (!(isnan(tau) || tau <= 0)) {
-            // r_off = r_off_i - r_off_j; r_off_k = +/- r_ts (sin phi, -cos phi)
-            // for a left/right shoulder contact part, 0 for the torso
-            double ox = 0.0, oy = 0.0;
-            if (ci != 0) {
-                double ex = P.rts * P.sn, ey = P.rts * (-P.cs);
-                ox = (ci == 1) ? (0.0 + ex) : (0.0 - ex);
-                oy = (ci == 1) ? (0.0 + ey) : (0.0 - ey);
-            }
-            if (cj != 0) {
-                double ex = Q.rts * Q.sn, ey = Q.rts * (-Q.cs);
-                ox = ox - ((cj == 1) ? (0.0 + ex) : (0.0 - ex));
-                oy = oy - ((cj == 1) ? (0.0 + ey) : (0.0 - ey));
-            }
-            double xr = P.x[0] - Q.x[0], yr = P.y[0] - Q.y[0];
-            double gx = (vrx - (a * (xr + 2 * ox) + b_min * vrx) / d_min) / a;
-            double gy = (vry - (a * (yr + 2 * oy) + b_min * vry) / d_min) / a;
-            double cm = (-M.m) * M.k;
-            double mag = magnitude(tau, M.tau0);
-            Fx = (cm * gx) * mag;
-            Fy = (cm * gy) * mag;
-            if (!me_P) { Fx = -Fx; Fy = -Fy; }
-            truncate2(Fx, Fy, F_SOC_MAX);
-        }
-    }
-    if (h_min < 0) {
-        double cx, cy;
-        force_contact(h_min, nx, ny, vrx, vry, M.mu, M.kappa, M.damp, cx, cy);
-        if (me_P) { Fx = Fx + cx; Fy = Fy + cy; }
-        else { Fx = Fx - cx; Fy = Fy - cy; }
-    }
-    fx += Fx;
-    fy += Fy;
-    tq += rmx * Fy - rmy * Fx;      // cross(r_moment, force)
-}
-
 // ---- walls -------------------------------------------------------------
 
 // distance_circle_line, core/distance.py:108-146 (wall tangent precomputed)
@@ -574,7 +420,13 @@ __global__ void k_gather(StepArgs a) {
         p[8] = make_double2(c[DAMP][i], sn);
         p[9] = make_double2(cs, 0.0);
         double e = extent_tc(x, y, c[XLS][i], c[YLS][i], c[XRS][i], c[YRS][i], c[RT][i], c[RS][i]);
-        a.cull[s] = make_float4((float)x, (float)y, up_f(e), 0.f);
+        float xh = (float)x, yh = (float)y;
+        a.cull[s] = make_float4(xh, yh, up_f(e), 0.f);
+        // position = float hi + float lo; shoulder centres relative to the torso
+        a.stage_f[2 * s] = make_float4((float)(x - (double)xh), (float)(y - (double)yh),
+                                       (float)c[RT][i], (float)c[RS][i]);
+        a.stage_f[2 * s + 1] = make_float4((float)(c[XLS][i] - x), (float)(c[YLS][i] - y),
+                                           (float)(c[XRS][i] - x), (float)(c[YRS][i] - y));
     }
 }
 
@@ -616,11 +468,323 @@ __device__ __forceinline__ void for_candidates(const StepArgs &a, const ScenDev 
     }
 }
 
+// ---- agent-agent evaluation in the calling agent's frame -------------------
+//
+// The reference evaluates pair (i, j) once with i the owner and adds force_i
+// to i and force_j to j.  Each agent here evaluates its own side with
+// relative quantities taken as (me - other).  Every shared quantity of the
+// reference's (P, Q) frame is then either identical (a, b, c, disc, d, tau,
+// h: products or sums of two negated values, sums of the same radii) or
+// exactly negated (x_rel, v_rel, r_off, n, the gradient), because IEEE
+// negation is exact.  Working it through the reference formulas, the calling
+// agent's contribution is the same expression for both sides:
+//   F = truncate((-m k) * grad_me * magnitude(tau, tau0_me)) + contact_me
+//   r_moment = (X[part_me] + r_me[part_me] * n_me) - x_me_torso
+// where X is the first agent's part positions (the reference takes
+// r_moment1 from x0[j_min], core/distance.py:103).  Orientation therefore only
+// decides the order in which the 3 x 3 sub-circle pairs are visited (first
+// minimum of h, first defined root, strict "<" replacement), which follows
+// the first agent's parts in the outer loop.
+
+// Sequence position k (first agent's part k / 3, second's k % 3) to the
+// calling agent's part (mine) and the other agent's part (theirs).
+__device__ __forceinline__ void seq_parts(int k, bool me_first, int &mine, int &theirs) {
+    int p = k / 3, q = k - 3 * (k / 3);
+    mine = me_first ? p : q;
+    theirs = me_first ? q : p;
+}
+
+__device__ __forceinline__ double part_r(const TC &A, int k) { return k == 0 ? A.rt : A.rs; }
+
+// r_off contribution of one agent's contact part: +/- r_ts (sin phi, -cos phi)
+// for the left / right shoulder, 0 for the torso (power_law.py:337-350).
+__device__ __forceinline__ void r_off_part(const TC &A, int part, double &ox, double &oy) {
+    double ex = A.rts * A.sn, ey = A.rts * (-A.cs);
+    ox = part == 1 ? (0.0 + ex) : (part == 2 ? (0.0 - ex) : 0.0);
+    oy = part == 1 ? (0.0 + ey) : (part == 2 ? (0.0 - ey) : 0.0);
+}
+
+// Circular pair, calling agent A, other agent B (interactions.py:51-70).
+__device__ __forceinline__ void pair_circular_me(const Circ &A, const Circ &B, double &fx,
+                                                 double &fy) {
+    double xx = A.x - B.x, xy = A.y - B.y;
+    double d = cdm_hypot(xx, xy);
+    double r_tot = A.r + B.r;
+    double h = d - r_tot;
+    if (!(h < SIGTH_SOC)) return;
+    double vrx = A.vx - B.vx, vry = A.vy - B.vy;
+    double a = vrx * vrx + vry * vry;
+    double b = -(xx * vrx + xy * vry);
+    double c = (xx * xx + xy * xy) - r_tot * r_tot;
+    double disc = b * b - a * c;
+    double Fx = 0.0, Fy = 0.0;
+    if (disc > 0 && a != 0) {                     // isnan(d) or d == 0 or a == 0
+        double dd = sqrt(disc);
+        double tau = (b - dd) / a;
+        if (!(tau <= 0 || tau > TAU_MAX)) {
+            double gx = (vrx - (vrx * b + xx * a) / dd) / a;
+            double gy = (vry - (vry * b + xy * a) / dd) / a;
+            double cm = (-A.m) * A.k;
+            double mag = magnitude(tau, A.tau0);
+            Fx = (cm * gx) * mag;
+            Fy = (cm * gy) * mag;
+            truncate2(Fx, Fy, F_SOC_MAX);
+        }
+    }
+    if (h < 0) {
+        double nx = 0.0, ny = 0.0;
+        if (d != 0.0) { nx = xx / d; ny = xy / d; }
+        double cx, cy;
+        force_contact(h, nx, ny, vrx, vry, A.mu, A.kappa, A.damp, cx, cy);
+        Fx = Fx + cx;
+        Fy = Fy + cy;
+    }
+    fx += Fx;
+    fy += Fy;
+}
+
+// Per-warp queue for the square root and division of the defined sub-circle
+// pairs of the warp's 32 current pairs (9 slots per lane).
+struct WarpQueue {
+    double b[32 * 9];
+    double disc[32 * 9];       // in: discriminant; out: its square root
+    double tau[32 * 9];
+    double a[32];
+    int off[33];
+};
+
+constexpr float PRESEL_MARGIN = 1e-4f;   // metres (float32 error of h is ~1e-6 m)
+
+// One ThreeCircle pair step for every lane of the warp (collective: all lanes
+// in `wmask` call it; `act` lanes have a pair, `me_first` its orientation).
+__device__ __forceinline__ void tc_pair_step(const TC &A, const float4 meC, const float4 meF0,
+                                             const float4 meF1, const StepArgs &a, bool act,
+                                             int t, bool me_first, WarpQueue &q, int lane,
+                                             unsigned wmask, int nlanes, double &fx, double &fy,
+                                             double &tq) {
+    TC B = A;
+    float4 oC = meC, oF0 = meF0, oF1 = meF1;
+    if (act) {
+        B = load_tc(a.stage, t);
+        oC = __ldg(&a.cull[t]);
+        oF0 = __ldg(&a.stage_f[2 * t]);
+        oF1 = __ldg(&a.stage_f[2 * t + 1]);
+    }
+    // -- distance_three_circles: float32 pre-selection of the minimum --
+    const float dxt = (meC.x - oC.x) + (meF0.x - oF0.x);
+    const float dyt = (meC.y - oC.y) + (meF0.y - oF0.y);
+    const float mox[3] = {0.f, meF1.x, meF1.z}, moy[3] = {0.f, meF1.y, meF1.w};
+    const float oox[3] = {0.f, oF1.x, oF1.z}, ooy[3] = {0.f, oF1.y, oF1.w};
+    const float mr[3] = {meF0.z, meF0.w, meF0.w}, orr[3] = {oF0.z, oF0.w, oF0.w};
+    float hf[9];
+    float hfmin = INFINITY;
+    bool anynan = false;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            float dx = (dxt + mox[i]) - oox[j], dy = (dyt + moy[i]) - ooy[j];
+            float h = sqrtf(dx * dx + dy * dy) - (mr[i] + orr[j]);
+            hf[3 * i + j] = h;
+            anynan |= (h != h);
+            hfmin = fminf(hfmin, h);
+        }
+    // candidates in visiting order (bit k: sequence position k); the margin
+    // covers float32 rounding of every input and operation above (each below
+    // 2^-24 of the magnitudes involved) many times over
+    const float scale = fabsf(dxt) + fabsf(dyt) + fabsf(meF1.x) + fabsf(meF1.y) + fabsf(meF1.z) +
+                        fabsf(meF1.w) + fabsf(oF1.x) + fabsf(oF1.y) + fabsf(oF1.z) + fabsf(oF1.w) +
+                        mr[0] + mr[1] + orr[0] + orr[1];
+    const float margin = PRESEL_MARGIN + 1e-6f * scale;
+    unsigned seq = 0;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        int p = k / 3, qq = k % 3;
+        float hk = me_first ? hf[3 * p + qq] : hf[3 * qq + p];
+        if (hk <= hfmin + margin) seq |= 1u << k;
+    }
+    if (anynan) seq = 0x1ffu;
+    if (!act) seq = 1u;
+    // exact float64 minimum over the candidates, first in visiting order wins
+    double h_min = __longlong_as_double(0x7ff8000000000000LL);
+    double sdx = 0.0, sdy = 0.0, sd = 0.0;
+    int mine_min = 0, theirs_min = 0;
+    {
+        int k = __ffs(seq) - 1;
+        unsigned rest = seq & (seq - 1);
+        int mi, ti;
+        seq_parts(k, me_first, mi, ti);
+        double dx = sel3(A.x, mi) - sel3(B.x, ti), dy = sel3(A.y, mi) - sel3(B.y, ti);
+        double d = cdm_hypot(dx, dy);
+        h_min = d - (part_r(A, mi) + part_r(B, ti));
+        sdx = dx; sdy = dy; sd = d; mine_min = mi; theirs_min = ti;
+        while (rest) {
+            k = __ffs(rest) - 1;
+            rest &= rest - 1;
+            seq_parts(k, me_first, mi, ti);
+            dx = sel3(A.x, mi) - sel3(B.x, ti);
+            dy = sel3(A.y, mi) - sel3(B.y, ti);
+            d = cdm_hypot(dx, dy);
+            double h = d - (part_r(A, mi) + part_r(B, ti));
+            if (h < h_min || isnan(h_min)) {
+                h_min = h; sdx = dx; sdy = dy; sd = d; mine_min = mi; theirs_min = ti;
+            }
+        }
+    }
+    const bool inter = act && (h_min < SIGTH_SOC);
+    double nx = 0.0, ny = 0.0;
+    if (inter && sd != 0.0) { nx = sdx / sd; ny = sdy / sd; }
+    // moment arm: (X[part_me] + r_me * n) - x_me_torso, X the first agent's parts
+    double rmx, rmy;
+    {
+        double xs = me_first ? sel3(A.x, mine_min) : sel3(B.x, mine_min);
+        double ys = me_first ? sel3(A.y, mine_min) : sel3(B.y, mine_min);
+        double r = part_r(A, mine_min);
+        rmx = (xs + r * nx) - A.x[0];
+        rmy = (ys + r * ny) - A.y[0];
+    }
+    // -- force_social_three_circle --
+    const double vrx = A.vx - B.vx, vry = A.vy - B.vy;
+    const double av = vrx * vrx + vry * vry;
+    const bool soc = inter && av != 0;
+    unsigned defmask = 0;
+    int cnt = 0;
+    double* qb = q.b + lane * 9;
+    double* qd = q.disc + lane * 9;
+    if (soc) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            int mi, ti;
+            seq_parts(k, me_first, mi, ti);
+            double xr = sel3(A.x, mi) - sel3(B.x, ti), yr = sel3(A.y, mi) - sel3(B.y, ti);
+            double r_tot = part_r(A, mi) + part_r(B, ti);
+            double b = -(xr * vrx + yr * vry);
+            double c = (xr * xr + yr * yr) - r_tot * r_tot;
+            double disc = b * b - av * c;
+            if (disc > 0) {                        // sqrt defined and non-zero
+                qb[cnt] = b;
+                qd[cnt] = disc;
+                ++cnt;
+                defmask |= 1u << k;
+            }
+        }
+    }
+    // warp exclusive scan of the item counts (active lanes are a prefix)
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int v = __shfl_up_sync(wmask, incl, o);
+        if (lane >= o) incl += v;
+    }
+    q.off[lane] = incl - cnt;
+    q.a[lane] = av;
+    const int total = __shfl_sync(wmask, incl, nlanes - 1);
+    if (lane == nlanes - 1) q.off[nlanes] = incl;
+    __syncwarp(wmask);
+    for (int base = 0; base < total; base += nlanes) {     // only nlanes lanes are live
+        int it = base + lane;
+        if (it < total) {
+            int lo = 0, hi = nlanes - 1;        // owner: last lane with off <= it
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (q.off[mid] <= it) lo = mid; else hi = mid - 1;
+            }
+            int slot = lo * 9 + (it - q.off[lo]);
+            double d = sqrt(q.disc[slot]);
+            q.tau[slot] = (q.b[slot] - d) / q.a[lo];
+            q.disc[slot] = d;
+        }
+    }
+    __syncwarp(wmask);
+    double tau = __longlong_as_double(0x7ff8000000000000LL);
+    double b_min = 0.0, d_min = 0.0;
+    int k_sel = 0;
+    {
+        int jj = 0;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            if (defmask & (1u << k)) {
+                double tau_new = q.tau[lane * 9 + jj];
+                double dk = qd[jj], bk = qb[jj];
+                ++jj;
+                if (isnan(tau) || (0 < tau_new && tau_new < tau)) {
+                    k_sel = k; tau = tau_new; b_min = bk; d_min = dk;
+                }
+            }
+        }
+    }
+    __syncwarp(wmask);
+    double Fx = 0.0, Fy = 0.0;
+    if (soc && !(isnan(tau) || tau <= 0)) {
+        int mi, ti;
+        seq_parts(k_sel, me_first, mi, ti);
+        double o1x, o1y, o2x, o2y;
+        r_off_part(A, mi, o1x, o1y);
+        r_off_part(B, ti, o2x, o2y);
+        double ox = o1x - o2x, oy = o1y - o2y;
+        double xr = A.x[0] - B.x[0], yr = A.y[0] - B.y[0];
+        double gx = (vrx - (av * (xr + 2 * ox) + b_min * vrx) / d_min) / av;
+        double gy = (vry - (av * (yr + 2 * oy) + b_min * vry) / d_min) / av;
+        double cm = (-A.m) * A.k;
+        double mag = magnitude(tau, A.tau0);
+        Fx = (cm * gx) * mag;
+        Fy = (cm * gy) * mag;
+        truncate2(Fx, Fy, F_SOC_MAX);
+    }
+    if (inter && h_min < 0) {
+        double cx, cy;
+        force_contact(h_min, nx, ny, vrx, vry, A.mu, A.kappa, A.damp, cx, cy);
+        Fx = Fx + cx;
+        Fy = Fy + cy;
+    }
+    if (inter) {
+        fx += Fx;
+        fy += Fy;
+        tq += rmx * Fy - rmy * Fx;                 // cross(r_moment, force)
+    }
+}
+
+// Resumable candidate enumeration into the thread's list (visiting order:
+// 3 x 3 cells in (dx, dy) lexicographic order, each cell ascending).
+struct EnumState { int ck, t; };
+
+__device__ __forceinline__ int enumerate_candidates(const StepArgs &a, const ScenDev &sc, int s,
+                                                    int my_cell, float4 me, int *mylist,
+                                                    EnumState &st) {
+    int local = my_cell - sc.cell_base;
+    int ix = local / sc.ny, iy = local - ix * sc.ny;
+    int nl = 0;
+    for (; st.ck < 9; ++st.ck, st.t = -1) {
+        int dx = st.ck / 3 - 1, dy = st.ck % 3 - 1;
+        int jx = ix + dx, jy = iy + dy;
+        if (jx < 0 || jx >= sc.nx || jy < 0 || jy >= sc.ny) continue;
+        int c2 = sc.cell_base + jx * sc.ny + jy;
+        int e = __ldg(&a.start[c2 + 1]);
+        if (st.t < 0) st.t = __ldg(&a.start[c2]);
+        bool fwd = (dx > 0) || (dx == 0 && dy > 0);
+        bool same = (dx == 0 && dy == 0);
+        for (; st.t < e; ++st.t) {
+            int t = st.t;
+            if (t == s) continue;
+            if (pair_far(me, __ldg(&a.cull[t]))) continue;
+            if (nl == LIST_CAP) return nl;       // resume at this candidate
+            mylist[nl * NT_FORCES] = (same ? (s < t) : fwd) ? ~t : t;
+            ++nl;
+        }
+    }
+    return nl;
+}
+
 template <int BODY>
 __global__ void __launch_bounds__(NT_FORCES) k_forces(StepArgs a) {
-    __shared__ int list[LIST_CAP * NT_FORCES];
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    extern __shared__ unsigned char smem[];
+    int *list = reinterpret_cast<int *>(smem);
+    WarpQueue *wq = reinterpret_cast<WarpQueue *>(smem + sizeof(int) * LIST_CAP * NT_FORCES);
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned wmask = __ballot_sync(0xffffffffu, s < a.n);
     if (s >= a.n) return;
+    const int lane = threadIdx.x & 31;
+    const int nlanes = __popc(wmask);           // active lanes form a prefix
     const int i = a.perm[s];
     const int sid = a.scen_of[i];
     const ScenDev sc = a.scen[sid];
@@ -653,45 +817,38 @@ __global__ void __launch_bounds__(NT_FORCES) k_forces(StepArgs a) {
         }
     }
 
-    // Agent-agent (core/interactions.py:147-166)
+    // Agent-agent (core/interactions.py:147-166), contributions summed in the
+    // reference's visiting order for this agent
     if (nodes & N_AGENT) {
         int *mylist = list + threadIdx.x;
+        EnumState st{0, -1};
         if (BODY == 0) {
             const Circ A = load_circ(a.stage, s);
-            int nl = 0;
-            auto flush = [&]() {
+            while (true) {
+                int nl = enumerate_candidates(a, sc, s, my_cell, me, mylist, st);
                 for (int k = 0; k < nl; ++k) {
                     int v = mylist[k * NT_FORCES];
-                    bool first = v < 0;
-                    const Circ B = load_circ(a.stage, first ? ~v : v);
-                    if (first) pair_circular(A, B, true, fx, fy);
-                    else pair_circular(B, A, false, fx, fy);
+                    const Circ B = load_circ(a.stage, v < 0 ? ~v : v);
+                    pair_circular_me(A, B, fx, fy);
                 }
-                nl = 0;
-            };
-            for_candidates(a, sc, s, my_cell, me, [&](int t, bool first) {
-                mylist[nl * NT_FORCES] = first ? ~t : t;
-                if (++nl == LIST_CAP) flush();
-            }, (int *)nullptr);
-            flush();
+                if (st.ck >= 9) break;
+            }
         } else {
             const TC A = load_tc(a.stage, s);
-            int nl = 0;
-            auto flush = [&]() {
-                for (int k = 0; k < nl; ++k) {
-                    int v = mylist[k * NT_FORCES];
-                    bool first = v < 0;
-                    const TC B = load_tc(a.stage, first ? ~v : v);
-                    if (first) pair_three_circle(A, B, true, fx, fy, tq);
-                    else pair_three_circle(B, A, false, fx, fy, tq);
+            const float4 meF0 = a.stage_f[2 * s], meF1 = a.stage_f[2 * s + 1];
+            WarpQueue &q = wq[threadIdx.x >> 5];
+            while (true) {
+                int nl = enumerate_candidates(a, sc, s, my_cell, me, mylist, st);
+                int kmax = __reduce_max_sync(wmask, (unsigned)nl);
+                for (int k = 0; k < kmax; ++k) {
+                    bool act = k < nl;
+                    int v = act ? mylist[k * NT_FORCES] : 0;
+                    int t = v < 0 ? ~v : v;
+                    tc_pair_step(A, me, meF0, meF1, a, act, t, v < 0, q, lane, wmask, nlanes,
+                                 fx, fy, tq);
                 }
-                nl = 0;
-            };
-            for_candidates(a, sc, s, my_cell, me, [&](int t, bool first) {
-                mylist[nl * NT_FORCES] = first ? ~t : t;
-                if (++nl == LIST_CAP) flush();
-            }, (int *)nullptr);
-            flush();
+                if (!__any_sync(wmask, st.ck < 9)) break;
+            }
         }
     }
 
@@ -953,10 +1110,25 @@ void launch_scatter(const StepArgs &a, cudaStream_t s) {
 void launch_gather(const StepArgs &a, cudaStream_t s) {
     if (a.n > 0) k_gather<<<nblk(a.n, 128), 128, 0, s>>>(a);
 }
+size_t forces_smem_bytes(int body) {
+    size_t b = sizeof(int) * LIST_CAP * NT_FORCES;
+    if (body == 1) b += sizeof(WarpQueue) * (NT_FORCES / 32);
+    return b;
+}
+int init_kernels() {
+    cudaError_t e = cudaFuncSetAttribute(k_forces<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)forces_smem_bytes(1));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_forces<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)forces_smem_bytes(0));
+    return e == cudaSuccess ? 0 : (int)e;
+}
 void launch_forces(const StepArgs &a, cudaStream_t s) {
     if (a.n <= 0) return;
-    if (a.body == 0) k_forces<0><<<nblk(a.n, NT_FORCES), NT_FORCES, 0, s>>>(a);
-    else k_forces<1><<<nblk(a.n, NT_FORCES), NT_FORCES, 0, s>>>(a);
+    if (a.body == 0)
+        k_forces<0><<<nblk(a.n, NT_FORCES), NT_FORCES, forces_smem_bytes(0), s>>>(a);
+    else
+        k_forces<1><<<nblk(a.n, NT_FORCES), NT_FORCES, forces_smem_bytes(1), s>>>(a);
 }
 void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s) {
     if (a.n > 0) k_pair_counts<<<nblk(a.n, 128), 128, 0, s>>>(a, counts);

@@ -180,7 +180,7 @@ int cd_measure_fp64_peak(double *gflops);
  * agent-agent forces as CD_NODE_AGENT_AGENT for one scenario, but keeps its
  * cell list and staging buffers in a fixed array that the library holds on
  * every device that loads it, for the life of the process
- * (about 3.4 MB).  It calls no cudaMalloc,
+ * (about 3.9 MB).  It calls no cudaMalloc,
  * cudaFree or allocating library routine.
  *
  * Limits: n <= CD_NOALLOC_MAX_AGENTS and nx * ny <= CD_NOALLOC_MAX_CELLS;

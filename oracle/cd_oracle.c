@@ -826,3 +826,120 @@ double orc_cdm(int which, double a, double b) {
     default: return NAN;
     }
 }
+
+/* ---- the same pair sums evaluated in each agent's own frame -------------
+ * Test support for the device kernel's formulation: every agent evaluates
+ * each of its pairs with relative quantities (me - other), visiting the 3 x 3
+ * sub-circle pairs in the owner-first order.  Must equal orc_agent_agent bit
+ * for bit (ThreeCircle only). */
+static void tc_pair_me(const arr_t *A, int64_t me, int64_t ot, int me_first,
+                       double *fx, double *fy, double *tq) {
+    v2 xm[3], xo[3];
+    double rm[3], ro[3];
+    three_parts(A, me, xm, rm);
+    three_parts(A, ot, xo, ro);
+    double h_min = NAN, sdx = 0, sdy = 0, sd = 0;
+    int mine_min = 0;
+    for (int k = 0; k < 9; ++k) {
+        int p = k / 3, q = k % 3, mi = me_first ? p : q, ti = me_first ? q : p;
+        double dx = xm[mi].x - xo[ti].x, dy = xm[mi].y - xo[ti].y;
+        double d = m_hypot(dx, dy);
+        double h = d - (rm[mi] + ro[ti]);
+        if (h < h_min || isnan(h_min)) { h_min = h; sdx = dx; sdy = dy; sd = d; mine_min = mi; }
+    }
+    if (!(h_min < SIGTH_SOC)) return;
+    double nx = 0, ny = 0;
+    if (sd != 0) { nx = sdx / sd; ny = sdy / sd; }
+    v2 xs = me_first ? xm[mine_min] : xo[mine_min];
+    double rmx = (xs.x + rm[mine_min] * nx) - xm[0].x;
+    double rmy = (xs.y + rm[mine_min] * ny) - xm[0].y;
+    v2 vm = ld2(A, me, F_VELOCITY), vo = ld2(A, ot, F_VELOCITY);
+    double vrx = vm.x - vo.x, vry = vm.y - vo.y;
+    double a = vrx * vrx + vry * vry;
+    double Fx = 0, Fy = 0;
+    if (a != 0) {
+        double tau = NAN, b_min = 0, d_min = 0;
+        int k_sel = 0;
+        for (int k = 0; k < 9; ++k) {
+            int p = k / 3, q = k % 3, mi = me_first ? p : q, ti = me_first ? q : p;
+            double xr = xm[mi].x - xo[ti].x, yr = xm[mi].y - xo[ti].y;
+            double r_tot = rm[mi] + ro[ti];
+            double b = -(xr * vrx + yr * vry);
+            double c = (xr * xr + yr * yr) - r_tot * r_tot;
+            double d = sqrt(b * b - a * c);
+            if (isnan(d) || d == 0) continue;
+            double tau_new = (b - d) / a;
+            if (isnan(tau) || (0 < tau_new && tau_new < tau)) { k_sel = k; tau = tau_new; b_min = b; d_min = d; }
+        }
+        if (!(isnan(tau) || tau <= 0)) {
+            int p = k_sel / 3, q = k_sel % 3, mi = me_first ? p : q, ti = me_first ? q : p;
+            double o[2][2];
+            int parts[2] = {mi, ti};
+            int64_t who[2] = {me, ot};
+            for (int u = 0; u < 2; ++u) {
+                double phi = ld(A, who[u], F_ORIENTATION), rts = ld(A, who[u], F_R_TS);
+                double ex = rts * m_sin(phi), ey = rts * (-m_cos(phi));
+                o[u][0] = parts[u] == 1 ? (0.0 + ex) : (parts[u] == 2 ? (0.0 - ex) : 0.0);
+                o[u][1] = parts[u] == 1 ? (0.0 + ey) : (parts[u] == 2 ? (0.0 - ey) : 0.0);
+            }
+            double ox = o[0][0] - o[1][0], oy = o[0][1] - o[1][1];
+            double xr = xm[0].x - xo[0].x, yr = xm[0].y - xo[0].y;
+            double gx = (vrx - (a * (xr + 2 * ox) + b_min * vrx) / d_min) / a;
+            double gy = (vry - (a * (yr + 2 * oy) + b_min * vry) / d_min) / a;
+            double cm = (-ld(A, me, F_MASS)) * ld(A, me, F_K_SOC);
+            double mag = magnitude(tau, ld(A, me, F_TAU_0));
+            v2 F = {(cm * gx) * mag, (cm * gy) * mag};
+            F = truncate(F, F_SOC_MAX);
+            Fx = F.x; Fy = F.y;
+        }
+    }
+    if (h_min < 0) {
+        v2 n = {nx, ny}, v = {vrx, vry};
+        v2 c = force_contact(h_min, n, v, rotate270(n), ld(A, me, F_MU), ld(A, me, F_KAPPA), ld(A, me, F_DAMPING));
+        Fx = Fx + c.x; Fy = Fy + c.y;
+    }
+    *fx += Fx; *fy += Fy;
+    *tq += rmx * Fy - rmy * Fx;
+}
+
+int orc_agent_agent_me_frame(char *base, int64_t n, int64_t itemsize, const int64_t *off,
+                             const grid_t *g) {
+    arr_t A = {base, itemsize, off};
+    int64_t ncells = g->nx * g->ny;
+    double *x = malloc(sizeof(double) * (n ? n : 1)), *y = malloc(sizeof(double) * (n ? n : 1));
+    int64_t *keys = malloc(sizeof(int64_t) * (n ? n : 1)), *pidx = malloc(sizeof(int64_t) * (n ? n : 1));
+    int64_t *cnt = malloc(sizeof(int64_t) * ncells), *cof = malloc(sizeof(int64_t) * ncells);
+    int64_t *rank = malloc(sizeof(int64_t) * (n ? n : 1));
+    double *acc = calloc((size_t)(n ? n : 1) * 3, sizeof(double));
+    positions_soa(&A, n, x, y);
+    int rc = orc_cell_list(x, y, n, g, keys, pidx, cnt, cof) ? -1 : 0;
+    if (!rc) {
+        for (int64_t c = 0; c < ncells; ++c)
+            for (int64_t s = 0; s < cnt[c]; ++s) rank[pidx[cof[c] + s]] = s;
+        for (int64_t a = 0; a < n; ++a) {
+            int64_t c = keys[a], ix = c / g->ny, iy = c % g->ny;
+            v2 f0 = ld2(&A, a, F_FORCE);
+            double fx = f0.x, fy = f0.y, m = ld(&A, a, F_TORQUE);
+            for (int dx = -1; dx <= 1; ++dx)
+                for (int dy = -1; dy <= 1; ++dy) {
+                    int64_t jx = ix + dx, jy = iy + dy;
+                    if (jx < 0 || jx >= g->nx || jy < 0 || jy >= g->ny) continue;
+                    int64_t c2 = jx * g->ny + jy;
+                    for (int64_t t = 0; t < cnt[c2]; ++t) {
+                        int64_t b = pidx[cof[c2] + t];
+                        if (b == a) continue;
+                        int first = (c2 == c) ? (rank[a] < t) : ((int64_t)dx * g->ny + dy > 0);
+                        tc_pair_me(&A, a, b, first, &fx, &fy, &m);
+                    }
+                }
+            acc[3 * a] = fx; acc[3 * a + 1] = fy; acc[3 * a + 2] = m;
+        }
+        for (int64_t a = 0; a < n; ++a) {
+            v2 f = {acc[3 * a], acc[3 * a + 1]};
+            st2(&A, a, F_FORCE, f);
+            st(&A, a, F_TORQUE, acc[3 * a + 2]);
+        }
+    }
+    free(x); free(y); free(keys); free(pidx); free(cnt); free(cof); free(rank); free(acc);
+    return rc;
+}

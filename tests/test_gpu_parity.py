@@ -74,9 +74,18 @@ def assert_identical(got, ref, what=''):
                     what, f, k, g[tuple(k)], r[tuple(k)], int((~same).sum())))
 
 
+def moving(scen, seed=3):
+    """Random velocities, so that every branch of the social force (defined
+    and undefined roots, both tau signs, the tau cut-off) is exercised."""
+    scen.agents['velocity'] = np.random.default_rng(seed).normal(0, 1.0, (len(scen.agents), 2))
+    return scen
+
+
 SCENARIOS = {
     'hallway': lambda: S.hallway(),
     'room': lambda: S.room(),
+    'room_moving': lambda: moving(S.room()),
+    'hallway_moving': lambda: moving(S.hallway()),
 }
 
 
