@@ -59,6 +59,7 @@ def parse():
     ap.add_argument('--impl', default='ours', choices=('ours', 'reference'))
     ap.add_argument('--agents', type=int, default=100_000)
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--no-batched', action='store_true')
     return ap.parse_args()
 
 
@@ -299,6 +300,8 @@ def run_ours(args, ws, rank, local):
                          'flops_per_launch': flops,
                          'peak_source': 'measured live: FP64 FMA chain kernel (2 flops per FMA)'},
             'clocks': clk.summary()}
+    if not args.no_batched:
+        line['batched'] = run_batched(args.steps, args.warmup, flush)
     if ws == 1 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
         steps = 2
@@ -312,6 +315,69 @@ def run_ours(args, ws, rank, local):
     b.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_batched(steps, warmup, flush=None):
+    """Batched form: the 512-scenario mix advanced as two contexts (one per
+    body type) launched concurrently, vs. the same scenarios advanced one
+    context at a time.  Returns a dict for the JSON line."""
+    import torch
+    from crowddynamics_gb300 import _native as N
+    from crowddynamics_gb300 import autotune
+    from crowddynamics_gb300 import scenarios as S
+    from crowddynamics_gb300.engine import batch_from_scenarios
+    nodes = N.NODE_ALL & ~N.NODE_FLUCTUATION
+    mix = S.batch_mix()
+    groups = [[s for s in mix if s.body == b] for b in ('circular', 'three_circle')]
+    batches = []
+    tuned = {}
+    for g in groups:
+        b, agents, _ = batch_from_scenarios(g)
+        v, times = autotune.tune(b, agents)
+        tuned[b.body] = {'variant': v, 'shape': N.variants()[v],
+                         'ms_per_variant': None if times is None else
+                         {str(k): round(t, 4) for k, t in times.items()}}
+        batches.append(b)
+    n_total = sum(b.n_agents for b in batches)
+    for b in batches:
+        b.run(max(warmup, 3), nodes)
+    el = 0.0
+    for k in range(steps):
+        if flush is not None:
+            flush.fill_(k & 0xff)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for b in batches:
+            b.launch(1, nodes)
+        for b in batches:
+            b.synchronize()
+        el += time.perf_counter() - t0
+    batched = n_total * steps / el
+    for b in batches:
+        b.close()
+    # the same scenarios one context at a time (each step a graph launch)
+    singles = []
+    for s in mix:
+        b, _, _ = batch_from_scenarios([s])
+        singles.append(b)
+    for b in singles:
+        b.run(2, nodes)
+    steps_single = max(2, steps // 4)
+    t0 = time.perf_counter()
+    for _ in range(steps_single):
+        for b in singles:
+            b.run(1, nodes)
+    el1 = time.perf_counter() - t0
+    one_by_one = n_total * steps_single / el1
+    for b in singles:
+        b.close()
+    return {'value': batched, 'unit': UNIT, 'scenario_by_scenario': one_by_one,
+            'speedup': batched / one_by_one, 'scenarios': len(mix), 'agents': n_total,
+            'walls': sum(len(s.walls) for s in mix), 'steps': steps,
+            'steps_scenario_by_scenario': steps_single,
+            'timing': 'host wall clock per step around both contexts\' graph launches and '
+                      'synchronisation, L2 flushed between steps',
+            'autotune': tuned}
 
 
 def main():

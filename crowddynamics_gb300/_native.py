@@ -36,7 +36,8 @@ SYMBOLS = (
     'cd_download_agents', 'cd_set_walls', 'cd_set_noise', 'cd_step', 'cd_run',
     'cd_synchronize', 'cd_get_time', 'cd_get_cell_list', 'cd_pair_counts',
     'cd_sizes', 'cd_set_timing', 'cd_kernel_time', 'cd_kernels_per_step',
-    'cd_measure_fp64_peak', 'cd_agent_agent_noalloc',
+    'cd_measure_fp64_peak', 'cd_agent_agent_noalloc', 'cd_variant_count',
+    'cd_variant_shape', 'cd_set_variant', 'cd_launch',
 )
 
 #: Limits and column order of cd_agent_agent_noalloc.
@@ -99,6 +100,11 @@ def load(path=None):
         'cd_kernel_time': (ctypes.c_int, [P, pd, pi64, pd, pd, pi64]),
         'cd_kernels_per_step': (ctypes.c_int, [P, ctypes.c_int, pi64]),
         'cd_measure_fp64_peak': (ctypes.c_int, [pd]),
+        'cd_variant_count': (ctypes.c_int, [ctypes.POINTER(ctypes.c_int)]),
+        'cd_variant_shape': (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                            ctypes.POINTER(ctypes.c_int)]),
+        'cd_set_variant': (ctypes.c_int, [P, ctypes.c_int]),
+        'cd_launch': (ctypes.c_int, [P, ctypes.c_int, i64]),
         'cd_agent_agent_noalloc': (ctypes.c_int, [ctypes.c_int, i64, P, P, P, P, ctypes.c_double,
                                                   ctypes.c_double, ctypes.c_double, i64, i64, P]),
     }
@@ -136,6 +142,19 @@ def i64ptr(a):
 
 def dptr(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def variants():
+    """[(threads_per_block, staged_per_thread)] of the force-kernel variants."""
+    L = load()
+    n = ctypes.c_int()
+    check(L.cd_variant_count(ctypes.byref(n)))
+    out = []
+    for v in range(n.value):
+        t, c = ctypes.c_int(), ctypes.c_int()
+        check(L.cd_variant_shape(v, ctypes.byref(t), ctypes.byref(c)))
+        out.append((t.value, c.value))
+    return out
 
 
 def measure_fp64_peak():

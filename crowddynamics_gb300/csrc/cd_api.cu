@@ -45,7 +45,7 @@ struct cd_ctx {
     bool noise_pending = false;
     unsigned long long *vmax = nullptr;
     double *v0max = nullptr, *dt = nullptr, *time_tot = nullptr;
-    int *err = nullptr;
+    int *err = nullptr, *work = nullptr;
     int *diag = nullptr;
 
     char *aos = nullptr;
@@ -59,6 +59,7 @@ struct cd_ctx {
 
     cudaGraphExec_t graph = nullptr;
     int graph_nodes = -1;
+    int variant = 0;
 
     bool timing = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs0 = nullptr, evs1 = nullptr;
@@ -114,6 +115,7 @@ StepArgs args_of(cd_ctx *c, int nodes) {
     a.dt = c->dt;
     a.time_tot = c->time_tot;
     a.err = c->err;
+    a.work = c->work;
     return a;
 }
 
@@ -132,7 +134,7 @@ void release(cd_ctx *c) {
                     c->perm_unsorted, c->perm, c->scan_scratch, c->stage, c->cull, c->stage_f,
                     c->walls_raw, c->walls, c->walls_f, c->wall_start, c->wall_idx,
                     c->noise_f, c->noise_m, c->vmax, c->v0max, c->dt, c->time_tot,
-                    c->err, c->diag, c->aos};
+                    c->err, c->work, c->diag, c->aos};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -233,7 +235,7 @@ void enqueue_step(cd_ctx *c, int nodes, bool timed, bool captured = false) {
     enqueue_cells(c, a);
     if (timed) cudaEventRecord(c->ev0, c->stream);
     if (captured) cudaEventRecordWithFlags(c->ev0, c->stream, cudaEventRecordExternal);
-    cdk::launch_forces(a, c->stream);
+    cdk::launch_forces(a, c->stream, c->variant);
     if (timed) cudaEventRecord(c->ev1, c->stream);
     if (captured) cudaEventRecordWithFlags(c->ev1, c->stream, cudaEventRecordExternal);
     if (timed) cudaEventRecord(c->evs1, c->stream);
@@ -398,6 +400,7 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->dt, n_scenarios));
     step(dalloc(c, &c->time_tot, n_scenarios));
     step(dalloc(c, &c->err, 1));
+    step(dalloc(c, &c->work, 1));
     step(dalloc(c, &c->diag, (int64_t)CD_COUNT_COLS * n));
     if (rc == CD_OK) {
         cudaMemcpy(c->scen_of, c->scen_of_host.data(), sizeof(int) * npad, cudaMemcpyHostToDevice);
@@ -562,11 +565,11 @@ int cd_step(cd_ctx *c, int nodes, double *dt) {
     return CD_OK;
 }
 
-int cd_run(cd_ctx *c, int nodes, int64_t steps) {
-    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+namespace {
+// Capture (or reuse) the graph of one step with `nodes`.
+int ensure_graph(cd_ctx *c, int nodes) {
     if (nodes & CD_NODE_FLUCTUATION)
-        return fail(c, CD_ERR_INVALID_VALUE, "cd_run cannot consume per-step host noise");
-    if (steps < 0) return fail(c, CD_ERR_INVALID_VALUE, "negative step count");
+        return fail(c, CD_ERR_INVALID_VALUE, "graph steps cannot consume per-step host noise");
     if (int rc = prepare_step(c, nodes)) return rc;
     if (!c->graph || c->graph_nodes != nodes) {
         if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
@@ -582,6 +585,23 @@ int cd_run(cd_ctx *c, int nodes, int64_t steps) {
         if (e != cudaSuccess) return fail(c, CD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
         c->graph_nodes = nodes;
     }
+    return CD_OK;
+}
+}  // namespace
+
+int cd_launch(cd_ctx *c, int nodes, int64_t steps) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (steps < 0) return fail(c, CD_ERR_INVALID_VALUE, "negative step count");
+    if (int rc = ensure_graph(c, nodes)) return rc;
+    for (int64_t k = 0; k < steps; ++k) CUDA_OR_FAIL(c, cudaGraphLaunch(c->graph, c->stream));
+    CUDA_OR_FAIL(c, cudaGetLastError());
+    return CD_OK;
+}
+
+int cd_run(cd_ctx *c, int nodes, int64_t steps) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (steps < 0) return fail(c, CD_ERR_INVALID_VALUE, "negative step count");
+    if (int rc = ensure_graph(c, nodes)) return rc;
     if (c->timing) cudaEventRecord(c->evr0, c->stream);
     for (int64_t k = 0; k < steps; ++k) CUDA_OR_FAIL(c, cudaGraphLaunch(c->graph, c->stream));
     CUDA_OR_FAIL(c, cudaGetLastError());
@@ -686,6 +706,35 @@ int cd_kernel_time(cd_ctx *c, double *force_ms, int64_t *force_launches, double 
     return CD_OK;
 }
 
+int cd_variant_count(int *count) {
+    if (!count) return fail(nullptr, CD_ERR_INVALID_VALUE, "count is NULL");
+    *count = cdk::N_VARIANTS;
+    return CD_OK;
+}
+
+int cd_variant_shape(int variant, int *threads, int *staged) {
+    static const int nt[cdk::N_VARIANTS] = {128, 64, 128, 64, 256};
+    static const int cap[cdk::N_VARIANTS] = {64, 64, 32, 32, 32};
+    if (variant < 0 || variant >= cdk::N_VARIANTS)
+        return fail(nullptr, CD_ERR_INVALID_VALUE, "unknown variant");
+    if (threads) *threads = nt[variant];
+    if (staged) *staged = cap[variant];
+    return CD_OK;
+}
+
+int cd_set_variant(cd_ctx *c, int variant) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (variant < 0 || variant >= cdk::N_VARIANTS)
+        return fail(c, CD_ERR_INVALID_VALUE, "unknown variant");
+    if (variant != c->variant && c->graph) {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+        c->graph_nodes = -1;
+    }
+    c->variant = variant;
+    return CD_OK;
+}
+
 int cd_kernels_per_step(const cd_ctx *c, int nodes, int64_t *kernels) {
     if (!c || !kernels) return fail(nullptr, CD_ERR_INVALID_VALUE, "NULL argument");
     *kernels = kernels_per_step(c, nodes);
@@ -728,7 +777,8 @@ constexpr size_t NA_OFF_CULL = NA_OFF_STAGE + na_align(sizeof(double2) * NA_N * 
 constexpr size_t NA_OFF_STAGEF = NA_OFF_CULL + na_align(sizeof(float4) * NA_N);
 constexpr size_t NA_OFF_VMAX = NA_OFF_STAGEF + na_align(sizeof(float4) * 2 * NA_N);
 constexpr size_t NA_OFF_ERR = NA_OFF_VMAX + na_align(sizeof(unsigned long long));
-constexpr size_t NA_BYTES = NA_OFF_ERR + na_align(sizeof(int));
+constexpr size_t NA_OFF_WORK = NA_OFF_ERR + na_align(sizeof(int));
+constexpr size_t NA_BYTES = NA_OFF_WORK + na_align(sizeof(int));
 static_assert(NA_BYTES < (4u << 20), "allocation-free scratch stays below 4 MiB");
 
 __device__ __align__(256) static unsigned char g_noalloc_scratch[NA_BYTES];
@@ -833,6 +883,7 @@ extern "C" int cd_agent_agent_noalloc(int body_type, int64_t n, const double *co
     a.stage_f = reinterpret_cast<float4 *>(base + NA_OFF_STAGEF);
     a.vmax = reinterpret_cast<unsigned long long *>(base + NA_OFF_VMAX);
     a.err = reinterpret_cast<int *>(base + NA_OFF_ERR);
+    a.work = reinterpret_cast<int *>(base + NA_OFF_WORK);
     int *scan = reinterpret_cast<int *>(base + NA_OFF_SCAN);
     // the array keeps the previous call's contents: zero what must start at 0
     CUDA_OR_FAIL(nullptr, cudaMemsetAsync(a.count, 0, sizeof(int) * ncells, st));
@@ -845,7 +896,7 @@ extern "C" int cd_agent_agent_noalloc(int body_type, int64_t n, const double *co
     cdk::launch_scan(a.count, a.start, ncells, scan, st);
     cdk::launch_scatter(a, st);
     cdk::launch_gather(a, st);
-    cdk::launch_forces(a, st);
+    cdk::launch_forces(a, st, 0);
     CUDA_OR_FAIL(nullptr, cudaGetLastError());
     int h = 0;
     CUDA_OR_FAIL(nullptr, cudaMemcpyAsync(&h, a.err, sizeof(int), cudaMemcpyDeviceToHost, st));

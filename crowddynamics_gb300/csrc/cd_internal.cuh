@@ -62,6 +62,7 @@ struct StepArgs {
     const double *v0max;         // per scenario max target_velocity
     double *dt, *time_tot;       // per scenario
     int *err;
+    int *work;                   // force-kernel work counter (zeroed per launch)
 };
 
 // Launchers (cd_kernels.cu)
@@ -71,7 +72,8 @@ int scan_scratch_ints(int n);
 void launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s);
 void launch_scatter(const StepArgs &a, cudaStream_t s);
 void launch_gather(const StepArgs &a, cudaStream_t s);
-void launch_forces(const StepArgs &a, cudaStream_t s);
+constexpr int N_VARIANTS = 5;       // launch variants of the force kernel
+void launch_forces(const StepArgs &a, cudaStream_t s, int variant);
 void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s);
 void launch_v0max(const StepArgs &a, double *v0max_out, cudaStream_t s);
 void launch_wall_prep(const double *raw, double *walls, float4 *walls_f, int nw,
@@ -82,7 +84,7 @@ void launch_soa_to_aos(char *aos, long long itemsize, const long long *off,
                        int n, int body, const double *const *col, cudaStream_t s);
 double fp64_peak_gflops();
 // Shared-memory bytes of the force kernel (dynamic) and one-time attributes.
-size_t forces_smem_bytes(int body);
+size_t forces_smem_bytes(int body, int variant);
 int init_kernels();
 
 }  // namespace cdk

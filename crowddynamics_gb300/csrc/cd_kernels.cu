@@ -24,6 +24,7 @@
 // exceeds the social cut-off plus both extents by a margin far above float32
 // rounding, i.e. pairs the reference evaluates to exactly no contribution.
 #include <cstdint>
+#include <algorithm>
 #include <cmath>
 #include "cd_internal.cuh"
 #include "cd_math.h"
@@ -37,8 +38,6 @@ constexpr double F_SOC_MAX = 2e3;      // core/motion/power_law.py:52
 constexpr double TAU_MAX = 30.0;       // core/motion/power_law.py:243
 constexpr double PI_D = 3.141592653589793;
 constexpr float CULL_MARGIN = 0.01f;   // metres, >> float32 error at 1e4 m
-constexpr int NT_FORCES = 128;
-constexpr int LIST_CAP = 64;           // survivors staged per thread per pass
 
 // ---- float64 helpers restating core/vector2D.py ------------------------
 
@@ -748,6 +747,7 @@ __device__ __forceinline__ void tc_pair_step(const TC &A, const float4 meC, cons
 // 3 x 3 cells in (dx, dy) lexicographic order, each cell ascending).
 struct EnumState { int ck, t; };
 
+template <int NT, int CAP>
 __device__ __forceinline__ int enumerate_candidates(const StepArgs &a, const ScenDev &sc, int s,
                                                     int my_cell, float4 me, int *mylist,
                                                     EnumState &st) {
@@ -767,20 +767,20 @@ __device__ __forceinline__ int enumerate_candidates(const StepArgs &a, const Sce
             int t = st.t;
             if (t == s) continue;
             if (pair_far(me, __ldg(&a.cull[t]))) continue;
-            if (nl == LIST_CAP) return nl;       // resume at this candidate
-            mylist[nl * NT_FORCES] = (same ? (s < t) : fwd) ? ~t : t;
+            if (nl == CAP) return nl;            // resume at this candidate
+            mylist[nl * NT] = (same ? (s < t) : fwd) ? ~t : t;
             ++nl;
         }
     }
     return nl;
 }
 
-template <int BODY>
-__global__ void __launch_bounds__(NT_FORCES) k_forces(StepArgs a) {
-    extern __shared__ unsigned char smem[];
-    int *list = reinterpret_cast<int *>(smem);
-    WarpQueue *wq = reinterpret_cast<WarpQueue *>(smem + sizeof(int) * LIST_CAP * NT_FORCES);
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+// All forces on the agent in cell-sorted slot s, then its integration.
+// Called by a whole warp (lanes with s >= n skip; warp collectives run over
+// the lanes that take part).
+template <int BODY, int NT, int CAP>
+__device__ __forceinline__ void force_agent(const StepArgs &a, const int s, int *list,
+                                            WarpQueue *wq) {
     const unsigned wmask = __ballot_sync(0xffffffffu, s < a.n);
     if (s >= a.n) return;
     const int lane = threadIdx.x & 31;
@@ -825,9 +825,9 @@ __global__ void __launch_bounds__(NT_FORCES) k_forces(StepArgs a) {
         if (BODY == 0) {
             const Circ A = load_circ(a.stage, s);
             while (true) {
-                int nl = enumerate_candidates(a, sc, s, my_cell, me, mylist, st);
+                int nl = enumerate_candidates<NT, CAP>(a, sc, s, my_cell, me, mylist, st);
                 for (int k = 0; k < nl; ++k) {
-                    int v = mylist[k * NT_FORCES];
+                    int v = mylist[k * NT];
                     const Circ B = load_circ(a.stage, v < 0 ? ~v : v);
                     pair_circular_me(A, B, fx, fy);
                 }
@@ -838,11 +838,11 @@ __global__ void __launch_bounds__(NT_FORCES) k_forces(StepArgs a) {
             const float4 meF0 = a.stage_f[2 * s], meF1 = a.stage_f[2 * s + 1];
             WarpQueue &q = wq[threadIdx.x >> 5];
             while (true) {
-                int nl = enumerate_candidates(a, sc, s, my_cell, me, mylist, st);
+                int nl = enumerate_candidates<NT, CAP>(a, sc, s, my_cell, me, mylist, st);
                 int kmax = __reduce_max_sync(wmask, (unsigned)nl);
                 for (int k = 0; k < kmax; ++k) {
                     bool act = k < nl;
-                    int v = act ? mylist[k * NT_FORCES] : 0;
+                    int v = act ? mylist[k * NT] : 0;
                     int t = v < 0 ? ~v : v;
                     tc_pair_step(A, me, meF0, meF1, a, act, t, v < 0, q, lane, wmask, nlanes,
                                  fx, fy, tq);
@@ -919,6 +919,26 @@ __global__ void __launch_bounds__(NT_FORCES) k_forces(StepArgs a) {
     } else {
         col[FX][i] = fx; col[FY][i] = fy;
         if (BODY == 1) col[TORQUE][i] = tq;
+    }
+}
+
+// Persistent grid (resident blocks only): each warp claims 32 consecutive
+// cell-sorted agents at a time from a counter, so uneven per-agent work
+// spreads over all SMs without a partial last wave.  NT threads per block,
+// CAP candidates staged per thread per pass (launch variants).
+template <int BODY, int NT, int CAP>
+__global__ void __launch_bounds__(NT) k_forces(StepArgs a) {
+    extern __shared__ unsigned char smem[];
+    int *list = reinterpret_cast<int *>(smem);
+    WarpQueue *wq = reinterpret_cast<WarpQueue *>(smem + sizeof(int) * CAP * NT);
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int chunk = 0;
+        if (lane == 0) chunk = atomicAdd(a.work, 1);
+        chunk = __shfl_sync(0xffffffffu, chunk, 0);
+        if (chunk * 32 >= a.n) return;
+        force_agent<BODY, NT, CAP>(a, chunk * 32 + lane, list, wq);
+        __syncwarp();
     }
 }
 
@@ -1110,26 +1130,61 @@ void launch_scatter(const StepArgs &a, cudaStream_t s) {
 void launch_gather(const StepArgs &a, cudaStream_t s) {
     if (a.n > 0) k_gather<<<nblk(a.n, 128), 128, 0, s>>>(a);
 }
-size_t forces_smem_bytes(int body) {
-    size_t b = sizeof(int) * LIST_CAP * NT_FORCES;
-    if (body == 1) b += sizeof(WarpQueue) * (NT_FORCES / 32);
+// Launch variants of the force kernel: (threads per block, staged candidates
+// per thread).
+struct Variant { int nt, cap; };
+constexpr Variant kVariants[N_VARIANTS] = {{128, 64}, {64, 64}, {128, 32}, {64, 32}, {256, 32}};
+
+size_t forces_smem_bytes(int body, int variant) {
+    const Variant v = kVariants[variant];
+    size_t b = sizeof(int) * (size_t)v.cap * v.nt;
+    if (body == 1) b += sizeof(WarpQueue) * (v.nt / 32);
     return b;
 }
+
+typedef void (*ForcesFn)(StepArgs);
+constexpr ForcesFn kForces[2][N_VARIANTS] = {
+    {k_forces<0, 128, 64>, k_forces<0, 64, 64>, k_forces<0, 128, 32>, k_forces<0, 64, 32>,
+     k_forces<0, 256, 32>},
+    {k_forces<1, 128, 64>, k_forces<1, 64, 64>, k_forces<1, 128, 32>, k_forces<1, 64, 32>,
+     k_forces<1, 256, 32>}};
+
+// Resident blocks of each force kernel variant on each device.
+int g_forces_blocks[64][2][N_VARIANTS];
+
 int init_kernels() {
-    cudaError_t e = cudaFuncSetAttribute(k_forces<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)forces_smem_bytes(1));
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_forces<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)forces_smem_bytes(0));
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    for (int body = 0; body < 2 && e == cudaSuccess; ++body)
+        for (int v = 0; v < N_VARIANTS && e == cudaSuccess; ++v) {
+            e = cudaFuncSetAttribute(kForces[body][v], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)forces_smem_bytes(body, v));
+            int nb = 0;
+            if (e == cudaSuccess)
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kForces[body][v],
+                                                                  kVariants[v].nt,
+                                                                  forces_smem_bytes(body, v));
+            if (e == cudaSuccess && dev >= 0 && dev < 64)
+                g_forces_blocks[dev][body][v] = (nb > 0 ? nb : 1) * sms;
+        }
     return e == cudaSuccess ? 0 : (int)e;
 }
-void launch_forces(const StepArgs &a, cudaStream_t s) {
+
+void launch_forces(const StepArgs &a, cudaStream_t s, int variant) {
     if (a.n <= 0) return;
-    if (a.body == 0)
-        k_forces<0><<<nblk(a.n, NT_FORCES), NT_FORCES, forces_smem_bytes(0), s>>>(a);
-    else
-        k_forces<1><<<nblk(a.n, NT_FORCES), NT_FORCES, forces_smem_bytes(1), s>>>(a);
+    if (variant < 0 || variant >= N_VARIANTS) variant = 0;
+    const Variant v = kVariants[variant];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int body = a.body ? 1 : 0;
+    int resident = (dev >= 0 && dev < 64) ? g_forces_blocks[dev][body][variant] : 0;
+    if (resident <= 0) resident = 152;
+    int blocks = std::min(nblk(a.n, v.nt), resident);
+    cudaMemsetAsync(a.work, 0, sizeof(int), s);
+    kForces[body][variant]<<<blocks, v.nt, forces_smem_bytes(body, variant), s>>>(a);
 }
+
 void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s) {
     if (a.n > 0) k_pair_counts<<<nblk(a.n, 128), 128, 0, s>>>(a, counts);
 }

@@ -143,6 +143,15 @@ class DeviceBatch:
         """``steps`` updates as CUDA-graph launches; waits and checks status."""
         self._chk(self._lib.cd_run(self._ctx, int(nodes), int(steps)))
 
+    def launch(self, steps, nodes=N.NODE_ALL & ~N.NODE_FLUCTUATION):
+        """Enqueue ``steps`` graph launches and return without waiting."""
+        self._chk(self._lib.cd_launch(self._ctx, int(nodes), int(steps)))
+
+    def set_variant(self, variant):
+        """Force-kernel launch variant (results identical; speed differs)."""
+        self._chk(self._lib.cd_set_variant(self._ctx, int(variant)))
+        self.variant = int(variant)
+
     def synchronize(self):
         self._chk(self._lib.cd_synchronize(self._ctx))
 

@@ -136,25 +136,29 @@ def place_lattice(rng, n, bounds, extent_max, walls, density, margin=0.01):
     """Seeded jittered square lattice: sites at spacing ~1/sqrt(density*1.06),
     each jittered by at most half of (spacing - 2*extent_max), sites closer
     than extent_max + margin to a wall dropped, then ``n`` sites chosen at
-    random.  Returns (n, 2)."""
+    random.  If walls leave too few sites the spacing shrinks by 5% steps.
+    Returns (n, 2)."""
     xmin, ymin, xmax, ymax = bounds
-    s = 1.0 / math.sqrt(density * 1.06)
-    xs = np.arange(xmin + s / 2, xmax - extent_max, s)
-    ys = np.arange(ymin + s / 2, ymax - extent_max, s)
-    gx, gy = np.meshgrid(xs, ys, indexing='ij')
-    sites = np.stack((gx.ravel(), gy.ravel()), -1)
-    jit = max(0.0, (s - 2 * extent_max - margin) / 2)
-    sites = sites + rng.uniform(-jit, jit, sites.shape)
-    keep = np.ones(len(sites), bool)
-    if len(walls):
-        for k0 in range(0, len(sites), 20000):
-            d = point_segment_distance(sites[k0:k0 + 20000, 0], sites[k0:k0 + 20000, 1], walls)
-            keep[k0:k0 + 20000] = d.min(axis=1) > extent_max + margin
-    sites = sites[keep]
-    if len(sites) < n:
-        raise RuntimeError('lattice has %d free sites, need %d' % (len(sites), n))
-    idx = rng.choice(len(sites), n, replace=False)
-    return sites[np.sort(idx)]
+    factor = 1.06
+    for _ in range(40):
+        s = 1.0 / math.sqrt(density * factor)
+        xs = np.arange(xmin + s / 2, xmax - extent_max, s)
+        ys = np.arange(ymin + s / 2, ymax - extent_max, s)
+        gx, gy = np.meshgrid(xs, ys, indexing='ij')
+        sites = np.stack((gx.ravel(), gy.ravel()), -1)
+        jit = max(0.0, (s - 2 * extent_max - margin) / 2)
+        sites = sites + rng.uniform(-jit, jit, sites.shape)
+        keep = np.ones(len(sites), bool)
+        if len(walls):
+            for k0 in range(0, len(sites), 20000):
+                d = point_segment_distance(sites[k0:k0 + 20000, 0], sites[k0:k0 + 20000, 1], walls)
+                keep[k0:k0 + 20000] = d.min(axis=1) > extent_max + margin
+        sites = sites[keep]
+        if len(sites) >= n:
+            idx = rng.choice(len(sites), n, replace=False)
+            return sites[np.sort(idx)]
+        factor *= 1.1025
+    raise RuntimeError('lattice has %d free sites, need %d' % (len(sites), n))
 
 
 def draw_noise(agents, rng):
@@ -382,3 +386,50 @@ def large_field(n=100_000, size=300.0, n_walls=600, seed=2, steps=200,
     shoulders(a)
     return Scenario('field_%d_n%d_w%d' % (size, n, n_walls), a, walls, bounds, cell_size,
                     steps=steps, seed=seed, extra={'direction_map': (fx, fy), 'map_step': step})
+
+
+def batch_mix(n_scenarios=512, seed=3, n_min=100, n_max=20000, steps=200):
+    """Independent scenarios of uneven size and type: agent count
+    log-uniform in [n_min, n_max], Circular or ThreeCircle at random, a
+    square room sized for a density uniform in [0.5, 2.5] agents/m^2, 0-200
+    random wall segments (fewer in small rooms), and per-scenario tau_0 ~
+    U(2, 4) s and k_soc ~ U(1, 2) written into every agent's fields.
+    Returns a list of Scenario."""
+    from crowddynamics_gb300.simulation.agents import agents_wrap_orientation
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_scenarios):
+        n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
+        body = 'circular' if rng.uniform() < 0.5 else 'three_circle'
+        density = rng.uniform(0.5, 2.5)
+        size = math.sqrt(n / density)
+        n_walls = int(rng.integers(0, 201))
+        n_walls = min(n_walls, int(size * size / 40))
+        bounds = (0.0, 0.0, size, size)
+        walls = random_walls(rng, n_walls, bounds, length=(1.0, min(15.0, size / 3)),
+                             min_gap=1.0) if n_walls else walls_array([])
+        a = new_agents(n, body)
+        if body == 'circular':
+            _circular_bodies(a, rng, n)
+            ext = float(np.max(a['radius']))
+        else:
+            _three_circle_bodies(a, rng, n)
+            ext = float(np.max(np.maximum(a['r_t'], a['r_ts'] + a['r_s'])))
+        # dense rooms leave less clearance than 2 * extent between lattice
+        # sites; placement then packs agents tighter than their extent
+        a['position'] = place_lattice(rng, n, bounds, min(ext, 0.5 / math.sqrt(density * 1.06)),
+                                      walls, density)
+        fx, fy, fstep = smooth_unit_field(rng, size, step=1.0, modes=3)
+        a['target_direction'] = lookup_direction(a['position'], (fx, fy), fstep)
+        a['velocity'] = a['target_direction'] * (0.5 * a['target_velocity'])[:, None]
+        a['tau_0'] = rng.uniform(2.0, 4.0)
+        a['k_soc'] = rng.uniform(1.0, 2.0)
+        if body == 'three_circle':
+            a['orientation'] = agents_wrap_orientation(rng.uniform(0.0, 2 * np.pi, n))
+            a['target_orientation'] = np.arctan2(a['target_direction'][:, 1],
+                                                 a['target_direction'][:, 0])
+            shoulders(a)
+        cell = SIGHT_SOC + 2 * max(0.35, ext)
+        out.append(Scenario('mix%03d_%s_n%d' % (k, body, n), a, walls, bounds, cell, steps=steps,
+                            seed=seed, extra={'density': density}))
+    return out

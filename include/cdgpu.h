@@ -168,6 +168,20 @@ int cd_kernel_time(cd_ctx *ctx, double *force_ms, int64_t *force_launches,
 /* Number of kernels one step with `nodes` launches (memsets excluded). */
 int cd_kernels_per_step(const cd_ctx *ctx, int nodes, int64_t *kernels);
 
+/* Launch variants of the agent-force kernel: threads per block and
+ * candidates staged per thread per pass.  Every variant gives bit-identical
+ * results; only the speed differs, so an autotuner may pick one per context
+ * (the choice is applied to the next captured graph). */
+int cd_variant_count(int *count);
+int cd_variant_shape(int variant, int *threads_per_block, int *staged_per_thread);
+int cd_set_variant(cd_ctx *ctx, int variant);
+
+/* Enqueue `steps` CUDA-graph launches of a step with `nodes` on the context
+ * stream and return at once (no host synchronisation), so several contexts
+ * (for example one per body type of a mixed batch) run concurrently.  Device
+ * errors surface at the next cd_synchronize / cd_run. */
+int cd_launch(cd_ctx *ctx, int nodes, int64_t steps);
+
 /* Measured FP64 FMA throughput of the current device in GFLOP/s (2 flops
  * per FMA), used as the roofline denominator. */
 int cd_measure_fp64_peak(double *gflops);
