@@ -60,6 +60,7 @@ def parse():
     ap.add_argument('--agents', type=int, default=100_000)
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-batched', action='store_true')
+    ap.add_argument('--no-adjoint', action='store_true')
     return ap.parse_args()
 
 
@@ -302,6 +303,8 @@ def run_ours(args, ws, rank, local):
             'clocks': clk.summary()}
     if not args.no_batched:
         line['batched'] = run_batched(args.steps, args.warmup, flush)
+    if not args.no_adjoint:
+        line['adjoint'] = run_adjoint()
     if ws == 1 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
         steps = 2
@@ -378,6 +381,64 @@ def run_batched(steps, warmup, flush=None):
             'timing': 'host wall clock per step around both contexts\' graph launches and '
                       'synchronisation, L2 flushed between steps',
             'autotune': tuned}
+
+
+def run_adjoint(n=5000, width=80.0, height=20.0, steps=400, ckpt=20, seed=4):
+    """Differentiable form: Circular hallway 80 m x 20 m, 5000 agents,
+    400-step rollout, loss = mean squared position error against a rollout
+    with hidden tau_adj ~ U(0.3, 0.7) and target speed ~ N(1.2, 0.2); the
+    gradient of the loss with respect to per-agent tau_adj, target speed,
+    tau_0 and k_soc through the hand-written adjoint, checkpoint every 20
+    steps.  Times (CUDA events inside the call) the forward rollout alone and
+    the forward + adjoint, and compares one directional derivative with
+    central differences of the device loss at h = 1e-6, 1e-7, 1e-8."""
+    import numpy as np
+    from crowddynamics_gb300 import scenarios as S
+    from crowddynamics_gb300.adjoint import PARAMS, make_target
+    from crowddynamics_gb300.engine import batch_from_scenarios
+    scen = S.hallway(n=n, width=width, height=height, seed=seed)
+    rng = np.random.default_rng(seed)
+    hidden = {'tau_adj': rng.uniform(0.3, 0.7, n), 'target_velocity': rng.normal(1.2, 0.2, n)}
+    target = make_target(scen, hidden, steps)
+    a = scen.agents.copy()
+    b, _, _ = batch_from_scenarios([scen])
+
+    def rollout(agents, grads):
+        b.upload(agents)
+        return b.rollout_loss(steps, target, ckpt, grads=grads)
+
+    rollout(a, True)                                    # warm-up (graph capture, allocation)
+    fwd_only = []
+    full = []
+    for _ in range(3):
+        fwd_only.append(rollout(a, False)[2])
+        loss, g, fms, ams = rollout(a, True)
+        full.append((fms, ams))
+    f_only = float(np.median(fwd_only))
+    f_ms = float(np.median([x[0] for x in full]))
+    a_ms = float(np.median([x[1] for x in full]))
+    base = np.stack([np.ascontiguousarray(a[k]) for k in PARAMS], 1)
+    u = rng.normal(size=base.shape) * np.abs(base)
+    fds = {}
+    for h in (1e-6, 1e-7, 1e-8):
+        lo, hi = a.copy(), a.copy()
+        for col, name in enumerate(PARAMS):
+            hi[name] = a[name] + h * u[:, col]
+            lo[name] = a[name] - h * u[:, col]
+        fds[h] = (rollout(hi, False)[0] - rollout(lo, False)[0]) / (2 * h)
+    ad = float((g * u).sum())
+    b.close()
+    return {'workload': 'hallway_80x20_circular_5000_rollout400_ckpt20', 'loss': loss,
+            'forward_only_ms': f_only, 'forward_ms': f_ms, 'adjoint_ms': a_ms,
+            'gradient_over_forward': (f_ms + a_ms) / f_only,
+            'agent_steps_per_s_forward': n * steps / (f_only / 1e3),
+            'directional_derivative': {
+                'adjoint': ad,
+                'central_difference': {str(h): v for h, v in fds.items()},
+                'rel_diff': {str(h): abs(ad - v) / max(abs(v), 1e-300) for h, v in fds.items()},
+                'direction': 'random, each component scaled by its parameter'},
+            'timing': 'CUDA events around the rollout and the adjoint inside cd_rollout_loss, '
+                      'median of 3 calls after one warm-up call'}
 
 
 def main():

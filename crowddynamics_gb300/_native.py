@@ -37,7 +37,7 @@ SYMBOLS = (
     'cd_synchronize', 'cd_get_time', 'cd_get_cell_list', 'cd_pair_counts',
     'cd_sizes', 'cd_set_timing', 'cd_kernel_time', 'cd_kernels_per_step',
     'cd_measure_fp64_peak', 'cd_agent_agent_noalloc', 'cd_variant_count',
-    'cd_variant_shape', 'cd_set_variant', 'cd_launch',
+    'cd_variant_shape', 'cd_set_variant', 'cd_launch', 'cd_rollout_loss',
 )
 
 #: Limits and column order of cd_agent_agent_noalloc.
@@ -105,6 +105,7 @@ def load(path=None):
                                             ctypes.POINTER(ctypes.c_int)]),
         'cd_set_variant': (ctypes.c_int, [P, ctypes.c_int]),
         'cd_launch': (ctypes.c_int, [P, ctypes.c_int, i64]),
+        'cd_rollout_loss': (ctypes.c_int, [P, i64, P, i64, pd, pd, pd, pd]),
         'cd_agent_agent_noalloc': (ctypes.c_int, [ctypes.c_int, i64, P, P, P, P, ctypes.c_double,
                                                   ctypes.c_double, ctypes.c_double, i64, i64, P]),
     }

@@ -751,6 +751,170 @@ int cd_measure_fp64_peak(double *gflops) {
 
 }  // extern "C"
 
+
+// ---- differentiable rollout ------------------------------------------------
+
+namespace {
+
+// State snapshot: columns x, y, vx, vy, fpx, fpy of n agents.
+// State a step reads: positions, velocities, previous and current force (the
+// current force is zero after a reset, the array's own value before step 0).
+constexpr int SNAP_COLS = 8;
+constexpr int kSnapCol[SNAP_COLS] = {cdk::X,   cdk::Y,   cdk::VX, cdk::VY,
+                                     cdk::FPX, cdk::FPY, cdk::FX, cdk::FY};
+
+int copy_state(cd_ctx *c, double *snap, bool save) {
+    for (int k = 0; k < SNAP_COLS; ++k) {
+        double *col = c->col[kSnapCol[k]], *buf = snap + (size_t)k * c->n;
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(save ? buf : col, save ? col : buf, sizeof(double) * c->n,
+                                        cudaMemcpyDeviceToDevice, c->stream));
+    }
+    return CD_OK;
+}
+
+struct DevBuf {
+    std::vector<void *> ptrs;
+    ~DevBuf() { for (void *p : ptrs) cudaFree(p); }
+    template <typename T> T *get(cd_ctx *c, int64_t count, int &rc) {
+        void *p = nullptr;
+        if (rc == CD_OK) rc = dalloc(c, reinterpret_cast<T **>(&p), count);
+        if (p) ptrs.push_back(p);
+        return static_cast<T *>(p);
+    }
+};
+
+}  // namespace
+
+extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, int64_t ckpt,
+                               double *loss, double *grads, double *forward_ms, double *adjoint_ms) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (c->body != CD_BODY_CIRCULAR)
+        return fail(c, CD_ERR_INVALID_TYPE, "the adjoint covers Circular agents only");
+    if (c->nscen != 1) return fail(c, CD_ERR_INVALID_VALUE, "the adjoint covers one scenario");
+    if (steps < 1 || ckpt < 1 || !target || !loss)
+        return fail(c, CD_ERR_INVALID_VALUE, "bad rollout arguments");
+    const int nodes = CD_NODE_ADJUSTING | CD_NODE_AGENT_AGENT | CD_NODE_AGENT_OBSTACLE |
+                      CD_NODE_INTEGRATE | CD_NODE_RESET;
+    const int64_t n = c->n;
+    if (forward_ms) *forward_ms = 0.0;
+    if (adjoint_ms) *adjoint_ms = 0.0;
+    if (n == 0) {                                  // nothing to differentiate: plain steps
+        *loss = 0.0;
+        return cd_run(c, nodes, steps);
+    }
+    ckpt = std::min(ckpt, steps);
+    if (int rc = ensure_graph(c, nodes)) return rc;
+    const int64_t nseg = (steps + ckpt - 1) / ckpt;
+    const size_t snap = (size_t)SNAP_COLS * (size_t)std::max<int64_t>(n, 1);
+    int rc = CD_OK;
+    DevBuf mem;
+    double *tgt = mem.get<double>(c, steps * 2 * n, rc);
+    double *ck = mem.get<double>(c, nseg * snap, rc);
+    double *seg = grads ? mem.get<double>(c, (ckpt + 1) * snap, rc) : nullptr;
+    double *fin = mem.get<double>(c, snap, rc);
+    double *dts = mem.get<double>(c, steps, rc);
+    double *partial = mem.get<double>(c, cdk::adj_partials((int)n), rc);
+    double *scal = mem.get<double>(c, 4, rc);           // loss, ldt, saved dt, saved time
+    double *adj = grads ? mem.get<double>(c, 16 * n + 4 * n, rc) : nullptr;
+    int *amax = grads ? mem.get<int>(c, 2, rc) : nullptr;
+    double *avals = grads ? mem.get<double>(c, 2, rc) : nullptr;
+    if (rc) return rc;
+    cudaStream_t st = c->stream;
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(tgt, target, sizeof(double) * steps * 2 * n,
+                                    cudaMemcpyHostToDevice, st));
+    CUDA_OR_FAIL(c, cudaMemsetAsync(scal, 0, sizeof(double) * 4, st));
+    const double scale = 1.0 / ((double)steps * (double)std::max<int64_t>(n, 1));
+    cudaEvent_t e0, e1, e2;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventCreate(&e2);
+    cudaEventRecord(e0, st);
+    // forward rollout with checkpoints and the loss
+    for (int64_t t = 0; t < steps; ++t) {
+        if (t % ckpt == 0)
+            if ((rc = copy_state(c, ck + (size_t)(t / ckpt) * snap, true))) break;
+        CUDA_OR_FAIL(c, cudaGraphLaunch(c->graph, st));
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(dts + t, c->dt, sizeof(double), cudaMemcpyDeviceToDevice, st));
+        cdk::launch_loss(c->col[cdk::X], c->col[cdk::Y], tgt + (size_t)t * 2 * n, (int)n, partial,
+                         scal, scale, st);
+    }
+    if (rc) return rc;
+    if ((rc = copy_state(c, fin, true))) return rc;
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(scal + 2, c->dt, sizeof(double), cudaMemcpyDeviceToDevice, st));
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(scal + 3, c->time_tot, sizeof(double), cudaMemcpyDeviceToDevice, st));
+    cudaEventRecord(e1, st);
+    if (grads) {
+        double *lx = adj, *lv = adj + 2 * n, *lfp = adj + 4 * n, *lF = adj + 6 * n;
+        double *lvt = adj + 8 * n, *lfp2 = adj + 10 * n, *lx2 = adj + 12 * n, *lv2 = adj + 14 * n;
+        double *g = adj + 16 * n;
+        CUDA_OR_FAIL(c, cudaMemsetAsync(adj, 0, sizeof(double) * (16 * n + 4 * n), st));
+        const int fnodes = CD_NODE_ADJUSTING | CD_NODE_AGENT_AGENT | CD_NODE_AGENT_OBSTACLE;
+        const cd_scenario &sc = c->scen_host[0];
+        for (int64_t sgi = nseg - 1; sgi >= 0 && rc == CD_OK; --sgi) {
+            const int64_t t0 = sgi * ckpt, t1 = std::min<int64_t>(t0 + ckpt, steps);
+            if ((rc = copy_state(c, ck + (size_t)sgi * snap, false))) break;
+            for (int64_t t = t0; t < t1; ++t) {            // recompute the segment
+                if ((rc = copy_state(c, seg + (size_t)(t - t0) * snap, true))) break;
+                CUDA_OR_FAIL(c, cudaGraphLaunch(c->graph, st));
+            }
+            if (rc || (rc = copy_state(c, seg + (size_t)(t1 - t0) * snap, true))) break;
+            for (int64_t t = t1 - 1; t >= t0; --t) {
+                const double *after = seg + (size_t)(t + 1 - t0) * snap;
+                cdk::launch_loss_grad(after, after + n, tgt + (size_t)t * 2 * n, (int)n, scale, lx, st);
+                if ((rc = copy_state(c, seg + (size_t)(t - t0) * snap, false))) break;
+                StepArgs a = args_of(c, fnodes);
+                enqueue_cells(c, a);
+                cdk::launch_forces(a, st, c->variant);    // total force of step t
+                cdk::AdjArgs q;
+                q.n = (int)n;
+                q.dt = dts + t;
+                q.mass = c->col[cdk::MASS];
+                q.fx = c->col[cdk::FX];
+                q.fy = c->col[cdk::FY];
+                q.vnx = after + 2 * n;
+                q.vny = after + 3 * n;
+                q.fpx = c->col[cdk::FPX];
+                q.fpy = c->col[cdk::FPY];
+                q.lx = lx; q.lv = lv; q.lfp = lfp;
+                q.lF = lF; q.lvt = lvt; q.lfp_out = lfp2;
+                q.lx_out = lx2; q.lv_out = lv2;
+                q.partial = partial;
+                q.ldt = scal + 1;
+                q.grad = g;
+                q.argmax_vals = avals;
+                q.argmax_idx = amax;
+                cdk::launch_adj_seed(q, st);
+                cdk::launch_adj_forces(a, q, st);
+                cdk::launch_adj_dt(q, sc.dt_min, sc.dt_max, c->col[cdk::VX], c->col[cdk::VY],
+                                   c->col[cdk::V0], st);
+                std::swap(lx, lx2);
+                std::swap(lv, lv2);
+                std::swap(lfp, lfp2);
+            }
+        }
+        if (rc) return rc;
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(grads, g, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st));
+    }
+    cudaEventRecord(e2, st);
+    // leave the context in the rollout's final state
+    if ((rc = copy_state(c, fin, false))) return rc;
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(c->dt, scal + 2, sizeof(double), cudaMemcpyDeviceToDevice, st));
+    // recomputed steps advanced time_tot a second time: restore the forward's value
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(c->time_tot, scal + 3, sizeof(double), cudaMemcpyDeviceToDevice, st));
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(loss, scal, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_OR_FAIL(c, cudaGetLastError());
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(st));
+    float f_ms = 0, a_ms = 0;
+    cudaEventElapsedTime(&f_ms, e0, e1);
+    cudaEventElapsedTime(&a_ms, e1, e2);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    if (forward_ms) *forward_ms = f_ms;
+    if (adjoint_ms) *adjoint_ms = a_ms;
+    return check_device_error(c);
+}
+
 // ---- agent-agent forces without device allocation -------------------------
 //
 // The cell list and staging buffers of one agent-agent pass live in the

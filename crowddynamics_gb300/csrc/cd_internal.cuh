@@ -65,6 +65,33 @@ struct StepArgs {
     int *work;                   // force-kernel work counter (zeroed per launch)
 };
 
+// Reverse-step arguments (cd_adjoint.cu); n x 2 arrays are interleaved,
+// state snapshots are columns.
+struct AdjArgs {
+    int n;
+    const double *dt;                      // this step's timestep (device scalar)
+    const double *mass, *fx, *fy;          // mass, recomputed total force
+    const double *vnx, *vny;               // velocity after the step
+    const double *fpx, *fpy;               // force_prev before the step
+    const double *lx, *lv, *lfp;           // incoming adjoints of x', v', fp'
+    double *lF, *lvt, *lfp_out;            // adjoint of F, of v' incl. x', of fp
+    double *lx_out, *lv_out;               // outgoing adjoints of x, v
+    double *partial, *ldt;                 // dt adjoint (block partials, total)
+    double *grad;                          // n x 4: tau_adj, v0, tau_0, k_soc
+    double *argmax_vals;                   // max |v|, max v0
+    int *argmax_idx;
+};
+
+int adj_partials(int n);
+void launch_adj_seed(const AdjArgs &q, cudaStream_t s);
+void launch_adj_forces(const StepArgs &a, const AdjArgs &q, cudaStream_t s);
+void launch_adj_dt(const AdjArgs &q, double dt_min, double dt_max, const double *vx,
+                   const double *vy, const double *v0, cudaStream_t s);
+void launch_loss(const double *x, const double *y, const double *target, int n,
+                 double *partial, double *loss, double scale, cudaStream_t s);
+void launch_loss_grad(const double *x, const double *y, const double *target, int n,
+                      double scale, double *lx, cudaStream_t s);
+
 // Launchers (cd_kernels.cu)
 void launch_prepare(const StepArgs &a, cudaStream_t s);
 void launch_dt(const StepArgs &a, cudaStream_t s);

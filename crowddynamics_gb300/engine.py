@@ -152,6 +152,23 @@ class DeviceBatch:
         self._chk(self._lib.cd_set_variant(self._ctx, int(variant)))
         self.variant = int(variant)
 
+    def rollout_loss(self, steps, target, checkpoint_every=20, grads=True):
+        """Run ``steps`` updates, return (loss, grads, forward_ms, adjoint_ms):
+        loss = mean over steps and agents of |x(t) - target[t]|^2, grads =
+        d loss / d (tau_adj, target_velocity, tau_0, k_soc) per agent (n x 4,
+        None unless ``grads``).  Circular agents, one scenario."""
+        tgt = np.ascontiguousarray(target, dtype=np.float64)
+        if tgt.shape != (int(steps), self.n_agents, 2):
+            raise InvalidValue('target must have shape (steps, n, 2)')
+        loss = ctypes.c_double()
+        fms, ams = ctypes.c_double(), ctypes.c_double()
+        g = np.zeros((self.n_agents, 4)) if grads else None
+        self._chk(self._lib.cd_rollout_loss(self._ctx, int(steps), N.ptr(tgt),
+                                            int(checkpoint_every), ctypes.byref(loss),
+                                            None if g is None else N.dptr(g),
+                                            ctypes.byref(fms), ctypes.byref(ams)))
+        return loss.value, g, fms.value, ams.value
+
     def synchronize(self):
         self._chk(self._lib.cd_synchronize(self._ctx))
 

@@ -186,6 +186,24 @@ int cd_launch(cd_ctx *ctx, int nodes, int64_t steps);
  * per FMA), used as the roofline denominator. */
 int cd_measure_fp64_peak(double *gflops);
 
+/* ---- differentiable rollout (Circular agents, one scenario) -------------
+ * Runs `steps` updates (adjusting, agent-agent, agent-wall, integrate,
+ * reset) from the current state and writes
+ *   loss = (1 / (steps * n)) * sum_t sum_i |x_i(t) - target[t][i]|^2
+ * where x(t) is the position after step t and `target` holds steps x n x 2
+ * float64 (host).  With `grads` non-NULL it also runs the hand-written
+ * adjoint of the whole rollout -- a checkpoint of (x, v, force_prev) every
+ * `checkpoint_every` steps, recomputation of each segment, and the reverse
+ * step -- and writes d loss / d (tau_adj, target_velocity, tau_0, k_soc) for
+ * every agent (n x 4).  The context ends in the rollout's final state.
+ * Replaces nothing in the reference (which has no gradients); the forward
+ * part is the same step as cd_step.  `forward_ms` / `adjoint_ms` (may be
+ * NULL) receive the device time of the forward rollout and of the reverse
+ * sweep (recomputation included). */
+int cd_rollout_loss(cd_ctx *ctx, int64_t steps, const double *target,
+                    int64_t checkpoint_every, double *loss, double *grads,
+                    double *forward_ms, double *adjoint_ms);
+
 /* ---- agent-agent forces without any device allocation ------------------
  * No counterpart in the reference: an extra entry point for callers that
  * cannot allocate device memory while they run -- for example a host
