@@ -58,98 +58,149 @@ __device__ __forceinline__ bool pair_far(float4 me, float4 o) {
     return dx * dx + dy * dy > lim * lim;
 }
 
-// Reverse of the contact force -h (mu n - kappa (v.t) t) + c (v.n) n with
-// h = |x| - r, n = x / |x|, t = rotate270(n), seed u; adds d(u.F)/dx, /dv.
+// Reverse of a sum of contact forces sharing one geometry,
+//   Phi = sum_s sigma_s u_s . [-h (mu_s n - kappa_s (v.t) t) + c_s (v.n) n],
+// given the combined seeds U_mu = sum sigma mu u, U_ka = sum sigma kappa u,
+// U_d = sum sigma c u (h = |x| - r, n = x / |x|, t = rotate270(n) = R n);
+// adds dPhi/dx and dPhi/dv.
+__device__ __forceinline__ void contact_vjp3(double xx, double xy, double d0, double h,
+                                             double vx, double vy, double umx, double umy,
+                                             double ukx, double uky, double udx, double udy,
+                                             double &gxx, double &gxy, double &gvx,
+                                             double &gvy) {
+    const double id0 = 1.0 / d0;
+    const double nx = xx * id0, ny = xy * id0;
+    const double tx = ny, ty = -nx;
+    const double vt = vx * tx + vy * ty, vn = vx * nx + vy * ny;
+    const double umn = umx * nx + umy * ny;
+    const double ukt = ukx * tx + uky * ty;
+    const double udn = udx * nx + udy * ny;
+    gvx += h * ukt * tx + udn * nx;
+    gvy += h * ukt * ty + udn * ny;
+    const double A = -umn + vt * ukt;                        // coefficient of dh = n . dx
+    const double w1x = -h * umx + udn * vx + vn * udx;       // through dn = P dx / |x|
+    const double w1y = -h * umy + udn * vy + vn * udy;
+    const double w2x = h * (ukt * vx + vt * ukx);            // through dt = R P dx / |x|
+    const double w2y = h * (ukt * vy + vt * uky);
+    const double qx = w1x - w2y, qy = w1y + w2x;             // w1 + R^T w2
+    const double pq = nx * qx + ny * qy;                     // P q = q - n (n . q)
+    gxx += A * nx + (qx - nx * pq) * id0;
+    gxy += A * ny + (qy - ny * pq) * id0;
+}
+
+// Single contact force with seed u.
 __device__ __forceinline__ void contact_vjp(double xx, double xy, double d0, double h, double vx,
                                             double vy, double mu, double kappa, double damp,
                                             double ux, double uy, double &gxx, double &gxy,
                                             double &gvx, double &gvy) {
-    double nx = xx / d0, ny = xy / d0;
-    double tx = ny, ty = -nx;
-    double vt = vx * tx + vy * ty, vn = vx * nx + vy * ny;
-    double ut = ux * tx + uy * ty, un = ux * nx + uy * ny;
-    gvx += h * kappa * ut * tx + damp * un * nx;
-    gvy += h * kappa * ut * ty + damp * un * ny;
-    double A = -mu * un + kappa * vt * ut;                   // coefficient of dh = n . dx
-    double w1x = -h * mu * ux + damp * (un * vx + vn * ux);  // through dn = P dx / |x|
-    double w1y = -h * mu * uy + damp * (un * vy + vn * uy);
-    double w2x = h * kappa * (ut * vx + vt * ux);            // through dt = R P dx / |x|
-    double w2y = h * kappa * (ut * vy + vt * uy);
-    double qx = w1x + (-w2y), qy = w1y + w2x;                // w1 + R^T w2
-    double pq = nx * qx + ny * qy;                           // P q = q - n (n . q)
-    gxx += A * nx + (qx - nx * pq) / d0;
-    gxy += A * ny + (qy - ny * pq) / d0;
+    contact_vjp3(xx, xy, d0, h, vx, vy, mu * ux, mu * uy, kappa * ux, kappa * uy, damp * ux,
+                 damp * uy, gxx, gxy, gvx, gvy);
 }
 
-// Reverse of one side's Circular pair force (interactions.py:51-70 with
-// power_law.py:213-259), evaluated in that side's frame (x = x_me - x_other,
-// v = v_me - v_other), seed u = adjoint of the side's total force.
-__device__ void pair_circ_vjp(double xx, double xy, double vx, double vy, double r_tot, double m,
-                              double k, double tau0, double mu, double kappa, double damp,
-                              double ux, double uy, double &gxx, double &gxy, double &gvx,
-                              double &gvy, double &gk, double &gtau0) {
-    double d0 = cdm_hypot(xx, xy);
-    double h = d0 - r_tot;
+// Seed of the untruncated force from the seed u of truncate(F, 2000 N)
+// (vector2D.py:166-187): u itself, or (s)(I - f f^T) u above the limit.
+__device__ __forceinline__ void truncate_vjp(double Fx, double Fy, double &ux, double &uy) {
+    const double L = cdm_hypot(Fx, Fy);
+    if (L > F_SOC_MAX) {
+        const double iL = 1.0 / L;
+        const double fx = Fx * iL, fy = Fy * iL, s = F_SOC_MAX * iL;
+        const double dot = ux * fx + uy * fy;
+        ux = s * (ux - dot * fx);
+        uy = s * (uy - dot * fy);
+    }
+}
+
+struct PairGrad {
+    double gxx, gxy, gvx, gvy;                 // d/d(x_i - x_j), d/d(v_i - v_j)
+    double gk, gt0;                            // d/dk_soc_i, d/dtau_0_i
+};
+
+// Social side s of a pair (power_law.py:215-259): F_s = trunc(c_s mg(tau, tau0_s)
+// sigma g), c_s = -m_s k_s, sigma = +1 for agent i and -1 for agent j (tau's
+// gradient in j's frame is -g).  Adds the side's seed of g to (lgx, lgy) and
+// of tau to ltau; returns (l_raw . g) sigma for the k_soc / tau_0 terms.
+__device__ __forceinline__ void social_side(double tau, double it, double it2, double gx,
+                                            double gy, double sigma, double m, double k,
+                                            double tau0, double ux, double uy, double &lgx,
+                                            double &lgy, double &ltau, double *gk,
+                                            double *gt0) {
+    const double i0 = 1.0 / tau0;
+    const double e = cdm_exp(-tau * i0);
+    const double mg = (2.0 * it + i0) * e * it2;
+    const double cm = (-m) * k;
+    const double cms = cm * mg * sigma;
+    double lx = ux, ly = uy;
+    truncate_vjp(cms * gx, cms * gy, lx, ly);
+    lgx += cms * lx;
+    lgy += cms * ly;
+    const double lgd = sigma * (lx * gx + ly * gy);
+    const double lmg = cm * lgd;
+    ltau -= lmg * e * it2 * (6.0 * it2 + 4.0 * it * i0 + i0 * i0);
+    if (gk) {
+        *gk += (-m) * mg * lgd;
+        *gt0 += lmg * e * i0 * i0 * (it2 + it * i0);
+    }
+}
+
+// Reverse of one pair's two forces (interactions.py:51-70): the seed is
+//   Phi = u_i . F_i(x, v) + u_j . F_j(-x, -v)
+// with x = x_i - x_j, v = v_i - v_j; both forces share h, tau and tau's
+// gradient g, so one pass back through the geometry serves both sides.
+// Adds dPhi/dx, dPhi/dv and agent i's k_soc, tau_0 terms.
+__device__ __forceinline__ void pair_vjp_both(const Circ &A, const Circ &B, double uix,
+                                              double uiy, double ujx, double ujy, PairGrad &G) {
+    const double xx = A.x - B.x, xy = A.y - B.y;
+    const double d0 = cdm_hypot(xx, xy);
+    const double r_tot = A.r + B.r;
+    const double h = d0 - r_tot;
     if (!(h < SIGTH_SOC)) return;
-    double a = vx * vx + vy * vy;
-    double b = -(xx * vx + xy * vy);
-    double c = (xx * xx + xy * xy) - r_tot * r_tot;
-    double disc = b * b - a * c;
+    const double vx = A.vx - B.vx, vy = A.vy - B.vy;
+    const double a = vx * vx + vy * vy;
+    const double b = -(xx * vx + xy * vy);
+    const double c = (xx * xx + xy * xy) - r_tot * r_tot;
+    const double disc = b * b - a * c;
     if (disc > 0 && a != 0) {
-        double dd = sqrt(disc);
-        double tau = (b - dd) / a;
+        const double dd = sqrt(disc);
+        const double tau = (b - dd) / a;
         if (!(tau <= 0 || tau > TAU_MAX)) {
-            double gx = (vx - (vx * b + xx * a) / dd) / a;   // grad of tau
-            double gy = (vy - (vy * b + xy * a) / dd) / a;
-            double cm = (-m) * k;
-            double e = cdm_exp(-tau / tau0);
-            double mg = (2.0 / tau + 1.0 / tau0) * e / (tau * tau);
-            double Fx = (cm * gx) * mg, Fy = (cm * gy) * mg;
-            double L = cdm_hypot(Fx, Fy);
-            double lx = ux, ly = uy;
-            if (L > F_SOC_MAX) {                             // truncate (vector2D.py:166-187)
-                double fx = Fx / L, fy = Fy / L, s = F_SOC_MAX / L;
-                double dot = ux * fx + uy * fy;
-                lx = s * (ux - dot * fx);
-                ly = s * (uy - dot * fy);
-            }
-            double lgx = cm * mg * lx, lgy = cm * mg * ly;   // F_raw = cm mg g
-            double lgdot = lx * gx + ly * gy;
-            double lmg = cm * lgdot;
-            gk += mg * lgdot * (-m);
-            double t2 = tau * tau, t3 = t2 * tau, t02 = tau0 * tau0;
-            double dmg_dtau = -e * (6.0 / (t3 * tau) + 4.0 / (t3 * tau0) + 1.0 / (t2 * t02));
-            double dmg_dtau0 = e * (1.0 / (t2 * t02) + 1.0 / (tau * t02 * tau0));
-            double ltau = lmg * dmg_dtau;
-            gtau0 += lmg * dmg_dtau0;
-            // g = v / a - b v / (a dd) - x / dd
-            double la = -(lgx * (gx + xx / dd) + lgy * (gy + xy / dd)) / a;
-            double lb = -(lgx * vx + lgy * vy) / (a * dd);
-            double ldd = (lgx * (b * vx / a + xx) + lgy * (b * vy / a + xy)) / (dd * dd);
-            double cv = 1.0 / a - b / (a * dd);
-            gvx += cv * lgx;
-            gvy += cv * lgy;
-            gxx += -lgx / dd;
-            gxy += -lgy / dd;
-            lb += ltau / a;                                  // tau = (b - dd) / a
-            ldd += -ltau / a;
-            la += -ltau * tau / a;
-            double ldisc = ldd / (2.0 * dd);                 // dd = sqrt(b^2 - a c)
+            const double ia = 1.0 / a, idd = 1.0 / dd;
+            const double gx = (vx - (vx * b + xx * a) * idd) * ia;   // grad of tau
+            const double gy = (vy - (vy * b + xy * a) * idd) * ia;
+            const double it = 1.0 / tau, it2 = it * it;
+            double lgx = 0.0, lgy = 0.0, ltau = 0.0;
+            social_side(tau, it, it2, gx, gy, 1.0, A.m, A.k, A.tau0, uix, uiy, lgx, lgy, ltau,
+                        &G.gk, &G.gt0);
+            social_side(tau, it, it2, gx, gy, -1.0, B.m, B.k, B.tau0, ujx, ujy, lgx, lgy, ltau,
+                        nullptr, nullptr);
+            // g = v / a - b v / (a dd) - x / dd,  tau = (b - dd) / a
+            double la = -(lgx * (gx + xx * idd) + lgy * (gy + xy * idd)) * ia;
+            double lb = -(lgx * vx + lgy * vy) * ia * idd;
+            double ldd = (lgx * (b * vx * ia + xx) + lgy * (b * vy * ia + xy)) * idd * idd;
+            const double cv = ia - b * ia * idd;
+            G.gvx += cv * lgx;
+            G.gvy += cv * lgy;
+            G.gxx -= lgx * idd;
+            G.gxy -= lgy * idd;
+            lb += ltau * ia;
+            ldd -= ltau * ia;
+            la -= ltau * tau * ia;
+            const double ldisc = 0.5 * ldd * idd;                  // dd = sqrt(b^2 - a c)
             lb += 2.0 * b * ldisc;
-            la += -c * ldisc;
-            double lc = -a * ldisc;
-            gxx += 2.0 * lc * xx;                            // c = x.x - r^2
-            gxy += 2.0 * lc * xy;
-            gxx += -lb * vx;                                 // b = -x.v
-            gxy += -lb * vy;
-            gvx += -lb * xx;
-            gvy += -lb * xy;
-            gvx += 2.0 * la * vx;                            // a = v.v
-            gvy += 2.0 * la * vy;
+            la -= c * ldisc;
+            const double lc = -a * ldisc;
+            G.gxx += 2.0 * lc * xx - lb * vx;                      // c = x.x - r^2, b = -x.v
+            G.gxy += 2.0 * lc * xy - lb * vy;
+            G.gvx += 2.0 * la * vx - lb * xx;                      // a = v.v
+            G.gvy += 2.0 * la * vy - lb * xy;
         }
     }
-    if (h < 0 && d0 != 0.0)
-        contact_vjp(xx, xy, d0, h, vx, vy, mu, kappa, damp, ux, uy, gxx, gxy, gvx, gvy);
+    if (h < 0 && d0 != 0.0) {
+        // F_i = C(p_i), F_j(-x, -v) = -C(p_j) in i's frame (interactions.py:63-66)
+        contact_vjp3(xx, xy, d0, h, vx, vy, A.mu * uix - B.mu * ujx, A.mu * uiy - B.mu * ujy,
+                     A.kappa * uix - B.kappa * ujx, A.kappa * uiy - B.kappa * ujy,
+                     A.damp * uix - B.damp * ujx, A.damp * uiy - B.damp * ujy, G.gxx, G.gxy,
+                     G.gvx, G.gvy);
+    }
 }
 
 // Reverse of the Circular agent-wall contact (interactions.py:107-120,
@@ -253,69 +304,94 @@ __global__ void k_loss_grad(const double *x, const double *y, const double *targ
     lx[2 * i + 1] += scale * 2.0 * (y[i] - target[2 * i + 1]);
 }
 
-// Pair, wall and adjusting terms of the reverse step for the agent in
-// cell-sorted slot s; writes lx_out, lv_out and accumulates parameter grads.
+// Pair, wall and adjusting terms of the reverse step.  A group of L lanes
+// takes the agent in cell-sorted slot s: its 3 x 3 neighbour cells are three
+// runs of consecutive slots, which the lanes stride through; the lanes'
+// partial sums meet in a fixed butterfly, so the result is deterministic.
+template <int L>
 __global__ void __launch_bounds__(NT) k_adj_forces(StepArgs a, AdjArgs q) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= a.n) return;
-    const int i = a.perm[s];
-    const ScenDev sc = a.scen[a.scen_of[i]];
-    double *const *col = a.col;
-    const float4 me = a.cull[s];
-    const int my_cell = a.key[i];
-    const Circ A = load_circ(a.stage, s);
-    const double uxi = q.lF[2 * i], uyi = q.lF[2 * i + 1];
-    double gxx = 0, gxy = 0, gvx = 0, gvy = 0, gk = 0, gt0 = 0;
-    // agent-agent, both sides of every pair, in the forward visiting order
-    int local = my_cell - sc.cell_base;
-    int ix = local / sc.ny, iy = local - ix * sc.ny;
-    for (int ck = 0; ck < 9; ++ck) {
-        int jx = ix + ck / 3 - 1, jy = iy + ck % 3 - 1;
-        if (jx < 0 || jx >= sc.nx || jy < 0 || jy >= sc.ny) continue;
-        int c2 = sc.cell_base + jx * sc.ny + jy;
-        int b = __ldg(&a.start[c2]), e = __ldg(&a.start[c2 + 1]);
-        for (int t = b; t < e; ++t) {
-            if (t == s) continue;
-            if (pair_far(me, __ldg(&a.cull[t]))) continue;
-            const Circ B = load_circ(a.stage, t);
-            const int j = a.perm[t];
-            // my side: F_i(x_i - x_j, v_i - v_j)
-            pair_circ_vjp(A.x - B.x, A.y - B.y, A.vx - B.vx, A.vy - B.vy, A.r + B.r, A.m, A.k,
-                          A.tau0, A.mu, A.kappa, A.damp, uxi, uyi, gxx, gxy, gvx, gvy, gk, gt0);
-            // neighbour's side: F_j(x_j - x_i, v_j - v_i), d/dx_i = -d/dx_rel
-            double hx = 0, hy = 0, hvx = 0, hvy = 0, dk = 0, dt0 = 0;
-            pair_circ_vjp(B.x - A.x, B.y - A.y, B.vx - A.vx, B.vy - A.vy, B.r + A.r, B.m, B.k,
-                          B.tau0, B.mu, B.kappa, B.damp, q.lF[2 * j], q.lF[2 * j + 1], hx, hy,
-                          hvx, hvy, dk, dt0);
-            gxx -= hx; gxy -= hy; gvx -= hvx; gvy -= hvy;
+    const int r = threadIdx.x & (L - 1);
+    const int s = (int)(((long long)blockIdx.x * NT + threadIdx.x) / L);
+    const bool valid = s < a.n;
+    PairGrad G{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    int i = 0;
+    double uxi = 0.0, uyi = 0.0;
+    if (valid) {
+        i = a.perm[s];
+        const ScenDev sc = a.scen[a.scen_of[i]];
+        const float4 me = a.cull[s];
+        const int my_cell = a.key[i];
+        const Circ A = load_circ(a.stage, s);
+        uxi = q.lF[2 * i];
+        uyi = q.lF[2 * i + 1];
+        const int local = my_cell - sc.cell_base;
+        const int ix = local / sc.ny, iy = local - ix * sc.ny;
+        const int jy0 = iy > 0 ? iy - 1 : 0, jy1 = iy + 1 < sc.ny ? iy + 1 : sc.ny - 1;
+        for (int jx = ix - 1; jx <= ix + 1; ++jx) {
+            if (jx < 0 || jx >= sc.nx) continue;
+            const int c0 = sc.cell_base + jx * sc.ny;
+            const int b = __ldg(&a.start[c0 + jy0]), e = __ldg(&a.start[c0 + jy1 + 1]);
+            for (int t = b + r; t < e; t += L) {
+                if (t == s || pair_far(me, __ldg(&a.cull[t]))) continue;
+                const Circ B = load_circ(a.stage, t);
+                const int j = a.perm[t];
+                pair_vjp_both(A, B, uxi, uyi, q.lF[2 * j], q.lF[2 * j + 1], G);
+            }
+        }
+        if (sc.wall_count > 0) {
+            const bool all_walls = me.z > (float)sc.wall_reach;
+            const int wb = all_walls ? sc.wall_begin : __ldg(&a.wall_start[my_cell]);
+            const int we = all_walls ? sc.wall_begin + sc.wall_count
+                                     : __ldg(&a.wall_start[my_cell + 1]);
+            for (int qw = wb + r; qw < we; qw += L) {
+                const int w = all_walls ? qw : __ldg(&a.wall_idx[qw]);
+                wall_circ_vjp(A, a.walls + (size_t)w * WALL_D, uxi, uyi, G.gxx, G.gxy, G.gvx,
+                              G.gvy);
+            }
         }
     }
-    // walls
-    if (sc.wall_count > 0) {
-        const bool all_walls = me.z > (float)sc.wall_reach;
-        int wb = all_walls ? sc.wall_begin : __ldg(&a.wall_start[my_cell]);
-        int we = all_walls ? sc.wall_begin + sc.wall_count : __ldg(&a.wall_start[my_cell + 1]);
-        for (int qw = wb; qw < we; ++qw) {
-            int w = all_walls ? qw : __ldg(&a.wall_idx[qw]);
-            wall_circ_vjp(A, a.walls + (size_t)w * WALL_D, uxi, uyi, gxx, gxy, gvx, gvy);
-        }
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) {
+        G.gxx += __shfl_xor_sync(0xffffffffu, G.gxx, o);
+        G.gxy += __shfl_xor_sync(0xffffffffu, G.gxy, o);
+        G.gvx += __shfl_xor_sync(0xffffffffu, G.gvx, o);
+        G.gvy += __shfl_xor_sync(0xffffffffu, G.gvy, o);
+        G.gk += __shfl_xor_sync(0xffffffffu, G.gk, o);
+        G.gt0 += __shfl_xor_sync(0xffffffffu, G.gt0, o);
     }
+    if (!valid || r != 0) return;
     // adjusting: F = (m / tau_adj) (v0 e0 - v)
+    double *const *col = a.col;
     const double m = col[MASS][i], ta = col[TAU_ADJ][i], v0 = col[V0][i];
     const double ex = col[E0X][i], ey = col[E0Y][i];
     const double kk = m / ta;
-    gvx -= kk * uxi;
-    gvy -= kk * uyi;
-    double g_ta = -(m / (ta * ta)) * (uxi * (v0 * ex - col[VX][i]) + uyi * (v0 * ey - col[VY][i]));
-    double g_v0 = kk * (uxi * ex + uyi * ey);
-    q.lx_out[2 * i] = q.lx[2 * i] + gxx;
-    q.lx_out[2 * i + 1] = q.lx[2 * i + 1] + gxy;
-    q.lv_out[2 * i] = q.lvt[2 * i] + gvx;
-    q.lv_out[2 * i + 1] = q.lvt[2 * i + 1] + gvy;
+    G.gvx -= kk * uxi;
+    G.gvy -= kk * uyi;
+    const double g_ta =
+        -(m / (ta * ta)) * (uxi * (v0 * ex - col[VX][i]) + uyi * (v0 * ey - col[VY][i]));
+    const double g_v0 = kk * (uxi * ex + uyi * ey);
+    q.lx_out[2 * i] = q.lx[2 * i] + G.gxx;
+    q.lx_out[2 * i + 1] = q.lx[2 * i + 1] + G.gxy;
+    q.lv_out[2 * i] = q.lvt[2 * i] + G.gvx;
+    q.lv_out[2 * i + 1] = q.lvt[2 * i + 1] + G.gvy;
     q.grad[4 * i + 0] += g_ta;
     q.grad[4 * i + 1] += g_v0;
-    q.grad[4 * i + 2] += gt0;
-    q.grad[4 * i + 3] += gk;
+    q.grad[4 * i + 2] += G.gt0;
+    q.grad[4 * i + 3] += G.gk;
+}
+
+// Copies of up to 8 state columns in one launch (checkpoint save / restore).
+struct ColCopy {
+    const double *src[8];
+    double *dst[8];
+    int ncol;
+};
+
+__global__ void k_copy_cols(ColCopy cc, int n) {
+    const int k = blockIdx.y;
+    if (k >= cc.ncol) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        cc.dst[k][i] = cc.src[k][i];
 }
 
 // max |v| and max v0 with their first indices (single block, index order).
@@ -371,7 +447,25 @@ void launch_adj_seed(const AdjArgs &q, cudaStream_t s) {
     k_adj_sum<<<1, 1, 0, s>>>(q.partial, nb, q.ldt, 1.0, 0);
 }
 void launch_adj_forces(const StepArgs &a, const AdjArgs &q, cudaStream_t s) {
-    if (a.n > 0) k_adj_forces<<<nblk(a.n, NT), NT, 0, s>>>(a, q);
+    if (a.n <= 0) return;
+    // lanes per agent: enough warps to fill the SMs at small agent counts
+    const long long n = a.n;
+    if (n < 20000) k_adj_forces<16><<<nblk(n * 16, NT), NT, 0, s>>>(a, q);
+    else if (n < 80000) k_adj_forces<8><<<nblk(n * 8, NT), NT, 0, s>>>(a, q);
+    else k_adj_forces<4><<<nblk(n * 4, NT), NT, 0, s>>>(a, q);
+}
+void launch_copy_cols(const double *const *src, double *const *dst, int ncol, int n,
+                      cudaStream_t s) {
+    if (n <= 0 || ncol <= 0) return;
+    ColCopy cc;
+    for (int k = 0; k < 8; ++k) {
+        cc.src[k] = k < ncol ? src[k] : nullptr;
+        cc.dst[k] = k < ncol ? dst[k] : nullptr;
+    }
+    cc.ncol = ncol < 8 ? ncol : 8;
+    int nb = nblk(n, 256);
+    if (nb > 1024) nb = 1024;
+    k_copy_cols<<<dim3(nb, cc.ncol), 256, 0, s>>>(cc, n);
 }
 void launch_adj_dt(const AdjArgs &q, double dt_min, double dt_max, const double *vx,
                    const double *vy, const double *v0, cudaStream_t s) {

@@ -764,11 +764,14 @@ constexpr int kSnapCol[SNAP_COLS] = {cdk::X,   cdk::Y,   cdk::VX, cdk::VY,
                                      cdk::FPX, cdk::FPY, cdk::FX, cdk::FY};
 
 int copy_state(cd_ctx *c, double *snap, bool save) {
+    const double *src[SNAP_COLS];
+    double *dst[SNAP_COLS];
     for (int k = 0; k < SNAP_COLS; ++k) {
         double *col = c->col[kSnapCol[k]], *buf = snap + (size_t)k * c->n;
-        CUDA_OR_FAIL(c, cudaMemcpyAsync(save ? buf : col, save ? col : buf, sizeof(double) * c->n,
-                                        cudaMemcpyDeviceToDevice, c->stream));
+        src[k] = save ? col : buf;
+        dst[k] = save ? buf : col;
     }
+    cdk::launch_copy_cols(src, dst, SNAP_COLS, (int)c->n, c->stream);
     return CD_OK;
 }
 
@@ -863,14 +866,13 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
                 cdk::launch_loss_grad(after, after + n, tgt + (size_t)t * 2 * n, (int)n, scale, lx, st);
                 if ((rc = copy_state(c, seg + (size_t)(t - t0) * snap, false))) break;
                 StepArgs a = args_of(c, fnodes);
-                enqueue_cells(c, a);
-                cdk::launch_forces(a, st, c->variant);    // total force of step t
+                enqueue_cells(c, a);                        // cell list of the state before step t
                 cdk::AdjArgs q;
                 q.n = (int)n;
                 q.dt = dts + t;
                 q.mass = c->col[cdk::MASS];
-                q.fx = c->col[cdk::FX];
-                q.fy = c->col[cdk::FY];
+                q.fx = after + 4 * n;                       // force_prev after the step = its force
+                q.fy = after + 5 * n;
                 q.vnx = after + 2 * n;
                 q.vny = after + 3 * n;
                 q.fpx = c->col[cdk::FPX];

@@ -70,7 +70,7 @@ struct StepArgs {
 struct AdjArgs {
     int n;
     const double *dt;                      // this step's timestep (device scalar)
-    const double *mass, *fx, *fy;          // mass, recomputed total force
+    const double *mass, *fx, *fy;          // mass, the step's total force
     const double *vnx, *vny;               // velocity after the step
     const double *fpx, *fpy;               // force_prev before the step
     const double *lx, *lv, *lfp;           // incoming adjoints of x', v', fp'
@@ -91,6 +91,8 @@ void launch_loss(const double *x, const double *y, const double *target, int n,
                  double *partial, double *loss, double scale, cudaStream_t s);
 void launch_loss_grad(const double *x, const double *y, const double *target, int n,
                       double scale, double *lx, cudaStream_t s);
+void launch_copy_cols(const double *const *src, double *const *dst, int ncol, int n,
+                      cudaStream_t s);
 
 // Launchers (cd_kernels.cu)
 void launch_prepare(const StepArgs &a, cudaStream_t s);
