@@ -102,6 +102,7 @@ def load(path=None):
         'cd_measure_fp64_peak': (ctypes.c_int, [pd]),
         'cd_variant_count': (ctypes.c_int, [ctypes.POINTER(ctypes.c_int)]),
         'cd_variant_shape': (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                            ctypes.POINTER(ctypes.c_int),
                                             ctypes.POINTER(ctypes.c_int)]),
         'cd_set_variant': (ctypes.c_int, [P, ctypes.c_int]),
         'cd_launch': (ctypes.c_int, [P, ctypes.c_int, i64]),
@@ -146,15 +147,16 @@ def dptr(a):
 
 
 def variants():
-    """[(threads_per_block, staged_per_thread)] of the force-kernel variants."""
+    """[(threads_per_block, staged_per_thread, lanes_per_agent)] of the
+    force-kernel variants."""
     L = load()
     n = ctypes.c_int()
     check(L.cd_variant_count(ctypes.byref(n)))
     out = []
     for v in range(n.value):
-        t, c = ctypes.c_int(), ctypes.c_int()
-        check(L.cd_variant_shape(v, ctypes.byref(t), ctypes.byref(c)))
-        out.append((t.value, c.value))
+        t, c, g = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(L.cd_variant_shape(v, ctypes.byref(t), ctypes.byref(c), ctypes.byref(g)))
+        out.append((t.value, c.value, g.value))
     return out
 
 

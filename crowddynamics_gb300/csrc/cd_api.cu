@@ -343,6 +343,7 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     cd_ctx *c = new cd_ctx();
     c->body = body_type;
     c->n = n;
+    c->variant = cdk::default_variant(n);
     c->nw = nw;
     c->ncells = ncells;
     c->nscen = (int)n_scenarios;
@@ -712,13 +713,12 @@ int cd_variant_count(int *count) {
     return CD_OK;
 }
 
-int cd_variant_shape(int variant, int *threads, int *staged) {
-    static const int nt[cdk::N_VARIANTS] = {128, 64, 128, 64, 256};
-    static const int cap[cdk::N_VARIANTS] = {64, 64, 32, 32, 32};
+int cd_variant_shape(int variant, int *threads, int *staged, int *lanes) {
     if (variant < 0 || variant >= cdk::N_VARIANTS)
         return fail(nullptr, CD_ERR_INVALID_VALUE, "unknown variant");
-    if (threads) *threads = nt[variant];
-    if (staged) *staged = cap[variant];
+    if (threads) *threads = cdk::variant_threads(variant);
+    if (staged) *staged = cdk::variant_staged(variant);
+    if (lanes) *lanes = cdk::variant_lanes(variant);
     return CD_OK;
 }
 
@@ -1062,7 +1062,7 @@ extern "C" int cd_agent_agent_noalloc(int body_type, int64_t n, const double *co
     cdk::launch_scan(a.count, a.start, ncells, scan, st);
     cdk::launch_scatter(a, st);
     cdk::launch_gather(a, st);
-    cdk::launch_forces(a, st, 0);
+    cdk::launch_forces(a, st, cdk::default_variant(n));
     CUDA_OR_FAIL(nullptr, cudaGetLastError());
     int h = 0;
     CUDA_OR_FAIL(nullptr, cudaMemcpyAsync(&h, a.err, sizeof(int), cudaMemcpyDeviceToHost, st));

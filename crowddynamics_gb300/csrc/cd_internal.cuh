@@ -101,7 +101,11 @@ int scan_scratch_ints(int n);
 void launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s);
 void launch_scatter(const StepArgs &a, cudaStream_t s);
 void launch_gather(const StepArgs &a, cudaStream_t s);
-constexpr int N_VARIANTS = 5;       // launch variants of the force kernel
+constexpr int N_VARIANTS = 9;       // launch variants of the force kernel
+int variant_lanes(int variant);
+int default_variant(long long n_agents);
+int variant_threads(int variant);
+int variant_staged(int variant);
 void launch_forces(const StepArgs &a, cudaStream_t s, int variant);
 void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s);
 void launch_v0max(const StepArgs &a, double *v0max_out, cudaStream_t s);

@@ -503,20 +503,23 @@ __device__ __forceinline__ void r_off_part(const TC &A, int part, double &ox, do
     oy = part == 1 ? (0.0 + ey) : (part == 2 ? (0.0 - ey) : 0.0);
 }
 
-// Circular pair, calling agent A, other agent B (interactions.py:51-70).
-__device__ __forceinline__ void pair_circular_me(const Circ &A, const Circ &B, double &fx,
-                                                 double &fy) {
+// Circular pair, calling agent A, other agent B (interactions.py:51-70):
+// A's force from the pair in (Fx, Fy); false when the pair does not interact
+// (h >= sight_soc: the reference adds nothing).
+__device__ __forceinline__ bool pair_circular_eval(const Circ &A, const Circ &B, double &Fx,
+                                                   double &Fy) {
+    Fx = 0.0;
+    Fy = 0.0;
     double xx = A.x - B.x, xy = A.y - B.y;
     double d = cdm_hypot(xx, xy);
     double r_tot = A.r + B.r;
     double h = d - r_tot;
-    if (!(h < SIGTH_SOC)) return;
+    if (!(h < SIGTH_SOC)) return false;
     double vrx = A.vx - B.vx, vry = A.vy - B.vy;
     double a = vrx * vrx + vry * vry;
     double b = -(xx * vrx + xy * vry);
     double c = (xx * xx + xy * xy) - r_tot * r_tot;
     double disc = b * b - a * c;
-    double Fx = 0.0, Fy = 0.0;
     if (disc > 0 && a != 0) {                     // isnan(d) or d == 0 or a == 0
         double dd = sqrt(disc);
         double tau = (b - dd) / a;
@@ -538,8 +541,16 @@ __device__ __forceinline__ void pair_circular_me(const Circ &A, const Circ &B, d
         Fx = Fx + cx;
         Fy = Fy + cy;
     }
-    fx += Fx;
-    fy += Fy;
+    return true;
+}
+
+__device__ __forceinline__ void pair_circular_me(const Circ &A, const Circ &B, double &fx,
+                                                 double &fy) {
+    double Fx, Fy;
+    if (pair_circular_eval(A, B, Fx, Fy)) {
+        fx += Fx;
+        fy += Fy;
+    }
 }
 
 // Per-warp queue for the square root and division of the defined sub-circle
@@ -554,13 +565,15 @@ struct WarpQueue {
 
 constexpr float PRESEL_MARGIN = 1e-4f;   // metres (float32 error of h is ~1e-6 m)
 
-// One ThreeCircle pair step for every lane of the warp (collective: all lanes
-// in `wmask` call it; `act` lanes have a pair, `me_first` its orientation).
-__device__ __forceinline__ void tc_pair_step(const TC &A, const float4 meC, const float4 meF0,
+// One ThreeCircle pair for every lane of the warp (collective: all lanes in
+// `wmask` call it; `act` lanes have a pair, `me_first` its orientation):
+// A's force and torque from the pair in (Fx, Fy, Tq); false when the pair
+// does not interact.
+__device__ __forceinline__ bool tc_pair_eval(const TC &A, const float4 meC, const float4 meF0,
                                              const float4 meF1, const StepArgs &a, bool act,
                                              int t, bool me_first, WarpQueue &q, int lane,
-                                             unsigned wmask, int nlanes, double &fx, double &fy,
-                                             double &tq) {
+                                             unsigned wmask, int nlanes, double &Fx_out,
+                                             double &Fy_out, double &Tq_out) {
     TC B = A;
     float4 oC = meC, oF0 = meF0, oF1 = meF1;
     if (act) {
@@ -736,10 +749,23 @@ __device__ __forceinline__ void tc_pair_step(const TC &A, const float4 meC, cons
         Fx = Fx + cx;
         Fy = Fy + cy;
     }
-    if (inter) {
+    Fx_out = Fx;
+    Fy_out = Fy;
+    Tq_out = rmx * Fy - rmy * Fx;                  // cross(r_moment, force)
+    return inter;
+}
+
+__device__ __forceinline__ void tc_pair_step(const TC &A, const float4 meC, const float4 meF0,
+                                             const float4 meF1, const StepArgs &a, bool act,
+                                             int t, bool me_first, WarpQueue &q, int lane,
+                                             unsigned wmask, int nlanes, double &fx, double &fy,
+                                             double &tq) {
+    double Fx, Fy, Tq;
+    if (tc_pair_eval(A, meC, meF0, meF1, a, act, t, me_first, q, lane, wmask, nlanes, Fx, Fy,
+                     Tq)) {
         fx += Fx;
         fy += Fy;
-        tq += rmx * Fy - rmy * Fx;                 // cross(r_moment, force)
+        tq += Tq;
     }
 }
 
@@ -775,34 +801,23 @@ __device__ __forceinline__ int enumerate_candidates(const StepArgs &a, const Sce
     return nl;
 }
 
-// All forces on the agent in cell-sorted slot s, then its integration.
-// Called by a whole warp (lanes with s >= n skip; warp collectives run over
-// the lanes that take part).
-template <int BODY, int NT, int CAP>
-__device__ __forceinline__ void force_agent(const StepArgs &a, const int s, int *list,
-                                            WarpQueue *wq) {
-    const unsigned wmask = __ballot_sync(0xffffffffu, s < a.n);
-    if (s >= a.n) return;
-    const int lane = threadIdx.x & 31;
-    const int nlanes = __popc(wmask);           // active lanes form a prefix
-    const int i = a.perm[s];
-    const int sid = a.scen_of[i];
-    const ScenDev sc = a.scen[sid];
+// Per-agent terms before agent-agent: the force (and torque) array's value,
+// fluctuation, orientation and adjusting, in the reference's node order.
+template <int BODY>
+__device__ __forceinline__ void agent_prologue(const StepArgs &a, const int i, double &fx,
+                                               double &fy, double &tq, double &phi0) {
     double *const *col = a.col;
-    const float4 me = a.cull[s];
-    const int my_cell = a.key[i];
     const int nodes = a.nodes;
-
-    double fx = col[FX][i], fy = col[FY][i];
-    double tq = (BODY == 1) ? col[TORQUE][i] : 0.0;
-
+    fx = col[FX][i];
+    fy = col[FY][i];
+    tq = (BODY == 1) ? col[TORQUE][i] : 0.0;
     // Fluctuation (simulation/logic.py:78-86), noise drawn on the host
     if ((nodes & N_FLUCT) && a.noise_f) {
         fx = fx + a.noise_f[2 * i];
         fy = fy + a.noise_f[2 * i + 1];
         if (BODY == 1 && a.noise_m) tq = tq + a.noise_m[i];
     }
-    double phi0 = (BODY == 1) ? col[PHI0][i] : 0.0;
+    phi0 = (BODY == 1) ? col[PHI0][i] : 0.0;
     // Orientation (core/steering/orientation.py:17-21)
     if (BODY == 1 && (nodes & N_ORIENT)) phi0 = cdm_atan2(col[E0Y][i], col[E0X][i]);
     // Adjusting (core/motion/adjusting.py:16-121)
@@ -816,42 +831,16 @@ __device__ __forceinline__ void force_agent(const StepArgs &a, const int s, int 
                           (wrap_to_pi(phi0 - col[PHI][i]) / PI_D * col[W0][i] - col[OMEGA][i]);
         }
     }
+}
 
-    // Agent-agent (core/interactions.py:147-166), contributions summed in the
-    // reference's visiting order for this agent
-    if (nodes & N_AGENT) {
-        int *mylist = list + threadIdx.x;
-        EnumState st{0, -1};
-        if (BODY == 0) {
-            const Circ A = load_circ(a.stage, s);
-            while (true) {
-                int nl = enumerate_candidates<NT, CAP>(a, sc, s, my_cell, me, mylist, st);
-                for (int k = 0; k < nl; ++k) {
-                    int v = mylist[k * NT];
-                    const Circ B = load_circ(a.stage, v < 0 ? ~v : v);
-                    pair_circular_me(A, B, fx, fy);
-                }
-                if (st.ck >= 9) break;
-            }
-        } else {
-            const TC A = load_tc(a.stage, s);
-            const float4 meF0 = a.stage_f[2 * s], meF1 = a.stage_f[2 * s + 1];
-            WarpQueue &q = wq[threadIdx.x >> 5];
-            while (true) {
-                int nl = enumerate_candidates<NT, CAP>(a, sc, s, my_cell, me, mylist, st);
-                int kmax = __reduce_max_sync(wmask, (unsigned)nl);
-                for (int k = 0; k < kmax; ++k) {
-                    bool act = k < nl;
-                    int v = act ? mylist[k * NT] : 0;
-                    int t = v < 0 ? ~v : v;
-                    tc_pair_step(A, me, meF0, meF1, a, act, t, v < 0, q, lane, wmask, nlanes,
-                                 fx, fy, tq);
-                }
-                if (!__any_sync(wmask, st.ck < 9)) break;
-            }
-        }
-    }
-
+// Per-agent terms after agent-agent: walls, then integration and reset.
+template <int BODY>
+__device__ __forceinline__ void agent_epilogue(const StepArgs &a, const int s, const int i,
+                                               const int sid, const ScenDev &sc,
+                                               const float4 me, const int my_cell, double fx,
+                                               double fy, double tq, const double phi0) {
+    double *const *col = a.col;
+    const int nodes = a.nodes;
     // Agent-wall (core/interactions.py:107-141,169-186), walls in index order
     if ((nodes & N_WALL) && sc.wall_count > 0) {
         const bool all_walls = me.z > (float)sc.wall_reach;
@@ -922,6 +911,197 @@ __device__ __forceinline__ void force_agent(const StepArgs &a, const int s, int 
     }
 }
 
+// All forces on the agent in cell-sorted slot s, then its integration.
+// Called by a whole warp (lanes with s >= n skip; warp collectives run over
+// the lanes that take part).
+template <int BODY, int NT, int CAP>
+__device__ __forceinline__ void force_agent(const StepArgs &a, const int s, int *list,
+                                            WarpQueue *wq) {
+    const unsigned wmask = __ballot_sync(0xffffffffu, s < a.n);
+    if (s >= a.n) return;
+    const int lane = threadIdx.x & 31;
+    const int nlanes = __popc(wmask);           // active lanes form a prefix
+    const int i = a.perm[s];
+    const int sid = a.scen_of[i];
+    const ScenDev sc = a.scen[sid];
+    const float4 me = a.cull[s];
+    const int my_cell = a.key[i];
+
+    double fx, fy, tq, phi0;
+    agent_prologue<BODY>(a, i, fx, fy, tq, phi0);
+
+    // Agent-agent (core/interactions.py:147-166), contributions summed in the
+    // reference's visiting order for this agent
+    if (a.nodes & N_AGENT) {
+        int *mylist = list + threadIdx.x;
+        EnumState st{0, -1};
+        if (BODY == 0) {
+            const Circ A = load_circ(a.stage, s);
+            while (true) {
+                int nl = enumerate_candidates<NT, CAP>(a, sc, s, my_cell, me, mylist, st);
+                for (int k = 0; k < nl; ++k) {
+                    int v = mylist[k * NT];
+                    const Circ B = load_circ(a.stage, v < 0 ? ~v : v);
+                    pair_circular_me(A, B, fx, fy);
+                }
+                if (st.ck >= 9) break;
+            }
+        } else {
+            const TC A = load_tc(a.stage, s);
+            const float4 meF0 = a.stage_f[2 * s], meF1 = a.stage_f[2 * s + 1];
+            WarpQueue &q = wq[threadIdx.x >> 5];
+            while (true) {
+                int nl = enumerate_candidates<NT, CAP>(a, sc, s, my_cell, me, mylist, st);
+                int kmax = __reduce_max_sync(wmask, (unsigned)nl);
+                for (int k = 0; k < kmax; ++k) {
+                    bool act = k < nl;
+                    int v = act ? mylist[k * NT] : 0;
+                    int t = v < 0 ? ~v : v;
+                    tc_pair_step(A, me, meF0, meF1, a, act, t, v < 0, q, lane, wmask, nlanes,
+                                 fx, fy, tq);
+                }
+                if (!__any_sync(wmask, st.ck < 9)) break;
+            }
+        }
+    }
+    agent_epilogue<BODY>(a, s, i, sid, sc, me, my_cell, fx, fy, tq, phi0);
+}
+
+// Lane-group form: L lanes share one agent (32 / L agents per warp).  The
+// agent's candidates are the slots of its 3 x 3 neighbour cells, which in
+// the reference's visiting order ((dx, dy) lexicographic, ascending within a
+// cell) are three runs of consecutive slots, one per dx.  The group culls L
+// candidates at a time, appends the near ones to its queue in order, and
+// evaluates L queued pairs at once, one per lane; the pair forces are then
+// added in queue order by every lane of the group (shuffles), so each lane
+// holds the same, reference-ordered sum.  The first lane of the group then
+// adds the walls and integrates.  Called by all 32 lanes of the warp.
+template <int BODY, int L>
+__device__ __forceinline__ void force_agent_group(const StepArgs &a, const int s,
+                                                  int *gq, WarpQueue *wq) {
+    constexpr unsigned FULL = 0xffffffffu;
+    constexpr unsigned GMASK = L == 32 ? 0xffffffffu : ((1u << L) - 1u);
+    const int lane = threadIdx.x & 31;
+    const int r = lane & (L - 1);
+    const int g0 = lane & ~(L - 1);              // first lane of the group
+    const bool valid = s < a.n;
+    int i = 0, sid = 0, my_cell = 0;
+    ScenDev sc;
+    float4 me = make_float4(0.f, 0.f, 0.f, 0.f);
+    double fx = 0.0, fy = 0.0, tq = 0.0, phi0 = 0.0;
+    if (valid) {
+        i = a.perm[s];
+        sid = a.scen_of[i];
+        sc = a.scen[sid];
+        me = a.cull[s];
+        my_cell = a.key[i];
+        agent_prologue<BODY>(a, i, fx, fy, tq, phi0);
+    }
+    if (a.nodes & N_AGENT) {
+        // candidate runs, one per dx in -1, 0, 1 (empty where off the grid)
+        int rb[3] = {0, 0, 0}, re[3] = {0, 0, 0};
+        if (valid) {
+            const int local = my_cell - sc.cell_base;
+            const int ix = local / sc.ny, iy = local - ix * sc.ny;
+            const int jy0 = iy > 0 ? iy - 1 : 0, jy1 = iy + 1 < sc.ny ? iy + 1 : sc.ny - 1;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const int jx = ix + d - 1;
+                if (jx < 0 || jx >= sc.nx) continue;
+                const int c0 = sc.cell_base + jx * sc.ny;
+                rb[d] = __ldg(&a.start[c0 + jy0]);
+                re[d] = __ldg(&a.start[c0 + jy1 + 1]);
+            }
+        }
+        // current run: index `run`, end `cur_e`; runs are selected without
+        // dynamic array indexing so that they stay in registers
+        int run = 0, cur_e = 0, p = 0;
+        bool done = true;
+#pragma unroll
+        for (int d = 2; d >= 0; --d)
+            if (rb[d] < re[d]) { run = d; p = rb[d]; cur_e = re[d]; done = false; }
+        int qlen = 0;
+        Circ Ac;
+        TC At;
+        float4 meF0 = make_float4(0.f, 0.f, 0.f, 0.f), meF1 = meF0;
+        if (valid) {
+            if (BODY == 0) Ac = load_circ(a.stage, s);
+            else {
+                At = load_tc(a.stage, s);
+                meF0 = a.stage_f[2 * s];
+                meF1 = a.stage_f[2 * s + 1];
+            }
+        }
+        while (true) {
+            // fill: until the group's queue holds L pairs or its candidates run out
+            while (true) {
+                const bool need = !done && qlen < L;
+                if (!__any_sync(FULL, need)) break;
+                const int t = p + r;
+                const bool near = need && t < cur_e && t != s &&
+                                  !pair_far(me, __ldg(&a.cull[t]));
+                const unsigned gb = (__ballot_sync(FULL, near) >> g0) & GMASK;
+                if (near) {
+                    // orientation: the dx = +1 run follows the agent's cell, the dx = -1
+                    // run precedes it, and within dx = 0 slot order decides
+                    const bool me_first = run == 2 || (run == 1 && t > s);
+                    gq[qlen + __popc(gb & ((1u << r) - 1u))] = me_first ? ~t : t;
+                }
+                if (need) {
+                    qlen += __popc(gb);
+                    p += L;
+                    if (p >= cur_e) {                // next non-empty run, if any
+                        if (run < 1 && rb[1] < re[1]) {
+                            run = 1; p = rb[1]; cur_e = re[1];
+                        } else if (run < 2 && rb[2] < re[2]) {
+                            run = 2; p = rb[2]; cur_e = re[2];
+                        } else {
+                            done = true;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+            const int cnt = qlen < L ? qlen : L;
+            const int cmax = (int)__reduce_max_sync(FULL, (unsigned)cnt);
+            if (cmax == 0) break;
+            const bool act = r < cnt;
+            const int v = act ? gq[r] : 0;
+            const int t = v < 0 ? ~v : v;
+            double Fx = 0.0, Fy = 0.0, Tq = 0.0;
+            bool inter = false;
+            if (BODY == 0) {
+                if (act) inter = pair_circular_eval(Ac, load_circ(a.stage, t), Fx, Fy);
+            } else {
+                inter = tc_pair_eval(At, me, meF0, meF1, a, act, t, v < 0, wq[threadIdx.x >> 5],
+                                     lane, FULL, 32, Fx, Fy, Tq);
+            }
+            // reference-ordered sum over the group's evaluated pairs
+            const unsigned ib = __ballot_sync(FULL, inter);
+            for (int k = 0; k < cmax; ++k) {
+                const double ax = __shfl_sync(FULL, Fx, g0 + k);
+                const double ay = __shfl_sync(FULL, Fy, g0 + k);
+                double aq = 0.0;
+                if (BODY == 1) aq = __shfl_sync(FULL, Tq, g0 + k);
+                if ((ib >> (g0 + k)) & 1u) {
+                    fx = fx + ax;
+                    fy = fy + ay;
+                    if (BODY == 1) tq = tq + aq;
+                }
+            }
+            // drop the evaluated pairs from the queue
+            const int rest = qlen - cnt;
+            const int moved = r < rest ? gq[cnt + r] : 0;
+            __syncwarp();
+            if (r < rest) gq[r] = moved;
+            qlen = rest;
+            __syncwarp();
+        }
+    }
+    if (!valid || r != 0) return;
+    agent_epilogue<BODY>(a, s, i, sid, sc, me, my_cell, fx, fy, tq, phi0);
+}
+
 // Persistent grid (resident blocks only): each warp claims 32 consecutive
 // cell-sorted agents at a time from a counter, so uneven per-agent work
 // spreads over all SMs without a partial last wave.  NT threads per block,
@@ -938,6 +1118,28 @@ __global__ void __launch_bounds__(NT) k_forces(StepArgs a) {
         chunk = __shfl_sync(0xffffffffu, chunk, 0);
         if (chunk * 32 >= a.n) return;
         force_agent<BODY, NT, CAP>(a, chunk * 32 + lane, list, wq);
+        __syncwarp();
+    }
+}
+
+// Persistent lane-group grid: each warp claims 32 / L consecutive cell-sorted
+// agents at a time from a counter.
+constexpr int NTG = 128;
+
+template <int BODY, int L>
+__global__ void __launch_bounds__(NTG) k_forces_group(StepArgs a) {
+    extern __shared__ unsigned char smem[];
+    int *gq_all = reinterpret_cast<int *>(smem);                 // 2L ints per group
+    WarpQueue *wq = reinterpret_cast<WarpQueue *>(smem + sizeof(int) * 2 * NTG);
+    int *gq = gq_all + 2 * (threadIdx.x & ~(L - 1));
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int chunk = 0;
+        if (lane == 0) chunk = atomicAdd(a.work, 1);
+        chunk = __shfl_sync(0xffffffffu, chunk, 0);
+        const int s0 = chunk * (32 / L);
+        if (s0 >= a.n) return;
+        force_agent_group<BODY, L>(a, s0 + lane / L, gq, wq);
         __syncwarp();
     }
 }
@@ -1132,12 +1334,17 @@ void launch_gather(const StepArgs &a, cudaStream_t s) {
 }
 // Launch variants of the force kernel: (threads per block, staged candidates
 // per thread).
-struct Variant { int nt, cap; };
-constexpr Variant kVariants[N_VARIANTS] = {{128, 64}, {64, 64}, {128, 32}, {64, 32}, {256, 32}};
+// Force-kernel launch variants: the per-thread kernel (k_forces, lanes = 1)
+// with NT threads per block and CAP candidates staged per thread per pass,
+// and the lane-group kernel (k_forces_group) with L lanes per agent.
+struct Variant { int nt, cap, lanes; };
+constexpr Variant kVariants[N_VARIANTS] = {{128, 64, 1}, {64, 64, 1}, {128, 32, 1}, {64, 32, 1},
+                                           {256, 32, 1}, {NTG, 0, 4},  {NTG, 0, 8}, {NTG, 0, 16},
+                                           {NTG, 0, 32}};
 
 size_t forces_smem_bytes(int body, int variant) {
     const Variant v = kVariants[variant];
-    size_t b = sizeof(int) * (size_t)v.cap * v.nt;
+    size_t b = v.lanes == 1 ? sizeof(int) * (size_t)v.cap * v.nt : sizeof(int) * 2 * (size_t)NTG;
     if (body == 1) b += sizeof(WarpQueue) * (v.nt / 32);
     return b;
 }
@@ -1145,9 +1352,31 @@ size_t forces_smem_bytes(int body, int variant) {
 typedef void (*ForcesFn)(StepArgs);
 constexpr ForcesFn kForces[2][N_VARIANTS] = {
     {k_forces<0, 128, 64>, k_forces<0, 64, 64>, k_forces<0, 128, 32>, k_forces<0, 64, 32>,
-     k_forces<0, 256, 32>},
+     k_forces<0, 256, 32>, k_forces_group<0, 4>, k_forces_group<0, 8>, k_forces_group<0, 16>,
+     k_forces_group<0, 32>},
     {k_forces<1, 128, 64>, k_forces<1, 64, 64>, k_forces<1, 128, 32>, k_forces<1, 64, 32>,
-     k_forces<1, 256, 32>}};
+     k_forces<1, 256, 32>, k_forces_group<1, 4>, k_forces_group<1, 8>, k_forces_group<1, 16>,
+     k_forces_group<1, 32>}};
+
+// Variant a new context starts with: lanes per agent such that the warps
+// cover the SMs several times over (measured on hallway, room and field
+// workloads of 400 to 100k agents).
+int default_variant(long long n) {
+    if (n < 1000) return 8;          // 32 lanes per agent
+    if (n < 15000) return 7;         // 16
+    if (n < 60000) return 6;         // 8
+    return 0;                        // one lane per agent, 128 threads, 64 staged
+}
+
+int variant_lanes(int variant) {
+    return variant >= 0 && variant < N_VARIANTS ? kVariants[variant].lanes : 0;
+}
+int variant_threads(int variant) {
+    return variant >= 0 && variant < N_VARIANTS ? kVariants[variant].nt : 0;
+}
+int variant_staged(int variant) {
+    return variant >= 0 && variant < N_VARIANTS ? kVariants[variant].cap : 0;
+}
 
 // Resident blocks of each force kernel variant on each device.
 int g_forces_blocks[64][2][N_VARIANTS];
@@ -1180,7 +1409,8 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant) {
     const int body = a.body ? 1 : 0;
     int resident = (dev >= 0 && dev < 64) ? g_forces_blocks[dev][body][variant] : 0;
     if (resident <= 0) resident = 152;
-    int blocks = std::min(nblk(a.n, v.nt), resident);
+    const long long threads = (long long)a.n * v.lanes;
+    int blocks = (int)std::min<long long>((threads + v.nt - 1) / v.nt, resident);
     cudaMemsetAsync(a.work, 0, sizeof(int), s);
     kForces[body][variant]<<<blocks, v.nt, forces_smem_bytes(body, variant), s>>>(a);
 }

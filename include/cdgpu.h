@@ -168,12 +168,16 @@ int cd_kernel_time(cd_ctx *ctx, double *force_ms, int64_t *force_launches,
 /* Number of kernels one step with `nodes` launches (memsets excluded). */
 int cd_kernels_per_step(const cd_ctx *ctx, int nodes, int64_t *kernels);
 
-/* Launch variants of the agent-force kernel: threads per block and
- * candidates staged per thread per pass.  Every variant gives bit-identical
- * results; only the speed differs, so an autotuner may pick one per context
- * (the choice is applied to the next captured graph). */
+/* Launch variants of the agent-force kernel: threads per block, candidates
+ * staged per thread per pass (lanes_per_agent == 1: one lane per agent) or
+ * lanes that share one agent (lanes_per_agent > 1, staged_per_thread 0).
+ * Every variant gives bit-identical results; only the speed differs, so an
+ * autotuner may pick one per context (the choice is applied to the next
+ * captured graph).  A new context starts with a variant chosen from its
+ * agent count. */
 int cd_variant_count(int *count);
-int cd_variant_shape(int variant, int *threads_per_block, int *staged_per_thread);
+int cd_variant_shape(int variant, int *threads_per_block, int *staged_per_thread,
+                     int *lanes_per_agent);
 int cd_set_variant(cd_ctx *ctx, int variant);
 
 /* Enqueue `steps` CUDA-graph launches of a step with `nodes` on the context

@@ -26,8 +26,10 @@ def oracle_grid(O, scen):
     return O.make_grid(*scen.grid)
 
 
-def device_step(scen, nodes, noise=None):
+def device_step(scen, nodes, noise=None, variant=None):
     b, agents, _ = batch_from_scenarios([scen])
+    if variant is not None:
+        b.set_variant(variant)
     if noise is not None:
         b.set_noise(*noise)
     dt = b.step(nodes, want_dt=True)
@@ -122,6 +124,20 @@ def test_full_step(oracle, native, name):
         for f in ('torque_prev', 'angular_velocity', 'orientation'):
             assert_vec_close(got[f], ref[f], RTOL, ATOL, f)
         assert_vec_close(got['position_ls'], ref['position_ls'], RTOL, ATOL, 'position_ls')
+
+
+@pytest.mark.parametrize('name', sorted(SCENARIOS))
+@pytest.mark.parametrize('variant', range(9))
+def test_full_step_every_variant(oracle, native, name, variant):
+    """Each force-kernel launch variant (one lane per agent, or 4 to 32 lanes
+    sharing an agent) reproduces the oracle's step bit for bit."""
+    assert len(N.variants()) == 9
+    scen = SCENARIOS[name]()
+    noise = S.draw_noise(scen.agents, np.random.default_rng(12))
+    got, dt_g = device_step(scen, N.NODE_ALL, noise, variant=variant)
+    exact, dt_e = oracle_step(oracle, scen, N.NODE_ALL, noise, exact=True)
+    assert dt_g == dt_e
+    assert_identical(got, exact, 'variant %d' % variant)
 
 
 @pytest.mark.parametrize('name', sorted(SCENARIOS))
