@@ -37,7 +37,8 @@ SYMBOLS = (
     'cd_synchronize', 'cd_get_time', 'cd_get_cell_list', 'cd_pair_counts',
     'cd_sizes', 'cd_set_timing', 'cd_kernel_time', 'cd_kernels_per_step',
     'cd_measure_fp64_peak', 'cd_agent_agent_noalloc', 'cd_variant_count',
-    'cd_variant_shape', 'cd_set_variant', 'cd_launch', 'cd_rollout_loss',
+    'cd_variant_shape', 'cd_set_variant', 'cd_set_near_list_capacity', 'cd_launch',
+    'cd_rollout_loss',
 )
 
 #: Limits and column order of cd_agent_agent_noalloc.
@@ -101,10 +102,9 @@ def load(path=None):
         'cd_kernels_per_step': (ctypes.c_int, [P, ctypes.c_int, pi64]),
         'cd_measure_fp64_peak': (ctypes.c_int, [pd]),
         'cd_variant_count': (ctypes.c_int, [ctypes.POINTER(ctypes.c_int)]),
-        'cd_variant_shape': (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int),
-                                            ctypes.POINTER(ctypes.c_int),
-                                            ctypes.POINTER(ctypes.c_int)]),
+        'cd_variant_shape': (ctypes.c_int, [ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 4),
         'cd_set_variant': (ctypes.c_int, [P, ctypes.c_int]),
+        'cd_set_near_list_capacity': (ctypes.c_int, [P, i64]),
         'cd_launch': (ctypes.c_int, [P, ctypes.c_int, i64]),
         'cd_rollout_loss': (ctypes.c_int, [P, i64, P, i64, pd, pd, pd, pd]),
         'cd_agent_agent_noalloc': (ctypes.c_int, [ctypes.c_int, i64, P, P, P, P, ctypes.c_double,
@@ -147,16 +147,16 @@ def dptr(a):
 
 
 def variants():
-    """[(threads_per_block, staged_per_thread, lanes_per_agent)] of the
-    force-kernel variants."""
+    """[(threads_per_block, staged_per_thread, lanes_per_agent, pair_pipeline)]
+    of the force-kernel variants."""
     L = load()
     n = ctypes.c_int()
     check(L.cd_variant_count(ctypes.byref(n)))
     out = []
     for v in range(n.value):
-        t, c, g = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-        check(L.cd_variant_shape(v, ctypes.byref(t), ctypes.byref(c), ctypes.byref(g)))
-        out.append((t.value, c.value, g.value))
+        f = [ctypes.c_int() for _ in range(4)]
+        check(L.cd_variant_shape(v, *[ctypes.byref(x) for x in f]))
+        out.append(tuple(x.value for x in f))
     return out
 
 

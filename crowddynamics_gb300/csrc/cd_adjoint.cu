@@ -54,7 +54,7 @@ __device__ __forceinline__ Circ load_circ(const double2 *__restrict__ st, int sl
 
 __device__ __forceinline__ bool pair_far(float4 me, float4 o) {
     float dx = me.x - o.x, dy = me.y - o.y;
-    float lim = (float)SIGTH_SOC + me.z + o.z + CULL_MARGIN;
+    float lim = (me.z + o.z) + ((float)SIGTH_SOC + CULL_MARGIN);
     return dx * dx + dy * dy > lim * lim;
 }
 

@@ -47,6 +47,14 @@ struct cd_ctx {
     double *v0max = nullptr, *dt = nullptr, *time_tot = nullptr;
     int *err = nullptr, *work = nullptr;
     int *diag = nullptr;
+    // near lists of the compute-once pair pipeline (entries allocated on use)
+    int *nl_cnt = nullptr, *nl_off = nullptr, *nl_fwd = nullptr, *nl_scan = nullptr;
+    int *nl_idx = nullptr;
+    double *nl_res = nullptr;
+    int *fw_cnt = nullptr, *fw_off = nullptr, *fw_scan = nullptr;
+    int2 *fw_pairs = nullptr;
+    int64_t nl_cap = 0;
+    bool nl_fixed = false;              // capacity set by cd_set_near_list_capacity
 
     char *aos = nullptr;
     int64_t aos_bytes = 0, itemsize = 0;
@@ -116,6 +124,17 @@ StepArgs args_of(cd_ctx *c, int nodes) {
     a.time_tot = c->time_tot;
     a.err = c->err;
     a.work = c->work;
+    a.nl_cnt = c->nl_cnt;
+    a.nl_off = c->nl_off;
+    a.nl_fwd = c->nl_fwd;
+    a.nl_idx = c->nl_idx;
+    a.nl_res = c->nl_res;
+    a.nl_cap = (int)c->nl_cap;
+    a.nl_scan = c->nl_scan;
+    a.fw_cnt = c->fw_cnt;
+    a.fw_off = c->fw_off;
+    a.fw_pairs = c->fw_pairs;
+    a.fw_scan = c->fw_scan;
     return a;
 }
 
@@ -134,7 +153,9 @@ void release(cd_ctx *c) {
                     c->perm_unsorted, c->perm, c->scan_scratch, c->stage, c->cull, c->stage_f,
                     c->walls_raw, c->walls, c->walls_f, c->wall_start, c->wall_idx,
                     c->noise_f, c->noise_m, c->vmax, c->v0max, c->dt, c->time_tot,
-                    c->err, c->work, c->diag, c->aos};
+                    c->err, c->work, c->diag, c->aos, c->nl_cnt, c->nl_off, c->nl_fwd,
+                    c->nl_scan, c->nl_idx, c->nl_res, c->fw_cnt, c->fw_off, c->fw_scan,
+                    c->fw_pairs};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -246,19 +267,76 @@ int64_t kernels_per_step(const cd_ctx *c, int nodes) {
     int64_t k = 5;                                      // prepare scatter rank gather forces
     k += (nodes & CD_NODE_INTEGRATE) ? 1 : 0;           // dt
     k += cdk::scan_scratch_ints((int)c->ncells) > 1 ? 3 : 1;
+    if (cdk::variant_pairs(c->variant) && (nodes & CD_NODE_AGENT_AGENT) && c->nl_cnt)
+        k += 4 + 2 * (cdk::scan_scratch_ints((int)c->n) > 1 ? 3 : 1);   // count fill pairs fallback + 2 scans
     return k;
+}
+
+// Entries of the near lists: `need` plus a quarter (density changes between
+// steps), reallocated when a step needed more than the current capacity.
+int alloc_near_lists(cd_ctx *c, int64_t cap) {
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    if (c->nl_idx) cudaFree(c->nl_idx);
+    if (c->nl_res) cudaFree(c->nl_res);
+    if (c->fw_pairs) cudaFree(c->fw_pairs);
+    c->nl_idx = nullptr;
+    c->nl_res = nullptr;
+    c->fw_pairs = nullptr;
+    c->nl_cap = 0;
+    const int64_t res_d = c->body == CD_BODY_CIRCULAR ? cdk::ADJ_RES_D : cdk::RES_D;
+    if (cap > 0) {
+        if (int rc = dalloc(c, &c->nl_idx, cap)) return rc;
+        if (int rc = dalloc(c, &c->nl_res, cap * res_d)) return rc;
+        if (int rc = dalloc(c, &c->fw_pairs, cap)) return rc;
+    }
+    c->nl_cap = cap;
+    if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; c->graph_nodes = -1; }
+    return CD_OK;
+}
+
+int grow_near_lists(cd_ctx *c, int64_t need) {
+    if (c->nl_fixed) return CD_OK;
+    int64_t cap = need + need / 4 + 1024;
+    if (cap > (int64_t)INT32_MAX / 8) cap = (int64_t)INT32_MAX / 8;
+    if (cap <= c->nl_cap) return CD_OK;
+    return alloc_near_lists(c, cap);
+}
+
+// First use of the pair pipeline: count the near lists of the current state
+// and allocate their entries.
+int ensure_near_lists(cd_ctx *c, int nodes) {
+    if (!cdk::variant_pairs(c->variant) || !(nodes & CD_NODE_AGENT_AGENT) || c->n == 0 ||
+        c->nl_cap > 0 || c->nl_fixed)
+        return CD_OK;
+    StepArgs a = args_of(c, CD_NODE_AGENT_AGENT);
+    enqueue_cells(c, a);
+    cdk::launch_near_count(a, c->stream, c->variant);
+    int need = 0;
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(&need, c->nl_off + c->n, sizeof(int), cudaMemcpyDeviceToHost,
+                                    c->stream));
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    return grow_near_lists(c, need);
 }
 
 int check_device_error(cd_ctx *c) {
     CUDA_OR_FAIL(c, cudaGetLastError());
-    int h = 0;
+    int h = 0, need = 0;
+    const bool pairs = cdk::variant_pairs(c->variant) && c->nl_cap > 0 && c->n > 0;
     CUDA_OR_FAIL(c, cudaMemcpyAsync(&h, c->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    if (pairs)
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(&need, c->nl_off + c->n, sizeof(int),
+                                        cudaMemcpyDeviceToHost, c->stream));
     CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    // the last step ran the lane-group fallback when its near lists did not fit
+    if (pairs && need > c->nl_cap)
+        if (int rc = grow_near_lists(c, need)) return rc;
     if (h) {
         cudaMemsetAsync(c->err, 0, sizeof(int), c->stream);
         cudaStreamSynchronize(c->stream);
         if (h & cdk::ERR_NOT_FINITE)
             return fail(c, CD_ERR_NOT_FINITE, "an agent position is not finite");
+        if (h & cdk::ERR_NEAR_LIST)
+            return fail(c, CD_ERR_CUDA, "internal error: a near list lacks a pair partner");
         return fail(c, CD_ERR_INVALID_VALUE, "device reported error bits " + std::to_string(h));
     }
     return CD_OK;
@@ -272,7 +350,7 @@ int prepare_step(cd_ctx *c, int nodes) {
             return fail(c, CD_ERR_INVALID_VALUE, "walls declared but cd_set_walls not called");
         if (int rc = bin_walls(c)) return rc;
     }
-    return CD_OK;
+    return ensure_near_lists(c, nodes);
 }
 
 bool aligned_field(int64_t off, int64_t itemsize, int width) {
@@ -403,6 +481,13 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->err, 1));
     step(dalloc(c, &c->work, 1));
     step(dalloc(c, &c->diag, (int64_t)CD_COUNT_COLS * n));
+    step(dalloc(c, &c->nl_cnt, n + 1));
+    step(dalloc(c, &c->nl_off, n + 1));
+    step(dalloc(c, &c->nl_fwd, n));
+    step(dalloc(c, &c->nl_scan, cdk::scan_scratch_ints((int)npad)));
+    step(dalloc(c, &c->fw_cnt, n + 1));
+    step(dalloc(c, &c->fw_off, n + 1));
+    step(dalloc(c, &c->fw_scan, cdk::scan_scratch_ints((int)npad)));
     if (rc == CD_OK) {
         cudaMemcpy(c->scen_of, c->scen_of_host.data(), sizeof(int) * npad, cudaMemcpyHostToDevice);
         cudaMemcpy(c->scen, c->scen_dev.data(), sizeof(ScenDev) * n_scenarios, cudaMemcpyHostToDevice);
@@ -713,13 +798,26 @@ int cd_variant_count(int *count) {
     return CD_OK;
 }
 
-int cd_variant_shape(int variant, int *threads, int *staged, int *lanes) {
+int cd_variant_shape(int variant, int *threads, int *staged, int *lanes, int *pairs) {
     if (variant < 0 || variant >= cdk::N_VARIANTS)
         return fail(nullptr, CD_ERR_INVALID_VALUE, "unknown variant");
     if (threads) *threads = cdk::variant_threads(variant);
     if (staged) *staged = cdk::variant_staged(variant);
     if (lanes) *lanes = cdk::variant_lanes(variant);
+    if (pairs) *pairs = cdk::variant_pairs(variant) ? 1 : 0;
     return CD_OK;
+}
+
+int cd_set_near_list_capacity(cd_ctx *c, int64_t entries) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (entries < 0) {                  // grow from the current capacity when a step needs more
+        c->nl_fixed = false;
+        return CD_OK;
+    }
+    if (entries > (int64_t)INT32_MAX / 8)
+        return fail(c, CD_ERR_CAPACITY, "near-list capacity above 2^28 entries");
+    c->nl_fixed = true;
+    return alloc_near_lists(c, entries);
 }
 
 int cd_set_variant(cd_ctx *c, int variant) {
@@ -1062,7 +1160,7 @@ extern "C" int cd_agent_agent_noalloc(int body_type, int64_t n, const double *co
     cdk::launch_scan(a.count, a.start, ncells, scan, st);
     cdk::launch_scatter(a, st);
     cdk::launch_gather(a, st);
-    cdk::launch_forces(a, st, cdk::default_variant(n));
+    cdk::launch_forces(a, st, cdk::default_group_variant(n));
     CUDA_OR_FAIL(nullptr, cudaGetLastError());
     int h = 0;
     CUDA_OR_FAIL(nullptr, cudaMemcpyAsync(&h, a.err, sizeof(int), cudaMemcpyDeviceToHost, st));

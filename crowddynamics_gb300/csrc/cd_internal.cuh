@@ -63,7 +63,26 @@ struct StepArgs {
     double *dt, *time_tot;       // per scenario
     int *err;
     int *work;                   // force-kernel work counter (zeroed per launch)
+    // near lists (compute-once pair pipeline): per cell-sorted slot, the
+    // slots of its near candidates in ascending order (= visiting order)
+    int *nl_cnt;                 // n + 1 counts (scan input)
+    int *nl_off;                 // n + 1 offsets; nl_off[n] = entries needed
+    int *nl_fwd;                 // per slot: first entry with a later slot
+    int *nl_idx;                 // nl_cap entries
+    double *nl_res;              // per entry: RES_D doubles of pair results
+    int nl_cap;
+    int *nl_scan;                // scan scratch for n counts
+    int *fw_cnt, *fw_off;        // per slot: entries with a later slot (n + 1 each)
+    int2 *fw_pairs;              // flat list of (slot, entry) for those entries
+    int *fw_scan;                // scan scratch
 };
+
+// Pair-result record of one near-list entry: (fx, fy, torque, interacts);
+// the adjoint's records (Circular contexts) hold ADJ_RES_D doubles.
+constexpr int RES_D = 4;
+constexpr int ADJ_RES_D = 6;
+// Device error bit: a pair partner's near list lacked the pair.
+constexpr int ERR_NEAR_LIST = 2;
 
 // Reverse-step arguments (cd_adjoint.cu); n x 2 arrays are interleaved,
 // state snapshots are columns.
@@ -101,12 +120,16 @@ int scan_scratch_ints(int n);
 void launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s);
 void launch_scatter(const StepArgs &a, cudaStream_t s);
 void launch_gather(const StepArgs &a, cudaStream_t s);
-constexpr int N_VARIANTS = 9;       // launch variants of the force kernel
+constexpr int N_VARIANTS = 12;      // launch variants of the force kernel
+bool variant_pairs(int variant);
 int variant_lanes(int variant);
 int default_variant(long long n_agents);
+int default_group_variant(long long n_agents);
 int variant_threads(int variant);
 int variant_staged(int variant);
 void launch_forces(const StepArgs &a, cudaStream_t s, int variant);
+// Near-list counts and their scan (nl_off) for the state staged in `a`.
+void launch_near_count(const StepArgs &a, cudaStream_t s, int variant);
 void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s);
 void launch_v0max(const StepArgs &a, double *v0max_out, cudaStream_t s);
 void launch_wall_prep(const double *raw, double *walls, float4 *walls_f, int nw,

@@ -430,9 +430,11 @@ __global__ void k_gather(StepArgs a) {
 }
 
 // Float32 conservative pre-check: true if the pair certainly has h >= 3.
+// Symmetric in its arguments (the two extents are added first), so both
+// agents of a pair agree on it.
 __device__ __forceinline__ bool pair_far(float4 me, float4 o) {
     float dx = me.x - o.x, dy = me.y - o.y;
-    float lim = (float)SIGTH_SOC + me.z + o.z + CULL_MARGIN;
+    float lim = (me.z + o.z) + ((float)SIGTH_SOC + CULL_MARGIN);
     return dx * dx + dy * dy > lim * lim;       // false for NaN
 }
 
@@ -551,6 +553,56 @@ __device__ __forceinline__ void pair_circular_me(const Circ &A, const Circ &B, d
         fx += Fx;
         fy += Fy;
     }
+}
+
+// Both forces of a Circular pair (interactions.py:51-70) with P = A the
+// first agent of the pair (the lower cell-sorted slot) and Q = B: each side
+// comes out exactly as pair_circular_eval computes it from that side (Q's
+// relative position, velocity, tau gradient and normal are exact negations
+// of P's), sharing the distance, the time-to-collision and its gradient.
+__device__ __forceinline__ bool pair_circular_both(const Circ &A, const Circ &B, double &FPx,
+                                                   double &FPy, double &FQx, double &FQy) {
+    FPx = 0.0; FPy = 0.0; FQx = 0.0; FQy = 0.0;
+    double xx = A.x - B.x, xy = A.y - B.y;
+    double d = cdm_hypot(xx, xy);
+    double r_tot = A.r + B.r;
+    double h = d - r_tot;
+    if (!(h < SIGTH_SOC)) return false;
+    double vrx = A.vx - B.vx, vry = A.vy - B.vy;
+    double a = vrx * vrx + vry * vry;
+    double b = -(xx * vrx + xy * vry);
+    double c = (xx * xx + xy * xy) - r_tot * r_tot;
+    double disc = b * b - a * c;
+    if (disc > 0 && a != 0) {
+        double dd = sqrt(disc);
+        double tau = (b - dd) / a;
+        if (!(tau <= 0 || tau > TAU_MAX)) {
+            double gx = (vrx - (vrx * b + xx * a) / dd) / a;
+            double gy = (vry - (vry * b + xy * a) / dd) / a;
+            double cmp = (-A.m) * A.k, cmq = (-B.m) * B.k;
+            double two_t = 2.0 / tau, tt = tau * tau;       // shared terms of magnitude()
+            double magp = (two_t + 1.0 / A.tau0) * cdm_exp(-tau / A.tau0) / tt;
+            double magq = (two_t + 1.0 / B.tau0) * cdm_exp(-tau / B.tau0) / tt;
+            FPx = (cmp * gx) * magp;
+            FPy = (cmp * gy) * magp;
+            truncate2(FPx, FPy, F_SOC_MAX);
+            FQx = (cmq * (-gx)) * magq;
+            FQy = (cmq * (-gy)) * magq;
+            truncate2(FQx, FQy, F_SOC_MAX);
+        }
+    }
+    if (h < 0) {
+        double nx = 0.0, ny = 0.0, mx = 0.0, my = 0.0;
+        if (d != 0.0) { nx = xx / d; ny = xy / d; mx = -nx; my = -ny; }   // (-x)/d == -(x/d)
+        double cx, cy;
+        force_contact(h, nx, ny, vrx, vry, A.mu, A.kappa, A.damp, cx, cy);
+        FPx = FPx + cx;
+        FPy = FPy + cy;
+        force_contact(h, mx, my, -vrx, -vry, B.mu, B.kappa, B.damp, cx, cy);
+        FQx = FQx + cx;
+        FQy = FQy + cy;
+    }
+    return true;
 }
 
 // Per-warp queue for the square root and division of the defined sub-circle
@@ -767,6 +819,202 @@ __device__ __forceinline__ void tc_pair_step(const TC &A, const float4 meC, cons
         fy += Fy;
         tq += Tq;
     }
+}
+
+// Both sides of a ThreeCircle pair (interactions.py:73-101,
+// power_law.py:264-363) with P = A first and Q = the pair partner: the
+// distance search, the time-to-collision selection and the tau gradient are
+// computed once; each side's force, contact and torque come out exactly as
+// tc_pair_eval computes them from that side.  Warp collective like
+// tc_pair_eval (all 32 lanes call it).
+__device__ __forceinline__ bool tc_pair_both(const TC &A, const float4 meC, const float4 meF0,
+                                             const float4 meF1, const StepArgs &a, bool act,
+                                             int t, WarpQueue &q, int lane, double &FPx,
+                                             double &FPy, double &TP, double &FQx, double &FQy,
+                                             double &TQ) {
+    constexpr unsigned wmask = 0xffffffffu;
+    constexpr int nlanes = 32;
+    TC B = A;
+    float4 oC = meC, oF0 = meF0, oF1 = meF1;
+    if (act) {
+        B = load_tc(a.stage, t);
+        oC = __ldg(&a.cull[t]);
+        oF0 = __ldg(&a.stage_f[2 * t]);
+        oF1 = __ldg(&a.stage_f[2 * t + 1]);
+    }
+    // -- distance_three_circles: float32 pre-selection (P's frame) --
+    const float dxt = (meC.x - oC.x) + (meF0.x - oF0.x);
+    const float dyt = (meC.y - oC.y) + (meF0.y - oF0.y);
+    const float mox[3] = {0.f, meF1.x, meF1.z}, moy[3] = {0.f, meF1.y, meF1.w};
+    const float oox[3] = {0.f, oF1.x, oF1.z}, ooy[3] = {0.f, oF1.y, oF1.w};
+    const float mr[3] = {meF0.z, meF0.w, meF0.w}, orr[3] = {oF0.z, oF0.w, oF0.w};
+    float hf[9];
+    float hfmin = INFINITY;
+    bool anynan = false;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            float dx = (dxt + mox[i]) - oox[j], dy = (dyt + moy[i]) - ooy[j];
+            float h = sqrtf(dx * dx + dy * dy) - (mr[i] + orr[j]);
+            hf[3 * i + j] = h;
+            anynan |= (h != h);
+            hfmin = fminf(hfmin, h);
+        }
+    const float scale = fabsf(dxt) + fabsf(dyt) + fabsf(meF1.x) + fabsf(meF1.y) + fabsf(meF1.z) +
+                        fabsf(meF1.w) + fabsf(oF1.x) + fabsf(oF1.y) + fabsf(oF1.z) + fabsf(oF1.w) +
+                        mr[0] + mr[1] + orr[0] + orr[1];
+    const float margin = PRESEL_MARGIN + 1e-6f * scale;
+    unsigned seq = 0;
+#pragma unroll
+    for (int k = 0; k < 9; ++k)
+        if (hf[k] <= hfmin + margin) seq |= 1u << k;
+    if (anynan) seq = 0x1ffu;
+    if (!act) seq = 1u;
+    // exact float64 minimum over the candidates, first in visiting order wins
+    double h_min = __longlong_as_double(0x7ff8000000000000LL);
+    double sdx = 0.0, sdy = 0.0, sd = 0.0;
+    int pp_min = 0, qp_min = 0;                  // P's and Q's part at the minimum
+    {
+        int k = __ffs(seq) - 1;
+        unsigned rest = seq & (seq - 1);
+        int mi = k / 3, ti = k % 3;
+        double dx = sel3(A.x, mi) - sel3(B.x, ti), dy = sel3(A.y, mi) - sel3(B.y, ti);
+        double d = cdm_hypot(dx, dy);
+        h_min = d - (part_r(A, mi) + part_r(B, ti));
+        sdx = dx; sdy = dy; sd = d; pp_min = mi; qp_min = ti;
+        while (rest) {
+            k = __ffs(rest) - 1;
+            rest &= rest - 1;
+            mi = k / 3; ti = k % 3;
+            dx = sel3(A.x, mi) - sel3(B.x, ti);
+            dy = sel3(A.y, mi) - sel3(B.y, ti);
+            d = cdm_hypot(dx, dy);
+            double h = d - (part_r(A, mi) + part_r(B, ti));
+            if (h < h_min || isnan(h_min)) {
+                h_min = h; sdx = dx; sdy = dy; sd = d; pp_min = mi; qp_min = ti;
+            }
+        }
+    }
+    const bool inter = act && (h_min < SIGTH_SOC);
+    double npx = 0.0, npy = 0.0, nqx = 0.0, nqy = 0.0;
+    if (inter && sd != 0.0) {
+        npx = sdx / sd; npy = sdy / sd;
+        nqx = -npx; nqy = -npy;                  // (-x)/d == -(x/d), signed zeros included
+    }
+    // moment arms: (X_P[part] + r_side * n_side) - x_side_torso, X_P the first
+    // agent's parts indexed by the side's own part
+    double rpx, rpy, rqx, rqy;
+    {
+        double r = part_r(A, pp_min);
+        rpx = (sel3(A.x, pp_min) + r * npx) - A.x[0];
+        rpy = (sel3(A.y, pp_min) + r * npy) - A.y[0];
+        r = part_r(B, qp_min);
+        rqx = (sel3(A.x, qp_min) + r * nqx) - B.x[0];
+        rqy = (sel3(A.y, qp_min) + r * nqy) - B.y[0];
+    }
+    // -- force_social_three_circle (shared time-to-collision) --
+    const double vrx = A.vx - B.vx, vry = A.vy - B.vy;
+    const double av = vrx * vrx + vry * vry;
+    const bool soc = inter && av != 0;
+    unsigned defmask = 0;
+    int cnt = 0;
+    double *qb = q.b + lane * 9;
+    double *qd = q.disc + lane * 9;
+    if (soc) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            int mi = k / 3, ti = k % 3;
+            double xr = sel3(A.x, mi) - sel3(B.x, ti), yr = sel3(A.y, mi) - sel3(B.y, ti);
+            double r_tot = part_r(A, mi) + part_r(B, ti);
+            double b = -(xr * vrx + yr * vry);
+            double c = (xr * xr + yr * yr) - r_tot * r_tot;
+            double disc = b * b - av * c;
+            if (disc > 0) {
+                qb[cnt] = b;
+                qd[cnt] = disc;
+                ++cnt;
+                defmask |= 1u << k;
+            }
+        }
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int v = __shfl_up_sync(wmask, incl, o);
+        if (lane >= o) incl += v;
+    }
+    q.off[lane] = incl - cnt;
+    q.a[lane] = av;
+    const int total = __shfl_sync(wmask, incl, nlanes - 1);
+    if (lane == nlanes - 1) q.off[nlanes] = incl;
+    __syncwarp(wmask);
+    for (int base = 0; base < total; base += nlanes) {
+        int it = base + lane;
+        if (it < total) {
+            int lo = 0, hi = nlanes - 1;
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (q.off[mid] <= it) lo = mid; else hi = mid - 1;
+            }
+            int slot = lo * 9 + (it - q.off[lo]);
+            double d = sqrt(q.disc[slot]);
+            q.tau[slot] = (q.b[slot] - d) / q.a[lo];
+            q.disc[slot] = d;
+        }
+    }
+    __syncwarp(wmask);
+    double tau = __longlong_as_double(0x7ff8000000000000LL);
+    double b_min = 0.0, d_min = 0.0;
+    int k_sel = 0;
+    {
+        int jj = 0;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            if (defmask & (1u << k)) {
+                double tau_new = q.tau[lane * 9 + jj];
+                double dk = qd[jj], bk = qb[jj];
+                ++jj;
+                if (isnan(tau) || (0 < tau_new && tau_new < tau)) {
+                    k_sel = k; tau = tau_new; b_min = bk; d_min = dk;
+                }
+            }
+        }
+    }
+    __syncwarp(wmask);
+    FPx = 0.0; FPy = 0.0; FQx = 0.0; FQy = 0.0;
+    if (soc && !(isnan(tau) || tau <= 0)) {
+        const int mi = k_sel / 3, ti = k_sel % 3;
+        double o1x, o1y, o2x, o2y;
+        r_off_part(A, mi, o1x, o1y);
+        r_off_part(B, ti, o2x, o2y);
+        double ox = o1x - o2x, oy = o1y - o2y;
+        double xr = A.x[0] - B.x[0], yr = A.y[0] - B.y[0];
+        double gx = (vrx - (av * (xr + 2 * ox) + b_min * vrx) / d_min) / av;
+        double gy = (vry - (av * (yr + 2 * oy) + b_min * vry) / d_min) / av;
+        double cmp = (-A.m) * A.k, cmq = (-B.m) * B.k;
+        double two_t = 2.0 / tau, tt = tau * tau;            // shared terms of magnitude()
+        double magp = (two_t + 1.0 / A.tau0) * cdm_exp(-tau / A.tau0) / tt;
+        double magq = (two_t + 1.0 / B.tau0) * cdm_exp(-tau / B.tau0) / tt;
+        FPx = (cmp * gx) * magp;
+        FPy = (cmp * gy) * magp;
+        truncate2(FPx, FPy, F_SOC_MAX);
+        FQx = (cmq * (-gx)) * magq;             // Q's gradient is -g exactly
+        FQy = (cmq * (-gy)) * magq;
+        truncate2(FQx, FQy, F_SOC_MAX);
+    }
+    if (inter && h_min < 0) {
+        double cx, cy;
+        force_contact(h_min, npx, npy, vrx, vry, A.mu, A.kappa, A.damp, cx, cy);
+        FPx = FPx + cx;
+        FPy = FPy + cy;
+        force_contact(h_min, nqx, nqy, -vrx, -vry, B.mu, B.kappa, B.damp, cx, cy);
+        FQx = FQx + cx;
+        FQy = FQy + cy;
+    }
+    TP = rpx * FPy - rpy * FPx;
+    TQ = rqx * FQy - rqy * FQx;
+    return inter;
 }
 
 // Resumable candidate enumeration into the thread's list (visiting order:
@@ -1144,6 +1392,233 @@ __global__ void __launch_bounds__(NTG) k_forces_group(StepArgs a) {
     }
 }
 
+// ---- compute-once pair pipeline --------------------------------------
+//
+// The reference visits every unordered pair once and adds both agents'
+// forces (interactions.py:147-166); the per-thread and lane-group kernels
+// instead evaluate each pair from both sides.  This pipeline evaluates each
+// pair once, in the reference's orientation (the lower cell-sorted slot is
+// the pair's first agent: the forward half-stencil reaches exactly the cells
+// with a larger flat index), and sums each agent's pair results in its
+// visiting order afterwards:
+//   k_nl_count / scan / k_nl_fill: every agent's near candidates (float32
+//     cull, symmetric) in ascending slot order, which is its visiting order;
+//   k_pairs: for every entry with a later slot, both sides of the pair, the
+//     first side into the entry, the second into the partner's entry for
+//     this agent (binary search in the partner's earlier-slot part);
+//   k_forces_gather: per agent, the entries' forces added in list order,
+//     then walls and integration.
+// When the entries exceed the allocated capacity the pair kernels do
+// nothing and k_forces_gather runs the lane-group path instead; nl_off[n]
+// tells the host how much to allocate.
+
+// Agent s's candidate runs, one per dx in -1, 0, 1 (empty where off the grid).
+__device__ __forceinline__ void candidate_runs(const StepArgs &a, const ScenDev &sc,
+                                               int my_cell, int rb[3], int re[3]) {
+    const int local = my_cell - sc.cell_base;
+    const int ix = local / sc.ny, iy = local - ix * sc.ny;
+    const int jy0 = iy > 0 ? iy - 1 : 0, jy1 = iy + 1 < sc.ny ? iy + 1 : sc.ny - 1;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        rb[d] = 0;
+        re[d] = 0;
+        const int jx = ix + d - 1;
+        if (jx < 0 || jx >= sc.nx) continue;
+        const int c0 = sc.cell_base + jx * sc.ny;
+        rb[d] = __ldg(&a.start[c0 + jy0]);
+        re[d] = __ldg(&a.start[c0 + jy1 + 1]);
+    }
+}
+
+template <int L>
+__global__ void __launch_bounds__(NTG) k_nl_count(StepArgs a) {
+    const int r = threadIdx.x & (L - 1);
+    const int s = (int)(((long long)blockIdx.x * NTG + threadIdx.x) / L);
+    int cnt = 0, fwd = 0;
+    if (s < a.n) {
+        const int i = a.perm[s];
+        const ScenDev sc = a.scen[a.scen_of[i]];
+        const float4 me = a.cull[s];
+        int rb[3], re[3];
+        candidate_runs(a, sc, a.key[i], rb, re);
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+            for (int t = rb[d] + r; t < re[d]; t += L)
+                if (t != s && !pair_far(me, __ldg(&a.cull[t]))) {
+                    ++cnt;
+                    fwd += t > s;
+                }
+    }
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) {
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        fwd += __shfl_xor_sync(0xffffffffu, fwd, o);
+    }
+    if (s < a.n && r == 0) {
+        a.nl_cnt[s] = cnt;
+        a.fw_cnt[s] = fwd;
+    }
+}
+
+template <int L>
+__global__ void __launch_bounds__(NTG) k_nl_fill(StepArgs a) {
+    if (a.nl_off[a.n] > a.nl_cap) return;                 // over capacity: fallback
+    constexpr unsigned GMASK = L == 32 ? 0xffffffffu : ((1u << L) - 1u);
+    const int lane = threadIdx.x & 31;
+    const int r = lane & (L - 1), g0 = lane & ~(L - 1);
+    const unsigned gm = GMASK << g0;
+    const int s = (int)(((long long)blockIdx.x * NTG + threadIdx.x) / L);
+    if (s >= a.n) return;                                 // whole groups leave together
+    const int i = a.perm[s];
+    const ScenDev sc = a.scen[a.scen_of[i]];
+    const float4 me = a.cull[s];
+    int rb[3], re[3];
+    candidate_runs(a, sc, a.key[i], rb, re);
+    // entries with a later slot follow all earlier ones (ascending order)
+    const int fwd0 = a.nl_off[s] + (a.nl_cnt[s] - a.fw_cnt[s]);
+    const int fbase = a.fw_off[s] - fwd0;
+    int pos = a.nl_off[s];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+        for (int base = rb[d]; base < re[d]; base += L) {
+            const int t = base + r;
+            const bool near = t < re[d] && t != s && !pair_far(me, __ldg(&a.cull[t]));
+            const unsigned gb = (__ballot_sync(gm, near) >> g0) & GMASK;
+            if (near) {
+                const int e = pos + __popc(gb & ((1u << r) - 1u));
+                a.nl_idx[e] = t;
+                if (t > s) a.fw_pairs[fbase + e] = make_int2(s, e);
+            }
+            pos += __popc(gb);
+        }
+    if (r == 0) a.nl_fwd[s] = fwd0;
+}
+
+// Entry of `s` in the earlier-slot part of `t`'s near list (s < t), or -1.
+__device__ __forceinline__ int partner_entry(const StepArgs &a, int t, int s) {
+    int lo = __ldg(&a.nl_off[t]), hi = __ldg(&a.nl_fwd[t]);
+    const int end = hi;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&a.nl_idx[mid]) < s) lo = mid + 1;
+        else hi = mid;
+    }
+    return (lo < end && __ldg(&a.nl_idx[lo]) == s) ? lo : -1;
+}
+
+__device__ __forceinline__ void put_res(double *res, int e, double fx, double fy, double tq,
+                                        bool inter) {
+    double4_32a v;
+    v.x = fx; v.y = fy; v.z = tq; v.w = inter ? 1.0 : 0.0;
+    *reinterpret_cast<double4_32a *>(res + (size_t)e * RES_D) = v;
+}
+
+// Every pair of the flat list once: warps claim 32 consecutive pairs at a
+// time (consecutive pairs mostly share their first agent).
+template <int BODY>
+__global__ void __launch_bounds__(NTG) k_pairs(StepArgs a) {
+    constexpr unsigned FULL = 0xffffffffu;
+    if (a.nl_off[a.n] > a.nl_cap) return;
+    extern __shared__ unsigned char smem[];
+    WarpQueue *wq = reinterpret_cast<WarpQueue *>(smem);
+    const int lane = threadIdx.x & 31;
+    const int npairs = a.fw_off[a.n];
+    for (;;) {
+        int chunk = 0;
+        if (lane == 0) chunk = atomicAdd(a.work, 1);
+        chunk = __shfl_sync(FULL, chunk, 0);
+        if (chunk * 32 >= npairs) return;
+        const int k = chunk * 32 + lane;
+        const bool act = k < npairs;
+        int s = 0, e = 0, t = 0;
+        if (act) {
+            const int2 pe = __ldg(&a.fw_pairs[k]);
+            s = pe.x;
+            e = pe.y;
+            t = __ldg(&a.nl_idx[e]);
+        }
+        double fpx = 0.0, fpy = 0.0, tp = 0.0, fqx = 0.0, fqy = 0.0, tq = 0.0;
+        bool inter = false;
+        if (BODY == 0) {
+            if (act)
+                inter = pair_circular_both(load_circ(a.stage, s), load_circ(a.stage, t), fpx, fpy,
+                                           fqx, fqy);
+        } else {
+            TC At;
+            float4 me = make_float4(0.f, 0.f, 0.f, 0.f), meF0 = me, meF1 = me;
+            if (act) {
+                At = load_tc(a.stage, s);
+                me = __ldg(&a.cull[s]);
+                meF0 = __ldg(&a.stage_f[2 * s]);
+                meF1 = __ldg(&a.stage_f[2 * s + 1]);
+            } else {
+                At = load_tc(a.stage, 0);
+            }
+            inter = tc_pair_both(At, me, meF0, meF1, a, act, t, wq[threadIdx.x >> 5], lane, fpx,
+                                 fpy, tp, fqx, fqy, tq);
+        }
+        if (act) {
+            put_res(a.nl_res, e, fpx, fpy, tp, inter);
+            const int eq = partner_entry(a, t, s);
+            if (eq >= 0) put_res(a.nl_res, eq, fqx, fqy, tq, inter);
+            else atomicOr(a.err, ERR_NEAR_LIST);
+        }
+    }
+}
+
+// Agent in slot s from its near-list results: one lane per agent, entries
+// added in list order (32-byte records, one sector each), then walls and
+// integration at full lane occupancy.
+template <int BODY>
+__device__ __forceinline__ void gather_agent(const StepArgs &a, const int s) {
+    const int i = a.perm[s];
+    const int sid = a.scen_of[i];
+    const ScenDev sc = a.scen[sid];
+    const float4 me = a.cull[s];
+    const int my_cell = a.key[i];
+    double fx, fy, tq, phi0;
+    agent_prologue<BODY>(a, i, fx, fy, tq, phi0);
+    if (a.nodes & N_AGENT) {
+        const int o1 = a.nl_off[s + 1];
+        for (int e = a.nl_off[s]; e < o1; ++e) {
+            const double4_32a v = *reinterpret_cast<const double4_32a *>(a.nl_res + (size_t)e * RES_D);
+            if (v.w != 0.0) {
+                fx = fx + v.x;
+                fy = fy + v.y;
+                if (BODY == 1) tq = tq + v.z;
+            }
+        }
+    }
+    agent_epilogue<BODY>(a, s, i, sid, sc, me, my_cell, fx, fy, tq, phi0);
+}
+
+template <int BODY>
+__global__ void __launch_bounds__(NTG) k_forces_gather(StepArgs a) {
+    if ((a.nodes & N_AGENT) && a.nl_off[a.n] > a.nl_cap) return;   // k_forces_fallback's step
+    const int s = blockIdx.x * NTG + threadIdx.x;
+    if (s < a.n) gather_agent<BODY>(a, s);
+}
+
+// The lane-group kernel, for a step whose near lists exceeded the capacity.
+template <int BODY, int L>
+__global__ void __launch_bounds__(NTG) k_forces_fallback(StepArgs a) {
+    if (!((a.nodes & N_AGENT) && a.nl_off[a.n] > a.nl_cap)) return;
+    extern __shared__ unsigned char smem[];
+    int *gq_all = reinterpret_cast<int *>(smem);
+    WarpQueue *wq = reinterpret_cast<WarpQueue *>(smem + sizeof(int) * 2 * NTG);
+    int *gq = gq_all + 2 * (threadIdx.x & ~(L - 1));
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int chunk = 0;
+        if (lane == 0) chunk = atomicAdd(a.work, 1);
+        chunk = __shfl_sync(0xffffffffu, chunk, 0);
+        const int s0 = chunk * (32 / L);
+        if (s0 >= a.n) return;
+        force_agent_group<BODY, L>(a, s0 + lane / L, gq, wq);
+        __syncwarp();
+    }
+}
+
 // Skin distance of a pair (same value whichever side is first).
 __device__ __forceinline__ double pair_h(const StepArgs &a, int s, int t) {
     if (a.body == 0) {
@@ -1336,36 +1811,61 @@ void launch_gather(const StepArgs &a, cudaStream_t s) {
 // per thread).
 // Force-kernel launch variants: the per-thread kernel (k_forces, lanes = 1)
 // with NT threads per block and CAP candidates staged per thread per pass,
-// and the lane-group kernel (k_forces_group) with L lanes per agent.
-struct Variant { int nt, cap, lanes; };
-constexpr Variant kVariants[N_VARIANTS] = {{128, 64, 1}, {64, 64, 1}, {128, 32, 1}, {64, 32, 1},
-                                           {256, 32, 1}, {NTG, 0, 4},  {NTG, 0, 8}, {NTG, 0, 16},
-                                           {NTG, 0, 32}};
+// the lane-group kernel (k_forces_group) with L lanes per agent, and the
+// compute-once pair pipeline (pairs = 1: near lists, k_pairs, gather) with
+// L lanes per agent.
+struct Variant { int nt, cap, lanes, pairs; };
+constexpr Variant kVariants[N_VARIANTS] = {
+    {128, 64, 1, 0}, {64, 64, 1, 0}, {128, 32, 1, 0}, {64, 32, 1, 0}, {256, 32, 1, 0},
+    {NTG, 0, 4, 0},  {NTG, 0, 8, 0}, {NTG, 0, 16, 0}, {NTG, 0, 32, 0},
+    {NTG, 0, 4, 1},  {NTG, 0, 8, 1}, {NTG, 0, 16, 1}};
 
 size_t forces_smem_bytes(int body, int variant) {
     const Variant v = kVariants[variant];
+    if (v.pairs) return 0;                                      // k_forces_gather
     size_t b = v.lanes == 1 ? sizeof(int) * (size_t)v.cap * v.nt : sizeof(int) * 2 * (size_t)NTG;
     if (body == 1) b += sizeof(WarpQueue) * (v.nt / 32);
     return b;
 }
 
+size_t pairs_smem_bytes(int body) { return body == 1 ? sizeof(WarpQueue) * (NTG / 32) : 0; }
+
 typedef void (*ForcesFn)(StepArgs);
 constexpr ForcesFn kForces[2][N_VARIANTS] = {
     {k_forces<0, 128, 64>, k_forces<0, 64, 64>, k_forces<0, 128, 32>, k_forces<0, 64, 32>,
      k_forces<0, 256, 32>, k_forces_group<0, 4>, k_forces_group<0, 8>, k_forces_group<0, 16>,
-     k_forces_group<0, 32>},
+     k_forces_group<0, 32>, k_forces_gather<0>, k_forces_gather<0>, k_forces_gather<0>},
     {k_forces<1, 128, 64>, k_forces<1, 64, 64>, k_forces<1, 128, 32>, k_forces<1, 64, 32>,
      k_forces<1, 256, 32>, k_forces_group<1, 4>, k_forces_group<1, 8>, k_forces_group<1, 16>,
-     k_forces_group<1, 32>}};
+     k_forces_group<1, 32>, k_forces_gather<1>, k_forces_gather<1>, k_forces_gather<1>}};
+
+// Near-list and pair kernels of the pair-pipeline variants (by lanes 4, 8, 16).
+constexpr int N_PAIR_L = 3;
+constexpr ForcesFn kNlCount[N_PAIR_L] = {k_nl_count<4>, k_nl_count<8>, k_nl_count<16>};
+constexpr ForcesFn kNlFill[N_PAIR_L] = {k_nl_fill<4>, k_nl_fill<8>, k_nl_fill<16>};
+constexpr ForcesFn kPairs[2] = {k_pairs<0>, k_pairs<1>};
+constexpr ForcesFn kFallback[2][N_PAIR_L] = {
+    {k_forces_fallback<0, 4>, k_forces_fallback<0, 8>, k_forces_fallback<0, 16>},
+    {k_forces_fallback<1, 4>, k_forces_fallback<1, 8>, k_forces_fallback<1, 16>}};
+inline int pair_l_index(int lanes) { return lanes == 4 ? 0 : (lanes == 8 ? 1 : 2); }
+
+bool variant_pairs(int variant) {
+    return variant >= 0 && variant < N_VARIANTS && kVariants[variant].pairs != 0;
+}
 
 // Variant a new context starts with: lanes per agent such that the warps
-// cover the SMs several times over (measured on hallway, room and field
-// workloads of 400 to 100k agents).
+// cover the SMs several times over, and the pair pipeline from 8k agents
+// (measured on hallway, room and field workloads of 400 to 100k agents).
 int default_variant(long long n) {
-    if (n < 1000) return 8;          // 32 lanes per agent
-    if (n < 15000) return 7;         // 16
-    if (n < 60000) return 6;         // 8
-    return 0;                        // one lane per agent, 128 threads, 64 staged
+    if (n < 1000) return 8;          // lane groups, 32 lanes per agent
+    if (n < 8000) return 7;          // lane groups, 16
+    return 10;                       // pair pipeline (8 lanes per agent in the list build)
+}
+
+// The same without the pair pipeline (contexts without near-list memory).
+int default_group_variant(long long n) {
+    const int v = default_variant(n);
+    return kVariants[v].pairs ? v - 4 : v;
 }
 
 int variant_lanes(int variant) {
@@ -1378,8 +1878,9 @@ int variant_staged(int variant) {
     return variant >= 0 && variant < N_VARIANTS ? kVariants[variant].cap : 0;
 }
 
-// Resident blocks of each force kernel variant on each device.
+// Resident blocks of each force kernel variant (and pair kernel) on each device.
 int g_forces_blocks[64][2][N_VARIANTS];
+int g_pairs_blocks[64][2][N_PAIR_L];
 
 int init_kernels() {
     int dev = 0, sms = 0;
@@ -1397,22 +1898,73 @@ int init_kernels() {
             if (e == cudaSuccess && dev >= 0 && dev < 64)
                 g_forces_blocks[dev][body][v] = (nb > 0 ? nb : 1) * sms;
         }
+    for (int body = 0; body < 2 && e == cudaSuccess; ++body)
+        for (int l = 0; l < N_PAIR_L && e == cudaSuccess; ++l) {
+            // the fallback kernel shares the lane-group variant's shared memory
+            e = cudaFuncSetAttribute(kFallback[body][l],
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)forces_smem_bytes(body, 5 + l));
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(kPairs[body],
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)pairs_smem_bytes(body));
+            int nb = 0;
+            if (e == cudaSuccess)
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kPairs[body], NTG,
+                                                                  pairs_smem_bytes(body));
+            if (e == cudaSuccess && dev >= 0 && dev < 64)
+                g_pairs_blocks[dev][body][l] = (nb > 0 ? nb : 1) * sms;
+        }
     return e == cudaSuccess ? 0 : (int)e;
 }
 
 void launch_forces(const StepArgs &a, cudaStream_t s, int variant) {
     if (a.n <= 0) return;
     if (variant < 0 || variant >= N_VARIANTS) variant = 0;
+    // the pair pipeline needs the near-list buffers: otherwise its lane-group twin
+    if (kVariants[variant].pairs && !a.nl_cnt) variant -= 4;
     const Variant v = kVariants[variant];
     int dev = 0;
     cudaGetDevice(&dev);
     const int body = a.body ? 1 : 0;
+    if (v.pairs && (a.nodes & N_AGENT)) {
+        const int l = pair_l_index(v.lanes);
+        const int nb = nblk((long long)a.n * v.lanes, NTG);
+        kNlCount[l]<<<nb, NTG, 0, s>>>(a);
+        launch_scan(a.nl_cnt, a.nl_off, a.n, a.nl_scan, s);
+        launch_scan(a.fw_cnt, a.fw_off, a.n, a.fw_scan, s);
+        kNlFill[l]<<<nb, NTG, 0, s>>>(a);
+        int rp = (dev >= 0 && dev < 64) ? g_pairs_blocks[dev][body][l] : 0;
+        if (rp <= 0) rp = 152;
+        cudaMemsetAsync(a.work, 0, sizeof(int), s);
+        // at most one warp per 32 pairs (about 16 pairs per agent): enough blocks
+        kPairs[body]<<<std::min(nblk((long long)a.n * 16, NTG), rp), NTG, pairs_smem_bytes(body),
+                       s>>>(a);
+    }
     int resident = (dev >= 0 && dev < 64) ? g_forces_blocks[dev][body][variant] : 0;
     if (resident <= 0) resident = 152;
     const long long threads = (long long)a.n * v.lanes;
     int blocks = (int)std::min<long long>((threads + v.nt - 1) / v.nt, resident);
+    if (v.pairs) blocks = nblk(a.n, NTG);                // gather: one lane per agent, full grid
     cudaMemsetAsync(a.work, 0, sizeof(int), s);
     kForces[body][variant]<<<blocks, v.nt, forces_smem_bytes(body, variant), s>>>(a);
+    if (v.pairs && (a.nodes & N_AGENT)) {
+        const int gv = variant - 4;                       // the lane-group twin
+        int rg = (dev >= 0 && dev < 64) ? g_forces_blocks[dev][body][gv] : 0;
+        if (rg <= 0) rg = 152;
+        cudaMemsetAsync(a.work, 0, sizeof(int), s);
+        kFallback[body][pair_l_index(v.lanes)]<<<(int)std::min<long long>(
+                                                    (threads + NTG - 1) / NTG, rg),
+                                                NTG, forces_smem_bytes(body, gv), s>>>(a);
+    }
+}
+
+void launch_near_count(const StepArgs &a, cudaStream_t s, int variant) {
+    if (a.n <= 0 || !variant_pairs(variant)) return;
+    const int lanes = kVariants[variant].lanes;
+    kNlCount[pair_l_index(lanes)]<<<nblk((long long)a.n * lanes, NTG), NTG, 0, s>>>(a);
+    launch_scan(a.nl_cnt, a.nl_off, a.n, a.nl_scan, s);
+    launch_scan(a.fw_cnt, a.fw_off, a.n, a.fw_scan, s);
 }
 
 void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s) {

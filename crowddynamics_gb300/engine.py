@@ -152,6 +152,11 @@ class DeviceBatch:
         self._chk(self._lib.cd_set_variant(self._ctx, int(variant)))
         self.variant = int(variant)
 
+    def set_near_list_capacity(self, entries):
+        """Fix the pair pipeline's near-list capacity (entries; a negative
+        value returns to automatic sizing)."""
+        self._chk(self._lib.cd_set_near_list_capacity(self._ctx, int(entries)))
+
     def rollout_loss(self, steps, target, checkpoint_every=20, grads=True):
         """Run ``steps`` updates, return (loss, grads, forward_ms, adjoint_ms):
         loss = mean over steps and agents of |x(t) - target[t]|^2, grads =

@@ -170,15 +170,24 @@ int cd_kernels_per_step(const cd_ctx *ctx, int nodes, int64_t *kernels);
 
 /* Launch variants of the agent-force kernel: threads per block, candidates
  * staged per thread per pass (lanes_per_agent == 1: one lane per agent) or
- * lanes that share one agent (lanes_per_agent > 1, staged_per_thread 0).
- * Every variant gives bit-identical results; only the speed differs, so an
- * autotuner may pick one per context (the choice is applied to the next
- * captured graph).  A new context starts with a variant chosen from its
- * agent count. */
+ * lanes that share one agent (lanes_per_agent > 1, staged_per_thread 0), and
+ * whether the variant is the compute-once pair pipeline (pair_pipeline 1:
+ * every unordered pair evaluated once into per-agent near lists, then summed
+ * per agent in visiting order; the lists' device memory is allocated on
+ * first use and grown after a step that needed more, that step falling back
+ * to the lane-group kernel).  Every variant gives bit-identical results;
+ * only the speed differs, so an autotuner may pick one per context (the
+ * choice is applied to the next captured graph).  A new context starts with
+ * a variant chosen from its agent count. */
 int cd_variant_count(int *count);
 int cd_variant_shape(int variant, int *threads_per_block, int *staged_per_thread,
-                     int *lanes_per_agent);
+                     int *lanes_per_agent, int *pair_pipeline);
 int cd_set_variant(cd_ctx *ctx, int variant);
+/* Near-list entries of the pair pipeline: `entries` >= 0 fixes the capacity
+ * (no growth; steps that need more run the lane-group kernel instead, with
+ * identical results); a negative value returns to automatic sizing, which
+ * grows the current capacity after a step that needed more. */
+int cd_set_near_list_capacity(cd_ctx *ctx, int64_t entries);
 
 /* Enqueue `steps` CUDA-graph launches of a step with `nodes` on the context
  * stream and return at once (no host synchronisation), so several contexts

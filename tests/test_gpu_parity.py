@@ -127,17 +127,62 @@ def test_full_step(oracle, native, name):
 
 
 @pytest.mark.parametrize('name', sorted(SCENARIOS))
-@pytest.mark.parametrize('variant', range(9))
+@pytest.mark.parametrize('variant', range(12))
 def test_full_step_every_variant(oracle, native, name, variant):
-    """Each force-kernel launch variant (one lane per agent, or 4 to 32 lanes
-    sharing an agent) reproduces the oracle's step bit for bit."""
-    assert len(N.variants()) == 9
+    """Each force-kernel launch variant (one lane per agent, 4 to 32 lanes
+    sharing an agent, or the compute-once pair pipeline) reproduces the
+    oracle's step bit for bit."""
+    assert len(N.variants()) == 12
     scen = SCENARIOS[name]()
     noise = S.draw_noise(scen.agents, np.random.default_rng(12))
     got, dt_g = device_step(scen, N.NODE_ALL, noise, variant=variant)
     exact, dt_e = oracle_step(oracle, scen, N.NODE_ALL, noise, exact=True)
     assert dt_g == dt_e
     assert_identical(got, exact, 'variant %d' % variant)
+
+
+@pytest.mark.parametrize('name', sorted(SCENARIOS))
+@pytest.mark.parametrize('capacity', [0, 10])
+def test_pair_pipeline_over_capacity(oracle, native, name, capacity):
+    """A pair-pipeline step whose near lists exceed the (fixed) capacity runs
+    the lane-group kernel instead, with the same bit-exact results."""
+    scen = SCENARIOS[name]()
+    noise = S.draw_noise(scen.agents, np.random.default_rng(13))
+    b, agents, _ = batch_from_scenarios([scen])
+    b.set_variant(10)
+    b.set_near_list_capacity(capacity)
+    b.set_noise(*noise)
+    dt = b.step(N.NODE_ALL, want_dt=True)
+    got = agents.copy()
+    b.download(got)
+    b.close()
+    exact, dt_e = oracle_step(oracle, scen, N.NODE_ALL, noise, exact=True)
+    assert dt[0] == dt_e
+    assert_identical(got, exact, 'capacity %d' % capacity)
+
+
+def test_pair_pipeline_grows_capacity(native):
+    """Automatic sizing from a too-small capacity: the first step runs the
+    fallback, the capacity grows after it, the later steps run the pair
+    pipeline; results stay identical to the one-lane kernel."""
+    scen = S.hallway(n=2000, width=30.0, height=10.0, seed=9)
+    outs = []
+    for variant, cap in ((0, None), (10, 1000)):
+        b, agents, _ = batch_from_scenarios([scen])
+        b.set_variant(variant)
+        if cap is not None:
+            b.set_near_list_capacity(cap)
+            b.run(2, N.NODE_ALL & ~N.NODE_FLUCTUATION)       # fixed: fallback steps
+            b.set_near_list_capacity(-1)                     # grows after the next run
+        else:
+            b.run(2, N.NODE_ALL & ~N.NODE_FLUCTUATION)
+        b.run(1, N.NODE_ALL & ~N.NODE_FLUCTUATION)
+        b.run(5, N.NODE_ALL & ~N.NODE_FLUCTUATION)
+        o = agents.copy()
+        b.download(o)
+        b.close()
+        outs.append(o)
+    assert_identical(outs[1], outs[0], 'pair pipeline vs one-lane kernel')
 
 
 @pytest.mark.parametrize('name', sorted(SCENARIOS))
