@@ -148,7 +148,8 @@ __device__ __forceinline__ void social_side(double tau, double it, double it2, d
 // gradient g, so one pass back through the geometry serves both sides.
 // Adds dPhi/dx, dPhi/dv and agent i's k_soc, tau_0 terms.
 __device__ __forceinline__ void pair_vjp_both(const Circ &A, const Circ &B, double uix,
-                                              double uiy, double ujx, double ujy, PairGrad &G) {
+                                              double uiy, double ujx, double ujy, PairGrad &G,
+                                              double *gk_j = nullptr, double *gt0_j = nullptr) {
     const double xx = A.x - B.x, xy = A.y - B.y;
     const double d0 = cdm_hypot(xx, xy);
     const double r_tot = A.r + B.r;
@@ -171,7 +172,7 @@ __device__ __forceinline__ void pair_vjp_both(const Circ &A, const Circ &B, doub
             social_side(tau, it, it2, gx, gy, 1.0, A.m, A.k, A.tau0, uix, uiy, lgx, lgy, ltau,
                         &G.gk, &G.gt0);
             social_side(tau, it, it2, gx, gy, -1.0, B.m, B.k, B.tau0, ujx, ujy, lgx, lgy, ltau,
-                        nullptr, nullptr);
+                        gk_j, gt0_j);
             // g = v / a - b v / (a dd) - x / dd,  tau = (b - dd) / a
             double la = -(lgx * (gx + xx * idd) + lgy * (gy + xy * idd)) * ia;
             double lb = -(lgx * vx + lgy * vy) * ia * idd;
@@ -304,12 +305,36 @@ __global__ void k_loss_grad(const double *x, const double *y, const double *targ
     lx[2 * i + 1] += scale * 2.0 * (y[i] - target[2 * i + 1]);
 }
 
+// Adjusting term (F = (m / tau_adj) (v0 e0 - v)) and the agent's outputs.
+__device__ __forceinline__ void adj_finish(const StepArgs &a, const AdjArgs &q, int i, double uxi,
+                                           double uyi, PairGrad G) {
+    double *const *col = a.col;
+    const double m = col[MASS][i], ta = col[TAU_ADJ][i], v0 = col[V0][i];
+    const double ex = col[E0X][i], ey = col[E0Y][i];
+    const double kk = m / ta;
+    G.gvx -= kk * uxi;
+    G.gvy -= kk * uyi;
+    const double g_ta =
+        -(m / (ta * ta)) * (uxi * (v0 * ex - col[VX][i]) + uyi * (v0 * ey - col[VY][i]));
+    const double g_v0 = kk * (uxi * ex + uyi * ey);
+    q.lx_out[2 * i] = q.lx[2 * i] + G.gxx;
+    q.lx_out[2 * i + 1] = q.lx[2 * i + 1] + G.gxy;
+    q.lv_out[2 * i] = q.lvt[2 * i] + G.gvx;
+    q.lv_out[2 * i + 1] = q.lvt[2 * i + 1] + G.gvy;
+    q.grad[4 * i + 0] += g_ta;
+    q.grad[4 * i + 1] += g_v0;
+    q.grad[4 * i + 2] += G.gt0;
+    q.grad[4 * i + 3] += G.gk;
+}
+
 // Pair, wall and adjusting terms of the reverse step.  A group of L lanes
 // takes the agent in cell-sorted slot s: its 3 x 3 neighbour cells are three
 // runs of consecutive slots, which the lanes stride through; the lanes'
 // partial sums meet in a fixed butterfly, so the result is deterministic.
 template <int L>
-__global__ void __launch_bounds__(NT) k_adj_forces(StepArgs a, AdjArgs q) {
+__global__ void __launch_bounds__(NT) k_adj_forces(StepArgs a, AdjArgs q, int only_if_over) {
+    // as the pair pipeline's fallback: only for a step whose near lists did not fit
+    if (only_if_over && !(a.nl_off[a.n] > a.nl_cap)) return;
     const int r = threadIdx.x & (L - 1);
     const int s = (int)(((long long)blockIdx.x * NT + threadIdx.x) / L);
     const bool valid = s < a.n;
@@ -360,24 +385,84 @@ __global__ void __launch_bounds__(NT) k_adj_forces(StepArgs a, AdjArgs q) {
         G.gt0 += __shfl_xor_sync(0xffffffffu, G.gt0, o);
     }
     if (!valid || r != 0) return;
-    // adjusting: F = (m / tau_adj) (v0 e0 - v)
-    double *const *col = a.col;
-    const double m = col[MASS][i], ta = col[TAU_ADJ][i], v0 = col[V0][i];
-    const double ex = col[E0X][i], ey = col[E0Y][i];
-    const double kk = m / ta;
-    G.gvx -= kk * uxi;
-    G.gvy -= kk * uyi;
-    const double g_ta =
-        -(m / (ta * ta)) * (uxi * (v0 * ex - col[VX][i]) + uyi * (v0 * ey - col[VY][i]));
-    const double g_v0 = kk * (uxi * ex + uyi * ey);
-    q.lx_out[2 * i] = q.lx[2 * i] + G.gxx;
-    q.lx_out[2 * i + 1] = q.lx[2 * i + 1] + G.gxy;
-    q.lv_out[2 * i] = q.lvt[2 * i] + G.gvx;
-    q.lv_out[2 * i + 1] = q.lvt[2 * i + 1] + G.gvy;
-    q.grad[4 * i + 0] += g_ta;
-    q.grad[4 * i + 1] += g_v0;
-    q.grad[4 * i + 2] += G.gt0;
-    q.grad[4 * i + 3] += G.gk;
+    adj_finish(a, q, i, uxi, uyi, G);
+}
+
+// ---- compute-once form over the near lists of the forward pipeline ----
+//
+// Every unordered pair once (flat list of (slot, entry) with the later slot
+// in the entry): G = dPhi/d(x_i - x_j), dPhi/d(v_i - v_j) of the pair's
+// seed Phi goes to the first agent's entry and -G to the partner's entry for
+// it, each with its own k_soc / tau_0 terms; a per-agent pass then adds the
+// entries in list order (deterministic), the walls and adjusting.
+
+__device__ __forceinline__ int partner_entry(const StepArgs &a, int t, int s) {
+    int lo = __ldg(&a.nl_off[t]), hi = __ldg(&a.nl_fwd[t]);
+    const int end = hi;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&a.nl_idx[mid]) < s) lo = mid + 1;
+        else hi = mid;
+    }
+    return (lo < end && __ldg(&a.nl_idx[lo]) == s) ? lo : -1;
+}
+
+__device__ __forceinline__ void put_adj(double *res, int e, double gx, double gy, double gvx,
+                                        double gvy, double gk, double gt0) {
+    double2 *p = reinterpret_cast<double2 *>(res + (size_t)e * ADJ_RES_D);
+    p[0] = make_double2(gx, gy);
+    p[1] = make_double2(gvx, gvy);
+    p[2] = make_double2(gk, gt0);
+}
+
+__global__ void __launch_bounds__(NT) k_adj_pairs(StepArgs a, AdjArgs q) {
+    if (a.nl_off[a.n] > a.nl_cap) return;
+    const int npairs = a.fw_off[a.n];
+    for (int k = blockIdx.x * NT + threadIdx.x; k < npairs; k += gridDim.x * NT) {
+        const int2 pe = __ldg(&a.fw_pairs[k]);
+        const int s = pe.x, e = pe.y;
+        const int t = __ldg(&a.nl_idx[e]);
+        const int i = a.perm[s], j = a.perm[t];
+        PairGrad G{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        double gkj = 0.0, gt0j = 0.0;
+        pair_vjp_both(load_circ(a.stage, s), load_circ(a.stage, t), q.lF[2 * i], q.lF[2 * i + 1],
+                      q.lF[2 * j], q.lF[2 * j + 1], G, &gkj, &gt0j);
+        put_adj(a.nl_res, e, G.gxx, G.gxy, G.gvx, G.gvy, G.gk, G.gt0);
+        const int eq = partner_entry(a, t, s);
+        if (eq >= 0) put_adj(a.nl_res, eq, -G.gxx, -G.gxy, -G.gvx, -G.gvy, gkj, gt0j);
+        else atomicOr(a.err, ERR_NEAR_LIST);
+    }
+}
+
+__global__ void __launch_bounds__(NT) k_adj_gather(StepArgs a, AdjArgs q) {
+    if (a.nl_off[a.n] > a.nl_cap) return;               // k_adj_forces' step
+    const int s = blockIdx.x * NT + threadIdx.x;
+    if (s >= a.n) return;
+    const int i = a.perm[s];
+    PairGrad G{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    const int o1 = a.nl_off[s + 1];
+    for (int e = a.nl_off[s]; e < o1; ++e) {
+        const double2 *p = reinterpret_cast<const double2 *>(a.nl_res + (size_t)e * ADJ_RES_D);
+        const double2 x = p[0], v = p[1], kt = p[2];
+        G.gxx += x.x; G.gxy += x.y;
+        G.gvx += v.x; G.gvy += v.y;
+        G.gk += kt.x; G.gt0 += kt.y;
+    }
+    const double uxi = q.lF[2 * i], uyi = q.lF[2 * i + 1];
+    const ScenDev sc = a.scen[a.scen_of[i]];
+    if (sc.wall_count > 0) {
+        const float4 me = a.cull[s];
+        const int my_cell = a.key[i];
+        const Circ A = load_circ(a.stage, s);
+        const bool all_walls = me.z > (float)sc.wall_reach;
+        const int wb = all_walls ? sc.wall_begin : __ldg(&a.wall_start[my_cell]);
+        const int we = all_walls ? sc.wall_begin + sc.wall_count : __ldg(&a.wall_start[my_cell + 1]);
+        for (int qw = wb; qw < we; ++qw) {
+            const int w = all_walls ? qw : __ldg(&a.wall_idx[qw]);
+            wall_circ_vjp(A, a.walls + (size_t)w * WALL_D, uxi, uyi, G.gxx, G.gxy, G.gvx, G.gvy);
+        }
+    }
+    adj_finish(a, q, i, uxi, uyi, G);
 }
 
 // Copies of up to 8 state columns in one launch (checkpoint save / restore).
@@ -448,11 +533,16 @@ void launch_adj_seed(const AdjArgs &q, cudaStream_t s) {
 }
 void launch_adj_forces(const StepArgs &a, const AdjArgs &q, cudaStream_t s) {
     if (a.n <= 0) return;
-    // lanes per agent: enough warps to fill the SMs at small agent counts
     const long long n = a.n;
-    if (n < 20000) k_adj_forces<16><<<nblk(n * 16, NT), NT, 0, s>>>(a, q);
-    else if (n < 80000) k_adj_forces<8><<<nblk(n * 8, NT), NT, 0, s>>>(a, q);
-    else k_adj_forces<4><<<nblk(n * 4, NT), NT, 0, s>>>(a, q);
+    const int over = a.nl_cnt != nullptr;     // pair pipeline first, this as its fallback
+    if (over) {
+        k_adj_pairs<<<nblk(n * 16, NT), NT, 0, s>>>(a, q);
+        k_adj_gather<<<nblk(n, NT), NT, 0, s>>>(a, q);
+    }
+    // lanes per agent: enough warps to fill the SMs at small agent counts
+    if (n < 20000) k_adj_forces<16><<<nblk(n * 16, NT), NT, 0, s>>>(a, q, over);
+    else if (n < 80000) k_adj_forces<8><<<nblk(n * 8, NT), NT, 0, s>>>(a, q, over);
+    else k_adj_forces<4><<<nblk(n * 4, NT), NT, 0, s>>>(a, q, over);
 }
 void launch_copy_cols(const double *const *src, double *const *dst, int ncol, int n,
                       cudaStream_t s) {

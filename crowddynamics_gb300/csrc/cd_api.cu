@@ -302,15 +302,13 @@ int grow_near_lists(cd_ctx *c, int64_t need) {
     return alloc_near_lists(c, cap);
 }
 
-// First use of the pair pipeline: count the near lists of the current state
-// and allocate their entries.
-int ensure_near_lists(cd_ctx *c, int nodes) {
-    if (!cdk::variant_pairs(c->variant) || !(nodes & CD_NODE_AGENT_AGENT) || c->n == 0 ||
-        c->nl_cap > 0 || c->nl_fixed)
-        return CD_OK;
+// Near-list entries for the current state (pair pipeline, adjoint), counted
+// and allocated on first use.
+int size_near_lists(cd_ctx *c) {
+    if (c->n == 0 || c->nl_cap > 0 || c->nl_fixed) return CD_OK;
     StepArgs a = args_of(c, CD_NODE_AGENT_AGENT);
     enqueue_cells(c, a);
-    cdk::launch_near_count(a, c->stream, c->variant);
+    cdk::launch_near_count(a, c->stream, cdk::variant_pairs(c->variant) ? c->variant : 10);
     int need = 0;
     CUDA_OR_FAIL(c, cudaMemcpyAsync(&need, c->nl_off + c->n, sizeof(int), cudaMemcpyDeviceToHost,
                                     c->stream));
@@ -318,16 +316,21 @@ int ensure_near_lists(cd_ctx *c, int nodes) {
     return grow_near_lists(c, need);
 }
 
+int ensure_near_lists(cd_ctx *c, int nodes) {
+    if (!cdk::variant_pairs(c->variant) || !(nodes & CD_NODE_AGENT_AGENT)) return CD_OK;
+    return size_near_lists(c);
+}
+
 int check_device_error(cd_ctx *c) {
     CUDA_OR_FAIL(c, cudaGetLastError());
     int h = 0, need = 0;
-    const bool pairs = cdk::variant_pairs(c->variant) && c->nl_cap > 0 && c->n > 0;
+    const bool pairs = c->nl_cap > 0 && c->n > 0;       // lists in use (pair pipeline, adjoint)
     CUDA_OR_FAIL(c, cudaMemcpyAsync(&h, c->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     if (pairs)
         CUDA_OR_FAIL(c, cudaMemcpyAsync(&need, c->nl_off + c->n, sizeof(int),
                                         cudaMemcpyDeviceToHost, c->stream));
     CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
-    // the last step ran the lane-group fallback when its near lists did not fit
+    // the last list build did not fit: its step ran the fallback; grow for the next
     if (pairs && need > c->nl_cap)
         if (int rc = grow_near_lists(c, need)) return rc;
     if (h) {
@@ -904,6 +907,8 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
         return cd_run(c, nodes, steps);
     }
     ckpt = std::min(ckpt, steps);
+    if (grads)                                      // near-list entries for the reverse pass
+        if (int rc = size_near_lists(c)) return rc;  // (before the graph: sizing drops it)
     if (int rc = ensure_graph(c, nodes)) return rc;
     const int64_t nseg = (steps + ckpt - 1) / ckpt;
     const size_t snap = (size_t)SNAP_COLS * (size_t)std::max<int64_t>(n, 1);
@@ -965,6 +970,7 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
                 if ((rc = copy_state(c, seg + (size_t)(t - t0) * snap, false))) break;
                 StepArgs a = args_of(c, fnodes);
                 enqueue_cells(c, a);                        // cell list of the state before step t
+                cdk::launch_near_lists(a, st);              // and its near lists
                 cdk::AdjArgs q;
                 q.n = (int)n;
                 q.dt = dts + t;

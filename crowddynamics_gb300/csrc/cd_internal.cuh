@@ -130,6 +130,8 @@ int variant_staged(int variant);
 void launch_forces(const StepArgs &a, cudaStream_t s, int variant);
 // Near-list counts and their scan (nl_off) for the state staged in `a`.
 void launch_near_count(const StepArgs &a, cudaStream_t s, int variant);
+// Near lists (counts, scans, fill; 8 lanes per agent) for the state staged in `a`.
+void launch_near_lists(const StepArgs &a, cudaStream_t s);
 void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s);
 void launch_v0max(const StepArgs &a, double *v0max_out, cudaStream_t s);
 void launch_wall_prep(const double *raw, double *walls, float4 *walls_f, int nw,

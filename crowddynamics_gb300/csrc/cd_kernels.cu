@@ -1967,6 +1967,15 @@ void launch_near_count(const StepArgs &a, cudaStream_t s, int variant) {
     launch_scan(a.fw_cnt, a.fw_off, a.n, a.fw_scan, s);
 }
 
+void launch_near_lists(const StepArgs &a, cudaStream_t s) {
+    if (a.n <= 0 || !a.nl_cnt) return;
+    const int nb = nblk((long long)a.n * 8, NTG);
+    kNlCount[1]<<<nb, NTG, 0, s>>>(a);
+    launch_scan(a.nl_cnt, a.nl_off, a.n, a.nl_scan, s);
+    launch_scan(a.fw_cnt, a.fw_off, a.n, a.fw_scan, s);
+    kNlFill[1]<<<nb, NTG, 0, s>>>(a);
+}
+
 void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s) {
     if (a.n > 0) k_pair_counts<<<nblk(a.n, 128), 128, 0, s>>>(a, counts);
 }

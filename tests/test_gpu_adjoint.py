@@ -194,3 +194,18 @@ def test_rollout_rejects_bad_input(native):
     with pytest.raises(InvalidType):
         bt.rollout_loss(STEPS, np.zeros((STEPS, len(tc.agents), 2)), CKPT)
     bt.close()
+
+
+def test_adjoint_over_capacity_fallback(native):
+    """With the near-list capacity fixed below what the reverse pass needs,
+    each reverse step runs the lane-group adjoint instead of the pair form:
+    the same gradient up to summation order."""
+    scen, a, target = _case('dense')
+    ref = _loss(scen, a, target)
+    b, _ = _device(scen, a)
+    b.set_near_list_capacity(0)
+    got = b.rollout_loss(STEPS, target, CKPT)
+    b.close()
+    assert got[0] == ref[0]                      # the forward is unchanged
+    scale = np.abs(ref[1]).max(0)
+    assert np.all(np.abs(got[1] - ref[1]) <= 1e-10 * scale)
