@@ -148,9 +148,16 @@ def algorithmic_flops(scen, counts):
     on this state (pair columns count each unordered pair twice)."""
     w = WEIGHTS[scen.body]
     tot = counts.sum(axis=0)
-    return (w['cand'] * tot[0] / 2 + w['near'] * tot[1] / 2 + w['inter'] * tot[2] / 2 +
-            w['contact'] * tot[3] / 2 + w['wall_near'] * tot[4] + w['wall_contact'] * tot[5] +
-            w['agent'] * len(scen.agents))
+    return (w['cand'] * tot[0] / 2 + pair_flops(scen, counts) + w['wall_near'] * tot[4] +
+            w['wall_contact'] * tot[5] + w['agent'] * len(scen.agents))
+
+
+def pair_flops(scen, counts):
+    """The part of algorithmic_flops done by the pair kernel: every unordered
+    pair that passes the bound check, once (distance, social force, contact)."""
+    w = WEIGHTS[scen.body]
+    tot = counts.sum(axis=0)
+    return w['near'] * tot[1] / 2 + w['inter'] * tot[2] / 2 + w['contact'] * tot[3] / 2
 
 
 def cpu_sample(scen, nodes_orc, steps, nthreads):
@@ -251,10 +258,17 @@ def run_ours(args, ws, rank, local):
         run_ms = float(t.item())
     value = ws * n * args.steps / (run_ms / 1e3)
     force_ms = kt['force_ms'] / max(kt['force_launches'], 1)
+    pair_ms = kt['pair_ms'] / max(kt['pair_launches'], 1) if kt['pair_launches'] else None
     counts1 = b.pair_counts()
     flops = 0.5 * (algorithmic_flops(scen, counts0) + algorithmic_flops(scen, counts1))
-    achieved = flops / (force_ms / 1e3) / 1e12
+    pflops = 0.5 * (pair_flops(scen, counts0) + pair_flops(scen, counts1))
+    stage_achieved = flops / (force_ms / 1e3) / 1e12
     peak = peak_gflops / 1e3
+    if pair_ms:                    # the pair pipeline: its pair kernel is the dominant kernel
+        kernel, kernel_ms, kflops = 'k_pairs', pair_ms, pflops
+    else:
+        kernel, kernel_ms, kflops = 'k_forces', force_ms, flops
+    achieved = kflops / (kernel_ms / 1e3) / 1e12
 
     # end to end through the C ABI with pinned host records
     host = torch.empty(n * agents.dtype.itemsize, dtype=torch.uint8, pin_memory=True)
@@ -279,7 +293,7 @@ def run_ours(args, ws, rank, local):
         try:
             tr = json.load(open(tpath))
             if tr.get('workload') == config_of(scen, '')['workload']:
-                traffic = tr.get('k_forces_dram_bytes_per_launch')
+                traffic = tr.get('%s_dram_bytes_per_launch' % kernel)
         except (OSError, ValueError):
             traffic = None
 
@@ -297,9 +311,16 @@ def run_ours(args, ws, rank, local):
             'gpu_launches': b.kernels_per_step(nodes) * args.steps,
             'roofline': {'bound': 'fp64', 'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s',
                          'frac': achieved / peak, 'traffic': traffic,
-                         'kernel': 'k_forces', 'kernel_ms': force_ms,
-                         'flops_per_launch': flops,
-                         'peak_source': 'measured live: FP64 FMA chain kernel (2 flops per FMA)'},
+                         'kernel': kernel, 'kernel_ms': kernel_ms,
+                         'flops_per_launch': kflops,
+                         'peak_source': 'measured live: FP64 FMA chain kernel (2 flops per FMA)',
+                         'force_stage': {'ms': force_ms, 'flops_per_step': flops,
+                                         'achieved': stage_achieved,
+                                         'frac': stage_achieved / peak,
+                                         'kernels': 'k_nl_count, near and forward scans, '
+                                                    'k_nl_fill, k_pairs, k_forces_gather, '
+                                                    'k_forces_fallback (exits at once unless '
+                                                    'the near lists overflowed)'}},
             'clocks': clk.summary()}
     if not args.no_batched:
         line['batched'] = run_batched(args.steps, args.warmup, flush)

@@ -37,7 +37,8 @@ SYMBOLS = (
     'cd_synchronize', 'cd_get_time', 'cd_get_cell_list', 'cd_pair_counts',
     'cd_sizes', 'cd_set_timing', 'cd_kernel_time', 'cd_kernels_per_step',
     'cd_measure_fp64_peak', 'cd_agent_agent_noalloc', 'cd_variant_count',
-    'cd_variant_shape', 'cd_set_variant', 'cd_set_near_list_capacity', 'cd_launch',
+    'cd_variant_shape', 'cd_set_variant', 'cd_set_near_list_capacity', 'cd_pair_kernel_time',
+    'cd_launch',
     'cd_rollout_loss',
 )
 
@@ -105,6 +106,7 @@ def load(path=None):
         'cd_variant_shape': (ctypes.c_int, [ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 4),
         'cd_set_variant': (ctypes.c_int, [P, ctypes.c_int]),
         'cd_set_near_list_capacity': (ctypes.c_int, [P, i64]),
+        'cd_pair_kernel_time': (ctypes.c_int, [P, pd, pi64]),
         'cd_launch': (ctypes.c_int, [P, ctypes.c_int, i64]),
         'cd_rollout_loss': (ctypes.c_int, [P, i64, P, i64, pd, pd, pd, pd]),
         'cd_agent_agent_noalloc': (ctypes.c_int, [ctypes.c_int, i64, P, P, P, P, ctypes.c_double,

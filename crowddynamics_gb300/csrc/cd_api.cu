@@ -72,6 +72,9 @@ struct cd_ctx {
     bool timing = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs0 = nullptr, evs1 = nullptr;
     cudaEvent_t evr0 = nullptr, evr1 = nullptr;
+    cudaEvent_t evp[2] = {nullptr, nullptr};     // around the pair kernel
+    double pair_ms = 0;
+    int64_t pair_launches = 0;
     double force_ms = 0, step_ms = 0, run_ms = 0;
     int64_t launches = 0, run_steps = 0;
 
@@ -164,6 +167,8 @@ void release(cd_ctx *c) {
     if (c->evs1) cudaEventDestroy(c->evs1);
     if (c->evr0) cudaEventDestroy(c->evr0);
     if (c->evr1) cudaEventDestroy(c->evr1);
+    if (c->evp[0]) cudaEventDestroy(c->evp[0]);
+    if (c->evp[1]) cudaEventDestroy(c->evp[1]);
     if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -256,7 +261,7 @@ void enqueue_step(cd_ctx *c, int nodes, bool timed, bool captured = false) {
     enqueue_cells(c, a);
     if (timed) cudaEventRecord(c->ev0, c->stream);
     if (captured) cudaEventRecordWithFlags(c->ev0, c->stream, cudaEventRecordExternal);
-    cdk::launch_forces(a, c->stream, c->variant);
+    cdk::launch_forces(a, c->stream, c->variant, (timed || captured) ? c->evp : nullptr, captured);
     if (timed) cudaEventRecord(c->ev1, c->stream);
     if (captured) cudaEventRecordWithFlags(c->ev1, c->stream, cudaEventRecordExternal);
     if (timed) cudaEventRecord(c->evs1, c->stream);
@@ -319,6 +324,16 @@ int size_near_lists(cd_ctx *c) {
 int ensure_near_lists(cd_ctx *c, int nodes) {
     if (!cdk::variant_pairs(c->variant) || !(nodes & CD_NODE_AGENT_AGENT)) return CD_OK;
     return size_near_lists(c);
+}
+
+// Pair-kernel time of the step just timed (pair pipeline with agent-agent).
+void add_pair_time(cd_ctx *c, int nodes) {
+    if (!cdk::variant_pairs(c->variant) || !(nodes & CD_NODE_AGENT_AGENT) || c->n == 0) return;
+    float pms = 0;
+    if (cudaEventElapsedTime(&pms, c->evp[0], c->evp[1]) == cudaSuccess) {
+        c->pair_ms += pms;
+        c->pair_launches += 1;
+    }
 }
 
 int check_device_error(cd_ctx *c) {
@@ -505,6 +520,8 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
         cudaEventCreate(&c->evs1);
         cudaEventCreate(&c->evr0);
         cudaEventCreate(&c->evr1);
+        cudaEventCreate(&c->evp[0]);
+        cudaEventCreate(&c->evp[1]);
         cudaError_t e = cudaDeviceSynchronize();
         if (e != cudaSuccess) rc = fail(c, CD_ERR_CUDA, cudaGetErrorString(e));
     }
@@ -646,6 +663,7 @@ int cd_step(cd_ctx *c, int nodes, double *dt) {
         c->force_ms += ms;
         c->step_ms += sms;
         c->launches += 1;
+        add_pair_time(c, nodes);
     }
     if (dt) {
         if (int rc = check_device_error(c)) return rc;
@@ -706,6 +724,7 @@ int cd_run(cd_ctx *c, int nodes, int64_t steps) {
             cudaEventElapsedTime(&fms, c->ev0, c->ev1);
             c->force_ms += fms;
             c->launches += 1;
+            add_pair_time(c, nodes);
         }
     }
     return check_device_error(c);
@@ -779,8 +798,15 @@ int cd_sizes(const cd_ctx *c, int64_t *n_agents, int64_t *n_walls, int64_t *n_ce
 int cd_set_timing(cd_ctx *c, int enable) {
     if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
     c->timing = enable != 0;
-    c->force_ms = c->step_ms = c->run_ms = 0;
-    c->launches = c->run_steps = 0;
+    c->force_ms = c->step_ms = c->run_ms = c->pair_ms = 0;
+    c->launches = c->run_steps = c->pair_launches = 0;
+    return CD_OK;
+}
+
+int cd_pair_kernel_time(cd_ctx *c, double *ms, int64_t *launches) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (ms) *ms = c->pair_ms;
+    if (launches) *launches = c->pair_launches;
     return CD_OK;
 }
 

@@ -127,7 +127,10 @@ int default_variant(long long n_agents);
 int default_group_variant(long long n_agents);
 int variant_threads(int variant);
 int variant_staged(int variant);
-void launch_forces(const StepArgs &a, cudaStream_t s, int variant);
+// The agent-force stage; with `pair_ev`, events recorded around the pair
+// kernel of the pair pipeline (as external event-record nodes if `captured`).
+void launch_forces(const StepArgs &a, cudaStream_t s, int variant,
+                   const cudaEvent_t *pair_ev = nullptr, bool captured = false);
 // Near-list counts and their scan (nl_off) for the state staged in `a`.
 void launch_near_count(const StepArgs &a, cudaStream_t s, int variant);
 // Near lists (counts, scans, fill; 8 lanes per agent) for the state staged in `a`.

@@ -582,7 +582,9 @@ __device__ __forceinline__ bool pair_circular_both(const Circ &A, const Circ &B,
             double cmp = (-A.m) * A.k, cmq = (-B.m) * B.k;
             double two_t = 2.0 / tau, tt = tau * tau;       // shared terms of magnitude()
             double magp = (two_t + 1.0 / A.tau0) * cdm_exp(-tau / A.tau0) / tt;
-            double magq = (two_t + 1.0 / B.tau0) * cdm_exp(-tau / B.tau0) / tt;
+            // magnitude() depends on (tau, tau_0) only: equal tau_0, equal value
+            double magq = B.tau0 == A.tau0 ? magp
+                                           : (two_t + 1.0 / B.tau0) * cdm_exp(-tau / B.tau0) / tt;
             FPx = (cmp * gx) * magp;
             FPy = (cmp * gy) * magp;
             truncate2(FPx, FPy, F_SOC_MAX);
@@ -616,6 +618,18 @@ struct WarpQueue {
 };
 
 constexpr float PRESEL_MARGIN = 1e-4f;   // metres (float32 error of h is ~1e-6 m)
+
+// Per-warp queue of tc_pair_both: the sub-circle pairs that may have a
+// time-to-collision (9 slots per lane) and each lane's pair geometry.
+constexpr int GEO_D = 19;   // P parts x[3] y[3], Q parts x[3] y[3], P rt rs, Q rt rs, vr, a
+struct PairQueue {
+    double b[32 * 9];
+    double disc[32 * 9];        // out: square root of the discriminant, or -1
+    double tau[32 * 9];
+    double geo[32 * GEO_D];
+    int off[33];
+    unsigned char kidx[32 * 9];
+};
 
 // One ThreeCircle pair for every lane of the warp (collective: all lanes in
 // `wmask` call it; `act` lanes have a pair, `me_first` its orientation):
@@ -829,7 +843,7 @@ __device__ __forceinline__ void tc_pair_step(const TC &A, const float4 meC, cons
 // tc_pair_eval (all 32 lanes call it).
 __device__ __forceinline__ bool tc_pair_both(const TC &A, const float4 meC, const float4 meF0,
                                              const float4 meF1, const StepArgs &a, bool act,
-                                             int t, WarpQueue &q, int lane, double &FPx,
+                                             int t, PairQueue &q, int lane, double &FPx,
                                              double &FPy, double &TP, double &FQx, double &FQy,
                                              double &TQ) {
     constexpr unsigned wmask = 0xffffffffu;
@@ -914,29 +928,44 @@ __device__ __forceinline__ bool tc_pair_both(const TC &A, const float4 meC, cons
         rqy = (sel3(A.y, qp_min) + r * nqy) - B.y[0];
     }
     // -- force_social_three_circle (shared time-to-collision) --
+    // float32 test of the 9 sub-circle discriminants: a sub-pair whose
+    // float32 discriminant is below -M has a negative float64 one (M bounds
+    // the float32 error of every input and operation several times over);
+    // the others go to the warp queue, where any lane evaluates the
+    // reference's float64 b, c, discriminant, root and time-to-collision
+    // from the owner's geometry in shared memory
     const double vrx = A.vx - B.vx, vry = A.vy - B.vy;
     const double av = vrx * vrx + vry * vry;
     const bool soc = inter && av != 0;
-    unsigned defmask = 0;
+    unsigned candmask = 0;
     int cnt = 0;
-    double *qb = q.b + lane * 9;
-    double *qd = q.disc + lane * 9;
     if (soc) {
+        const float vxf = (float)vrx, vyf = (float)vry;
+        const float af = vxf * vxf + vyf * vyf;
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
-            int mi = k / 3, ti = k % 3;
-            double xr = sel3(A.x, mi) - sel3(B.x, ti), yr = sel3(A.y, mi) - sel3(B.y, ti);
-            double r_tot = part_r(A, mi) + part_r(B, ti);
-            double b = -(xr * vrx + yr * vry);
-            double c = (xr * xr + yr * yr) - r_tot * r_tot;
-            double disc = b * b - av * c;
-            if (disc > 0) {
-                qb[cnt] = b;
-                qd[cnt] = disc;
+            const int i = k / 3, j = k % 3;
+            const float dx = (dxt + mox[i]) - oox[j], dy = (dyt + moy[i]) - ooy[j];
+            const float rt = mr[i] + orr[j];
+            const float bf = -(dx * vxf + dy * vyf);
+            const float x2 = dx * dx + dy * dy;
+            const float cf = x2 - rt * rt;
+            const float acf = af * cf;
+            const float discf = bf * bf - acf;
+            const float m = 1e-5f * af * (1.f + x2 + rt * rt) + 1e-6f * (bf * bf + fabsf(acf));
+            if (!(discf < -m)) {
+                q.kidx[lane * 9 + cnt] = (unsigned char)k;
                 ++cnt;
-                defmask |= 1u << k;
+                candmask |= 1u << k;
             }
         }
+        double *g = q.geo + lane * GEO_D;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            g[k] = A.x[k]; g[3 + k] = A.y[k]; g[6 + k] = B.x[k]; g[9 + k] = B.y[k];
+        }
+        g[12] = A.rt; g[13] = A.rs; g[14] = B.rt; g[15] = B.rs;
+        g[16] = vrx; g[17] = vry; g[18] = av;
     }
     int incl = cnt;
 #pragma unroll
@@ -945,22 +974,35 @@ __device__ __forceinline__ bool tc_pair_both(const TC &A, const float4 meC, cons
         if (lane >= o) incl += v;
     }
     q.off[lane] = incl - cnt;
-    q.a[lane] = av;
     const int total = __shfl_sync(wmask, incl, nlanes - 1);
     if (lane == nlanes - 1) q.off[nlanes] = incl;
     __syncwarp(wmask);
     for (int base = 0; base < total; base += nlanes) {
         int it = base + lane;
         if (it < total) {
-            int lo = 0, hi = nlanes - 1;
+            int lo = 0, hi = nlanes - 1;        // owner: last lane with off <= it
             while (lo < hi) {
                 int mid = (lo + hi + 1) >> 1;
                 if (q.off[mid] <= it) lo = mid; else hi = mid - 1;
             }
-            int slot = lo * 9 + (it - q.off[lo]);
-            double d = sqrt(q.disc[slot]);
-            q.tau[slot] = (q.b[slot] - d) / q.a[lo];
-            q.disc[slot] = d;
+            const int slot = lo * 9 + (it - q.off[lo]);
+            const int k = q.kidx[slot];
+            const int i = k / 3, j = k % 3;
+            const double *g = q.geo + lo * GEO_D;
+            const double gvx = g[16], gvy = g[17], ga = g[18];
+            const double xr = g[i] - g[6 + j], yr = g[3 + i] - g[9 + j];
+            const double r_tot = g[12 + (i > 0)] + g[14 + (j > 0)];
+            const double b = -(xr * gvx + yr * gvy);
+            const double c = (xr * xr + yr * yr) - r_tot * r_tot;
+            const double disc = b * b - ga * c;
+            double d = -1.0, tau_k = 0.0;
+            if (disc > 0) {                      // sqrt defined and non-zero
+                d = sqrt(disc);
+                tau_k = (b - d) / ga;
+            }
+            q.b[slot] = b;
+            q.disc[slot] = d;                    // -1: no time-to-collision
+            q.tau[slot] = tau_k;
         }
     }
     __syncwarp(wmask);
@@ -971,12 +1013,15 @@ __device__ __forceinline__ bool tc_pair_both(const TC &A, const float4 meC, cons
         int jj = 0;
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
-            if (defmask & (1u << k)) {
-                double tau_new = q.tau[lane * 9 + jj];
-                double dk = qd[jj], bk = qb[jj];
+            if (candmask & (1u << k)) {
+                const int slot = lane * 9 + jj;
                 ++jj;
-                if (isnan(tau) || (0 < tau_new && tau_new < tau)) {
-                    k_sel = k; tau = tau_new; b_min = bk; d_min = dk;
+                const double dk = q.disc[slot];
+                if (dk > 0) {
+                    const double tau_new = q.tau[slot];
+                    if (isnan(tau) || (0 < tau_new && tau_new < tau)) {
+                        k_sel = k; tau = tau_new; b_min = q.b[slot]; d_min = dk;
+                    }
                 }
             }
         }
@@ -995,7 +1040,9 @@ __device__ __forceinline__ bool tc_pair_both(const TC &A, const float4 meC, cons
         double cmp = (-A.m) * A.k, cmq = (-B.m) * B.k;
         double two_t = 2.0 / tau, tt = tau * tau;            // shared terms of magnitude()
         double magp = (two_t + 1.0 / A.tau0) * cdm_exp(-tau / A.tau0) / tt;
-        double magq = (two_t + 1.0 / B.tau0) * cdm_exp(-tau / B.tau0) / tt;
+        // magnitude() depends on (tau, tau_0) only: equal tau_0, equal value
+        double magq = B.tau0 == A.tau0 ? magp
+                                       : (two_t + 1.0 / B.tau0) * cdm_exp(-tau / B.tau0) / tt;
         FPx = (cmp * gx) * magp;
         FPy = (cmp * gy) * magp;
         truncate2(FPx, FPy, F_SOC_MAX);
@@ -1520,7 +1567,7 @@ __global__ void __launch_bounds__(NTG) k_pairs(StepArgs a) {
     constexpr unsigned FULL = 0xffffffffu;
     if (a.nl_off[a.n] > a.nl_cap) return;
     extern __shared__ unsigned char smem[];
-    WarpQueue *wq = reinterpret_cast<WarpQueue *>(smem);
+    PairQueue *wq = reinterpret_cast<PairQueue *>(smem);
     const int lane = threadIdx.x & 31;
     const int npairs = a.fw_off[a.n];
     for (;;) {
@@ -1828,7 +1875,7 @@ size_t forces_smem_bytes(int body, int variant) {
     return b;
 }
 
-size_t pairs_smem_bytes(int body) { return body == 1 ? sizeof(WarpQueue) * (NTG / 32) : 0; }
+size_t pairs_smem_bytes(int body) { return body == 1 ? sizeof(PairQueue) * (NTG / 32) : 0; }
 
 typedef void (*ForcesFn)(StepArgs);
 constexpr ForcesFn kForces[2][N_VARIANTS] = {
@@ -1918,7 +1965,8 @@ int init_kernels() {
     return e == cudaSuccess ? 0 : (int)e;
 }
 
-void launch_forces(const StepArgs &a, cudaStream_t s, int variant) {
+void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEvent_t *pair_ev,
+                   bool captured) {
     if (a.n <= 0) return;
     if (variant < 0 || variant >= N_VARIANTS) variant = 0;
     // the pair pipeline needs the near-list buffers: otherwise its lane-group twin
@@ -1938,8 +1986,10 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant) {
         if (rp <= 0) rp = 152;
         cudaMemsetAsync(a.work, 0, sizeof(int), s);
         // at most one warp per 32 pairs (about 16 pairs per agent): enough blocks
+        if (pair_ev) cudaEventRecordWithFlags(pair_ev[0], s, captured ? cudaEventRecordExternal : 0);
         kPairs[body]<<<std::min(nblk((long long)a.n * 16, NTG), rp), NTG, pairs_smem_bytes(body),
                        s>>>(a);
+        if (pair_ev) cudaEventRecordWithFlags(pair_ev[1], s, captured ? cudaEventRecordExternal : 0);
     }
     int resident = (dev >= 0 && dev < 64) ? g_forces_blocks[dev][body][variant] : 0;
     if (resident <= 0) resident = 152;

@@ -204,14 +204,17 @@ class DeviceBatch:
         self._chk(self._lib.cd_set_timing(self._ctx, int(bool(enable))))
 
     def kernel_time(self):
-        """dict(force_ms, force_launches, step_ms, run_ms, run_steps) since
-        the last set_timing."""
+        """dict(force_ms, force_launches, step_ms, run_ms, run_steps, pair_ms,
+        pair_launches) since the last set_timing."""
         f, s, r = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         n, rn = ctypes.c_int64(), ctypes.c_int64()
         self._chk(self._lib.cd_kernel_time(self._ctx, ctypes.byref(f), ctypes.byref(n),
                                            ctypes.byref(s), ctypes.byref(r), ctypes.byref(rn)))
+        pm, pn = ctypes.c_double(), ctypes.c_int64()
+        self._chk(self._lib.cd_pair_kernel_time(self._ctx, ctypes.byref(pm), ctypes.byref(pn)))
         return dict(force_ms=f.value, force_launches=n.value, step_ms=s.value,
-                    run_ms=r.value, run_steps=rn.value)
+                    run_ms=r.value, run_steps=rn.value, pair_ms=pm.value,
+                    pair_launches=pn.value)
 
     def kernels_per_step(self, nodes=N.NODE_ALL):
         k = ctypes.c_int64()

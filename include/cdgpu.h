@@ -165,6 +165,9 @@ int cd_sizes(const cd_ctx *ctx, int64_t *n_agents, int64_t *n_walls,
 int cd_set_timing(cd_ctx *ctx, int enable);
 int cd_kernel_time(cd_ctx *ctx, double *force_ms, int64_t *force_launches,
                    double *step_ms, double *run_ms, int64_t *run_steps);
+/* Time and launches of the pair kernel alone (pair-pipeline variants, steps
+ * with agent-agent), accumulated like cd_kernel_time. */
+int cd_pair_kernel_time(cd_ctx *ctx, double *ms, int64_t *launches);
 /* Number of kernels one step with `nodes` launches (memsets excluded). */
 int cd_kernels_per_step(const cd_ctx *ctx, int nodes, int64_t *kernels);
 
