@@ -45,6 +45,8 @@ struct cd_ctx {
     bool noise_pending = false;
     unsigned long long *vmax = nullptr;
     double *v0max = nullptr, *dt = nullptr, *time_tot = nullptr;
+    double *ext = nullptr, *max_partial = nullptr;      // per-scenario max extent, scratch
+    double *ext_host = nullptr;                        // pinned copy of ext
     int *err = nullptr, *work = nullptr;
     int *diag = nullptr;
     // near lists of the compute-once pair pipeline (entries allocated on use)
@@ -158,7 +160,7 @@ void release(cd_ctx *c) {
                     c->noise_f, c->noise_m, c->vmax, c->v0max, c->dt, c->time_tot,
                     c->err, c->work, c->diag, c->aos, c->nl_cnt, c->nl_off, c->nl_fwd,
                     c->nl_scan, c->nl_idx, c->nl_res, c->fw_cnt, c->fw_off, c->fw_scan,
-                    c->fw_pairs};
+                    c->fw_pairs, c->ext, c->max_partial};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -169,6 +171,7 @@ void release(cd_ctx *c) {
     if (c->evr1) cudaEventDestroy(c->evr1);
     if (c->evp[0]) cudaEventDestroy(c->evp[0]);
     if (c->evp[1]) cudaEventDestroy(c->evp[1]);
+    if (c->ext_host) cudaFreeHost(c->ext_host);
     if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -375,34 +378,6 @@ bool aligned_field(int64_t off, int64_t itemsize, int width) {
     return off >= 0 && (off % 4) == 0 && off + 8 * width <= itemsize;
 }
 
-// Largest torso-to-skin extent per scenario, from packed records.
-void host_extents(cd_ctx *c, const char *rec, int64_t itemsize, const int64_t *off) {
-    c->extent_max.assign(c->nscen, 0.0);
-    auto rd = [&](int64_t i, int f, int comp) {
-        double v;
-        std::memcpy(&v, rec + i * itemsize + off[f] + 8 * comp, 8);
-        return v;
-    };
-    for (int s = 0; s < c->nscen; ++s) {
-        const cd_scenario &sc = c->scen_host[s];
-        double m = 0.0;
-        for (int64_t i = sc.agent_begin; i < sc.agent_begin + sc.agent_count; ++i) {
-            double e;
-            if (c->body == CD_BODY_CIRCULAR) {
-                e = rd(i, CD_F_RADIUS, 0);
-            } else {
-                double x = rd(i, CD_F_POSITION, 0), y = rd(i, CD_F_POSITION, 1);
-                double rs = rd(i, CD_F_R_S, 0);
-                double l = std::hypot(rd(i, CD_F_POSITION_LS, 0) - x, rd(i, CD_F_POSITION_LS, 1) - y) + rs;
-                double r = std::hypot(rd(i, CD_F_POSITION_RS, 0) - x, rd(i, CD_F_POSITION_RS, 1) - y) + rs;
-                e = std::max(std::max(rd(i, CD_F_R_T, 0), rd(i, CD_F_R_TS, 0) + rs), std::max(l, r));
-            }
-            if (std::isfinite(e)) m = std::max(m, e);
-        }
-        if (m > c->extent_max[s]) c->extent_max[s] = m;
-    }
-}
-
 }  // namespace
 
 extern "C" {
@@ -494,6 +469,10 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->noise_m, n));
     step(dalloc(c, &c->vmax, n_scenarios));
     step(dalloc(c, &c->v0max, n_scenarios));
+    step(dalloc(c, &c->ext, n_scenarios));
+    step(dalloc(c, &c->max_partial, cdk::scen_max_partials((int)n_scenarios)));
+    if (rc == CD_OK && cudaMallocHost((void **)&c->ext_host, sizeof(double) * n_scenarios) != cudaSuccess)
+        rc = fail(c, CD_ERR_CUDA, "cudaMallocHost failed");
     step(dalloc(c, &c->dt, n_scenarios));
     step(dalloc(c, &c->time_tot, n_scenarios));
     step(dalloc(c, &c->err, 1));
@@ -585,16 +564,23 @@ int cd_upload_agents(cd_ctx *c, const void *records, int64_t n, int64_t itemsize
         cdk::launch_aos_to_soa(c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
     }
     StepArgs a = args_of(c, 0);
-    cdk::launch_v0max(a, c->v0max, c->stream);
-    // Wall bins depend on the agents' extent.
-    std::vector<double> prev = c->extent_max;
-    host_extents(c, static_cast<const char *>(records), itemsize, off);
-    for (int s = 0; s < c->nscen; ++s)
-        if (prev.empty() || c->extent_max[s] > prev[s]) c->walls_dirty = true;
-    if (!c->walls_dirty && !prev.empty()) c->extent_max = prev;
-    c->have_records = true;
+    cdk::launch_scen_max(a, c->v0max, c->ext, c->max_partial, c->stream);
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(c->ext_host, c->ext, sizeof(double) * c->nscen,
+                                    cudaMemcpyDeviceToHost, c->stream));
     CUDA_OR_FAIL(c, cudaGetLastError());
     CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    // Wall bins depend on the agents' extent: rebuilt when it grew.
+    if (c->extent_max.empty()) {
+        c->extent_max.assign(c->ext_host, c->ext_host + c->nscen);
+        c->walls_dirty = true;
+    } else {
+        for (int s = 0; s < c->nscen; ++s)
+            if (c->ext_host[s] > c->extent_max[s]) c->walls_dirty = true;
+        if (c->walls_dirty)
+            for (int s = 0; s < c->nscen; ++s)
+                c->extent_max[s] = std::max(c->extent_max[s], c->ext_host[s]);
+    }
+    c->have_records = true;
     return CD_OK;
 }
 

@@ -136,7 +136,11 @@ void launch_near_count(const StepArgs &a, cudaStream_t s, int variant);
 // Near lists (counts, scans, fill; 8 lanes per agent) for the state staged in `a`.
 void launch_near_lists(const StepArgs &a, cudaStream_t s);
 void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s);
-void launch_v0max(const StepArgs &a, double *v0max_out, cudaStream_t s);
+// Per-scenario max target_velocity and (if `ext`) max agent extent;
+// `partial` holds scen_max_partials(n_scen) doubles.
+void launch_scen_max(const StepArgs &a, double *v0max, double *ext, double *partial,
+                     cudaStream_t s);
+int scen_max_partials(int n_scen);
 void launch_wall_prep(const double *raw, double *walls, float4 *walls_f, int nw,
                       cudaStream_t s);
 void launch_aos_to_soa(const char *aos, long long itemsize, const long long *off,

@@ -276,27 +276,81 @@ __global__ void k_dt(StepArgs a) {
 }
 
 // Per-scenario max of target_velocity (np.max propagates NaN).
-__global__ void k_v0max(StepArgs a, double *out) {
-    int s = blockIdx.x;
-    if (s >= a.n_scen) return;
+// Per-scenario max target_velocity (NaN if any is NaN, like numpy's max) and
+// max agent extent (finite values only) in two passes: V0MAX_B blocks per
+// scenario write partials, then one warp per scenario combines them.  fmax
+// is exact, so the result does not depend on the order.
+constexpr int V0MAX_B = 64;
+
+__device__ __forceinline__ double extent_tc(double x, double y, double xl, double yl,
+                                            double xr, double yr, double rt, double rs);
+
+// Wall-binning extent of an agent: ThreeCircle also counts r_ts + r_s, the
+// shoulders' reach at any orientation.
+__device__ __forceinline__ double agent_extent(const StepArgs &a, int i) {
+    double *const *c = a.col;
+    if (a.body == 0) return c[R][i];
+    const double e = extent_tc(c[X][i], c[Y][i], c[XLS][i], c[YLS][i], c[XRS][i], c[YRS][i],
+                               c[RT][i], c[RS][i]);
+    return fmax(e, c[RTS][i] + c[RS][i]);
+}
+
+__global__ void k_scen_max_partial(StepArgs a, double *partial) {
+    const int s = blockIdx.y;
     const ScenDev sc = a.scen[s];
-    __shared__ double red[256];
+    __shared__ double rv[256], re[256];
     __shared__ int any_nan;
     if (threadIdx.x == 0) any_nan = 0;
     __syncthreads();
-    double m = -INFINITY;
-    for (int k = threadIdx.x; k < sc.agent_count; k += blockDim.x) {
-        double v = a.col[V0][sc.agent_begin + k];
+    double m = -INFINITY, e = 0.0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < sc.agent_count;
+         k += gridDim.x * blockDim.x) {
+        const int i = sc.agent_begin + k;
+        const double v = a.col[V0][i];
         if (isnan(v)) any_nan = 1;
         else m = fmax(m, v);
+        const double x = agent_extent(a, i);
+        if (isfinite(x)) e = fmax(e, x);
     }
-    red[threadIdx.x] = m;
+    rv[threadIdx.x] = m;
+    re[threadIdx.x] = e;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+        if (threadIdx.x < o) {
+            rv[threadIdx.x] = fmax(rv[threadIdx.x], rv[threadIdx.x + o]);
+            re[threadIdx.x] = fmax(re[threadIdx.x], re[threadIdx.x + o]);
+        }
         __syncthreads();
     }
-    if (threadIdx.x == 0) out[s] = any_nan ? __longlong_as_double(0x7ff8000000000000LL) : red[0];
+    if (threadIdx.x == 0) {
+        double *p = partial + 2 * ((size_t)s * gridDim.x + blockIdx.x);
+        p[0] = any_nan ? __longlong_as_double(0x7ff8000000000000LL) : rv[0];
+        p[1] = re[0];
+    }
+}
+
+__global__ void k_scen_max_final(const double *partial, int nb, int n_scen, double *v0max,
+                                 double *ext) {
+    const int s = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    if (s >= n_scen) return;
+    double m = -INFINITY, e = 0.0;
+    bool nan = false;
+    for (int b = lane; b < nb; b += 32) {
+        const double *p = partial + 2 * ((size_t)s * nb + b);
+        if (isnan(p[0])) nan = true;
+        else m = fmax(m, p[0]);
+        e = fmax(e, p[1]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        e = fmax(e, __shfl_xor_sync(0xffffffffu, e, o));
+    }
+    nan = __any_sync(0xffffffffu, nan);
+    if (lane == 0) {
+        v0max[s] = nan ? __longlong_as_double(0x7ff8000000000000LL) : m;
+        if (ext) ext[s] = e;
+    }
 }
 
 // -- exclusive scan (block-local, then block totals) --
@@ -2029,9 +2083,13 @@ void launch_near_lists(const StepArgs &a, cudaStream_t s) {
 void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s) {
     if (a.n > 0) k_pair_counts<<<nblk(a.n, 128), 128, 0, s>>>(a, counts);
 }
-void launch_v0max(const StepArgs &a, double *out, cudaStream_t s) {
-    if (a.n_scen > 0) k_v0max<<<a.n_scen, 256, 0, s>>>(a, out);
+void launch_scen_max(const StepArgs &a, double *v0max, double *ext, double *partial,
+                     cudaStream_t s) {
+    if (a.n_scen <= 0) return;
+    k_scen_max_partial<<<dim3(V0MAX_B, a.n_scen), 256, 0, s>>>(a, partial);
+    k_scen_max_final<<<(a.n_scen + 7) / 8, 256, 0, s>>>(partial, V0MAX_B, a.n_scen, v0max, ext);
 }
+int scen_max_partials(int n_scen) { return 2 * V0MAX_B * (n_scen > 0 ? n_scen : 1); }
 void launch_wall_prep(const double *raw, double *walls, float4 *wf, int nw, cudaStream_t s) {
     if (nw > 0) k_wall_prep<<<nblk(nw, 128), 128, 0, s>>>(raw, walls, wf, nw);
 }
