@@ -43,6 +43,9 @@ struct cd_ctx {
     int64_t wall_idx_cap = 0;
     double *noise_f = nullptr, *noise_m = nullptr;
     bool noise_pending = false;
+    int *tgt = nullptr;                              // per-agent target index
+    double2 *navmap = nullptr;                       // all scenarios' direction maps
+    std::vector<std::vector<double>> nav_host;       // per scenario: x maps then y maps
     unsigned long long *vmax = nullptr;
     double *v0max = nullptr, *dt = nullptr, *time_tot = nullptr;
     double *ext = nullptr, *max_partial = nullptr;      // per-scenario max extent, scratch
@@ -123,6 +126,8 @@ StepArgs args_of(cd_ctx *c, int nodes) {
     a.wall_idx = c->wall_idx;
     a.noise_f = c->noise_f;
     a.noise_m = c->noise_m;
+    a.tgt = c->tgt;
+    a.navmap = c->navmap;
     a.vmax = c->vmax;
     a.v0max = c->v0max;
     a.dt = c->dt;
@@ -160,7 +165,7 @@ void release(cd_ctx *c) {
                     c->noise_f, c->noise_m, c->vmax, c->v0max, c->dt, c->time_tot,
                     c->err, c->work, c->diag, c->aos, c->nl_cnt, c->nl_off, c->nl_fwd,
                     c->nl_scan, c->nl_idx, c->nl_res, c->fw_cnt, c->fw_off, c->fw_scan,
-                    c->fw_pairs, c->ext, c->max_partial};
+                    c->fw_pairs, c->ext, c->max_partial, c->tgt, c->navmap};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -364,7 +369,8 @@ int check_device_error(cd_ctx *c) {
 }
 
 int prepare_step(cd_ctx *c, int nodes) {
-    if (nodes & ~CD_NODE_ALL) return fail(c, CD_ERR_INVALID_VALUE, "unknown node flags");
+    if (nodes & ~(CD_NODE_ALL | CD_NODE_NAVIGATION))
+        return fail(c, CD_ERR_INVALID_VALUE, "unknown node flags");
     if (!c->have_records) return fail(c, CD_ERR_INVALID_VALUE, "no agents uploaded");
     if ((nodes & CD_NODE_AGENT_OBSTACLE) && c->walls_dirty && c->nw > 0) {
         if (c->walls_host.empty())
@@ -420,6 +426,7 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     c->nscen = (int)n_scenarios;
     c->scen_host.assign(scen, scen + n_scenarios);
     c->scen_dev.resize(n_scenarios);
+    c->nav_host.resize(n_scenarios);
     c->scen_of_host.resize(std::max<int64_t>(n, 1));
     std::fill(c->off, c->off + CD_F_COUNT, -1);
     int64_t base = 0;
@@ -433,6 +440,8 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
         d.cell_base = (int)base;
         d.agent_begin = (int)sc.agent_begin; d.agent_count = (int)sc.agent_count;
         d.wall_begin = (int)sc.wall_begin; d.wall_count = (int)sc.wall_count;
+        d.nav_x0 = 0.0; d.nav_y0 = 0.0; d.nav_step = 1.0;
+        d.nav_nx = 0; d.nav_ny = 0; d.nav_targets = 0; d.nav_off = 0;
         base += sc.nx * sc.ny;
         for (int64_t i = sc.agent_begin; i < sc.agent_begin + sc.agent_count; ++i)
             c->scen_of_host[i] = (int)s;
@@ -467,6 +476,7 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->wall_start, ncells + 1));
     step(dalloc(c, &c->noise_f, 2 * n));
     step(dalloc(c, &c->noise_m, n));
+    step(dalloc(c, &c->tgt, n));
     step(dalloc(c, &c->vmax, n_scenarios));
     step(dalloc(c, &c->v0max, n_scenarios));
     step(dalloc(c, &c->ext, n_scenarios));
@@ -562,6 +572,9 @@ int cd_upload_agents(cd_ctx *c, const void *records, int64_t n, int64_t itemsize
         long long offl[CD_F_COUNT];
         for (int k = 0; k < CD_F_COUNT; ++k) offl[k] = off[k];
         cdk::launch_aos_to_soa(c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
+        const bool have_target = off[CD_F_TARGET] >= 0 && off[CD_F_TARGET] + 8 <= itemsize;
+        cdk::launch_targets(c->aos, itemsize, have_target ? off[CD_F_TARGET] : -1, (int)n, c->tgt,
+                            c->stream);
     }
     StepArgs a = args_of(c, 0);
     cdk::launch_scen_max(a, c->v0max, c->ext, c->max_partial, c->stream);
@@ -613,6 +626,56 @@ int cd_set_walls(cd_ctx *c, const double *walls, int64_t n_walls) {
     c->walls_dirty = true;
     CUDA_OR_FAIL(c, cudaGetLastError());
     CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    return CD_OK;
+}
+
+int cd_set_direction_maps(cd_ctx *c, int64_t scenario, int64_t n_targets, const double *dir_x,
+                          const double *dir_y, int64_t ny, int64_t nx, double minx, double miny,
+                          double step) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (scenario < 0 || scenario >= c->nscen) return fail(c, CD_ERR_INVALID_VALUE, "bad scenario");
+    if (n_targets < 0) return fail(c, CD_ERR_INVALID_VALUE, "negative target count");
+    if (n_targets > 0) {
+        if (!dir_x || !dir_y) return fail(c, CD_ERR_INVALID_VALUE, "NULL direction map");
+        if (nx < 1 || ny < 1 || nx > INT32_MAX || ny > INT32_MAX || n_targets > INT32_MAX)
+            return fail(c, CD_ERR_INVALID_VALUE, "bad direction map shape");
+        if (!(step > 0) || !std::isfinite(step) || !std::isfinite(minx) || !std::isfinite(miny))
+            return fail(c, CD_ERR_INVALID_VALUE, "bad meshgrid origin or step");
+    }
+    const int64_t cells = n_targets * ny * nx;
+    std::vector<double> &h = c->nav_host[scenario];
+    h.assign(dir_x, dir_x + (n_targets > 0 ? cells : 0));
+    if (n_targets > 0) h.insert(h.end(), dir_y, dir_y + cells);
+    ScenDev &d = c->scen_dev[scenario];
+    d.nav_targets = (int)n_targets;
+    d.nav_nx = n_targets > 0 ? (int)nx : 0;
+    d.nav_ny = n_targets > 0 ? (int)ny : 0;
+    d.nav_x0 = minx;
+    d.nav_y0 = miny;
+    d.nav_step = n_targets > 0 ? step : 1.0;
+    // rebuild the interleaved device copy of every scenario's maps
+    std::vector<double> all;
+    for (int s = 0; s < c->nscen; ++s) {
+        ScenDev &e = c->scen_dev[s];
+        e.nav_off = (long long)(all.size() / 2);
+        const std::vector<double> &m = c->nav_host[s];
+        const size_t k = m.size() / 2;
+        for (size_t q = 0; q < k; ++q) {
+            all.push_back(m[q]);
+            all.push_back(m[k + q]);
+        }
+    }
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    if (c->navmap) cudaFree(c->navmap);
+    c->navmap = nullptr;
+    if (!all.empty()) {
+        if (int rc = dalloc(c, &c->navmap, (int64_t)(all.size() / 2))) return rc;
+        CUDA_OR_FAIL(c, cudaMemcpy(c->navmap, all.data(), sizeof(double) * all.size(),
+                                   cudaMemcpyHostToDevice));
+    }
+    CUDA_OR_FAIL(c, cudaMemcpy(c->scen, c->scen_dev.data(), sizeof(ScenDev) * c->nscen,
+                               cudaMemcpyHostToDevice));
+    if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; c->graph_nodes = -1; }
     return CD_OK;
 }
 

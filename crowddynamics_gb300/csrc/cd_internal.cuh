@@ -25,7 +25,7 @@ constexpr int ERR_NOT_FINITE = 1;
 
 // Node flags (mirror CD_NODE_* of include/cdgpu.h).
 constexpr int N_FLUCT = 1, N_ORIENT = 2, N_ADJUST = 4, N_AGENT = 8,
-              N_WALL = 16, N_INTEG = 32, N_RESET = 64;
+              N_WALL = 16, N_INTEG = 32, N_RESET = 64, N_NAV = 128;
 
 struct ScenDev {
     double x0, y0, cell;
@@ -35,6 +35,10 @@ struct ScenDev {
     int cell_base;              // first flat cell of this scenario
     int agent_begin, agent_count;
     int wall_begin, wall_count;
+    // navigation: direction maps on a meshgrid (origin, spacing), targets x ny x nx
+    double nav_x0, nav_y0, nav_step;
+    int nav_nx, nav_ny, nav_targets;
+    long long nav_off;           // first double2 of the scenario's maps
 };
 
 struct StepArgs {
@@ -57,6 +61,9 @@ struct StepArgs {
     const int *wall_start, *wall_idx;   // per-cell CSR of wall ids
     // fluctuation (host-drawn)
     const double *noise_f, *noise_m;
+    // navigation
+    const int *tgt;              // per agent: target index, -1 for none
+    const double2 *navmap;       // (dir_x, dir_y) per map cell
     // timestep
     unsigned long long *vmax;    // per scenario, ordered bits of max |v|
     const double *v0max;         // per scenario max target_velocity
@@ -145,6 +152,9 @@ void launch_wall_prep(const double *raw, double *walls, float4 *walls_f, int nw,
                       cudaStream_t s);
 void launch_aos_to_soa(const char *aos, long long itemsize, const long long *off,
                        int n, int body, double *const *col, cudaStream_t s);
+// Per-agent target index (int64 record field at `off_target`, or -1 if < 0).
+void launch_targets(const char *aos, long long itemsize, long long off_target, int n, int *tgt,
+                    cudaStream_t s);
 void launch_soa_to_aos(char *aos, long long itemsize, const long long *off,
                        int n, int body, const double *const *col, cudaStream_t s);
 double fp64_peak_gflops();

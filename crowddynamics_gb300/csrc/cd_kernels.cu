@@ -1150,13 +1150,33 @@ __device__ __forceinline__ int enumerate_candidates(const StepArgs &a, const Sce
     return nl;
 }
 
-// Per-agent terms before agent-agent: the force (and torque) array's value,
-// fluctuation, orientation and adjusting, in the reference's node order.
+// Navigation (simulation/logic.py:152-165, core/steering/navigation.py:60-78,
+// core/steering/quickest_path.py:40-43): an agent with target t in range
+// takes map t's direction at ((position - origin) / step) truncated toward
+// zero, (y, x) as (row, column), when inside the map.  Non-finite quotients
+// leave the direction unchanged.
+__device__ __forceinline__ void navigate(const StepArgs &a, const ScenDev &sc, const int i) {
+    const int t = a.tgt[i];
+    if (t < 0 || t >= sc.nav_targets) return;
+    double *const *col = a.col;
+    const double tx = trunc((col[X][i] - sc.nav_x0) / sc.nav_step);
+    const double ty = trunc((col[Y][i] - sc.nav_y0) / sc.nav_step);
+    if (!(tx >= 0.0 && tx < (double)sc.nav_nx && ty >= 0.0 && ty < (double)sc.nav_ny)) return;
+    const double2 e = a.navmap[sc.nav_off + ((long long)t * sc.nav_ny + (long long)ty) * sc.nav_nx +
+                               (long long)tx];
+    col[E0X][i] = e.x;
+    col[E0Y][i] = e.y;
+}
+
+// Per-agent terms before agent-agent: navigation, the force (and torque)
+// array's value, fluctuation, orientation and adjusting, in the reference's
+// node order.
 template <int BODY>
 __device__ __forceinline__ void agent_prologue(const StepArgs &a, const int i, double &fx,
                                                double &fy, double &tq, double &phi0) {
     double *const *col = a.col;
     const int nodes = a.nodes;
+    if (nodes & N_NAV) navigate(a, a.scen[a.scen_of[i]], i);
     fx = col[FX][i];
     fy = col[FY][i];
     tq = (BODY == 1) ? col[TORQUE][i] : 0.0;
@@ -1817,9 +1837,9 @@ __constant__ FieldMap kMapTC[34] = {
     {8, 0, RTS}, {10, 0, INERTIA}, {12, 0, W0}, {22, 0, PHI}, {23, 0, OMEGA},
     {24, 0, PHI0}, {25, 0, TORQUE}, {26, 0, TORQUE_PREV}, {27, 0, TAU_ROT}};
 // Columns the step writes (downloaded back into the records).
-__constant__ int kOutCirc[8] = {X, Y, VX, VY, FX, FY, FPX, FPY};
-__constant__ int kOutTC[17] = {X, Y, VX, VY, FX, FY, FPX, FPY, XLS, YLS, XRS, YRS,
-                               PHI, OMEGA, PHI0, TORQUE, TORQUE_PREV};
+__constant__ int kOutCirc[10] = {X, Y, VX, VY, FX, FY, FPX, FPY, E0X, E0Y};
+__constant__ int kOutTC[19] = {X, Y, VX, VY, FX, FY, FPX, FPY, XLS, YLS, XRS, YRS,
+                               PHI, OMEGA, PHI0, TORQUE, TORQUE_PREV, E0X, E0Y};
 
 struct OffTable { long long off[32]; };
 struct ColPtrs { double *p[NCOL]; };
@@ -1855,7 +1875,7 @@ __global__ void k_soa_to_aos(char *aos, long long itemsize, OffTable off, int n,
     char *rec = aos + (size_t)i * itemsize;
     const FieldMap *map = body == 0 ? kMapCirc : kMapTC;
     const int *outs = body == 0 ? kOutCirc : kOutTC;
-    int nm = body == 0 ? 19 : 34, no = body == 0 ? 8 : 17;
+    int nm = body == 0 ? 19 : 34, no = body == 0 ? 10 : 19;
     for (int k = 0; k < nm; ++k) {
         bool written = false;
         for (int q = 0; q < no; ++q) written |= (outs[q] == map[k].col);
@@ -1863,6 +1883,23 @@ __global__ void k_soa_to_aos(char *aos, long long itemsize, OffTable off, int n,
         if (!written || o < 0) continue;
         st_rec(rec, o + 8 * map[k].comp, cols.p[map[k].col][i]);
     }
+}
+
+// The target field of the packed records is an int64 at any byte offset (2 in
+// the reference dtypes, after two bools): read byte by byte, little-endian.
+__global__ void k_targets(const char *aos, long long itemsize, long long off, int n, int *tgt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    long long t = -1;
+    if (off >= 0) {
+        const unsigned char *p =
+            reinterpret_cast<const unsigned char *>(aos + (size_t)i * itemsize + off);
+        unsigned long long v = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v |= (unsigned long long)p[k] << (8 * k);
+        t = (long long)v;
+    }
+    tgt[i] = (t >= 0 && t <= 0x7fffffffLL) ? (int)t : -1;
 }
 
 __global__ void k_fp64_fma(double *out, int iters, double b, double c) {
@@ -2101,6 +2138,10 @@ void launch_aos_to_soa(const char *aos, long long itemsize, const long long *off
     ColPtrs c;
     for (int k = 0; k < NCOL; ++k) c.p[k] = col[k];
     k_aos_to_soa<<<nblk(n, 128), 128, 0, s>>>(aos, itemsize, t, n, body, c);
+}
+void launch_targets(const char *aos, long long itemsize, long long off_target, int n, int *tgt,
+                    cudaStream_t s) {
+    if (n > 0) k_targets<<<nblk(n, 256), 256, 0, s>>>(aos, itemsize, off_target, n, tgt);
 }
 void launch_soa_to_aos(char *aos, long long itemsize, const long long *off, int n, int body,
                        const double *const *col, cudaStream_t s) {

@@ -117,6 +117,24 @@ class DeviceBatch:
         rows = walls_as_rows(walls)
         self._chk(self._lib.cd_set_walls(self._ctx, N.ptr(rows), len(rows)))
 
+    def set_direction_maps(self, scenario, dir_x, dir_y, minx, miny, step):
+        """Direction maps of one scenario for NODE_NAVIGATION: dir_x, dir_y of
+        shape (targets, ny, nx) or (ny, nx), indexed [row = y, column = x] on
+        the meshgrid with origin (minx, miny) and spacing ``step``.  Empty
+        (0 targets) removes the scenario's maps."""
+        mx = np.asarray(dir_x, dtype=np.float64)
+        my = np.asarray(dir_y, dtype=np.float64)
+        if mx.ndim == 2:
+            mx, my = mx[None], my[None]
+        if mx.ndim != 3 or mx.shape != my.shape:
+            raise InvalidValue('direction maps must have shape (targets, ny, nx)')
+        mx = np.ascontiguousarray(mx)
+        my = np.ascontiguousarray(my)
+        t, ny, nx = mx.shape
+        self._chk(self._lib.cd_set_direction_maps(self._ctx, int(scenario), t, N.ptr(mx),
+                                                  N.ptr(my), ny, nx, float(minx), float(miny),
+                                                  float(step)))
+
     def set_noise(self, force, torque=None):
         f = np.ascontiguousarray(force, dtype=np.float64)
         if f.shape != (self.n_agents, 2):

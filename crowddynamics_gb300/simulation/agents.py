@@ -84,14 +84,15 @@ BODY_CIRCULAR = 0
 BODY_THREE_CIRCLE = 1
 
 #: Field identifiers of the C ABI's offset table, in ``CD_F_*`` order.  Each
-#: entry names a float64 field (vectors are two consecutive float64s).
+#: entry names a float64 field (vectors are two consecutive float64s), except
+#: ``target`` (int64).
 FIELD_NAMES = (
     'position', 'velocity', 'target_direction', 'force', 'force_prev',
     'radius', 'r_t', 'r_s', 'r_ts', 'mass', 'inertia_rot', 'target_velocity',
     'target_angular_velocity', 'tau_adj', 'k_soc', 'tau_0', 'mu', 'kappa',
     'damping', 'std_rand_force', 'position_ls', 'position_rs', 'orientation',
     'angular_velocity', 'target_orientation', 'torque', 'torque_prev',
-    'tau_rot', 'std_rand_torque',
+    'tau_rot', 'std_rand_torque', 'target',
 )
 
 

@@ -14,7 +14,7 @@ shape the cell size; the kernels use the reference's constants 3.0 m and
 import numpy as np
 
 from crowddynamics_gb300 import _native as N
-from crowddynamics_gb300.scenarios import draw_noise, lookup_direction
+from crowddynamics_gb300.scenarios import draw_noise
 from crowddynamics_gb300.simulation.base import LogicNodeBase
 
 
@@ -100,19 +100,22 @@ class Orientation(DeviceNode):
     FLAG = N.NODE_ORIENTATION
 
 
-class Navigation(LogicNode):
-    """Target direction from a precomputed direction map by nearest-cell
-    lookup (``simulation/logic.py:135-165`` with
-    ``core/steering/navigation.py:69-78``); runs on the host.  The map is
-    ``(mx, my)`` indexed [y, x] on a grid of ``step`` from ``origin``."""
-    direction_map = None
+class Navigation(DeviceNode):
+    """Target direction from direction maps (``simulation/logic.py:135-165``):
+    every agent whose ``target`` is t takes map t's direction at its nearest
+    meshgrid index (``core/steering/navigation.py:69-78`` with the indicer of
+    ``core/steering/quickest_path.py:40-43``); other agents and agents outside
+    the map keep theirs.  Runs on the device.  The reference computes the maps
+    by fast marching (``field.navigation_to_target``); here they are inputs:
+    ``direction_maps`` is a list of (dir_x, dir_y) arrays indexed [y, x], one
+    per target, on the meshgrid with origin ``origin`` and spacing ``step``."""
+    FLAG = N.NODE_NAVIGATION
+    direction_maps = None
     step = 0.1
     origin = (0.0, 0.0)
 
     def update(self):
-        if self.direction_map is None:
+        if not self.direction_maps:
             return
-        a = self.simulation.agents.array
-        a['target_direction'] = lookup_direction(
-            a['position'], self.direction_map, self.step, self.origin[0], self.origin[1],
-            defaults=a['target_direction'])
+        self.simulation._use_direction_maps(self)
+        super().update()

@@ -25,8 +25,8 @@ from crowddynamics_gb300.simulation.field import Field
 from crowddynamics_gb300.simulation.logic import (
     AgentAgentInteractions, DeviceNode, Integrator)
 
-_ORDER = [N.NODE_FLUCTUATION, N.NODE_ORIENTATION, N.NODE_ADJUSTING, N.NODE_AGENT_AGENT,
-          N.NODE_AGENT_OBSTACLE, N.NODE_INTEGRATE, N.NODE_RESET]
+_ORDER = [N.NODE_FLUCTUATION, N.NODE_NAVIGATION, N.NODE_ORIENTATION, N.NODE_ADJUSTING,
+          N.NODE_AGENT_AGENT, N.NODE_AGENT_OBSTACLE, N.NODE_INTEGRATE, N.NODE_RESET]
 _RANK = {f: k for k, f in enumerate(_ORDER)}
 
 
@@ -127,6 +127,19 @@ class MultiAgentSimulation:
             self.agents._mirror = _Mirror(self)
             self._time_offset = self.data.get('time_tot', 0.0) if 'time_tot' in self.data else 0.0
         return self._batch
+
+    def _use_direction_maps(self, node):
+        """Upload the Navigation node's maps when they change."""
+        b = self._ensure_batch()
+        key = (id(node), tuple((id(mx), id(my)) for mx, my in node.direction_maps),
+               float(node.step), tuple(node.origin))
+        if getattr(self, '_nav_key', None) != key or getattr(self, '_nav_batch', None) is not b:
+            self._flush()
+            mx = np.stack([np.asarray(m[0], dtype=np.float64) for m in node.direction_maps])
+            my = np.stack([np.asarray(m[1], dtype=np.float64) for m in node.direction_maps])
+            b.set_direction_maps(0, mx, my, node.origin[0], node.origin[1], node.step)
+            self._nav_key = key
+            self._nav_batch = b
 
     def _queue_device_node(self, node):
         flag = node.FLAG

@@ -30,6 +30,10 @@
  *   CD_NODE_RESET ......... Reset.update, simulation/logic.py:59-64
  *   CD_NODE_FLUCTUATION ... Fluctuation.update, simulation/logic.py:78-86
  *                           (noise drawn on the host, passed by cd_set_noise)
+ *   CD_NODE_NAVIGATION .... Navigation.update, simulation/logic.py:135-165, with
+ *                           getdefault, core/steering/navigation.py:69-78, and the
+ *                           meshgrid indicer, core/steering/quickest_path.py:40-43
+ *                           (direction maps passed by cd_set_direction_maps)
  *   cd_upload_agents /
  *   cd_download_agents .... the in-place numpy structured agent arrays the
  *                           nodes read and write (simulation/agents.py:447-448)
@@ -65,7 +69,8 @@ extern "C" {
 #define CD_NODE_AGENT_OBSTACLE 16
 #define CD_NODE_INTEGRATE 32
 #define CD_NODE_RESET 64
-#define CD_NODE_ALL 127
+#define CD_NODE_ALL 127          /* the standard tree (navigation excluded) */
+#define CD_NODE_NAVIGATION 128   /* runs first: target direction from the maps */
 
 /* ---- float64 fields of an agent record (offset-table order) ------------ */
 enum {
@@ -75,7 +80,9 @@ enum {
     CD_F_TAU_ADJ, CD_F_K_SOC, CD_F_TAU_0, CD_F_MU, CD_F_KAPPA, CD_F_DAMPING,
     CD_F_STD_RAND_FORCE, CD_F_POSITION_LS, CD_F_POSITION_RS, CD_F_ORIENTATION,
     CD_F_ANGULAR_VELOCITY, CD_F_TARGET_ORIENTATION, CD_F_TORQUE,
-    CD_F_TORQUE_PREV, CD_F_TAU_ROT, CD_F_STD_RAND_TORQUE, CD_F_COUNT
+    CD_F_TORQUE_PREV, CD_F_TAU_ROT, CD_F_STD_RAND_TORQUE,
+    CD_F_TARGET,                  /* int64: target index, -1 for none */
+    CD_F_COUNT
 };
 
 /* One scenario of a batch.  The cell grid covers [x0, x0 + nx*cell_size) x
@@ -106,7 +113,8 @@ void cd_destroy(cd_ctx *ctx);
 
 /* Copy `n` (= total agents) packed host records of `itemsize` bytes into the
  * device.  `field_offsets` holds CD_F_COUNT byte offsets (-1 = absent);
- * float64 fields must be 4-byte aligned.  Recomputes timestep maxima. */
+ * float64 fields must be 4-byte aligned, the int64 CD_F_TARGET may sit at
+ * any offset.  Recomputes timestep maxima. */
 int cd_upload_agents(cd_ctx *ctx, const void *records, int64_t n,
                      int64_t itemsize, const int64_t *field_offsets);
 /* Write the device state back into `n` packed host records.  Whole records
@@ -119,6 +127,17 @@ int cd_download_agents(cd_ctx *ctx, void *records, int64_t n, int64_t itemsize,
  * among scenarios by their wall ranges.  Walls are binned into the cells of
  * their scenario's grid. */
 int cd_set_walls(cd_ctx *ctx, const double *walls, int64_t n_walls);
+
+/* Direction maps of scenario `scenario` for CD_NODE_NAVIGATION: for each of
+ * `n_targets` targets, dir_x and dir_y (ny x nx float64, row = y) on the
+ * meshgrid with origin (minx, miny) and spacing `step`, targets stored one
+ * after another.  An agent whose `target` field is t in [0, n_targets) takes
+ * map t's entry at index ((position - origin) / step) truncated toward zero,
+ * (y, x) as (row, column), when inside the map; other agents keep their
+ * target direction.  n_targets = 0 removes the scenario's maps. */
+int cd_set_direction_maps(cd_ctx *ctx, int64_t scenario, int64_t n_targets,
+                          const double *dir_x, const double *dir_y, int64_t ny, int64_t nx,
+                          double minx, double miny, double step);
 
 /* Host-drawn fluctuation added by the next step that runs
  * CD_NODE_FLUCTUATION: force (n x 2) and torque (n; ignored for Circular,

@@ -46,7 +46,7 @@ enum {
     F_TARGET_ANGULAR_VELOCITY, F_TAU_ADJ, F_K_SOC, F_TAU_0, F_MU, F_KAPPA,
     F_DAMPING, F_STD_RAND_FORCE, F_POSITION_LS, F_POSITION_RS, F_ORIENTATION,
     F_ANGULAR_VELOCITY, F_TARGET_ORIENTATION, F_TORQUE, F_TORQUE_PREV,
-    F_TAU_ROT, F_STD_RAND_TORQUE, F_COUNT
+    F_TAU_ROT, F_STD_RAND_TORQUE, F_TARGET, F_COUNT
 };
 
 enum { BODY_CIRCULAR = 0, BODY_THREE_CIRCLE = 1 };
@@ -54,7 +54,8 @@ enum { BODY_CIRCULAR = 0, BODY_THREE_CIRCLE = 1 };
 enum {
     ORC_FLUCTUATION = 1, ORC_ORIENTATION = 2, ORC_ADJUSTING = 4,
     ORC_AGENT_AGENT = 8, ORC_AGENT_OBSTACLE = 16, ORC_INTEGRATE = 32,
-    ORC_RESET = 64
+    ORC_RESET = 64,
+    ORC_NAVIGATION = 128
 };
 
 /* core/interactions.py:45 and core/motion/power_law.py:52 */
@@ -787,6 +788,52 @@ void orc_add_noise(char *base, int64_t n, int64_t itemsize, const int64_t *off, 
     }
 }
 
+/* Direction maps for Navigation: n_targets maps of ny x nx (row = y) on the
+ * meshgrid (minx, miny, step); set before orc_step, used while it runs. */
+static struct {
+    int64_t n_targets, ny, nx;
+    double minx, miny, step;
+    const double *dx, *dy;
+} g_nav;
+
+void orc_set_navigation(int64_t n_targets, const double *dx, const double *dy, int64_t ny,
+                        int64_t nx, double minx, double miny, double step) {
+    g_nav.n_targets = n_targets;
+    g_nav.dx = dx;
+    g_nav.dy = dy;
+    g_nav.ny = ny;
+    g_nav.nx = nx;
+    g_nav.minx = minx;
+    g_nav.miny = miny;
+    g_nav.step = step;
+}
+
+/* Navigation.update (simulation/logic.py:152-165): for every target t, the
+ * agents with target == t take getdefault(indices, dir_map_t, e0)
+ * (core/steering/navigation.py:69-78) with indices the meshgrid indicer
+ * ((position - (minx, miny)) / step).astype(int64) (core/steering/
+ * quickest_path.py:40-43) flipped to (row = y, column = x); is_inside
+ * (navigation.py:60-64) keeps e0 outside the map.  astype(int64) truncates
+ * toward zero; non-finite quotients leave e0 unchanged (numpy on x86 maps
+ * them to INT64_MIN, outside every map). */
+void orc_navigation(char *base, int64_t n, int64_t itemsize, const int64_t *off) {
+    arr_t A = {base, itemsize, off};
+    if (off[F_TARGET] < 0) return;
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t t;
+        memcpy(&t, base + i * itemsize + off[F_TARGET], sizeof t);
+        if (t < 0 || t >= g_nav.n_targets) continue;
+        v2 p = ld2(&A, i, F_POSITION);
+        double qx = (p.x - g_nav.minx) / g_nav.step;
+        double qy = (p.y - g_nav.miny) / g_nav.step;
+        double tx = trunc(qx), ty = trunc(qy);
+        if (!(tx >= 0.0 && tx < (double)g_nav.nx && ty >= 0.0 && ty < (double)g_nav.ny)) continue;
+        int64_t k = (t * g_nav.ny + (int64_t)ty) * g_nav.nx + (int64_t)tx;
+        v2 e = {g_nav.dx[k], g_nav.dy[k]};
+        st2(&A, i, F_TARGET_DIRECTION, e);
+    }
+}
+
 /* One MultiAgentSimulation.update() (simulation/multiagent.py:51-55) for the
  * standard tree Reset << Integrator << (Fluctuation, Adjusting << Orientation,
  * AgentAgentInteractions, AgentObstacleInteractions), post-order.  `flags`
@@ -797,6 +844,7 @@ double orc_step(char *base, int64_t n, int64_t itemsize, const int64_t *off, int
                 const double *noise_f, const double *noise_m,
                 double dt_min, double dt_max, int nthreads) {
     double dt = 0.0;
+    if (flags & ORC_NAVIGATION) orc_navigation(base, n, itemsize, off);
     if (flags & ORC_FLUCTUATION) orc_add_noise(base, n, itemsize, off, body, noise_f, noise_m);
     if ((flags & ORC_ORIENTATION) && body == BODY_THREE_CIRCLE)
         orc_orient_towards_target_direction(base, n, itemsize, off);

@@ -21,6 +21,7 @@ ORC_AGENT_OBSTACLE = 16
 ORC_INTEGRATE = 32
 ORC_RESET = 64
 ORC_FULL = 127
+ORC_NAVIGATION = 128
 
 BODY_CIRCULAR = 0
 BODY_THREE_CIRCLE = 1
@@ -32,7 +33,7 @@ FIELD_NAMES = (
     'target_angular_velocity', 'tau_adj', 'k_soc', 'tau_0', 'mu', 'kappa',
     'damping', 'std_rand_force', 'position_ls', 'position_rs', 'orientation',
     'angular_velocity', 'target_orientation', 'torque', 'torque_prev',
-    'tau_rot', 'std_rand_torque',
+    'tau_rot', 'std_rand_torque', 'target',
 )
 
 
@@ -83,6 +84,10 @@ def lib():
         L.orc_cdm.restype = d
         L.orc_wrap_to_pi.argtypes = [d]
         L.orc_wrap_to_pi.restype = d
+        L.orc_set_navigation.argtypes = [i64, P, P, i64, i64, d, d, d]
+        L.orc_set_navigation.restype = None
+        L.orc_navigation.argtypes = [P, i64, i64, P]
+        L.orc_navigation.restype = None
         _lib = L
     return _lib
 
@@ -200,10 +205,23 @@ def wrap_to_pi(x):
 
 
 def step(agents, grid, walls=None, noise_f=None, noise_m=None, flags=ORC_FULL,
-         dt_min=0.001, dt_max=0.01, nthreads=1):
+         dt_min=0.001, dt_max=0.01, nthreads=1, nav=None):
     """One MultiAgentSimulation.update() of the standard node tree
-    (simulation/multiagent.py:51-55); returns dt."""
+    (simulation/multiagent.py:51-55); returns dt.  ``nav`` = (dir_x, dir_y,
+    minx, miny, step) with dir_x, dir_y of shape (targets, ny, nx) for
+    ORC_NAVIGATION."""
     _check(agents)
+    keep = None
+    if nav is not None:
+        mx, my, minx, miny, step_ = nav
+        mx = np.ascontiguousarray(mx, dtype=np.float64)
+        my = np.ascontiguousarray(my, dtype=np.float64)
+        keep = (mx, my)
+        lib().orc_set_navigation(mx.shape[0], _ptr(mx), _ptr(my), mx.shape[1], mx.shape[2],
+                                 float(minx), float(miny), float(step_))
+    else:
+        lib().orc_set_navigation(0, None, None, 0, 0, 0.0, 0.0, 1.0)
+        flags &= ~ORC_NAVIGATION
     off = _offsets(agents)
     w = np.zeros((0, 4)) if walls is None or len(walls) == 0 else \
         np.ascontiguousarray(np.asarray(walls).view(np.float64).reshape(-1, 4))
@@ -218,6 +236,19 @@ def step(agents, grid, walls=None, noise_f=None, noise_m=None, flags=ORC_FULL,
     if dt != dt:
         raise ValueError('non-finite agent position')
     return dt
+
+
+def navigation(agents, dir_x, dir_y, minx, miny, step):
+    """Navigation.update alone: target directions from the maps (targets, ny,
+    nx) for the agents whose ``target`` names a map."""
+    _check(agents)
+    mx = np.ascontiguousarray(dir_x, dtype=np.float64)
+    my = np.ascontiguousarray(dir_y, dtype=np.float64)
+    lib().orc_set_navigation(mx.shape[0], _ptr(mx), _ptr(my), mx.shape[1], mx.shape[2],
+                             float(minx), float(miny), float(step))
+    off = _offsets(agents)
+    lib().orc_navigation(_ptr(agents), len(agents), agents.dtype.itemsize, _ptr(off))
+    lib().orc_set_navigation(0, None, None, 0, 0, 0.0, 0.0, 1.0)
 
 
 def cell_list(x, y, grid):

@@ -247,6 +247,64 @@ def load():
     return ns
 
 
+def _extract(rel, names, ns):
+    """Execute the top-level definitions ``names`` of a reference file (parsed
+    unchanged, other statements and imports left out) in ``ns``."""
+    import ast
+    path = os.path.join(REFERENCE_ROOT, rel)
+    tree = ast.parse(open(path).read(), path)
+    body = [n for n in tree.body
+            if (isinstance(n, ast.FunctionDef) and n.name in names) or
+            (isinstance(n, ast.Assign) and
+             any(isinstance(t, ast.Name) and t.id in names for t in n.targets))]
+    missing = set(names) - {getattr(n, 'name', None) or n.targets[0].id for n in body}
+    if missing:
+        raise RuntimeError('not found in %s: %s' % (rel, sorted(missing)))
+    exec(compile(ast.Module(body=body, type_ignores=[]), path, 'exec'), ns)
+
+
+_nav = None
+
+
+def load_navigation():
+    """The reference's navigation lookup: ``meshgrid`` (with its indicer) from
+    core/steering/quickest_path.py:22-49 and ``is_inside`` / ``getdefault``
+    from core/steering/navigation.py:59-78.  Their modules import fast
+    marching, shapely and skimage, absent here, so only these definitions are
+    executed (with the numba stub)."""
+    global _nav
+    if _nav is not None:
+        return _nav
+    if not available():
+        raise RuntimeError('reference source tree not found at ' + REFERENCE_ROOT)
+    import typing
+    nb, _ = _make_numba()
+    ns = {'np': np, 'numba': nb, 'f8': nb.f8, 'i8': nb.i8, 'NamedTuple': typing.NamedTuple,
+          'Callable': typing.Callable, 'Tuple': typing.Tuple, 'Optional': typing.Optional}
+    _extract('crowddynamics/core/steering/quickest_path.py', ('MeshGrid', 'meshgrid'), ns)
+    _extract('crowddynamics/core/steering/navigation.py', ('is_inside', 'getdefault'), ns)
+    _nav = types.SimpleNamespace(meshgrid=ns['meshgrid'], getdefault=ns['getdefault'],
+                                 is_inside=ns['is_inside'])
+    return _nav
+
+
+def navigation(agents, dir_maps, step, bounds):
+    """Navigation.update (simulation/logic.py:152-165) with the reference's own
+    meshgrid indicer and getdefault, for precomputed maps: ``dir_maps`` is a
+    list of (dir_x, dir_y) per target on ``meshgrid(step, *bounds)``."""
+    nav = load_navigation()
+    mgrid = nav.meshgrid(step, *bounds)
+    for target in range(len(dir_maps)):
+        has_target = agents['target'] == target
+        if not has_target.size:
+            continue
+        indices = np.fliplr(mgrid.indicer(agents[has_target]['position']))
+        new_direction = nav.getdefault(indices, dir_maps[target],
+                                       agents[has_target]['target_direction'])
+        agents['target_direction'][has_target] = new_direction
+    return mgrid
+
+
 def configure_grid(x0, y0, cell, nx, ny):
     CellGrid.x0, CellGrid.y0, CellGrid.cell = float(x0), float(y0), float(cell)
     CellGrid.nx, CellGrid.ny = int(nx), int(ny)

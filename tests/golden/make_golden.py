@@ -157,14 +157,52 @@ def misc_cases():
     save('misc', wrap_x=x, wrap_y=w, dt_agents=a, dts=dts, dt_zero=np.float64(dt_zero))
 
 
+def navigation_cases():
+    """Navigation.update with the reference's meshgrid indicer and getdefault
+    on two seeded direction maps: agents on every target value (none, each
+    map, beyond the maps), positions inside, on grid lines, just below the
+    origin (truncation toward zero), beyond the far edge and far outside."""
+    rng = np.random.default_rng(31)
+    step, bounds = 0.25, (-2.0, 1.0, 8.0, 6.0)
+    mg = RL.load_navigation().meshgrid(step, *bounds)
+    ny, nx = mg.shape
+    ang = rng.uniform(0, 2 * np.pi, (2, ny, nx))
+    maps = [(np.cos(ang[k]), np.sin(ang[k])) for k in range(2)]
+    out = {}
+    for body in ('circular', 'three_circle'):
+        n = 400
+        a = new_agents(n, body)
+        p = np.column_stack([rng.uniform(-3.0, 9.0, n), rng.uniform(0.0, 7.0, n)])
+        edge = np.array([[-2.0, 1.0], [-2.1, 1.0], [-2.0, 0.9], [-2.24, 0.76], [-2.26, 1.0],
+                         [8.0, 6.0], [8.2, 6.2], [8.25, 6.25], [8.3, 6.0], [1e6, 3.0],
+                         [-1e6, 3.0], [0.0, 0.0], [3.0, 3.25], [3.125, 3.375]])
+        p[:len(edge)] = edge
+        a['position'] = p
+        a['target'] = rng.integers(-1, 4, n)          # -1 none, 0-1 maps, 2-3 beyond
+        a['target'][:len(edge)] = 0
+        a['target_direction'] = np.column_stack([np.full(n, 7.0), np.full(n, -7.0)])
+        before = a.copy()
+        RL.navigation(a, maps, step, bounds)
+        out[body + '_before'] = before
+        out[body + '_after'] = a
+    save('navigation', step=np.float64(step), bounds=np.array(bounds),
+         dir_x=np.stack([m[0] for m in maps]), dir_y=np.stack([m[1] for m in maps]), **out)
+
+
+CASES = {'scenarios': lambda: (
+             scenario_case('hallway_small', S.hallway(n=120, width=20.0, height=6.0, seed=3), 3,
+                           21),
+             scenario_case('room_small', S.room(n=150, size=12.0, seed=4), 3, 22)),
+         'pairs': pair_cases, 'walls': wall_cases, 'misc': misc_cases,
+         'navigation': navigation_cases}
+
+
 def main():
+    """Generate every fixture, or only the cases named on the command line."""
     if not RL.available():
         sys.exit('reference source tree not found; set CROWDDYNAMICS_REFERENCE')
-    scenario_case('hallway_small', S.hallway(n=120, width=20.0, height=6.0, seed=3), 3, 21)
-    scenario_case('room_small', S.room(n=150, size=12.0, seed=4), 3, 22)
-    pair_cases()
-    wall_cases()
-    misc_cases()
+    for name in (sys.argv[1:] or list(CASES)):
+        CASES[name]()
 
 
 if __name__ == '__main__':

@@ -53,10 +53,12 @@ def test_record_layout():
     assert c.fields['radius'][1] == 28 and c.fields['position'][1] == 92
     assert t.fields['position'][1] == 124 and t.fields['orientation'][1] == 260
     for dt in (c, t):
-        off = A.field_offsets(dt)
+        off = A.field_offsets(dt)[:29]          # float64 fields: 4-byte aligned
         assert np.all(off[off >= 0] % 4 == 0)
         assert off[A.FIELD_NAMES.index('position')] == dt.fields['position'][1]
-    assert np.all(A.field_offsets(c)[20:] == -1)
+    # Circular records have none of the ThreeCircle fields; both have target
+    assert np.all(A.field_offsets(c)[20:29] == -1)
+    assert A.field_offsets(c)[A.FIELD_NAMES.index('target')] == c.fields['target'][1]
 
 
 def test_layout_matches_reference_definition():
@@ -250,3 +252,27 @@ def test_shared_math_accuracy(oracle):
     assert oracle.cdm('exp', 800) == math.inf and oracle.cdm('exp', -800) == 0.0
     assert oracle.cdm('exp', -740) == math.exp(-740)
     assert math.isnan(oracle.cdm('sin', math.inf))
+
+
+def test_navigation_fuses_into_the_step(monkeypatch):
+    """Navigation (a device node) fuses with the rest of the standard tree
+    into one launch; it runs first in the device step, which commutes with
+    Fluctuation (different fields)."""
+    from crowddynamics_gb300 import _native as N
+    from crowddynamics_gb300.simulation import logic as L
+    from crowddynamics_gb300.simulation.multiagent import MultiAgentSimulation
+    from crowddynamics_gb300.simulation.agents import Agents
+    sim = MultiAgentSimulation(agents=Agents('circular', size=3), rng=np.random.default_rng(0))
+    nav = L.Navigation(sim)
+    nav.direction_maps = [(np.zeros((2, 2)), np.zeros((2, 2)))]
+    sim.logic = L.Reset(sim) << (L.Integrator(sim) << (
+        L.Fluctuation(sim), L.Adjusting(sim) << (nav, L.Orientation(sim)),
+        L.AgentAgentInteractions(sim)))
+    launched = []
+    monkeypatch.setattr(sim, '_use_direction_maps', lambda node: None)
+    monkeypatch.setattr(sim, '_flush', lambda: (launched.append(sim._pending),
+                                                setattr(sim, '_pending', 0)))
+    sim.update()
+    assert [x for x in launched if x] == [
+        N.NODE_FLUCTUATION | N.NODE_NAVIGATION | N.NODE_ORIENTATION | N.NODE_ADJUSTING |
+        N.NODE_AGENT_AGENT | N.NODE_INTEGRATE | N.NODE_RESET]

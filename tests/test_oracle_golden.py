@@ -93,3 +93,39 @@ def test_misc(oracle):
         assert oracle.adaptive_timestep(a, lo, hi) == dt
     from crowddynamics_gb300.simulation.agents import new_agents
     assert oracle.adaptive_timestep(new_agents(3, 'circular'), 0.001, 0.01) == g['dt_zero']
+
+
+def test_oracle_navigation_matches_golden(oracle):
+    """Navigation.update: the oracle's lookup reproduces the reference's
+    meshgrid indicer + getdefault output bit for bit (fixture from the
+    reference's own code)."""
+    d = np.load(os.path.join(GOLDEN, 'navigation.npz'))
+    b = d['bounds']
+    for body in ('circular', 'three_circle'):
+        a = d[body + '_before'].copy()
+        oracle.navigation(a, d['dir_x'], d['dir_y'], b[0], b[1], float(d['step']))
+        want = d[body + '_after']
+        assert np.array_equal(a['target_direction'], want['target_direction']), body
+
+
+def test_oracle_navigation_live_against_reference(oracle):
+    """Fresh seeds: the oracle and the reference's own navigation code agree."""
+    from oracle import ref_loader as RL
+    if not RL.available():
+        pytest.skip('reference source tree not present')
+    from crowddynamics_gb300.simulation.agents import new_agents
+    rng = np.random.default_rng(77)
+    for step, bounds in ((0.1, (0.0, 0.0, 5.0, 3.0)), (0.05, (-1.5, 2.0, 2.5, 4.0))):
+        mg = RL.load_navigation().meshgrid(step, *bounds)
+        ny, nx = mg.shape
+        maps = [(rng.normal(size=(ny, nx)), rng.normal(size=(ny, nx))) for _ in range(3)]
+        a = new_agents(300, 'circular')
+        a['position'] = np.column_stack([rng.uniform(bounds[0] - 1, bounds[2] + 1, 300),
+                                         rng.uniform(bounds[1] - 1, bounds[3] + 1, 300)])
+        a['target'] = rng.integers(-1, 4, 300)
+        a['target_direction'] = rng.normal(size=(300, 2))
+        ref = a.copy()
+        RL.navigation(ref, maps, step, bounds)
+        oracle.navigation(a, np.stack([m[0] for m in maps]), np.stack([m[1] for m in maps]),
+                          bounds[0], bounds[1], step)
+        assert np.array_equal(a['target_direction'], ref['target_direction'])
