@@ -62,6 +62,7 @@ def parse():
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-batched', action='store_true')
     ap.add_argument('--no-adjoint', action='store_true')
+    ap.add_argument('--no-navigation', action='store_true')
     return ap.parse_args()
 
 
@@ -325,6 +326,8 @@ def run_ours(args, ws, rank, local):
         line['batched'] = run_batched(args.steps, args.warmup, flush)
     if not args.no_adjoint:
         line['adjoint'] = run_adjoint()
+    if not args.no_navigation:
+        line['navigation'] = run_navigation(args.steps)
     if ws == 1 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
         steps = 2
@@ -484,6 +487,61 @@ def run_adjoint(n=5000, width=80.0, height=20.0, steps=400, ckpt=20, seed=4, fd_
             'timing': 'CUDA events around the rollout and the adjoint inside cd_rollout_loss, '
                       'median of 3 calls after one warm-up call; adjoint_ms includes the '
                       'recomputation of each 20-step segment'}
+
+
+def run_navigation(steps, n=2000, size=30.0):
+    """Navigation on the device: the ThreeCircle room (30 m x 30 m, one 1.2 m
+    exit, 2000 agents) steering by the exit direction map on a 0.05 m grid,
+    every agent with target 0.  Agent-steps/s of the standard step without
+    navigation, with CD_NODE_NAVIGATION in the same graph, and with the lookup
+    done on the host between device steps (download, lookup, upload: the round
+    trip the device node removes)."""
+    import numpy as np
+    import torch
+    from crowddynamics_gb300 import _native as N
+    from crowddynamics_gb300 import scenarios as S
+    from crowddynamics_gb300.engine import batch_from_scenarios
+    scen = S.room(n=n, size=size, seed=1)
+    scen.agents['target'] = 0
+    e0, e1 = size / 2 - 0.6, size / 2 + 0.6
+    mx, my, step = S.room_exit_direction_map(size, size, e0, e1, step=0.05)
+    b, agents, _ = batch_from_scenarios([scen])
+    b.set_direction_maps(0, mx, my, 0.0, 0.0, step)
+    base = N.NODE_ALL & ~N.NODE_FLUCTUATION
+    out = {'workload': 'room_30x30_threecircle_2000_exit_map_0.05m', 'map_cells': int(mx.size)}
+
+    def timed(nodes):
+        b.upload(agents)
+        b.run(3, nodes)
+        b.synchronize()
+        b.set_timing(True)
+        b.run(steps, nodes)
+        kt = b.kernel_time()
+        b.set_timing(False)
+        return n * steps / (kt['run_ms'] / 1e3)
+
+    out['without_navigation'] = timed(base)
+    out['device_navigation'] = timed(base | N.NODE_NAVIGATION)
+    # host lookup between steps: pinned records down, lookup, up, step
+    host = torch.empty(n * agents.dtype.itemsize, dtype=torch.uint8, pin_memory=True)
+    rec = host.numpy().view(agents.dtype)
+    rec[:] = agents
+    b.upload(rec)
+    b.run(3, base)
+    b.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        b.download(rec)
+        rec['target_direction'] = S.lookup_direction(rec['position'], (mx, my), step,
+                                                     defaults=rec['target_direction'])
+        b.upload(rec)
+        b.run(1, base)
+    out['host_navigation'] = n * steps / (time.perf_counter() - t0)
+    out['unit'] = UNIT
+    out['timing'] = ('device: CUDA events around `steps` graph launches; host: wall clock '
+                     'around download, numpy lookup, upload and one graph launch per step')
+    b.close()
+    return out
 
 
 def main():

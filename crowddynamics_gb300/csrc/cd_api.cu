@@ -43,6 +43,9 @@ struct cd_ctx {
     int64_t wall_idx_cap = 0;
     double *noise_f = nullptr, *noise_m = nullptr;
     bool noise_pending = false;
+    bool noise_dev = false;                          // fluctuation drawn on the device
+    uint64_t noise_seed = 0;
+    unsigned long long *rng_step = nullptr;          // generator counter of the last step
     int *tgt = nullptr;                              // per-agent target index
     double2 *navmap = nullptr;                       // all scenarios' direction maps
     std::vector<std::vector<double>> nav_host;       // per scenario: x maps then y maps
@@ -126,6 +129,9 @@ StepArgs args_of(cd_ctx *c, int nodes) {
     a.wall_idx = c->wall_idx;
     a.noise_f = c->noise_f;
     a.noise_m = c->noise_m;
+    a.noise_dev = c->noise_dev ? 1 : 0;
+    a.noise_seed = c->noise_seed;
+    a.rng_step = c->rng_step;
     a.tgt = c->tgt;
     a.navmap = c->navmap;
     a.vmax = c->vmax;
@@ -165,7 +171,7 @@ void release(cd_ctx *c) {
                     c->noise_f, c->noise_m, c->vmax, c->v0max, c->dt, c->time_tot,
                     c->err, c->work, c->diag, c->aos, c->nl_cnt, c->nl_off, c->nl_fwd,
                     c->nl_scan, c->nl_idx, c->nl_res, c->fw_cnt, c->fw_off, c->fw_scan,
-                    c->fw_pairs, c->ext, c->max_partial, c->tgt, c->navmap};
+                    c->fw_pairs, c->ext, c->max_partial, c->tgt, c->navmap, c->rng_step};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -477,6 +483,7 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->noise_f, 2 * n));
     step(dalloc(c, &c->noise_m, n));
     step(dalloc(c, &c->tgt, n));
+    step(dalloc(c, &c->rng_step, 1));
     step(dalloc(c, &c->vmax, n_scenarios));
     step(dalloc(c, &c->v0max, n_scenarios));
     step(dalloc(c, &c->ext, n_scenarios));
@@ -502,6 +509,7 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
         cudaMemset(c->time_tot, 0, sizeof(double) * n_scenarios);
         cudaMemset(c->dt, 0, sizeof(double) * n_scenarios);
         cudaMemset(c->err, 0, sizeof(int));
+        cudaMemset(c->rng_step, 0, sizeof(unsigned long long));
         cudaMemset(c->wall_start, 0, sizeof(int) * (ncells + 1));
         cudaEventCreate(&c->ev0);
         cudaEventCreate(&c->ev1);
@@ -679,6 +687,20 @@ int cd_set_direction_maps(cd_ctx *c, int64_t scenario, int64_t n_targets, const 
     return CD_OK;
 }
 
+int cd_set_noise_mode(cd_ctx *c, int device, uint64_t seed, uint64_t step) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    const bool dev = device != 0;
+    if (dev != c->noise_dev || (dev && seed != c->noise_seed)) {
+        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; c->graph_nodes = -1; }
+    }
+    c->noise_dev = dev;
+    c->noise_seed = seed;
+    const unsigned long long st = step;
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(c->rng_step, &st, sizeof st, cudaMemcpyHostToDevice, c->stream));
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    return CD_OK;
+}
+
 int cd_set_noise(cd_ctx *c, const double *force, const double *torque) {
     if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
     if (c->n > 0 && !force) return fail(c, CD_ERR_INVALID_VALUE, "force noise is NULL");
@@ -699,10 +721,10 @@ int cd_set_noise(cd_ctx *c, const double *force, const double *torque) {
 int cd_step(cd_ctx *c, int nodes, double *dt) {
     if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
     if (int rc = prepare_step(c, nodes)) return rc;
-    if ((nodes & CD_NODE_FLUCTUATION) && !c->noise_pending)
+    if ((nodes & CD_NODE_FLUCTUATION) && !c->noise_dev && !c->noise_pending)
         return fail(c, CD_ERR_INVALID_VALUE, "cd_set_noise must precede a step with fluctuation");
     enqueue_step(c, nodes, c->timing);
-    if (nodes & CD_NODE_FLUCTUATION) c->noise_pending = false;
+    if ((nodes & CD_NODE_FLUCTUATION) && !c->noise_dev) c->noise_pending = false;
     CUDA_OR_FAIL(c, cudaGetLastError());
     if (c->timing) {
         CUDA_OR_FAIL(c, cudaEventSynchronize(c->evs1));
@@ -724,8 +746,9 @@ int cd_step(cd_ctx *c, int nodes, double *dt) {
 namespace {
 // Capture (or reuse) the graph of one step with `nodes`.
 int ensure_graph(cd_ctx *c, int nodes) {
-    if (nodes & CD_NODE_FLUCTUATION)
-        return fail(c, CD_ERR_INVALID_VALUE, "graph steps cannot consume per-step host noise");
+    if ((nodes & CD_NODE_FLUCTUATION) && !c->noise_dev)
+        return fail(c, CD_ERR_INVALID_VALUE,
+                    "graph steps cannot consume per-step host noise (use device noise)");
     if (int rc = prepare_step(c, nodes)) return rc;
     if (!c->graph || c->graph_nodes != nodes) {
         if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }

@@ -10,7 +10,7 @@ enum Col {
     X, Y, VX, VY, FX, FY, FPX, FPY, E0X, E0Y, R, MASS, TAU_ADJ, K_SOC, TAU0,
     MU, KAPPA, DAMP, V0,
     XLS, YLS, XRS, YRS, RT, RS, RTS, INERTIA, W0, PHI, OMEGA, PHI0, TORQUE,
-    TORQUE_PREV, TAU_ROT,
+    TORQUE_PREV, TAU_ROT, SRF, SRT,      // std_rand_force, std_rand_torque
     NCOL
 };
 
@@ -59,8 +59,12 @@ struct StepArgs {
     const double *walls;         // WALL_D doubles per wall
     const float4 *walls_f;       // (p0x, p0y, p1x, p1y) as float
     const int *wall_start, *wall_idx;   // per-cell CSR of wall ids
-    // fluctuation (host-drawn)
+    // fluctuation: host-drawn arrays, or drawn on the device (noise_dev) from
+    // the counter generator with `noise_seed` at step *rng_step
     const double *noise_f, *noise_m;
+    int noise_dev;
+    unsigned long long noise_seed;
+    unsigned long long *rng_step;
     // navigation
     const int *tgt;              // per agent: target index, -1 for none
     const double2 *navmap;       // (dir_x, dir_y) per map cell

@@ -28,6 +28,7 @@
 #include <cmath>
 #include "cd_internal.cuh"
 #include "cd_math.h"
+#include "cd_noise.h"
 
 namespace cdk {
 
@@ -221,6 +222,8 @@ __device__ __forceinline__ void wall_three_circle(const TC &A, const double *w,
 
 __global__ void k_prepare(StepArgs a) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
+    // device fluctuation: this step's generator counter (read by the force stage)
+    if (i == 0 && a.noise_dev && (a.nodes & N_FLUCT)) *a.rng_step += 1;
     int s = -1;
     double l = 0.0;
     if (i < a.n) {
@@ -1180,8 +1183,17 @@ __device__ __forceinline__ void agent_prologue(const StepArgs &a, const int i, d
     fx = col[FX][i];
     fy = col[FY][i];
     tq = (BODY == 1) ? col[TORQUE][i] : 0.0;
-    // Fluctuation (simulation/logic.py:78-86), noise drawn on the host
-    if ((nodes & N_FLUCT) && a.noise_f) {
+    // Fluctuation (simulation/logic.py:78-86): noise drawn on the host, or on
+    // the device by the counter generator (cd_noise.h)
+    if ((nodes & N_FLUCT) && a.noise_dev) {
+        double nx, ny, nq;
+        cdn_fluctuation(a.noise_seed, *a.rng_step, (uint32_t)i, col[MASS][i], col[SRF][i],
+                        BODY == 1 ? col[INERTIA][i] : 0.0, BODY == 1 ? col[SRT][i] : 0.0,
+                        BODY == 1, &nx, &ny, &nq);
+        fx = fx + nx;
+        fy = fy + ny;
+        if (BODY == 1) tq = tq + nq;
+    } else if ((nodes & N_FLUCT) && a.noise_f) {
         fx = fx + a.noise_f[2 * i];
         fy = fy + a.noise_f[2 * i + 1];
         if (BODY == 1 && a.noise_m) tq = tq + a.noise_m[i];
@@ -1823,16 +1835,16 @@ __global__ void k_wall_prep(const double *raw, double *walls, float4 *wf, int nw
 
 struct FieldMap { int field, comp, col; };
 // (CD_F_* field, vector component, column)
-__constant__ FieldMap kMapCirc[19] = {
+__constant__ FieldMap kMapCirc[20] = {
     {0, 0, X}, {0, 1, Y}, {1, 0, VX}, {1, 1, VY}, {2, 0, E0X}, {2, 1, E0Y},
     {3, 0, FX}, {3, 1, FY}, {4, 0, FPX}, {4, 1, FPY}, {5, 0, R}, {9, 0, MASS},
     {11, 0, V0}, {13, 0, TAU_ADJ}, {14, 0, K_SOC}, {15, 0, TAU0}, {16, 0, MU},
-    {17, 0, KAPPA}, {18, 0, DAMP}};
-__constant__ FieldMap kMapTC[34] = {
+    {17, 0, KAPPA}, {18, 0, DAMP}, {19, 0, SRF}};
+__constant__ FieldMap kMapTC[36] = {
     {0, 0, X}, {0, 1, Y}, {1, 0, VX}, {1, 1, VY}, {2, 0, E0X}, {2, 1, E0Y},
     {3, 0, FX}, {3, 1, FY}, {4, 0, FPX}, {4, 1, FPY}, {5, 0, R}, {9, 0, MASS},
     {11, 0, V0}, {13, 0, TAU_ADJ}, {14, 0, K_SOC}, {15, 0, TAU0}, {16, 0, MU},
-    {17, 0, KAPPA}, {18, 0, DAMP},
+    {17, 0, KAPPA}, {18, 0, DAMP}, {19, 0, SRF}, {28, 0, SRT},
     {20, 0, XLS}, {20, 1, YLS}, {21, 0, XRS}, {21, 1, YRS}, {6, 0, RT}, {7, 0, RS},
     {8, 0, RTS}, {10, 0, INERTIA}, {12, 0, W0}, {22, 0, PHI}, {23, 0, OMEGA},
     {24, 0, PHI0}, {25, 0, TORQUE}, {26, 0, TORQUE_PREV}, {27, 0, TAU_ROT}};
@@ -1860,7 +1872,7 @@ __global__ void k_aos_to_soa(const char *aos, long long itemsize, OffTable off, 
     if (i >= n) return;
     const char *rec = aos + (size_t)i * itemsize;
     const FieldMap *map = body == 0 ? kMapCirc : kMapTC;
-    int nm = body == 0 ? 19 : 34;
+    int nm = body == 0 ? 20 : 36;
     for (int k = 0; k < nm; ++k) {
         long long o = off.off[map[k].field];
         if (o < 0) continue;
@@ -1875,7 +1887,7 @@ __global__ void k_soa_to_aos(char *aos, long long itemsize, OffTable off, int n,
     char *rec = aos + (size_t)i * itemsize;
     const FieldMap *map = body == 0 ? kMapCirc : kMapTC;
     const int *outs = body == 0 ? kOutCirc : kOutTC;
-    int nm = body == 0 ? 19 : 34, no = body == 0 ? 10 : 19;
+    int nm = body == 0 ? 20 : 36, no = body == 0 ? 10 : 19;
     for (int k = 0; k < nm; ++k) {
         bool written = false;
         for (int q = 0; q < no; ++q) written |= (outs[q] == map[k].col);

@@ -19,6 +19,10 @@
  *   sincos : Cody & Waite reduction by pi/2 with a three-part constant (exact
  *            products for |k| < 2^20), Taylor series to degree 17 / 18 on
  *            |r| <= pi/4; quadrant by k mod 4
+ *   log    : x = m 2^e with m in [sqrt(1/2), sqrt(2)) (frexp, exact), then
+ *            log m = 2 atanh(s), s = (m - 1) / (m + 1), |s| <= 3 - 2 sqrt(2),
+ *            by the series 2 (s + s^3/3 + ... + s^25/25); e ln 2 with the
+ *            two-part ln 2 of exp
  *   atan2  : reduction of t = min/max in [0, 1] by atan(t) = atan(c) +
  *            atan((t - c) / (1 + t c)) with c = tan(pi/8) or 1, Taylor series
  *            of atan to degree 23 on |u| <= tan(pi/16); quadrant and signed
@@ -61,6 +65,35 @@ CDM_FN double cdm_exp(double x) {
     p = p * r + 1.0;
     p = p * r + 1.0;
     return ldexp(p, (int)k);
+}
+
+CDM_FN double cdm_log(double x) {
+    if (!(x > 0)) return x == 0 ? -INFINITY : NAN;     /* NaN and negative: NaN */
+    if (x == INFINITY) return x;
+    int e;
+    double m = frexp(x, &e);                            /* m in [1/2, 1) */
+    if (m < 0x1.6a09e667f3bcdp-1) {                     /* sqrt(1/2) */
+        m = m * 2.0;
+        e -= 1;
+    }
+    const double s = (m - 1.0) / (m + 1.0);
+    const double s2 = s * s;
+    double p = 0x1.47ae147ae147bp-5;            /* 1/25 */
+    p = p * s2 + 0x1.642c8590b2164p-5;          /* 1/23 */
+    p = p * s2 + 0x1.8618618618618p-5;          /* 1/21 */
+    p = p * s2 + 0x1.af286bca1af28p-5;          /* 1/19 */
+    p = p * s2 + 0x1.e1e1e1e1e1e1ep-5;          /* 1/17 */
+    p = p * s2 + 0x1.1111111111111p-4;          /* 1/15 */
+    p = p * s2 + 0x1.3b13b13b13b14p-4;          /* 1/13 */
+    p = p * s2 + 0x1.745d1745d1746p-4;          /* 1/11 */
+    p = p * s2 + 0x1.c71c71c71c71cp-4;          /* 1/9  */
+    p = p * s2 + 0x1.2492492492492p-3;          /* 1/7  */
+    p = p * s2 + 0x1.999999999999ap-3;          /* 1/5  */
+    p = p * s2 + 0x1.5555555555555p-2;          /* 1/3  */
+    const double two_s = 2.0 * s;
+    const double lm = two_s + two_s * (s2 * p);
+    const double de = (double)e;
+    return de * 0x1.62e42ff000000p-1 + (de * (-0x1.718432a1b0e26p-35) + lm);
 }
 
 CDM_FN void cdm_sincos(double x, double *s, double *c) {

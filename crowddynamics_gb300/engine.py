@@ -135,6 +135,13 @@ class DeviceBatch:
                                                   N.ptr(my), ny, nx, float(minx), float(miny),
                                                   float(step)))
 
+    def set_noise_mode(self, device, seed=0, step=0):
+        """Fluctuation noise from the host (``device=False``: set_noise before
+        each step) or drawn on the device from the counter generator with
+        ``seed``; the next step uses counter ``step + 1``."""
+        self._chk(self._lib.cd_set_noise_mode(self._ctx, 1 if device else 0, int(seed),
+                                              int(step)))
+
     def set_noise(self, force, torque=None):
         f = np.ascontiguousarray(force, dtype=np.float64)
         if f.shape != (self.n_agents, 2):

@@ -54,13 +54,15 @@ class Integrator(DeviceNode):
 
 
 class Fluctuation(DeviceNode):
-    """Random force and torque, drawn on the host each step with
-    ``simulation.rng`` and added on the device (``simulation/logic.py:78-86``)."""
+    """Random force and torque (``simulation/logic.py:78-86``): drawn on the
+    host each step with ``simulation.rng`` and added on the device, or drawn
+    on the device when the simulation has a ``device_noise_seed``."""
     FLAG = N.NODE_FLUCTUATION
 
     def update(self):
-        agents = self.simulation.agents._array
-        self.simulation._pending_noise = draw_noise(agents, self.simulation.rng)
+        if getattr(self.simulation, 'device_noise_seed', None) is None:
+            agents = self.simulation.agents._array
+            self.simulation._pending_noise = draw_noise(agents, self.simulation.rng)
         super().update()
 
 

@@ -61,10 +61,15 @@ class _Mirror:
 
 
 class MultiAgentSimulation:
-    """Simulation of ``agents`` in ``field`` driven by the ``logic`` tree."""
+    """Simulation of ``agents`` in ``field`` driven by the ``logic`` tree.
+
+    Fluctuation noise is drawn on the host from ``rng`` (numpy/scipy, as the
+    reference does) unless ``device_noise_seed`` is set: then the device
+    draws it from its counter generator with that seed, and the host round
+    trip of the noise arrays disappears."""
 
     def __init__(self, agents=None, field=None, logic=None, name=None, rng=None,
-                 grid_margin=20.0):
+                 grid_margin=20.0, device_noise_seed=None):
         self.name = name or self.__class__.__name__
         self.metadata = collections.OrderedDict(name=self.name)
         self.data = _Data(self)
@@ -82,6 +87,7 @@ class MultiAgentSimulation:
         self._pending = 0
         self._pending_noise = None
         self._time_stale = False
+        self.device_noise_seed = device_noise_seed
 
     # -- device management --
     def _config(self):
@@ -126,6 +132,9 @@ class MultiAgentSimulation:
                 self._batch.set_walls(walls)
             self.agents._mirror = _Mirror(self)
             self._time_offset = self.data.get('time_tot', 0.0) if 'time_tot' in self.data else 0.0
+            if self.device_noise_seed is not None:
+                self._batch.set_noise_mode(True, self.device_noise_seed,
+                                           int(self.data.get('iterations', 0)))
         return self._batch
 
     def _use_direction_maps(self, node):
@@ -157,7 +166,7 @@ class MultiAgentSimulation:
         if mirror.host_dirty:
             b.upload(self.agents._array)
             mirror.host_dirty = False
-        if nodes & N.NODE_FLUCTUATION:
+        if nodes & N.NODE_FLUCTUATION and self.device_noise_seed is None:
             f, m = self._pending_noise
             b.set_noise(f, m)
             self._pending_noise = None

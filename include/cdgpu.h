@@ -139,6 +139,16 @@ int cd_set_direction_maps(cd_ctx *ctx, int64_t scenario, int64_t n_targets,
                           const double *dir_x, const double *dir_y, int64_t ny, int64_t nx,
                           double minx, double miny, double step);
 
+/* Where CD_NODE_FLUCTUATION's noise comes from.  device = 0 (default): host
+ * arrays passed by cd_set_noise before each such step.  device = 1: drawn on
+ * the device from a Philox4x32-10 counter generator keyed by `seed`, one
+ * counter value per step (the step after this call uses step + 1), one
+ * stream per agent: force = mass * std_rand_force * xi * (cos phi, sin phi),
+ * xi ~ N(0,1) on [0, 3], phi ~ U(0, 2 pi); torque = inertia_rot *
+ * std_rand_torque * eta, eta ~ N(0,1) on [-3, 3] (Box-Muller with
+ * rejection).  Device noise also runs inside cd_run / cd_launch graphs. */
+int cd_set_noise_mode(cd_ctx *ctx, int device, uint64_t seed, uint64_t step);
+
 /* Host-drawn fluctuation added by the next step that runs
  * CD_NODE_FLUCTUATION: force (n x 2) and torque (n; ignored for Circular,
  * may be NULL). */
@@ -148,7 +158,7 @@ int cd_set_noise(cd_ctx *ctx, const double *force, const double *torque);
  * NULL the call waits for the step and writes each scenario's timestep. */
 int cd_step(cd_ctx *ctx, int nodes, double *dt);
 /* Run `steps` updates with the selected nodes as one CUDA-graph launch per
- * step (captured on first use).  CD_NODE_FLUCTUATION is not allowed.
+ * step (captured on first use).  CD_NODE_FLUCTUATION needs device noise.
  * Waits for completion and checks the device status. */
 int cd_run(cd_ctx *ctx, int nodes, int64_t steps);
 /* Wait for all work of the context and report device-side errors. */

@@ -28,6 +28,7 @@
 #include <omp.h>
 #endif
 #include "cd_math.h"
+#include "cd_noise.h"
 
 /* Elementary functions: the C library's by default (the plain restatement),
  * or the shared cd_math.h implementations that the device kernels use, so
@@ -834,6 +835,29 @@ void orc_navigation(char *base, int64_t n, int64_t itemsize, const int64_t *off)
     }
 }
 
+/* Philox4x32-10 of cd_noise.h, exported for known-answer tests. */
+void orc_philox4x32_10(const uint32_t *ctr, const uint32_t *key, uint32_t *out) {
+    cdn_philox4x32_10(ctr, key, out);
+}
+
+/* The device's fluctuation noise of step `step` (cd_noise.h): force (n x 2)
+ * and, for ThreeCircle, torque (n), from mass, std_rand_force, inertia_rot
+ * and std_rand_torque (core/motion/fluctuation.py:14-62). */
+void orc_device_noise(const char *base, int64_t n, int64_t itemsize, const int64_t *off, int body,
+                      uint64_t seed, uint64_t step, double *force, double *torque) {
+    arr_t A = {(char *)base, itemsize, off};
+    const int three = body == BODY_THREE_CIRCLE;
+    for (int64_t i = 0; i < n; ++i) {
+        double fx, fy, tq;
+        cdn_fluctuation(seed, step, (uint32_t)i, ld(&A, i, F_MASS), ld(&A, i, F_STD_RAND_FORCE),
+                        three ? ld(&A, i, F_INERTIA_ROT) : 0.0,
+                        three ? ld(&A, i, F_STD_RAND_TORQUE) : 0.0, three, &fx, &fy, &tq);
+        force[2 * i] = fx;
+        force[2 * i + 1] = fy;
+        if (torque) torque[i] = tq;
+    }
+}
+
 /* One MultiAgentSimulation.update() (simulation/multiagent.py:51-55) for the
  * standard tree Reset << Integrator << (Fluctuation, Adjusting << Orientation,
  * AgentAgentInteractions, AgentObstacleInteractions), post-order.  `flags`
@@ -871,6 +895,7 @@ double orc_cdm(int which, double a, double b) {
     case 2: return cdm_sin(a);
     case 3: return cdm_cos(a);
     case 4: return cdm_atan2(a, b);
+    case 5: return cdm_log(a);
     default: return NAN;
     }
 }

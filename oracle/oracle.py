@@ -84,6 +84,11 @@ def lib():
         L.orc_cdm.restype = d
         L.orc_wrap_to_pi.argtypes = [d]
         L.orc_wrap_to_pi.restype = d
+        L.orc_philox4x32_10.argtypes = [P, P, P]
+        L.orc_philox4x32_10.restype = None
+        L.orc_device_noise.argtypes = [P, i64, i64, P, ctypes.c_int, ctypes.c_uint64,
+                                       ctypes.c_uint64, P, P]
+        L.orc_device_noise.restype = None
         L.orc_set_navigation.argtypes = [i64, P, P, i64, i64, d, d, d]
         L.orc_set_navigation.restype = None
         L.orc_navigation.argtypes = [P, i64, i64, P]
@@ -195,7 +200,7 @@ def reset(agents):
 
 def cdm(name, a, b=0.0):
     """One of the shared elementary functions: hypot, exp, sin, cos, atan2."""
-    which = ('hypot', 'exp', 'sin', 'cos', 'atan2').index(name)
+    which = ('hypot', 'exp', 'sin', 'cos', 'atan2', 'log').index(name)
     return lib().orc_cdm(which, float(a), float(b))
 
 
@@ -249,6 +254,29 @@ def navigation(agents, dir_x, dir_y, minx, miny, step):
     off = _offsets(agents)
     lib().orc_navigation(_ptr(agents), len(agents), agents.dtype.itemsize, _ptr(off))
     lib().orc_set_navigation(0, None, None, 0, 0, 0.0, 0.0, 1.0)
+
+
+def philox4x32_10(ctr, key):
+    """Philox4x32-10 of the shared noise header: 4 output words."""
+    c = np.ascontiguousarray(ctr, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    out = np.zeros(4, np.uint32)
+    lib().orc_philox4x32_10(_ptr(c), _ptr(k), _ptr(out))
+    return out
+
+
+def device_noise(agents, seed, step):
+    """The fluctuation noise the device draws at step `step` with `seed`:
+    (force (n, 2), torque (n,) or None)."""
+    _check(agents)
+    off = _offsets(agents)
+    n = len(agents)
+    f = np.zeros((n, 2))
+    three = _body(agents) == BODY_THREE_CIRCLE
+    m = np.zeros(n) if three else None
+    lib().orc_device_noise(_ptr(agents), n, agents.dtype.itemsize, _ptr(off), _body(agents),
+                           int(seed), int(step), _ptr(f), None if m is None else _ptr(m))
+    return f, m
 
 
 def cell_list(x, y, grid):
