@@ -63,6 +63,7 @@ def parse():
     ap.add_argument('--no-batched', action='store_true')
     ap.add_argument('--no-adjoint', action='store_true')
     ap.add_argument('--no-navigation', action='store_true')
+    ap.add_argument('--no-noise', action='store_true')
     return ap.parse_args()
 
 
@@ -328,6 +329,8 @@ def run_ours(args, ws, rank, local):
         line['adjoint'] = run_adjoint()
     if not args.no_navigation:
         line['navigation'] = run_navigation(args.steps)
+    if not args.no_noise:
+        line['fluctuation'] = run_noise(b, agents, scen, args.steps)
     if ws == 1 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
         steps = 2
@@ -341,6 +344,37 @@ def run_ours(args, ws, rank, local):
     b.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_noise(b, agents, scen, steps):
+    """The full step including Fluctuation on the 100k field: noise drawn on
+    the device inside the step graph, against noise drawn on the host with
+    numpy/scipy (as the reference does) and copied in before each step."""
+    from crowddynamics_gb300 import _native as N
+    from crowddynamics_gb300 import scenarios as S
+    import numpy as np
+    n = len(agents)
+    b.upload(agents)
+    b.set_noise_mode(True, 2024, 0)
+    b.run(3, N.NODE_ALL)
+    b.synchronize()
+    b.set_timing(True)
+    b.run(steps, N.NODE_ALL)
+    dev = n * steps / (b.kernel_time()['run_ms'] / 1e3)
+    b.set_timing(False)
+    b.set_noise_mode(False)
+    rng = np.random.default_rng(5)
+    host_steps = max(3, steps // 4)
+    t0 = time.perf_counter()
+    for _ in range(host_steps):
+        b.set_noise(*S.draw_noise(scen.agents, rng))
+        b.step(N.NODE_ALL)
+    b.synchronize()
+    host = n * host_steps / (time.perf_counter() - t0)
+    return {'device_noise': dev, 'host_noise': host, 'unit': UNIT,
+            'workload': 'large_field_threecircle_100k, standard tree with Fluctuation',
+            'timing': 'device: CUDA events around graph launches; host: wall clock around '
+                      'numpy/scipy draw, cd_set_noise and cd_step'}
 
 
 def run_batched(steps, warmup, flush=None):

@@ -30,6 +30,7 @@ NODE_INTEGRATE = 32
 NODE_RESET = 64
 NODE_ALL = 127
 NODE_NAVIGATION = 128
+SNAPSHOT_SLOTS = 8
 
 #: Exported entry points (every function declared in include/cdgpu.h).
 SYMBOLS = (
@@ -39,7 +40,7 @@ SYMBOLS = (
     'cd_sizes', 'cd_set_timing', 'cd_kernel_time', 'cd_kernels_per_step',
     'cd_measure_fp64_peak', 'cd_agent_agent_noalloc', 'cd_variant_count',
     'cd_variant_shape', 'cd_set_variant', 'cd_set_near_list_capacity', 'cd_pair_kernel_time',
-    'cd_set_direction_maps', 'cd_set_noise_mode',
+    'cd_set_direction_maps', 'cd_set_noise_mode', 'cd_snapshot_agents', 'cd_snapshot_wait',
     'cd_launch',
     'cd_rollout_loss',
 )
@@ -110,6 +111,8 @@ def load(path=None):
         'cd_set_near_list_capacity': (ctypes.c_int, [P, i64]),
         'cd_pair_kernel_time': (ctypes.c_int, [P, pd, pi64]),
         'cd_set_noise_mode': (ctypes.c_int, [P, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64]),
+        'cd_snapshot_agents': (ctypes.c_int, [P, ctypes.c_int, P, i64, i64, pi64, pd, pd]),
+        'cd_snapshot_wait': (ctypes.c_int, [P, ctypes.c_int]),
         'cd_set_direction_maps': (ctypes.c_int, [P, i64, i64, P, P, i64, i64, ctypes.c_double,
                                                  ctypes.c_double, ctypes.c_double]),
         'cd_launch': (ctypes.c_int, [P, ctypes.c_int, i64]),

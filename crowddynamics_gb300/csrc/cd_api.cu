@@ -81,6 +81,7 @@ struct cd_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs0 = nullptr, evs1 = nullptr;
     cudaEvent_t evr0 = nullptr, evr1 = nullptr;
     cudaEvent_t evp[2] = {nullptr, nullptr};     // around the pair kernel
+    cudaEvent_t evsnap[CD_SNAPSHOT_SLOTS] = {};  // completion of asynchronous snapshots
     double pair_ms = 0;
     int64_t pair_launches = 0;
     double force_ms = 0, step_ms = 0, run_ms = 0;
@@ -182,6 +183,8 @@ void release(cd_ctx *c) {
     if (c->evr1) cudaEventDestroy(c->evr1);
     if (c->evp[0]) cudaEventDestroy(c->evp[0]);
     if (c->evp[1]) cudaEventDestroy(c->evp[1]);
+    for (cudaEvent_t e : c->evsnap)
+        if (e) cudaEventDestroy(e);
     if (c->ext_host) cudaFreeHost(c->ext_host);
     if (c->stream) cudaStreamDestroy(c->stream);
 }
@@ -519,6 +522,7 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
         cudaEventCreate(&c->evr1);
         cudaEventCreate(&c->evp[0]);
         cudaEventCreate(&c->evp[1]);
+        for (cudaEvent_t &e : c->evsnap) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
         cudaError_t e = cudaDeviceSynchronize();
         if (e != cudaSuccess) rc = fail(c, CD_ERR_CUDA, cudaGetErrorString(e));
     }
@@ -619,6 +623,40 @@ int cd_download_agents(cd_ctx *c, void *records, int64_t n, int64_t itemsize, co
     CUDA_OR_FAIL(c, cudaGetLastError());
     CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
     return check_device_error(c);
+}
+
+int cd_snapshot_agents(cd_ctx *c, int slot, void *records, int64_t n, int64_t itemsize,
+                       const int64_t *off, double *dt, double *time_tot) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (slot < 0 || slot >= CD_SNAPSHOT_SLOTS) return fail(c, CD_ERR_INVALID_VALUE, "bad slot");
+    if (!c->have_records) return fail(c, CD_ERR_INVALID_VALUE, "no agents uploaded");
+    if (n != c->n || itemsize != c->itemsize || !off ||
+        std::memcmp(off, c->off, sizeof(int64_t) * CD_F_COUNT) != 0)
+        return fail(c, CD_ERR_INVALID_VALUE, "record layout differs from the upload");
+    if (n > 0) {
+        if (!records) return fail(c, CD_ERR_INVALID_VALUE, "records is NULL");
+        long long offl[CD_F_COUNT];
+        for (int k = 0; k < CD_F_COUNT; ++k) offl[k] = off[k];
+        cdk::launch_soa_to_aos(c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(records, c->aos, n * itemsize, cudaMemcpyDeviceToHost,
+                                        c->stream));
+    }
+    if (dt)
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(dt, c->dt, sizeof(double) * c->nscen,
+                                        cudaMemcpyDeviceToHost, c->stream));
+    if (time_tot)
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(time_tot, c->time_tot, sizeof(double) * c->nscen,
+                                        cudaMemcpyDeviceToHost, c->stream));
+    CUDA_OR_FAIL(c, cudaEventRecord(c->evsnap[slot], c->stream));
+    CUDA_OR_FAIL(c, cudaGetLastError());
+    return CD_OK;
+}
+
+int cd_snapshot_wait(cd_ctx *c, int slot) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (slot < 0 || slot >= CD_SNAPSHOT_SLOTS) return fail(c, CD_ERR_INVALID_VALUE, "bad slot");
+    CUDA_OR_FAIL(c, cudaEventSynchronize(c->evsnap[slot]));
+    return CD_OK;
 }
 
 int cd_set_walls(cd_ctx *c, const double *walls, int64_t n_walls) {

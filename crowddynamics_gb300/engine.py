@@ -113,6 +113,23 @@ class DeviceBatch:
         self._chk(self._lib.cd_download_agents(self._ctx, N.ptr(records), len(records),
                                                records.dtype.itemsize, N.i64ptr(off)))
 
+    def snapshot(self, slot, records, dt=None, time_tot=None):
+        """Enqueue an asynchronous copy of the state (after the steps already
+        enqueued) into ``records`` and the per-scenario ``dt`` / ``time_tot``
+        arrays; completion is awaited with ``snapshot_wait(slot)``.  The
+        buffers must stay alive until then; page-locked memory makes the copy
+        asynchronous."""
+        if not records.flags.c_contiguous or not records.flags.writeable:
+            raise InvalidValue('agent array must be C-contiguous and writeable')
+        off = field_offsets(records.dtype)
+        self._chk(self._lib.cd_snapshot_agents(
+            self._ctx, int(slot), N.ptr(records), len(records), records.dtype.itemsize,
+            N.i64ptr(off), None if dt is None else N.dptr(dt),
+            None if time_tot is None else N.dptr(time_tot)))
+
+    def snapshot_wait(self, slot):
+        self._chk(self._lib.cd_snapshot_wait(self._ctx, int(slot)))
+
     def set_walls(self, walls):
         rows = walls_as_rows(walls)
         self._chk(self._lib.cd_set_walls(self._ctx, N.ptr(rows), len(rows)))

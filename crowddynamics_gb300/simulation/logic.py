@@ -11,9 +11,14 @@ Traits keep the reference's names and defaults.  As in the reference, the
 shape the cell size; the kernels use the reference's constants 3.0 m and
 2000 N (``core/interactions.py:45``, ``core/motion/power_law.py:52``).
 """
+import os
+import queue
+import threading
+
 import numpy as np
 
 from crowddynamics_gb300 import _native as N
+from crowddynamics_gb300.io import AgentFrameWriter, save_csv, save_geometry_json
 from crowddynamics_gb300.scenarios import draw_noise
 from crowddynamics_gb300.simulation.base import LogicNodeBase
 
@@ -121,3 +126,125 @@ class Navigation(DeviceNode):
             return
         self.simulation._use_direction_maps(self)
         super().update()
+
+
+class SaveSimulationData(LogicNode):
+    """Saving simulation data (``simulation/logic.py:264-337``) in the
+    reference's formats (``crowddynamics/io.py``): ``metadata.csv`` and
+    ``geometry.json`` once, then every update one frame of agent records and
+    one row of ``simulation.data``; ``agents_{k}.npy`` and ``data.csv`` are
+    written when ``save_condition(simulation)`` is true.
+
+    The frame comes from the device without stopping it: the update enqueues
+    an asynchronous copy of the state (and of dt, time_tot) into one of a few
+    page-locked slots, behind the steps already enqueued; a writer thread
+    waits for each copy, appends it to the frame file and writes the data row.
+    The host never waits for the device here except when all slots are busy.
+    (The reference buffers references to the live agent array, so every frame
+    of one of its files shows the state at the dump; here each frame is the
+    state at its own update.)"""
+    save_condition = None
+    base_directory = '.'
+    save_directory = None
+    slots = 4
+
+    def __init__(self, simulation, name=None, **traits):
+        super().__init__(simulation, name=name, **traits)
+        if self.save_condition is None:
+            self.save_condition = lambda sim: True
+        if self.save_directory is None:
+            self.save_directory = simulation.name_with_timestamp
+        os.makedirs(self.full_path, exist_ok=True)
+        meta = save_csv(self.full_path, 'metadata')
+        meta.send(None)
+        meta.send(simulation.metadata)
+        meta.send(True)
+        field = simulation.field
+        save_geometry_json(os.path.join(self.full_path, 'geometry.json'),
+                           {name: getattr(field, name, None)
+                            for name in ('domain', 'obstacles', 'targets', 'spawns')})
+        self._data_csv = save_csv(self.full_path, 'data')
+        self._data_csv.send(None)
+        self._frames = None
+        self._thread = None
+
+    @property
+    def full_path(self):
+        return os.path.join(os.path.abspath(self.base_directory), self.save_directory)
+
+    def add_to_simulation_logic(self):
+        self.simulation.logic['Reset'].inject_before(self)
+
+    def _start(self, batch, dtype, n):
+        import torch                                  # page-locked host memory
+        k = max(1, min(int(self.slots), N.SNAPSHOT_SLOTS))
+        self._pinned = [torch.empty(max(n, 1) * dtype.itemsize, dtype=torch.uint8,
+                                    pin_memory=True) for _ in range(k)]
+        self._records = [p.numpy()[:n * dtype.itemsize].view(dtype) for p in self._pinned]
+        self._times = [np.zeros((2, batch.n_scenarios)) for _ in range(k)]
+        self._free = queue.Queue()
+        for q in range(k):
+            self._free.put(q)
+        self._work = queue.Queue()
+        self._frames = AgentFrameWriter(self.full_path, 'agents', dtype, n)
+        self._error = None
+        self._thread = threading.Thread(target=self._writer, daemon=True)
+        self._thread.start()
+
+    def _writer(self):
+        while True:
+            item = self._work.get()
+            if item is None:
+                self._work.task_done()
+                return
+            batch, slot, keys, values, save, offset = item
+            try:
+                batch.snapshot_wait(slot)
+                self._frames.append(self._records[slot])
+                dt, tt = float(self._times[slot][0][0]), float(self._times[slot][1][0])
+                self._free.put(slot)
+                row = {k: (dt if k == 'dt' else tt + offset if k == 'time_tot' else values[k])
+                       for k in keys}
+                self._data_csv.send(row)
+                self._data_csv.send(save)
+                if save:
+                    self._frames.dump()
+            except Exception as exc:                    # reported by the next update
+                self._error = exc
+                self._free.put(slot)
+            self._work.task_done()
+
+    def update(self):
+        sim = self.simulation
+        save = bool(self.save_condition(sim))
+        b = sim._ensure_batch()
+        arr = sim.agents._array
+        mirror = sim.agents._mirror
+        if mirror is not None and mirror.host_dirty:    # host edits since the last step
+            b.upload(arr)
+            mirror.host_dirty = False
+        if self._thread is None:
+            self._start(b, arr.dtype, len(arr))
+        if self._error is not None:
+            raise self._error
+        slot = self._free.get()
+        times = self._times[slot]
+        b.snapshot(slot, self._records[slot], times[0], times[1])
+        keys = list(sim.data.keys())
+        values = {k: dict.__getitem__(sim.data, k) for k in keys if k not in ('dt', 'time_tot')}
+        self._work.put((b, slot, keys, values, save, getattr(sim, '_time_offset', 0.0)))
+
+    def drain(self):
+        """Wait until every queued frame has been written."""
+        if self._thread is not None:
+            self._work.join()
+            if self._error is not None:
+                raise self._error
+
+    def close(self):
+        if self._thread is not None:
+            self.drain()
+            self._work.put(None)
+            self._thread.join()
+            self._thread = None
+            self._frames.close()

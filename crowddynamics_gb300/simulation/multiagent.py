@@ -12,6 +12,7 @@ again before the next device step.  ``data['dt']`` and ``data['time_tot']``
 are read from the device when looked up.
 """
 import collections
+import datetime
 import math
 
 import numpy as np
@@ -71,7 +72,9 @@ class MultiAgentSimulation:
     def __init__(self, agents=None, field=None, logic=None, name=None, rng=None,
                  grid_margin=20.0, device_noise_seed=None):
         self.name = name or self.__class__.__name__
+        self.timestamp = datetime.datetime.now(tz=datetime.timezone.utc)
         self.metadata = collections.OrderedDict(name=self.name)
+        self.metadata['timestamp'] = str(self.timestamp)
         self.data = _Data(self)
         self.data['iterations'] = 0
         self.data['time_tot'] = 0.0
@@ -196,12 +199,30 @@ class MultiAgentSimulation:
         self._flush()
         self.data['iterations'] += 1
 
+    @property
+    def name_with_timestamp(self):
+        """Name with timestamp (``simulation/base.py:115-118``)."""
+        return '_'.join((self.name, str(self.timestamp).replace(' ', '_')))
+
     def run(self):
-        """Update until ``exit_condition(self)`` is true (``simulation/base.py:123-125``)."""
+        """Update until ``exit_condition(self)`` is true (``simulation/base.py:123-125``);
+        then wait for background writers (SaveSimulationData) to finish."""
         while self.exit_condition is None or not self.exit_condition(self):
             self.update()
+        self.finish_writers()
+
+    def finish_writers(self):
+        """Wait until every queued save has reached the disk."""
+        if self.logic is not None:
+            for node in post_order(self.logic.root):
+                if hasattr(node, 'drain'):
+                    node.drain()
 
     def close(self):
+        if self.logic is not None:
+            for node in post_order(self.logic.root):
+                if hasattr(node, 'close'):
+                    node.close()
         if self._batch is not None:
             if self.agents._mirror is not None:
                 self.agents._mirror.pull()

@@ -123,6 +123,19 @@ int cd_upload_agents(cd_ctx *ctx, const void *records, int64_t n,
 int cd_download_agents(cd_ctx *ctx, void *records, int64_t n, int64_t itemsize,
                        const int64_t *field_offsets);
 
+/* Asynchronous snapshot for SaveSimulationData (simulation/logic.py:264-337):
+ * enqueue on the context stream, behind the steps already enqueued, the
+ * copy of the agent state into `n` packed host records (layout as uploaded;
+ * page-locked memory makes the copy asynchronous), and of every scenario's
+ * dt and time_tot (may be NULL), then record completion in `slot` (0 ..
+ * CD_SNAPSHOT_SLOTS - 1).  Returns at once.  cd_snapshot_wait blocks until
+ * the snapshot of `slot` is in host memory; it may be called from another
+ * host thread. */
+#define CD_SNAPSHOT_SLOTS 8
+int cd_snapshot_agents(cd_ctx *ctx, int slot, void *records, int64_t n, int64_t itemsize,
+                       const int64_t *field_offsets, double *dt, double *time_tot);
+int cd_snapshot_wait(cd_ctx *ctx, int slot);
+
 /* Replace all walls: `n_walls` rows of (p0x, p0y, p1x, p1y) float64, split
  * among scenarios by their wall ranges.  Walls are binned into the cells of
  * their scenario's grid. */
