@@ -64,6 +64,7 @@ def parse():
     ap.add_argument('--no-adjoint', action='store_true')
     ap.add_argument('--no-navigation', action='store_true')
     ap.add_argument('--no-noise', action='store_true')
+    ap.add_argument('--no-save', action='store_true')
     return ap.parse_args()
 
 
@@ -331,6 +332,8 @@ def run_ours(args, ws, rank, local):
         line['navigation'] = run_navigation(args.steps)
     if not args.no_noise:
         line['fluctuation'] = run_noise(b, agents, scen, args.steps)
+    if not args.no_save:
+        line['save'] = run_save(max(args.steps, 20))
     if ws == 1 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
         steps = 2
@@ -344,6 +347,80 @@ def run_ours(args, ws, rank, local):
     b.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_save(steps, n=2000, size=30.0):
+    """SaveSimulationData every update on the ThreeCircle room (2000 agents,
+    632 kB of records per frame), dumping every 10 frames: the standard tree
+    with device noise and no saving, with the node (asynchronous snapshots
+    and a writer thread), and with the reference's way (the host array
+    downloaded after every update, then its save_npy / save_csv protocol)."""
+    import shutil
+    import tempfile
+    import numpy as np
+    from crowddynamics_gb300 import io as IO
+    from crowddynamics_gb300 import scenarios as S
+    from crowddynamics_gb300.simulation import logic as L
+    from crowddynamics_gb300.simulation.agents import Agents
+    from crowddynamics_gb300.simulation.field import Field
+    from crowddynamics_gb300.simulation.multiagent import MultiAgentSimulation
+    scen = S.room(n=n, size=size, seed=1)
+    base = tempfile.mkdtemp(prefix='cdsave')
+
+    def make():
+        sim = MultiAgentSimulation(agents=Agents(array=scen.agents.copy()),
+                                   field=Field(domain=scen.bounds, obstacles=scen.walls),
+                                   device_noise_seed=7, name='room')
+        sim.logic = L.Reset(sim) << (L.Integrator(sim, dt_min=0.001, dt_max=0.01) << (
+            L.Fluctuation(sim), L.Adjusting(sim) << L.Orientation(sim),
+            L.AgentAgentInteractions(sim, max_agent_radius=0.35), L.AgentObstacleInteractions(sim)))
+        return sim
+
+    def timed(sim, each=None):
+        for _ in range(3):
+            sim.update()
+            if each:
+                each(sim)
+        sim.finish_writers()
+        sim._batch.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            sim.update()
+            if each:
+                each(sim)
+        sim.finish_writers()
+        sim._batch.synchronize()
+        return n * steps / (time.perf_counter() - t0)
+
+    out = {'workload': 'room_30x30_threecircle_2000, save every update, dump every 10',
+           'unit': UNIT, 'bytes_per_frame': n * scen.agents.dtype.itemsize}
+    sim = make()
+    out['no_save'] = timed(sim)
+    sim.close()
+    sim = make()
+    node = L.SaveSimulationData(sim, base_directory=base, save_directory='async',
+                                save_condition=lambda s: (s.data['iterations'] + 1) % 10 == 0)
+    node.add_to_simulation_logic()
+    out['async_save'] = timed(sim)
+    sim.close()
+    sim = make()
+    d = os.path.join(base, 'sync')
+    os.makedirs(d)
+    npy, rows = IO.save_npy(d, 'agents'), IO.save_csv(d, 'data')
+    npy.send(None)
+    rows.send(None)
+
+    def host_save(s):
+        save = s.data['iterations'] % 10 == 0
+        npy.send(s.agents.array)
+        npy.send(save)
+        rows.send(dict(s.data))
+        rows.send(save)
+    out['host_save'] = timed(sim, host_save)
+    sim.close()
+    shutil.rmtree(base, ignore_errors=True)
+    out['timing'] = 'wall clock around `steps` updates, writers drained before and after'
+    return out
 
 
 def run_noise(b, agents, scen, steps):
