@@ -65,6 +65,7 @@ def parse():
     ap.add_argument('--no-navigation', action='store_true')
     ap.add_argument('--no-noise', action='store_true')
     ap.add_argument('--no-save', action='store_true')
+    ap.add_argument('--no-states', action='store_true')
     return ap.parse_args()
 
 
@@ -334,6 +335,8 @@ def run_ours(args, ws, rank, local):
         line['fluctuation'] = run_noise(b, agents, scen, args.steps)
     if not args.no_save:
         line['save'] = run_save(max(args.steps, 20))
+    if not args.no_states:
+        line['states'] = run_states(max(args.steps, 10))
     if ws == 1 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
         steps = 2
@@ -420,6 +423,47 @@ def run_save(steps, n=2000, size=30.0):
     sim.close()
     shutil.rmtree(base, ignore_errors=True)
     out['timing'] = 'wall clock around `steps` updates, writers drained before and after'
+    return out
+
+
+def run_states(steps, n=2000, size=30.0):
+    """The state nodes between steps on the ThreeCircle room (2000 agents,
+    5 walls plus 3 interior walls): LeaderFollowerWithHerding (10% leaders,
+    70% followers, 5 nearest within 10 m), InsideDomain and TargetReached;
+    agent-updates/s of each call (CUDA-synchronised wall clock)."""
+    import numpy as np
+    from crowddynamics_gb300 import scenarios as S
+    from crowddynamics_gb300.engine import DeviceBatch, walls_as_rows
+    rng = np.random.default_rng(3)
+    scen = S.room(n=n, size=size, seed=1)
+    walls = np.concatenate([scen.walls, S.walls_array([((8.0, 5.0), (8.0, 20.0)),
+                                                       ((15.0, 25.0), (25.0, 15.0)),
+                                                       ((2.0, 12.0), (12.0, 12.5))])])
+    a = scen.agents
+    a['velocity'] = rng.normal(0, 1, (n, 2))
+    a['is_leader'] = rng.uniform(size=n) < 0.1
+    a['is_follower'] = ~a['is_leader'] & (rng.uniform(size=n) < 0.7)
+    a['target'] = np.where(a['is_leader'], 0, -1)
+    b = DeviceBatch('three_circle', [dict(n_agents=n, n_walls=len(walls), grid=scen.grid)])
+    b.upload(a)
+    b.set_walls(walls)
+    domain = np.array([[0, 0], [size, 0], [size, size], [0, size], [0, 0]], float)
+    exit_ = [np.array([[size - 1, size / 2 - 1], [size, size / 2 - 1], [size, size / 2 + 1],
+                       [size - 1, size / 2 + 1]], float)]
+    out = {'workload': 'room_30x30_threecircle_2000, 8 walls', 'unit': 'agent-updates/s'}
+    for name, fn in (('leader_follower_with_herding', lambda: b.herding(True)),
+                     ('leader_follower', lambda: b.herding(False, sight_follower=1.0)),
+                     ('inside_domain', lambda: b.inside_domain(0, domain)),
+                     ('target_reached', lambda: b.target_reached(0, exit_))):
+        fn()
+        b.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            fn()
+        b.synchronize()
+        out[name] = n * steps / (time.perf_counter() - t0)
+    b.close()
+    out['timing'] = 'wall clock around `steps` calls, each synchronised (they return host values)'
     return out
 
 

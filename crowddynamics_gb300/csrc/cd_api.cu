@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "cd_internal.cuh"
+#include "cd_math.h"
 #include "../../include/cdgpu.h"
 
 using cdk::StepArgs;
@@ -47,6 +48,19 @@ struct cd_ctx {
     uint64_t noise_seed = 0;
     unsigned long long *rng_step = nullptr;          // generator counter of the last step
     int *tgt = nullptr;                              // per-agent target index
+    int *states = nullptr;                           // active, leader, follower, index_leader,
+                                                     // familiar_exit (n each)
+    bool states_dirty = false;                       // changed on the device since the upload
+    // leader-follower / domain nodes (allocated on first use)
+    int *herd = nullptr;                             // neighbours, flags, scan, list, targets
+    int herd_k = 0;
+    ScenDev *scen_h = nullptr;
+    unsigned long long *counters = nullptr;          // domain changes, per-target counts
+    unsigned char *reached = nullptr;                // per target x agent
+    int64_t reached_targets = 0;
+    double2 *polys = nullptr;
+    int *poly_off = nullptr;
+    int64_t poly_cap = 0;
     double2 *navmap = nullptr;                       // all scenarios' direction maps
     std::vector<std::vector<double>> nav_host;       // per scenario: x maps then y maps
     unsigned long long *vmax = nullptr;
@@ -172,7 +186,9 @@ void release(cd_ctx *c) {
                     c->noise_f, c->noise_m, c->vmax, c->v0max, c->dt, c->time_tot,
                     c->err, c->work, c->diag, c->aos, c->nl_cnt, c->nl_off, c->nl_fwd,
                     c->nl_scan, c->nl_idx, c->nl_res, c->fw_cnt, c->fw_off, c->fw_scan,
-                    c->fw_pairs, c->ext, c->max_partial, c->tgt, c->navmap, c->rng_step};
+                    c->fw_pairs, c->ext, c->max_partial, c->tgt, c->navmap, c->rng_step,
+                    c->states, c->herd, c->scen_h, c->counters, c->reached, c->polys,
+                    c->poly_off};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -353,6 +369,33 @@ void add_pair_time(cd_ctx *c, int nodes) {
     }
 }
 
+// Offsets of the integer and bool fields that fit the record (-1 otherwise).
+cdk::StateOffsets state_offsets(const int64_t *off, int64_t itemsize) {
+    auto f = [&](int field, int bytes) -> long long {
+        return (off[field] >= 0 && off[field] + bytes <= itemsize) ? off[field] : -1;
+    };
+    cdk::StateOffsets o;
+    o.target = f(CD_F_TARGET, 8);
+    o.active = f(CD_F_ACTIVE, 1);
+    o.leader = f(CD_F_IS_LEADER, 1);
+    o.follower = f(CD_F_IS_FOLLOWER, 1);
+    o.index_leader = f(CD_F_INDEX_LEADER, 8);
+    o.familiar_exit = f(CD_F_FAMILIAR_EXIT, 8);
+    return o;
+}
+
+cdk::StateCols state_cols(cd_ctx *c) {
+    const int64_t np = std::max<int64_t>(c->n, 1);
+    cdk::StateCols k;
+    k.target = c->tgt;
+    k.active = c->states;
+    k.leader = c->states + np;
+    k.follower = c->states + 2 * np;
+    k.index_leader = c->states + 3 * np;
+    k.familiar_exit = c->states + 4 * np;
+    return k;
+}
+
 int check_device_error(cd_ctx *c) {
     CUDA_OR_FAIL(c, cudaGetLastError());
     int h = 0, need = 0;
@@ -486,6 +529,7 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->noise_f, 2 * n));
     step(dalloc(c, &c->noise_m, n));
     step(dalloc(c, &c->tgt, n));
+    step(dalloc(c, &c->states, 5 * npad));
     step(dalloc(c, &c->rng_step, 1));
     step(dalloc(c, &c->vmax, n_scenarios));
     step(dalloc(c, &c->v0max, n_scenarios));
@@ -584,9 +628,9 @@ int cd_upload_agents(cd_ctx *c, const void *records, int64_t n, int64_t itemsize
         long long offl[CD_F_COUNT];
         for (int k = 0; k < CD_F_COUNT; ++k) offl[k] = off[k];
         cdk::launch_aos_to_soa(c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
-        const bool have_target = off[CD_F_TARGET] >= 0 && off[CD_F_TARGET] + 8 <= itemsize;
-        cdk::launch_targets(c->aos, itemsize, have_target ? off[CD_F_TARGET] : -1, (int)n, c->tgt,
-                            c->stream);
+        cdk::launch_states_in(c->aos, itemsize, state_offsets(off, itemsize), (int)n,
+                              state_cols(c), c->stream);
+        c->states_dirty = false;
     }
     StepArgs a = args_of(c, 0);
     cdk::launch_scen_max(a, c->v0max, c->ext, c->max_partial, c->stream);
@@ -619,6 +663,9 @@ int cd_download_agents(cd_ctx *c, void *records, int64_t n, int64_t itemsize, co
     long long offl[CD_F_COUNT];
     for (int k = 0; k < CD_F_COUNT; ++k) offl[k] = off[k];
     cdk::launch_soa_to_aos(c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
+    if (c->states_dirty)
+        cdk::launch_states_out(c->aos, itemsize, state_offsets(off, itemsize), (int)n,
+                               state_cols(c), c->stream);
     CUDA_OR_FAIL(c, cudaMemcpyAsync(records, c->aos, n * itemsize, cudaMemcpyDeviceToHost, c->stream));
     CUDA_OR_FAIL(c, cudaGetLastError());
     CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
@@ -638,6 +685,9 @@ int cd_snapshot_agents(cd_ctx *c, int slot, void *records, int64_t n, int64_t it
         long long offl[CD_F_COUNT];
         for (int k = 0; k < CD_F_COUNT; ++k) offl[k] = off[k];
         cdk::launch_soa_to_aos(c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
+        if (c->states_dirty)
+            cdk::launch_states_out(c->aos, itemsize, state_offsets(off, itemsize), (int)n,
+                                   state_cols(c), c->stream);
         CUDA_OR_FAIL(c, cudaMemcpyAsync(records, c->aos, n * itemsize, cudaMemcpyDeviceToHost,
                                         c->stream));
     }
@@ -673,6 +723,157 @@ int cd_set_walls(cd_ctx *c, const double *walls, int64_t n_walls) {
     CUDA_OR_FAIL(c, cudaGetLastError());
     CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
     return CD_OK;
+}
+
+int cd_herding(cd_ctx *c, int with_herding, double sight_follower, int64_t size_nearest_other,
+               double sight_leader, double phi, double w_herding, double w_leader,
+               double w_direction) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (!c->have_records) return fail(c, CD_ERR_INVALID_VALUE, "no agents uploaded");
+    if (with_herding && (size_nearest_other < 1 || size_nearest_other > 16))
+        return fail(c, CD_ERR_INVALID_VALUE, "size_nearest_other must be in [1, 16]");
+    if (!(sight_follower > 0) || !std::isfinite(sight_follower) || !(sight_leader >= 0))
+        return fail(c, CD_ERR_INVALID_VALUE, "bad sight");
+    const int64_t n = c->n;
+    if (n == 0) return CD_OK;
+    const int K = with_herding ? (int)size_nearest_other : 1;
+    const int64_t scan = cdk::scan_scratch_ints((int)n);
+    if (!c->herd) {
+        if (int rc = dalloc(c, &c->herd, 16 * n + 2 * (n + 1) + 2 * n + scan)) return rc;
+        if (int rc = dalloc(c, &c->scen_h, c->nscen)) return rc;
+    }
+    int *nbr = c->herd, *flags = nbr + 16 * n, *pos = flags + (n + 1), *list = pos + (n + 1);
+    int *before = list + n, *scratch = before + n;
+    // herding grid: the scenario's origin, cells of the follower sight
+    std::vector<ScenDev> hs(c->scen_dev);
+    int64_t base = 0;
+    for (int s = 0; s < c->nscen; ++s) {
+        const cd_scenario &sc = c->scen_host[s];
+        hs[s].cell = sight_follower;
+        hs[s].nx = (int)std::max<int64_t>(1, (int64_t)std::ceil(sc.nx * sc.cell_size / sight_follower));
+        hs[s].ny = (int)std::max<int64_t>(1, (int64_t)std::ceil(sc.ny * sc.cell_size / sight_follower));
+        hs[s].cell_base = (int)base;
+        base += (int64_t)hs[s].nx * hs[s].ny;
+    }
+    if (with_herding && base > c->ncells)
+        return fail(c, CD_ERR_CAPACITY, "follower sight smaller than the cell size");
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(c->scen_h, hs.data(), sizeof(ScenDev) * c->nscen,
+                                    cudaMemcpyHostToDevice, c->stream));
+    StepArgs a = args_of(c, 0);
+    a.scen = c->scen_h;
+    if (with_herding) enqueue_cells(c, a);                   // cell list on the herding grid
+    cdk::HerdArgs h;
+    h.n = (int)n;
+    h.K = K;
+    h.with_herding = with_herding ? 1 : 0;
+    h.perm = c->perm;
+    h.key = c->key;
+    h.start = c->start;
+    h.scen_of = c->scen_of;
+    h.scen_h = c->scen_h;
+    for (int k = 0; k < cdk::NCOL; ++k) h.col[k] = c->col[k];
+    h.walls = c->walls;
+    h.st = state_cols(c);
+    h.nbr = nbr;
+    h.leaders = list;
+    h.n_leaders = pos + n;
+    h.tgt_before = before;
+    h.sight_f = sight_follower;
+    h.sight_l = sight_leader;
+    h.cos_phi = cdm_cos(phi);
+    h.w_herd = w_herding;
+    h.w_lead = w_leader;
+    h.w_dir = w_direction;
+    cdk::launch_herd_neighbors(h, c->stream);
+    cdk::launch_leaders(h, flags, pos, scratch, list, c->stream);
+    cdk::launch_herd_follow(h, c->stream);
+    c->states_dirty = true;
+    CUDA_OR_FAIL(c, cudaGetLastError());
+    return check_device_error(c);
+}
+
+namespace {
+int upload_polygons(cd_ctx *c, int64_t n_polys, const double *xy, const int64_t *voff) {
+    const int64_t nv = voff[n_polys];
+    if (nv < 0 || nv > INT32_MAX) return fail(c, CD_ERR_INVALID_VALUE, "bad vertex offsets");
+    for (int64_t t = 0; t < n_polys; ++t)
+        if (voff[t + 1] < voff[t]) return fail(c, CD_ERR_INVALID_VALUE, "bad vertex offsets");
+    if (nv + n_polys + 1 > c->poly_cap) {
+        if (c->polys) cudaFree(c->polys);
+        if (c->poly_off) cudaFree(c->poly_off);
+        c->polys = nullptr;
+        c->poly_off = nullptr;
+        c->poly_cap = 0;
+        if (int rc = dalloc(c, &c->polys, nv + 1)) return rc;
+        if (int rc = dalloc(c, &c->poly_off, nv + n_polys + 2)) return rc;
+        c->poly_cap = nv + n_polys + 1;
+    }
+    std::vector<int> off(voff, voff + n_polys + 1);
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(c->polys, xy, sizeof(double) * 2 * nv, cudaMemcpyHostToDevice,
+                                    c->stream));
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(c->poly_off, off.data(), sizeof(int) * off.size(),
+                                    cudaMemcpyHostToDevice, c->stream));
+    if (!c->counters)
+        if (int rc = dalloc(c, &c->counters, 1 + 256)) return rc;
+    return CD_OK;
+}
+}  // namespace
+
+int cd_inside_domain(cd_ctx *c, int64_t scenario, const double *xy, int64_t n_vertices,
+                     int64_t *changed) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (scenario < 0 || scenario >= c->nscen) return fail(c, CD_ERR_INVALID_VALUE, "bad scenario");
+    if (n_vertices < 1 || !xy) return fail(c, CD_ERR_INVALID_VALUE, "empty polygon");
+    if (!c->have_records) return fail(c, CD_ERR_INVALID_VALUE, "no agents uploaded");
+    const int64_t voff[2] = {0, n_vertices};
+    if (int rc = upload_polygons(c, 1, xy, voff)) return rc;
+    CUDA_OR_FAIL(c, cudaMemsetAsync(c->counters, 0, sizeof(unsigned long long), c->stream));
+    const cd_scenario &sc = c->scen_host[scenario];
+    cdk::launch_inside_domain((int)sc.agent_begin, (int)sc.agent_count, c->col[cdk::X],
+                              c->col[cdk::Y], state_cols(c).active, c->polys, (int)n_vertices,
+                              c->counters, c->stream);
+    unsigned long long h = 0;
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(&h, c->counters, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    c->states_dirty = true;
+    if (changed) *changed = (int64_t)h;
+    return check_device_error(c);
+}
+
+int cd_target_reached(cd_ctx *c, int64_t scenario, int64_t n_targets, const double *xy,
+                      const int64_t *vertex_offsets, int reset, int64_t *counts) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (scenario < 0 || scenario >= c->nscen) return fail(c, CD_ERR_INVALID_VALUE, "bad scenario");
+    if (n_targets < 0 || n_targets > 256) return fail(c, CD_ERR_INVALID_VALUE, "0-256 targets");
+    if (!c->have_records) return fail(c, CD_ERR_INVALID_VALUE, "no agents uploaded");
+    if (n_targets == 0) return CD_OK;
+    if (!xy || !vertex_offsets) return fail(c, CD_ERR_INVALID_VALUE, "NULL polygons");
+    if (int rc = upload_polygons(c, n_targets, xy, vertex_offsets)) return rc;
+    const int64_t n = std::max<int64_t>(c->n, 1);
+    if (n_targets > c->reached_targets) {
+        if (c->reached) cudaFree(c->reached);
+        c->reached = nullptr;
+        c->reached_targets = 0;
+        if (int rc = dalloc(c, &c->reached, n_targets * n)) return rc;
+        CUDA_OR_FAIL(c, cudaMemsetAsync(c->reached, 0, n_targets * n, c->stream));
+        c->reached_targets = n_targets;
+    } else if (reset) {
+        CUDA_OR_FAIL(c, cudaMemsetAsync(c->reached, 0, n_targets * n, c->stream));
+    }
+    CUDA_OR_FAIL(c, cudaMemsetAsync(c->counters + 1, 0, sizeof(unsigned long long) * n_targets,
+                                    c->stream));
+    const cd_scenario &sc = c->scen_host[scenario];
+    for (int t = 0; t < n_targets; ++t)
+        cdk::launch_target_reached((int)sc.agent_begin, (int)sc.agent_count, c->col[cdk::X],
+                                   c->col[cdk::Y], c->reached + (size_t)t * n + sc.agent_begin,
+                                   c->polys, c->poly_off, t, c->counters + 1, c->stream);
+    std::vector<unsigned long long> h(n_targets);
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(h.data(), c->counters + 1, sizeof(unsigned long long) * n_targets,
+                                    cudaMemcpyDeviceToHost, c->stream));
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    if (counts)
+        for (int64_t t = 0; t < n_targets; ++t) counts[t] = (int64_t)h[t];
+    return check_device_error(c);
 }
 
 int cd_set_direction_maps(cd_ctx *c, int64_t scenario, int64_t n_targets, const double *dir_x,

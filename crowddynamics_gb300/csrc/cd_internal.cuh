@@ -95,6 +95,41 @@ constexpr int ADJ_RES_D = 6;
 // Device error bit: a pair partner's near list lacked the pair.
 constexpr int ERR_NEAR_LIST = 2;
 
+// Integer and bool state fields: byte offsets in the records (-1 = absent)
+// and their device columns (indices outside [0, 2^31) read as -1).
+struct StateOffsets {
+    long long target, active, leader, follower, index_leader, familiar_exit;
+};
+struct StateCols {
+    int *target, *active, *leader, *follower, *index_leader, *familiar_exit;
+};
+
+// Leader-follower / herding arguments (cd_states.cu).  The cell list is the
+// one built on the herding grid (cell = follower sight).
+struct HerdArgs {
+    int n, K, with_herding;
+    const int *perm, *key, *start, *scen_of;
+    const ScenDev *scen_h;           // herding grid per scenario (walls as in the step)
+    double *col[NCOL];
+    const double *walls;             // WALL_D doubles per wall
+    StateCols st;
+    int *nbr;                        // n x K nearest unobstructed neighbours, -1 missing
+    const int *leaders;              // leader agents in ascending order
+    const int *n_leaders;
+    int *tgt_before;                 // targets before the update
+    double sight_f, sight_l, cos_phi, w_herd, w_lead, w_dir;
+};
+void launch_herd_neighbors(const HerdArgs &h, cudaStream_t s);
+void launch_leaders(const HerdArgs &h, int *flags, int *pos, int *scan_scratch, int *list,
+                    cudaStream_t s);
+void launch_herd_follow(const HerdArgs &h, cudaStream_t s);
+void launch_inside_domain(int begin, int count, const double *x, const double *y, int *active,
+                          const double2 *poly, int m, unsigned long long *changed,
+                          cudaStream_t s);
+void launch_target_reached(int begin, int count, const double *x, const double *y,
+                           unsigned char *reached, const double2 *polys, const int *voff, int t,
+                           unsigned long long *counts, cudaStream_t s);
+
 // Reverse-step arguments (cd_adjoint.cu); n x 2 arrays are interleaved,
 // state snapshots are columns.
 struct AdjArgs {
@@ -156,9 +191,11 @@ void launch_wall_prep(const double *raw, double *walls, float4 *walls_f, int nw,
                       cudaStream_t s);
 void launch_aos_to_soa(const char *aos, long long itemsize, const long long *off,
                        int n, int body, double *const *col, cudaStream_t s);
-// Per-agent target index (int64 record field at `off_target`, or -1 if < 0).
-void launch_targets(const char *aos, long long itemsize, long long off_target, int n, int *tgt,
-                    cudaStream_t s);
+void launch_states_in(const char *aos, long long itemsize, const StateOffsets &o, int n,
+                      const StateCols &c, cudaStream_t s);
+// Writes target, index_leader and active back into the records.
+void launch_states_out(char *aos, long long itemsize, const StateOffsets &o, int n,
+                       const StateCols &c, cudaStream_t s);
 void launch_soa_to_aos(char *aos, long long itemsize, const long long *off,
                        int n, int body, const double *const *col, cudaStream_t s);
 double fp64_peak_gflops();

@@ -1897,21 +1897,45 @@ __global__ void k_soa_to_aos(char *aos, long long itemsize, OffTable off, int n,
     }
 }
 
-// The target field of the packed records is an int64 at any byte offset (2 in
-// the reference dtypes, after two bools): read byte by byte, little-endian.
-__global__ void k_targets(const char *aos, long long itemsize, long long off, int n, int *tgt) {
+// Integer and bool state fields of the packed records (target, active,
+// is_leader, is_follower, index_leader, familiar_exit) sit at any byte offset
+// (target at 2 in the reference dtypes, after two bools): read and written
+// byte by byte, little-endian.
+__device__ __forceinline__ long long ld_int(const char *rec, long long off, int bytes) {
+    const unsigned char *p = reinterpret_cast<const unsigned char *>(rec + off);
+    unsigned long long v = 0;
+    for (int k = 0; k < bytes; ++k) v |= (unsigned long long)p[k] << (8 * k);
+    return (long long)v;
+}
+__device__ __forceinline__ void st_int(char *rec, long long off, int bytes, long long v) {
+    unsigned char *p = reinterpret_cast<unsigned char *>(rec + off);
+    for (int k = 0; k < bytes; ++k) p[k] = (unsigned char)((unsigned long long)v >> (8 * k));
+}
+__device__ __forceinline__ int clamp_index(long long t) {
+    return (t >= 0 && t <= 0x7fffffffLL) ? (int)t : -1;
+}
+
+__global__ void k_states_in(const char *aos, long long itemsize, StateOffsets o, int n,
+                            StateCols c) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    long long t = -1;
-    if (off >= 0) {
-        const unsigned char *p =
-            reinterpret_cast<const unsigned char *>(aos + (size_t)i * itemsize + off);
-        unsigned long long v = 0;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) v |= (unsigned long long)p[k] << (8 * k);
-        t = (long long)v;
-    }
-    tgt[i] = (t >= 0 && t <= 0x7fffffffLL) ? (int)t : -1;
+    const char *rec = aos + (size_t)i * itemsize;
+    c.target[i] = o.target >= 0 ? clamp_index(ld_int(rec, o.target, 8)) : -1;
+    c.active[i] = o.active >= 0 ? (ld_int(rec, o.active, 1) != 0) : 1;
+    c.leader[i] = o.leader >= 0 ? (ld_int(rec, o.leader, 1) != 0) : 0;
+    c.follower[i] = o.follower >= 0 ? (ld_int(rec, o.follower, 1) != 0) : 0;
+    c.index_leader[i] = o.index_leader >= 0 ? clamp_index(ld_int(rec, o.index_leader, 8)) : -1;
+    c.familiar_exit[i] = o.familiar_exit >= 0 ? clamp_index(ld_int(rec, o.familiar_exit, 8)) : -1;
+}
+
+// The state fields the herding and domain nodes change: target, index_leader, active.
+__global__ void k_states_out(char *aos, long long itemsize, StateOffsets o, int n, StateCols c) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    char *rec = aos + (size_t)i * itemsize;
+    if (o.target >= 0) st_int(rec, o.target, 8, c.target[i]);
+    if (o.index_leader >= 0) st_int(rec, o.index_leader, 8, c.index_leader[i]);
+    if (o.active >= 0) st_int(rec, o.active, 1, c.active[i] ? 1 : 0);
 }
 
 __global__ void k_fp64_fma(double *out, int iters, double b, double c) {
@@ -2151,9 +2175,13 @@ void launch_aos_to_soa(const char *aos, long long itemsize, const long long *off
     for (int k = 0; k < NCOL; ++k) c.p[k] = col[k];
     k_aos_to_soa<<<nblk(n, 128), 128, 0, s>>>(aos, itemsize, t, n, body, c);
 }
-void launch_targets(const char *aos, long long itemsize, long long off_target, int n, int *tgt,
-                    cudaStream_t s) {
-    if (n > 0) k_targets<<<nblk(n, 256), 256, 0, s>>>(aos, itemsize, off_target, n, tgt);
+void launch_states_in(const char *aos, long long itemsize, const StateOffsets &o, int n,
+                      const StateCols &c, cudaStream_t s) {
+    if (n > 0) k_states_in<<<nblk(n, 256), 256, 0, s>>>(aos, itemsize, o, n, c);
+}
+void launch_states_out(char *aos, long long itemsize, const StateOffsets &o, int n,
+                       const StateCols &c, cudaStream_t s) {
+    if (n > 0) k_states_out<<<nblk(n, 256), 256, 0, s>>>(aos, itemsize, o, n, c);
 }
 void launch_soa_to_aos(char *aos, long long itemsize, const long long *off, int n, int body,
                        const double *const *col, cudaStream_t s) {

@@ -1,0 +1,321 @@
+// cd_states.cu -- the per-step state nodes around the force step:
+// InsideDomain and TargetReached (simulation/logic.py:343-387) and the
+// leader-follower nodes with and without herding (simulation/logic.py:168-217,
+// core/steering/collective_motion.py:15-279).
+//
+// Herding follows the reference's sequence exactly:
+//  * nearest unobstructed neighbours (find_nearest_neighbors, :71-104): the
+//    reference visits every unordered pair of the cell list once (cell size =
+//    the follower sight) and offers the pair to both agents, each keeping its
+//    size_nearest_other closest in an array whose largest entry (first
+//    arg-max) is replaced.  An agent's array changes only through its own
+//    offers, which it receives in its visiting order (3 x 3 cells in (dx, dy)
+//    order, ascending within a cell), so one thread per agent replays them in
+//    that order.  The line-of-sight test (is_obstacle_between_points over all
+//    walls, with the pair's own orientation) only matters when the distance
+//    would enter the array, and is only evaluated then;
+//  * herding_interaction (:107-155), leader_follower_interaction_brute
+//    (:158-218; leaders in increasing distance, ties by index) and the
+//    combination of leader_follower[_with_herding]_interaction (:221-279),
+//    one thread per follower.
+// Leaders are assumed not to be followers themselves (a follower reads the
+// target of the leader it follows as it was before the update).
+#include <cstdint>
+#include <cmath>
+#include "cd_internal.cuh"
+#include "cd_math.h"
+
+namespace cdk {
+namespace {
+
+constexpr int HNT = 128;
+constexpr int KMAX = 16;
+
+__device__ __forceinline__ void normalize(double &x, double &y) {
+    const double l = cdm_hypot(x, y);
+    if (l != 0.0) {                              // `v / l if l else v`
+        x = x / l;
+        y = y / l;
+    }
+}
+
+// geom2D.line_intersect (core/geom2D.py:36-59)
+__device__ __forceinline__ bool line_intersect(double x0x, double x0y, double x1x, double x1y,
+                                               double y0x, double y0y, double y1x, double y1y) {
+    const double ux = x1x - x0x, uy = x1y - x0y;
+    const double vx = y1x - y0x, vy = y1y - y0y;
+    const double bx = y0x - x0x, by = y0y - x0y;
+    const double d = ux * vy - uy * vx;
+    if (d == 0) return false;
+    const double t0 = bx * vy - by * vx;
+    const double t1 = bx * uy - by * ux;
+    const double s0 = t0 / d, s1 = t1 / d;
+    return 0 <= s0 && s0 <= 1 && 0 <= s1 && s1 <= 1;
+}
+
+// sensory_region.is_obstacle_between_points (core/sensory_region.py:9-16)
+__device__ __forceinline__ bool blocked(const HerdArgs &h, const ScenDev &sc, double ax, double ay,
+                                        double bx, double by) {
+    for (int w = sc.wall_begin; w < sc.wall_begin + sc.wall_count; ++w) {
+        const double *p = h.walls + (size_t)w * WALL_D;
+        if (line_intersect(ax, ay, bx, by, p[0], p[1], p[2], p[3])) return true;
+    }
+    return false;
+}
+
+// herding_relationship (collective_motion.py:24-57): first element.
+__device__ __forceinline__ bool heading_away(const HerdArgs &h, double x1x, double x1y,
+                                             double x2x, double x2y, double v1x, double v1y,
+                                             double v2x, double v2y) {
+    if (cdm_hypot(v1x, v1y) == 0 || cdm_hypot(v2x, v2y) == 0) return false;
+    double ex = x2x - x1x, ey = x2y - x1y;
+    normalize(ex, ey);
+    double n1x = v1x, n1y = v1y, n2x = v2x, n2y = v2y;
+    normalize(n1x, n1y);
+    normalize(n2x, n2y);
+    const double c_i = ex * n1x + ey * n1y;
+    const double c_j = -(ex * n2x + ey * n2y);
+    const double cp = h.cos_phi;
+    (void)c_i;                 // both branches on c_i give the same first element:
+    return !(cp < c_j && c_j < 1.0);           // the other is not heading towards us
+}
+
+__global__ void __launch_bounds__(HNT) k_herd_neighbors(HerdArgs h) {
+    const int s = blockIdx.x * HNT + threadIdx.x;
+    if (s >= h.n) return;
+    const int i = h.perm[s];
+    const ScenDev sc = h.scen_h[h.scen_of[i]];
+    const double *const *col = h.col;
+    const double xi = col[X][i], yi = col[Y][i];
+    int nb[KMAX];
+    double dist[KMAX];
+    const int K = h.K;
+    for (int k = 0; k < K; ++k) { nb[k] = -1; dist[k] = h.sight_f; }
+    double dmax = h.sight_f;
+    const int local = h.key[i] - sc.cell_base;
+    const int ix = local / sc.ny, iy = local - ix * sc.ny;
+    for (int ck = 0; ck < 9; ++ck) {
+        const int jx = ix + ck / 3 - 1, jy = iy + ck % 3 - 1;
+        if (jx < 0 || jx >= sc.nx || jy < 0 || jy >= sc.ny) continue;
+        const int c2 = sc.cell_base + jx * sc.ny + jy;
+        for (int t = h.start[c2]; t < h.start[c2 + 1]; ++t) {
+            if (t == s) continue;
+            const int j = h.perm[t];
+            const double xj = col[X][j], yj = col[Y][j];
+            const double l = cdm_hypot(xi - xj, yi - yj);
+            if (!(l < dmax)) continue;
+            // the pair's first agent is the lower slot
+            const bool first = s < t;
+            if (first ? blocked(h, sc, xi, yi, xj, yj) : blocked(h, sc, xj, yj, xi, yi)) continue;
+            int am = 0;                                 // set_neighbor: first arg-max
+            for (int k = 1; k < K; ++k)
+                if (dist[k] > dist[am]) am = k;
+            nb[am] = j;
+            dist[am] = l;
+            dmax = dist[0];
+            for (int k = 1; k < K; ++k) dmax = dist[k] > dmax ? dist[k] : dmax;
+        }
+    }
+    for (int k = 0; k < K; ++k) h.nbr[(size_t)i * K + k] = nb[k];
+}
+
+__global__ void k_leader_flags(HerdArgs h, int *flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < h.n) flags[i] = h.st.leader[i] ? 1 : 0;
+}
+
+__global__ void k_leader_list(HerdArgs h, const int *pos, int *list) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < h.n && h.st.leader[i]) list[pos[i]] = i;
+}
+
+__global__ void k_target_snapshot(HerdArgs h) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < h.n) h.tgt_before[i] = h.st.target[i];
+}
+
+__global__ void __launch_bounds__(HNT) k_herd_follow(HerdArgs h) {
+    const int i = blockIdx.x * HNT + threadIdx.x;
+    if (i >= h.n || !h.st.follower[i]) return;
+    double *const *col = h.col;
+    const int sid = h.scen_of[i];
+    const ScenDev sc = h.scen_h[sid];
+    const double xi = col[X][i], yi = col[Y][i], vxi = col[VX][i], vyi = col[VY][i];
+    // herding_interaction: average of the neighbours heading away
+    double dhx = 0.0, dhy = 0.0;
+    bool has_dir = false;
+    if (h.with_herding) {
+        double mpx = 0.0, mpy = 0.0, mvx = 0.0, mvy = 0.0;
+        int num = 0;
+        for (int k = 0; k < h.K; ++k) {
+            const int j = h.nbr[(size_t)i * h.K + k];
+            if (j < 0) continue;
+            if (heading_away(h, xi, yi, col[X][j], col[Y][j], vxi, vyi, col[VX][j], col[VY][j])) {
+                mpx += col[X][j];
+                mpy += col[Y][j];
+                mvx += col[VX][j];
+                mvy += col[VY][j];
+                num += 1;
+            }
+        }
+        if (num > 0) {
+            double ax = mpx / num - xi, ay = mpy / num - yi;
+            normalize(ax, ay);
+            double bx = mvx, by = mvy;
+            normalize(bx, by);
+            dhx = h.w_herd * ax + (1 - h.w_herd) * bx;
+            dhy = h.w_herd * ay + (1 - h.w_herd) * by;
+            normalize(dhx, dhy);
+            has_dir = true;
+            h.st.target[i] = -1;                       // NO_TARGET
+        }
+    }
+    // leader_follower_interaction_brute: leaders from the nearest
+    double dlx = 0.0, dly = 0.0;
+    bool strategy = false;
+    int behind = 0, away = 0;
+    const int nl = *h.n_leaders;
+    double pd = -INFINITY;
+    int pj = -1;
+    while (true) {
+        double bd = INFINITY;
+        int bj = -1;
+        for (int q = 0; q < nl; ++q) {
+            const int j = h.leaders[q];
+            if (h.scen_of[j] != sid) continue;
+            const double d = cdm_hypot(xi - col[X][j], yi - col[Y][j]);
+            const bool after = d > pd || (d == pd && j > pj);
+            if (after && (d < bd || (d == bd && j < bj))) { bd = d; bj = j; }
+        }
+        if (bj < 0 || bd > h.sight_l) break;           // the rest are farther
+        pd = bd;
+        pj = bj;
+        const int j = bj;
+        if (blocked(h, sc, xi, yi, col[X][j], col[Y][j])) {
+            const int leader = h.st.index_leader[i];
+            if (leader != -1 && leader == j) {
+                behind += 1;
+                h.st.target[i] = h.tgt_before[leader];
+                strategy = true;
+                break;
+            }
+            continue;
+        }
+        if (heading_away(h, xi, yi, col[X][j], col[Y][j], vxi, vyi, col[VX][j], col[VY][j])) {
+            away += 1;
+            h.st.index_leader[i] = j;
+            h.st.target[i] = -1;
+            double ax = col[X][j] - xi, ay = col[Y][j] - yi;
+            normalize(ax, ay);
+            double bx = col[VX][j], by = col[VY][j];
+            normalize(bx, by);
+            dlx = h.w_lead * ax + (1 - h.w_lead) * bx;
+            dly = h.w_lead * ay + (1 - h.w_lead) * by;
+            normalize(dlx, dly);
+            strategy = true;
+            break;
+        }
+    }
+    if (behind == 0 && away == 0) {
+        const int leader = h.st.index_leader[i];
+        if (leader != -1) {
+            h.st.target[i] = h.tgt_before[leader];
+            strategy = true;
+        }
+    }
+    if (!(has_dir || strategy)) h.st.target[i] = h.st.familiar_exit[i];   // familiar exit
+    double ex = dlx, ey = dly;
+    if (h.with_herding) {
+        ex = h.w_dir * dlx + (1 - h.w_dir) * dhx;
+        ey = h.w_dir * dly + (1 - h.w_dir) * dhy;
+        normalize(ex, ey);
+    }
+    col[E0X][i] = ex;
+    col[E0Y][i] = ey;
+}
+
+// Crossings test (E. Haines, "Point in polygon strategies", Graphics Gems IV,
+// 1994): a horizontal ray from the point crosses the edges an odd number of
+// times.  The ring's closing edge runs from the last vertex to the first.
+__device__ __forceinline__ bool inside_polygon(double tx, double ty, const double2 *v, int m) {
+    bool inside = false;
+    double2 p0 = v[m - 1];
+    bool y0 = p0.y >= ty;
+    for (int k = 0; k < m; ++k) {
+        const double2 p1 = v[k];
+        const bool y1 = p1.y >= ty;
+        if (y0 != y1) {
+            if (((p1.y - ty) * (p0.x - p1.x) >= (p1.x - tx) * (p0.y - p1.y)) == y1)
+                inside = !inside;
+        }
+        y0 = y1;
+        p0 = p1;
+    }
+    return inside;
+}
+
+__global__ void k_inside_domain(int begin, int count, const double *x, const double *y,
+                                int *active, const double2 *poly, int m,
+                                unsigned long long *changed) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int change = 0;
+    if (k < count) {
+        const int i = begin + k;
+        const int now = inside_polygon(x[i], y[i], poly, m) ? 1 : 0;
+        change = active[i] != now;
+        active[i] = now;
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, change);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(changed, (unsigned long long)__popc(b));
+}
+
+__global__ void k_target_reached(int begin, int count, const double *x, const double *y,
+                                 unsigned char *reached, const double2 *polys, const int *voff,
+                                 int t, unsigned long long *counts) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int now = 0;
+    if (k < count) {
+        unsigned char &r = reached[k];
+        if (!r && inside_polygon(x[begin + k], y[begin + k], polys + voff[t],
+                                 voff[t + 1] - voff[t]))
+            r = 1;
+        now = r;
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, now);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(&counts[t], (unsigned long long)__popc(b));
+}
+
+inline int nblk(long long n, int nt) { return (int)((n + nt - 1) / nt); }
+
+}  // namespace
+
+void launch_herd_neighbors(const HerdArgs &h, cudaStream_t s) {
+    if (h.n > 0 && h.with_herding) k_herd_neighbors<<<nblk(h.n, HNT), HNT, 0, s>>>(h);
+}
+void launch_leaders(const HerdArgs &h, int *flags, int *pos, int *scan_scratch, int *list,
+                    cudaStream_t s) {
+    if (h.n <= 0) return;
+    k_leader_flags<<<nblk(h.n, 256), 256, 0, s>>>(h, flags);
+    launch_scan(flags, pos, h.n, scan_scratch, s);      // pos[n] = number of leaders
+    k_leader_list<<<nblk(h.n, 256), 256, 0, s>>>(h, pos, list);
+    k_target_snapshot<<<nblk(h.n, 256), 256, 0, s>>>(h);
+}
+void launch_herd_follow(const HerdArgs &h, cudaStream_t s) {
+    if (h.n > 0) k_herd_follow<<<nblk(h.n, HNT), HNT, 0, s>>>(h);
+}
+void launch_inside_domain(int begin, int count, const double *x, const double *y, int *active,
+                          const double2 *poly, int m, unsigned long long *changed,
+                          cudaStream_t s) {
+    if (count > 0 && m > 0)
+        k_inside_domain<<<nblk(count, 256), 256, 0, s>>>(begin, count, x, y, active, poly, m,
+                                                         changed);
+}
+void launch_target_reached(int begin, int count, const double *x, const double *y,
+                           unsigned char *reached, const double2 *polys, const int *voff, int t,
+                           unsigned long long *counts, cudaStream_t s) {
+    if (count > 0)
+        k_target_reached<<<nblk(count, 256), 256, 0, s>>>(begin, count, x, y, reached, polys, voff,
+                                                          t, counts);
+}
+
+}  // namespace cdk

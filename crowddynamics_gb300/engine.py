@@ -130,6 +130,40 @@ class DeviceBatch:
     def snapshot_wait(self, slot):
         self._chk(self._lib.cd_snapshot_wait(self._ctx, int(slot)))
 
+    def herding(self, with_herding=True, sight_follower=10.0, size_nearest_other=5,
+                sight_leader=20.0, phi=0.45 * math.pi, w_herding=0.15, w_leader=0.40,
+                w_direction=0.65):
+        """Leader-follower update of every follower's target direction,
+        target and index_leader (with herding: nearest unobstructed
+        neighbours as well); defaults are the reference's."""
+        self._chk(self._lib.cd_herding(self._ctx, 1 if with_herding else 0, float(sight_follower),
+                                       int(size_nearest_other), float(sight_leader), float(phi),
+                                       float(w_herding), float(w_leader), float(w_direction)))
+
+    def inside_domain(self, scenario, polygon):
+        """Set ``active`` = inside ``polygon`` ((m, 2) vertices); returns the
+        number of agents whose state changed."""
+        xy = np.ascontiguousarray(polygon, dtype=np.float64).reshape(-1, 2)
+        changed = ctypes.c_int64()
+        self._chk(self._lib.cd_inside_domain(self._ctx, int(scenario), N.ptr(xy), len(xy),
+                                             ctypes.byref(changed)))
+        return changed.value
+
+    def target_reached(self, scenario, polygons, reset=False):
+        """Agents that have been inside each target polygon (since the first
+        call or ``reset``): counts per target."""
+        polys = [np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 2) for p in polygons]
+        if not polys:
+            return np.zeros(0, np.int64)
+        xy = np.ascontiguousarray(np.concatenate(polys))
+        off = np.zeros(len(polys) + 1, np.int64)
+        off[1:] = np.cumsum([len(p) for p in polys])
+        counts = np.zeros(len(polys), np.int64)
+        self._chk(self._lib.cd_target_reached(self._ctx, int(scenario), len(polys), N.ptr(xy),
+                                              N.i64ptr(off), 1 if reset else 0,
+                                              N.i64ptr(counts)))
+        return counts
+
     def set_walls(self, walls):
         rows = walls_as_rows(walls)
         self._chk(self._lib.cd_set_walls(self._ctx, N.ptr(rows), len(rows)))

@@ -85,14 +85,15 @@ BODY_THREE_CIRCLE = 1
 
 #: Field identifiers of the C ABI's offset table, in ``CD_F_*`` order.  Each
 #: entry names a float64 field (vectors are two consecutive float64s), except
-#: ``target`` (int64).
+#: the integer and bool state fields from ``target`` on.
 FIELD_NAMES = (
     'position', 'velocity', 'target_direction', 'force', 'force_prev',
     'radius', 'r_t', 'r_s', 'r_ts', 'mass', 'inertia_rot', 'target_velocity',
     'target_angular_velocity', 'tau_adj', 'k_soc', 'tau_0', 'mu', 'kappa',
     'damping', 'std_rand_force', 'position_ls', 'position_rs', 'orientation',
     'angular_velocity', 'target_orientation', 'torque', 'torque_prev',
-    'tau_rot', 'std_rand_torque', 'target',
+    'tau_rot', 'std_rand_torque', 'target', 'active', 'is_leader', 'is_follower',
+    'index_leader', 'familiar_exit',
 )
 
 

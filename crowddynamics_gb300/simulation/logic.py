@@ -11,6 +11,7 @@ Traits keep the reference's names and defaults.  As in the reference, the
 shape the cell size; the kernels use the reference's constants 3.0 m and
 2000 N (``core/interactions.py:45``, ``core/motion/power_law.py:52``).
 """
+import math
 import os
 import queue
 import threading
@@ -248,3 +249,86 @@ class SaveSimulationData(LogicNode):
             self._thread.join()
             self._thread = None
             self._frames.close()
+
+
+def _polygon_of(geom):
+    """(m, 2) vertices of a polygon given as a shapely-like object (its
+    exterior ring), a (xmin, ymin, xmax, ymax) box, or a vertex array."""
+    if hasattr(geom, 'exterior'):
+        return np.asarray(geom.exterior.coords, dtype=np.float64)
+    arr = np.asarray(geom, dtype=np.float64)
+    if arr.shape == (4,):
+        x0, y0, x1, y1 = arr
+        return np.array([[x0, y0], [x1, y0], [x1, y1], [x0, y1], [x0, y0]])
+    return arr.reshape(-1, 2)
+
+
+class LeaderFollower(LogicNode):
+    """Followers steer towards the nearest visible leader heading away from
+    them, or keep following a leader behind an obstacle, or fall back on a
+    familiar exit (``simulation/logic.py:168-180``,
+    ``core/steering/collective_motion.py:158-243``).  Runs on the device."""
+    sight = 20.0
+
+    def update(self):
+        b = self.simulation._device_state()
+        b.herding(False, sight_follower=1.0, sight_leader=self.sight)
+        self.simulation._device_changed()
+
+
+class LeaderFollowerWithHerding(LogicNode):
+    """Followers average the heading of their ``size_nearest_other`` nearest
+    unobstructed neighbours within ``sight_follower`` that head away from them
+    and combine it with leader following (``simulation/logic.py:183-217``,
+    ``core/steering/collective_motion.py:71-155,246-279``).  Runs on the
+    device."""
+    sight_follower = 10.0
+    size_nearest_other = 5
+
+    def update(self):
+        b = self.simulation._device_state()
+        b.herding(True, sight_follower=self.sight_follower,
+                  size_nearest_other=self.size_nearest_other)
+        self.simulation._device_changed()
+
+
+class InsideDomain(LogicNode):
+    """Agents outside the field's domain become inactive; counts state changes
+    in ``data['inactive']`` (``simulation/logic.py:343-357``).  Runs on the
+    device (crossings point-in-polygon test)."""
+
+    def __init__(self, simulation, name=None, **traits):
+        super().__init__(simulation, name=name, **traits)
+        self.simulation.data['inactive'] = 0
+        self.polygon = _polygon_of(simulation.field.domain)
+
+    def update(self):
+        sim = self.simulation
+        changed = sim._device_state().inside_domain(0, self.polygon)
+        sim._device_changed()
+        sim.data['inactive'] = dict.__getitem__(sim.data, 'inactive') + changed
+
+
+class TargetReached(LogicNode):
+    """Counts, per target polygon of the field, the agents that have reached
+    it, in ``data['target_{index}']`` (``simulation/logic.py:360-387``; the
+    reference passes the whole agent array where the positions are meant).
+    Runs on the device."""
+    prefix = 'target_{index}'
+
+    def __init__(self, simulation, name=None, **traits):
+        super().__init__(simulation, name=name, **traits)
+        self.polygons = [_polygon_of(t) for t in simulation.field.targets]
+        self.names = [self.prefix.format(index=i) for i in range(len(self.polygons))]
+        for name_ in self.names:
+            self.simulation.data[name_] = 0
+        self._first = True
+
+    def update(self):
+        if not self.polygons:
+            return
+        sim = self.simulation
+        counts = sim._device_state().target_reached(0, self.polygons, reset=self._first)
+        self._first = False
+        for name_, c in zip(self.names, counts):
+            sim.data[name_] = int(c)

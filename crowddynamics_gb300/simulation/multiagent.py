@@ -140,6 +140,21 @@ class MultiAgentSimulation:
                                            int(self.data.get('iterations', 0)))
         return self._batch
 
+    def _device_state(self):
+        """The device batch holding the current state, for host nodes that act
+        on it (pending device nodes already flushed; host edits uploaded)."""
+        b = self._ensure_batch()
+        mirror = self.agents._mirror
+        if mirror is not None and mirror.host_dirty:
+            b.upload(self.agents._array)
+            mirror.host_dirty = False
+        return b
+
+    def _device_changed(self):
+        """A host node changed the device state."""
+        if self.agents._mirror is not None:
+            self.agents._mirror.device_newer = True
+
     def _use_direction_maps(self, node):
         """Upload the Navigation node's maps when they change."""
         b = self._ensure_batch()

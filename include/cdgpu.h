@@ -82,6 +82,11 @@ enum {
     CD_F_ANGULAR_VELOCITY, CD_F_TARGET_ORIENTATION, CD_F_TORQUE,
     CD_F_TORQUE_PREV, CD_F_TAU_ROT, CD_F_STD_RAND_TORQUE,
     CD_F_TARGET,                  /* int64: target index, -1 for none */
+    CD_F_ACTIVE,                  /* bool */
+    CD_F_IS_LEADER,               /* bool */
+    CD_F_IS_FOLLOWER,             /* bool */
+    CD_F_INDEX_LEADER,            /* int64: leader agent, -1 for none */
+    CD_F_FAMILIAR_EXIT,           /* int64: target, -1 for none */
     CD_F_COUNT
 };
 
@@ -113,8 +118,8 @@ void cd_destroy(cd_ctx *ctx);
 
 /* Copy `n` (= total agents) packed host records of `itemsize` bytes into the
  * device.  `field_offsets` holds CD_F_COUNT byte offsets (-1 = absent);
- * float64 fields must be 4-byte aligned, the int64 CD_F_TARGET may sit at
- * any offset.  Recomputes timestep maxima. */
+ * float64 fields must be 4-byte aligned; the integer and bool fields
+ * (CD_F_TARGET and after) may sit at any offset.  Recomputes timestep maxima. */
 int cd_upload_agents(cd_ctx *ctx, const void *records, int64_t n,
                      int64_t itemsize, const int64_t *field_offsets);
 /* Write the device state back into `n` packed host records.  Whole records
@@ -135,6 +140,31 @@ int cd_download_agents(cd_ctx *ctx, void *records, int64_t n, int64_t itemsize,
 int cd_snapshot_agents(cd_ctx *ctx, int slot, void *records, int64_t n, int64_t itemsize,
                        const int64_t *field_offsets, double *dt, double *time_tot);
 int cd_snapshot_wait(cd_ctx *ctx, int slot);
+
+/* ---- state nodes between steps ------------------------------------------ */
+/* LeaderFollowerWithHerding (with_herding = 1; simulation/logic.py:183-217 with
+ * leader_follower_with_herding_interaction, core/steering/collective_motion.py:
+ * 246-279) or LeaderFollower (with_herding = 0; logic.py:168-180 with
+ * leader_follower_interaction, :221-243) for every follower: the target
+ * direction, target and index_leader (and, with herding, the nearest
+ * `size_nearest_other` <= 16 unobstructed neighbours within `sight_follower`,
+ * on a cell list of that cell size).  Reference arguments: sight_leader 20
+ * (herding) or the node's sight, phi 0.45 pi, weights 0.15 (herding
+ * position), 0.40 (leader position), 0.65 (leader direction). */
+int cd_herding(cd_ctx *ctx, int with_herding, double sight_follower,
+               int64_t size_nearest_other, double sight_leader, double phi,
+               double w_herding, double w_leader, double w_direction);
+/* InsideDomain (simulation/logic.py:343-357): `active` = position inside the
+ * polygon (n_vertices (x, y) pairs, a ring) for the scenario's agents;
+ * `changed` receives the number of agents whose state flipped. */
+int cd_inside_domain(cd_ctx *ctx, int64_t scenario, const double *xy, int64_t n_vertices,
+                     int64_t *changed);
+/* TargetReached (simulation/logic.py:360-387): per target polygon t (vertices
+ * xy[vertex_offsets[t] .. vertex_offsets[t+1])), remember the agents found
+ * inside it (since the first call, or since `reset`) and return their
+ * number in counts[t].  At most 256 targets. */
+int cd_target_reached(cd_ctx *ctx, int64_t scenario, int64_t n_targets, const double *xy,
+                      const int64_t *vertex_offsets, int reset, int64_t *counts);
 
 /* Replace all walls: `n_walls` rows of (p0x, p0y, p1x, p1y) float64, split
  * among scenarios by their wall ranges.  Walls are binned into the cells of

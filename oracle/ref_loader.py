@@ -28,6 +28,7 @@ executes the reference files by path, unchanged:
 Files executed: core/vector2D.py, core/structures.py, core/distance.py,
 core/motion/contact.py, core/motion/power_law.py, core/motion/adjusting.py,
 core/integrator.py, core/interactions.py, core/steering/orientation.py,
+core/geom2D.py, core/sensory_region.py, core/steering/collective_motion.py,
 exceptions.py.
 """
 import importlib.util
@@ -94,6 +95,8 @@ def _make_numba():
     tys = types.ModuleType('numba.types')
     tys.Tuple = _Inert()
     tys.UniTuple = _Inert()
+    tys.f8 = _Inert()
+    tys.boolean = _Inert()
     tys.Float = Float
     tys.Array = Array
     nb.types = tys
@@ -168,6 +171,8 @@ def _make_agents_module():
     m.agent_type_three_circle = A.agent_type_three_circle
     m.AgentModelToType = A.AgentModelToType
     m.is_model = A.is_model
+    m.NO_TARGET = -1                  # simulation/agents.py:27-28
+    m.NO_LEADER = -1
 
     def shoulders(agents):
         # simulation/agents.py:482-486, element by element
@@ -193,6 +198,10 @@ _FILES = [
     ('crowddynamics.core.integrator', 'crowddynamics/core/integrator.py'),
     ('crowddynamics.core.interactions', 'crowddynamics/core/interactions.py'),
     ('crowddynamics.core.steering.orientation', 'crowddynamics/core/steering/orientation.py'),
+    ('crowddynamics.core.geom2D', 'crowddynamics/core/geom2D.py'),
+    ('crowddynamics.core.sensory_region', 'crowddynamics/core/sensory_region.py'),
+    ('crowddynamics.core.steering.collective_motion',
+     'crowddynamics/core/steering/collective_motion.py'),
 ]
 
 _loaded = None
@@ -212,8 +221,13 @@ def load():
     nb, tys = _make_numba()
     traitlets = types.ModuleType('traitlets')
     traitlets.TraitError = type('TraitError', (Exception,), {})
+    typing_mod = types.ModuleType('numba.typing')
+    typeof_mod = types.ModuleType('numba.typing.typeof')
+    typeof_mod.typeof = lambda x: _Inert()
+    typing_mod.typeof = typeof_mod
     stubs = {
         'numba': nb, 'numba.types': tys, 'traitlets': traitlets,
+        'numba.typing': typing_mod, 'numba.typing.typeof': typeof_mod,
         'cell_lists': _make_cell_lists(),
     }
     for pkg in ('crowddynamics', 'crowddynamics.core', 'crowddynamics.core.motion',

@@ -189,12 +189,57 @@ def navigation_cases():
          dir_x=np.stack([m[0] for m in maps]), dir_y=np.stack([m[1] for m in maps]), **out)
 
 
+def herding_cases():
+    """LeaderFollowerWithHerding and LeaderFollower (simulation/logic.py:
+    168-217) through the reference's own collective_motion code: a walled
+    room with interior walls (line of sight), 10% leaders with targets, 70%
+    followers, random velocities, some followers remembering a leader; the
+    herding cell list (cell = follower sight) on the grid the device uses
+    (the scenario's origin, ceil(extent / sight) cells per axis)."""
+    import math
+    R = RL.load()
+    out = {}
+    for mode, seed in (('herding', 41), ('leader', 42)):
+        rng = np.random.default_rng(seed)
+        scen = S.room(n=240, size=24.0, seed=seed)
+        walls = S.walls_array([((6.0, 4.0), (6.0, 16.0)), ((12.0, 20.0), (20.0, 12.0)),
+                               ((2.0, 10.0), (9.0, 10.5))])
+        walls = np.concatenate([scen.walls, walls])
+        a = scen.agents
+        n = len(a)
+        a['velocity'] = rng.normal(0, 1, (n, 2))
+        a['velocity'][rng.uniform(size=n) < 0.05] = 0.0
+        a['is_leader'] = rng.uniform(size=n) < 0.1
+        a['is_follower'] = ~a['is_leader'] & (rng.uniform(size=n) < 0.7)
+        a['target'] = np.where(a['is_leader'], rng.integers(0, 3, n), -1)
+        a['familiar_exit'] = rng.integers(-1, 3, n)
+        leaders = np.flatnonzero(a['is_leader'])
+        mem = a['is_follower'] & (rng.uniform(size=n) < 0.3)
+        a['index_leader'][mem] = rng.choice(leaders, mem.sum())
+        before = a.copy()
+        x0, y0, cell, nx, ny = scen.grid
+        if mode == 'herding':
+            sight = 10.0
+            RL.configure_grid(x0, y0, sight, max(1, math.ceil(nx * cell / sight)),
+                              max(1, math.ceil(ny * cell / sight)))
+            d = R.collective_motion.leader_follower_with_herding_interaction(a, walls, sight, 5)
+        else:
+            d = R.collective_motion.leader_follower_interaction(a, walls, 20.0)
+        f = a['is_follower']
+        a['target_direction'][f] = d[f]
+        out[mode + '_before'] = before
+        out[mode + '_after'] = a.copy()
+        out[mode + '_walls'] = walls
+        out[mode + '_grid'] = np.array(scen.grid, dtype=np.float64)
+    save('herding', **out)
+
+
 CASES = {'scenarios': lambda: (
              scenario_case('hallway_small', S.hallway(n=120, width=20.0, height=6.0, seed=3), 3,
                            21),
              scenario_case('room_small', S.room(n=150, size=12.0, seed=4), 3, 22)),
          'pairs': pair_cases, 'walls': wall_cases, 'misc': misc_cases,
-         'navigation': navigation_cases}
+         'navigation': navigation_cases, 'herding': herding_cases}
 
 
 def main():

@@ -129,3 +129,29 @@ def test_oracle_navigation_live_against_reference(oracle):
         oracle.navigation(a, np.stack([m[0] for m in maps]), np.stack([m[1] for m in maps]),
                           bounds[0], bounds[1], step)
         assert np.array_equal(a['target_direction'], ref['target_direction'])
+
+
+def test_herding_fixture_reproduces_reference():
+    """The herding fixture is the reference's own collective_motion output
+    (re-run live when the reference source is present)."""
+    import math
+    from oracle import ref_loader as RL
+    if not RL.available():
+        pytest.skip('reference source tree not present')
+    R = RL.load()
+    d = np.load(os.path.join(GOLDEN, 'herding.npz'))
+    for mode in ('herding', 'leader'):
+        a = d[mode + '_before'].copy()
+        walls = d[mode + '_walls']
+        x0, y0, cell, nx, ny = d[mode + '_grid']
+        if mode == 'herding':
+            RL.configure_grid(x0, y0, 10.0, max(1, math.ceil(nx * cell / 10.0)),
+                              max(1, math.ceil(ny * cell / 10.0)))
+            e = R.collective_motion.leader_follower_with_herding_interaction(a, walls, 10.0, 5)
+        else:
+            e = R.collective_motion.leader_follower_interaction(a, walls, 20.0)
+        f = a['is_follower']
+        a['target_direction'][f] = e[f]
+        want = d[mode + '_after']
+        for name in ('target_direction', 'target', 'index_leader'):
+            assert np.array_equal(a[name], want[name]), (mode, name)
