@@ -54,13 +54,16 @@ __device__ __forceinline__ bool line_intersect(double x0x, double x0y, double x1
 }
 
 // sensory_region.is_obstacle_between_points (core/sensory_region.py:9-16)
-__device__ __forceinline__ bool blocked(const HerdArgs &h, const ScenDev &sc, double ax, double ay,
-                                        double bx, double by) {
-    for (int w = sc.wall_begin; w < sc.wall_begin + sc.wall_count; ++w) {
+// over a warp: lanes take the walls in turn (the result does not depend on
+// the order).  Called by all 32 lanes with the same arguments.
+__device__ __forceinline__ bool blocked_warp(const HerdArgs &h, const ScenDev &sc, double ax,
+                                             double ay, double bx, double by, int lane) {
+    bool hit = false;
+    for (int w = sc.wall_begin + lane; w < sc.wall_begin + sc.wall_count && !hit; w += 32) {
         const double *p = h.walls + (size_t)w * WALL_D;
-        if (line_intersect(ax, ay, bx, by, p[0], p[1], p[2], p[3])) return true;
+        hit = line_intersect(ax, ay, bx, by, p[0], p[1], p[2], p[3]);
     }
-    return false;
+    return __any_sync(0xffffffffu, hit);
 }
 
 // herding_relationship (collective_motion.py:24-57): first element.
@@ -80,9 +83,13 @@ __device__ __forceinline__ bool heading_away(const HerdArgs &h, double x1x, doub
     return !(cp < c_j && c_j < 1.0);           // the other is not heading towards us
 }
 
+// One warp per agent: the lanes measure 32 candidates at a time; those
+// closer than the agent's current farthest kept neighbour (which only
+// shrinks) are offered in slot order with all lanes carrying the same array.
 __global__ void __launch_bounds__(HNT) k_herd_neighbors(HerdArgs h) {
-    const int s = blockIdx.x * HNT + threadIdx.x;
-    if (s >= h.n) return;
+    const int s = (int)(((long long)blockIdx.x * HNT + threadIdx.x) / 32);
+    const int lane = threadIdx.x & 31;
+    if (s >= h.n) return;                                // whole warps leave together
     const int i = h.perm[s];
     const ScenDev sc = h.scen_h[h.scen_of[i]];
     const double *const *col = h.col;
@@ -90,7 +97,8 @@ __global__ void __launch_bounds__(HNT) k_herd_neighbors(HerdArgs h) {
     int nb[KMAX];
     double dist[KMAX];
     const int K = h.K;
-    for (int k = 0; k < K; ++k) { nb[k] = -1; dist[k] = h.sight_f; }
+#pragma unroll
+    for (int k = 0; k < KMAX; ++k) { nb[k] = -1; dist[k] = h.sight_f; }
     double dmax = h.sight_f;
     const int local = h.key[i] - sc.cell_base;
     const int ix = local / sc.ny, iy = local - ix * sc.ny;
@@ -98,25 +106,47 @@ __global__ void __launch_bounds__(HNT) k_herd_neighbors(HerdArgs h) {
         const int jx = ix + ck / 3 - 1, jy = iy + ck % 3 - 1;
         if (jx < 0 || jx >= sc.nx || jy < 0 || jy >= sc.ny) continue;
         const int c2 = sc.cell_base + jx * sc.ny + jy;
-        for (int t = h.start[c2]; t < h.start[c2 + 1]; ++t) {
-            if (t == s) continue;
-            const int j = h.perm[t];
-            const double xj = col[X][j], yj = col[Y][j];
-            const double l = cdm_hypot(xi - xj, yi - yj);
-            if (!(l < dmax)) continue;
-            // the pair's first agent is the lower slot
-            const bool first = s < t;
-            if (first ? blocked(h, sc, xi, yi, xj, yj) : blocked(h, sc, xj, yj, xi, yi)) continue;
-            int am = 0;                                 // set_neighbor: first arg-max
-            for (int k = 1; k < K; ++k)
-                if (dist[k] > dist[am]) am = k;
-            nb[am] = j;
-            dist[am] = l;
-            dmax = dist[0];
-            for (int k = 1; k < K; ++k) dmax = dist[k] > dmax ? dist[k] : dmax;
+        const int b = h.start[c2], e = h.start[c2 + 1];
+        for (int base = b; base < e; base += 32) {
+            const int t = base + lane;
+            int j = -1;
+            double l = INFINITY;
+            if (t < e && t != s) {
+                j = h.perm[t];
+                l = cdm_hypot(xi - col[X][j], yi - col[Y][j]);
+            }
+            unsigned m = __ballot_sync(0xffffffffu, l < dmax);
+            while (m) {
+                const int k = __ffs(m) - 1;
+                m &= m - 1;
+                const double lk = __shfl_sync(0xffffffffu, l, k);
+                const int jk = __shfl_sync(0xffffffffu, j, k);
+                if (!(lk < dmax)) continue;
+                const double xj = col[X][jk], yj = col[Y][jk];
+                // the pair's first agent is the lower slot
+                const bool first = s < base + k;
+                if (first ? blocked_warp(h, sc, xi, yi, xj, yj, lane)
+                          : blocked_warp(h, sc, xj, yj, xi, yi, lane))
+                    continue;
+                int am = 0;                                  // set_neighbor: first arg-max
+#pragma unroll
+                for (int q = 1; q < KMAX; ++q)
+                    if (q < K && dist[q] > dist[am]) am = q;
+#pragma unroll
+                for (int q = 0; q < KMAX; ++q)
+                    if (q == am) { nb[q] = jk; dist[q] = lk; }
+                dmax = dist[0];
+#pragma unroll
+                for (int q = 1; q < KMAX; ++q)
+                    if (q < K) dmax = dist[q] > dmax ? dist[q] : dmax;
+            }
         }
     }
-    for (int k = 0; k < K; ++k) h.nbr[(size_t)i * K + k] = nb[k];
+    if (lane < K) {
+#pragma unroll
+        for (int q = 0; q < KMAX; ++q)
+            if (q == lane) h.nbr[(size_t)i * K + q] = nb[q];
+    }
 }
 
 __global__ void k_leader_flags(HerdArgs h, int *flags) {
@@ -134,9 +164,13 @@ __global__ void k_target_snapshot(HerdArgs h) {
     if (i < h.n) h.tgt_before[i] = h.st.target[i];
 }
 
+// One warp per follower: every lane carries the same values (control flow is
+// uniform), the lanes share the scan for the next-nearest leader, lane 0
+// writes.
 __global__ void __launch_bounds__(HNT) k_herd_follow(HerdArgs h) {
-    const int i = blockIdx.x * HNT + threadIdx.x;
-    if (i >= h.n || !h.st.follower[i]) return;
+    const int i = (int)(((long long)blockIdx.x * HNT + threadIdx.x) / 32);
+    const int lane = threadIdx.x & 31;
+    if (i >= h.n || !h.st.follower[i]) return;          // whole warps leave together
     double *const *col = h.col;
     const int sid = h.scen_of[i];
     const ScenDev sc = h.scen_h[sid];
@@ -166,8 +200,7 @@ __global__ void __launch_bounds__(HNT) k_herd_follow(HerdArgs h) {
             dhx = h.w_herd * ax + (1 - h.w_herd) * bx;
             dhy = h.w_herd * ay + (1 - h.w_herd) * by;
             normalize(dhx, dhy);
-            has_dir = true;
-            h.st.target[i] = -1;                       // NO_TARGET
+            has_dir = true;                            // target becomes NO_TARGET
         }
     }
     // leader_follower_interaction_brute: leaders from the nearest
@@ -177,25 +210,33 @@ __global__ void __launch_bounds__(HNT) k_herd_follow(HerdArgs h) {
     const int nl = *h.n_leaders;
     double pd = -INFINITY;
     int pj = -1;
+    int leader_now = h.st.index_leader[i];
+    int target_now = has_dir ? -1 : h.st.target[i];
     while (true) {
         double bd = INFINITY;
-        int bj = -1;
-        for (int q = 0; q < nl; ++q) {
+        int bj = 0x7fffffff;
+        for (int q = lane; q < nl; q += 32) {
             const int j = h.leaders[q];
             if (h.scen_of[j] != sid) continue;
             const double d = cdm_hypot(xi - col[X][j], yi - col[Y][j]);
             const bool after = d > pd || (d == pd && j > pj);
             if (after && (d < bd || (d == bd && j < bj))) { bd = d; bj = j; }
         }
-        if (bj < 0 || bd > h.sight_l) break;           // the rest are farther
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {               // nearest (distance, index) in the warp
+            const double od = __shfl_xor_sync(0xffffffffu, bd, o);
+            const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+            if (od < bd || (od == bd && oj < bj)) { bd = od; bj = oj; }
+        }
+        if (bj == 0x7fffffff || bd > h.sight_l) break;  // the rest are farther
         pd = bd;
         pj = bj;
         const int j = bj;
-        if (blocked(h, sc, xi, yi, col[X][j], col[Y][j])) {
-            const int leader = h.st.index_leader[i];
+        if (blocked_warp(h, sc, xi, yi, col[X][j], col[Y][j], lane)) {
+            const int leader = leader_now;
             if (leader != -1 && leader == j) {
                 behind += 1;
-                h.st.target[i] = h.tgt_before[leader];
+                target_now = h.tgt_before[leader];
                 strategy = true;
                 break;
             }
@@ -203,8 +244,8 @@ __global__ void __launch_bounds__(HNT) k_herd_follow(HerdArgs h) {
         }
         if (heading_away(h, xi, yi, col[X][j], col[Y][j], vxi, vyi, col[VX][j], col[VY][j])) {
             away += 1;
-            h.st.index_leader[i] = j;
-            h.st.target[i] = -1;
+            leader_now = j;
+            target_now = -1;
             double ax = col[X][j] - xi, ay = col[Y][j] - yi;
             normalize(ax, ay);
             double bx = col[VX][j], by = col[VY][j];
@@ -217,21 +258,25 @@ __global__ void __launch_bounds__(HNT) k_herd_follow(HerdArgs h) {
         }
     }
     if (behind == 0 && away == 0) {
-        const int leader = h.st.index_leader[i];
+        const int leader = leader_now;
         if (leader != -1) {
-            h.st.target[i] = h.tgt_before[leader];
+            target_now = h.tgt_before[leader];
             strategy = true;
         }
     }
-    if (!(has_dir || strategy)) h.st.target[i] = h.st.familiar_exit[i];   // familiar exit
+    if (!(has_dir || strategy)) target_now = h.st.familiar_exit[i];   // familiar exit
     double ex = dlx, ey = dly;
     if (h.with_herding) {
         ex = h.w_dir * dlx + (1 - h.w_dir) * dhx;
         ey = h.w_dir * dly + (1 - h.w_dir) * dhy;
         normalize(ex, ey);
     }
-    col[E0X][i] = ex;
-    col[E0Y][i] = ey;
+    if (lane == 0) {
+        h.st.index_leader[i] = leader_now;
+        h.st.target[i] = target_now;
+        col[E0X][i] = ex;
+        col[E0Y][i] = ey;
+    }
 }
 
 // Crossings test (E. Haines, "Point in polygon strategies", Graphics Gems IV,
@@ -290,7 +335,8 @@ inline int nblk(long long n, int nt) { return (int)((n + nt - 1) / nt); }
 }  // namespace
 
 void launch_herd_neighbors(const HerdArgs &h, cudaStream_t s) {
-    if (h.n > 0 && h.with_herding) k_herd_neighbors<<<nblk(h.n, HNT), HNT, 0, s>>>(h);
+    if (h.n > 0 && h.with_herding)
+        k_herd_neighbors<<<nblk((long long)h.n * 32, HNT), HNT, 0, s>>>(h);
 }
 void launch_leaders(const HerdArgs &h, int *flags, int *pos, int *scan_scratch, int *list,
                     cudaStream_t s) {
@@ -301,7 +347,7 @@ void launch_leaders(const HerdArgs &h, int *flags, int *pos, int *scan_scratch, 
     k_target_snapshot<<<nblk(h.n, 256), 256, 0, s>>>(h);
 }
 void launch_herd_follow(const HerdArgs &h, cudaStream_t s) {
-    if (h.n > 0) k_herd_follow<<<nblk(h.n, HNT), HNT, 0, s>>>(h);
+    if (h.n > 0) k_herd_follow<<<nblk((long long)h.n * 32, HNT), HNT, 0, s>>>(h);
 }
 void launch_inside_domain(int begin, int count, const double *x, const double *y, int *active,
                           const double2 *poly, int m, unsigned long long *changed,

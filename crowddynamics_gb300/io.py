@@ -9,9 +9,9 @@
 
 ``save_npy`` and ``save_csv`` keep the reference's coroutine protocol: send
 ``None`` to start, then alternately a value and a bool (True dumps).
-``AgentFrameWriter`` is the form the device path uses: frames are appended to
-a raw file as they arrive and turned into the ``.npy`` file at a dump, so the
-host holds at most one frame.
+``AgentFrameWriter`` is the form the device path uses: frames are appended as
+they arrive (kept in memory, or in a raw side file beyond a size limit) and
+written as the ``.npy`` file at a dump.
 """
 import csv
 import json
@@ -61,41 +61,61 @@ def load_npy_concatenated(directory, basename):
 
 class AgentFrameWriter:
     """``{basename}_{index}.npy`` files built from frames appended one at a
-    time: each frame goes to a raw side file; ``dump()`` writes the ``.npy``
-    (same format as ``np.save(np.vstack(frames))``) and starts over."""
+    time.  Frames are kept in memory until ``dump()`` writes them with
+    ``np.save`` (the reference's format: the stacked frames); beyond
+    ``spill_bytes`` of buffered frames they go to a raw side file instead and
+    the dump copies them from there."""
 
-    def __init__(self, directory, basename, dtype, n):
+    def __init__(self, directory, basename, dtype, n, spill_bytes=256 << 20):
         self.path = os.path.join(directory, basename + '_{index}.npy')
         self.raw = os.path.join(directory, '.' + basename + '.frames')
         self.dtype = np.dtype(dtype)
         self.n = int(n)
+        self.spill_bytes = int(spill_bytes)
         self.index = 0
-        self.frames = 0
-        self._fp = open(self.raw, 'wb')
+        self.frames = []
+        self.spilled = 0
+        self._fp = None
 
     def append(self, records):
-        rec = np.ascontiguousarray(records)
-        assert rec.dtype == self.dtype and rec.shape == (self.n,)
-        self._fp.write(rec.tobytes())
-        self.frames += 1
+        rec = np.array(records, dtype=self.dtype, copy=True)
+        assert rec.shape == (self.n,)
+        if self._fp is None and (len(self.frames) + 1) * rec.nbytes > self.spill_bytes:
+            self._fp = open(self.raw, 'wb')
+            for f in self.frames:
+                self._fp.write(f.tobytes())
+            self.spilled = len(self.frames)
+            self.frames = []
+        if self._fp is not None:
+            self._fp.write(rec.tobytes())
+            self.spilled += 1
+        else:
+            self.frames.append(rec)
 
     def dump(self):
-        self._fp.flush()
-        self._fp.close()
-        out = np.lib.format.open_memmap(self.path.format(index=self.index), mode='w+',
-                                        dtype=self.dtype, shape=(self.frames, self.n))
-        if self.frames and self.n:
-            raw = np.memmap(self.raw, dtype=self.dtype, mode='r', shape=(self.frames, self.n))
-            out[:] = raw
-            del raw
-        out.flush()
-        del out
+        path = self.path.format(index=self.index)
+        if self._fp is None:
+            np.save(path, np.stack(self.frames) if self.frames else
+                    np.zeros((0, self.n), self.dtype))
+        else:
+            self._fp.close()
+            self._fp = None
+            out = np.lib.format.open_memmap(path, mode='w+', dtype=self.dtype,
+                                            shape=(self.spilled, self.n))
+            if self.spilled and self.n:
+                out[:] = np.memmap(self.raw, dtype=self.dtype, mode='r',
+                                   shape=(self.spilled, self.n))
+            out.flush()
+            del out
+            os.unlink(self.raw)
         self.index += 1
-        self.frames = 0
-        self._fp = open(self.raw, 'wb')
+        self.frames = []
+        self.spilled = 0
 
     def close(self):
-        self._fp.close()
+        if self._fp is not None:
+            self._fp.close()
+            self._fp = None
         if os.path.exists(self.raw):
             os.unlink(self.raw)
 

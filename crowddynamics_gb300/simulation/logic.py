@@ -139,8 +139,9 @@ class SaveSimulationData(LogicNode):
     The frame comes from the device without stopping it: the update enqueues
     an asynchronous copy of the state (and of dt, time_tot) into one of a few
     page-locked slots, behind the steps already enqueued; a writer thread
-    waits for each copy, appends it to the frame file and writes the data row.
-    The host never waits for the device here except when all slots are busy.
+    waits for each copy, keeps the frame and writes the data row; a dump
+    writes the buffered frames.  The host never waits for the device here
+    except when all slots are busy.
     (The reference buffers references to the live agent array, so every frame
     of one of its files shows the state at the dump; here each frame is the
     state at its own update.)"""
@@ -201,7 +202,7 @@ class SaveSimulationData(LogicNode):
             batch, slot, keys, values, save, offset = item
             try:
                 batch.snapshot_wait(slot)
-                self._frames.append(self._records[slot])
+                self._frames.append(self._records[slot])          # copies the slot
                 dt, tt = float(self._times[slot][0][0]), float(self._times[slot][1][0])
                 self._free.put(slot)
                 row = {k: (dt if k == 'dt' else tt + offset if k == 'time_tot' else values[k])

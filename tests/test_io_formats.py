@@ -62,9 +62,11 @@ def test_save_csv_matches_reference(tmp_path):
     assert open(tmp_path / 'ref' / 'x.csv').read() == open(tmp_path / 'ours' / 'x.csv').read()
 
 
-def test_frame_writer_equals_np_save(tmp_path):
+@pytest.mark.parametrize('spill', [256 << 20, 3 * 316 * 30])
+def test_frame_writer_equals_np_save(tmp_path, spill):
+    """In memory and spilled to the side file: the same .npy bytes."""
     a = S.room(n=30, size=8.0, seed=2).agents
-    w = IO.AgentFrameWriter(str(tmp_path), 'agents', a.dtype, len(a))
+    w = IO.AgentFrameWriter(str(tmp_path), 'agents', a.dtype, len(a), spill_bytes=spill)
     frames = []
     for k in range(5):
         f = a.copy()
