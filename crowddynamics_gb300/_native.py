@@ -41,7 +41,7 @@ SYMBOLS = (
     'cd_measure_fp64_peak', 'cd_agent_agent_noalloc', 'cd_variant_count',
     'cd_variant_shape', 'cd_set_variant', 'cd_set_near_list_capacity', 'cd_pair_kernel_time',
     'cd_set_direction_maps', 'cd_set_noise_mode', 'cd_snapshot_agents', 'cd_snapshot_wait',
-    'cd_herding', 'cd_inside_domain', 'cd_target_reached',
+    'cd_herding', 'cd_inside_domain', 'cd_target_reached', 'cd_exit_detection',
     'cd_launch',
     'cd_rollout_loss',
 )
@@ -118,6 +118,7 @@ def load(path=None):
                                       ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_double]),
         'cd_inside_domain': (ctypes.c_int, [P, i64, P, i64, pi64]),
+        'cd_exit_detection': (ctypes.c_int, [P, i64, P, i64, ctypes.c_double]),
         'cd_target_reached': (ctypes.c_int, [P, i64, i64, P, pi64, ctypes.c_int, pi64]),
         'cd_set_direction_maps': (ctypes.c_int, [P, i64, i64, P, P, i64, i64, ctypes.c_double,
                                                  ctypes.c_double, ctypes.c_double]),

@@ -840,6 +840,25 @@ int cd_inside_domain(cd_ctx *c, int64_t scenario, const double *xy, int64_t n_ve
     return check_device_error(c);
 }
 
+int cd_exit_detection(cd_ctx *c, int64_t scenario, const double *centers, int64_t n_doors,
+                      double detection_range) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (scenario < 0 || scenario >= c->nscen) return fail(c, CD_ERR_INVALID_VALUE, "bad scenario");
+    if (n_doors < 0 || (n_doors > 0 && !centers))
+        return fail(c, CD_ERR_INVALID_VALUE, "bad door centres");
+    if (!c->have_records) return fail(c, CD_ERR_INVALID_VALUE, "no agents uploaded");
+    if (n_doors == 0) return CD_OK;
+    std::vector<int64_t> voff = {0, n_doors};
+    if (int rc = upload_polygons(c, 1, centers, voff.data())) return rc;
+    const cd_scenario &sc = c->scen_host[scenario];
+    cdk::launch_exit_detection((int)sc.agent_begin, (int)sc.agent_count, c->col[cdk::X],
+                               c->col[cdk::Y], c->walls, (int)sc.wall_begin, (int)sc.wall_count,
+                               c->polys, (int)n_doors, detection_range, state_cols(c), c->stream);
+    c->states_dirty = true;
+    CUDA_OR_FAIL(c, cudaGetLastError());
+    return check_device_error(c);
+}
+
 int cd_target_reached(cd_ctx *c, int64_t scenario, int64_t n_targets, const double *xy,
                       const int64_t *vertex_offsets, int reset, int64_t *counts) {
     if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");

@@ -126,6 +126,10 @@ void launch_herd_follow(const HerdArgs &h, cudaStream_t s);
 void launch_inside_domain(int begin, int count, const double *x, const double *y, int *active,
                           const double2 *poly, int m, unsigned long long *changed,
                           cudaStream_t s);
+void launch_exit_detection(int begin, int count, const double *x, const double *y,
+                           const double *walls, int wall_begin, int wall_count,
+                           const double2 *doors, int n_doors, double range, const StateCols &st,
+                           cudaStream_t s);
 void launch_target_reached(int begin, int count, const double *x, const double *y,
                            unsigned char *reached, const double2 *polys, const int *voff, int t,
                            unsigned long long *counts, cudaStream_t s);
@@ -193,7 +197,7 @@ void launch_aos_to_soa(const char *aos, long long itemsize, const long long *off
                        int n, int body, double *const *col, cudaStream_t s);
 void launch_states_in(const char *aos, long long itemsize, const StateOffsets &o, int n,
                       const StateCols &c, cudaStream_t s);
-// Writes target, index_leader and active back into the records.
+// Writes target, index_leader, active and is_follower back into the records.
 void launch_states_out(char *aos, long long itemsize, const StateOffsets &o, int n,
                        const StateCols &c, cudaStream_t s);
 void launch_soa_to_aos(char *aos, long long itemsize, const long long *off,

@@ -1928,7 +1928,8 @@ __global__ void k_states_in(const char *aos, long long itemsize, StateOffsets o,
     c.familiar_exit[i] = o.familiar_exit >= 0 ? clamp_index(ld_int(rec, o.familiar_exit, 8)) : -1;
 }
 
-// The state fields the herding and domain nodes change: target, index_leader, active.
+// The state fields the state nodes change: target, index_leader, active,
+// is_follower.
 __global__ void k_states_out(char *aos, long long itemsize, StateOffsets o, int n, StateCols c) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -1936,6 +1937,7 @@ __global__ void k_states_out(char *aos, long long itemsize, StateOffsets o, int 
     if (o.target >= 0) st_int(rec, o.target, 8, c.target[i]);
     if (o.index_leader >= 0) st_int(rec, o.index_leader, 8, c.index_leader[i]);
     if (o.active >= 0) st_int(rec, o.active, 1, c.active[i] ? 1 : 0);
+    if (o.follower >= 0) st_int(rec, o.follower, 1, c.follower[i] ? 1 : 0);
 }
 
 __global__ void k_fp64_fma(double *out, int iters, double b, double c) {

@@ -279,6 +279,40 @@ __global__ void __launch_bounds__(HNT) k_herd_follow(HerdArgs h) {
     }
 }
 
+// ExitDetection (simulation/logic.py:220-237 with exit_detection,
+// core/evacuation.py:139-174): the nearest door centre within the range that
+// is in line of sight (agent to door); a follower that sees one takes it as
+// its target and stops following.
+__global__ void k_exit_detection(int begin, int count, const double *x, const double *y,
+                                 const double *walls, int wall_begin, int wall_count,
+                                 const double2 *doors, int n_doors, double range,
+                                 StateCols st) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const int i = begin + k;
+    const double px = x[i], py = y[i];
+    double dist = range;
+    int found = -1;
+    for (int c = 0; c < n_doors; ++c) {
+        const double2 d = doors[c];
+        bool hit = false;
+        for (int w = wall_begin; w < wall_begin + wall_count && !hit; ++w) {
+            const double *p = walls + (size_t)w * WALL_D;
+            hit = line_intersect(px, py, d.x, d.y, p[0], p[1], p[2], p[3]);
+        }
+        if (hit) continue;
+        const double l = cdm_hypot(d.x - px, d.y - py);
+        if (l < dist) {
+            dist = l;
+            found = c;
+        }
+    }
+    if (found >= 0 && st.follower[i]) {
+        st.target[i] = found;
+        st.follower[i] = 0;
+    }
+}
+
 // Crossings test (E. Haines, "Point in polygon strategies", Graphics Gems IV,
 // 1994): a horizontal ray from the point crosses the edges an odd number of
 // times.  The ring's closing edge runs from the last vertex to the first.
@@ -355,6 +389,14 @@ void launch_inside_domain(int begin, int count, const double *x, const double *y
     if (count > 0 && m > 0)
         k_inside_domain<<<nblk(count, 256), 256, 0, s>>>(begin, count, x, y, active, poly, m,
                                                          changed);
+}
+void launch_exit_detection(int begin, int count, const double *x, const double *y,
+                           const double *walls, int wall_begin, int wall_count,
+                           const double2 *doors, int n_doors, double range, const StateCols &st,
+                           cudaStream_t s) {
+    if (count > 0)
+        k_exit_detection<<<nblk(count, 256), 256, 0, s>>>(begin, count, x, y, walls, wall_begin,
+                                                          wall_count, doors, n_doors, range, st);
 }
 void launch_target_reached(int begin, int count, const double *x, const double *y,
                            unsigned char *reached, const double2 *polys, const int *voff, int t,

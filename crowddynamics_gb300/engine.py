@@ -149,6 +149,13 @@ class DeviceBatch:
                                              ctypes.byref(changed)))
         return changed.value
 
+    def exit_detection(self, scenario, centers, detection_range=20.0):
+        """Followers that see a door centre within range take the nearest as
+        their target and stop following."""
+        c = np.ascontiguousarray(centers, dtype=np.float64).reshape(-1, 2)
+        self._chk(self._lib.cd_exit_detection(self._ctx, int(scenario), N.ptr(c), len(c),
+                                              float(detection_range)))
+
     def target_reached(self, scenario, polygons, reset=False):
         """Agents that have been inside each target polygon (since the first
         call or ``reset``): counts per target."""

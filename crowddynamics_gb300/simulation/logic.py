@@ -333,3 +333,19 @@ class TargetReached(LogicNode):
         self._first = False
         for name_, c in zip(self.names, counts):
             sim.data[name_] = int(c)
+
+
+class ExitDetection(LogicNode):
+    """Followers that see the centre of a target (door) within
+    ``detection_range`` take the nearest as their target and stop following
+    (``simulation/logic.py:220-237``, ``core/evacuation.py:139-174``).  Door
+    centres are the means of the targets' vertices.  Runs on the device."""
+    detection_range = 20.0
+
+    def update(self):
+        sim = self.simulation
+        centers = np.array([np.mean(_polygon_of(t), axis=0) for t in sim.field.targets])
+        if not len(centers):
+            return
+        sim._device_state().exit_detection(0, centers, self.detection_range)
+        sim._device_changed()

@@ -159,6 +159,12 @@ int cd_herding(cd_ctx *ctx, int with_herding, double sight_follower,
  * `changed` receives the number of agents whose state flipped. */
 int cd_inside_domain(cd_ctx *ctx, int64_t scenario, const double *xy, int64_t n_vertices,
                      int64_t *changed);
+/* ExitDetection (simulation/logic.py:220-237, core/evacuation.py:139-174): for
+ * the scenario's agents, the nearest of the `n_doors` door centres (x, y
+ * pairs) within `detection_range` in line of sight; a follower that detects
+ * one takes it as its target and stops following. */
+int cd_exit_detection(cd_ctx *ctx, int64_t scenario, const double *centers, int64_t n_doors,
+                      double detection_range);
 /* TargetReached (simulation/logic.py:360-387): per target polygon t (vertices
  * xy[vertex_offsets[t] .. vertex_offsets[t+1])), remember the agents found
  * inside it (since the first call, or since `reset`) and return their

@@ -29,7 +29,7 @@ Files executed: core/vector2D.py, core/structures.py, core/distance.py,
 core/motion/contact.py, core/motion/power_law.py, core/motion/adjusting.py,
 core/integrator.py, core/interactions.py, core/steering/orientation.py,
 core/geom2D.py, core/sensory_region.py, core/steering/collective_motion.py,
-exceptions.py.
+core/evacuation.py, exceptions.py.
 """
 import importlib.util
 import os
@@ -89,7 +89,7 @@ def _make_numba():
     nb.njit = jit
     nb.vectorize = vectorize
     nb.generated_jit = generated_jit
-    for name in ('f8', 'i8', 'void', 'float64', 'int64', 'boolean', 'b1'):
+    for name in ('f8', 'i8', 'void', 'float64', 'int64', 'boolean', 'b1', 'optional'):
         setattr(nb, name, _Inert())
     nb.typeof = lambda x: _Inert()
     tys = types.ModuleType('numba.types')
@@ -202,6 +202,7 @@ _FILES = [
     ('crowddynamics.core.sensory_region', 'crowddynamics/core/sensory_region.py'),
     ('crowddynamics.core.steering.collective_motion',
      'crowddynamics/core/steering/collective_motion.py'),
+    ('crowddynamics.core.evacuation', 'crowddynamics/core/evacuation.py'),
 ]
 
 _loaded = None

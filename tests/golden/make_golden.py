@@ -234,12 +234,35 @@ def herding_cases():
     save('herding', **out)
 
 
+def exit_cases():
+    """ExitDetection (simulation/logic.py:220-237) through the reference's own
+    exit_detection: a walled room with an interior wall, three door centres,
+    followers taking the nearest visible door within 20 m."""
+    R = RL.load()
+    rng = np.random.default_rng(51)
+    scen = S.room(n=300, size=30.0, seed=51)
+    walls = np.concatenate([scen.walls, S.walls_array([((10.0, 5.0), (10.0, 25.0)),
+                                                       ((18.0, 10.0), (26.0, 12.0))])])
+    a = scen.agents
+    n = len(a)
+    a['is_follower'] = rng.uniform(size=n) < 0.6
+    a['target'] = -1
+    doors = np.array([[30.0, 15.0], [0.0, 15.0], [15.0, 30.0]])
+    before = a.copy()
+    targets, detected = R.evacuation.exit_detection(doors, a['position'], walls, 20.0)
+    mask = a['is_follower'] & detected
+    a['target'][mask] = targets[mask]
+    a['is_follower'][mask] = False
+    save('exit', before=before, after=a, walls=walls, doors=doors,
+         grid=np.array(scen.grid, dtype=np.float64))
+
+
 CASES = {'scenarios': lambda: (
              scenario_case('hallway_small', S.hallway(n=120, width=20.0, height=6.0, seed=3), 3,
                            21),
              scenario_case('room_small', S.room(n=150, size=12.0, seed=4), 3, 22)),
          'pairs': pair_cases, 'walls': wall_cases, 'misc': misc_cases,
-         'navigation': navigation_cases, 'herding': herding_cases}
+         'navigation': navigation_cases, 'herding': herding_cases, 'exit': exit_cases}
 
 
 def main():

@@ -121,3 +121,19 @@ def test_state_nodes_in_simulation(native):
     assert sim.data['target_0'] == int((a['position'][:, 0] >= 15.0).sum())
     assert int((~sim.agents.array['active']).sum()) == 40
     sim.close()
+
+
+def test_exit_detection_matches_reference(native):
+    d = np.load(os.path.join(GOLDEN, 'exit.npz'))
+    before, want, walls = d['before'], d['after'], d['walls']
+    g = d['grid']
+    b = DeviceBatch('three_circle', [dict(n_agents=len(before), n_walls=len(walls),
+                                          grid=(g[0], g[1], g[2], int(g[3]), int(g[4])))])
+    b.upload(before)
+    b.set_walls(walls)
+    b.exit_detection(0, d['doors'], 20.0)
+    got = before.copy()
+    b.download(got)
+    b.close()
+    assert np.array_equal(got['target'], want['target'])
+    assert np.array_equal(got['is_follower'], want['is_follower'])

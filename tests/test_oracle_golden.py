@@ -155,3 +155,17 @@ def test_herding_fixture_reproduces_reference():
         want = d[mode + '_after']
         for name in ('target_direction', 'target', 'index_leader'):
             assert np.array_equal(a[name], want[name]), (mode, name)
+
+
+def test_exit_fixture_reproduces_reference():
+    from oracle import ref_loader as RL
+    if not RL.available():
+        pytest.skip('reference source tree not present')
+    R = RL.load()
+    d = np.load(os.path.join(GOLDEN, 'exit.npz'))
+    a = d['before'].copy()
+    targets, detected = R.evacuation.exit_detection(d['doors'], a['position'], d['walls'], 20.0)
+    mask = a['is_follower'] & detected
+    a['target'][mask] = targets[mask]
+    a['is_follower'][mask] = False
+    assert np.array_equal(a, d['after'])
