@@ -67,6 +67,7 @@ struct cd_ctx {
     double *v0max = nullptr, *dt = nullptr, *time_tot = nullptr;
     double *ext = nullptr, *max_partial = nullptr;      // per-scenario max extent, scratch
     double *ext_host = nullptr;                        // pinned copy of ext
+    int *status_host = nullptr;                        // pinned: error word, near-list need
     int *err = nullptr, *work = nullptr;
     int *diag = nullptr;
     // near lists of the compute-once pair pipeline (entries allocated on use)
@@ -202,6 +203,7 @@ void release(cd_ctx *c) {
     for (cudaEvent_t e : c->evsnap)
         if (e) cudaEventDestroy(e);
     if (c->ext_host) cudaFreeHost(c->ext_host);
+    if (c->status_host) cudaFreeHost(c->status_host);
     if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -396,15 +398,29 @@ cdk::StateCols state_cols(cd_ctx *c) {
     return k;
 }
 
-int check_device_error(cd_ctx *c) {
-    CUDA_OR_FAIL(c, cudaGetLastError());
-    int h = 0, need = 0;
-    const bool pairs = c->nl_cap > 0 && c->n > 0;       // lists in use (pair pipeline, adjoint)
-    CUDA_OR_FAIL(c, cudaMemcpyAsync(&h, c->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    if (pairs)
-        CUDA_OR_FAIL(c, cudaMemcpyAsync(&need, c->nl_off + c->n, sizeof(int),
+// Enqueue the copies of the error word and the near-list need into pinned
+// host memory (asynchronous; read by check_device_error after the next
+// synchronisation).
+int enqueue_status(cd_ctx *c) {
+    c->status_host[1] = 0;
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(&c->status_host[0], c->err, sizeof(int),
+                                    cudaMemcpyDeviceToHost, c->stream));
+    if (c->nl_cap > 0 && c->n > 0)
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(&c->status_host[1], c->nl_off + c->n, sizeof(int),
                                         cudaMemcpyDeviceToHost, c->stream));
-    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    return CD_OK;
+}
+
+// `enqueued`: the caller already enqueued the status copies before its own
+// synchronisation (one synchronisation for both).
+int check_device_error(cd_ctx *c, bool enqueued = false) {
+    CUDA_OR_FAIL(c, cudaGetLastError());
+    const bool pairs = c->nl_cap > 0 && c->n > 0;       // lists in use (pair pipeline, adjoint)
+    if (!enqueued) {
+        if (int rc = enqueue_status(c)) return rc;
+        CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    }
+    const int h = c->status_host[0], need = c->status_host[1];
     // the last list build did not fit: its step ran the fallback; grow for the next
     if (pairs && need > c->nl_cap)
         if (int rc = grow_near_lists(c, need)) return rc;
@@ -537,6 +553,8 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->max_partial, cdk::scen_max_partials((int)n_scenarios)));
     if (rc == CD_OK && cudaMallocHost((void **)&c->ext_host, sizeof(double) * n_scenarios) != cudaSuccess)
         rc = fail(c, CD_ERR_CUDA, "cudaMallocHost failed");
+    if (rc == CD_OK && cudaMallocHost((void **)&c->status_host, sizeof(int) * 2) != cudaSuccess)
+        rc = fail(c, CD_ERR_CUDA, "cudaMallocHost failed");
     step(dalloc(c, &c->dt, n_scenarios));
     step(dalloc(c, &c->time_tot, n_scenarios));
     step(dalloc(c, &c->err, 1));
@@ -668,8 +686,9 @@ int cd_download_agents(cd_ctx *c, void *records, int64_t n, int64_t itemsize, co
                                state_cols(c), c->stream);
     CUDA_OR_FAIL(c, cudaMemcpyAsync(records, c->aos, n * itemsize, cudaMemcpyDeviceToHost, c->stream));
     CUDA_OR_FAIL(c, cudaGetLastError());
+    if (int rc = enqueue_status(c)) return rc;
     CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
-    return check_device_error(c);
+    return check_device_error(c, true);
 }
 
 int cd_snapshot_agents(cd_ctx *c, int slot, void *records, int64_t n, int64_t itemsize,

@@ -13,7 +13,20 @@ import numpy as np
 from crowddynamics_gb300 import _native as N
 from crowddynamics_gb300.exceptions import InvalidType, InvalidValue
 from crowddynamics_gb300.simulation.agents import (
-    BODY_CIRCULAR, BODY_THREE_CIRCLE, body_type_of, field_offsets)
+    BODY_CIRCULAR, BODY_THREE_CIRCLE, body_type_of)
+from crowddynamics_gb300.simulation.agents import field_offsets as _field_offsets
+
+_OFFSETS = {}
+
+
+def field_offsets(dtype):
+    """The C ABI offset table of ``dtype`` (computed once per dtype, read-only)."""
+    off = _OFFSETS.get(dtype)
+    if off is None:
+        off = _field_offsets(dtype)
+        off.flags.writeable = False
+        _OFFSETS[dtype] = off
+    return off
 
 
 def walls_as_rows(walls):
