@@ -75,6 +75,7 @@ struct cd_ctx {
     int *nl_idx = nullptr;
     double *nl_res = nullptr;
     int *fw_cnt = nullptr, *fw_off = nullptr, *fw_scan = nullptr;
+    int *fs_cnt = nullptr, *fs_off = nullptr, *fs_scan = nullptr;
     int2 *fw_pairs = nullptr;
     int64_t nl_cap = 0;
     bool nl_fixed = false;              // capacity set by cd_set_near_list_capacity
@@ -167,6 +168,9 @@ StepArgs args_of(cd_ctx *c, int nodes) {
     a.fw_off = c->fw_off;
     a.fw_pairs = c->fw_pairs;
     a.fw_scan = c->fw_scan;
+    a.fs_cnt = c->fs_cnt;
+    a.fs_off = c->fs_off;
+    a.fs_scan = c->fs_scan;
     return a;
 }
 
@@ -189,7 +193,7 @@ void release(cd_ctx *c) {
                     c->nl_scan, c->nl_idx, c->nl_res, c->fw_cnt, c->fw_off, c->fw_scan,
                     c->fw_pairs, c->ext, c->max_partial, c->tgt, c->navmap, c->rng_step,
                     c->states, c->herd, c->scen_h, c->counters, c->reached, c->polys,
-                    c->poly_off};
+                    c->poly_off, c->fs_cnt, c->fs_off, c->fs_scan};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -308,7 +312,7 @@ int64_t kernels_per_step(const cd_ctx *c, int nodes) {
     k += (nodes & CD_NODE_INTEGRATE) ? 1 : 0;           // dt
     k += cdk::scan_scratch_ints((int)c->ncells) > 1 ? 3 : 1;
     if (cdk::variant_pairs(c->variant) && (nodes & CD_NODE_AGENT_AGENT) && c->nl_cnt)
-        k += 4 + 2 * (cdk::scan_scratch_ints((int)c->n) > 1 ? 3 : 1);   // count fill pairs fallback + 2 scans
+        k += 4 + 3 * (cdk::scan_scratch_ints((int)c->n) > 1 ? 3 : 1);   // count fill pairs fallback + 3 scans
     return k;
 }
 
@@ -567,6 +571,9 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->fw_cnt, n + 1));
     step(dalloc(c, &c->fw_off, n + 1));
     step(dalloc(c, &c->fw_scan, cdk::scan_scratch_ints((int)npad)));
+    step(dalloc(c, &c->fs_cnt, n + 1));
+    step(dalloc(c, &c->fs_off, n + 1));
+    step(dalloc(c, &c->fs_scan, cdk::scan_scratch_ints((int)npad)));
     if (rc == CD_OK) {
         cudaMemcpy(c->scen_of, c->scen_of_host.data(), sizeof(int) * npad, cudaMemcpyHostToDevice);
         cudaMemcpy(c->scen, c->scen_dev.data(), sizeof(ScenDev) * n_scenarios, cudaMemcpyHostToDevice);

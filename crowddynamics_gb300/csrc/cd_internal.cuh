@@ -86,6 +86,8 @@ struct StepArgs {
     int *fw_cnt, *fw_off;        // per slot: entries with a later slot (n + 1 each)
     int2 *fw_pairs;              // flat list of (slot, entry) for those entries
     int *fw_scan;                // scan scratch
+    int *fs_cnt, *fs_off;        // per agent: those guessed to need the social force, scan
+    int *fs_scan;                // scan scratch
 };
 
 // Pair-result record of one near-list entry: (fx, fy, torque, interacts);

@@ -1563,33 +1563,58 @@ __device__ __forceinline__ void candidate_runs(const StepArgs &a, const ScenDev 
     }
 }
 
+// Velocity of cell-sorted slot s in the staged records.
+__device__ __forceinline__ double2 staged_velocity(const StepArgs &a, int s) {
+    return a.body ? a.stage[(size_t)s * STAGE_Q_TC + 3] : a.stage[(size_t)s * STAGE_Q_CIRC + 1];
+}
+
+// Float32 guess that a forward pair will need the social force: the bound
+// on the skin distance below 3 m and the two approaching.  Only the order of
+// the flat pair list depends on it (pairs guessed so come first, so that
+// warps of the pair kernel mostly take the same branches); every pair writes
+// only its own two entries, so no result does.
+__device__ __forceinline__ bool social_guess(float4 me, float4 o, double2 vme, double2 vo) {
+    const float dx = me.x - o.x, dy = me.y - o.y;
+    const float hb = sqrtf(dx * dx + dy * dy) - (me.z + o.z);
+    const float b = -(dx * ((float)vme.x - (float)vo.x) + dy * ((float)vme.y - (float)vo.y));
+    return hb < 3.0f && b > 0.0f;
+}
+
 template <int L>
 __global__ void __launch_bounds__(NTG) k_nl_count(StepArgs a) {
     const int r = threadIdx.x & (L - 1);
     const int s = (int)(((long long)blockIdx.x * NTG + threadIdx.x) / L);
-    int cnt = 0, fwd = 0;
+    int cnt = 0, fwd = 0, soc = 0;
     if (s < a.n) {
         const int i = a.perm[s];
         const ScenDev sc = a.scen[a.scen_of[i]];
         const float4 me = a.cull[s];
+        const double2 vme = staged_velocity(a, s);
         int rb[3], re[3];
         candidate_runs(a, sc, a.key[i], rb, re);
 #pragma unroll
         for (int d = 0; d < 3; ++d)
-            for (int t = rb[d] + r; t < re[d]; t += L)
-                if (t != s && !pair_far(me, __ldg(&a.cull[t]))) {
+            for (int t = rb[d] + r; t < re[d]; t += L) {
+                const float4 o = __ldg(&a.cull[t]);
+                if (t != s && !pair_far(me, o)) {
                     ++cnt;
-                    fwd += t > s;
+                    if (t > s) {
+                        ++fwd;
+                        soc += social_guess(me, o, vme, staged_velocity(a, t));
+                    }
                 }
+            }
     }
 #pragma unroll
     for (int o = L / 2; o > 0; o >>= 1) {
         cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
         fwd += __shfl_xor_sync(0xffffffffu, fwd, o);
+        soc += __shfl_xor_sync(0xffffffffu, soc, o);
     }
     if (s < a.n && r == 0) {
         a.nl_cnt[s] = cnt;
         a.fw_cnt[s] = fwd;
+        a.fs_cnt[s] = soc;
     }
 }
 
@@ -1609,20 +1634,36 @@ __global__ void __launch_bounds__(NTG) k_nl_fill(StepArgs a) {
     candidate_runs(a, sc, a.key[i], rb, re);
     // entries with a later slot follow all earlier ones (ascending order)
     const int fwd0 = a.nl_off[s] + (a.nl_cnt[s] - a.fw_cnt[s]);
-    const int fbase = a.fw_off[s] - fwd0;
     int pos = a.nl_off[s];
+    // the flat list of pairs: first every pair guessed to need the social
+    // force, then the others, each part in slot order
+    int p0 = a.fs_off[s];
+    int p1 = a.fs_off[a.n] + (a.fw_off[s] - a.fs_off[s]);
+    const double2 vme = staged_velocity(a, s);
+    const unsigned lower = (1u << r) - 1u;
 #pragma unroll
     for (int d = 0; d < 3; ++d)
         for (int base = rb[d]; base < re[d]; base += L) {
             const int t = base + r;
-            const bool near = t < re[d] && t != s && !pair_far(me, __ldg(&a.cull[t]));
+            bool near = false, guess = false;
+            if (t < re[d] && t != s) {
+                const float4 o = __ldg(&a.cull[t]);
+                near = !pair_far(me, o);
+                if (near && t > s) guess = social_guess(me, o, vme, staged_velocity(a, t));
+            }
             const unsigned gb = (__ballot_sync(gm, near) >> g0) & GMASK;
+            const unsigned fb = (__ballot_sync(gm, near && t > s) >> g0) & GMASK;
+            const unsigned sb = (__ballot_sync(gm, guess) >> g0) & GMASK;
             if (near) {
-                const int e = pos + __popc(gb & ((1u << r) - 1u));
+                const int e = pos + __popc(gb & lower);
                 a.nl_idx[e] = t;
-                if (t > s) a.fw_pairs[fbase + e] = make_int2(s, e);
+                if (t > s)
+                    a.fw_pairs[guess ? p0 + __popc(sb & lower)
+                                     : p1 + __popc(fb & ~sb & lower)] = make_int2(s, e);
             }
             pos += __popc(gb);
+            p0 += __popc(sb);
+            p1 += __popc(fb & ~sb);
         }
     if (r == 0) a.nl_fwd[s] = fwd0;
 }
@@ -1712,9 +1753,10 @@ __device__ __forceinline__ void gather_agent(const StepArgs &a, const int s) {
     double fx, fy, tq, phi0;
     agent_prologue<BODY>(a, i, fx, fy, tq, phi0);
     if (a.nodes & N_AGENT) {
+        const double4_32a *res = reinterpret_cast<const double4_32a *>(a.nl_res);
         const int o1 = a.nl_off[s + 1];
         for (int e = a.nl_off[s]; e < o1; ++e) {
-            const double4_32a v = *reinterpret_cast<const double4_32a *>(a.nl_res + (size_t)e * RES_D);
+            const double4_32a v = res[e];
             if (v.w != 0.0) {
                 fx = fx + v.x;
                 fy = fy + v.y;
@@ -2110,6 +2152,7 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
         kNlCount[l]<<<nb, NTG, 0, s>>>(a);
         launch_scan(a.nl_cnt, a.nl_off, a.n, a.nl_scan, s);
         launch_scan(a.fw_cnt, a.fw_off, a.n, a.fw_scan, s);
+        launch_scan(a.fs_cnt, a.fs_off, a.n, a.fs_scan, s);
         kNlFill[l]<<<nb, NTG, 0, s>>>(a);
         int rp = (dev >= 0 && dev < 64) ? g_pairs_blocks[dev][body][l] : 0;
         if (rp <= 0) rp = 152;
@@ -2152,6 +2195,7 @@ void launch_near_lists(const StepArgs &a, cudaStream_t s) {
     kNlCount[1]<<<nb, NTG, 0, s>>>(a);
     launch_scan(a.nl_cnt, a.nl_off, a.n, a.nl_scan, s);
     launch_scan(a.fw_cnt, a.fw_off, a.n, a.fw_scan, s);
+    launch_scan(a.fs_cnt, a.fs_off, a.n, a.fs_scan, s);
     kNlFill[1]<<<nb, NTG, 0, s>>>(a);
 }
 
