@@ -26,6 +26,7 @@
 #include <cstdint>
 #include <algorithm>
 #include <cmath>
+#include <cuda_fp16.h>
 #include "cd_internal.cuh"
 #include "cd_math.h"
 #include "cd_noise.h"
@@ -439,6 +440,17 @@ __device__ __forceinline__ double extent_tc(double x, double y, double xl, doubl
     return e;
 }
 
+// Velocity as two halves in one float's bits (the cull record's w): used
+// only for the order of the flat pair list, never for a result.
+__device__ __forceinline__ float pack_velocity(double vx, double vy) {
+    const __half2 h = __floats2half2_rn((float)vx, (float)vy);
+    return __uint_as_float(*reinterpret_cast<const unsigned *>(&h));
+}
+__device__ __forceinline__ float2 unpack_velocity(float w) {
+    const unsigned u = __float_as_uint(w);
+    return __half22float2(*reinterpret_cast<const __half2 *>(&u));
+}
+
 __device__ __forceinline__ float up_f(double v) {
     float f = (float)v;
     return f + fabsf(f) * 1e-6f + 1e-6f;
@@ -458,7 +470,8 @@ __global__ void k_gather(StepArgs a) {
         p[4] = make_double2(c[MU][i], c[KAPPA][i]);
         p[5] = make_double2(c[DAMP][i], 0.0);
         double e = c[R][i];
-        a.cull[s] = make_float4((float)c[X][i], (float)c[Y][i], up_f(e), 0.f);
+        a.cull[s] = make_float4((float)c[X][i], (float)c[Y][i], up_f(e),
+                                pack_velocity(c[VX][i], c[VY][i]));
     } else {
         double2 *p = a.stage + (size_t)s * STAGE_Q_TC;
         double x = c[X][i], y = c[Y][i];
@@ -477,7 +490,7 @@ __global__ void k_gather(StepArgs a) {
         p[9] = make_double2(cs, 0.0);
         double e = extent_tc(x, y, c[XLS][i], c[YLS][i], c[XRS][i], c[YRS][i], c[RT][i], c[RS][i]);
         float xh = (float)x, yh = (float)y;
-        a.cull[s] = make_float4(xh, yh, up_f(e), 0.f);
+        a.cull[s] = make_float4(xh, yh, up_f(e), pack_velocity(c[VX][i], c[VY][i]));
         // position = float hi + float lo; shoulder centres relative to the torso
         a.stage_f[2 * s] = make_float4((float)(x - (double)xh), (float)(y - (double)yh),
                                        (float)c[RT][i], (float)c[RS][i]);
@@ -1563,20 +1576,16 @@ __device__ __forceinline__ void candidate_runs(const StepArgs &a, const ScenDev 
     }
 }
 
-// Velocity of cell-sorted slot s in the staged records.
-__device__ __forceinline__ double2 staged_velocity(const StepArgs &a, int s) {
-    return a.body ? a.stage[(size_t)s * STAGE_Q_TC + 3] : a.stage[(size_t)s * STAGE_Q_CIRC + 1];
-}
-
 // Float32 guess that a forward pair will need the social force: the bound
 // on the skin distance below 3 m and the two approaching.  Only the order of
 // the flat pair list depends on it (pairs guessed so come first, so that
 // warps of the pair kernel mostly take the same branches); every pair writes
 // only its own two entries, so no result does.
-__device__ __forceinline__ bool social_guess(float4 me, float4 o, double2 vme, double2 vo) {
+__device__ __forceinline__ bool social_guess(float4 me, float4 o) {
     const float dx = me.x - o.x, dy = me.y - o.y;
+    const float2 vm = unpack_velocity(me.w), vo = unpack_velocity(o.w);
     const float hb = sqrtf(dx * dx + dy * dy) - (me.z + o.z);
-    const float b = -(dx * ((float)vme.x - (float)vo.x) + dy * ((float)vme.y - (float)vo.y));
+    const float b = -(dx * (vm.x - vo.x) + dy * (vm.y - vo.y));
     return hb < 3.0f && b > 0.0f;
 }
 
@@ -1589,7 +1598,6 @@ __global__ void __launch_bounds__(NTG) k_nl_count(StepArgs a) {
         const int i = a.perm[s];
         const ScenDev sc = a.scen[a.scen_of[i]];
         const float4 me = a.cull[s];
-        const double2 vme = staged_velocity(a, s);
         int rb[3], re[3];
         candidate_runs(a, sc, a.key[i], rb, re);
 #pragma unroll
@@ -1600,7 +1608,7 @@ __global__ void __launch_bounds__(NTG) k_nl_count(StepArgs a) {
                     ++cnt;
                     if (t > s) {
                         ++fwd;
-                        soc += social_guess(me, o, vme, staged_velocity(a, t));
+                        soc += social_guess(me, o);
                     }
                 }
             }
@@ -1639,7 +1647,6 @@ __global__ void __launch_bounds__(NTG) k_nl_fill(StepArgs a) {
     // force, then the others, each part in slot order
     int p0 = a.fs_off[s];
     int p1 = a.fs_off[a.n] + (a.fw_off[s] - a.fs_off[s]);
-    const double2 vme = staged_velocity(a, s);
     const unsigned lower = (1u << r) - 1u;
 #pragma unroll
     for (int d = 0; d < 3; ++d)
@@ -1649,7 +1656,7 @@ __global__ void __launch_bounds__(NTG) k_nl_fill(StepArgs a) {
             if (t < re[d] && t != s) {
                 const float4 o = __ldg(&a.cull[t]);
                 near = !pair_far(me, o);
-                if (near && t > s) guess = social_guess(me, o, vme, staged_velocity(a, t));
+                if (near && t > s) guess = social_guess(me, o);
             }
             const unsigned gb = (__ballot_sync(gm, near) >> g0) & GMASK;
             const unsigned fb = (__ballot_sync(gm, near && t > s) >> g0) & GMASK;
