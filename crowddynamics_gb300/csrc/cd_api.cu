@@ -82,6 +82,7 @@ struct cd_ctx {
 
     char *aos = nullptr;
     int64_t aos_bytes = 0, itemsize = 0;
+    bool direct_host = true;               // pinned host records: device reads/writes them
     int64_t off[CD_F_COUNT];
     bool have_records = false;
 
@@ -456,6 +457,26 @@ bool aligned_field(int64_t off, int64_t itemsize, int width) {
     return off >= 0 && (off % 4) == 0 && off + 8 * width <= itemsize;
 }
 
+// The device address of host memory [p, p + bytes) when all of it is pinned
+// and mapped for the device (both ends inside one mapping), else null.
+const void *device_view_of_host(const void *p, int64_t bytes) {
+    if (!p || bytes <= 0) return nullptr;
+    cudaPointerAttributes a0{}, a1{};
+    const char *last = static_cast<const char *>(p) + (bytes - 1);
+    if (cudaPointerGetAttributes(&a0, p) != cudaSuccess ||
+        cudaPointerGetAttributes(&a1, last) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer ||
+        !a1.devicePointer)
+        return nullptr;
+    const char *d0 = static_cast<const char *>(a0.devicePointer);
+    if (static_cast<const char *>(a1.devicePointer) - d0 != bytes - 1) return nullptr;
+    if (reinterpret_cast<uintptr_t>(d0) % 4) return nullptr;
+    return d0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -639,6 +660,12 @@ int cd_upload_agents(cd_ctx *c, const void *records, int64_t n, int64_t itemsize
                 return fail(c, CD_ERR_INVALID_TYPE, "record lacks a ThreeCircle field");
         }
     if (itemsize % 4) return fail(c, CD_ERR_INVALID_TYPE, "record size must be a multiple of 4");
+    // optional float64 fields, where present, obey the same alignment
+    for (int f = 0; f < CD_F_TARGET; ++f) {
+        const int width = (f <= CD_F_FORCE_PREV || f == CD_F_POSITION_LS || f == CD_F_POSITION_RS) ? 2 : 1;
+        if (off[f] >= 0 && !aligned_field(off[f], itemsize, width))
+            return fail(c, CD_ERR_INVALID_TYPE, "float64 record field not 4-byte aligned");
+    }
     int64_t bytes = n * itemsize;
     if (bytes > c->aos_bytes) {
         if (c->aos) cudaFree(c->aos);
@@ -649,10 +676,18 @@ int cd_upload_agents(cd_ctx *c, const void *records, int64_t n, int64_t itemsize
     c->itemsize = itemsize;
     std::memcpy(c->off, off, sizeof(int64_t) * CD_F_COUNT);
     if (n > 0) {
-        CUDA_OR_FAIL(c, cudaMemcpyAsync(c->aos, records, bytes, cudaMemcpyHostToDevice, c->stream));
         long long offl[CD_F_COUNT];
         for (int k = 0; k < CD_F_COUNT; ++k) offl[k] = off[k];
-        cdk::launch_aos_to_soa(c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
+        const void *dv = (c->direct_host && cdk::records_per_block(itemsize) > 0)
+                             ? device_view_of_host(records, bytes)
+                             : nullptr;
+        if (dv) {
+            cdk::launch_records_in(dv, c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
+        } else {
+            CUDA_OR_FAIL(c, cudaMemcpyAsync(c->aos, records, bytes, cudaMemcpyHostToDevice,
+                                            c->stream));
+            cdk::launch_aos_to_soa(c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
+        }
         cdk::launch_states_in(c->aos, itemsize, state_offsets(off, itemsize), (int)n,
                               state_cols(c), c->stream);
         c->states_dirty = false;
@@ -687,15 +722,29 @@ int cd_download_agents(cd_ctx *c, void *records, int64_t n, int64_t itemsize, co
     if (n == 0) return CD_OK;
     long long offl[CD_F_COUNT];
     for (int k = 0; k < CD_F_COUNT; ++k) offl[k] = off[k];
-    cdk::launch_soa_to_aos(c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
     if (c->states_dirty)
         cdk::launch_states_out(c->aos, itemsize, state_offsets(off, itemsize), (int)n,
                                state_cols(c), c->stream);
-    CUDA_OR_FAIL(c, cudaMemcpyAsync(records, c->aos, n * itemsize, cudaMemcpyDeviceToHost, c->stream));
+    void *dv = (c->direct_host && cdk::records_per_block(itemsize) > 0)
+                   ? const_cast<void *>(device_view_of_host(records, n * itemsize))
+                   : nullptr;
+    if (dv) {
+        cdk::launch_records_out(dv, c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
+    } else {
+        cdk::launch_soa_to_aos(c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(records, c->aos, n * itemsize, cudaMemcpyDeviceToHost,
+                                        c->stream));
+    }
     CUDA_OR_FAIL(c, cudaGetLastError());
     if (int rc = enqueue_status(c)) return rc;
     CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
     return check_device_error(c, true);
+}
+
+int cd_set_direct_host_access(cd_ctx *c, int enable) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    c->direct_host = enable != 0;
+    return CD_OK;
 }
 
 int cd_snapshot_agents(cd_ctx *c, int slot, void *records, int64_t n, int64_t itemsize,

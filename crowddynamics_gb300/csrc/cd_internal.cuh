@@ -204,6 +204,15 @@ void launch_states_out(char *aos, long long itemsize, const StateOffsets &o, int
                        const StateCols &c, cudaStream_t s);
 void launch_soa_to_aos(char *aos, long long itemsize, const long long *off,
                        int n, int body, const double *const *col, cudaStream_t s);
+// Packed records straight from / into device-addressable host memory (the
+// copy and the transpose in one pass; `aos` keeps the device copy of the
+// records for the fields the step does not write).  0 records per block:
+// records too large for shared memory, use the staged path.
+int records_per_block(long long itemsize);
+void launch_records_in(const void *src, char *aos, long long itemsize, const long long *off,
+                       int n, int body, double *const *col, cudaStream_t s);
+void launch_records_out(void *dst, const char *aos, long long itemsize, const long long *off,
+                        int n, int body, const double *const *col, cudaStream_t s);
 double fp64_peak_gflops();
 // Shared-memory bytes of the force kernel (dynamic) and one-time attributes.
 size_t forces_smem_bytes(int body, int variant);

@@ -1884,23 +1884,32 @@ __global__ void k_wall_prep(const double *raw, double *walls, float4 *wf, int nw
 
 struct FieldMap { int field, comp, col; };
 // (CD_F_* field, vector component, column)
-__constant__ FieldMap kMapCirc[20] = {
-    {0, 0, X}, {0, 1, Y}, {1, 0, VX}, {1, 1, VY}, {2, 0, E0X}, {2, 1, E0Y},
-    {3, 0, FX}, {3, 1, FY}, {4, 0, FPX}, {4, 1, FPY}, {5, 0, R}, {9, 0, MASS},
-    {11, 0, V0}, {13, 0, TAU_ADJ}, {14, 0, K_SOC}, {15, 0, TAU0}, {16, 0, MU},
-    {17, 0, KAPPA}, {18, 0, DAMP}, {19, 0, SRF}};
-__constant__ FieldMap kMapTC[36] = {
-    {0, 0, X}, {0, 1, Y}, {1, 0, VX}, {1, 1, VY}, {2, 0, E0X}, {2, 1, E0Y},
-    {3, 0, FX}, {3, 1, FY}, {4, 0, FPX}, {4, 1, FPY}, {5, 0, R}, {9, 0, MASS},
-    {11, 0, V0}, {13, 0, TAU_ADJ}, {14, 0, K_SOC}, {15, 0, TAU0}, {16, 0, MU},
-    {17, 0, KAPPA}, {18, 0, DAMP}, {19, 0, SRF}, {28, 0, SRT},
-    {20, 0, XLS}, {20, 1, YLS}, {21, 0, XRS}, {21, 1, YRS}, {6, 0, RT}, {7, 0, RS},
-    {8, 0, RTS}, {10, 0, INERTIA}, {12, 0, W0}, {22, 0, PHI}, {23, 0, OMEGA},
-    {24, 0, PHI0}, {25, 0, TORQUE}, {26, 0, TORQUE_PREV}, {27, 0, TAU_ROT}};
+#define CD_MAP_CIRC                                                                      \
+    {0, 0, X}, {0, 1, Y}, {1, 0, VX}, {1, 1, VY}, {2, 0, E0X}, {2, 1, E0Y},             \
+    {3, 0, FX}, {3, 1, FY}, {4, 0, FPX}, {4, 1, FPY}, {5, 0, R}, {9, 0, MASS},          \
+    {11, 0, V0}, {13, 0, TAU_ADJ}, {14, 0, K_SOC}, {15, 0, TAU0}, {16, 0, MU},          \
+    {17, 0, KAPPA}, {18, 0, DAMP}, {19, 0, SRF}
+#define CD_MAP_TC                                                                        \
+    {0, 0, X}, {0, 1, Y}, {1, 0, VX}, {1, 1, VY}, {2, 0, E0X}, {2, 1, E0Y},             \
+    {3, 0, FX}, {3, 1, FY}, {4, 0, FPX}, {4, 1, FPY}, {5, 0, R}, {9, 0, MASS},          \
+    {11, 0, V0}, {13, 0, TAU_ADJ}, {14, 0, K_SOC}, {15, 0, TAU0}, {16, 0, MU},          \
+    {17, 0, KAPPA}, {18, 0, DAMP}, {19, 0, SRF}, {28, 0, SRT},                          \
+    {20, 0, XLS}, {20, 1, YLS}, {21, 0, XRS}, {21, 1, YRS}, {6, 0, RT}, {7, 0, RS},     \
+    {8, 0, RTS}, {10, 0, INERTIA}, {12, 0, W0}, {22, 0, PHI}, {23, 0, OMEGA},           \
+    {24, 0, PHI0}, {25, 0, TORQUE}, {26, 0, TORQUE_PREV}, {27, 0, TAU_ROT}
+#define CD_OUT_CIRC X, Y, VX, VY, FX, FY, FPX, FPY, E0X, E0Y
+#define CD_OUT_TC                                                                        \
+    X, Y, VX, VY, FX, FY, FPX, FPY, XLS, YLS, XRS, YRS, PHI, OMEGA, PHI0, TORQUE,        \
+    TORQUE_PREV, E0X, E0Y
+__constant__ FieldMap kMapCirc[20] = {CD_MAP_CIRC};
+__constant__ FieldMap kMapTC[36] = {CD_MAP_TC};
 // Columns the step writes (downloaded back into the records).
-__constant__ int kOutCirc[10] = {X, Y, VX, VY, FX, FY, FPX, FPY, E0X, E0Y};
-__constant__ int kOutTC[19] = {X, Y, VX, VY, FX, FY, FPX, FPY, XLS, YLS, XRS, YRS,
-                               PHI, OMEGA, PHI0, TORQUE, TORQUE_PREV, E0X, E0Y};
+__constant__ int kOutCirc[10] = {CD_OUT_CIRC};
+__constant__ int kOutTC[19] = {CD_OUT_TC};
+constexpr FieldMap hMapCirc[20] = {CD_MAP_CIRC};
+constexpr FieldMap hMapTC[36] = {CD_MAP_TC};
+constexpr int hOutCirc[10] = {CD_OUT_CIRC};
+constexpr int hOutTC[19] = {CD_OUT_TC};
 
 struct OffTable { long long off[32]; };
 struct ColPtrs { double *p[NCOL]; };
@@ -1944,6 +1953,96 @@ __global__ void k_soa_to_aos(char *aos, long long itemsize, OffTable off, int n,
         if (!written || o < 0) continue;
         st_rec(rec, o + 8 * map[k].comp, cols.p[map[k].col][i]);
     }
+}
+
+// Records moved straight between host memory the device can address (pinned,
+// on this Grace-Blackwell part over the chip-to-chip link) and the columns:
+// a block takes REC_BLOCK consecutive records, copies their 32-bit words with
+// coalesced loads or stores into shared memory, and moves the float64 fields
+// between shared memory and the columns there, so the copy and the transpose
+// are one pass and no staging copy is made.
+constexpr int XFER_NT = 256;
+struct XferTable { int n; int word[40]; int col[40]; };   // field word offset, column
+
+__global__ void __launch_bounds__(XFER_NT)
+k_records_in(const unsigned *__restrict__ src, unsigned *__restrict__ copy, int wpr, int per_block,
+             int n, XferTable t, ColPtrs cols) {
+    extern __shared__ __align__(16) unsigned rec_sm[];
+    const int i0 = blockIdx.x * per_block;
+    const int nrec = min(per_block, n - i0);
+    const size_t w0 = (size_t)i0 * wpr;
+    const int words = nrec * wpr;
+    // 16-byte words where the chunk starts on a 16-byte boundary (both
+    // buffers), then the remaining 32-bit words
+    int done = 0;
+    if ((((uintptr_t)(src + w0) | (uintptr_t)(copy + w0)) & 15) == 0) {
+        const uint4 *s4 = reinterpret_cast<const uint4 *>(src + w0);
+        uint4 *c4 = reinterpret_cast<uint4 *>(copy + w0);
+        uint4 *m4 = reinterpret_cast<uint4 *>(rec_sm);
+        const int q = words / 4;
+        int w = threadIdx.x;
+        for (; w + XFER_NT < q; w += 2 * XFER_NT) {
+            const uint4 a = s4[w], b = s4[w + XFER_NT];
+            m4[w] = a;
+            m4[w + XFER_NT] = b;
+            c4[w] = a;
+            c4[w + XFER_NT] = b;
+        }
+        for (; w < q; w += XFER_NT) {
+            const uint4 a = s4[w];
+            m4[w] = a;
+            c4[w] = a;
+        }
+        done = 4 * q;
+    }
+    for (int w = done + threadIdx.x; w < words; w += XFER_NT) {
+        const unsigned v = src[w0 + w];
+        rec_sm[w] = v;
+        copy[w0 + w] = v;
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < t.n * nrec; it += XFER_NT) {
+        const int k = it / nrec, r = it - k * nrec;
+        const unsigned *p = rec_sm + r * wpr + t.word[k];
+        cols.p[t.col[k]][i0 + r] = __hiloint2double((int)p[1], (int)p[0]);
+    }
+}
+
+__global__ void __launch_bounds__(XFER_NT)
+k_records_out(unsigned *__restrict__ dst, const unsigned *__restrict__ base, int wpr,
+              int per_block, int n, XferTable t, ColPtrs cols) {
+    extern __shared__ __align__(16) unsigned rec_sm[];
+    const int i0 = blockIdx.x * per_block;
+    const int nrec = min(per_block, n - i0);
+    const size_t w0 = (size_t)i0 * wpr;
+    const int words = nrec * wpr;
+    int first = 0;
+    if (((uintptr_t)(base + w0) & 15) == 0) {
+        const uint4 *b4 = reinterpret_cast<const uint4 *>(base + w0);
+        uint4 *m4 = reinterpret_cast<uint4 *>(rec_sm);
+        const int q = words / 4;
+        for (int w = threadIdx.x; w < q; w += XFER_NT) m4[w] = b4[w];
+        first = 4 * q;
+    }
+    for (int w = first + threadIdx.x; w < words; w += XFER_NT) rec_sm[w] = base[w0 + w];
+    __syncthreads();
+    for (int it = threadIdx.x; it < t.n * nrec; it += XFER_NT) {
+        const int k = it / nrec, r = it - k * nrec;
+        unsigned *p = rec_sm + r * wpr + t.word[k];
+        const double v = cols.p[t.col[k]][i0 + r];
+        p[0] = (unsigned)__double2loint(v);
+        p[1] = (unsigned)__double2hiint(v);
+    }
+    __syncthreads();
+    int done = 0;
+    if (((uintptr_t)(dst + w0) & 15) == 0) {
+        uint4 *d4 = reinterpret_cast<uint4 *>(dst + w0);
+        const uint4 *m4 = reinterpret_cast<const uint4 *>(rec_sm);
+        const int q = words / 4;
+        for (int w = threadIdx.x; w < q; w += XFER_NT) d4[w] = m4[w];
+        done = 4 * q;
+    }
+    for (int w = done + threadIdx.x; w < words; w += XFER_NT) dst[w0 + w] = rec_sm[w];
 }
 
 // Integer and bool state fields of the packed records (target, active,
@@ -2244,6 +2343,52 @@ void launch_soa_to_aos(char *aos, long long itemsize, const long long *off, int 
     ColPtrs c;
     for (int k = 0; k < NCOL; ++k) c.p[k] = const_cast<double *>(col[k]);
     k_soa_to_aos<<<nblk(n, 128), 128, 0, s>>>(aos, itemsize, t, n, body, c);
+}
+
+int records_per_block(long long itemsize) {
+    const long long r = (48 * 1024) / itemsize;
+    return (int)std::min<long long>(64, r);
+}
+
+static XferTable xfer_table(const long long *off, int body, bool outputs_only) {
+    XferTable t{};
+    const FieldMap *map = body == 0 ? hMapCirc : hMapTC;
+    const int nm = body == 0 ? 20 : 36;
+    const int *outs = body == 0 ? hOutCirc : hOutTC;
+    const int no = body == 0 ? 10 : 19;
+    for (int k = 0; k < nm; ++k) {
+        const long long o = off[map[k].field];
+        if (o < 0) continue;
+        bool written = false;
+        for (int q = 0; q < no; ++q) written |= outs[q] == map[k].col;
+        if (outputs_only && !written) continue;
+        t.word[t.n] = (int)((o + 8 * map[k].comp) / 4);
+        t.col[t.n] = map[k].col;
+        ++t.n;
+    }
+    return t;
+}
+
+void launch_records_in(const void *src, char *aos, long long itemsize, const long long *off,
+                       int n, int body, double *const *col, cudaStream_t s) {
+    const int per = records_per_block(itemsize);
+    if (n <= 0 || per <= 0) return;
+    ColPtrs c;
+    for (int k = 0; k < NCOL; ++k) c.p[k] = col[k];
+    k_records_in<<<nblk(n, per), XFER_NT, (size_t)per * itemsize, s>>>(
+        static_cast<const unsigned *>(src), reinterpret_cast<unsigned *>(aos), (int)(itemsize / 4),
+        per, n, xfer_table(off, body, false), c);
+}
+
+void launch_records_out(void *dst, const char *aos, long long itemsize, const long long *off,
+                        int n, int body, const double *const *col, cudaStream_t s) {
+    const int per = records_per_block(itemsize);
+    if (n <= 0 || per <= 0) return;
+    ColPtrs c;
+    for (int k = 0; k < NCOL; ++k) c.p[k] = const_cast<double *>(col[k]);
+    k_records_out<<<nblk(n, per), XFER_NT, (size_t)per * itemsize, s>>>(
+        static_cast<unsigned *>(dst), reinterpret_cast<const unsigned *>(aos), (int)(itemsize / 4),
+        per, n, xfer_table(off, body, true), c);
 }
 
 double fp64_peak_gflops() {

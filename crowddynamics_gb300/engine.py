@@ -206,6 +206,12 @@ class DeviceBatch:
                                                   N.ptr(my), ny, nx, float(minx), float(miny),
                                                   float(step)))
 
+    def set_direct_host_access(self, enable=True):
+        """Pinned host records are read and written by the device directly
+        (copy and transpose in one pass); False stages every transfer
+        through a copy.  Both give the same bytes."""
+        self._chk(self._lib.cd_set_direct_host_access(self._ctx, 1 if enable else 0))
+
     def set_noise_mode(self, device, seed=0, step=0):
         """Fluctuation noise from the host (``device=False``: set_noise before
         each step) or drawn on the device from the counter generator with

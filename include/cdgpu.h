@@ -127,6 +127,11 @@ int cd_upload_agents(cd_ctx *ctx, const void *records, int64_t n,
  * last cd_upload_agents. */
 int cd_download_agents(cd_ctx *ctx, void *records, int64_t n, int64_t itemsize,
                        const int64_t *field_offsets);
+/* Host records in pinned (page-locked, device-mapped) memory are read and
+ * written by the device directly, copy and transpose in one kernel pass;
+ * other host memory goes through a staged copy.  Both give the same bytes.
+ * `enable` = 0 makes every transfer staged (default 1). */
+int cd_set_direct_host_access(cd_ctx *ctx, int enable);
 
 /* Asynchronous snapshot for SaveSimulationData (simulation/logic.py:264-337):
  * enqueue on the context stream, behind the steps already enqueued, the

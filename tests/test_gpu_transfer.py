@@ -1,0 +1,106 @@
+"""Host record transfers: pinned host records are read and written by the
+device directly (copy and transpose in one kernel pass), other host memory
+through a staged copy.  Both must move exactly the same bytes, for both body
+types, agent counts that do not fill the last block of records, and records
+that carry fields of their own beyond the reference's."""
+import numpy as np
+import pytest
+import torch
+
+from crowddynamics_gb300 import _native as N
+from crowddynamics_gb300 import scenarios as S
+from crowddynamics_gb300.engine import batch_from_scenarios, field_offsets
+
+pytestmark = pytest.mark.gpu
+
+NODES = N.NODE_ALL & ~N.NODE_FLUCTUATION
+
+
+def pinned_like(a):
+    """A copy of structured array ``a`` in page-locked host memory."""
+    buf = torch.empty(max(a.nbytes, 1), dtype=torch.uint8, pin_memory=True)
+    out = buf.numpy()[:a.nbytes].view(a.dtype)
+    out[:] = a
+    return out, buf
+
+
+def with_extra_field(a):
+    """``a`` with an extra float32 field after the reference's fields."""
+    dt = np.dtype(a.dtype.descr + [('user_tag', '<f4')])
+    out = np.zeros(len(a), dt)
+    for name in a.dtype.names:
+        out[name] = a[name]
+    out['user_tag'] = np.arange(len(a), dtype=np.float32) * 0.5 + 3.0
+    return out
+
+
+def c_upload(b, records):
+    """cd_upload_agents on any record layout (the Python layer accepts only
+    the reference's exact dtypes; the C ABI takes any field offsets)."""
+    off = field_offsets(records.dtype)
+    assert b._lib.cd_upload_agents(b._ctx, N.ptr(records), len(records), records.dtype.itemsize,
+                                   N.i64ptr(off)) == 0
+
+
+def c_download(b, records):
+    off = field_offsets(records.dtype)
+    assert b._lib.cd_download_agents(b._ctx, N.ptr(records), len(records),
+                                     records.dtype.itemsize, N.i64ptr(off)) == 0
+
+
+def advance(scen, records, direct, steps=3):
+    b, agents, _ = batch_from_scenarios([scen])
+    b.set_direct_host_access(direct)
+    c_upload(b, records)
+    b.run(steps, NODES)
+    return b
+
+
+@pytest.mark.parametrize('make', [
+    lambda: S.hallway(n=130, seed=5),
+    lambda: S.room(n=197, seed=6),
+    lambda: S.hallway(n=1, seed=7),
+])
+@pytest.mark.parametrize('extra', [False, True])
+def test_direct_and_staged_transfers_identical(native, make, extra):
+    scen = make()
+    recs = with_extra_field(scen.agents) if extra else scen.agents.copy()
+    pinned, keep_in = pinned_like(recs)
+    # direct upload from pinned memory, staged upload from pageable memory
+    bd = advance(scen, pinned, True)
+    bs = advance(scen, recs.copy(), False)
+    outs = {}
+    for name, b in (('direct', bd), ('staged', bs)):
+        o_pin, keep = pinned_like(np.zeros_like(recs))
+        c_download(b, o_pin)                                   # direct when enabled
+        o_page = np.zeros_like(recs)
+        c_download(b, o_page)                                  # staged
+        assert o_pin.tobytes() == o_page.tobytes(), name
+        outs[name] = o_pin.copy()
+        b.close()
+        del keep
+    assert outs['direct'].tobytes() == outs['staged'].tobytes()
+    if extra:
+        assert np.array_equal(outs['direct']['user_tag'], recs['user_tag'])
+    else:
+        ref, _, _ = batch_from_scenarios([scen])
+        ref.run(3, NODES)
+        r = np.zeros_like(recs)
+        ref.download(r)
+        ref.close()
+        assert r.tobytes() == outs['direct'].tobytes()
+    del keep_in
+
+
+def test_direct_upload_round_trip(native):
+    """Upload from pinned memory and download at once: the records come back
+    byte for byte (no step in between)."""
+    scen = S.room(n=300, seed=9)
+    recs, keep = pinned_like(scen.agents)
+    b, _, _ = batch_from_scenarios([scen])
+    b.upload(recs)
+    back, keep2 = pinned_like(np.zeros_like(recs))
+    b.download(back)
+    b.close()
+    assert back.tobytes() == scen.agents.tobytes()
+    del keep, keep2
