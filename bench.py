@@ -44,11 +44,20 @@ UNIT = 'agent-steps/s'
 # pair (bound check), near pair (distance), interacting pair (h < 3: social
 # force, both sides), contact pair (h < 0: contact, both sides), near wall
 # (distance), wall contact, agent (adjusting, timestep, Verlet, shoulders).
+# Float64 operations of the reference's step per unit of work, on the
+# branches it takes (add, sub, mul, div, sqrt, compare = 1; exp = 31, hypot
+# = 4, the operation counts of the shared elementary functions): `inter` the
+# interacting-pair gate, accumulation, torques and relative speed; `soc` the
+# nine sub-pair discriminants of the ThreeCircle social force (Circular: in
+# `inter`); `soc_def` per defined time-to-collision root; `soc_valid` the
+# gradient, two magnitudes, two forces and truncations of a pair with a valid
+# time-to-collision.  A candidate rejected by the distance bound is charged
+# the bound check only.
 WEIGHTS = {
-    'three_circle': dict(cand=6, near=104, inter=311, contact=48, wall_near=81, wall_contact=30,
-                         agent=64),
-    'circular': dict(cand=6, near=11, inter=139, contact=48, wall_near=27, wall_contact=24,
-                     agent=30),
+    'three_circle': dict(cand=6, near=104, inter=19, soc=155, soc_def=3, soc_valid=120,
+                         contact=48, wall_near=81, wall_contact=30, agent=64),
+    'circular': dict(cand=6, near=11, inter=28, soc=0, soc_def=4, soc_valid=112, contact=48,
+                     wall_near=27, wall_contact=24, agent=30),
 }
 
 
@@ -159,10 +168,12 @@ def algorithmic_flops(scen, counts):
 
 def pair_flops(scen, counts):
     """The part of algorithmic_flops done by the pair kernel: every unordered
-    pair that passes the bound check, once (distance, social force, contact)."""
+    pair that passes the bound check, once (distance, social force, contact).
+    Columns 1-3 count each pair twice, the social-branch columns 6-8 once."""
     w = WEIGHTS[scen.body]
     tot = counts.sum(axis=0)
-    return w['near'] * tot[1] / 2 + w['inter'] * tot[2] / 2 + w['contact'] * tot[3] / 2
+    return (w['near'] * tot[1] / 2 + w['inter'] * tot[2] / 2 + w['contact'] * tot[3] / 2 +
+            w['soc'] * tot[6] + w['soc_def'] * tot[7] + w['soc_valid'] * tot[8])
 
 
 def cpu_sample(scen, nodes_orc, steps, nthreads):

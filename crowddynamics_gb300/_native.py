@@ -53,7 +53,8 @@ NA_COLS = ('x', 'y', 'vx', 'vy', 'mass', 'k_soc', 'tau_0', 'mu', 'kappa', 'dampi
            'r_t', 'r_s', 'r_ts', 'x_ls', 'y_ls', 'x_rs', 'y_rs', 'orientation')
 
 #: Columns of cd_pair_counts.
-COUNT_COLS = ('candidates', 'near', 'interacting', 'contact', 'walls_near', 'walls_contact')
+COUNT_COLS = ('candidates', 'near', 'interacting', 'contact', 'walls_near', 'walls_contact',
+              'social', 'social_defined', 'social_valid')
 
 
 class Scenario(ctypes.Structure):

@@ -1171,6 +1171,8 @@ int cd_get_cell_list(cd_ctx *c, int64_t *keys, int64_t *order, int64_t *cells_co
     return CD_OK;
 }
 
+static_assert(CD_COUNT_COLS == cdk::COUNT_COLS, "count columns differ");
+
 int cd_pair_counts(cd_ctx *c, int64_t *counts) {
     if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
     if (!c->have_records) return fail(c, CD_ERR_INVALID_VALUE, "no agents uploaded");

@@ -23,6 +23,9 @@ constexpr int WALL_D = 8;          // p0x p0y p1x p1y tx ty lw -
 // Device error bits (StepArgs::err).
 constexpr int ERR_NOT_FINITE = 1;
 
+// Columns of the per-agent interaction counts (CD_COUNT_COLS of cdgpu.h).
+constexpr int COUNT_COLS = 9;
+
 // Node flags (mirror CD_NODE_* of include/cdgpu.h).
 constexpr int N_FLUCT = 1, N_ORIENT = 2, N_ADJUST = 4, N_AGENT = 8,
               N_WALL = 16, N_INTEG = 32, N_RESET = 64, N_NAV = 128;

@@ -1576,17 +1576,24 @@ __device__ __forceinline__ void candidate_runs(const StepArgs &a, const ScenDev 
     }
 }
 
-// Float32 guess that a forward pair will need the social force: the bound
-// on the skin distance below 3 m and the two approaching.  Only the order of
-// the flat pair list depends on it (pairs guessed so come first, so that
-// warps of the pair kernel mostly take the same branches); every pair writes
-// only its own two entries, so no result does.
+// Float32 guess that a forward pair will need the social force: within
+// sight, and the two enclosing circles (radius = extent) on a collision
+// course (their time-to-collision discriminant positive, and approaching or
+// overlapping).  Sub-circles lie inside the enclosing circles, so a pair with
+// a positive time-to-collision always passes, up to rounding.  Only the order
+// of the flat pair list depends on the guess (pairs guessed so come first, so
+// that warps of the pair kernel mostly take the same branches); every pair
+// writes only its own two entries, so no result does.
 __device__ __forceinline__ bool social_guess(float4 me, float4 o) {
     const float dx = me.x - o.x, dy = me.y - o.y;
     const float2 vm = unpack_velocity(me.w), vo = unpack_velocity(o.w);
-    const float hb = sqrtf(dx * dx + dy * dy) - (me.z + o.z);
-    const float b = -(dx * (vm.x - vo.x) + dy * (vm.y - vo.y));
-    return hb < 3.0f && b > 0.0f;
+    const float vx = vm.x - vo.x, vy = vm.y - vo.y;
+    const float re = me.z + o.z;
+    const float x2 = dx * dx + dy * dy;
+    const float b = -(dx * vx + dy * vy);
+    const float c = x2 - re * re;
+    const float disc = b * b - (vx * vx + vy * vy) * c;
+    return sqrtf(x2) - re < 3.0f && disc > 0.0f && (b > 0.0f || c < 0.0f);
 }
 
 template <int L>
@@ -1818,21 +1825,70 @@ __device__ __forceinline__ double pair_h(const StepArgs &a, int s, int t) {
     return h_min;
 }
 
+// Which branches of the reference's social force the pair (s first, t
+// second) takes (core/motion/power_law.py:213-259 Circular, :262-363
+// ThreeCircle): `soc` the sub-pair loop runs (ThreeCircle: relative speed
+// non-zero; Circular: always), `ndef` sub-pairs with a defined square root
+// (Circular: defined and a != 0), `valid` a force is computed (tau > 0, and
+// tau <= 30 for Circular).  Work accounting only: plain float64 arithmetic.
+__device__ __forceinline__ void social_branches(const StepArgs &a, int s, int t, int &soc,
+                                                int &ndef, int &valid) {
+    soc = 0; ndef = 0; valid = 0;
+    if (a.body == 0) {
+        const Circ A = load_circ(a.stage, s), B = load_circ(a.stage, t);
+        const double xr = A.x - B.x, yr = A.y - B.y, vx = A.vx - B.vx, vy = A.vy - B.vy;
+        const double r = A.r + B.r;
+        const double av = vx * vx + vy * vy, b = -(xr * vx + yr * vy);
+        const double c = (xr * xr + yr * yr) - r * r;
+        const double d = sqrt(b * b - av * c);
+        soc = 1;
+        if (isnan(d) || d == 0 || av == 0) return;
+        ndef = 1;
+        const double tau = (b - d) / av;
+        valid = !(tau <= 0 || tau > 30.0);
+        return;
+    }
+    const TC A = load_tc(a.stage, s), B = load_tc(a.stage, t);
+    const double vx = A.vx - B.vx, vy = A.vy - B.vy;
+    const double av = vx * vx + vy * vy;
+    if (av == 0) return;
+    soc = 1;
+    double tau = __longlong_as_double(0x7ff8000000000000LL);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const double xr = A.x[i] - B.x[j], yr = A.y[i] - B.y[j];
+            const double r = (i == 0 ? A.rt : A.rs) + (j == 0 ? B.rt : B.rs);
+            const double b = -(xr * vx + yr * vy), c = (xr * xr + yr * yr) - r * r;
+            const double d = sqrt(b * b - av * c);
+            if (isnan(d) || d == 0) continue;
+            ++ndef;
+            const double tn = (b - d) / av;
+            if (isnan(tau) || (0 < tn && tn < tau)) tau = tn;
+        }
+    valid = !(isnan(tau) || tau <= 0);
+}
+
 // Per-agent interaction counts (diagnostics / algorithmic work accounting):
 // candidates, pre-check survivors, h < 3, h < 0, walls past the pre-check,
-// walls in contact.
+// walls in contact; then, over the interacting pairs this agent comes first
+// in (each unordered pair once), the social-force branches taken.
 __global__ void k_pair_counts(StepArgs a, int *out) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= a.n) return;
     int i = a.perm[s];
     const ScenDev sc = a.scen[a.scen_of[i]];
     const float4 me = a.cull[s];
-    int nc = 0, nn = 0, ni = 0, nt = 0, wn = 0, wc = 0;
-    for_candidates(a, sc, s, a.key[i], me, [&](int t, bool) {
+    int nc = 0, nn = 0, ni = 0, nt = 0, wn = 0, wc = 0, ns = 0, nd = 0, nv = 0;
+    for_candidates(a, sc, s, a.key[i], me, [&](int t, bool s_first) {
         ++nn;
         double h = pair_h(a, s, t);
         ni += (h < SIGTH_SOC);
         nt += (h < 0);
+        if (h < SIGTH_SOC && s_first) {
+            int so, de, va;
+            social_branches(a, s, t, so, de, va);
+            ns += so; nd += de; nv += va;
+        }
     }, &nc);
     if (sc.wall_count > 0) {
         const bool all_walls = me.z > (float)sc.wall_reach;
@@ -1862,8 +1918,9 @@ __global__ void k_pair_counts(StepArgs a, int *out) {
             (void)fx; (void)fy; (void)tq;
         }
     }
-    int *o = out + (size_t)i * 6;
+    int *o = out + (size_t)i * COUNT_COLS;
     o[0] = nc; o[1] = nn; o[2] = ni; o[3] = nt; o[4] = wn; o[5] = wc;
+    o[6] = ns; o[7] = nd; o[8] = nv;
 }
 
 __global__ void k_wall_prep(const double *raw, double *walls, float4 *wf, int nw) {

@@ -296,8 +296,11 @@ class DeviceBatch:
         return keys, order, cnt, off
 
     def pair_counts(self):
-        """Per-agent counts (n, 6): candidates, near, interacting (h < 3),
-        contact (h < 0), walls near, walls in contact."""
+        """Per-agent counts (n, 9): candidates, near, interacting (h < 3),
+        contact (h < 0), walls near, walls in contact (pair columns count
+        each unordered pair twice); then social-force branches over the
+        pairs the agent comes first in (each pair once): sub-pair loop run,
+        defined time-to-collision roots, valid time-to-collision."""
         c = np.zeros((self.n_agents, len(N.COUNT_COLS)), np.int64)
         self._chk(self._lib.cd_pair_counts(self._ctx, N.i64ptr(c)))
         return c

@@ -231,9 +231,13 @@ int cd_get_cell_list(cd_ctx *ctx, int64_t *keys, int64_t *order,
  * (row-major n x CD_COUNT_COLS): candidate partners (same or adjacent cell),
  * partners that survive the conservative distance pre-check, partners with
  * skin distance h < 3 (interacting), partners with h < 0 (contact), wall
- * segments that survive the pre-check, walls in contact.  Summing a pair
- * column over agents counts every unordered pair twice. */
-#define CD_COUNT_COLS 6
+ * segments that survive the pre-check, walls in contact.  Summing one of
+ * these pair columns over agents counts every unordered pair twice.  Then,
+ * over the interacting pairs whose first agent (in the cell-list order) is
+ * this one, so each unordered pair once: pairs whose social force runs its
+ * sub-pair loop, sub-pairs with a defined time-to-collision root, pairs with
+ * a valid time-to-collision (a force is computed). */
+#define CD_COUNT_COLS 9
 int cd_pair_counts(cd_ctx *ctx, int64_t *counts);
 
 /* Total cells over all scenarios and agents/walls of the context. */

@@ -246,6 +246,87 @@ def test_candidate_pairs_bit_exact(oracle, native):
         assert np.all(near >= need)
 
 
+def social_branches_np(a, first, second):
+    """(sub-pair loop run, defined roots, valid time-to-collision) per pair
+    (first, second), restated from core/motion/power_law.py:213-363."""
+    v = a['velocity'][first] - a['velocity'][second]
+    av = (v * v).sum(1)
+    if 'position_ls' not in a.dtype.names:
+        x = a['position'][first] - a['position'][second]
+        r = a['radius'][first] + a['radius'][second]
+        b = -(x[:, 0] * v[:, 0] + x[:, 1] * v[:, 1])
+        c = (x[:, 0] * x[:, 0] + x[:, 1] * x[:, 1]) - r * r
+        with np.errstate(invalid='ignore', divide='ignore'):
+            d = np.sqrt(b * b - av * c)
+            defined = ~(np.isnan(d) | (d == 0) | (av == 0))
+            tau = (b - d) / av
+        return np.ones(len(first), int), defined.astype(int), (defined & ~((tau <= 0) | (tau > 30))).astype(int)
+    parts = ('position', 'position_ls', 'position_rs')
+    radii = ('r_t', 'r_s', 'r_s')
+    soc = av != 0
+    tau = np.full(len(first), np.nan)
+    ndef = np.zeros(len(first), int)
+    for i in range(3):
+        for j in range(3):
+            x = a[parts[i]][first] - a[parts[j]][second]
+            r = a[radii[i]][first] + a[radii[j]][second]
+            b = -(x[:, 0] * v[:, 0] + x[:, 1] * v[:, 1])
+            c = (x[:, 0] * x[:, 0] + x[:, 1] * x[:, 1]) - r * r
+            with np.errstate(invalid='ignore', divide='ignore'):
+                d = np.sqrt(b * b - av * c)
+                ok = soc & ~(np.isnan(d) | (d == 0))
+                tn = (b - d) / av
+            ndef += ok
+            take = ok & (np.isnan(tau) | ((0 < tn) & (tn < tau)))
+            tau = np.where(take, tn, tau)
+    valid = soc & ~(np.isnan(tau) | (tau <= 0))
+    return soc.astype(int), ndef, valid.astype(int)
+
+
+def skin_distance_np(a, i, j):
+    if 'position_ls' not in a.dtype.names:
+        x = a['position'][i] - a['position'][j]
+        return np.sqrt(x[:, 0] * x[:, 0] + x[:, 1] * x[:, 1]) - (a['radius'][i] + a['radius'][j])
+    parts = ('position', 'position_ls', 'position_rs')
+    radii = ('r_t', 'r_s', 'r_s')
+    h = np.full(len(i), np.inf)
+    for p in range(3):
+        for q in range(3):
+            x = a[parts[p]][i] - a[parts[q]][j]
+            h = np.minimum(h, np.sqrt(x[:, 0] * x[:, 0] + x[:, 1] * x[:, 1]) -
+                           (a[radii[p]][i] + a[radii[q]][j]))
+    return h
+
+
+def test_social_branch_counts(oracle, native):
+    """The social-force branch counts used for work accounting equal a numpy
+    restatement over the interacting pairs, each attributed to the pair's
+    first agent (the lower cell-sorted slot)."""
+    for scen in (S.hallway(), S.room()):
+        b, agents, _ = batch_from_scenarios([scen])
+        b.run(15, N.NODE_ALL & ~N.NODE_FLUCTUATION)      # agents under way
+        a = agents.copy()
+        b.download(a)
+        counts = b.pair_counts()
+        _, order, _, _ = b.cell_list()
+        b.close()
+        slot = np.empty(len(order), np.int64)
+        slot[order] = np.arange(len(order))
+        x = np.ascontiguousarray(a['position'][:, 0])
+        y = np.ascontiguousarray(a['position'][:, 1])
+        pairs = oracle.candidate_pairs(x, y, oracle_grid(oracle, scen))
+        lo = np.where(slot[pairs[:, 0]] < slot[pairs[:, 1]], pairs[:, 0], pairs[:, 1])
+        hi = np.where(slot[pairs[:, 0]] < slot[pairs[:, 1]], pairs[:, 1], pairs[:, 0])
+        inter = skin_distance_np(a, lo, hi) < 3.0
+        lo, hi = lo[inter], hi[inter]
+        soc, ndef, valid = social_branches_np(a, lo, hi)
+        n = len(a)
+        assert np.array_equal(counts[:, 6], np.bincount(lo, soc, n).astype(int)), scen.name
+        assert np.array_equal(counts[:, 7], np.bincount(lo, ndef, n).astype(int)), scen.name
+        assert np.array_equal(counts[:, 8], np.bincount(lo, valid, n).astype(int)), scen.name
+        assert counts[:, 8].sum() > 0
+
+
 def test_large_field_forces(oracle, native):
     """Full-size 100k ThreeCircle step: agent-agent + walls + adjusting vs the
     oracle's agent-parallel restatement."""
