@@ -72,6 +72,8 @@ struct cd_ctx {
     int *diag = nullptr;
     // near lists of the compute-once pair pipeline (entries allocated on use)
     int *nl_cnt = nullptr, *nl_off = nullptr, *nl_fwd = nullptr, *nl_scan = nullptr;
+    unsigned *nl_mask = nullptr;
+    int *nl_nch = nullptr;
     int *nl_idx = nullptr;
     double *nl_res = nullptr;
     int *fw_cnt = nullptr, *fw_off = nullptr, *fw_scan = nullptr;
@@ -161,6 +163,8 @@ StepArgs args_of(cd_ctx *c, int nodes) {
     a.nl_cnt = c->nl_cnt;
     a.nl_off = c->nl_off;
     a.nl_fwd = c->nl_fwd;
+    a.nl_mask = c->nl_mask;
+    a.nl_nch = c->nl_nch;
     a.nl_idx = c->nl_idx;
     a.nl_res = c->nl_res;
     a.nl_cap = (int)c->nl_cap;
@@ -194,7 +198,7 @@ void release(cd_ctx *c) {
                     c->nl_scan, c->nl_idx, c->nl_res, c->fw_cnt, c->fw_off, c->fw_scan,
                     c->fw_pairs, c->ext, c->max_partial, c->tgt, c->navmap, c->rng_step,
                     c->states, c->herd, c->scen_h, c->counters, c->reached, c->polys,
-                    c->poly_off, c->fs_cnt, c->fs_off, c->fs_scan};
+                    c->poly_off, c->fs_cnt, c->fs_off, c->fs_scan, c->nl_mask, c->nl_nch};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -588,6 +592,8 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->nl_cnt, n + 1));
     step(dalloc(c, &c->nl_off, n + 1));
     step(dalloc(c, &c->nl_fwd, n));
+    step(dalloc(c, &c->nl_mask, (int64_t)n * cdk::NL_MASK_CHUNKS));
+    step(dalloc(c, &c->nl_nch, n + 1));
     step(dalloc(c, &c->nl_scan, cdk::scan_scratch_ints((int)npad)));
     step(dalloc(c, &c->fw_cnt, n + 1));
     step(dalloc(c, &c->fw_off, n + 1));

@@ -23,6 +23,10 @@ constexpr int WALL_D = 8;          // p0x p0y p1x p1y tx ty lw -
 // Device error bits (StepArgs::err).
 constexpr int ERR_NOT_FINITE = 1;
 
+// Candidate chunks per agent whose ballots the near-list count keeps for the
+// fill (an agent with more is evaluated again by the fill).
+constexpr int NL_MASK_CHUNKS = 64;
+
 // Columns of the per-agent interaction counts (CD_COUNT_COLS of cdgpu.h).
 constexpr int COUNT_COLS = 9;
 
@@ -82,6 +86,8 @@ struct StepArgs {
     int *nl_cnt;                 // n + 1 counts (scan input)
     int *nl_off;                 // n + 1 offsets; nl_off[n] = entries needed
     int *nl_fwd;                 // per slot: first entry with a later slot
+    unsigned *nl_mask;           // per slot NL_MASK_CHUNKS chunk ballots (k_nl_count -> k_nl_fill)
+    int *nl_nch;                 // per slot: its candidate chunks
     int *nl_idx;                 // nl_cap entries
     double *nl_res;              // per entry: RES_D doubles of pair results
     int nl_cap;

@@ -689,6 +689,12 @@ struct WarpQueue {
 
 constexpr float PRESEL_MARGIN = 1e-4f;   // metres (float32 error of h is ~1e-6 m)
 
+// Kinds of a pair-result record (its flag word): not interacting; a force
+// (fx, fy, torque as computed); interacting with no force on either side, its
+// torque r x (+0, +0) a signed zero whose sign the gather resolves only when
+// it can change the agent's sum.
+constexpr int RES_NONE = 0, RES_FORCE = 1, RES_ZERO_FORCE = 2;
+
 // Per-warp queue of tc_pair_both: the sub-circle pairs that may have a
 // time-to-collision (9 slots per lane) and each lane's pair geometry.
 constexpr int GEO_D = 19;   // P parts x[3] y[3], Q parts x[3] y[3], P rt rs, Q rt rs, vr, a
@@ -905,28 +911,18 @@ __device__ __forceinline__ void tc_pair_step(const TC &A, const float4 meC, cons
     }
 }
 
-// Both sides of a ThreeCircle pair (interactions.py:73-101,
-// power_law.py:264-363) with P = A first and Q = the pair partner: the
-// distance search, the time-to-collision selection and the tau gradient are
-// computed once; each side's force, contact and torque come out exactly as
-// tc_pair_eval computes them from that side.  Warp collective like
-// tc_pair_eval (all 32 lanes call it).
-__device__ __forceinline__ bool tc_pair_both(const TC &A, const float4 meC, const float4 meF0,
-                                             const float4 meF1, const StepArgs &a, bool act,
-                                             int t, PairQueue &q, int lane, double &FPx,
-                                             double &FPy, double &TP, double &FQx, double &FQy,
-                                             double &TQ) {
-    constexpr unsigned wmask = 0xffffffffu;
-    constexpr int nlanes = 32;
-    TC B = A;
-    float4 oC = meC, oF0 = meF0, oF1 = meF1;
-    if (act) {
-        B = load_tc(a.stage, t);
-        oC = __ldg(&a.cull[t]);
-        oF0 = __ldg(&a.stage_f[2 * t]);
-        oF1 = __ldg(&a.stage_f[2 * t + 1]);
-    }
-    // -- distance_three_circles: float32 pre-selection (P's frame) --
+// distance_three_circles (core/distance.py:50-105) in P's frame: the
+// minimum skin distance over the 3 x 3 sub-circle pairs, the first in
+// visiting order winning ties, with the relative position and centre
+// distance of that sub-pair and the parts of P and Q at it.  A float32
+// pre-selection keeps only the sub-pairs within a certified margin of the
+// float32 minimum; those get the exact float64 evaluation in visiting order.
+struct TcDist { double h, sdx, sdy, sd; int pp, qp; };
+
+__device__ __forceinline__ TcDist tc_distance_min(const TC &A, const TC &B, const float4 meC,
+                                                  const float4 meF0, const float4 meF1,
+                                                  const float4 oC, const float4 oF0,
+                                                  const float4 oF1, bool act) {
     const float dxt = (meC.x - oC.x) + (meF0.x - oF0.x);
     const float dyt = (meC.y - oC.y) + (meF0.y - oF0.y);
     const float mox[3] = {0.f, meF1.x, meF1.z}, moy[3] = {0.f, meF1.y, meF1.w};
@@ -955,48 +951,80 @@ __device__ __forceinline__ bool tc_pair_both(const TC &A, const float4 meC, cons
         if (hf[k] <= hfmin + margin) seq |= 1u << k;
     if (anynan) seq = 0x1ffu;
     if (!act) seq = 1u;
-    // exact float64 minimum over the candidates, first in visiting order wins
-    double h_min = __longlong_as_double(0x7ff8000000000000LL);
-    double sdx = 0.0, sdy = 0.0, sd = 0.0;
-    int pp_min = 0, qp_min = 0;                  // P's and Q's part at the minimum
-    {
-        int k = __ffs(seq) - 1;
-        unsigned rest = seq & (seq - 1);
-        int mi = k / 3, ti = k % 3;
-        double dx = sel3(A.x, mi) - sel3(B.x, ti), dy = sel3(A.y, mi) - sel3(B.y, ti);
-        double d = cdm_hypot(dx, dy);
-        h_min = d - (part_r(A, mi) + part_r(B, ti));
-        sdx = dx; sdy = dy; sd = d; pp_min = mi; qp_min = ti;
-        while (rest) {
-            k = __ffs(rest) - 1;
-            rest &= rest - 1;
-            mi = k / 3; ti = k % 3;
-            dx = sel3(A.x, mi) - sel3(B.x, ti);
-            dy = sel3(A.y, mi) - sel3(B.y, ti);
-            d = cdm_hypot(dx, dy);
-            double h = d - (part_r(A, mi) + part_r(B, ti));
-            if (h < h_min || isnan(h_min)) {
-                h_min = h; sdx = dx; sdy = dy; sd = d; pp_min = mi; qp_min = ti;
-            }
+    TcDist D;
+    int k = __ffs(seq) - 1;
+    unsigned rest = seq & (seq - 1);
+    int mi = k / 3, ti = k % 3;
+    double dx = sel3(A.x, mi) - sel3(B.x, ti), dy = sel3(A.y, mi) - sel3(B.y, ti);
+    double d = cdm_hypot(dx, dy);
+    D.h = d - (part_r(A, mi) + part_r(B, ti));
+    D.sdx = dx; D.sdy = dy; D.sd = d; D.pp = mi; D.qp = ti;
+    while (rest) {
+        k = __ffs(rest) - 1;
+        rest &= rest - 1;
+        mi = k / 3; ti = k % 3;
+        dx = sel3(A.x, mi) - sel3(B.x, ti);
+        dy = sel3(A.y, mi) - sel3(B.y, ti);
+        d = cdm_hypot(dx, dy);
+        const double h = d - (part_r(A, mi) + part_r(B, ti));
+        if (h < D.h || isnan(D.h)) {
+            D.h = h; D.sdx = dx; D.sdy = dy; D.sd = d; D.pp = mi; D.qp = ti;
         }
     }
-    const bool inter = act && (h_min < SIGTH_SOC);
-    double npx = 0.0, npy = 0.0, nqx = 0.0, nqy = 0.0;
-    if (inter && sd != 0.0) {
-        npx = sdx / sd; npy = sdy / sd;
+    return D;
+}
+
+// Unit normals of both sides at the minimum and the moment arms
+// (X_P[part] + r_side * n_side) - x_side_torso, X_P the first agent's parts
+// indexed by the side's own part (core/distance.py:100-103).
+__device__ __forceinline__ void tc_moment_arms(const TC &A, const TC &B, const TcDist &D,
+                                               double &npx, double &npy, double &nqx,
+                                               double &nqy, double &rpx, double &rpy,
+                                               double &rqx, double &rqy) {
+    npx = 0.0; npy = 0.0; nqx = 0.0; nqy = 0.0;
+    if (D.sd != 0.0) {
+        npx = D.sdx / D.sd; npy = D.sdy / D.sd;
         nqx = -npx; nqy = -npy;                  // (-x)/d == -(x/d), signed zeros included
     }
-    // moment arms: (X_P[part] + r_side * n_side) - x_side_torso, X_P the first
-    // agent's parts indexed by the side's own part
-    double rpx, rpy, rqx, rqy;
-    {
-        double r = part_r(A, pp_min);
-        rpx = (sel3(A.x, pp_min) + r * npx) - A.x[0];
-        rpy = (sel3(A.y, pp_min) + r * npy) - A.y[0];
-        r = part_r(B, qp_min);
-        rqx = (sel3(A.x, qp_min) + r * nqx) - B.x[0];
-        rqy = (sel3(A.y, qp_min) + r * nqy) - B.y[0];
+    double r = part_r(A, D.pp);
+    rpx = (sel3(A.x, D.pp) + r * npx) - A.x[0];
+    rpy = (sel3(A.y, D.pp) + r * npy) - A.y[0];
+    r = part_r(B, D.qp);
+    rqx = (sel3(A.x, D.qp) + r * nqx) - B.x[0];
+    rqy = (sel3(A.y, D.qp) + r * nqy) - B.y[0];
+}
+
+// Both sides of a ThreeCircle pair (interactions.py:73-101,
+// power_law.py:264-363) with P = A first and Q = the pair partner: the
+// distance search, the time-to-collision selection and the tau gradient are
+// computed once; each side's force, contact and torque come out exactly as
+// tc_pair_eval computes them from that side.  Warp collective like
+// tc_pair_eval (all 32 lanes call it).  Returns the record kind: RES_NONE,
+// RES_FORCE, or RES_ZERO_FORCE (normals, moment arms and torques skipped).
+__device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const float4 meF0,
+                                             const float4 meF1, const StepArgs &a, bool act,
+                                             int t, PairQueue &q, int lane, double &FPx,
+                                             double &FPy, double &TP, double &FQx, double &FQy,
+                                             double &TQ) {
+    constexpr unsigned wmask = 0xffffffffu;
+    constexpr int nlanes = 32;
+    TC B = A;
+    float4 oC = meC, oF0 = meF0, oF1 = meF1;
+    if (act) {
+        B = load_tc(a.stage, t);
+        oC = __ldg(&a.cull[t]);
+        oF0 = __ldg(&a.stage_f[2 * t]);
+        oF1 = __ldg(&a.stage_f[2 * t + 1]);
     }
+    const TcDist D = tc_distance_min(A, B, meC, meF0, meF1, oC, oF0, oF1, act);
+    const double h_min = D.h;
+    const bool inter = act && (h_min < SIGTH_SOC);
+    // float32 geometry of the sub-circles (P's frame) for the discriminant test
+    const float dxt = (meC.x - oC.x) + (meF0.x - oF0.x);
+    const float dyt = (meC.y - oC.y) + (meF0.y - oF0.y);
+    const float mox[3] = {0.f, meF1.x, meF1.z}, moy[3] = {0.f, meF1.y, meF1.w};
+    const float oox[3] = {0.f, oF1.x, oF1.z}, ooy[3] = {0.f, oF1.y, oF1.w};
+    const float mr[3] = {meF0.z, meF0.w, meF0.w}, orr[3] = {oF0.z, oF0.w, oF0.w};
     // -- force_social_three_circle (shared time-to-collision) --
     // float32 test of the 9 sub-circle discriminants: a sub-pair whose
     // float32 discriminant is below -M has a negative float64 one (M bounds
@@ -1098,7 +1126,8 @@ __device__ __forceinline__ bool tc_pair_both(const TC &A, const float4 meC, cons
     }
     __syncwarp(wmask);
     FPx = 0.0; FPy = 0.0; FQx = 0.0; FQy = 0.0;
-    if (soc && !(isnan(tau) || tau <= 0)) {
+    const bool social = soc && !(isnan(tau) || tau <= 0);
+    if (social) {
         const int mi = k_sel / 3, ti = k_sel % 3;
         double o1x, o1y, o2x, o2y;
         r_off_part(A, mi, o1x, o1y);
@@ -1120,7 +1149,17 @@ __device__ __forceinline__ bool tc_pair_both(const TC &A, const float4 meC, cons
         FQy = (cmq * (-gy)) * magq;
         truncate2(FQx, FQy, F_SOC_MAX);
     }
-    if (inter && h_min < 0) {
+    const bool contact = inter && h_min < 0;
+    if (!(social || contact)) {
+        // no force on either side: each side's torque is r x (+0, +0), a
+        // signed zero; the gather resolves its sign only where it matters
+        TP = 0.0;
+        TQ = 0.0;
+        return inter ? RES_ZERO_FORCE : RES_NONE;
+    }
+    double npx, npy, nqx, nqy, rpx, rpy, rqx, rqy;
+    tc_moment_arms(A, B, D, npx, npy, nqx, nqy, rpx, rpy, rqx, rqy);
+    if (contact) {
         double cx, cy;
         force_contact(h_min, npx, npy, vrx, vry, A.mu, A.kappa, A.damp, cx, cy);
         FPx = FPx + cx;
@@ -1131,7 +1170,7 @@ __device__ __forceinline__ bool tc_pair_both(const TC &A, const float4 meC, cons
     }
     TP = rpx * FPy - rpy * FPx;
     TQ = rqx * FQy - rqy * FQx;
-    return inter;
+    return RES_FORCE;
 }
 
 // Resumable candidate enumeration into the thread's list (visiting order:
@@ -1596,47 +1635,16 @@ __device__ __forceinline__ bool social_guess(float4 me, float4 o) {
     return sqrtf(x2) - re < 3.0f && disc > 0.0f && (b > 0.0f || c < 0.0f);
 }
 
+// Near lists in two passes over the same candidate chunks (L consecutive
+// candidates of one run per chunk, one lane each).  k_nl_count evaluates the
+// bound check and the social-force guess, counts, and keeps each chunk's two
+// ballots (near bits low, guessed bits high) in the agent's mask row;
+// k_nl_fill then places the entries from the masks alone.  An agent with more
+// chunks than a row holds is evaluated again by the fill.
 template <int L>
 __global__ void __launch_bounds__(NTG) k_nl_count(StepArgs a) {
-    const int r = threadIdx.x & (L - 1);
-    const int s = (int)(((long long)blockIdx.x * NTG + threadIdx.x) / L);
-    int cnt = 0, fwd = 0, soc = 0;
-    if (s < a.n) {
-        const int i = a.perm[s];
-        const ScenDev sc = a.scen[a.scen_of[i]];
-        const float4 me = a.cull[s];
-        int rb[3], re[3];
-        candidate_runs(a, sc, a.key[i], rb, re);
-#pragma unroll
-        for (int d = 0; d < 3; ++d)
-            for (int t = rb[d] + r; t < re[d]; t += L) {
-                const float4 o = __ldg(&a.cull[t]);
-                if (t != s && !pair_far(me, o)) {
-                    ++cnt;
-                    if (t > s) {
-                        ++fwd;
-                        soc += social_guess(me, o);
-                    }
-                }
-            }
-    }
-#pragma unroll
-    for (int o = L / 2; o > 0; o >>= 1) {
-        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-        fwd += __shfl_xor_sync(0xffffffffu, fwd, o);
-        soc += __shfl_xor_sync(0xffffffffu, soc, o);
-    }
-    if (s < a.n && r == 0) {
-        a.nl_cnt[s] = cnt;
-        a.fw_cnt[s] = fwd;
-        a.fs_cnt[s] = soc;
-    }
-}
-
-template <int L>
-__global__ void __launch_bounds__(NTG) k_nl_fill(StepArgs a) {
-    if (a.nl_off[a.n] > a.nl_cap) return;                 // over capacity: fallback
-    constexpr unsigned GMASK = L == 32 ? 0xffffffffu : ((1u << L) - 1u);
+    static_assert(L <= 16, "two ballots per 32-bit mask word");
+    constexpr unsigned GMASK = (1u << L) - 1u;
     const int lane = threadIdx.x & 31;
     const int r = lane & (L - 1), g0 = lane & ~(L - 1);
     const unsigned gm = GMASK << g0;
@@ -1647,14 +1655,8 @@ __global__ void __launch_bounds__(NTG) k_nl_fill(StepArgs a) {
     const float4 me = a.cull[s];
     int rb[3], re[3];
     candidate_runs(a, sc, a.key[i], rb, re);
-    // entries with a later slot follow all earlier ones (ascending order)
-    const int fwd0 = a.nl_off[s] + (a.nl_cnt[s] - a.fw_cnt[s]);
-    int pos = a.nl_off[s];
-    // the flat list of pairs: first every pair guessed to need the social
-    // force, then the others, each part in slot order
-    int p0 = a.fs_off[s];
-    int p1 = a.fs_off[a.n] + (a.fw_off[s] - a.fs_off[s]);
-    const unsigned lower = (1u << r) - 1u;
+    unsigned *mrow = a.nl_mask + (size_t)s * NL_MASK_CHUNKS;
+    int cnt = 0, fwd = 0, soc = 0, ch = 0;
 #pragma unroll
     for (int d = 0; d < 3; ++d)
         for (int base = rb[d]; base < re[d]; base += L) {
@@ -1665,20 +1667,95 @@ __global__ void __launch_bounds__(NTG) k_nl_fill(StepArgs a) {
                 near = !pair_far(me, o);
                 if (near && t > s) guess = social_guess(me, o);
             }
-            const unsigned gb = (__ballot_sync(gm, near) >> g0) & GMASK;
+            const unsigned nb = (__ballot_sync(gm, near) >> g0) & GMASK;
             const unsigned fb = (__ballot_sync(gm, near && t > s) >> g0) & GMASK;
             const unsigned sb = (__ballot_sync(gm, guess) >> g0) & GMASK;
-            if (near) {
-                const int e = pos + __popc(gb & lower);
-                a.nl_idx[e] = t;
-                if (t > s)
-                    a.fw_pairs[guess ? p0 + __popc(sb & lower)
-                                     : p1 + __popc(fb & ~sb & lower)] = make_int2(s, e);
-            }
-            pos += __popc(gb);
-            p0 += __popc(sb);
-            p1 += __popc(fb & ~sb);
+            if (r == 0 && ch < NL_MASK_CHUNKS) mrow[ch] = nb | (sb << 16);
+            ++ch;
+            cnt += __popc(nb);
+            fwd += __popc(fb);
+            soc += __popc(sb);
         }
+    if (r == 0) {
+        a.nl_cnt[s] = cnt;
+        a.fw_cnt[s] = fwd;
+        a.fs_cnt[s] = soc;
+        a.nl_nch[s] = ch;
+    }
+}
+
+template <int L>
+__global__ void __launch_bounds__(NTG) k_nl_fill(StepArgs a) {
+    if (a.nl_off[a.n] > a.nl_cap) return;                 // over capacity: fallback
+    constexpr unsigned GMASK = (1u << L) - 1u;
+    const int lane = threadIdx.x & 31;
+    const int r = lane & (L - 1), g0 = lane & ~(L - 1);
+    const unsigned gm = GMASK << g0;
+    const int s = (int)(((long long)blockIdx.x * NTG + threadIdx.x) / L);
+    if (s >= a.n) return;                                 // whole groups leave together
+    const int i = a.perm[s];
+    const ScenDev sc = a.scen[a.scen_of[i]];
+    int rb[3], re[3];
+    candidate_runs(a, sc, a.key[i], rb, re);
+    // entries with a later slot follow all earlier ones (ascending order)
+    const int fwd0 = a.nl_off[s] + (a.nl_cnt[s] - a.fw_cnt[s]);
+    int pos = a.nl_off[s];
+    // the flat list of pairs: first every pair guessed to need the social
+    // force, then the others, each part in slot order
+    int p0 = a.fs_off[s];
+    int p1 = a.fs_off[a.n] + (a.fw_off[s] - a.fs_off[s]);
+    const unsigned lower = (1u << r) - 1u;
+    if (a.nl_nch[s] <= NL_MASK_CHUNKS) {
+        const unsigned *mrow = a.nl_mask + (size_t)s * NL_MASK_CHUNKS;
+        int ch = 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+            for (int base = rb[d]; base < re[d]; base += L) {
+                const unsigned m = mrow[ch++];
+                const unsigned nb = m & 0xffffu, sb = m >> 16;
+                const int k0 = s - base + 1;              // lanes r >= k0 have t > s
+                const unsigned fl = k0 <= 0 ? GMASK : (k0 >= L ? 0u : (GMASK & ~((1u << k0) - 1u)));
+                const unsigned fb = nb & fl;
+                const int t = base + r;
+                if ((nb >> r) & 1u) {
+                    const int e = pos + __popc(nb & lower);
+                    a.nl_idx[e] = t;
+                    if (t > s)
+                        a.fw_pairs[((sb >> r) & 1u) ? p0 + __popc(sb & lower)
+                                                    : p1 + __popc(fb & ~sb & lower)] =
+                            make_int2(s, e);
+                }
+                pos += __popc(nb);
+                p0 += __popc(sb);
+                p1 += __popc(fb & ~sb);
+            }
+    } else {
+        const float4 me = a.cull[s];
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+            for (int base = rb[d]; base < re[d]; base += L) {
+                const int t = base + r;
+                bool near = false, guess = false;
+                if (t < re[d] && t != s) {
+                    const float4 o = __ldg(&a.cull[t]);
+                    near = !pair_far(me, o);
+                    if (near && t > s) guess = social_guess(me, o);
+                }
+                const unsigned gb = (__ballot_sync(gm, near) >> g0) & GMASK;
+                const unsigned fb = (__ballot_sync(gm, near && t > s) >> g0) & GMASK;
+                const unsigned sb = (__ballot_sync(gm, guess) >> g0) & GMASK;
+                if (near) {
+                    const int e = pos + __popc(gb & lower);
+                    a.nl_idx[e] = t;
+                    if (t > s)
+                        a.fw_pairs[guess ? p0 + __popc(sb & lower)
+                                         : p1 + __popc(fb & ~sb & lower)] = make_int2(s, e);
+                }
+                pos += __popc(gb);
+                p0 += __popc(sb);
+                p1 += __popc(fb & ~sb);
+            }
+    }
     if (r == 0) a.nl_fwd[s] = fwd0;
 }
 
@@ -1695,9 +1772,9 @@ __device__ __forceinline__ int partner_entry(const StepArgs &a, int t, int s) {
 }
 
 __device__ __forceinline__ void put_res(double *res, int e, double fx, double fy, double tq,
-                                        bool inter) {
+                                        int kind) {
     double4_32a v;
-    v.x = fx; v.y = fy; v.z = tq; v.w = inter ? 1.0 : 0.0;
+    v.x = fx; v.y = fy; v.z = tq; v.w = (double)kind;
     *reinterpret_cast<double4_32a *>(res + (size_t)e * RES_D) = v;
 }
 
@@ -1726,11 +1803,11 @@ __global__ void __launch_bounds__(NTG) k_pairs(StepArgs a) {
             t = __ldg(&a.nl_idx[e]);
         }
         double fpx = 0.0, fpy = 0.0, tp = 0.0, fqx = 0.0, fqy = 0.0, tq = 0.0;
-        bool inter = false;
+        int kind = RES_NONE;
         if (BODY == 0) {
-            if (act)
-                inter = pair_circular_both(load_circ(a.stage, s), load_circ(a.stage, t), fpx, fpy,
-                                           fqx, fqy);
+            if (act && pair_circular_both(load_circ(a.stage, s), load_circ(a.stage, t), fpx, fpy,
+                                          fqx, fqy))
+                kind = RES_FORCE;
         } else {
             TC At;
             float4 me = make_float4(0.f, 0.f, 0.f, 0.f), meF0 = me, meF1 = me;
@@ -1742,16 +1819,30 @@ __global__ void __launch_bounds__(NTG) k_pairs(StepArgs a) {
             } else {
                 At = load_tc(a.stage, 0);
             }
-            inter = tc_pair_both(At, me, meF0, meF1, a, act, t, wq[threadIdx.x >> 5], lane, fpx,
-                                 fpy, tp, fqx, fqy, tq);
+            kind = tc_pair_both(At, me, meF0, meF1, a, act, t, wq[threadIdx.x >> 5], lane, fpx,
+                                fpy, tp, fqx, fqy, tq);
         }
         if (act) {
-            put_res(a.nl_res, e, fpx, fpy, tp, inter);
+            put_res(a.nl_res, e, fpx, fpy, tp, kind);
             const int eq = partner_entry(a, t, s);
-            if (eq >= 0) put_res(a.nl_res, eq, fqx, fqy, tq, inter);
+            if (eq >= 0) put_res(a.nl_res, eq, fqx, fqy, tq, kind);
             else atomicOr(a.err, ERR_NEAR_LIST);
         }
     }
+}
+
+// Torque of slot s's side of the interacting pair (s, t) that exerts no
+// force: r x (+0, +0) with the exact moment arm r, as tc_pair_both would have
+// computed it (the same distance search and arms; `zero` is +0).
+__device__ __noinline__ double tc_zero_force_torque(const StepArgs &a, int s, int t, double zero) {
+    const int p = s < t ? s : t, q = s < t ? t : s;
+    const TC A = load_tc(a.stage, p), B = load_tc(a.stage, q);
+    const TcDist D = tc_distance_min(A, B, __ldg(&a.cull[p]), __ldg(&a.stage_f[2 * p]),
+                                     __ldg(&a.stage_f[2 * p + 1]), __ldg(&a.cull[q]),
+                                     __ldg(&a.stage_f[2 * q]), __ldg(&a.stage_f[2 * q + 1]), true);
+    double npx, npy, nqx, nqy, rpx, rpy, rqx, rqy;
+    tc_moment_arms(A, B, D, npx, npy, nqx, nqy, rpx, rpy, rqx, rqy);
+    return s == p ? rpx * zero - rpy * zero : rqx * zero - rqy * zero;
 }
 
 // Agent in slot s from its near-list results: one lane per agent, entries
@@ -1769,12 +1860,24 @@ __device__ __forceinline__ void gather_agent(const StepArgs &a, const int s) {
     if (a.nodes & N_AGENT) {
         const double4_32a *res = reinterpret_cast<const double4_32a *>(a.nl_res);
         const int o1 = a.nl_off[s + 1];
+        constexpr long long ZERO_FORCE_BITS = 0x4000000000000000LL;   // 2.0
+        constexpr long long NEG_ZERO_BITS = (long long)0x8000000000000000ULL;
         for (int e = a.nl_off[s]; e < o1; ++e) {
             const double4_32a v = res[e];
-            if (v.w != 0.0) {
+            // the kind is 0.0, 1.0 or 2.0 (put_res): tested on its bits, off the FP64 pipe
+            const long long kind = __double_as_longlong(v.w);
+            if (kind != 0) {
                 fx = fx + v.x;
                 fy = fy + v.y;
-                if (BODY == 1) tq = tq + v.z;
+                if (BODY == 1) {
+                    // a zero-force record's torque is +0 or -0; adding either
+                    // leaves any sum but -0 unchanged, so only then is its
+                    // sign needed
+                    if (kind == ZERO_FORCE_BITS && __double_as_longlong(tq) == NEG_ZERO_BITS)
+                        tq = tq + tc_zero_force_torque(a, s, __ldg(&a.nl_idx[e]), v.x);
+                    else
+                        tq = tq + v.z;
+                }
             }
         }
     }

@@ -66,10 +66,12 @@ STATE = ('position', 'velocity', 'force', 'force_prev', 'torque', 'torque_prev',
 
 
 def assert_identical(got, ref, what=''):
+    """Every state field bit for bit (signed zeros included; any NaN matches
+    any NaN)."""
     for f in STATE:
         if f in ref.dtype.fields:
-            g, r = got[f], ref[f]
-            same = (g == r) | (np.isnan(g) & np.isnan(r))
+            g, r = np.ascontiguousarray(got[f]), np.ascontiguousarray(ref[f])
+            same = (g.view(np.uint64) == r.view(np.uint64)) | (np.isnan(g) & np.isnan(r))
             if not same.all():
                 k = np.argwhere(~same)[0]
                 raise AssertionError('%s %s differs at %s: %r vs %r (%d values)' % (
@@ -325,6 +327,30 @@ def test_social_branch_counts(oracle, native):
         assert np.array_equal(counts[:, 7], np.bincount(lo, ndef, n).astype(int)), scen.name
         assert np.array_equal(counts[:, 8], np.bincount(lo, valid, n).astype(int)), scen.name
         assert counts[:, 8].sum() > 0
+
+
+@pytest.mark.parametrize('move', [False, True])
+def test_zero_force_torque_signs(oracle, native, move):
+    """A ThreeCircle pair that exerts no force adds r x (+0, +0), a signed
+    zero, to each agent's torque.  The pair kernel leaves its sign to the
+    gather, which resolves it only when the agent's running torque is -0.
+    Records whose torque starts at -0 (no adjusting, no reset), in a sparse
+    room (a few partners per agent), make these terms decide the result:
+    the torques must match the oracle bit for bit, and some agents with
+    interacting partners must end at -0 (so adding +0 would be wrong)."""
+    scen = S.room(n=60, seed=12)
+    if move:
+        scen = moving(scen, seed=5)
+    scen.agents['torque'] = -0.0
+    nodes = N.NODE_AGENT_AGENT | N.NODE_AGENT_OBSTACLE
+    b, agents, _ = batch_from_scenarios([scen])
+    inter = b.pair_counts()[:, 2]
+    b.close()
+    got, _ = device_step(scen, nodes)
+    ref, _ = oracle_step(oracle, scen, nodes, exact=True)
+    assert_identical(got, ref, 'zero-force torque')
+    neg = np.signbit(ref['torque']) & (ref['torque'] == 0)
+    assert (neg & (inter > 0)).any() and (~neg & (inter > 0)).any()
 
 
 def test_large_field_forces(oracle, native):
