@@ -305,11 +305,14 @@ def run_ours(args, ws, rank, local):
 
     # DRAM bytes per launch of the dominant kernel, from the committed summary
     # of one ncu capture of this workload
-    traffic = None
+    traffic = pipe = None
     tpath = os.path.join(ROOT, 'profiles', '%s_field100k_threecircle.md' % kernel)
     if n == 100_000 and scen.body == 'three_circle' and os.path.exists(tpath):
-        m = re.search(r'^%s DRAM bytes per launch: (\d+)' % kernel, open(tpath).read(), re.M)
+        text = open(tpath).read()
+        m = re.search(r'^%s DRAM bytes per launch: (\d+)' % kernel, text, re.M)
         traffic = int(m.group(1)) if m else None
+        m = re.search(r'^%s FP64 pipe active: ([\d.]+)' % kernel, text, re.M)
+        pipe = float(m.group(1)) / 100 if m else None
 
     if rank != 0:
         if dist is not None:
@@ -328,6 +331,14 @@ def run_ours(args, ws, rank, local):
                          'kernel': kernel, 'kernel_ms': kernel_ms,
                          'flops_per_launch': kflops,
                          'peak_source': 'measured live: FP64 FMA chain kernel (2 flops per FMA)',
+                         # achieved counts the reference algorithm's float64
+                         # operations on the branches it takes (div, sqrt = 1);
+                         # the kernel skips some of them exactly (float32-
+                         # certified roots, zero-force torques), so frac can
+                         # pass 1; the hardware view is the FP64 pipe's
+                         # active fraction in the committed ncu capture
+                         'work': 'reference algorithm, branch-exact counts of the state',
+                         'fp64_pipe_active_ncu': pipe,
                          'force_stage': {'ms': force_ms, 'flops_per_step': flops,
                                          'achieved': stage_achieved,
                                          'frac': stage_achieved / peak,

@@ -689,11 +689,9 @@ struct WarpQueue {
 
 constexpr float PRESEL_MARGIN = 1e-4f;   // metres (float32 error of h is ~1e-6 m)
 
-// Kinds of a pair-result record (its flag word): not interacting; a force
-// (fx, fy, torque as computed); interacting with no force on either side, its
-// torque r x (+0, +0) a signed zero whose sign the gather resolves only when
-// it can change the agent's sum.
-constexpr int RES_NONE = 0, RES_FORCE = 1, RES_ZERO_FORCE = 2;
+// Kinds of a pair-result record (its flag word): not interacting, or
+// interacting (fx, fy, torque added by the gather).
+constexpr int RES_NONE = 0, RES_INTER = 1;
 
 // Per-warp queue of tc_pair_both: the sub-circle pairs that may have a
 // time-to-collision (9 slots per lane) and each lane's pair geometry.
@@ -994,13 +992,51 @@ __device__ __forceinline__ void tc_moment_arms(const TC &A, const TC &B, const T
     rqy = (sel3(A.y, D.qp) + r * nqy) - B.y[0];
 }
 
+// Sign bits of the four moment-arm components (rpx, rpy, rqx, rqy as
+// tc_moment_arms computes them: bits 0-3) from the float32 geometry, or -1
+// when a component is too close to zero to be certain.  A component is
+// (part offset from the side's torso) + r * n with n the unit normal; its
+// float32 value carries an error below E: positions 1e-6 of the magnitudes
+// involved (as in the distance pre-selection), n 2 E0 / d + 1e-6, products
+// and sums 1e-6 relative; the float64 rounding of the exact expression is
+// below 1e-12 m.  A value beyond 4 E + 1e-12 has the sign of the exact one
+// (and is non-zero).
+__device__ __forceinline__ int tc_arm_signs_f32(float dxt, float dyt, const float mox[3],
+                                                const float moy[3], const float oox[3],
+                                                const float ooy[3], const float mr[3],
+                                                const float orr[3], int pp, int qp) {
+    const float sx = (dxt + mox[pp]) - oox[qp], sy = (dyt + moy[pp]) - ooy[qp];
+    const float d = sqrtf(sx * sx + sy * sy);
+    if (!(d > 1e-3f)) return -1;
+    const float nx = sx / d, ny = sy / d;
+    const float e0 = 1e-6f * (1.f + fabsf(dxt) + fabsf(dyt) + fabsf(mox[1]) + fabsf(moy[1]) +
+                              fabsf(mox[2]) + fabsf(moy[2]) + fabsf(oox[1]) + fabsf(ooy[1]) +
+                              fabsf(oox[2]) + fabsf(ooy[2]));
+    const float en = 2.f * e0 / d + 1e-6f;
+    const float rp = mr[pp], rq = orr[qp];
+    // P: X_P[pp] - X_P[0] + r_P n;  Q: X_P[qp] - X_Q[0] - r_Q n (the first
+    // agent's part indexed by Q's part, core/distance.py:103)
+    const float dpx = mox[pp], dpy = moy[pp];
+    const float dqx = dxt + mox[qp], dqy = dyt + moy[qp];
+    const float v[4] = {dpx + rp * nx, dpy + rp * ny, dqx - rq * nx, dqy - rq * ny};
+    const float dd[4] = {dpx, dpy, dqx, dqy};
+    const float rr[4] = {rp, rp, rq, rq};
+    int bits = 0;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const float e = e0 + rr[c] * en + 1e-6f * (fabsf(dd[c]) + rr[c] + fabsf(v[c]));
+        if (!(fabsf(v[c]) > 4.f * e + 1e-12f)) return -1;
+        bits |= (v[c] < 0.f) << c;
+    }
+    return bits;
+}
+
 // Both sides of a ThreeCircle pair (interactions.py:73-101,
 // power_law.py:264-363) with P = A first and Q = the pair partner: the
 // distance search, the time-to-collision selection and the tau gradient are
 // computed once; each side's force, contact and torque come out exactly as
 // tc_pair_eval computes them from that side.  Warp collective like
-// tc_pair_eval (all 32 lanes call it).  Returns the record kind: RES_NONE,
-// RES_FORCE, or RES_ZERO_FORCE (normals, moment arms and torques skipped).
+// tc_pair_eval (all 32 lanes call it).  Returns the record kind.
 __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const float4 meF0,
                                              const float4 meF1, const StepArgs &a, bool act,
                                              int t, PairQueue &q, int lane, double &FPx,
@@ -1151,11 +1187,24 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
     }
     const bool contact = inter && h_min < 0;
     if (!(social || contact)) {
-        // no force on either side: each side's torque is r x (+0, +0), a
-        // signed zero; the gather resolves its sign only where it matters
+        // No force on either side: each side's torque is r x (+0, +0) =
+        // r.x * (+0) - r.y * (+0), which is -0 exactly when r.x has its sign
+        // bit set and r.y has not.  The signs come from float32 where that is
+        // certain, so the normal's divisions and the arms are skipped.
         TP = 0.0;
         TQ = 0.0;
-        return inter ? RES_ZERO_FORCE : RES_NONE;
+        if (!inter) return RES_NONE;
+        const int sg = tc_arm_signs_f32(dxt, dyt, mox, moy, oox, ooy, mr, orr, D.pp, D.qp);
+        if (sg >= 0) {
+            TP = ((sg & 3) == 1) ? -0.0 : 0.0;
+            TQ = ((sg & 12) == 4) ? -0.0 : 0.0;
+        } else {
+            double npx, npy, nqx, nqy, rpx, rpy, rqx, rqy;
+            tc_moment_arms(A, B, D, npx, npy, nqx, nqy, rpx, rpy, rqx, rqy);
+            TP = rpx * FPy - rpy * FPx;
+            TQ = rqx * FQy - rqy * FQx;
+        }
+        return RES_INTER;
     }
     double npx, npy, nqx, nqy, rpx, rpy, rqx, rqy;
     tc_moment_arms(A, B, D, npx, npy, nqx, nqy, rpx, rpy, rqx, rqy);
@@ -1170,7 +1219,7 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
     }
     TP = rpx * FPy - rpy * FPx;
     TQ = rqx * FQy - rqy * FQx;
-    return RES_FORCE;
+    return RES_INTER;
 }
 
 // Resumable candidate enumeration into the thread's list (visiting order:
@@ -1807,7 +1856,7 @@ __global__ void __launch_bounds__(NTG) k_pairs(StepArgs a) {
         if (BODY == 0) {
             if (act && pair_circular_both(load_circ(a.stage, s), load_circ(a.stage, t), fpx, fpy,
                                           fqx, fqy))
-                kind = RES_FORCE;
+                kind = RES_INTER;
         } else {
             TC At;
             float4 me = make_float4(0.f, 0.f, 0.f, 0.f), meF0 = me, meF1 = me;
@@ -1831,20 +1880,6 @@ __global__ void __launch_bounds__(NTG) k_pairs(StepArgs a) {
     }
 }
 
-// Torque of slot s's side of the interacting pair (s, t) that exerts no
-// force: r x (+0, +0) with the exact moment arm r, as tc_pair_both would have
-// computed it (the same distance search and arms; `zero` is +0).
-__device__ __noinline__ double tc_zero_force_torque(const StepArgs &a, int s, int t, double zero) {
-    const int p = s < t ? s : t, q = s < t ? t : s;
-    const TC A = load_tc(a.stage, p), B = load_tc(a.stage, q);
-    const TcDist D = tc_distance_min(A, B, __ldg(&a.cull[p]), __ldg(&a.stage_f[2 * p]),
-                                     __ldg(&a.stage_f[2 * p + 1]), __ldg(&a.cull[q]),
-                                     __ldg(&a.stage_f[2 * q]), __ldg(&a.stage_f[2 * q + 1]), true);
-    double npx, npy, nqx, nqy, rpx, rpy, rqx, rqy;
-    tc_moment_arms(A, B, D, npx, npy, nqx, nqy, rpx, rpy, rqx, rqy);
-    return s == p ? rpx * zero - rpy * zero : rqx * zero - rqy * zero;
-}
-
 // Agent in slot s from its near-list results: one lane per agent, entries
 // added in list order (32-byte records, one sector each), then walls and
 // integration at full lane occupancy.
@@ -1860,24 +1895,13 @@ __device__ __forceinline__ void gather_agent(const StepArgs &a, const int s) {
     if (a.nodes & N_AGENT) {
         const double4_32a *res = reinterpret_cast<const double4_32a *>(a.nl_res);
         const int o1 = a.nl_off[s + 1];
-        constexpr long long ZERO_FORCE_BITS = 0x4000000000000000LL;   // 2.0
-        constexpr long long NEG_ZERO_BITS = (long long)0x8000000000000000ULL;
         for (int e = a.nl_off[s]; e < o1; ++e) {
             const double4_32a v = res[e];
-            // the kind is 0.0, 1.0 or 2.0 (put_res): tested on its bits, off the FP64 pipe
-            const long long kind = __double_as_longlong(v.w);
-            if (kind != 0) {
+            // the kind is 0.0 or 1.0 (put_res): tested on its bits, off the FP64 pipe
+            if (__double_as_longlong(v.w) != 0) {
                 fx = fx + v.x;
                 fy = fy + v.y;
-                if (BODY == 1) {
-                    // a zero-force record's torque is +0 or -0; adding either
-                    // leaves any sum but -0 unchanged, so only then is its
-                    // sign needed
-                    if (kind == ZERO_FORCE_BITS && __double_as_longlong(tq) == NEG_ZERO_BITS)
-                        tq = tq + tc_zero_force_torque(a, s, __ldg(&a.nl_idx[e]), v.x);
-                    else
-                        tq = tq + v.z;
-                }
+                if (BODY == 1) tq = tq + v.z;
             }
         }
     }
