@@ -1704,7 +1704,9 @@ __global__ void __launch_bounds__(NTG) k_nl_count(StepArgs a) {
     const float4 me = a.cull[s];
     int rb[3], re[3];
     candidate_runs(a, sc, a.key[i], rb, re);
-    unsigned *mrow = a.nl_mask + (size_t)s * NL_MASK_CHUNKS;
+    // the group's mask row is staged in shared memory and written out whole
+    __shared__ unsigned srow[(NTG / L) * NL_MASK_CHUNKS];
+    unsigned *row = srow + (threadIdx.x / L) * NL_MASK_CHUNKS;
     int cnt = 0, fwd = 0, soc = 0, ch = 0;
 #pragma unroll
     for (int d = 0; d < 3; ++d)
@@ -1717,14 +1719,19 @@ __global__ void __launch_bounds__(NTG) k_nl_count(StepArgs a) {
                 if (near && t > s) guess = social_guess(me, o);
             }
             const unsigned nb = (__ballot_sync(gm, near) >> g0) & GMASK;
-            const unsigned fb = (__ballot_sync(gm, near && t > s) >> g0) & GMASK;
             const unsigned sb = (__ballot_sync(gm, guess) >> g0) & GMASK;
-            if (r == 0 && ch < NL_MASK_CHUNKS) mrow[ch] = nb | (sb << 16);
+            const int k0 = s - base + 1;                  // lanes r >= k0 have t > s
+            const unsigned fl = k0 <= 0 ? GMASK : (k0 >= L ? 0u : (GMASK & ~((1u << k0) - 1u)));
+            if (r == 0 && ch < NL_MASK_CHUNKS) row[ch] = nb | (sb << 16);
             ++ch;
             cnt += __popc(nb);
-            fwd += __popc(fb);
+            fwd += __popc(nb & fl);
             soc += __popc(sb);
         }
+    __syncwarp(gm);
+    unsigned *mrow = a.nl_mask + (size_t)s * NL_MASK_CHUNKS;
+    const int nst = ch < NL_MASK_CHUNKS ? ch : NL_MASK_CHUNKS;
+    for (int c = r; c < nst; c += L) mrow[c] = row[c];
     if (r == 0) {
         a.nl_cnt[s] = cnt;
         a.fw_cnt[s] = fwd;
