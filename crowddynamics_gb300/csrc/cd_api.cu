@@ -317,7 +317,7 @@ int64_t kernels_per_step(const cd_ctx *c, int nodes) {
     k += (nodes & CD_NODE_INTEGRATE) ? 1 : 0;           // dt
     k += cdk::scan_scratch_ints((int)c->ncells) > 1 ? 3 : 1;
     if (cdk::variant_pairs(c->variant) && (nodes & CD_NODE_AGENT_AGENT) && c->nl_cnt)
-        k += 4 + 3 * (cdk::scan_scratch_ints((int)c->n) > 1 ? 3 : 1);   // count fill pairs fallback + 3 scans
+        k += 4 + (cdk::scan_scratch_ints((int)c->n) > 1 ? 3 : 1);   // count fill pairs fallback + scans
     return k;
 }
 

@@ -361,7 +361,13 @@ __global__ void k_scen_max_final(const double *partial, int nb, int n_scen, doub
 
 constexpr int SCAN_NT = 1024, SCAN_IPT = 4, SCAN_TILE = SCAN_NT * SCAN_IPT;
 
-__global__ void __launch_bounds__(SCAN_NT) k_scan_local(const int *in, int *out, int *blocksums, int n) {
+// Up to three arrays of the same length scanned by one launch (blockIdx.y).
+struct ScanSet { const int *in[3]; int *out[3]; int *sums[3]; };
+
+__global__ void __launch_bounds__(SCAN_NT) k_scan_local(ScanSet S, int n) {
+    const int *in = S.in[blockIdx.y];
+    int *out = S.out[blockIdx.y];
+    int *blocksums = S.sums[blockIdx.y];
     __shared__ int wtot[SCAN_NT / 32];
     int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_IPT;
     int v[SCAN_IPT];
@@ -402,7 +408,9 @@ __global__ void __launch_bounds__(SCAN_NT) k_scan_local(const int *in, int *out,
     }
 }
 
-__global__ void k_scan_add(int *out, const int *offs, int n, int nb) {
+__global__ void k_scan_add(ScanSet S, int n, int nb) {
+    int *out = S.out[blockIdx.y];
+    const int *offs = S.in[blockIdx.y];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] += offs[i / SCAN_TILE];
     else if (i == n) out[n] = offs[nb];          // total
@@ -2303,16 +2311,43 @@ int scan_scratch_ints(int n) {
     int nb = nblk(n, SCAN_TILE);
     return nb > 1 ? 2 * (nb + 1) : 1;
 }
-void launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s) {
-    int nb = nblk(n, SCAN_TILE);
+void launch_scans(int k, const int *const *in, int *const *out, int n, int *const *scratch,
+                  cudaStream_t s) {
+    const int nb = nblk(n, SCAN_TILE);
+    ScanSet S{};
+    for (int j = 0; j < k; ++j) {
+        S.in[j] = in[j];
+        S.out[j] = out[j];
+        S.sums[j] = nb > 1 ? scratch[j] : nullptr;
+    }
     if (nb <= 1) {
-        k_scan_local<<<1, SCAN_NT, 0, s>>>(in, out, nullptr, n);
+        k_scan_local<<<dim3(1, k), SCAN_NT, 0, s>>>(S, n);
         return;
     }
-    int *sums = scratch, *offs = scratch + nb + 1;
-    k_scan_local<<<nb, SCAN_NT, 0, s>>>(in, out, sums, n);
-    k_scan_local<<<1, SCAN_NT, 0, s>>>(sums, offs, nullptr, nb);   // offs[nb] = total
-    k_scan_add<<<nblk(n + 1, 256), 256, 0, s>>>(out, offs, n, nb);
+    k_scan_local<<<dim3(nb, k), SCAN_NT, 0, s>>>(S, n);
+    ScanSet T{};                          // block totals, offsets after them (offs[nb] = total)
+    for (int j = 0; j < k; ++j) {
+        T.in[j] = scratch[j];
+        T.out[j] = scratch[j] + nb + 1;
+        T.sums[j] = nullptr;
+    }
+    k_scan_local<<<dim3(1, k), SCAN_NT, 0, s>>>(T, nb);
+    ScanSet U{};
+    for (int j = 0; j < k; ++j) {
+        U.in[j] = scratch[j] + nb + 1;
+        U.out[j] = out[j];
+    }
+    k_scan_add<<<dim3(nblk(n + 1, 256), k), 256, 0, s>>>(U, n, nb);
+}
+void launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s) {
+    launch_scans(1, &in, &out, n, &scratch, s);
+}
+// Near, forward and guessed-social counts scanned together.
+void launch_near_scans(const StepArgs &a, cudaStream_t s) {
+    const int *in[3] = {a.nl_cnt, a.fw_cnt, a.fs_cnt};
+    int *out[3] = {a.nl_off, a.fw_off, a.fs_off};
+    int *scr[3] = {a.nl_scan, a.fw_scan, a.fs_scan};
+    launch_scans(3, in, out, a.n, scr, s);
 }
 void launch_scatter(const StepArgs &a, cudaStream_t s) {
     if (a.n <= 0) return;
@@ -2447,9 +2482,7 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
         const int l = pair_l_index(v.lanes);
         const int nb = nblk((long long)a.n * v.lanes, NTG);
         kNlCount[l]<<<nb, NTG, 0, s>>>(a);
-        launch_scan(a.nl_cnt, a.nl_off, a.n, a.nl_scan, s);
-        launch_scan(a.fw_cnt, a.fw_off, a.n, a.fw_scan, s);
-        launch_scan(a.fs_cnt, a.fs_off, a.n, a.fs_scan, s);
+        launch_near_scans(a, s);
         kNlFill[l]<<<nb, NTG, 0, s>>>(a);
         int rp = (dev >= 0 && dev < 64) ? g_pairs_blocks[dev][body][l] : 0;
         if (rp <= 0) rp = 152;
@@ -2482,17 +2515,14 @@ void launch_near_count(const StepArgs &a, cudaStream_t s, int variant) {
     if (a.n <= 0 || !variant_pairs(variant)) return;
     const int lanes = kVariants[variant].lanes;
     kNlCount[pair_l_index(lanes)]<<<nblk((long long)a.n * lanes, NTG), NTG, 0, s>>>(a);
-    launch_scan(a.nl_cnt, a.nl_off, a.n, a.nl_scan, s);
-    launch_scan(a.fw_cnt, a.fw_off, a.n, a.fw_scan, s);
+    launch_near_scans(a, s);
 }
 
 void launch_near_lists(const StepArgs &a, cudaStream_t s) {
     if (a.n <= 0 || !a.nl_cnt) return;
     const int nb = nblk((long long)a.n * 8, NTG);
     kNlCount[1]<<<nb, NTG, 0, s>>>(a);
-    launch_scan(a.nl_cnt, a.nl_off, a.n, a.nl_scan, s);
-    launch_scan(a.fw_cnt, a.fw_off, a.n, a.fw_scan, s);
-    launch_scan(a.fs_cnt, a.fs_off, a.n, a.fs_scan, s);
+    launch_near_scans(a, s);
     kNlFill[1]<<<nb, NTG, 0, s>>>(a);
 }
 
