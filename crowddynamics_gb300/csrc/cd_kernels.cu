@@ -920,20 +920,17 @@ __device__ __forceinline__ void tc_pair_step(const TC &A, const float4 meC, cons
 // distance_three_circles (core/distance.py:50-105) in P's frame: the
 // minimum skin distance over the 3 x 3 sub-circle pairs, the first in
 // visiting order winning ties, with the relative position and centre
-// distance of that sub-pair and the parts of P and Q at it.  A float32
-// pre-selection keeps only the sub-pairs within a certified margin of the
-// float32 minimum; those get the exact float64 evaluation in visiting order.
+// distance of that sub-pair and the parts of P and Q at it.  tc_presel keeps,
+// in float32, the sub-pairs within a certified margin of the float32 minimum
+// (the margin bounds the float32 error of every h many times over);
+// tc_distance_exact evaluates those in float64 in visiting order.
 struct TcDist { double h, sdx, sdy, sd; int pp, qp; };
+struct TcPre { unsigned seq; float hmin, margin; };
 
-__device__ __forceinline__ TcDist tc_distance_min(const TC &A, const TC &B, const float4 meC,
-                                                  const float4 meF0, const float4 meF1,
-                                                  const float4 oC, const float4 oF0,
-                                                  const float4 oF1, bool act) {
-    const float dxt = (meC.x - oC.x) + (meF0.x - oF0.x);
-    const float dyt = (meC.y - oC.y) + (meF0.y - oF0.y);
-    const float mox[3] = {0.f, meF1.x, meF1.z}, moy[3] = {0.f, meF1.y, meF1.w};
-    const float oox[3] = {0.f, oF1.x, oF1.z}, ooy[3] = {0.f, oF1.y, oF1.w};
-    const float mr[3] = {meF0.z, meF0.w, meF0.w}, orr[3] = {oF0.z, oF0.w, oF0.w};
+__device__ __forceinline__ TcPre tc_presel(float dxt, float dyt, const float mox[3],
+                                          const float moy[3], const float oox[3],
+                                          const float ooy[3], const float mr[3],
+                                          const float orr[3], bool act) {
     float hf[9];
     float hfmin = INFINITY;
     bool anynan = false;
@@ -947,16 +944,24 @@ __device__ __forceinline__ TcDist tc_distance_min(const TC &A, const TC &B, cons
             anynan |= (h != h);
             hfmin = fminf(hfmin, h);
         }
-    const float scale = fabsf(dxt) + fabsf(dyt) + fabsf(meF1.x) + fabsf(meF1.y) + fabsf(meF1.z) +
-                        fabsf(meF1.w) + fabsf(oF1.x) + fabsf(oF1.y) + fabsf(oF1.z) + fabsf(oF1.w) +
-                        mr[0] + mr[1] + orr[0] + orr[1];
-    const float margin = PRESEL_MARGIN + 1e-6f * scale;
-    unsigned seq = 0;
+    const float scale = fabsf(dxt) + fabsf(dyt) + fabsf(mox[1]) + fabsf(moy[1]) + fabsf(mox[2]) +
+                        fabsf(moy[2]) + fabsf(oox[1]) + fabsf(ooy[1]) + fabsf(oox[2]) +
+                        fabsf(ooy[2]) + mr[0] + mr[1] + orr[0] + orr[1];
+    TcPre P;
+    P.margin = PRESEL_MARGIN + 1e-6f * scale;
+    P.hmin = hfmin;
+    P.seq = 0;
 #pragma unroll
     for (int k = 0; k < 9; ++k)
-        if (hf[k] <= hfmin + margin) seq |= 1u << k;
-    if (anynan) seq = 0x1ffu;
-    if (!act) seq = 1u;
+        if (hf[k] <= hfmin + P.margin) P.seq |= 1u << k;
+    if (anynan) P.seq = 0x1ffu;
+    if (!act) P.seq = 1u;
+    return P;
+}
+
+// The exact float64 minimum over the pre-selected sub-pairs `seq`, the first
+// in visiting order winning ties.
+__device__ __forceinline__ TcDist tc_distance_exact(const TC &A, const TC &B, unsigned seq) {
     TcDist D;
     int k = __ffs(seq) - 1;
     unsigned rest = seq & (seq - 1);
@@ -1060,30 +1065,65 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
         oF0 = __ldg(&a.stage_f[2 * t]);
         oF1 = __ldg(&a.stage_f[2 * t + 1]);
     }
-    const TcDist D = tc_distance_min(A, B, meC, meF0, meF1, oC, oF0, oF1, act);
-    const double h_min = D.h;
-    const bool inter = act && (h_min < SIGTH_SOC);
-    // float32 geometry of the sub-circles (P's frame) for the discriminant test
+    // float32 geometry of the sub-circles (P's frame)
     const float dxt = (meC.x - oC.x) + (meF0.x - oF0.x);
     const float dyt = (meC.y - oC.y) + (meF0.y - oF0.y);
     const float mox[3] = {0.f, meF1.x, meF1.z}, moy[3] = {0.f, meF1.y, meF1.w};
     const float oox[3] = {0.f, oF1.x, oF1.z}, ooy[3] = {0.f, oF1.y, oF1.w};
     const float mr[3] = {meF0.z, meF0.w, meF0.w}, orr[3] = {oF0.z, oF0.w, oF0.w};
+
+    // -- distance_three_circles --
+    // The exact minimum is needed for a force (normal, contact, moment arms)
+    // and wherever float32 cannot decide the pair: several sub-pairs near the
+    // minimum, or h near 3 (interaction) or 0 (contact).  Elsewhere the
+    // single pre-selected sub-pair is the minimum and its float32 h decides.
+    const TcPre pre = tc_presel(dxt, dyt, mox, moy, oox, ooy, mr, orr, act);
+    const bool unique = (pre.seq & (pre.seq - 1u)) == 0u;
+    const bool far_cert = pre.hmin - pre.margin >= (float)SIGTH_SOC;
+    const bool near_cert = pre.hmin + pre.margin < (float)SIGTH_SOC && pre.hmin - pre.margin > 0.f;
+    const bool dist_cert = act && unique && (far_cert || near_cert);
+    TcDist D;
+    D.pp = (__ffs(pre.seq) - 1) / 3;
+    D.qp = (__ffs(pre.seq) - 1) % 3;
+    bool have_d = false;
+    if (act && !dist_cert) {
+        D = tc_distance_exact(A, B, pre.seq);
+        have_d = true;
+    }
+    const double h_min = have_d ? D.h : 0.0;
+    const bool inter = act && (have_d ? h_min < SIGTH_SOC : near_cert);
+    const bool contact = inter && have_d && h_min < 0;
+
     // -- force_social_three_circle (shared time-to-collision) --
-    // float32 test of the 9 sub-circle discriminants: a sub-pair whose
-    // float32 discriminant is below -M has a negative float64 one (M bounds
-    // the float32 error of every input and operation several times over);
-    // the others go to the warp queue, where any lane evaluates the
-    // reference's float64 b, c, discriminant, root and time-to-collision
-    // from the owner's geometry in shared memory
+    // The selected tau is positive exactly when the first sub-pair (visiting
+    // order) with a defined root has a positive root: a non-positive first
+    // root is never replaced.  float32 classifies each sub-pair's
+    // discriminant (below -M: no root; above M: a root) and, for the first
+    // sub-pair with a root, the sign of tau = (b - d) / a from the signs of b
+    // and c (b < 0, or c < 0 with a|c| not negligible against b^2: the
+    // float64 d exceeds b, tau < 0; b > 0 and c > 0 likewise: tau > 0).  A
+    // pair certified to have no positive tau takes no float64 work here; the
+    // others put their candidate sub-pairs in the warp queue, where any lane
+    // evaluates the reference's float64 b, c, discriminant, root and tau from
+    // the owner's geometry in shared memory, and select tau as the reference.
     const double vrx = A.vx - B.vx, vry = A.vy - B.vy;
-    const double av = vrx * vrx + vry * vry;
-    const bool soc = inter && av != 0;
+    const float vxf = (float)vrx, vyf = (float)vry;
+    double av = 0.0;
+    bool have_av = false;
+    bool soc = inter;
+    if (inter && !(fabsf(vxf) > 1e-20f || fabsf(vyf) > 1e-20f)) {
+        av = vrx * vrx + vry * vry;                      // a == 0 only for (near) zero speed
+        have_av = true;
+        soc = av != 0;
+    }
     unsigned candmask = 0;
     int cnt = 0;
     if (soc) {
-        const float vxf = (float)vrx, vyf = (float)vry;
         const float af = vxf * vxf + vyf * vyf;
+        const float e0 = 1e-6f * (1.f + fabsf(dxt) + fabsf(dyt) + fabsf(mox[1]) + fabsf(moy[1]) +
+                                  fabsf(mox[2]) + fabsf(moy[2]) + fabsf(oox[1]) + fabsf(ooy[1]) +
+                                  fabsf(oox[2]) + fabsf(ooy[2]));
+        int first = -1;                                  // class of the first sub-pair with a root
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
             const int i = k / 3, j = k % 3;
@@ -1096,10 +1136,37 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
             const float discf = bf * bf - acf;
             const float m = 1e-5f * af * (1.f + x2 + rt * rt) + 1e-6f * (bf * bf + fabsf(acf));
             if (!(discf < -m)) {
-                q.kidx[lane * 9 + cnt] = (unsigned char)k;
-                ++cnt;
                 candmask |= 1u << k;
+                if (first < 0) {
+                    // 0: decide in float64; 1: tau < 0 certain; 2: tau > 0 certain
+                    first = 0;
+                    if (discf > m) {
+                        const float mb = 4.f * e0 * (fabsf(vxf) + fabsf(vyf)) +
+                                         1e-6f * (fabsf(dx * vxf) + fabsf(dy * vyf));
+                        const float mc = 8.f * e0 * (fabsf(dx) + fabsf(dy) + rt) +
+                                         1e-6f * (x2 + rt * rt);
+                        const float bb = (fabsf(bf) + mb) * (fabsf(bf) + mb);
+                        if (bf < -mb) first = 1;
+                        else if (cf < -mc && 0.99f * af * (-cf - mc) > 1e-9f * bb) first = 1;
+                        else if (bf > mb && cf > mc && 0.99f * af * (cf - mc) > 1e-9f * bb)
+                            first = 2;
+                    }
+                }
             }
+        }
+        if (first == 1) candmask = 0;                     // no positive tau: no force
+    }
+    if (candmask) {
+        if (!have_av) {
+            av = vrx * vrx + vry * vry;
+            have_av = true;
+        }
+        unsigned mrest = candmask;
+        while (mrest) {
+            const int k = __ffs(mrest) - 1;
+            mrest &= mrest - 1;
+            q.kidx[lane * 9 + cnt] = (unsigned char)k;
+            ++cnt;
         }
         double *g = q.geo + lane * GEO_D;
 #pragma unroll
@@ -1170,7 +1237,7 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
     }
     __syncwarp(wmask);
     FPx = 0.0; FPy = 0.0; FQx = 0.0; FQy = 0.0;
-    const bool social = soc && !(isnan(tau) || tau <= 0);
+    const bool social = soc && candmask && !(isnan(tau) || tau <= 0);
     if (social) {
         const int mi = k_sel / 3, ti = k_sel % 3;
         double o1x, o1y, o2x, o2y;
@@ -1193,7 +1260,6 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
         FQy = (cmq * (-gy)) * magq;
         truncate2(FQx, FQy, F_SOC_MAX);
     }
-    const bool contact = inter && h_min < 0;
     if (!(social || contact)) {
         // No force on either side: each side's torque is r x (+0, +0) =
         // r.x * (+0) - r.y * (+0), which is -0 exactly when r.x has its sign
@@ -1207,6 +1273,7 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
             TP = ((sg & 3) == 1) ? -0.0 : 0.0;
             TQ = ((sg & 12) == 4) ? -0.0 : 0.0;
         } else {
+            if (!have_d) D = tc_distance_exact(A, B, pre.seq);
             double npx, npy, nqx, nqy, rpx, rpy, rqx, rqy;
             tc_moment_arms(A, B, D, npx, npy, nqx, nqy, rpx, rpy, rqx, rqy);
             TP = rpx * FPy - rpy * FPx;
@@ -1214,6 +1281,7 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
         }
         return RES_INTER;
     }
+    if (!have_d) D = tc_distance_exact(A, B, pre.seq);
     double npx, npy, nqx, nqy, rpx, rpy, rqx, rqy;
     tc_moment_arms(A, B, D, npx, npy, nqx, nqy, rpx, rpy, rqx, rqy);
     if (contact) {
