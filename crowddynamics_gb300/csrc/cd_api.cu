@@ -76,6 +76,7 @@ struct cd_ctx {
     int *nl_nch = nullptr;
     int *nl_idx = nullptr;
     double *nl_res = nullptr;
+    unsigned char *nl_kind = nullptr;
     int *fw_cnt = nullptr, *fw_off = nullptr, *fw_scan = nullptr;
     int *fs_cnt = nullptr, *fs_off = nullptr, *fs_scan = nullptr;
     int2 *fw_pairs = nullptr;
@@ -167,6 +168,7 @@ StepArgs args_of(cd_ctx *c, int nodes) {
     a.nl_nch = c->nl_nch;
     a.nl_idx = c->nl_idx;
     a.nl_res = c->nl_res;
+    a.nl_kind = c->nl_kind;
     a.nl_cap = (int)c->nl_cap;
     a.nl_scan = c->nl_scan;
     a.fw_cnt = c->fw_cnt;
@@ -195,7 +197,7 @@ void release(cd_ctx *c) {
                     c->walls_raw, c->walls, c->walls_f, c->wall_start, c->wall_idx,
                     c->noise_f, c->noise_m, c->vmax, c->v0max, c->dt, c->time_tot,
                     c->err, c->work, c->diag, c->aos, c->nl_cnt, c->nl_off, c->nl_fwd,
-                    c->nl_scan, c->nl_idx, c->nl_res, c->fw_cnt, c->fw_off, c->fw_scan,
+                    c->nl_scan, c->nl_idx, c->nl_res, c->nl_kind, c->fw_cnt, c->fw_off, c->fw_scan,
                     c->fw_pairs, c->ext, c->max_partial, c->tgt, c->navmap, c->rng_step,
                     c->states, c->herd, c->scen_h, c->counters, c->reached, c->polys,
                     c->poly_off, c->fs_cnt, c->fs_off, c->fs_scan, c->nl_mask, c->nl_nch};
@@ -327,15 +329,18 @@ int alloc_near_lists(cd_ctx *c, int64_t cap) {
     CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
     if (c->nl_idx) cudaFree(c->nl_idx);
     if (c->nl_res) cudaFree(c->nl_res);
+    if (c->nl_kind) cudaFree(c->nl_kind);
     if (c->fw_pairs) cudaFree(c->fw_pairs);
     c->nl_idx = nullptr;
     c->nl_res = nullptr;
+    c->nl_kind = nullptr;
     c->fw_pairs = nullptr;
     c->nl_cap = 0;
     const int64_t res_d = c->body == CD_BODY_CIRCULAR ? cdk::ADJ_RES_D : cdk::RES_D;
     if (cap > 0) {
         if (int rc = dalloc(c, &c->nl_idx, cap)) return rc;
         if (int rc = dalloc(c, &c->nl_res, cap * res_d)) return rc;
+        if (int rc = dalloc(c, &c->nl_kind, cap)) return rc;
         if (int rc = dalloc(c, &c->fw_pairs, cap)) return rc;
     }
     c->nl_cap = cap;

@@ -89,7 +89,8 @@ struct StepArgs {
     unsigned *nl_mask;           // per slot NL_MASK_CHUNKS chunk ballots (k_nl_count -> k_nl_fill)
     int *nl_nch;                 // per slot: its candidate chunks
     int *nl_idx;                 // nl_cap entries
-    double *nl_res;              // per entry: RES_D doubles of pair results
+    double *nl_res;              // per entry: RES_D doubles of pair results (forces only)
+    unsigned char *nl_kind;      // per entry: none / zero force (+0 or -0 torque) / force
     int nl_cap;
     int *nl_scan;                // scan scratch for n counts
     int *fw_cnt, *fw_off;        // per slot: entries with a later slot (n + 1 each)

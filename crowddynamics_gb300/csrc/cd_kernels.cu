@@ -633,19 +633,24 @@ __device__ __forceinline__ void pair_circular_me(const Circ &A, const Circ &B, d
     }
 }
 
+// Outcome of a pair evaluation: not interacting, interacting without a force
+// on either side (each side's torque a signed zero), or with a force.
+constexpr int RES_NONE = 0, RES_ZERO = 1, RES_FORCE = 2;
+
 // Both forces of a Circular pair (interactions.py:51-70) with P = A the
 // first agent of the pair (the lower cell-sorted slot) and Q = B: each side
 // comes out exactly as pair_circular_eval computes it from that side (Q's
 // relative position, velocity, tau gradient and normal are exact negations
 // of P's), sharing the distance, the time-to-collision and its gradient.
-__device__ __forceinline__ bool pair_circular_both(const Circ &A, const Circ &B, double &FPx,
-                                                   double &FPy, double &FQx, double &FQy) {
+__device__ __forceinline__ int pair_circular_both(const Circ &A, const Circ &B, double &FPx,
+                                                  double &FPy, double &FQx, double &FQy) {
     FPx = 0.0; FPy = 0.0; FQx = 0.0; FQy = 0.0;
+    bool forced = false;
     double xx = A.x - B.x, xy = A.y - B.y;
     double d = cdm_hypot(xx, xy);
     double r_tot = A.r + B.r;
     double h = d - r_tot;
-    if (!(h < SIGTH_SOC)) return false;
+    if (!(h < SIGTH_SOC)) return RES_NONE;
     double vrx = A.vx - B.vx, vry = A.vy - B.vy;
     double a = vrx * vrx + vry * vry;
     double b = -(xx * vrx + xy * vry);
@@ -655,6 +660,7 @@ __device__ __forceinline__ bool pair_circular_both(const Circ &A, const Circ &B,
         double dd = sqrt(disc);
         double tau = (b - dd) / a;
         if (!(tau <= 0 || tau > TAU_MAX)) {
+            forced = true;
             double gx = (vrx - (vrx * b + xx * a) / dd) / a;
             double gy = (vry - (vry * b + xy * a) / dd) / a;
             double cmp = (-A.m) * A.k, cmq = (-B.m) * B.k;
@@ -672,6 +678,7 @@ __device__ __forceinline__ bool pair_circular_both(const Circ &A, const Circ &B,
         }
     }
     if (h < 0) {
+        forced = true;
         double nx = 0.0, ny = 0.0, mx = 0.0, my = 0.0;
         if (d != 0.0) { nx = xx / d; ny = xy / d; mx = -nx; my = -ny; }   // (-x)/d == -(x/d)
         double cx, cy;
@@ -682,7 +689,7 @@ __device__ __forceinline__ bool pair_circular_both(const Circ &A, const Circ &B,
         FQx = FQx + cx;
         FQy = FQy + cy;
     }
-    return true;
+    return forced ? RES_FORCE : RES_ZERO;
 }
 
 // Per-warp queue for the square root and division of the defined sub-circle
@@ -697,9 +704,6 @@ struct WarpQueue {
 
 constexpr float PRESEL_MARGIN = 1e-4f;   // metres (float32 error of h is ~1e-6 m)
 
-// Kinds of a pair-result record (its flag word): not interacting, or
-// interacting (fx, fy, torque added by the gather).
-constexpr int RES_NONE = 0, RES_INTER = 1;
 
 // Per-warp queue of tc_pair_both: the sub-circle pairs that may have a
 // time-to-collision (9 slots per lane) and each lane's pair geometry.
@@ -1049,7 +1053,8 @@ __device__ __forceinline__ int tc_arm_signs_f32(float dxt, float dyt, const floa
 // distance search, the time-to-collision selection and the tau gradient are
 // computed once; each side's force, contact and torque come out exactly as
 // tc_pair_eval computes them from that side.  Warp collective like
-// tc_pair_eval (all 32 lanes call it).  Returns the record kind.
+// tc_pair_eval (all 32 lanes call it).  Returns RES_NONE, RES_ZERO (forces
+// +0, TP and TQ the exact signed zeros) or RES_FORCE.
 __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const float4 meF0,
                                              const float4 meF1, const StepArgs &a, bool act,
                                              int t, PairQueue &q, int lane, double &FPx,
@@ -1279,7 +1284,7 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
             TP = rpx * FPy - rpy * FPx;
             TQ = rqx * FQy - rqy * FQx;
         }
-        return RES_INTER;
+        return RES_ZERO;
     }
     if (!have_d) D = tc_distance_exact(A, B, pre.seq);
     double npx, npy, nqx, nqy, rpx, rpy, rqx, rqy;
@@ -1295,7 +1300,7 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
     }
     TP = rpx * FPy - rpy * FPx;
     TQ = rqx * FQy - rqy * FQx;
-    return RES_INTER;
+    return RES_FORCE;
 }
 
 // Resumable candidate enumeration into the thread's list (visiting order:
@@ -1903,11 +1908,23 @@ __device__ __forceinline__ int partner_entry(const StepArgs &a, int t, int s) {
     return (lo < end && __ldg(&a.nl_idx[lo]) == s) ? lo : -1;
 }
 
-__device__ __forceinline__ void put_res(double *res, int e, double fx, double fy, double tq,
-                                        int kind) {
-    double4_32a v;
-    v.x = fx; v.y = fy; v.z = tq; v.w = (double)kind;
-    *reinterpret_cast<double4_32a *>(res + (size_t)e * RES_D) = v;
+// One side of a pair into its near-list entry: the entry's kind byte, and
+// for a force its 32-byte record (fx, fy, torque).  A pair without a force
+// contributes (+0, +0) and a torque of +0 or -0; the kind says which.
+constexpr unsigned char KIND_NONE = 0, KIND_ZERO_POS = 1, KIND_ZERO_NEG = 2, KIND_FORCE = 3;
+
+__device__ __forceinline__ void put_pair(const StepArgs &a, int e, int res, double fx, double fy,
+                                         double tq) {
+    unsigned char kind = KIND_NONE;
+    if (res == RES_FORCE) {
+        kind = KIND_FORCE;
+        double4_32a v;
+        v.x = fx; v.y = fy; v.z = tq; v.w = 0.0;
+        *reinterpret_cast<double4_32a *>(a.nl_res + (size_t)e * RES_D) = v;
+    } else if (res == RES_ZERO) {
+        kind = signbit(tq) ? KIND_ZERO_NEG : KIND_ZERO_POS;
+    }
+    a.nl_kind[e] = kind;
 }
 
 // Every pair of the flat list once: warps claim 32 consecutive pairs at a
@@ -1937,9 +1954,9 @@ __global__ void __launch_bounds__(NTG) k_pairs(StepArgs a) {
         double fpx = 0.0, fpy = 0.0, tp = 0.0, fqx = 0.0, fqy = 0.0, tq = 0.0;
         int kind = RES_NONE;
         if (BODY == 0) {
-            if (act && pair_circular_both(load_circ(a.stage, s), load_circ(a.stage, t), fpx, fpy,
-                                          fqx, fqy))
-                kind = RES_INTER;
+            if (act)
+                kind = pair_circular_both(load_circ(a.stage, s), load_circ(a.stage, t), fpx, fpy,
+                                          fqx, fqy);
         } else {
             TC At;
             float4 me = make_float4(0.f, 0.f, 0.f, 0.f), meF0 = me, meF1 = me;
@@ -1955,9 +1972,9 @@ __global__ void __launch_bounds__(NTG) k_pairs(StepArgs a) {
                                 fpy, tp, fqx, fqy, tq);
         }
         if (act) {
-            put_res(a.nl_res, e, fpx, fpy, tp, kind);
+            put_pair(a, e, kind, fpx, fpy, tp);
             const int eq = partner_entry(a, t, s);
-            if (eq >= 0) put_res(a.nl_res, eq, fqx, fqy, tq, kind);
+            if (eq >= 0) put_pair(a, eq, kind, fqx, fqy, tq);
             else atomicOr(a.err, ERR_NEAR_LIST);
         }
     }
@@ -1978,13 +1995,20 @@ __device__ __forceinline__ void gather_agent(const StepArgs &a, const int s) {
     if (a.nodes & N_AGENT) {
         const double4_32a *res = reinterpret_cast<const double4_32a *>(a.nl_res);
         const int o1 = a.nl_off[s + 1];
+        constexpr long long NEG_ZERO = (long long)0x8000000000000000ULL;
         for (int e = a.nl_off[s]; e < o1; ++e) {
-            const double4_32a v = res[e];
-            // the kind is 0.0 or 1.0 (put_res): tested on its bits, off the FP64 pipe
-            if (__double_as_longlong(v.w) != 0) {
+            const unsigned char kind = __ldg(&a.nl_kind[e]);
+            if (kind == KIND_FORCE) {
+                const double4_32a v = res[e];
                 fx = fx + v.x;
                 fy = fy + v.y;
                 if (BODY == 1) tq = tq + v.z;
+            } else if (kind != KIND_NONE) {
+                // adding +0 changes only -0 (to +0); adding -0 changes nothing
+                if (__double_as_longlong(fx) == NEG_ZERO) fx = 0.0;
+                if (__double_as_longlong(fy) == NEG_ZERO) fy = 0.0;
+                if (BODY == 1 && kind == KIND_ZERO_POS && __double_as_longlong(tq) == NEG_ZERO)
+                    tq = 0.0;
             }
         }
     }
