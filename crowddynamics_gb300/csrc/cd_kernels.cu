@@ -1930,7 +1930,7 @@ __device__ __forceinline__ void put_pair(const StepArgs &a, int e, int res, doub
 // Every pair of the flat list once: warps claim 32 consecutive pairs at a
 // time (consecutive pairs mostly share their first agent).
 template <int BODY>
-__global__ void __launch_bounds__(NTG) k_pairs(StepArgs a) {
+__global__ void __launch_bounds__(NTG, 4) k_pairs(StepArgs a) {
     constexpr unsigned FULL = 0xffffffffu;
     if (a.nl_off[a.n] > a.nl_cap) return;
     extern __shared__ unsigned char smem[];
