@@ -1128,9 +1128,23 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
         const float e0 = 1e-6f * (1.f + fabsf(dxt) + fabsf(dyt) + fabsf(mox[1]) + fabsf(moy[1]) +
                                   fabsf(mox[2]) + fabsf(moy[2]) + fabsf(oox[1]) + fabsf(ooy[1]) +
                                   fabsf(oox[2]) + fabsf(ooy[2]));
-        int first = -1;                                  // class of the first sub-pair with a root
+        // Enclosing circles (radius = extent, rounded up, about the torsos)
+        // contain every sub-circle.  Apart now and for all t > 0 (c > 0, and
+        // b <= 0 or b^2 < a c, each with its error margin): no sub-pair ever
+        // overlaps at t > 0, so every root is negative and there is no force.
+        const float re = meC.z + oC.z;
+        const float xe2 = dxt * dxt + dyt * dyt;
+        const float be = -(dxt * vxf + dyt * vyf);
+        const float ce = xe2 - re * re;
+        const float mbe = 4.f * e0 * (fabsf(vxf) + fabsf(vyf)) +
+                          1e-6f * (fabsf(dxt * vxf) + fabsf(dyt * vyf));
+        const float mce = 8.f * e0 * (fabsf(dxt) + fabsf(dyt) + re) + 1e-6f * (xe2 + re * re);
+        const float bbe = fabsf(be) + mbe;
+        const bool apart = ce - mce > 0.f && (be + mbe <= 0.f || bbe * bbe < 0.99f * af * (ce - mce));
+        int first = apart ? 1 : -1;                      // class of the first sub-pair with a root
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
+            if (apart) break;
             const int i = k / 3, j = k % 3;
             const float dx = (dxt + mox[i]) - oox[j], dy = (dyt + moy[i]) - ooy[j];
             const float rt = mr[i] + orr[j];
