@@ -77,6 +77,7 @@ struct cd_ctx {
     int *nl_idx = nullptr;
     double *nl_res = nullptr;
     unsigned char *nl_kind = nullptr;
+    int *fix_count = nullptr, *fix_list = nullptr;
     int *fw_cnt = nullptr, *fw_off = nullptr, *fw_scan = nullptr;
     int *fs_cnt = nullptr, *fs_off = nullptr, *fs_scan = nullptr;
     int2 *fw_pairs = nullptr;
@@ -169,6 +170,8 @@ StepArgs args_of(cd_ctx *c, int nodes) {
     a.nl_idx = c->nl_idx;
     a.nl_res = c->nl_res;
     a.nl_kind = c->nl_kind;
+    a.fix_count = c->fix_count;
+    a.fix_list = c->fix_list;
     a.nl_cap = (int)c->nl_cap;
     a.nl_scan = c->nl_scan;
     a.fw_cnt = c->fw_cnt;
@@ -200,7 +203,8 @@ void release(cd_ctx *c) {
                     c->nl_scan, c->nl_idx, c->nl_res, c->nl_kind, c->fw_cnt, c->fw_off, c->fw_scan,
                     c->fw_pairs, c->ext, c->max_partial, c->tgt, c->navmap, c->rng_step,
                     c->states, c->herd, c->scen_h, c->counters, c->reached, c->polys,
-                    c->poly_off, c->fs_cnt, c->fs_off, c->fs_scan, c->nl_mask, c->nl_nch};
+                    c->poly_off, c->fs_cnt, c->fs_off, c->fs_scan, c->nl_mask, c->nl_nch,
+                    c->fix_count, c->fix_list};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -319,7 +323,8 @@ int64_t kernels_per_step(const cd_ctx *c, int nodes) {
     k += (nodes & CD_NODE_INTEGRATE) ? 1 : 0;           // dt
     k += cdk::scan_scratch_ints((int)c->ncells) > 1 ? 3 : 1;
     if (cdk::variant_pairs(c->variant) && (nodes & CD_NODE_AGENT_AGENT) && c->nl_cnt)
-        k += 4 + (cdk::scan_scratch_ints((int)c->n) > 1 ? 3 : 1);   // count fill pairs fallback + scans
+        k += 4 + (cdk::scan_scratch_ints((int)c->n) > 1 ? 3 : 1) +   // count fill pairs fallback + scans
+             (c->body == CD_BODY_THREE_CIRCLE ? 1 : 0);                // fixup
     return k;
 }
 
@@ -597,6 +602,8 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->nl_cnt, n + 1));
     step(dalloc(c, &c->nl_off, n + 1));
     step(dalloc(c, &c->nl_fwd, n));
+    step(dalloc(c, &c->fix_count, 1));
+    step(dalloc(c, &c->fix_list, n));
     step(dalloc(c, &c->nl_mask, (int64_t)n * cdk::NL_MASK_CHUNKS));
     step(dalloc(c, &c->nl_nch, n + 1));
     step(dalloc(c, &c->nl_scan, cdk::scan_scratch_ints((int)npad)));

@@ -225,6 +225,7 @@ __global__ void k_prepare(StepArgs a) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     // device fluctuation: this step's generator counter (read by the force stage)
     if (i == 0 && a.noise_dev && (a.nodes & N_FLUCT)) *a.rng_step += 1;
+    if (i == 0 && a.fix_count) *a.fix_count = 0;   // agents k_forces_fixup redoes
     int s = -1;
     double l = 0.0;
     if (i < a.n) {
@@ -1009,52 +1010,13 @@ __device__ __forceinline__ void tc_moment_arms(const TC &A, const TC &B, const T
     rqy = (sel3(A.y, D.qp) + r * nqy) - B.y[0];
 }
 
-// Sign bits of the four moment-arm components (rpx, rpy, rqx, rqy as
-// tc_moment_arms computes them: bits 0-3) from the float32 geometry, or -1
-// when a component is too close to zero to be certain.  A component is
-// (part offset from the side's torso) + r * n with n the unit normal; its
-// float32 value carries an error below E: positions 1e-6 of the magnitudes
-// involved (as in the distance pre-selection), n 2 E0 / d + 1e-6, products
-// and sums 1e-6 relative; the float64 rounding of the exact expression is
-// below 1e-12 m.  A value beyond 4 E + 1e-12 has the sign of the exact one
-// (and is non-zero).
-__device__ __forceinline__ int tc_arm_signs_f32(float dxt, float dyt, const float mox[3],
-                                                const float moy[3], const float oox[3],
-                                                const float ooy[3], const float mr[3],
-                                                const float orr[3], int pp, int qp) {
-    const float sx = (dxt + mox[pp]) - oox[qp], sy = (dyt + moy[pp]) - ooy[qp];
-    const float d = sqrtf(sx * sx + sy * sy);
-    if (!(d > 1e-3f)) return -1;
-    const float nx = sx / d, ny = sy / d;
-    const float e0 = 1e-6f * (1.f + fabsf(dxt) + fabsf(dyt) + fabsf(mox[1]) + fabsf(moy[1]) +
-                              fabsf(mox[2]) + fabsf(moy[2]) + fabsf(oox[1]) + fabsf(ooy[1]) +
-                              fabsf(oox[2]) + fabsf(ooy[2]));
-    const float en = 2.f * e0 / d + 1e-6f;
-    const float rp = mr[pp], rq = orr[qp];
-    // P: X_P[pp] - X_P[0] + r_P n;  Q: X_P[qp] - X_Q[0] - r_Q n (the first
-    // agent's part indexed by Q's part, core/distance.py:103)
-    const float dpx = mox[pp], dpy = moy[pp];
-    const float dqx = dxt + mox[qp], dqy = dyt + moy[qp];
-    const float v[4] = {dpx + rp * nx, dpy + rp * ny, dqx - rq * nx, dqy - rq * ny};
-    const float dd[4] = {dpx, dpy, dqx, dqy};
-    const float rr[4] = {rp, rp, rq, rq};
-    int bits = 0;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        const float e = e0 + rr[c] * en + 1e-6f * (fabsf(dd[c]) + rr[c] + fabsf(v[c]));
-        if (!(fabsf(v[c]) > 4.f * e + 1e-12f)) return -1;
-        bits |= (v[c] < 0.f) << c;
-    }
-    return bits;
-}
-
 // Both sides of a ThreeCircle pair (interactions.py:73-101,
 // power_law.py:264-363) with P = A first and Q = the pair partner: the
 // distance search, the time-to-collision selection and the tau gradient are
 // computed once; each side's force, contact and torque come out exactly as
 // tc_pair_eval computes them from that side.  Warp collective like
-// tc_pair_eval (all 32 lanes call it).  Returns RES_NONE, RES_ZERO (forces
-// +0, TP and TQ the exact signed zeros) or RES_FORCE.
+// tc_pair_eval (all 32 lanes call it).  Returns RES_NONE, RES_ZERO (no
+// force: forces +0, torques signed zeros left to the gather) or RES_FORCE.
 __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const float4 meF0,
                                              const float4 meF1, const StepArgs &a, bool act,
                                              int t, PairQueue &q, int lane, double &FPx,
@@ -1062,14 +1024,23 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
                                              double &TQ) {
     constexpr unsigned wmask = 0xffffffffu;
     constexpr int nlanes = 32;
-    TC B = A;
+    // Q's staged record is loaded only where a float64 path needs it
+    TC B;
+    bool have_b = false;
     float4 oC = meC, oF0 = meF0, oF1 = meF1;
+    double2 vq = make_double2(A.vx, A.vy);
     if (act) {
-        B = load_tc(a.stage, t);
         oC = __ldg(&a.cull[t]);
         oF0 = __ldg(&a.stage_f[2 * t]);
         oF1 = __ldg(&a.stage_f[2 * t + 1]);
+        vq = a.stage[(size_t)t * STAGE_Q_TC + 3];
     }
+    auto need_b = [&]() {
+        if (!have_b) {
+            B = load_tc(a.stage, t);
+            have_b = true;
+        }
+    };
     // float32 geometry of the sub-circles (P's frame)
     const float dxt = (meC.x - oC.x) + (meF0.x - oF0.x);
     const float dyt = (meC.y - oC.y) + (meF0.y - oF0.y);
@@ -1079,24 +1050,48 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
 
     // -- distance_three_circles --
     // The exact minimum is needed for a force (normal, contact, moment arms)
-    // and wherever float32 cannot decide the pair: several sub-pairs near the
-    // minimum, or h near 3 (interaction) or 0 (contact).  Elsewhere the
-    // single pre-selected sub-pair is the minimum and its float32 h decides.
-    const TcPre pre = tc_presel(dxt, dyt, mox, moy, oox, ooy, mr, orr, act);
-    const bool unique = (pre.seq & (pre.seq - 1u)) == 0u;
-    const bool far_cert = pre.hmin - pre.margin >= (float)SIGTH_SOC;
-    const bool near_cert = pre.hmin + pre.margin < (float)SIGTH_SOC && pre.hmin - pre.margin > 0.f;
-    const bool dist_cert = act && unique && (far_cert || near_cert);
+    // and wherever float32 cannot decide the pair.  The torso pair's skin
+    // distance bounds the minimum h from above, the enclosing circles' (radius
+    // = extent, rounded up) from below: with both clear of 3 and 0 by the
+    // float32 margin, the pair interacts without contact, or does not
+    // interact.  Otherwise the pre-selection keeps the sub-pairs near the
+    // float32 minimum; a single one with its h clear of 3 and 0 decides too,
+    // and the rest take the exact float64 minimum.
+    const float xe2 = dxt * dxt + dyt * dyt;
+    const float xe = sqrtf(xe2);
+    const float re = meC.z + oC.z;
+    const float dmarg = PRESEL_MARGIN +
+                        1e-6f * (fabsf(dxt) + fabsf(dyt) + fabsf(mox[1]) + fabsf(moy[1]) +
+                                 fabsf(mox[2]) + fabsf(moy[2]) + fabsf(oox[1]) + fabsf(ooy[1]) +
+                                 fabsf(oox[2]) + fabsf(ooy[2]) + mr[0] + mr[1] + orr[0] + orr[1]);
+    const float h_lo = xe - re, h_hi = xe - (mr[0] + orr[0]);
+    TcPre pre;
+    pre.seq = 1u;
+    bool have_pre = false;
     TcDist D;
-    D.pp = (__ffs(pre.seq) - 1) / 3;
-    D.qp = (__ffs(pre.seq) - 1) % 3;
     bool have_d = false;
-    if (act && !dist_cert) {
-        D = tc_distance_exact(A, B, pre.seq);
-        have_d = true;
+    bool inter = false;
+    if (act && !(h_lo - dmarg >= (float)SIGTH_SOC)) {
+        if (h_hi + dmarg < (float)SIGTH_SOC && h_lo - dmarg > 0.f) {
+            inter = true;
+        } else {
+            pre = tc_presel(dxt, dyt, mox, moy, oox, ooy, mr, orr, act);
+            have_pre = true;
+            const bool unique = (pre.seq & (pre.seq - 1u)) == 0u;
+            const bool far_cert = pre.hmin - pre.margin >= (float)SIGTH_SOC;
+            const bool near_cert =
+                pre.hmin + pre.margin < (float)SIGTH_SOC && pre.hmin - pre.margin > 0.f;
+            if (unique && (far_cert || near_cert)) {
+                inter = near_cert;
+            } else {
+                need_b();
+                D = tc_distance_exact(A, B, pre.seq);
+                have_d = true;
+                inter = D.h < SIGTH_SOC;
+            }
+        }
     }
     const double h_min = have_d ? D.h : 0.0;
-    const bool inter = act && (have_d ? h_min < SIGTH_SOC : near_cert);
     const bool contact = inter && have_d && h_min < 0;
 
     // -- force_social_three_circle (shared time-to-collision) --
@@ -1111,7 +1106,7 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
     // others put their candidate sub-pairs in the warp queue, where any lane
     // evaluates the reference's float64 b, c, discriminant, root and tau from
     // the owner's geometry in shared memory, and select tau as the reference.
-    const double vrx = A.vx - B.vx, vry = A.vy - B.vy;
+    const double vrx = A.vx - vq.x, vry = A.vy - vq.y;
     const float vxf = (float)vrx, vyf = (float)vry;
     double av = 0.0;
     bool have_av = false;
@@ -1180,6 +1175,7 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
             av = vrx * vrx + vry * vry;
             have_av = true;
         }
+        need_b();
         unsigned mrest = candmask;
         while (mrest) {
             const int k = __ffs(mrest) - 1;
@@ -1258,6 +1254,7 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
     FPx = 0.0; FPy = 0.0; FQx = 0.0; FQy = 0.0;
     const bool social = soc && candmask && !(isnan(tau) || tau <= 0);
     if (social) {
+        need_b();
         const int mi = k_sel / 3, ti = k_sel % 3;
         double o1x, o1y, o2x, o2y;
         r_off_part(A, mi, o1x, o1y);
@@ -1279,28 +1276,17 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
         FQy = (cmq * (-gy)) * magq;
         truncate2(FQx, FQy, F_SOC_MAX);
     }
-    if (!(social || contact)) {
-        // No force on either side: each side's torque is r x (+0, +0) =
-        // r.x * (+0) - r.y * (+0), which is -0 exactly when r.x has its sign
-        // bit set and r.y has not.  The signs come from float32 where that is
-        // certain, so the normal's divisions and the arms are skipped.
-        TP = 0.0;
-        TQ = 0.0;
-        if (!inter) return RES_NONE;
-        const int sg = tc_arm_signs_f32(dxt, dyt, mox, moy, oox, ooy, mr, orr, D.pp, D.qp);
-        if (sg >= 0) {
-            TP = ((sg & 3) == 1) ? -0.0 : 0.0;
-            TQ = ((sg & 12) == 4) ? -0.0 : 0.0;
-        } else {
-            if (!have_d) D = tc_distance_exact(A, B, pre.seq);
-            double npx, npy, nqx, nqy, rpx, rpy, rqx, rqy;
-            tc_moment_arms(A, B, D, npx, npy, nqx, nqy, rpx, rpy, rqx, rqy);
-            TP = rpx * FPy - rpy * FPx;
-            TQ = rqx * FQy - rqy * FQx;
-        }
-        return RES_ZERO;
+    TP = 0.0;
+    TQ = 0.0;
+    // No force on either side: forces (+0, +0), and each side's torque
+    // r x (+0, +0) a signed zero that the gather needs only when the agent's
+    // running torque is -0 (then k_forces_fixup evaluates it)
+    if (!(social || contact)) return inter ? RES_ZERO : RES_NONE;
+    need_b();
+    if (!have_d) {
+        if (!have_pre) pre = tc_presel(dxt, dyt, mox, moy, oox, ooy, mr, orr, act);
+        D = tc_distance_exact(A, B, pre.seq);
     }
-    if (!have_d) D = tc_distance_exact(A, B, pre.seq);
     double npx, npy, nqx, nqy, rpx, rpy, rqx, rqy;
     tc_moment_arms(A, B, D, npx, npy, nqx, nqy, rpx, rpy, rqx, rqy);
     if (contact) {
@@ -1924,8 +1910,8 @@ __device__ __forceinline__ int partner_entry(const StepArgs &a, int t, int s) {
 
 // One side of a pair into its near-list entry: the entry's kind byte, and
 // for a force its 32-byte record (fx, fy, torque).  A pair without a force
-// contributes (+0, +0) and a torque of +0 or -0; the kind says which.
-constexpr unsigned char KIND_NONE = 0, KIND_ZERO_POS = 1, KIND_ZERO_NEG = 2, KIND_FORCE = 3;
+// contributes (+0, +0) and a signed-zero torque.
+constexpr unsigned char KIND_NONE = 0, KIND_ZERO = 1, KIND_FORCE = 3;
 
 __device__ __forceinline__ void put_pair(const StepArgs &a, int e, int res, double fx, double fy,
                                          double tq) {
@@ -1936,7 +1922,7 @@ __device__ __forceinline__ void put_pair(const StepArgs &a, int e, int res, doub
         v.x = fx; v.y = fy; v.z = tq; v.w = 0.0;
         *reinterpret_cast<double4_32a *>(a.nl_res + (size_t)e * RES_D) = v;
     } else if (res == RES_ZERO) {
-        kind = signbit(tq) ? KIND_ZERO_NEG : KIND_ZERO_POS;
+        kind = KIND_ZERO;
     }
     a.nl_kind[e] = kind;
 }
@@ -1994,10 +1980,37 @@ __global__ void __launch_bounds__(NTG, 4) k_pairs(StepArgs a) {
     }
 }
 
+// Torque of slot s's side of the interacting pair (s, t) that exerts no
+// force: r x (+0, +0) with the exact moment arm r, as tc_pair_both computes
+// it for a pair with a force (the same distance search and arms).
+__device__ __noinline__ double tc_zero_force_torque(const StepArgs &a, int s, int t) {
+    const int p = s < t ? s : t, q = s < t ? t : s;
+    const TC A = load_tc(a.stage, p), B = load_tc(a.stage, q);
+    const float4 meC = __ldg(&a.cull[p]), meF0 = __ldg(&a.stage_f[2 * p]),
+                 meF1 = __ldg(&a.stage_f[2 * p + 1]);
+    const float4 oC = __ldg(&a.cull[q]), oF0 = __ldg(&a.stage_f[2 * q]),
+                 oF1 = __ldg(&a.stage_f[2 * q + 1]);
+    const float dxt = (meC.x - oC.x) + (meF0.x - oF0.x);
+    const float dyt = (meC.y - oC.y) + (meF0.y - oF0.y);
+    const float mox[3] = {0.f, meF1.x, meF1.z}, moy[3] = {0.f, meF1.y, meF1.w};
+    const float oox[3] = {0.f, oF1.x, oF1.z}, ooy[3] = {0.f, oF1.y, oF1.w};
+    const float mr[3] = {meF0.z, meF0.w, meF0.w}, orr[3] = {oF0.z, oF0.w, oF0.w};
+    const TcPre pre = tc_presel(dxt, dyt, mox, moy, oox, ooy, mr, orr, true);
+    const TcDist D = tc_distance_exact(A, B, pre.seq);
+    double npx, npy, nqx, nqy, rpx, rpy, rqx, rqy;
+    tc_moment_arms(A, B, D, npx, npy, nqx, nqy, rpx, rpy, rqx, rqy);
+    return s == p ? rpx * 0.0 - rpy * 0.0 : rqx * 0.0 - rqy * 0.0;
+}
+
 // Agent in slot s from its near-list results: one lane per agent, entries
 // added in list order (32-byte records, one sector each), then walls and
 // integration at full lane occupancy.
-template <int BODY>
+// A record without a force adds (+0, +0) and a signed-zero torque: that
+// changes a running force only from -0 to +0, and a running torque only when
+// it is -0, the one case in which the torque's sign is needed.  The gather
+// then leaves the agent (writing nothing) to k_forces_fixup, which runs it
+// again with EXACT, evaluating those signs.
+template <int BODY, bool EXACT>
 __device__ __forceinline__ void gather_agent(const StepArgs &a, const int s) {
     const int i = a.perm[s];
     const int sid = a.scen_of[i];
@@ -2017,12 +2030,16 @@ __device__ __forceinline__ void gather_agent(const StepArgs &a, const int s) {
                 fx = fx + v.x;
                 fy = fy + v.y;
                 if (BODY == 1) tq = tq + v.z;
-            } else if (kind != KIND_NONE) {
-                // adding +0 changes only -0 (to +0); adding -0 changes nothing
+            } else if (kind == KIND_ZERO) {
                 if (__double_as_longlong(fx) == NEG_ZERO) fx = 0.0;
                 if (__double_as_longlong(fy) == NEG_ZERO) fy = 0.0;
-                if (BODY == 1 && kind == KIND_ZERO_POS && __double_as_longlong(tq) == NEG_ZERO)
-                    tq = 0.0;
+                if (BODY == 1 && __double_as_longlong(tq) == NEG_ZERO) {
+                    if (!EXACT) {
+                        a.fix_list[atomicAdd(a.fix_count, 1)] = s;
+                        return;
+                    }
+                    tq = tq + tc_zero_force_torque(a, s, __ldg(&a.nl_idx[e]));
+                }
             }
         }
     }
@@ -2033,7 +2050,16 @@ template <int BODY>
 __global__ void __launch_bounds__(NTG) k_forces_gather(StepArgs a) {
     if ((a.nodes & N_AGENT) && a.nl_off[a.n] > a.nl_cap) return;   // k_forces_fallback's step
     const int s = blockIdx.x * NTG + threadIdx.x;
-    if (s < a.n) gather_agent<BODY>(a, s);
+    if (s < a.n) gather_agent<BODY, false>(a, s);
+}
+
+// The agents the gather left: each evaluated again with the exact torque
+// signs of its records without a force.
+template <int BODY>
+__global__ void __launch_bounds__(NTG) k_forces_fixup(StepArgs a) {
+    const int nfix = *a.fix_count;
+    for (int f = blockIdx.x * NTG + threadIdx.x; f < nfix; f += gridDim.x * NTG)
+        gather_agent<BODY, true>(a, a.fix_list[f]);
 }
 
 // The lane-group kernel, for a step whose near lists exceeded the capacity.
@@ -2606,6 +2632,8 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
     if (v.pairs) blocks = nblk(a.n, NTG);                // gather: one lane per agent, full grid
     cudaMemsetAsync(a.work, 0, sizeof(int), s);
     kForces[body][variant]<<<blocks, v.nt, forces_smem_bytes(body, variant), s>>>(a);
+    if (v.pairs && (a.nodes & N_AGENT) && body == 1)
+        k_forces_fixup<1><<<4, NTG, 0, s>>>(a);
     if (v.pairs && (a.nodes & N_AGENT)) {
         const int gv = variant - 4;                       // the lane-group twin
         int rg = (dev >= 0 && dev < 64) ? g_forces_blocks[dev][body][gv] : 0;
