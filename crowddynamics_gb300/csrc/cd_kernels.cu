@@ -1897,9 +1897,30 @@ __global__ void __launch_bounds__(NTG) k_nl_fill(StepArgs a) {
 }
 
 // Entry of `s` in the earlier-slot part of `t`'s near list (s < t), or -1.
+// The part is scanned 32 entries at a time with eight independent 16-byte
+// loads from a 4-aligned start (one memory round trip for most lists);
+// entries outside the part are ignored.  Near the end of the allocation a
+// binary search replaces the wide loads.
 __device__ __forceinline__ int partner_entry(const StepArgs &a, int t, int s) {
     int lo = __ldg(&a.nl_off[t]), hi = __ldg(&a.nl_fwd[t]);
     const int end = hi;
+    for (int base = lo & ~3; base < end && base + 32 <= a.nl_cap; base += 32) {
+        const int4 *p = reinterpret_cast<const int4 *>(a.nl_idx + base);
+        int4 q[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) q[k] = __ldg(p + k);
+        int found = -1;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int e = base + 4 * k;
+            if (q[k].x == s && e >= lo && e < end) found = e;
+            if (q[k].y == s && e + 1 >= lo && e + 1 < end) found = e + 1;
+            if (q[k].z == s && e + 2 >= lo && e + 2 < end) found = e + 2;
+            if (q[k].w == s && e + 3 >= lo && e + 3 < end) found = e + 3;
+        }
+        if (found >= 0) return found;
+        lo = base + 32 > lo ? base + 32 : lo;
+    }
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
         if (__ldg(&a.nl_idx[mid]) < s) lo = mid + 1;
