@@ -1191,66 +1191,69 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
         g[12] = A.rt; g[13] = A.rs; g[14] = B.rt; g[15] = B.rs;
         g[16] = vrx; g[17] = vry; g[18] = av;
     }
-    int incl = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        int v = __shfl_up_sync(wmask, incl, o);
-        if (lane >= o) incl += v;
-    }
-    q.off[lane] = incl - cnt;
-    const int total = __shfl_sync(wmask, incl, nlanes - 1);
-    if (lane == nlanes - 1) q.off[nlanes] = incl;
-    __syncwarp(wmask);
-    for (int base = 0; base < total; base += nlanes) {
-        int it = base + lane;
-        if (it < total) {
-            int lo = 0, hi = nlanes - 1;        // owner: last lane with off <= it
-            while (lo < hi) {
-                int mid = (lo + hi + 1) >> 1;
-                if (q.off[mid] <= it) lo = mid; else hi = mid - 1;
-            }
-            const int slot = lo * 9 + (it - q.off[lo]);
-            const int k = q.kidx[slot];
-            const int i = k / 3, j = k % 3;
-            const double *g = q.geo + lo * GEO_D;
-            const double gvx = g[16], gvy = g[17], ga = g[18];
-            const double xr = g[i] - g[6 + j], yr = g[3 + i] - g[9 + j];
-            const double r_tot = g[12 + (i > 0)] + g[14 + (j > 0)];
-            const double b = -(xr * gvx + yr * gvy);
-            const double c = (xr * xr + yr * yr) - r_tot * r_tot;
-            const double disc = b * b - ga * c;
-            double d = -1.0, tau_k = 0.0;
-            if (disc > 0) {                      // sqrt defined and non-zero
-                d = sqrt(disc);
-                tau_k = (b - d) / ga;
-            }
-            q.b[slot] = b;
-            q.disc[slot] = d;                    // -1: no time-to-collision
-            q.tau[slot] = tau_k;
-        }
-    }
-    __syncwarp(wmask);
     double tau = __longlong_as_double(0x7ff8000000000000LL);
     double b_min = 0.0, d_min = 0.0;
     int k_sel = 0;
-    {
-        int jj = 0;
+    // the queue (scan, float64 roots, selection) only where a lane needs it
+    if (__any_sync(wmask, cnt > 0)) {
+        int incl = cnt;
 #pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            if (candmask & (1u << k)) {
-                const int slot = lane * 9 + jj;
-                ++jj;
-                const double dk = q.disc[slot];
-                if (dk > 0) {
-                    const double tau_new = q.tau[slot];
-                    if (isnan(tau) || (0 < tau_new && tau_new < tau)) {
-                        k_sel = k; tau = tau_new; b_min = q.b[slot]; d_min = dk;
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(wmask, incl, o);
+            if (lane >= o) incl += v;
+        }
+        q.off[lane] = incl - cnt;
+        const int total = __shfl_sync(wmask, incl, nlanes - 1);
+        if (lane == nlanes - 1) q.off[nlanes] = incl;
+        __syncwarp(wmask);
+        for (int base = 0; base < total; base += nlanes) {
+            int it = base + lane;
+            if (it < total) {
+                int lo = 0, hi = nlanes - 1;        // owner: last lane with off <= it
+                while (lo < hi) {
+                    int mid = (lo + hi + 1) >> 1;
+                    if (q.off[mid] <= it) lo = mid; else hi = mid - 1;
+                }
+                const int slot = lo * 9 + (it - q.off[lo]);
+                const int k = q.kidx[slot];
+                const int i = k / 3, j = k % 3;
+                const double *g = q.geo + lo * GEO_D;
+                const double gvx = g[16], gvy = g[17], ga = g[18];
+                const double xr = g[i] - g[6 + j], yr = g[3 + i] - g[9 + j];
+                const double r_tot = g[12 + (i > 0)] + g[14 + (j > 0)];
+                const double b = -(xr * gvx + yr * gvy);
+                const double c = (xr * xr + yr * yr) - r_tot * r_tot;
+                const double disc = b * b - ga * c;
+                double d = -1.0, tau_k = 0.0;
+                if (disc > 0) {                      // sqrt defined and non-zero
+                    d = sqrt(disc);
+                    tau_k = (b - d) / ga;
+                }
+                q.b[slot] = b;
+                q.disc[slot] = d;                    // -1: no time-to-collision
+                q.tau[slot] = tau_k;
+            }
+        }
+        __syncwarp(wmask);
+        {
+            int jj = 0;
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                if (candmask & (1u << k)) {
+                    const int slot = lane * 9 + jj;
+                    ++jj;
+                    const double dk = q.disc[slot];
+                    if (dk > 0) {
+                        const double tau_new = q.tau[slot];
+                        if (isnan(tau) || (0 < tau_new && tau_new < tau)) {
+                            k_sel = k; tau = tau_new; b_min = q.b[slot]; d_min = dk;
+                        }
                     }
                 }
             }
         }
+        __syncwarp(wmask);
     }
-    __syncwarp(wmask);
     FPx = 0.0; FPy = 0.0; FQx = 0.0; FQy = 0.0;
     const bool social = soc && candmask && !(isnan(tau) || tau <= 0);
     if (social) {
