@@ -1765,7 +1765,8 @@ __device__ __forceinline__ bool social_guess(float4 me, float4 o) {
     const float b = -(dx * vx + dy * vy);
     const float c = x2 - re * re;
     const float disc = b * b - (vx * vx + vy * vy) * c;
-    return sqrtf(x2) - re < 3.0f && disc > 0.0f && (b > 0.0f || c < 0.0f);
+    const float sight = 3.0f + re;                      // skin distance below 3 m
+    return x2 < sight * sight && disc > 0.0f && (b > 0.0f || c < 0.0f);
 }
 
 // Near lists in two passes over the same candidate chunks (L consecutive
