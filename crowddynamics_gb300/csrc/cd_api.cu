@@ -77,7 +77,7 @@ struct cd_ctx {
     int *nl_idx = nullptr;
     double *nl_res = nullptr;
     unsigned char *nl_kind = nullptr;
-    int *fix_count = nullptr, *fix_list = nullptr;
+    int *fix_count = nullptr, *fix_list = nullptr, *slot_of = nullptr;
     int *fw_cnt = nullptr, *fw_off = nullptr, *fw_scan = nullptr;
     int *fs_cnt = nullptr, *fs_off = nullptr, *fs_scan = nullptr;
     int2 *fw_pairs = nullptr;
@@ -172,6 +172,7 @@ StepArgs args_of(cd_ctx *c, int nodes) {
     a.nl_kind = c->nl_kind;
     a.fix_count = c->fix_count;
     a.fix_list = c->fix_list;
+    a.slot_of = c->slot_of;
     a.nl_cap = (int)c->nl_cap;
     a.nl_scan = c->nl_scan;
     a.fw_cnt = c->fw_cnt;
@@ -204,7 +205,7 @@ void release(cd_ctx *c) {
                     c->fw_pairs, c->ext, c->max_partial, c->tgt, c->navmap, c->rng_step,
                     c->states, c->herd, c->scen_h, c->counters, c->reached, c->polys,
                     c->poly_off, c->fs_cnt, c->fs_off, c->fs_scan, c->nl_mask, c->nl_nch,
-                    c->fix_count, c->fix_list};
+                    c->fix_count, c->fix_list, c->slot_of};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -604,6 +605,7 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->nl_fwd, n));
     step(dalloc(c, &c->fix_count, 1));
     step(dalloc(c, &c->fix_list, n));
+    step(dalloc(c, &c->slot_of, n));
     step(dalloc(c, &c->nl_mask, (int64_t)n * cdk::NL_MASK_CHUNKS));
     step(dalloc(c, &c->nl_nch, n + 1));
     step(dalloc(c, &c->nl_scan, cdk::scan_scratch_ints((int)npad)));

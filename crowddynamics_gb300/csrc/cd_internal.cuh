@@ -82,6 +82,7 @@ struct StepArgs {
     int *err;
     int *work;                   // force-kernel work counter (zeroed per launch)
     int *fix_count, *fix_list;   // agents the gather leaves to k_forces_fixup
+    int *slot_of;                // per agent: its cell-sorted slot (k_rank)
     // near lists (compute-once pair pipeline): per cell-sorted slot, the
     // slots of its near candidates in ascending order (= visiting order)
     int *nl_cnt;                 // n + 1 counts (scan input)

@@ -436,6 +436,7 @@ __global__ void k_rank(StepArgs a) {
     int r = 0;
     for (int q = b; q < e; ++q) r += (a.perm_unsorted[q] < i);
     a.perm[b + r] = i;
+    if (a.slot_of) a.slot_of[i] = b + r;
 }
 
 // Extent: distance from the torso centre to the farthest skin point.
@@ -465,10 +466,14 @@ __device__ __forceinline__ float up_f(double v) {
     return f + fabsf(f) * 1e-6f + 1e-6f;
 }
 
+// One lane per agent where the slots are known (column reads coalesced, the
+// staged records written whole), else one lane per slot.
 __global__ void k_gather(StepArgs a) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= a.n) return;
-    int i = a.perm[s];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.n) return;
+    int s, i;
+    if (a.slot_of) { i = t; s = a.slot_of[t]; }
+    else { s = t; i = a.perm[t]; }
     double *const *c = a.col;
     if (a.body == 0) {
         double2 *p = a.stage + (size_t)s * STAGE_Q_CIRC;
@@ -2036,8 +2041,7 @@ __device__ __noinline__ double tc_zero_force_torque(const StepArgs &a, int s, in
 // then leaves the agent (writing nothing) to k_forces_fixup, which runs it
 // again with EXACT, evaluating those signs.
 template <int BODY, bool EXACT>
-__device__ __forceinline__ void gather_agent(const StepArgs &a, const int s) {
-    const int i = a.perm[s];
+__device__ __forceinline__ void gather_agent(const StepArgs &a, const int s, const int i) {
     const int sid = a.scen_of[i];
     const ScenDev sc = a.scen[sid];
     const float4 me = a.cull[s];
@@ -2074,8 +2078,9 @@ __device__ __forceinline__ void gather_agent(const StepArgs &a, const int s) {
 template <int BODY>
 __global__ void __launch_bounds__(NTG) k_forces_gather(StepArgs a) {
     if ((a.nodes & N_AGENT) && a.nl_off[a.n] > a.nl_cap) return;   // k_forces_fallback's step
+    // one lane per slot: the entries of neighbouring lanes are neighbours
     const int s = blockIdx.x * NTG + threadIdx.x;
-    if (s < a.n) gather_agent<BODY, false>(a, s);
+    if (s < a.n) gather_agent<BODY, false>(a, s, a.perm[s]);
 }
 
 // The agents the gather left: each evaluated again with the exact torque
@@ -2083,8 +2088,10 @@ __global__ void __launch_bounds__(NTG) k_forces_gather(StepArgs a) {
 template <int BODY>
 __global__ void __launch_bounds__(NTG) k_forces_fixup(StepArgs a) {
     const int nfix = *a.fix_count;
-    for (int f = blockIdx.x * NTG + threadIdx.x; f < nfix; f += gridDim.x * NTG)
-        gather_agent<BODY, true>(a, a.fix_list[f]);
+    for (int f = blockIdx.x * NTG + threadIdx.x; f < nfix; f += gridDim.x * NTG) {
+        const int s = a.fix_list[f];
+        gather_agent<BODY, true>(a, s, a.perm[s]);
+    }
 }
 
 // The lane-group kernel, for a step whose near lists exceeded the capacity.
