@@ -2079,7 +2079,9 @@ template <int BODY>
 __global__ void __launch_bounds__(NTG) k_forces_gather(StepArgs a) {
     if ((a.nodes & N_AGENT) && a.nl_off[a.n] > a.nl_cap) return;   // k_forces_fallback's step
     // one lane per slot: the entries of neighbouring lanes are neighbours
-    const int s = blockIdx.x * NTG + threadIdx.x;
+    // (launched in one-warp blocks: the float64 epilogue spreads evenly
+    // over the SMs)
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s < a.n) gather_agent<BODY, false>(a, s, a.perm[s]);
 }
 
@@ -2661,9 +2663,13 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
     if (resident <= 0) resident = 152;
     const long long threads = (long long)a.n * v.lanes;
     int blocks = (int)std::min<long long>((threads + v.nt - 1) / v.nt, resident);
-    if (v.pairs) blocks = nblk(a.n, NTG);                // gather: one lane per agent, full grid
+    int nt = v.nt;
+    if (v.pairs) {                                       // gather: one lane per slot, full grid
+        nt = 32;
+        blocks = nblk(a.n, nt);
+    }
     cudaMemsetAsync(a.work, 0, sizeof(int), s);
-    kForces[body][variant]<<<blocks, v.nt, forces_smem_bytes(body, variant), s>>>(a);
+    kForces[body][variant]<<<blocks, nt, forces_smem_bytes(body, variant), s>>>(a);
     if (v.pairs && (a.nodes & N_AGENT) && body == 1)
         k_forces_fixup<1><<<4, NTG, 0, s>>>(a);
     if (v.pairs && (a.nodes & N_AGENT)) {
