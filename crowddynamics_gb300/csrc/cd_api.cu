@@ -296,7 +296,8 @@ void enqueue_cells(cd_ctx *c, const StepArgs &a) {
     cudaMemsetAsync(c->fill, 0, sizeof(int) * c->ncells, c->stream);
     cudaMemsetAsync(c->vmax, 0, sizeof(unsigned long long) * c->nscen, c->stream);
     cdk::launch_prepare(a, c->stream);
-    if (a.nodes & cdk::N_INTEG) cdk::launch_dt(a, c->stream);
+    // dt is computed by the scatter kernel, launched only for agents
+    if ((a.nodes & cdk::N_INTEG) && a.n == 0) cdk::launch_dt(a, c->stream);
     cdk::launch_scan(c->count, c->start, (int)c->ncells, c->scan_scratch, c->stream);
     cdk::launch_scatter(a, c->stream);
     cdk::launch_gather(a, c->stream);
@@ -320,12 +321,10 @@ void enqueue_step(cd_ctx *c, int nodes, bool timed, bool captured = false) {
 
 int64_t kernels_per_step(const cd_ctx *c, int nodes) {
     if (c->n == 0) return (nodes & CD_NODE_INTEGRATE) ? 1 : 0;
-    int64_t k = 5;                                      // prepare scatter rank gather forces
-    k += (nodes & CD_NODE_INTEGRATE) ? 1 : 0;           // dt
-    k += cdk::scan_scratch_ints((int)c->ncells) > 1 ? 3 : 1;
+    int64_t k = 5;                                      // prepare scatter(+dt) rank gather forces
+    k += cdk::scan_launches_single((int)c->ncells);
     if (cdk::variant_pairs(c->variant) && (nodes & CD_NODE_AGENT_AGENT) && c->nl_cnt)
-        k += 4 + (cdk::scan_scratch_ints((int)c->n) > 1 ? 3 : 1) +   // count fill pairs fallback + scans
-             (c->body == CD_BODY_THREE_CIRCLE ? 1 : 0);                // fixup
+        k += 4 + (cdk::scan_scratch_ints((int)c->n) > 1 ? 3 : 1);   // count fill pairs fallback + scans
     return k;
 }
 

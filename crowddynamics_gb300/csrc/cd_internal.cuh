@@ -182,6 +182,7 @@ void launch_prepare(const StepArgs &a, cudaStream_t s);
 void launch_dt(const StepArgs &a, cudaStream_t s);
 int scan_scratch_ints(int n);
 void launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s);
+int scan_launches_single(int n);          // kernels launch_scan uses for n elements
 void launch_scatter(const StepArgs &a, cudaStream_t s);
 void launch_gather(const StepArgs &a, cudaStream_t s);
 constexpr int N_VARIANTS = 12;      // launch variants of the force kernel

@@ -225,7 +225,7 @@ __global__ void k_prepare(StepArgs a) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     // device fluctuation: this step's generator counter (read by the force stage)
     if (i == 0 && a.noise_dev && (a.nodes & N_FLUCT)) *a.rng_step += 1;
-    if (i == 0 && a.fix_count) *a.fix_count = 0;   // agents k_forces_fixup redoes
+    if (i == 0 && a.fix_count) *a.fix_count = 0;   // agents the gather leaves for a redo
     int s = -1;
     double l = 0.0;
     if (i < a.n) {
@@ -260,9 +260,7 @@ __global__ void k_prepare(StepArgs a) {
 }
 
 // adaptive_timestep, core/integrator.py:29-97; accumulates time_tot.
-__global__ void k_dt(StepArgs a) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= a.n_scen) return;
+__device__ __forceinline__ void scenario_dt(const StepArgs &a, int s) {
     const ScenDev sc = a.scen[s];
     double v_max = __longlong_as_double((long long)a.vmax[s]);
     double dt;
@@ -278,6 +276,11 @@ __global__ void k_dt(StepArgs a) {
     }
     a.dt[s] = dt;
     a.time_tot[s] += dt;
+}
+
+__global__ void k_dt(StepArgs a) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < a.n_scen) scenario_dt(a, s);
 }
 
 // Per-scenario max of target_velocity (np.max propagates NaN).
@@ -409,6 +412,52 @@ __global__ void __launch_bounds__(SCAN_NT) k_scan_local(ScanSet S, int n) {
     }
 }
 
+// One block scanning up to a few tiles in turn (one launch for small arrays).
+__global__ void __launch_bounds__(SCAN_NT) k_scan_single(const int *in, int *out, int n) {
+    __shared__ int wtot[SCAN_NT / 32];
+    __shared__ int tile_total;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int carry = 0;
+    for (int t0 = 0; t0 < n; t0 += SCAN_TILE) {
+        const int base = t0 + threadIdx.x * SCAN_IPT;
+        int v[SCAN_IPT];
+        int sum = 0;
+#pragma unroll
+        for (int k = 0; k < SCAN_IPT; ++k) {
+            v[k] = (base + k < n) ? in[base + k] : 0;
+            sum += v[k];
+        }
+        int incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) wtot[w] = incl;
+        __syncthreads();
+        if (w == 0) {
+            int x = wtot[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int t = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += t;
+            }
+            wtot[lane] = x;
+            if (lane == 31) tile_total = x;
+        }
+        __syncthreads();
+        int excl = carry + incl - sum + (w > 0 ? wtot[w - 1] : 0);
+#pragma unroll
+        for (int k = 0; k < SCAN_IPT; ++k) {
+            if (base + k < n) out[base + k] = excl;
+            excl += v[k];
+        }
+        carry += tile_total;
+        __syncthreads();                      // wtot and tile_total reused
+    }
+    if (threadIdx.x == 0) out[n] = carry;
+}
+
 __global__ void k_scan_add(ScanSet S, int n, int nb) {
     int *out = S.out[blockIdx.y];
     const int *offs = S.in[blockIdx.y];
@@ -418,6 +467,9 @@ __global__ void k_scan_add(ScanSet S, int n, int nb) {
 }
 
 __global__ void k_scatter(StepArgs a) {
+    // the step's dt: k_prepare's max |v| is complete once this kernel runs
+    if (blockIdx.x == 0 && (a.nodes & N_INTEG))
+        for (int sc = threadIdx.x; sc < a.n_scen; sc += blockDim.x) scenario_dt(a, sc);
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     int c = a.key[i];
@@ -1288,7 +1340,7 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
     TQ = 0.0;
     // No force on either side: forces (+0, +0), and each side's torque
     // r x (+0, +0) a signed zero that the gather needs only when the agent's
-    // running torque is -0 (then k_forces_fixup evaluates it)
+    // running torque is -0 (the agent is then redone with exact signs)
     if (!(social || contact)) return inter ? RES_ZERO : RES_NONE;
     need_b();
     if (!have_d) {
@@ -2038,8 +2090,9 @@ __device__ __noinline__ double tc_zero_force_torque(const StepArgs &a, int s, in
 // A record without a force adds (+0, +0) and a signed-zero torque: that
 // changes a running force only from -0 to +0, and a running torque only when
 // it is -0, the one case in which the torque's sign is needed.  The gather
-// then leaves the agent (writing nothing) to k_forces_fixup, which runs it
-// again with EXACT, evaluating those signs.
+// then leaves the agent (writing nothing) to the next kernel
+// (k_forces_fallback, which otherwise has nothing to do), which runs it again
+// with EXACT, evaluating those signs.
 template <int BODY, bool EXACT>
 __device__ __forceinline__ void gather_agent(const StepArgs &a, const int s, const int i) {
     const int sid = a.scen_of[i];
@@ -2085,21 +2138,21 @@ __global__ void __launch_bounds__(NTG) k_forces_gather(StepArgs a) {
     if (s < a.n) gather_agent<BODY, false>(a, s, a.perm[s]);
 }
 
-// The agents the gather left: each evaluated again with the exact torque
-// signs of its records without a force.
-template <int BODY>
-__global__ void __launch_bounds__(NTG) k_forces_fixup(StepArgs a) {
-    const int nfix = *a.fix_count;
-    for (int f = blockIdx.x * NTG + threadIdx.x; f < nfix; f += gridDim.x * NTG) {
-        const int s = a.fix_list[f];
-        gather_agent<BODY, true>(a, s, a.perm[s]);
-    }
-}
-
 // The lane-group kernel, for a step whose near lists exceeded the capacity.
 template <int BODY, int L>
 __global__ void __launch_bounds__(NTG) k_forces_fallback(StepArgs a) {
-    if (!((a.nodes & N_AGENT) && a.nl_off[a.n] > a.nl_cap)) return;
+    if (!((a.nodes & N_AGENT) && a.nl_off[a.n] > a.nl_cap)) {
+        // the gather ran: redo the agents it left (their torque reached -0)
+        if (BODY == 1) {
+            const int nfix = *a.fix_count;
+            for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nfix;
+                 f += gridDim.x * blockDim.x) {
+                const int s = a.fix_list[f];
+                gather_agent<BODY, true>(a, s, a.perm[s]);
+            }
+        }
+        return;
+    }
     extern __shared__ unsigned char smem[];
     int *gq_all = reinterpret_cast<int *>(smem);
     WarpQueue *wq = reinterpret_cast<WarpQueue *>(smem + sizeof(int) * 2 * NTG);
@@ -2473,6 +2526,7 @@ void launch_prepare(const StepArgs &a, cudaStream_t s) {
 void launch_dt(const StepArgs &a, cudaStream_t s) {
     if (a.n_scen > 0) k_dt<<<nblk(a.n_scen, 128), 128, 0, s>>>(a);
 }
+int scan_launches_single(int n) { return nblk(n, SCAN_TILE) <= 4 ? 1 : 3; }
 int scan_scratch_ints(int n) {
     int nb = nblk(n, SCAN_TILE);
     return nb > 1 ? 2 * (nb + 1) : 1;
@@ -2506,6 +2560,10 @@ void launch_scans(int k, const int *const *in, int *const *out, int n, int *cons
     k_scan_add<<<dim3(nblk(n + 1, 256), k), 256, 0, s>>>(U, n, nb);
 }
 void launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s) {
+    if (n > SCAN_TILE && n <= 4 * SCAN_TILE) {
+        k_scan_single<<<1, SCAN_NT, 0, s>>>(in, out, n);
+        return;
+    }
     launch_scans(1, &in, &out, n, &scratch, s);
 }
 // Near, forward and guessed-social counts scanned together.
@@ -2670,8 +2728,6 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
     }
     cudaMemsetAsync(a.work, 0, sizeof(int), s);
     kForces[body][variant]<<<blocks, nt, forces_smem_bytes(body, variant), s>>>(a);
-    if (v.pairs && (a.nodes & N_AGENT) && body == 1)
-        k_forces_fixup<1><<<4, NTG, 0, s>>>(a);
     if (v.pairs && (a.nodes & N_AGENT)) {
         const int gv = variant - 4;                       // the lane-group twin
         int rg = (dev >= 0 && dev < 64) ? g_forces_blocks[dev][body][gv] : 0;
