@@ -292,9 +292,8 @@ int bin_walls(cd_ctx *c) {
 
 // Cell list + staging for the current state (no forces).
 void enqueue_cells(cd_ctx *c, const StepArgs &a) {
-    cudaMemsetAsync(c->count, 0, sizeof(int) * c->ncells, c->stream);
-    cudaMemsetAsync(c->fill, 0, sizeof(int) * c->ncells, c->stream);
-    cudaMemsetAsync(c->vmax, 0, sizeof(unsigned long long) * c->nscen, c->stream);
+    // count, fill and vmax are zero between cell lists (zeroed at creation,
+    // then by k_rank and k_scatter once used)
     cdk::launch_prepare(a, c->stream);
     // dt is computed by the scatter kernel, launched only for agents
     if ((a.nodes & cdk::N_INTEG) && a.n == 0) cdk::launch_dt(a, c->stream);
@@ -623,6 +622,9 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
         cudaMemset(c->err, 0, sizeof(int));
         cudaMemset(c->rng_step, 0, sizeof(unsigned long long));
         cudaMemset(c->wall_start, 0, sizeof(int) * (ncells + 1));
+        cudaMemset(c->count, 0, sizeof(int) * ncells);       // zero between cell lists
+        cudaMemset(c->fill, 0, sizeof(int) * ncells);
+        cudaMemset(c->vmax, 0, sizeof(unsigned long long) * n_scenarios);
         cudaEventCreate(&c->ev0);
         cudaEventCreate(&c->ev1);
         cudaEventCreate(&c->evs0);

@@ -468,8 +468,12 @@ __global__ void k_scan_add(ScanSet S, int n, int nb) {
 
 __global__ void k_scatter(StepArgs a) {
     // the step's dt: k_prepare's max |v| is complete once this kernel runs
-    if (blockIdx.x == 0 && (a.nodes & N_INTEG))
-        for (int sc = threadIdx.x; sc < a.n_scen; sc += blockDim.x) scenario_dt(a, sc);
+    // (then the max is used up: zero for the next cell list)
+    if (blockIdx.x == 0)
+        for (int sc = threadIdx.x; sc < a.n_scen; sc += blockDim.x) {
+            if (a.nodes & N_INTEG) scenario_dt(a, sc);
+            a.vmax[sc] = 0;
+        }
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     int c = a.key[i];
@@ -489,6 +493,11 @@ __global__ void k_rank(StepArgs a) {
     for (int q = b; q < e; ++q) r += (a.perm_unsorted[q] < i);
     a.perm[b + r] = i;
     if (a.slot_of) a.slot_of[i] = b + r;
+    // the cell's count and fill are used up: zero for the next cell list
+    if (p == b) {
+        a.count[c] = 0;
+        a.fill[c] = 0;
+    }
 }
 
 // Extent: distance from the torso centre to the farthest skin point.
@@ -1884,6 +1893,7 @@ __global__ void __launch_bounds__(NTG) k_nl_count(StepArgs a) {
 
 template <int L>
 __global__ void __launch_bounds__(NTG) k_nl_fill(StepArgs a) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.work = 0;   // k_pairs' work counter
     if (a.nl_off[a.n] > a.nl_cap) return;                 // over capacity: fallback
     constexpr unsigned GMASK = (1u << L) - 1u;
     const int lane = threadIdx.x & 31;
@@ -2130,6 +2140,7 @@ __device__ __forceinline__ void gather_agent(const StepArgs &a, const int s, con
 
 template <int BODY>
 __global__ void __launch_bounds__(NTG) k_forces_gather(StepArgs a) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.work = 0;   // k_forces_fallback's work counter
     if ((a.nodes & N_AGENT) && a.nl_off[a.n] > a.nl_cap) return;   // k_forces_fallback's step
     // one lane per slot: the entries of neighbouring lanes are neighbours
     // (launched in one-warp blocks: the float64 epilogue spreads evenly
@@ -2710,7 +2721,6 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
         kNlFill[l]<<<nb, NTG, 0, s>>>(a);
         int rp = (dev >= 0 && dev < 64) ? g_pairs_blocks[dev][body][l] : 0;
         if (rp <= 0) rp = 152;
-        cudaMemsetAsync(a.work, 0, sizeof(int), s);
         // at most one warp per 32 pairs (about 16 pairs per agent): enough blocks
         if (pair_ev) cudaEventRecordWithFlags(pair_ev[0], s, captured ? cudaEventRecordExternal : 0);
         kPairs[body]<<<std::min(nblk((long long)a.n * 16, NTG), rp), NTG, pairs_smem_bytes(body),
@@ -2726,13 +2736,12 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
         nt = 32;
         blocks = nblk(a.n, nt);
     }
-    cudaMemsetAsync(a.work, 0, sizeof(int), s);
+    if (!v.pairs) cudaMemsetAsync(a.work, 0, sizeof(int), s);     // the gather zeroes it itself
     kForces[body][variant]<<<blocks, nt, forces_smem_bytes(body, variant), s>>>(a);
     if (v.pairs && (a.nodes & N_AGENT)) {
         const int gv = variant - 4;                       // the lane-group twin
         int rg = (dev >= 0 && dev < 64) ? g_forces_blocks[dev][body][gv] : 0;
         if (rg <= 0) rg = 152;
-        cudaMemsetAsync(a.work, 0, sizeof(int), s);
         kFallback[body][pair_l_index(v.lanes)]<<<(int)std::min<long long>(
                                                     (threads + NTG - 1) / NTG, rg),
                                                 NTG, forces_smem_bytes(body, gv), s>>>(a);
