@@ -353,6 +353,95 @@ def test_zero_force_torque_signs(oracle, native, move):
     assert (neg & (inter > 0)).any() and (~neg & (inter > 0)).any()
 
 
+def edge_pairs(seed=17):
+    """Isolated ThreeCircle pairs (15 m apart) placed at the edges of the
+    pair kernel's float32 certificates: torso skin distance within 1e-7 ..
+    1e-3 m of 3 (interaction) and of 0 (contact), exactly at them, and
+    coincident centres; moving head-on, grazing (miss distance within 1e-9 m
+    of the torsos' radii sum), receding, together (a = 0), with a relative
+    speed of 1e-150 (a tiny) and of 1e-170 (a underflows to 0), or at random."""
+    from crowddynamics_gb300.simulation.agents import new_agents, shoulders
+    rng = np.random.default_rng(seed)
+    cases = []
+    for target in (3.0, 0.0):
+        for dh in (-1e-3, -1e-5, -1e-7, 0.0, 1e-7, 1e-5, 1e-3):
+            for motion in ('head_on', 'graze', 'receding', 'together', 'tiny', 'underflow',
+                           'random'):
+                cases.append((target + dh, motion))
+    cases += [(None, 'random'), (None, 'head_on')]
+    n = 2 * len(cases)
+    a = new_agents(n, 'three_circle')
+    S._three_circle_bodies(a, rng, n)
+    side = int(np.ceil(np.sqrt(len(cases))))
+    spacing = 15.0
+    for k, (h, motion) in enumerate(cases):
+        A, B = 2 * k, 2 * k + 1
+        th = rng.uniform(0, 2 * np.pi)
+        u = np.array([np.cos(th), np.sin(th)])
+        nrm = np.array([-u[1], u[0]])
+        a['orientation'][A], a['orientation'][B] = th, th + np.pi
+        rsum = a['r_t'][A] + a['r_t'][B]
+        d = 0.0 if h is None else h + rsum
+        pa = np.array([10.0 + spacing * (k % side), 10.0 + spacing * (k // side)])
+        a['position'][A] = pa
+        a['position'][B] = pa + d * u
+        v = rng.normal(0.0, 1.0, 2)
+        if motion == 'head_on':
+            va, vb = 0.8 * u, -0.8 * u
+        elif motion == 'graze':
+            s = min(1.0, (rsum + rng.choice([-1e-9, 1e-9])) / max(d, 1e-9))
+            rel = 1.3 * (np.sqrt(1 - s * s) * u + s * nrm)      # from A towards B, missing by ~rsum
+            va, vb = rel / 2, -rel / 2
+        elif motion == 'receding':
+            va, vb = -0.8 * u, 0.8 * u
+        elif motion == 'together':
+            va, vb = v, v
+        elif motion == 'tiny':
+            va, vb = v, v + 1e-150
+        elif motion == 'underflow':
+            va, vb = v, v + 1e-170
+        else:
+            va, vb = v, rng.normal(0.0, 1.0, 2)
+        a['velocity'][A], a['velocity'][B] = va, vb
+    e0 = rng.normal(0.0, 1.0, (n, 2))
+    a['target_direction'] = e0 / np.hypot(*e0.T)[:, None]
+    a['target_orientation'] = np.arctan2(a['target_direction'][:, 1], a['target_direction'][:, 0])
+    shoulders(a)
+    rows = int(np.ceil(len(cases) / side))
+    bounds = (0.0, 0.0, 20.0 + spacing * side, 20.0 + spacing * rows)
+    return S.Scenario('edge_pairs', a, S.walls_array([]), bounds, 3.6)
+
+
+@pytest.mark.parametrize('variant', [9, 10, 11])
+def test_certificate_edges(oracle, native, variant):
+    """The pair kernel's float32 certificates (distance bounds, pre-selection,
+    no time to collision) at their edges: one full step bit for bit."""
+    scen = edge_pairs()
+    nodes = N.NODE_ALL & ~N.NODE_FLUCTUATION
+    got, _ = device_step(scen, nodes, variant=variant)
+    ref, _ = oracle_step(oracle, scen, nodes, exact=True)
+    assert_identical(got, ref, 'edge pairs')
+
+
+def test_certificate_edges_rollout(oracle, native):
+    """The same pairs over 30 steps (they approach, touch, graze and part)."""
+    scen = edge_pairs(seed=23)
+    nodes = N.NODE_ALL & ~N.NODE_FLUCTUATION
+    b, agents, _ = batch_from_scenarios([scen])
+    b.set_variant(10)
+    ref = scen.agents.copy()
+    grid = oracle_grid(oracle, scen)
+    with oracle.exact_math():
+        for _ in range(30):
+            b.step(nodes)
+            oracle.step(ref, grid, scen.walls, flags=orc_flags(nodes), dt_min=scen.dt_min,
+                        dt_max=scen.dt_max)
+    got = agents.copy()
+    b.download(got)
+    b.close()
+    assert_identical(got, ref, 'edge pairs rollout')
+
+
 def test_large_field_forces(oracle, native):
     """Full-size 100k ThreeCircle step: agent-agent + walls + adjusting vs the
     oracle's agent-parallel restatement."""
