@@ -81,7 +81,7 @@ struct StepArgs {
     double *dt, *time_tot;       // per scenario
     int *err;
     int *work;                   // force-kernel work counter (zeroed per launch)
-    int *fix_count, *fix_list;   // agents the gather leaves to k_forces_fixup
+    int *fix_count, *fix_list;   // agents the gather leaves to k_forces_fallback
     int *slot_of;                // per agent: its cell-sorted slot (k_rank)
     // near lists (compute-once pair pipeline): per cell-sorted slot, the
     // slots of its near candidates in ascending order (= visiting order)
@@ -102,7 +102,7 @@ struct StepArgs {
     int *fs_scan;                // scan scratch
 };
 
-// Pair-result record of one near-list entry: (fx, fy, torque, interacts);
+// Pair-result record of a near-list entry with a force: (fx, fy, torque, -);
 // the adjoint's records (Circular contexts) hold ADJ_RES_D doubles.
 constexpr int RES_D = 4;
 constexpr int ADJ_RES_D = 6;

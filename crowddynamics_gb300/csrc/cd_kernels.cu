@@ -1789,11 +1789,14 @@ __global__ void __launch_bounds__(NTG) k_forces_group(StepArgs a) {
 //     cull, symmetric) in ascending slot order, which is its visiting order;
 //   k_pairs: for every entry with a later slot, both sides of the pair, the
 //     first side into the entry, the second into the partner's entry for
-//     this agent (binary search in the partner's earlier-slot part);
+//     this agent (found in the partner's earlier-slot part); a kind byte
+//     per entry, a 32-byte record only for a force;
 //   k_forces_gather: per agent, the entries' forces added in list order,
-//     then walls and integration.
+//     then walls and integration;
+//   k_forces_fallback: the agents the gather left (a signed-zero torque
+//     decides), evaluated again with exact signs.
 // When the entries exceed the allocated capacity the pair kernels do
-// nothing and k_forces_gather runs the lane-group path instead; nl_off[n]
+// nothing and k_forces_fallback runs the lane-group path instead; nl_off[n]
 // tells the host how much to allocate.
 
 // Agent s's candidate runs, one per dx in -1, 0, 1 (empty where off the grid).
@@ -2011,7 +2014,7 @@ __device__ __forceinline__ void put_pair(const StepArgs &a, int e, int res, doub
     if (res == RES_FORCE) {
         kind = KIND_FORCE;
         double4_32a v;
-        v.x = fx; v.y = fy; v.z = tq; v.w = 0.0;
+        v.x = fx; v.y = fy; v.z = tq; v.w = 0.0;   // w unused (32-byte records)
         *reinterpret_cast<double4_32a *>(a.nl_res + (size_t)e * RES_D) = v;
     } else if (res == RES_ZERO) {
         kind = KIND_ZERO;
