@@ -1838,15 +1838,31 @@ __device__ __forceinline__ bool social_guess(float4 me, float4 o) {
     return x2 < sight * sight && disc > 0.0f && (b > 0.0f || c < 0.0f);
 }
 
-// Near lists in two passes over the same candidate chunks (L consecutive
-// candidates of one run per chunk, one lane each).  k_nl_count evaluates the
-// bound check and the social-force guess, counts, and keeps each chunk's two
-// ballots (near bits low, guessed bits high) in the agent's mask row;
-// k_nl_fill then places the entries from the masks alone.  An agent with more
-// chunks than a row holds is evaluated again by the fill.
+// Near lists in two passes over the same candidate chunks (CW consecutive
+// candidates of one run per chunk: C per lane, candidate base + c L + r on
+// lane r).  k_nl_count evaluates the bound check and the social-force guess,
+// counts, and keeps each chunk's bits (near low 16, guessed high 16; bit j is
+// candidate base + j) in the agent's mask row; k_nl_fill then places the
+// entries from the masks alone.  An agent with more chunks than a row holds is
+// evaluated again by the fill.
+template <int L> struct NlChunk {
+    static constexpr int C = L <= 8 ? 2 : 1;          // candidates per lane and chunk
+    static constexpr int CW = C * L;                   // candidates per chunk, <= 16
+    static constexpr unsigned CMASK = (1u << CW) - 1u;
+};
+
+// Bits of a chunk's candidates that follow slot s (bit j: candidate base + j).
+template <int L>
+__device__ __forceinline__ unsigned later_bits(int s, int base) {
+    const int k0 = s - base + 1;
+    return k0 <= 0 ? NlChunk<L>::CMASK
+                   : (k0 >= NlChunk<L>::CW ? 0u : (NlChunk<L>::CMASK & ~((1u << k0) - 1u)));
+}
+
 template <int L>
 __global__ void __launch_bounds__(NTG) k_nl_count(StepArgs a) {
-    static_assert(L <= 16, "two ballots per 32-bit mask word");
+    static_assert(NlChunk<L>::CW <= 16, "two 16-bit masks per 32-bit word");
+    constexpr int C = NlChunk<L>::C, CW = NlChunk<L>::CW;
     constexpr unsigned GMASK = (1u << L) - 1u;
     const int lane = threadIdx.x & 31;
     const int r = lane & (L - 1), g0 = lane & ~(L - 1);
@@ -1864,22 +1880,24 @@ __global__ void __launch_bounds__(NTG) k_nl_count(StepArgs a) {
     int cnt = 0, fwd = 0, soc = 0, ch = 0;
 #pragma unroll
     for (int d = 0; d < 3; ++d)
-        for (int base = rb[d]; base < re[d]; base += L) {
-            const int t = base + r;
-            bool near = false, guess = false;
-            if (t < re[d] && t != s) {
-                const float4 o = __ldg(&a.cull[t]);
-                near = !pair_far(me, o);
-                if (near && t > s) guess = social_guess(me, o);
+        for (int base = rb[d]; base < re[d]; base += CW) {
+            unsigned nb = 0, sb = 0;
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                const int t = base + c * L + r;
+                bool near = false, guess = false;
+                if (t < re[d] && t != s) {
+                    const float4 o = __ldg(&a.cull[t]);
+                    near = !pair_far(me, o);
+                    if (near && t > s) guess = social_guess(me, o);
+                }
+                nb |= ((__ballot_sync(gm, near) >> g0) & GMASK) << (c * L);
+                sb |= ((__ballot_sync(gm, guess) >> g0) & GMASK) << (c * L);
             }
-            const unsigned nb = (__ballot_sync(gm, near) >> g0) & GMASK;
-            const unsigned sb = (__ballot_sync(gm, guess) >> g0) & GMASK;
-            const int k0 = s - base + 1;                  // lanes r >= k0 have t > s
-            const unsigned fl = k0 <= 0 ? GMASK : (k0 >= L ? 0u : (GMASK & ~((1u << k0) - 1u)));
             if (r == 0 && ch < NL_MASK_CHUNKS) row[ch] = nb | (sb << 16);
             ++ch;
             cnt += __popc(nb);
-            fwd += __popc(nb & fl);
+            fwd += __popc(nb & later_bits<L>(s, base));
             soc += __popc(sb);
         }
     __syncwarp(gm);
@@ -1917,24 +1935,28 @@ __global__ void __launch_bounds__(NTG) k_nl_fill(StepArgs a) {
     int p1 = a.fs_off[a.n] + (a.fw_off[s] - a.fs_off[s]);
     const unsigned lower = (1u << r) - 1u;
     if (a.nl_nch[s] <= NL_MASK_CHUNKS) {
+        constexpr int C = NlChunk<L>::C, CW = NlChunk<L>::CW;
         const unsigned *mrow = a.nl_mask + (size_t)s * NL_MASK_CHUNKS;
         int ch = 0;
 #pragma unroll
         for (int d = 0; d < 3; ++d)
-            for (int base = rb[d]; base < re[d]; base += L) {
+            for (int base = rb[d]; base < re[d]; base += CW) {
                 const unsigned m = mrow[ch++];
                 const unsigned nb = m & 0xffffu, sb = m >> 16;
-                const int k0 = s - base + 1;              // lanes r >= k0 have t > s
-                const unsigned fl = k0 <= 0 ? GMASK : (k0 >= L ? 0u : (GMASK & ~((1u << k0) - 1u)));
-                const unsigned fb = nb & fl;
-                const int t = base + r;
-                if ((nb >> r) & 1u) {
-                    const int e = pos + __popc(nb & lower);
-                    a.nl_idx[e] = t;
-                    if (t > s)
-                        a.fw_pairs[((sb >> r) & 1u) ? p0 + __popc(sb & lower)
-                                                    : p1 + __popc(fb & ~sb & lower)] =
-                            make_int2(s, e);
+                const unsigned fb = nb & later_bits<L>(s, base);
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    const int j = c * L + r;
+                    const unsigned below = (1u << j) - 1u;
+                    const int t = base + j;
+                    if ((nb >> j) & 1u) {
+                        const int e = pos + __popc(nb & below);
+                        a.nl_idx[e] = t;
+                        if (t > s)
+                            a.fw_pairs[((sb >> j) & 1u) ? p0 + __popc(sb & below)
+                                                        : p1 + __popc(fb & ~sb & below)] =
+                                make_int2(s, e);
+                    }
                 }
                 pos += __popc(nb);
                 p0 += __popc(sb);
