@@ -563,14 +563,20 @@ __global__ void k_gather(StepArgs a) {
         cdm_sincos(phi, &sn, &cs);
         p[8] = make_double2(c[DAMP][i], sn);
         p[9] = make_double2(cs, 0.0);
-        double e = extent_tc(x, y, c[XLS][i], c[YLS][i], c[XRS][i], c[YRS][i], c[RT][i], c[RS][i]);
         float xh = (float)x, yh = (float)y;
-        a.cull[s] = make_float4(xh, yh, up_f(e), pack_velocity(c[VX][i], c[VY][i]));
         // position = float hi + float lo; shoulder centres relative to the torso
-        a.stage_f[2 * s] = make_float4((float)(x - (double)xh), (float)(y - (double)yh),
-                                       (float)c[RT][i], (float)c[RS][i]);
-        a.stage_f[2 * s + 1] = make_float4((float)(c[XLS][i] - x), (float)(c[YLS][i] - y),
-                                           (float)(c[XRS][i] - x), (float)(c[YRS][i] - y));
+        const float oxl = (float)(c[XLS][i] - x), oyl = (float)(c[YLS][i] - y);
+        const float oxr = (float)(c[XRS][i] - x), oyr = (float)(c[YRS][i] - y);
+        const float rtf = (float)c[RT][i], rsf = (float)c[RS][i];
+        a.stage_f[2 * s] = make_float4((float)(x - (double)xh), (float)(y - (double)yh), rtf, rsf);
+        a.stage_f[2 * s + 1] = make_float4(oxl, oyl, oxr, oyr);
+        // extent (extent_tc) in float32 from the same offsets: its error is
+        // below 1e-6 relative, the 1e-5 added makes it an upper bound, which
+        // is all the pre-check records need
+        const float ef = fmaxf(rtf, fmaxf(sqrtf(oxl * oxl + oyl * oyl) + rsf,
+                                          sqrtf(oxr * oxr + oyr * oyr) + rsf));
+        a.cull[s] = make_float4(xh, yh, ef + ef * 1e-5f + 1e-5f,
+                                pack_velocity(c[VX][i], c[VY][i]));
     }
 }
 
