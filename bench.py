@@ -85,6 +85,22 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x, dist=None, device='cuda'):
+    """The largest `x` over all ranks (the slowest replica's time); `x` itself
+    without a process group."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world_size, agents, steps, seconds):
+    """agent-steps/s of all replicas together, timed by the slowest."""
+    return world_size * agents * steps / seconds
+
+
 def workload(n_agents):
     from crowddynamics_gb300 import scenarios as S
     if n_agents == 100_000:
@@ -295,12 +311,8 @@ def run_ours(args, ws, rank, local):
     barrier()
     kt = b.kernel_time()
     b.set_timing(False)
-    run_ms = kt['run_ms']
-    if dist is not None:
-        t = torch.tensor([run_ms], device='cuda', dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        run_ms = float(t.item())
-    value = ws * n * args.steps / (run_ms / 1e3)
+    run_ms = max_over_ranks(kt['run_ms'], dist)
+    value = whole_job_rate(ws, n, args.steps, run_ms / 1e3)
     force_ms = kt['force_ms'] / max(kt['force_launches'], 1)
     pair_ms = kt['pair_ms'] / max(kt['pair_launches'], 1) if kt['pair_launches'] else None
     counts1 = b.pair_counts()
@@ -333,12 +345,8 @@ def run_ours(args, ws, rank, local):
             b.upload(rec)
             b.run(1, nodes)
             b.download(rec)
-        e2e_s = time.perf_counter() - t0
-        if dist is not None:
-            t = torch.tensor([e2e_s], device='cuda', dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        trials.append(ws * n * args.steps / e2e_s)
+        e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
+        trials.append(whole_job_rate(ws, n, args.steps, e2e_s))
     e2e = sorted(trials)[1]
 
     # DRAM bytes per launch of the dominant kernel, from the committed summary
