@@ -442,6 +442,50 @@ def test_certificate_edges_rollout(oracle, native):
     assert_identical(got, ref, 'edge pairs rollout')
 
 
+def crowded(seed, speed=1.0):
+    """A dense ThreeCircle field (2.5 agents/m^2) with positions jittered
+    into overlaps (contacts) and random velocities."""
+    from crowddynamics_gb300.simulation.agents import shoulders
+    scen = S.large_field(n=4000, size=40.0, n_walls=10, seed=seed)
+    rng = np.random.default_rng(seed)
+    a = scen.agents
+    a['position'] += rng.normal(0.0, 0.25, (len(a), 2))
+    a['velocity'] = rng.normal(0.0, speed, (len(a), 2))
+    shoulders(a)
+    return scen
+
+
+@pytest.mark.parametrize('case', [('room', 1, 0.1), ('room', 2, 1.0), ('room', 3, 3.0),
+                                  ('crowded', 4, 0.3), ('crowded', 5, 1.0), ('crowded', 6, 2.5)])
+def test_pair_pipeline_random_sweep(oracle, native, case):
+    """Random states for the pair pipeline's float32 decisions: moving rooms at
+    several speed scales and dense, overlapping fields; three steps bit for bit."""
+    kind, seed, speed = case
+    if kind == 'room':
+        scen = S.room(n=1500, size=25.0, seed=seed)
+        scen.agents['velocity'] = np.random.default_rng(seed).normal(0.0, speed,
+                                                                      (len(scen.agents), 2))
+    else:
+        scen = crowded(seed, speed)
+    nodes = N.NODE_ALL & ~N.NODE_FLUCTUATION
+    b, agents, _ = batch_from_scenarios([scen])
+    b.set_variant(10)
+    b.run(3, nodes)
+    got = agents.copy()
+    b.download(got)
+    counts = b.pair_counts()
+    b.close()
+    ref = scen.agents.copy()
+    grid = oracle_grid(oracle, scen)
+    with oracle.exact_math():
+        for _ in range(3):
+            oracle.step(ref, grid, scen.walls, flags=orc_flags(nodes), dt_min=scen.dt_min,
+                        dt_max=scen.dt_max)
+    assert_identical(got, ref, '%s seed %d' % (kind, seed))
+    if kind == 'crowded':
+        assert counts[:, 3].sum() > 0                  # contacts occur
+
+
 def test_large_field_forces(oracle, native):
     """Full-size 100k ThreeCircle step: agent-agent + walls + adjusting vs the
     oracle's agent-parallel restatement."""
