@@ -1190,6 +1190,7 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
     }
     unsigned candmask = 0;
     int cnt = 0;
+    bool least_rule = false;             // select the least positive root (first root > 0)
     if (soc) {
         const float af = vxf * vxf + vyf * vyf;
         const float e0 = 1e-6f * (1.f + fabsf(dxt) + fabsf(dyt) + fabsf(mox[1]) + fabsf(moy[1]) +
@@ -1209,6 +1210,7 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
         const float bbe = fabsf(be) + mbe;
         const bool apart = ce - mce > 0.f && (be + mbe <= 0.f || bbe * bbe < 0.99f * af * (ce - mce));
         int first = apart ? 1 : -1;                      // class of the first sub-pair with a root
+        float min_hi = INFINITY;                         // least upper bound of a certain tau > 0
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
             if (apart) break;
@@ -1223,24 +1225,57 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
             const float m = 1e-5f * af * (1.f + x2 + rt * rt) + 1e-6f * (bf * bf + fabsf(acf));
             if (!(discf < -m)) {
                 candmask |= 1u << k;
+                const float mb = 4.f * e0 * (fabsf(vxf) + fabsf(vyf)) +
+                                 1e-6f * (fabsf(dx * vxf) + fabsf(dy * vyf));
+                const float mc = 8.f * e0 * (fabsf(dx) + fabsf(dy) + rt) + 1e-6f * (x2 + rt * rt);
+                const float bb = (fabsf(bf) + mb) * (fabsf(bf) + mb);
+                const bool pos = discf > m && bf > mb && cf > mc &&
+                                 0.99f * af * (cf - mc) > 1e-9f * bb;
                 if (first < 0) {
                     // 0: decide in float64; 1: tau < 0 certain; 2: tau > 0 certain
                     first = 0;
                     if (discf > m) {
-                        const float mb = 4.f * e0 * (fabsf(vxf) + fabsf(vyf)) +
-                                         1e-6f * (fabsf(dx * vxf) + fabsf(dy * vyf));
-                        const float mc = 8.f * e0 * (fabsf(dx) + fabsf(dy) + rt) +
-                                         1e-6f * (x2 + rt * rt);
-                        const float bb = (fabsf(bf) + mb) * (fabsf(bf) + mb);
                         if (bf < -mb) first = 1;
                         else if (cf < -mc && 0.99f * af * (-cf - mc) > 1e-9f * bb) first = 1;
-                        else if (bf > mb && cf > mc && 0.99f * af * (cf - mc) > 1e-9f * bb)
-                            first = 2;
+                        else if (pos) first = 2;
                     }
                 }
+                // tau = c / (b + sqrt(D)) (b > 0): an upper bound from the
+                // margins of b, c and D (and 1e-5 for every rounding)
+                if (pos)
+                    min_hi = fminf(min_hi, (cf + mc) / ((bf - mb) + sqrtf(discf - m)) * 1.00001f);
             }
         }
         if (first == 1) candmask = 0;                     // no positive tau: no force
+        if (first == 2 && (candmask & (candmask - 1u))) {
+            // The first root is positive: the selected tau is the least
+            // positive root (the earliest of equals).  A root certainly
+            // negative, or whose lower bound exceeds another root's upper
+            // bound, is never selected: not evaluated in float64.
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                if (!(candmask & (1u << k))) continue;
+                const int i = k / 3, j = k % 3;
+                const float dx = (dxt + mox[i]) - oox[j], dy = (dyt + moy[i]) - ooy[j];
+                const float rt = mr[i] + orr[j];
+                const float bf = -(dx * vxf + dy * vyf);
+                const float x2 = dx * dx + dy * dy;
+                const float cf = x2 - rt * rt;
+                const float acf = af * cf;
+                const float discf = bf * bf - acf;
+                const float m = 1e-5f * af * (1.f + x2 + rt * rt) + 1e-6f * (bf * bf + fabsf(acf));
+                if (!(discf > m)) continue;
+                const float mb = 4.f * e0 * (fabsf(vxf) + fabsf(vyf)) +
+                                 1e-6f * (fabsf(dx * vxf) + fabsf(dy * vyf));
+                const float mc = 8.f * e0 * (fabsf(dx) + fabsf(dy) + rt) + 1e-6f * (x2 + rt * rt);
+                const float bb = (fabsf(bf) + mb) * (fabsf(bf) + mb);
+                bool drop = bf < -mb || (cf < -mc && 0.99f * af * (-cf - mc) > 1e-9f * bb);
+                if (!drop && bf > mb && cf > mc && 0.99f * af * (cf - mc) > 1e-9f * bb)
+                    drop = (cf - mc) / ((bf + mb) + sqrtf(discf + m)) * 0.99999f > min_hi;
+                if (drop) candmask &= ~(1u << k);
+            }
+        }
+        least_rule = first == 2;
     }
     if (candmask) {
         if (!have_av) {
@@ -1317,7 +1352,10 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
                     const double dk = q.disc[slot];
                     if (dk > 0) {
                         const double tau_new = q.tau[slot];
-                        if (isnan(tau) || (0 < tau_new && tau_new < tau)) {
+                        const bool take =
+                            least_rule ? (0 < tau_new && (isnan(tau) || tau_new < tau))
+                                       : (isnan(tau) || (0 < tau_new && tau_new < tau));
+                        if (take) {
                             k_sel = k; tau = tau_new; b_min = q.b[slot]; d_min = dk;
                         }
                     }
