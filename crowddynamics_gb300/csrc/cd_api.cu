@@ -28,6 +28,9 @@ struct cd_ctx {
     std::vector<ScenDev> scen_dev;
     std::vector<int> scen_of_host;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;              // beside the near-list build
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    double *pro = nullptr;
     int device = 0;
 
     double *colbuf = nullptr;
@@ -173,6 +176,7 @@ StepArgs args_of(cd_ctx *c, int nodes) {
     a.fix_count = c->fix_count;
     a.fix_list = c->fix_list;
     a.slot_of = c->slot_of;
+    a.pro = c->pro;
     a.nl_cap = (int)c->nl_cap;
     a.nl_scan = c->nl_scan;
     a.fw_cnt = c->fw_cnt;
@@ -205,7 +209,7 @@ void release(cd_ctx *c) {
                     c->fw_pairs, c->ext, c->max_partial, c->tgt, c->navmap, c->rng_step,
                     c->states, c->herd, c->scen_h, c->counters, c->reached, c->polys,
                     c->poly_off, c->fs_cnt, c->fs_off, c->fs_scan, c->nl_mask, c->nl_nch,
-                    c->fix_count, c->fix_list, c->slot_of};
+                    c->fix_count, c->fix_list, c->slot_of, c->pro};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -221,6 +225,9 @@ void release(cd_ctx *c) {
     if (c->ext_host) cudaFreeHost(c->ext_host);
     if (c->status_host) cudaFreeHost(c->status_host);
     if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->stream2) cudaStreamDestroy(c->stream2);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
 }
 
 // Flat cell range of a coordinate interval along one axis (clamped).
@@ -312,7 +319,9 @@ void enqueue_step(cd_ctx *c, int nodes, bool timed, bool captured = false) {
     enqueue_cells(c, a);
     if (timed) cudaEventRecord(c->ev0, c->stream);
     if (captured) cudaEventRecordWithFlags(c->ev0, c->stream, cudaEventRecordExternal);
-    cdk::launch_forces(a, c->stream, c->variant, (timed || captured) ? c->evp : nullptr, captured);
+    const cdk::Fork fork{c->stream2, c->ev_fork, c->ev_join};
+    cdk::launch_forces(a, c->stream, c->variant, (timed || captured) ? c->evp : nullptr, captured,
+                       &fork);
     if (timed) cudaEventRecord(c->ev1, c->stream);
     if (captured) cudaEventRecordWithFlags(c->ev1, c->stream, cudaEventRecordExternal);
     if (timed) cudaEventRecord(c->evs1, c->stream);
@@ -322,6 +331,7 @@ int64_t kernels_per_step(const cd_ctx *c, int nodes) {
     if (c->n == 0) return (nodes & CD_NODE_INTEGRATE) ? 1 : 0;
     int64_t k = 5;                                      // prepare scatter(+dt) rank gather forces
     k += cdk::scan_launches_single((int)c->ncells);
+    if (cdk::variant_pairs(c->variant) && c->nl_cnt) k += 1;     // prologue
     if (cdk::variant_pairs(c->variant) && (nodes & CD_NODE_AGENT_AGENT) && c->nl_cnt)
         k += 4 + (cdk::scan_scratch_ints((int)c->n) > 1 ? 3 : 1);   // count fill pairs fallback + scans
     return k;
@@ -558,7 +568,10 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     if (int e = cdk::init_kernels())
         rc = fail(c, CD_ERR_CUDA, std::string("kernel attributes: ") +
                                      cudaGetErrorString((cudaError_t)e));
-    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess)
         rc = fail(c, CD_ERR_CUDA, "cudaStreamCreate failed");
     const int64_t npad = std::max<int64_t>(n, 1);
     if (rc == CD_OK && step(dalloc(c, &c->colbuf, npad * cdk::NCOL)))
@@ -604,6 +617,7 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->fix_count, 1));
     step(dalloc(c, &c->fix_list, n));
     step(dalloc(c, &c->slot_of, n));
+    step(dalloc(c, &c->pro, 4 * (int64_t)n));
     step(dalloc(c, &c->nl_mask, (int64_t)n * cdk::NL_MASK_CHUNKS));
     step(dalloc(c, &c->nl_nch, n + 1));
     step(dalloc(c, &c->nl_scan, cdk::scan_scratch_ints((int)npad)));

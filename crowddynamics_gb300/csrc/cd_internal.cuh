@@ -83,6 +83,7 @@ struct StepArgs {
     int *work;                   // force-kernel work counter (zeroed per launch)
     int *fix_count, *fix_list;   // agents the gather leaves to k_forces_fallback
     int *slot_of;                // per agent: its cell-sorted slot (k_rank)
+    double *pro;                 // per agent: prologue force, torque and phi0 (4 doubles)
     // near lists (compute-once pair pipeline): per cell-sorted slot, the
     // slots of its near candidates in ascending order (= visiting order)
     int *nl_cnt;                 // n + 1 counts (scan input)
@@ -192,10 +193,14 @@ int default_variant(long long n_agents);
 int default_group_variant(long long n_agents);
 int variant_threads(int variant);
 int variant_staged(int variant);
+// A second stream for work that runs beside the near-list build (fork after
+// the work already on the main stream, join before the gather).
+struct Fork { cudaStream_t s2; cudaEvent_t fork, join; };
 // The agent-force stage; with `pair_ev`, events recorded around the pair
 // kernel of the pair pipeline (as external event-record nodes if `captured`).
 void launch_forces(const StepArgs &a, cudaStream_t s, int variant,
-                   const cudaEvent_t *pair_ev = nullptr, bool captured = false);
+                   const cudaEvent_t *pair_ev = nullptr, bool captured = false,
+                   const Fork *fork = nullptr);
 // Near-list counts and their scan (nl_off) for the state staged in `a`.
 void launch_near_count(const StepArgs &a, cudaStream_t s, int variant);
 // Near lists (counts, scans, fill; 8 lanes per agent) for the state staged in `a`.

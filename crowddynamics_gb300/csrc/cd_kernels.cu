@@ -2172,6 +2172,21 @@ __device__ __noinline__ double tc_zero_force_torque(const StepArgs &a, int s, in
 // then leaves the agent (writing nothing) to the next kernel
 // (k_forces_fallback, which otherwise has nothing to do), which runs it again
 // with EXACT, evaluating those signs.
+// The per-agent terms before agent-agent (navigation, fluctuation,
+// orientation, adjusting) of every agent, one lane per agent, for the gather:
+// they do not depend on the pairs, so they run beside the near-list build
+// (which leaves the float64 pipe idle).
+template <int BODY>
+__global__ void __launch_bounds__(128) k_prologue(StepArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    double fx, fy, tq, phi0;
+    agent_prologue<BODY>(a, i, fx, fy, tq, phi0);
+    double4_32a v;
+    v.x = fx; v.y = fy; v.z = tq; v.w = phi0;
+    *reinterpret_cast<double4_32a *>(a.pro + 4 * (size_t)i) = v;
+}
+
 template <int BODY, bool EXACT>
 __device__ __forceinline__ void gather_agent(const StepArgs &a, const int s, const int i) {
     const int sid = a.scen_of[i];
@@ -2179,7 +2194,12 @@ __device__ __forceinline__ void gather_agent(const StepArgs &a, const int s, con
     const float4 me = a.cull[s];
     const int my_cell = a.key[i];
     double fx, fy, tq, phi0;
-    agent_prologue<BODY>(a, i, fx, fy, tq, phi0);
+    if (a.pro) {                                   // k_prologue's terms
+        const double4_32a v = *reinterpret_cast<const double4_32a *>(a.pro + 4 * (size_t)i);
+        fx = v.x; fy = v.y; tq = v.z; phi0 = v.w;
+    } else {
+        agent_prologue<BODY>(a, i, fx, fy, tq, phi0);
+    }
     if (a.nodes & N_AGENT) {
         const double4_32a *res = reinterpret_cast<const double4_32a *>(a.nl_res);
         const int o1 = a.nl_off[s + 1];
@@ -2773,7 +2793,7 @@ int init_kernels() {
 }
 
 void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEvent_t *pair_ev,
-                   bool captured) {
+                   bool captured, const Fork *fork) {
     if (a.n <= 0) return;
     if (variant < 0 || variant >= N_VARIANTS) variant = 0;
     // the pair pipeline needs the near-list buffers: otherwise its lane-group twin
@@ -2782,6 +2802,20 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
     int dev = 0;
     cudaGetDevice(&dev);
     const int body = a.body ? 1 : 0;
+    // the gather takes the prologue from k_prologue, on the second stream
+    // beside the near lists when there is one
+    const bool pro = v.pairs && a.pro;
+    if (pro) {
+        cudaStream_t sp = s;
+        if (fork) {
+            cudaEventRecord(fork->fork, s);
+            cudaStreamWaitEvent(fork->s2, fork->fork, 0);
+            sp = fork->s2;
+        }
+        if (body) k_prologue<1><<<nblk(a.n, 128), 128, 0, sp>>>(a);
+        else k_prologue<0><<<nblk(a.n, 128), 128, 0, sp>>>(a);
+        if (fork) cudaEventRecord(fork->join, fork->s2);
+    }
     if (v.pairs && (a.nodes & N_AGENT)) {
         const int l = pair_l_index(v.lanes);
         const int nb = nblk((long long)a.n * v.lanes, NTG);
@@ -2806,6 +2840,7 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
         blocks = nblk(a.n, nt);
     }
     if (!v.pairs) cudaMemsetAsync(a.work, 0, sizeof(int), s);     // the gather zeroes it itself
+    if (pro && fork) cudaStreamWaitEvent(s, fork->join, 0);
     kForces[body][variant]<<<blocks, nt, forces_smem_bytes(body, variant), s>>>(a);
     if (v.pairs && (a.nodes & N_AGENT)) {
         const int gv = variant - 4;                       // the lane-group twin
