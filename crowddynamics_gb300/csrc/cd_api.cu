@@ -29,7 +29,7 @@ struct cd_ctx {
     std::vector<int> scen_of_host;
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;              // beside the near-list build
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join_stage = nullptr;
     double *pro = nullptr;
     int device = 0;
 
@@ -228,6 +228,7 @@ void release(cd_ctx *c) {
     if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->ev_join_stage) cudaEventDestroy(c->ev_join_stage);
 }
 
 // Flat cell range of a coordinate interval along one axis (clamped).
@@ -298,7 +299,9 @@ int bin_walls(cd_ctx *c) {
 }
 
 // Cell list + staging for the current state (no forces).
-void enqueue_cells(cd_ctx *c, const StepArgs &a) {
+// `defer_stage`: only the pre-check records here; the force stage writes the
+// float64 staged records beside the near-list build.
+void enqueue_cells(cd_ctx *c, const StepArgs &a, bool defer_stage = false) {
     // count, fill and vmax are zero between cell lists (zeroed at creation,
     // then by k_rank and k_scatter once used)
     cdk::launch_prepare(a, c->stream);
@@ -306,7 +309,7 @@ void enqueue_cells(cd_ctx *c, const StepArgs &a) {
     if ((a.nodes & cdk::N_INTEG) && a.n == 0) cdk::launch_dt(a, c->stream);
     cdk::launch_scan(c->count, c->start, (int)c->ncells, c->scan_scratch, c->stream);
     cdk::launch_scatter(a, c->stream);
-    cdk::launch_gather(a, c->stream);
+    cdk::launch_gather(a, c->stream, defer_stage ? 1 : 0);
 }
 
 // One step on the context stream.  `timed`: record the step and force-kernel
@@ -315,13 +318,15 @@ void enqueue_cells(cd_ctx *c, const StepArgs &a) {
 // (a plain cudaEventRecord under capture only marks a capture dependency).
 void enqueue_step(cd_ctx *c, int nodes, bool timed, bool captured = false) {
     StepArgs a = args_of(c, nodes);
+    // the pair pipeline writes the float64 staged records beside the near lists
+    const bool defer = cdk::variant_pairs(c->variant) && c->nl_cnt;
     if (timed) cudaEventRecord(c->evs0, c->stream);
-    enqueue_cells(c, a);
+    enqueue_cells(c, a, defer);
     if (timed) cudaEventRecord(c->ev0, c->stream);
     if (captured) cudaEventRecordWithFlags(c->ev0, c->stream, cudaEventRecordExternal);
-    const cdk::Fork fork{c->stream2, c->ev_fork, c->ev_join};
+    const cdk::Fork fork{c->stream2, c->ev_fork, c->ev_join, c->ev_join_stage};
     cdk::launch_forces(a, c->stream, c->variant, (timed || captured) ? c->evp : nullptr, captured,
-                       &fork);
+                       &fork, defer);
     if (timed) cudaEventRecord(c->ev1, c->stream);
     if (captured) cudaEventRecordWithFlags(c->ev1, c->stream, cudaEventRecordExternal);
     if (timed) cudaEventRecord(c->evs1, c->stream);
@@ -331,7 +336,7 @@ int64_t kernels_per_step(const cd_ctx *c, int nodes) {
     if (c->n == 0) return (nodes & CD_NODE_INTEGRATE) ? 1 : 0;
     int64_t k = 5;                                      // prepare scatter(+dt) rank gather forces
     k += cdk::scan_launches_single((int)c->ncells);
-    if (cdk::variant_pairs(c->variant) && c->nl_cnt) k += 1;     // prologue
+    if (cdk::variant_pairs(c->variant) && c->nl_cnt) k += 2;     // prologue, float64 staging
     if (cdk::variant_pairs(c->variant) && (nodes & CD_NODE_AGENT_AGENT) && c->nl_cnt)
         k += 4 + (cdk::scan_scratch_ints((int)c->n) > 1 ? 3 : 1);   // count fill pairs fallback + scans
     return k;
@@ -571,7 +576,8 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_join_stage, cudaEventDisableTiming) != cudaSuccess)
         rc = fail(c, CD_ERR_CUDA, "cudaStreamCreate failed");
     const int64_t npad = std::max<int64_t>(n, 1);
     if (rc == CD_OK && step(dalloc(c, &c->colbuf, npad * cdk::NCOL)))

@@ -185,7 +185,9 @@ int scan_scratch_ints(int n);
 void launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s);
 int scan_launches_single(int n);          // kernels launch_scan uses for n elements
 void launch_scatter(const StepArgs &a, cudaStream_t s);
-void launch_gather(const StepArgs &a, cudaStream_t s);
+// Staged records of the cell-sorted agents: part 0 all, 1 the float32
+// pre-check records, 2 the float64 records.
+void launch_gather(const StepArgs &a, cudaStream_t s, int part = 0);
 constexpr int N_VARIANTS = 12;      // launch variants of the force kernel
 bool variant_pairs(int variant);
 int variant_lanes(int variant);
@@ -195,12 +197,12 @@ int variant_threads(int variant);
 int variant_staged(int variant);
 // A second stream for work that runs beside the near-list build (fork after
 // the work already on the main stream, join before the gather).
-struct Fork { cudaStream_t s2; cudaEvent_t fork, join; };
+struct Fork { cudaStream_t s2; cudaEvent_t fork, join, join_stage; };
 // The agent-force stage; with `pair_ev`, events recorded around the pair
 // kernel of the pair pipeline (as external event-record nodes if `captured`).
 void launch_forces(const StepArgs &a, cudaStream_t s, int variant,
                    const cudaEvent_t *pair_ev = nullptr, bool captured = false,
-                   const Fork *fork = nullptr);
+                   const Fork *fork = nullptr, bool stage_deferred = false);
 // Near-list counts and their scan (nl_off) for the state staged in `a`.
 void launch_near_count(const StepArgs &a, cudaStream_t s, int variant);
 // Near lists (counts, scans, fill; 8 lanes per agent) for the state staged in `a`.

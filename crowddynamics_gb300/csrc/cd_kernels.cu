@@ -528,8 +528,10 @@ __device__ __forceinline__ float up_f(double v) {
 }
 
 // One lane per agent where the slots are known (column reads coalesced, the
-// staged records written whole), else one lane per slot.
-__global__ void k_gather(StepArgs a) {
+// staged records written whole), else one lane per slot.  `part`: 0 all
+// records; 1 the float32 pre-check records only (all the near-list build
+// reads); 2 the float64 staged records only.
+__global__ void k_gather(StepArgs a, int part) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.n) return;
     int s, i;
@@ -537,32 +539,36 @@ __global__ void k_gather(StepArgs a) {
     else { s = t; i = a.perm[t]; }
     double *const *c = a.col;
     if (a.body == 0) {
-        double2 *p = a.stage + (size_t)s * STAGE_Q_CIRC;
-        p[0] = make_double2(c[X][i], c[Y][i]);
-        p[1] = make_double2(c[VX][i], c[VY][i]);
-        p[2] = make_double2(c[R][i], c[MASS][i]);
-        p[3] = make_double2(c[K_SOC][i], c[TAU0][i]);
-        p[4] = make_double2(c[MU][i], c[KAPPA][i]);
-        p[5] = make_double2(c[DAMP][i], 0.0);
-        double e = c[R][i];
-        a.cull[s] = make_float4((float)c[X][i], (float)c[Y][i], up_f(e),
-                                pack_velocity(c[VX][i], c[VY][i]));
+        if (part != 1) {
+            double2 *p = a.stage + (size_t)s * STAGE_Q_CIRC;
+            p[0] = make_double2(c[X][i], c[Y][i]);
+            p[1] = make_double2(c[VX][i], c[VY][i]);
+            p[2] = make_double2(c[R][i], c[MASS][i]);
+            p[3] = make_double2(c[K_SOC][i], c[TAU0][i]);
+            p[4] = make_double2(c[MU][i], c[KAPPA][i]);
+            p[5] = make_double2(c[DAMP][i], 0.0);
+        }
+        if (part != 2)
+            a.cull[s] = make_float4((float)c[X][i], (float)c[Y][i], up_f(c[R][i]),
+                                    pack_velocity(c[VX][i], c[VY][i]));
     } else {
-        double2 *p = a.stage + (size_t)s * STAGE_Q_TC;
         double x = c[X][i], y = c[Y][i];
-        double phi = c[PHI][i];
-        p[0] = make_double2(x, y);
-        p[1] = make_double2(c[XLS][i], c[YLS][i]);
-        p[2] = make_double2(c[XRS][i], c[YRS][i]);
-        p[3] = make_double2(c[VX][i], c[VY][i]);
-        p[4] = make_double2(c[RT][i], c[RS][i]);
-        p[5] = make_double2(c[RTS][i], c[MASS][i]);
-        p[6] = make_double2(c[K_SOC][i], c[TAU0][i]);
-        p[7] = make_double2(c[MU][i], c[KAPPA][i]);
-        double sn, cs;
-        cdm_sincos(phi, &sn, &cs);
-        p[8] = make_double2(c[DAMP][i], sn);
-        p[9] = make_double2(cs, 0.0);
+        if (part != 1) {
+            double2 *p = a.stage + (size_t)s * STAGE_Q_TC;
+            p[0] = make_double2(x, y);
+            p[1] = make_double2(c[XLS][i], c[YLS][i]);
+            p[2] = make_double2(c[XRS][i], c[YRS][i]);
+            p[3] = make_double2(c[VX][i], c[VY][i]);
+            p[4] = make_double2(c[RT][i], c[RS][i]);
+            p[5] = make_double2(c[RTS][i], c[MASS][i]);
+            p[6] = make_double2(c[K_SOC][i], c[TAU0][i]);
+            p[7] = make_double2(c[MU][i], c[KAPPA][i]);
+            double sn, cs;
+            cdm_sincos(c[PHI][i], &sn, &cs);
+            p[8] = make_double2(c[DAMP][i], sn);
+            p[9] = make_double2(cs, 0.0);
+        }
+        if (part == 2) return;
         float xh = (float)x, yh = (float)y;
         // position = float hi + float lo; shoulder centres relative to the torso
         const float oxl = (float)(c[XLS][i] - x), oyl = (float)(c[YLS][i] - y);
@@ -2678,8 +2684,8 @@ void launch_scatter(const StepArgs &a, cudaStream_t s) {
     k_scatter<<<nblk(a.n, 256), 256, 0, s>>>(a);
     k_rank<<<nblk(a.n, 256), 256, 0, s>>>(a);
 }
-void launch_gather(const StepArgs &a, cudaStream_t s) {
-    if (a.n > 0) k_gather<<<nblk(a.n, 128), 128, 0, s>>>(a);
+void launch_gather(const StepArgs &a, cudaStream_t s, int part) {
+    if (a.n > 0) k_gather<<<nblk(a.n, 128), 128, 0, s>>>(a, part);
 }
 // Launch variants of the force kernel: (threads per block, staged candidates
 // per thread).
@@ -2793,7 +2799,7 @@ int init_kernels() {
 }
 
 void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEvent_t *pair_ev,
-                   bool captured, const Fork *fork) {
+                   bool captured, const Fork *fork, bool stage_deferred) {
     if (a.n <= 0) return;
     if (variant < 0 || variant >= N_VARIANTS) variant = 0;
     // the pair pipeline needs the near-list buffers: otherwise its lane-group twin
@@ -2804,6 +2810,7 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
     const int body = a.body ? 1 : 0;
     // the gather takes the prologue from k_prologue, on the second stream
     // beside the near lists when there is one
+    // and, when the cell list left them, the float64 staged records first
     const bool pro = v.pairs && a.pro;
     if (pro) {
         cudaStream_t sp = s;
@@ -2812,9 +2819,15 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
             cudaStreamWaitEvent(fork->s2, fork->fork, 0);
             sp = fork->s2;
         }
+        if (stage_deferred) {
+            launch_gather(a, sp, 2);
+            if (fork) cudaEventRecord(fork->join_stage, fork->s2);
+        }
         if (body) k_prologue<1><<<nblk(a.n, 128), 128, 0, sp>>>(a);
         else k_prologue<0><<<nblk(a.n, 128), 128, 0, sp>>>(a);
         if (fork) cudaEventRecord(fork->join, fork->s2);
+    } else if (stage_deferred) {
+        launch_gather(a, s, 2);
     }
     if (v.pairs && (a.nodes & N_AGENT)) {
         const int l = pair_l_index(v.lanes);
@@ -2825,6 +2838,7 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
         int rp = (dev >= 0 && dev < 64) ? g_pairs_blocks[dev][body][l] : 0;
         if (rp <= 0) rp = 152;
         // at most one warp per 32 pairs (about 16 pairs per agent): enough blocks
+        if (pro && stage_deferred && fork) cudaStreamWaitEvent(s, fork->join_stage, 0);
         if (pair_ev) cudaEventRecordWithFlags(pair_ev[0], s, captured ? cudaEventRecordExternal : 0);
         kPairs[body]<<<std::min(nblk((long long)a.n * 16, NTG), rp), NTG, pairs_smem_bytes(body),
                        s>>>(a);
