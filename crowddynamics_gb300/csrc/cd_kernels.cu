@@ -2104,20 +2104,29 @@ __global__ void __launch_bounds__(NTG, 4) k_pairs(StepArgs a) {
     PairQueue *wq = reinterpret_cast<PairQueue *>(smem);
     const int lane = threadIdx.x & 31;
     const int npairs = a.fw_off[a.n];
-    for (;;) {
+    // the next chunk's pair and partner are loaded before this chunk is
+    // evaluated, so that their load latency overlaps its work
+    auto claim = [&](int &s_, int &e_, int &t_) {
         int chunk = 0;
         if (lane == 0) chunk = atomicAdd(a.work, 1);
         chunk = __shfl_sync(FULL, chunk, 0);
-        if (chunk * 32 >= npairs) return;
-        const int k = chunk * 32 + lane;
-        const bool act = k < npairs;
-        int s = 0, e = 0, t = 0;
-        if (act) {
-            const int2 pe = __ldg(&a.fw_pairs[k]);
-            s = pe.x;
-            e = pe.y;
-            t = __ldg(&a.nl_idx[e]);
+        const int k_ = chunk * 32 + lane;
+        s_ = 0; e_ = 0; t_ = 0;
+        if (k_ < npairs) {
+            const int2 pe = __ldg(&a.fw_pairs[k_]);
+            s_ = pe.x;
+            e_ = pe.y;
+            t_ = __ldg(&a.nl_idx[e_]);
         }
+        return chunk * 32 < npairs ? k_ : -1;
+    };
+    int ns, ne, nt;
+    int nk = claim(ns, ne, nt);
+    for (;;) {
+        if (nk < 0) return;
+        const int k = nk, s = ns, e = ne, t = nt;
+        const bool act = k < npairs;
+        nk = claim(ns, ne, nt);
         double fpx = 0.0, fpy = 0.0, tp = 0.0, fqx = 0.0, fqy = 0.0, tq = 0.0;
         int kind = RES_NONE;
         if (BODY == 0) {
