@@ -623,7 +623,7 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->fix_count, 1));
     step(dalloc(c, &c->fix_list, n));
     step(dalloc(c, &c->slot_of, n));
-    step(dalloc(c, &c->pro, 4 * (int64_t)n));
+    step(dalloc(c, &c->pro, cdk::PRO_D * (int64_t)n));
     step(dalloc(c, &c->nl_mask, (int64_t)n * cdk::NL_MASK_CHUNKS));
     step(dalloc(c, &c->nl_nch, n + 1));
     step(dalloc(c, &c->nl_scan, cdk::scan_scratch_ints((int)npad)));

@@ -27,6 +27,9 @@ constexpr int ERR_NOT_FINITE = 1;
 // fill (an agent with more is evaluated again by the fill).
 constexpr int NL_MASK_CHUNKS = 64;
 
+// Doubles per agent of k_prologue's record (two 32-byte halves).
+constexpr int PRO_D = 8;
+
 // Columns of the per-agent interaction counts (CD_COUNT_COLS of cdgpu.h).
 constexpr int COUNT_COLS = 9;
 
@@ -83,7 +86,8 @@ struct StepArgs {
     int *work;                   // force-kernel work counter (zeroed per launch)
     int *fix_count, *fix_list;   // agents the gather leaves to k_forces_fallback
     int *slot_of;                // per agent: its cell-sorted slot (k_rank)
-    double *pro;                 // per agent: prologue force, torque and phi0 (4 doubles)
+    double *pro;                 // per agent PRO_D doubles: prologue fx, fy, torque, phi0;
+                                 // old accelerations (force_prev / m, torque_prev / I)
     // near lists (compute-once pair pipeline): per cell-sorted slot, the
     // slots of its near candidates in ascending order (= visiting order)
     int *nl_cnt;                 // n + 1 counts (scan input)

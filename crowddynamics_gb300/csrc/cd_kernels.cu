@@ -1520,7 +1520,8 @@ template <int BODY>
 __device__ __forceinline__ void agent_epilogue(const StepArgs &a, const int s, const int i,
                                                const int sid, const ScenDev &sc,
                                                const float4 me, const int my_cell, double fx,
-                                               double fy, double tq, const double phi0) {
+                                               double fy, double tq, const double phi0,
+                                               const double *old_acc = nullptr) {
     double *const *col = a.col;
     const int nodes = a.nodes;
     // Agent-wall (core/interactions.py:107-141,169-186), walls in index order
@@ -1557,7 +1558,9 @@ __device__ __forceinline__ void agent_epilogue(const StepArgs &a, const int s, c
         const double dt = a.dt[sid];
         const double dt2 = dt * dt;
         double m = col[MASS][i];
-        double oax = col[FPX][i] / m, oay = col[FPY][i] / m;
+        // the old accelerations, from k_prologue when it ran (same divisions)
+        double oax = old_acc ? old_acc[0] : col[FPX][i] / m;
+        double oay = old_acc ? old_acc[1] : col[FPY][i] / m;
         double nax = fx / m, nay = fy / m;
         double vx = col[VX][i] + (oax + nax) / 2 * dt;
         double vy = col[VY][i] + (oay + nay) / 2 * dt;
@@ -1568,7 +1571,7 @@ __device__ __forceinline__ void agent_epilogue(const StepArgs &a, const int s, c
         col[X][i] = x; col[Y][i] = y;
         if (BODY == 1) {
             double I = col[INERTIA][i];
-            double oaa = col[TORQUE_PREV][i] / I, naa = tq / I;
+            double oaa = old_acc ? old_acc[2] : col[TORQUE_PREV][i] / I, naa = tq / I;
             col[TORQUE_PREV][i] = tq;
             double w = col[OMEGA][i] + (oaa + naa) / 2 * dt;
             double phi = wrap_to_pi(col[PHI][i] + (w * dt + naa / 2 * dt2));
@@ -2199,7 +2202,20 @@ __global__ void __launch_bounds__(128) k_prologue(StepArgs a) {
     agent_prologue<BODY>(a, i, fx, fy, tq, phi0);
     double4_32a v;
     v.x = fx; v.y = fy; v.z = tq; v.w = phi0;
-    *reinterpret_cast<double4_32a *>(a.pro + 4 * (size_t)i) = v;
+    double4_32a *p = reinterpret_cast<double4_32a *>(a.pro + PRO_D * (size_t)i);
+    p[0] = v;
+    // the integrator's old accelerations: this step's force_prev / m and
+    // torque_prev / I, inputs no kernel before the gather changes
+    if (a.nodes & N_INTEG) {
+        double *const *col = a.col;
+        const double m = col[MASS][i];
+        double4_32a w;
+        w.x = col[FPX][i] / m;
+        w.y = col[FPY][i] / m;
+        w.z = BODY == 1 ? col[TORQUE_PREV][i] / col[INERTIA][i] : 0.0;
+        w.w = 0.0;
+        p[1] = w;
+    }
 }
 
 template <int BODY, bool EXACT>
@@ -2210,7 +2226,7 @@ __device__ __forceinline__ void gather_agent(const StepArgs &a, const int s, con
     const int my_cell = a.key[i];
     double fx, fy, tq, phi0;
     if (a.pro) {                                   // k_prologue's terms
-        const double4_32a v = *reinterpret_cast<const double4_32a *>(a.pro + 4 * (size_t)i);
+        const double4_32a v = *reinterpret_cast<const double4_32a *>(a.pro + PRO_D * (size_t)i);
         fx = v.x; fy = v.y; tq = v.z; phi0 = v.w;
     } else {
         agent_prologue<BODY>(a, i, fx, fy, tq, phi0);
@@ -2239,7 +2255,8 @@ __device__ __forceinline__ void gather_agent(const StepArgs &a, const int s, con
             }
         }
     }
-    agent_epilogue<BODY>(a, s, i, sid, sc, me, my_cell, fx, fy, tq, phi0);
+    agent_epilogue<BODY>(a, s, i, sid, sc, me, my_cell, fx, fy, tq, phi0,
+                         a.pro ? a.pro + PRO_D * (size_t)i + 4 : nullptr);
 }
 
 template <int BODY>
