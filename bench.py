@@ -343,7 +343,7 @@ def run_ours(args, ws, rank, local):
         t0 = time.perf_counter()
         for _ in range(args.steps):
             b.upload(rec)
-            b.run(1, nodes)
+            b.launch(1, nodes)     # download waits for the step and checks its status
             b.download(rec)
         e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
         trials.append(whole_job_rate(ws, n, args.steps, e2e_s))
@@ -373,7 +373,8 @@ def run_ours(args, ws, rank, local):
                     'd2h_bytes_per_step': n * agents.dtype.itemsize,
                     'trials': trials,
                     'timing': 'host wall clock around upload (pinned records), one graph '
-                              'step and download, per step; median of 3 passes'},
+                              'step launch and download (waits, checks the step status), '
+                              'per step; median of 3 passes'},
             'gpu_launches': b.kernels_per_step(nodes) * args.steps,
             'roofline': {'bound': 'fp64', 'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s',
                          'frac': achieved / peak, 'traffic': traffic,

@@ -30,6 +30,9 @@ struct cd_ctx {
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;              // beside the near-list build
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join_stage = nullptr;
+    cudaEvent_t ev_read = nullptr;               // an upload has read the host records
+    cudaEvent_t ev_ext = nullptr;                // an upload's extents are in ext_host
+    bool ext_pending = false;                    // ext_host not yet folded into extent_max
     double *pro = nullptr;
     int device = 0;
 
@@ -229,6 +232,8 @@ void release(cd_ctx *c) {
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->ev_join_stage) cudaEventDestroy(c->ev_join_stage);
+    if (c->ev_read) cudaEventDestroy(c->ev_read);
+    if (c->ev_ext) cudaEventDestroy(c->ev_ext);
 }
 
 // Flat cell range of a coordinate interval along one axis (clamped).
@@ -446,6 +451,33 @@ int enqueue_status(cd_ctx *c) {
 
 // `enqueued`: the caller already enqueued the status copies before its own
 // synchronisation (one synchronisation for both).
+// Folds the extents read back by the last upload into the wall-bin sizing;
+// the bins are rebuilt before the next step when an agent grew beyond the
+// extent they were built for.  This runs where the host waits for the stream
+// anyway (after a step's or a download's synchronisation, before the next
+// upload), so the step right after an upload always runs on the bins it
+// found: an agent that outgrew them scans every wall of its scenario (its
+// float32 extent exceeds the scenario's wall_reach), with the same walls
+// skipped as too far, and the results do not depend on the bins.
+int absorb_extent(cd_ctx *c) {
+    if (!c->ext_pending) return CD_OK;
+    CUDA_OR_FAIL(c, cudaEventSynchronize(c->ev_ext));
+    c->ext_pending = false;
+    if (c->extent_max.empty()) {
+        c->extent_max.assign(c->ext_host, c->ext_host + c->nscen);
+        c->walls_dirty = true;
+    } else {
+        bool grew = false;
+        for (int s = 0; s < c->nscen; ++s) grew |= c->ext_host[s] > c->extent_max[s];
+        if (grew) {
+            c->walls_dirty = true;
+            for (int s = 0; s < c->nscen; ++s)
+                c->extent_max[s] = std::max(c->extent_max[s], c->ext_host[s]);
+        }
+    }
+    return CD_OK;
+}
+
 int check_device_error(cd_ctx *c, bool enqueued = false) {
     CUDA_OR_FAIL(c, cudaGetLastError());
     const bool pairs = c->nl_cap > 0 && c->n > 0;       // lists in use (pair pipeline, adjoint)
@@ -453,6 +485,7 @@ int check_device_error(cd_ctx *c, bool enqueued = false) {
         if (int rc = enqueue_status(c)) return rc;
         CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
     }
+    if (int rc = absorb_extent(c)) return rc;       // complete: the stream was synchronised
     const int h = c->status_host[0], need = c->status_host[1];
     // the last list build did not fit: its step ran the fallback; grow for the next
     if (pairs && need > c->nl_cap)
@@ -577,7 +610,9 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
         cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_join_stage, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&c->ev_join_stage, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_read, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_ext, cudaEventDisableTiming) != cudaSuccess)
         rc = fail(c, CD_ERR_CUDA, "cudaStreamCreate failed");
     const int64_t npad = std::max<int64_t>(n, 1);
     if (rc == CD_OK && step(dalloc(c, &c->colbuf, npad * cdk::NCOL)))
@@ -707,6 +742,8 @@ int cd_upload_agents(cd_ctx *c, const void *records, int64_t n, int64_t itemsize
         if (off[f] >= 0 && !aligned_field(off[f], itemsize, width))
             return fail(c, CD_ERR_INVALID_TYPE, "float64 record field not 4-byte aligned");
     }
+    // the previous upload's read-back lands in ext_host: fold it in first
+    if (int rc = absorb_extent(c)) return rc;
     int64_t bytes = n * itemsize;
     if (bytes > c->aos_bytes) {
         if (c->aos) cudaFree(c->aos);
@@ -729,6 +766,7 @@ int cd_upload_agents(cd_ctx *c, const void *records, int64_t n, int64_t itemsize
                                             c->stream));
             cdk::launch_aos_to_soa(c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
         }
+        CUDA_OR_FAIL(c, cudaEventRecord(c->ev_read, c->stream));
         cdk::launch_states_in(c->aos, itemsize, state_offsets(off, itemsize), (int)n,
                               state_cols(c), c->stream);
         c->states_dirty = false;
@@ -737,20 +775,16 @@ int cd_upload_agents(cd_ctx *c, const void *records, int64_t n, int64_t itemsize
     cdk::launch_scen_max(a, c->v0max, c->ext, c->max_partial, c->stream);
     CUDA_OR_FAIL(c, cudaMemcpyAsync(c->ext_host, c->ext, sizeof(double) * c->nscen,
                                     cudaMemcpyDeviceToHost, c->stream));
+    CUDA_OR_FAIL(c, cudaEventRecord(c->ev_ext, c->stream));
     CUDA_OR_FAIL(c, cudaGetLastError());
-    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
-    // Wall bins depend on the agents' extent: rebuilt when it grew.
-    if (c->extent_max.empty()) {
-        c->extent_max.assign(c->ext_host, c->ext_host + c->nscen);
-        c->walls_dirty = true;
-    } else {
-        for (int s = 0; s < c->nscen; ++s)
-            if (c->ext_host[s] > c->extent_max[s]) c->walls_dirty = true;
-        if (c->walls_dirty)
-            for (int s = 0; s < c->nscen; ++s)
-                c->extent_max[s] = std::max(c->extent_max[s], c->ext_host[s]);
-    }
+    c->ext_pending = true;
     c->have_records = true;
+    // The caller may reuse `records` once this returns: wait for the read of
+    // them, not for the extent reduction behind it.
+    if (n > 0) CUDA_OR_FAIL(c, cudaEventSynchronize(c->ev_read));
+    // Wall bins depend on the agents' extent: the first upload sizes them.
+    if (c->extent_max.empty())
+        if (int rc = absorb_extent(c)) return rc;
     return CD_OK;
 }
 
@@ -1217,6 +1251,7 @@ static_assert(CD_COUNT_COLS == cdk::COUNT_COLS, "count columns differ");
 int cd_pair_counts(cd_ctx *c, int64_t *counts) {
     if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
     if (!c->have_records) return fail(c, CD_ERR_INVALID_VALUE, "no agents uploaded");
+    if (int rc = absorb_extent(c)) return rc;
     if (c->walls_dirty && c->nw > 0) {
         if (c->walls_host.empty())
             return fail(c, CD_ERR_INVALID_VALUE, "walls declared but cd_set_walls not called");

@@ -283,12 +283,12 @@ __global__ void k_dt(StepArgs a) {
     if (s < a.n_scen) scenario_dt(a, s);
 }
 
-// Per-scenario max of target_velocity (np.max propagates NaN).
 // Per-scenario max target_velocity (NaN if any is NaN, like numpy's max) and
-// max agent extent (finite values only) in two passes: V0MAX_B blocks per
-// scenario write partials, then one warp per scenario combines them.  fmax
-// is exact, so the result does not depend on the order.
-constexpr int V0MAX_B = 64;
+// max agent extent (finite values only) in two passes: up to V0MAX_B blocks
+// per scenario (about two agents per thread at the mean scenario size) write
+// partials, then one warp per scenario combines them.  fmax is exact, so the
+// result does not depend on the order.
+constexpr int V0MAX_B = 256;
 
 __device__ __forceinline__ double extent_tc(double x, double y, double xl, double yl,
                                             double xr, double yr, double rt, double rs);
@@ -2913,8 +2913,10 @@ void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s) {
 void launch_scen_max(const StepArgs &a, double *v0max, double *ext, double *partial,
                      cudaStream_t s) {
     if (a.n_scen <= 0) return;
-    k_scen_max_partial<<<dim3(V0MAX_B, a.n_scen), 256, 0, s>>>(a, partial);
-    k_scen_max_final<<<(a.n_scen + 7) / 8, 256, 0, s>>>(partial, V0MAX_B, a.n_scen, v0max, ext);
+    const long long mean = ((long long)a.n + a.n_scen - 1) / a.n_scen;
+    const int nb = (int)std::min<long long>(V0MAX_B, std::max<long long>(1, (mean + 511) / 512));
+    k_scen_max_partial<<<dim3(nb, a.n_scen), 256, 0, s>>>(a, partial);
+    k_scen_max_final<<<(a.n_scen + 7) / 8, 256, 0, s>>>(partial, nb, a.n_scen, v0max, ext);
 }
 int scen_max_partials(int n_scen) { return 2 * V0MAX_B * (n_scen > 0 ? n_scen : 1); }
 void launch_wall_prep(const double *raw, double *walls, float4 *wf, int nw, cudaStream_t s) {

@@ -212,6 +212,36 @@ def test_rollout_50_steps(oracle, native, name):
     assert d.max() <= 1e-6, d.max()
 
 
+@pytest.mark.parametrize('grow', [0.0, 0.2])
+def test_wall_bins_after_extent_growth(oracle, native, grow):
+    """An upload whose agents outgrew the extent the wall bins were built
+    for: the step right after it runs on the old bins (the grown agents scan
+    every wall of the scenario), the bins are rebuilt at that step's
+    synchronisation, and the second step runs on the new ones.  Both match
+    the oracle bit for bit."""
+    scen = S.hallway(n=300, seed=4, max_agent_radius=0.6)
+    nodes = N.NODE_ALL & ~N.NODE_FLUCTUATION
+    b, agents, _ = batch_from_scenarios([scen])
+    b.step(nodes)
+    rec = agents.copy()
+    b.download(rec)
+    y = rec['position'][:, 1]
+    near = np.argsort(np.minimum(y, 10.0 - y))[:20]
+    rec['radius'][near] += grow + 0.05
+    ref = rec.copy()
+    b.upload(rec)
+    grid = oracle_grid(oracle, scen)
+    with oracle.exact_math():
+        for k in range(2):
+            b.step(nodes)
+            oracle.step(ref, grid, scen.walls, None, None, flags=orc_flags(nodes),
+                        dt_min=scen.dt_min, dt_max=scen.dt_max)
+            got = rec.copy()
+            b.download(got)
+            assert_identical(got, ref, 'step %d after the upload' % k)
+    b.close()
+
+
 def test_cell_list_bit_exact(oracle, native):
     for scen in (S.hallway(), S.room(), S.large_field(n=20000, size=140.0, n_walls=100, seed=9)):
         b, agents, _ = batch_from_scenarios([scen])
