@@ -343,7 +343,7 @@ int64_t kernels_per_step(const cd_ctx *c, int nodes) {
     k += cdk::scan_launches_single((int)c->ncells);
     if (cdk::variant_pairs(c->variant) && c->nl_cnt) k += 2;     // prologue, float64 staging
     if (cdk::variant_pairs(c->variant) && (nodes & CD_NODE_AGENT_AGENT) && c->nl_cnt)
-        k += 4 + (cdk::scan_scratch_ints((int)c->n) > 1 ? 3 : 1);   // count fill pairs fallback + scans
+        k += 5;                                   // count, scans, fill, pairs, fallback
     return k;
 }
 
@@ -661,13 +661,13 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->pro, cdk::PRO_D * (int64_t)n));
     step(dalloc(c, &c->nl_mask, (int64_t)n * cdk::NL_MASK_CHUNKS));
     step(dalloc(c, &c->nl_nch, n + 1));
-    step(dalloc(c, &c->nl_scan, cdk::scan_scratch_ints((int)npad)));
+    step(dalloc(c, &c->nl_scan, cdk::near_scan_ints((int)npad)));
     step(dalloc(c, &c->fw_cnt, n + 1));
     step(dalloc(c, &c->fw_off, n + 1));
-    step(dalloc(c, &c->fw_scan, cdk::scan_scratch_ints((int)npad)));
+    step(dalloc(c, &c->fw_scan, cdk::near_scan_ints((int)npad)));
     step(dalloc(c, &c->fs_cnt, n + 1));
     step(dalloc(c, &c->fs_off, n + 1));
-    step(dalloc(c, &c->fs_scan, cdk::scan_scratch_ints((int)npad)));
+    step(dalloc(c, &c->fs_scan, cdk::near_scan_ints((int)npad)));
     if (rc == CD_OK) {
         cudaMemcpy(c->scen_of, c->scen_of_host.data(), sizeof(int) * npad, cudaMemcpyHostToDevice);
         cudaMemcpy(c->scen, c->scen_dev.data(), sizeof(ScenDev) * n_scenarios, cudaMemcpyHostToDevice);
@@ -680,6 +680,8 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
         cudaMemset(c->count, 0, sizeof(int) * ncells);       // zero between cell lists
         cudaMemset(c->fill, 0, sizeof(int) * ncells);
         cudaMemset(c->vmax, 0, sizeof(unsigned long long) * n_scenarios);
+        for (int *p : {c->nl_scan, c->fw_scan, c->fs_scan})   // the scans' tile counters
+            cudaMemset(p, 0, sizeof(int) * cdk::near_scan_ints((int)npad));
         cudaEventCreate(&c->ev0);
         cudaEventCreate(&c->ev1);
         cudaEventCreate(&c->evs0);

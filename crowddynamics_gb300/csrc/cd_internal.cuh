@@ -186,6 +186,9 @@ void launch_copy_cols(const double *const *src, double *const *dst, int ncol, in
 void launch_prepare(const StepArgs &a, cudaStream_t s);
 void launch_dt(const StepArgs &a, cudaStream_t s);
 int scan_scratch_ints(int n);
+// Scratch ints of each near-list scan (tile totals, tile offsets, a counter;
+// zeroed once at allocation).
+int near_scan_ints(int n);
 void launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s);
 int scan_launches_single(int n);          // kernels launch_scan uses for n elements
 void launch_scatter(const StepArgs &a, cudaStream_t s);

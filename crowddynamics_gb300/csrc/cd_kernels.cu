@@ -412,8 +412,10 @@ __global__ void __launch_bounds__(SCAN_NT) k_scan_local(ScanSet S, int n) {
     }
 }
 
-// One block scanning up to a few tiles in turn (one launch for small arrays).
-__global__ void __launch_bounds__(SCAN_NT) k_scan_single(const int *in, int *out, int n) {
+// One block scanning n values in tiles, in turn: exclusive offsets into
+// out[0, n); returns the total (the same in every thread).  Loads go through
+// L2 only, so values other blocks of the same launch wrote are seen.
+__device__ int scan_one_block(const int *in, int *out, int n) {
     __shared__ int wtot[SCAN_NT / 32];
     __shared__ int tile_total;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -424,7 +426,7 @@ __global__ void __launch_bounds__(SCAN_NT) k_scan_single(const int *in, int *out
         int sum = 0;
 #pragma unroll
         for (int k = 0; k < SCAN_IPT; ++k) {
-            v[k] = (base + k < n) ? in[base + k] : 0;
+            v[k] = (base + k < n) ? __ldcg(in + base + k) : 0;
             sum += v[k];
         }
         int incl = sum;
@@ -455,7 +457,75 @@ __global__ void __launch_bounds__(SCAN_NT) k_scan_single(const int *in, int *out
         carry += tile_total;
         __syncthreads();                      // wtot and tile_total reused
     }
-    if (threadIdx.x == 0) out[n] = carry;
+    return carry;
+}
+
+// One block scanning up to a few tiles in turn (one launch for small arrays).
+__global__ void __launch_bounds__(SCAN_NT) k_scan_single(const int *in, int *out, int n) {
+    const int total = scan_one_block(in, out, n);
+    if (threadIdx.x == 0) out[n] = total;
+}
+
+// Up to three arrays scanned by one launch, for the near lists: every tile
+// writes its exclusive offsets relative to the tile and its total
+// (sums[tile]); the last tile to finish (counted at sums[2 nb + 2]; no block
+// waits for another) scans the totals into tile offsets (sums[nb + 1 + j]),
+// writes the grand total at out[n] and re-arms the counter.  The near-list
+// fill adds its agent's tile offset and writes the final offset back.
+__global__ void __launch_bounds__(SCAN_NT) k_scan_tiles(ScanSet S, int n, int nb) {
+    const int *in = S.in[blockIdx.y];
+    int *out = S.out[blockIdx.y];
+    int *sums = S.sums[blockIdx.y];
+    __shared__ int wtot[SCAN_NT / 32];
+    __shared__ int last;
+    const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_IPT;
+    int v[SCAN_IPT];
+    int sum = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_IPT; ++k) {
+        v[k] = (base + k < n) ? in[base + k] : 0;
+        sum += v[k];
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) wtot[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int x = wtot[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += t;
+        }
+        wtot[lane] = x;
+    }
+    __syncthreads();
+    int excl = incl - sum + (w > 0 ? wtot[w - 1] : 0);
+#pragma unroll
+    for (int k = 0; k < SCAN_IPT; ++k) {
+        if (base + k < n) out[base + k] = excl;
+        excl += v[k];
+    }
+    if (threadIdx.x == SCAN_NT - 1) {
+        sums[blockIdx.x] = excl;                        // the tile's total
+        __threadfence();
+        unsigned *done = reinterpret_cast<unsigned *>(sums + 2 * nb + 2);
+        last = atomicAdd(done, 1u) == (unsigned)(nb - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const int total = scan_one_block(sums, sums + nb + 1, nb);
+    if (threadIdx.x == 0) {
+        sums[nb + 1 + nb] = total;
+        out[n] = total;
+        sums[2 * nb + 2] = 0;
+    }
 }
 
 __global__ void k_scan_add(ScanSet S, int n, int nb) {
@@ -1979,13 +2049,19 @@ __global__ void __launch_bounds__(NTG) k_nl_fill(StepArgs a) {
     const ScenDev sc = a.scen[a.scen_of[i]];
     int rb[3], re[3];
     candidate_runs(a, sc, a.key[i], rb, re);
+    // the scans left offsets relative to the slot's tile: add the tile's
+    // offset (written back below, once every lane of the group has read)
+    const int off_at = (a.n + SCAN_TILE - 1) / SCAN_TILE + 1 + s / SCAN_TILE;
+    const int nl_s = a.nl_off[s] + a.nl_scan[off_at];
+    const int fw_s = a.fw_off[s] + a.fw_scan[off_at];
+    const int fs_s = a.fs_off[s] + a.fs_scan[off_at];
     // entries with a later slot follow all earlier ones (ascending order)
-    const int fwd0 = a.nl_off[s] + (a.nl_cnt[s] - a.fw_cnt[s]);
-    int pos = a.nl_off[s];
+    const int fwd0 = nl_s + (a.nl_cnt[s] - a.fw_cnt[s]);
+    int pos = nl_s;
     // the flat list of pairs: first every pair guessed to need the social
     // force, then the others, each part in slot order
-    int p0 = a.fs_off[s];
-    int p1 = a.fs_off[a.n] + (a.fw_off[s] - a.fs_off[s]);
+    int p0 = fs_s;
+    int p1 = a.fs_off[a.n] + (fw_s - fs_s);
     const unsigned lower = (1u << r) - 1u;
     if (a.nl_nch[s] <= NL_MASK_CHUNKS) {
         constexpr int C = NlChunk<L>::C, CW = NlChunk<L>::CW;
@@ -2042,7 +2118,13 @@ __global__ void __launch_bounds__(NTG) k_nl_fill(StepArgs a) {
                 p1 += __popc(fb & ~sb);
             }
     }
-    if (r == 0) a.nl_fwd[s] = fwd0;
+    __syncwarp(gm);
+    if (r == 0) {
+        a.nl_fwd[s] = fwd0;
+        a.nl_off[s] = nl_s;
+        a.fw_off[s] = fw_s;
+        a.fs_off[s] = fs_s;
+    }
 }
 
 // Entry of `s` in the earlier-slot part of `t`'s near list (s < t), or -1.
@@ -2663,6 +2745,7 @@ int scan_scratch_ints(int n) {
     int nb = nblk(n, SCAN_TILE);
     return nb > 1 ? 2 * (nb + 1) : 1;
 }
+int near_scan_ints(int n) { return 2 * (nblk(n, SCAN_TILE) + 1) + 1; }
 void launch_scans(int k, const int *const *in, int *const *out, int n, int *const *scratch,
                   cudaStream_t s) {
     const int nb = nblk(n, SCAN_TILE);
@@ -2700,10 +2783,12 @@ void launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s) {
 }
 // Near, forward and guessed-social counts scanned together.
 void launch_near_scans(const StepArgs &a, cudaStream_t s) {
-    const int *in[3] = {a.nl_cnt, a.fw_cnt, a.fs_cnt};
-    int *out[3] = {a.nl_off, a.fw_off, a.fs_off};
-    int *scr[3] = {a.nl_scan, a.fw_scan, a.fs_scan};
-    launch_scans(3, in, out, a.n, scr, s);
+    const int nb = nblk(a.n, SCAN_TILE);
+    if (nb <= 0) return;
+    const ScanSet S{{a.nl_cnt, a.fw_cnt, a.fs_cnt},
+                    {a.nl_off, a.fw_off, a.fs_off},
+                    {a.nl_scan, a.fw_scan, a.fs_scan}};
+    k_scan_tiles<<<dim3(nb, 3), SCAN_NT, 0, s>>>(S, a.n, nb);
 }
 void launch_scatter(const StepArgs &a, cudaStream_t s) {
     if (a.n <= 0) return;
