@@ -311,10 +311,13 @@ void enqueue_cells(cd_ctx *c, const StepArgs &a, bool defer_stage = false) {
     // then by k_rank and k_scatter once used)
     cdk::launch_prepare(a, c->stream);
     // dt is computed by the scatter kernel, launched only for agents
-    if ((a.nodes & cdk::N_INTEG) && a.n == 0) cdk::launch_dt(a, c->stream);
-    cdk::launch_scan(c->count, c->start, (int)c->ncells, c->scan_scratch, c->stream);
-    cdk::launch_scatter(a, c->stream);
-    cdk::launch_gather(a, c->stream, defer_stage ? 1 : 0);
+    const bool dt_kernel = (a.nodes & cdk::N_INTEG) && a.n == 0;
+    if (dt_kernel) cdk::launch_dt(a, c->stream);
+    // each kernel of the cell list chained to the one before it
+    cdk::launch_scan(c->count, c->start, (int)c->ncells, c->scan_scratch, c->stream,
+                     a.n > 0 || dt_kernel);
+    cdk::launch_scatter(a, c->stream, true);
+    cdk::launch_gather(a, c->stream, defer_stage ? 1 : 0, true);
 }
 
 // One step on the context stream.  `timed`: record the step and force-kernel

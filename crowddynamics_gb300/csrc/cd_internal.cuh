@@ -189,12 +189,15 @@ int scan_scratch_ints(int n);
 // Scratch ints of each near-list scan (tile totals, tile offsets, a counter;
 // zeroed once at allocation).
 int near_scan_ints(int n);
-void launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s);
+// `after_kernel`: the last operation on `s` is a kernel launch; the first
+// kernel here is then launched as its programmatic dependent.
+void launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s,
+                 bool after_kernel = false);
 int scan_launches_single(int n);          // kernels launch_scan uses for n elements
-void launch_scatter(const StepArgs &a, cudaStream_t s);
+void launch_scatter(const StepArgs &a, cudaStream_t s, bool after_kernel = false);
 // Staged records of the cell-sorted agents: part 0 all, 1 the float32
 // pre-check records, 2 the float64 records.
-void launch_gather(const StepArgs &a, cudaStream_t s, int part = 0);
+void launch_gather(const StepArgs &a, cudaStream_t s, int part = 0, bool after_kernel = false);
 constexpr int N_VARIANTS = 12;      // launch variants of the force kernel
 bool variant_pairs(int variant);
 int variant_lanes(int variant);

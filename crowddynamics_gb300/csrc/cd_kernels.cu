@@ -221,7 +221,18 @@ __device__ __forceinline__ void wall_three_circle(const TC &A, const double *w,
 
 // ---- kernels ------------------------------------------------------------
 
+// Programmatic dependent launch, first statement of the step's chained
+// kernels: wait until the kernel before this one on the stream has completed
+// and its memory is visible (returns at once after an ordinary launch), then
+// allow the next kernel's blocks to be scheduled beside this one's last
+// blocks (they wait here in turn).
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __global__ void k_prepare(StepArgs a) {
+    pdl_enter();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     // device fluctuation: this step's generator counter (read by the force stage)
     if (i == 0 && a.noise_dev && (a.nodes & N_FLUCT)) *a.rng_step += 1;
@@ -369,6 +380,7 @@ constexpr int SCAN_NT = 1024, SCAN_IPT = 4, SCAN_TILE = SCAN_NT * SCAN_IPT;
 struct ScanSet { const int *in[3]; int *out[3]; int *sums[3]; };
 
 __global__ void __launch_bounds__(SCAN_NT) k_scan_local(ScanSet S, int n) {
+    pdl_enter();
     const int *in = S.in[blockIdx.y];
     int *out = S.out[blockIdx.y];
     int *blocksums = S.sums[blockIdx.y];
@@ -462,6 +474,7 @@ __device__ int scan_one_block(const int *in, int *out, int n) {
 
 // One block scanning up to a few tiles in turn (one launch for small arrays).
 __global__ void __launch_bounds__(SCAN_NT) k_scan_single(const int *in, int *out, int n) {
+    pdl_enter();
     const int total = scan_one_block(in, out, n);
     if (threadIdx.x == 0) out[n] = total;
 }
@@ -473,6 +486,7 @@ __global__ void __launch_bounds__(SCAN_NT) k_scan_single(const int *in, int *out
 // writes the grand total at out[n] and re-arms the counter.  The near-list
 // fill adds its agent's tile offset and writes the final offset back.
 __global__ void __launch_bounds__(SCAN_NT) k_scan_tiles(ScanSet S, int n, int nb) {
+    pdl_enter();
     const int *in = S.in[blockIdx.y];
     int *out = S.out[blockIdx.y];
     int *sums = S.sums[blockIdx.y];
@@ -529,6 +543,7 @@ __global__ void __launch_bounds__(SCAN_NT) k_scan_tiles(ScanSet S, int n, int nb
 }
 
 __global__ void k_scan_add(ScanSet S, int n, int nb) {
+    pdl_enter();
     int *out = S.out[blockIdx.y];
     const int *offs = S.in[blockIdx.y];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -537,6 +552,7 @@ __global__ void k_scan_add(ScanSet S, int n, int nb) {
 }
 
 __global__ void k_scatter(StepArgs a) {
+    pdl_enter();
     // the step's dt: k_prepare's max |v| is complete once this kernel runs
     // (then the max is used up: zero for the next cell list)
     if (blockIdx.x == 0)
@@ -554,6 +570,7 @@ __global__ void k_scatter(StepArgs a) {
 // Stable order inside a cell: rank = number of agents of the cell with a
 // smaller index.
 __global__ void k_rank(StepArgs a) {
+    pdl_enter();
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= a.n) return;
     int i = a.perm_unsorted[p];
@@ -602,6 +619,7 @@ __device__ __forceinline__ float up_f(double v) {
 // records; 1 the float32 pre-check records only (all the near-list build
 // reads); 2 the float64 staged records only.
 __global__ void k_gather(StepArgs a, int part) {
+    pdl_enter();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.n) return;
     int s, i;
@@ -1984,6 +2002,7 @@ __device__ __forceinline__ unsigned later_bits(int s, int base) {
 
 template <int L>
 __global__ void __launch_bounds__(NTG) k_nl_count(StepArgs a) {
+    pdl_enter();
     static_assert(NlChunk<L>::CW <= 16, "two 16-bit masks per 32-bit word");
     constexpr int C = NlChunk<L>::C, CW = NlChunk<L>::CW;
     constexpr unsigned GMASK = (1u << L) - 1u;
@@ -2037,6 +2056,7 @@ __global__ void __launch_bounds__(NTG) k_nl_count(StepArgs a) {
 
 template <int L>
 __global__ void __launch_bounds__(NTG) k_nl_fill(StepArgs a) {
+    pdl_enter();
     if (blockIdx.x == 0 && threadIdx.x == 0) *a.work = 0;   // k_pairs' work counter
     if (a.nl_off[a.n] > a.nl_cap) return;                 // over capacity: fallback
     constexpr unsigned GMASK = (1u << L) - 1u;
@@ -2343,6 +2363,7 @@ __device__ __forceinline__ void gather_agent(const StepArgs &a, const int s, con
 
 template <int BODY>
 __global__ void __launch_bounds__(NTG) k_forces_gather(StepArgs a) {
+    pdl_enter();
     if (blockIdx.x == 0 && threadIdx.x == 0) *a.work = 0;   // k_forces_fallback's work counter
     if ((a.nodes & N_AGENT) && a.nl_off[a.n] > a.nl_cap) return;   // k_forces_fallback's step
     // one lane per slot: the entries of neighbouring lanes are neighbours
@@ -2355,6 +2376,7 @@ __global__ void __launch_bounds__(NTG) k_forces_gather(StepArgs a) {
 // The lane-group kernel, for a step whose near lists exceeded the capacity.
 template <int BODY, int L>
 __global__ void __launch_bounds__(NTG) k_forces_fallback(StepArgs a) {
+    pdl_enter();
     if (!((a.nodes & N_AGENT) && a.nl_off[a.n] > a.nl_cap)) {
         // the gather ran: redo the agents it left (their torque reached -0)
         if (BODY == 1) {
@@ -2732,6 +2754,29 @@ __global__ void k_fp64_fma(double *out, int iters, double b, double c) {
 
 inline int nblk(long long n, int nt) { return (int)((n + nt - 1) / nt); }
 
+// Launch of kernel `k` on `s`.  `dep`: as the programmatic dependent of the
+// kernel launched just before it on `s` (every such kernel starts with
+// pdl_enter), so that its launch overlaps that kernel's last blocks.
+template <typename... P, typename... A>
+void launch_k(bool dep, void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+              A... args) {
+    if (!dep) {
+        k<<<grid, block, smem, s>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 }  // namespace
 
 void launch_prepare(const StepArgs &a, cudaStream_t s) {
@@ -2747,7 +2792,7 @@ int scan_scratch_ints(int n) {
 }
 int near_scan_ints(int n) { return 2 * (nblk(n, SCAN_TILE) + 1) + 1; }
 void launch_scans(int k, const int *const *in, int *const *out, int n, int *const *scratch,
-                  cudaStream_t s) {
+                  cudaStream_t s, bool dep) {
     const int nb = nblk(n, SCAN_TILE);
     ScanSet S{};
     for (int j = 0; j < k; ++j) {
@@ -2756,30 +2801,30 @@ void launch_scans(int k, const int *const *in, int *const *out, int n, int *cons
         S.sums[j] = nb > 1 ? scratch[j] : nullptr;
     }
     if (nb <= 1) {
-        k_scan_local<<<dim3(1, k), SCAN_NT, 0, s>>>(S, n);
+        launch_k(dep, k_scan_local, dim3(1, k), SCAN_NT, 0, s, S, n);
         return;
     }
-    k_scan_local<<<dim3(nb, k), SCAN_NT, 0, s>>>(S, n);
+    launch_k(dep, k_scan_local, dim3(nb, k), SCAN_NT, 0, s, S, n);
     ScanSet T{};                          // block totals, offsets after them (offs[nb] = total)
     for (int j = 0; j < k; ++j) {
         T.in[j] = scratch[j];
         T.out[j] = scratch[j] + nb + 1;
         T.sums[j] = nullptr;
     }
-    k_scan_local<<<dim3(1, k), SCAN_NT, 0, s>>>(T, nb);
+    launch_k(true, k_scan_local, dim3(1, k), SCAN_NT, 0, s, T, nb);
     ScanSet U{};
     for (int j = 0; j < k; ++j) {
         U.in[j] = scratch[j] + nb + 1;
         U.out[j] = out[j];
     }
-    k_scan_add<<<dim3(nblk(n + 1, 256), k), 256, 0, s>>>(U, n, nb);
+    launch_k(true, k_scan_add, dim3(nblk(n + 1, 256), k), 256, 0, s, U, n, nb);
 }
-void launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s) {
+void launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s, bool after_kernel) {
     if (n > SCAN_TILE && n <= 4 * SCAN_TILE) {
-        k_scan_single<<<1, SCAN_NT, 0, s>>>(in, out, n);
+        launch_k(after_kernel, k_scan_single, 1, SCAN_NT, 0, s, in, out, n);
         return;
     }
-    launch_scans(1, &in, &out, n, &scratch, s);
+    launch_scans(1, &in, &out, n, &scratch, s, after_kernel);
 }
 // Near, forward and guessed-social counts scanned together.
 void launch_near_scans(const StepArgs &a, cudaStream_t s) {
@@ -2788,15 +2833,15 @@ void launch_near_scans(const StepArgs &a, cudaStream_t s) {
     const ScanSet S{{a.nl_cnt, a.fw_cnt, a.fs_cnt},
                     {a.nl_off, a.fw_off, a.fs_off},
                     {a.nl_scan, a.fw_scan, a.fs_scan}};
-    k_scan_tiles<<<dim3(nb, 3), SCAN_NT, 0, s>>>(S, a.n, nb);
+    launch_k(true, k_scan_tiles, dim3(nb, 3), SCAN_NT, 0, s, S, a.n, nb);   // after the count
 }
-void launch_scatter(const StepArgs &a, cudaStream_t s) {
+void launch_scatter(const StepArgs &a, cudaStream_t s, bool after_kernel) {
     if (a.n <= 0) return;
-    k_scatter<<<nblk(a.n, 256), 256, 0, s>>>(a);
-    k_rank<<<nblk(a.n, 256), 256, 0, s>>>(a);
+    launch_k(after_kernel, k_scatter, nblk(a.n, 256), 256, 0, s, a);
+    launch_k(true, k_rank, nblk(a.n, 256), 256, 0, s, a);
 }
-void launch_gather(const StepArgs &a, cudaStream_t s, int part) {
-    if (a.n > 0) k_gather<<<nblk(a.n, 128), 128, 0, s>>>(a, part);
+void launch_gather(const StepArgs &a, cudaStream_t s, int part, bool after_kernel) {
+    if (a.n > 0) launch_k(after_kernel, k_gather, nblk(a.n, 128), 128, 0, s, a, part);
 }
 // Launch variants of the force kernel: (threads per block, staged candidates
 // per thread).
@@ -2945,7 +2990,7 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
         const int nb = nblk((long long)a.n * v.lanes, NTG);
         kNlCount[l]<<<nb, NTG, 0, s>>>(a);
         launch_near_scans(a, s);
-        kNlFill[l]<<<nb, NTG, 0, s>>>(a);
+        launch_k(true, kNlFill[l], nb, NTG, 0, s, a);
         int rp = (dev >= 0 && dev < 64) ? g_pairs_blocks[dev][body][l] : 0;
         if (rp <= 0) rp = 152;
         // at most one warp per 32 pairs (about 16 pairs per agent): enough blocks
@@ -2971,9 +3016,9 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
         const int gv = variant - 4;                       // the lane-group twin
         int rg = (dev >= 0 && dev < 64) ? g_forces_blocks[dev][body][gv] : 0;
         if (rg <= 0) rg = 152;
-        kFallback[body][pair_l_index(v.lanes)]<<<(int)std::min<long long>(
-                                                    (threads + NTG - 1) / NTG, rg),
-                                                NTG, forces_smem_bytes(body, gv), s>>>(a);
+        launch_k(true, kFallback[body][pair_l_index(v.lanes)],
+                 (int)std::min<long long>((threads + NTG - 1) / NTG, rg), NTG,
+                 forces_smem_bytes(body, gv), s, a);          // after the gather
     }
 }
 
@@ -2989,7 +3034,7 @@ void launch_near_lists(const StepArgs &a, cudaStream_t s) {
     const int nb = nblk((long long)a.n * 8, NTG);
     kNlCount[1]<<<nb, NTG, 0, s>>>(a);
     launch_near_scans(a, s);
-    kNlFill[1]<<<nb, NTG, 0, s>>>(a);
+    launch_k(true, kNlFill[1], nb, NTG, 0, s, a);
 }
 
 void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s) {
