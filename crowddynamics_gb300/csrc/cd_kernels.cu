@@ -231,7 +231,9 @@ __device__ __forceinline__ void pdl_enter() {
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
-__global__ void k_prepare(StepArgs a) {
+constexpr int PREP_NT = 256;                     // k_prepare's block size
+
+__global__ void __launch_bounds__(PREP_NT) k_prepare(StepArgs a) {
     pdl_enter();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     // device fluctuation: this step's generator counter (read by the force stage)
@@ -253,18 +255,29 @@ __global__ void k_prepare(StepArgs a) {
         atomicAdd(&a.count[key], 1);
         l = cdm_hypot(a.col[VX][i], a.col[VY][i]);      // length(velocity)
     }
-    // per-scenario max |v| (NaN and 0 ignored, like `if l > v_max`)
-    unsigned mask = __activemask();
-    int s0 = __shfl_sync(mask, s, 0);
-    bool uniform = __all_sync(mask, s == s0);
-    if (uniform) {
+    // per-scenario max |v| (NaN and 0 ignored, like `if l > v_max`): one
+    // atomic per block when its agents share a scenario (fmax is exact, so
+    // the order does not matter)
+    __shared__ int s_block;
+    __shared__ double wmax[PREP_NT / 32];
+    if (threadIdx.x == 0) s_block = s;
+    __syncthreads();
+    if (__syncthreads_and(s == s_block || s < 0)) {
         double m = (l > 0) ? l : 0.0;
         for (int o = 16; o > 0; o >>= 1) {
-            double t = __shfl_xor_sync(mask, m, o);
+            const double t = __shfl_xor_sync(0xffffffffu, m, o);
             m = (t > m) ? t : m;
         }
-        if ((threadIdx.x & 31) == 0 && s0 >= 0 && m > 0)
-            atomicMax(&a.vmax[s0], ord_bits(m));
+        if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            m = threadIdx.x < PREP_NT / 32 ? wmax[threadIdx.x] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) {
+                const double t = __shfl_xor_sync(0xffffffffu, m, o);
+                m = (t > m) ? t : m;
+            }
+            if (threadIdx.x == 0 && s_block >= 0 && m > 0) atomicMax(&a.vmax[s_block], ord_bits(m));
+        }
     } else if (s >= 0 && l > 0) {
         atomicMax(&a.vmax[s], ord_bits(l));
     }
@@ -2361,8 +2374,11 @@ __device__ __forceinline__ void gather_agent(const StepArgs &a, const int s, con
                          a.pro ? a.pro + PRO_D * (size_t)i + 4 : nullptr);
 }
 
+// One-warp blocks; 24 resident per SM (80 registers, a few spilled): the
+// float64 epilogue's latency wants the warps more than the registers.
+constexpr int GATHER_NT = 32;
 template <int BODY>
-__global__ void __launch_bounds__(NTG) k_forces_gather(StepArgs a) {
+__global__ void __launch_bounds__(GATHER_NT, 24) k_forces_gather(StepArgs a) {
     pdl_enter();
     if (blockIdx.x == 0 && threadIdx.x == 0) *a.work = 0;   // k_forces_fallback's work counter
     if ((a.nodes & N_AGENT) && a.nl_off[a.n] > a.nl_cap) return;   // k_forces_fallback's step
@@ -2780,7 +2796,7 @@ void launch_k(bool dep, void (*k)(P...), dim3 grid, dim3 block, size_t smem, cud
 }  // namespace
 
 void launch_prepare(const StepArgs &a, cudaStream_t s) {
-    if (a.n > 0) k_prepare<<<nblk(a.n, 256), 256, 0, s>>>(a);
+    if (a.n > 0) k_prepare<<<nblk(a.n, PREP_NT), PREP_NT, 0, s>>>(a);
 }
 void launch_dt(const StepArgs &a, cudaStream_t s) {
     if (a.n_scen > 0) k_dt<<<nblk(a.n_scen, 128), 128, 0, s>>>(a);
@@ -2928,9 +2944,9 @@ int init_kernels() {
                                      (int)forces_smem_bytes(body, v));
             int nb = 0;
             if (e == cudaSuccess)
-                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kForces[body][v],
-                                                                  kVariants[v].nt,
-                                                                  forces_smem_bytes(body, v));
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    &nb, kForces[body][v], kVariants[v].pairs ? GATHER_NT : kVariants[v].nt,
+                    forces_smem_bytes(body, v));
             if (e == cudaSuccess && dev >= 0 && dev < 64)
                 g_forces_blocks[dev][body][v] = (nb > 0 ? nb : 1) * sms;
         }
@@ -3006,7 +3022,7 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
     int blocks = (int)std::min<long long>((threads + v.nt - 1) / v.nt, resident);
     int nt = v.nt;
     if (v.pairs) {                                       // gather: one lane per slot, full grid
-        nt = 32;
+        nt = GATHER_NT;
         blocks = nblk(a.n, nt);
     }
     if (!v.pairs) cudaMemsetAsync(a.work, 0, sizeof(int), s);     // the gather zeroes it itself
