@@ -87,6 +87,7 @@ struct cd_ctx {
     int *fw_cnt = nullptr, *fw_off = nullptr, *fw_scan = nullptr;
     int *fs_cnt = nullptr, *fs_off = nullptr, *fs_scan = nullptr;
     int2 *fw_pairs = nullptr;
+    int *defer_list = nullptr;                     // ThreeCircle: the float32 pass's leftovers
     int64_t nl_cap = 0;
     bool nl_fixed = false;              // capacity set by cd_set_near_list_capacity
 
@@ -185,6 +186,7 @@ StepArgs args_of(cd_ctx *c, int nodes) {
     a.fw_cnt = c->fw_cnt;
     a.fw_off = c->fw_off;
     a.fw_pairs = c->fw_pairs;
+    a.defer_list = c->defer_list;
     a.fw_scan = c->fw_scan;
     a.fs_cnt = c->fs_cnt;
     a.fs_off = c->fs_off;
@@ -209,7 +211,7 @@ void release(cd_ctx *c) {
                     c->noise_f, c->noise_m, c->vmax, c->v0max, c->dt, c->time_tot,
                     c->err, c->work, c->diag, c->aos, c->nl_cnt, c->nl_off, c->nl_fwd,
                     c->nl_scan, c->nl_idx, c->nl_res, c->nl_kind, c->fw_cnt, c->fw_off, c->fw_scan,
-                    c->fw_pairs, c->ext, c->max_partial, c->tgt, c->navmap, c->rng_step,
+                    c->fw_pairs, c->defer_list, c->ext, c->max_partial, c->tgt, c->navmap, c->rng_step,
                     c->states, c->herd, c->scen_h, c->counters, c->reached, c->polys,
                     c->poly_off, c->fs_cnt, c->fs_off, c->fs_scan, c->nl_mask, c->nl_nch,
                     c->fix_count, c->fix_list, c->slot_of, c->pro};
@@ -346,7 +348,7 @@ int64_t kernels_per_step(const cd_ctx *c, int nodes) {
     k += cdk::scan_launches_single((int)c->ncells);
     if (cdk::variant_pairs(c->variant) && c->nl_cnt) k += 2;     // prologue, float64 staging
     if (cdk::variant_pairs(c->variant) && (nodes & CD_NODE_AGENT_AGENT) && c->nl_cnt)
-        k += 5;                                   // count, scans, fill, pairs, fallback
+        k += 5 + (c->defer_list ? 1 : 0);         // count, scans, fill, (float32 pass,) pairs, fallback
     return k;
 }
 
@@ -358,6 +360,8 @@ int alloc_near_lists(cd_ctx *c, int64_t cap) {
     if (c->nl_res) cudaFree(c->nl_res);
     if (c->nl_kind) cudaFree(c->nl_kind);
     if (c->fw_pairs) cudaFree(c->fw_pairs);
+    if (c->defer_list) cudaFree(c->defer_list);
+    c->defer_list = nullptr;
     c->nl_idx = nullptr;
     c->nl_res = nullptr;
     c->nl_kind = nullptr;
@@ -369,6 +373,8 @@ int alloc_near_lists(cd_ctx *c, int64_t cap) {
         if (int rc = dalloc(c, &c->nl_res, cap * res_d)) return rc;
         if (int rc = dalloc(c, &c->nl_kind, cap)) return rc;
         if (int rc = dalloc(c, &c->fw_pairs, cap)) return rc;
+        if (c->body == CD_BODY_THREE_CIRCLE)
+            if (int rc = dalloc(c, &c->defer_list, cap)) return rc;
     }
     c->nl_cap = cap;
     if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; c->graph_nodes = -1; }
@@ -653,7 +659,7 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->dt, n_scenarios));
     step(dalloc(c, &c->time_tot, n_scenarios));
     step(dalloc(c, &c->err, 1));
-    step(dalloc(c, &c->work, 1));
+    step(dalloc(c, &c->work, 2));
     step(dalloc(c, &c->diag, (int64_t)CD_COUNT_COLS * n));
     step(dalloc(c, &c->nl_cnt, n + 1));
     step(dalloc(c, &c->nl_off, n + 1));

@@ -83,7 +83,8 @@ struct StepArgs {
     const double *v0max;         // per scenario max target_velocity
     double *dt, *time_tot;       // per scenario
     int *err;
-    int *work;                   // force-kernel work counter (zeroed per launch)
+    int *work;                   // [0] force-kernel work counter (zeroed per launch),
+                                 // [1] pairs the float32 pair pass left to k_pairs
     int *fix_count, *fix_list;   // agents the gather leaves to k_forces_fallback
     int *slot_of;                // per agent: its cell-sorted slot (k_rank)
     double *pro;                 // per agent PRO_D doubles: prologue fx, fy, torque, phi0;
@@ -102,6 +103,8 @@ struct StepArgs {
     int *nl_scan;                // scan scratch for n counts
     int *fw_cnt, *fw_off;        // per slot: entries with a later slot (n + 1 each)
     int2 *fw_pairs;              // flat list of (slot, entry) for those entries
+    int *defer_list;             // flat-list indices the float32 pair pass left to k_pairs
+                                 // (nl_cap entries; ThreeCircle contexts, else null)
     int *fw_scan;                // scan scratch
     int *fs_cnt, *fs_off;        // per agent: those guessed to need the social force, scan
     int *fs_scan;                // scan scratch

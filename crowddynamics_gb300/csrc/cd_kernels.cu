@@ -816,6 +816,7 @@ __device__ __forceinline__ void pair_circular_me(const Circ &A, const Circ &B, d
 // Outcome of a pair evaluation: not interacting, interacting without a force
 // on either side (each side's torque a signed zero), or with a force.
 constexpr int RES_NONE = 0, RES_ZERO = 1, RES_FORCE = 2;
+constexpr int RES_DEFER = 3;                // tc_pair_light: float64 needed
 
 // Both forces of a Circular pair (interactions.py:51-70) with P = A the
 // first agent of the pair (the lower cell-sorted slot) and Q = B: each side
@@ -1523,6 +1524,88 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
     return RES_FORCE;
 }
 
+// The float32 part of tc_pair_both alone, for a pair (s, t): RES_NONE or
+// RES_ZERO where its certificates decide the pair (no contact, no positive
+// time to collision; the same tests and margins, so the same decision), and
+// RES_DEFER where tc_pair_both would need float64 (the exact distance, the
+// roots, a zero relative speed).  Reads 96 bytes of pre-check records and
+// the two velocities; holds no float64 geometry.
+__device__ __forceinline__ int tc_pair_light(const StepArgs &a, int s, int t) {
+    const float4 meC = __ldg(&a.cull[s]), meF0 = __ldg(&a.stage_f[2 * s]),
+                 meF1 = __ldg(&a.stage_f[2 * s + 1]);
+    const float4 oC = __ldg(&a.cull[t]), oF0 = __ldg(&a.stage_f[2 * t]),
+                 oF1 = __ldg(&a.stage_f[2 * t + 1]);
+    const float dxt = (meC.x - oC.x) + (meF0.x - oF0.x);
+    const float dyt = (meC.y - oC.y) + (meF0.y - oF0.y);
+    const float mox[3] = {0.f, meF1.x, meF1.z}, moy[3] = {0.f, meF1.y, meF1.w};
+    const float oox[3] = {0.f, oF1.x, oF1.z}, ooy[3] = {0.f, oF1.y, oF1.w};
+    const float mr[3] = {meF0.z, meF0.w, meF0.w}, orr[3] = {oF0.z, oF0.w, oF0.w};
+    // distance bounds (torso pair above, enclosing circles below), then the
+    // pre-selection's single candidate
+    const float xe2 = dxt * dxt + dyt * dyt;
+    const float xe = sqrtf(xe2);
+    const float re = meC.z + oC.z;
+    const float dmarg = PRESEL_MARGIN +
+                        1e-6f * (fabsf(dxt) + fabsf(dyt) + fabsf(mox[1]) + fabsf(moy[1]) +
+                                 fabsf(mox[2]) + fabsf(moy[2]) + fabsf(oox[1]) + fabsf(ooy[1]) +
+                                 fabsf(oox[2]) + fabsf(ooy[2]) + mr[0] + mr[1] + orr[0] + orr[1]);
+    const float h_lo = xe - re, h_hi = xe - (mr[0] + orr[0]);
+    if (h_lo - dmarg >= (float)SIGTH_SOC) return RES_NONE;
+    if (!(h_hi + dmarg < (float)SIGTH_SOC && h_lo - dmarg > 0.f)) {
+        const TcPre pre = tc_presel(dxt, dyt, mox, moy, oox, ooy, mr, orr, true);
+        const bool unique = (pre.seq & (pre.seq - 1u)) == 0u;
+        const bool far_cert = pre.hmin - pre.margin >= (float)SIGTH_SOC;
+        const bool near_cert =
+            pre.hmin + pre.margin < (float)SIGTH_SOC && pre.hmin - pre.margin > 0.f;
+        if (!(unique && (far_cert || near_cert))) return RES_DEFER;
+        if (!near_cert) return RES_NONE;
+    }
+    // interacting without contact: a force only from a positive time to
+    // collision (the relative velocity as tc_pair_both forms it)
+    const double2 vp = __ldg(&a.stage[(size_t)s * STAGE_Q_TC + 3]);
+    const double2 vq = __ldg(&a.stage[(size_t)t * STAGE_Q_TC + 3]);
+    const float vxf = (float)(vp.x - vq.x), vyf = (float)(vp.y - vq.y);
+    if (!(fabsf(vxf) > 1e-20f || fabsf(vyf) > 1e-20f)) return RES_DEFER;
+    const float af = vxf * vxf + vyf * vyf;
+    const float e0 = 1e-6f * (1.f + fabsf(dxt) + fabsf(dyt) + fabsf(mox[1]) + fabsf(moy[1]) +
+                              fabsf(mox[2]) + fabsf(moy[2]) + fabsf(oox[1]) + fabsf(ooy[1]) +
+                              fabsf(oox[2]) + fabsf(ooy[2]));
+    {
+        const float be = -(dxt * vxf + dyt * vyf);
+        const float ce = xe2 - re * re;
+        const float mbe = 4.f * e0 * (fabsf(vxf) + fabsf(vyf)) +
+                          1e-6f * (fabsf(dxt * vxf) + fabsf(dyt * vyf));
+        const float mce = 8.f * e0 * (fabsf(dxt) + fabsf(dyt) + re) + 1e-6f * (xe2 + re * re);
+        const float bbe = fabsf(be) + mbe;
+        if (ce - mce > 0.f && (be + mbe <= 0.f || bbe * bbe < 0.99f * af * (ce - mce)))
+            return RES_ZERO;                             // enclosing circles apart for t > 0
+    }
+    // the first sub-pair (visiting order) that may have a root decides:
+    // a certainly negative first root, no force; anything else, float64
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        const int i = k / 3, j = k % 3;
+        const float dx = (dxt + mox[i]) - oox[j], dy = (dyt + moy[i]) - ooy[j];
+        const float rt = mr[i] + orr[j];
+        const float bf = -(dx * vxf + dy * vyf);
+        const float x2 = dx * dx + dy * dy;
+        const float cf = x2 - rt * rt;
+        const float acf = af * cf;
+        const float discf = bf * bf - acf;
+        const float m = 1e-5f * af * (1.f + x2 + rt * rt) + 1e-6f * (bf * bf + fabsf(acf));
+        if (discf < -m) continue;
+        if (!(discf > m)) return RES_DEFER;
+        const float mb = 4.f * e0 * (fabsf(vxf) + fabsf(vyf)) +
+                         1e-6f * (fabsf(dx * vxf) + fabsf(dy * vyf));
+        const float mc = 8.f * e0 * (fabsf(dx) + fabsf(dy) + rt) + 1e-6f * (x2 + rt * rt);
+        const float bb = (fabsf(bf) + mb) * (fabsf(bf) + mb);
+        if (bf < -mb) return RES_ZERO;
+        if (cf < -mc && 0.99f * af * (-cf - mc) > 1e-9f * bb) return RES_ZERO;
+        return RES_DEFER;
+    }
+    return RES_ZERO;                                     // no sub-pair has a root
+}
+
 // Resumable candidate enumeration into the thread's list (visiting order:
 // 3 x 3 cells in (dx, dy) lexicographic order, each cell ascending).
 struct EnumState { int ck, t; };
@@ -2070,7 +2153,10 @@ __global__ void __launch_bounds__(NTG) k_nl_count(StepArgs a) {
 template <int L>
 __global__ void __launch_bounds__(NTG) k_nl_fill(StepArgs a) {
     pdl_enter();
-    if (blockIdx.x == 0 && threadIdx.x == 0) *a.work = 0;   // k_pairs' work counter
+    if (blockIdx.x == 0 && threadIdx.x == 0) {     // k_pairs' work counter, pairs deferred
+        a.work[0] = 0;
+        a.work[1] = 0;
+    }
     if (a.nl_off[a.n] > a.nl_cap) return;                 // over capacity: fallback
     constexpr unsigned GMASK = (1u << L) - 1u;
     const int lane = threadIdx.x & 31;
@@ -2212,16 +2298,61 @@ __device__ __forceinline__ void put_pair(const StepArgs &a, int e, int res, doub
     a.nl_kind[e] = kind;
 }
 
+// ThreeCircle bodies: the pairs of the flat list's second part (not guessed
+// to need the social force), in float32 alone (tc_pair_light): a decided
+// pair writes the kind bytes of both its entries; the others are appended
+// to defer_list for k_pairs, which takes them after the first part.  Few
+// registers, so many warps per SM hide the loads.  Warps take 32
+// consecutive pairs at a time, in turn.
+__global__ void __launch_bounds__(NTG) k_pairs_light(StepArgs a) {
+    pdl_enter();
+    constexpr unsigned FULL = 0xffffffffu;
+    if (a.nl_off[a.n] > a.nl_cap) return;
+    const int lane = threadIdx.x & 31;
+    const int k0 = a.fs_off[a.n], npairs = a.fw_off[a.n];
+    const int warps = gridDim.x * (NTG / 32);
+    for (int base = k0 + (blockIdx.x * (NTG / 32) + (threadIdx.x >> 5)) * 32; base < npairs;
+         base += warps * 32) {
+        const int k = base + lane;
+        int res = RES_NONE, s = 0, e = 0, t = 0;
+        if (k < npairs) {
+            const int2 pe = __ldg(&a.fw_pairs[k]);
+            s = pe.x;
+            e = pe.y;
+            t = __ldg(&a.nl_idx[e]);
+            res = tc_pair_light(a, s, t);
+        }
+        const unsigned dm = __ballot_sync(FULL, k < npairs && res == RES_DEFER);
+        if (dm) {
+            int d0 = 0;
+            if (lane == 0) d0 = atomicAdd(a.work + 1, __popc(dm));
+            d0 = __shfl_sync(FULL, d0, 0);
+            if ((dm >> lane) & 1u) a.defer_list[d0 + __popc(dm & ((1u << lane) - 1u))] = k;
+        }
+        if (k < npairs && res != RES_DEFER) {
+            put_pair(a, e, res, 0.0, 0.0, 0.0);
+            const int eq = partner_entry(a, t, s);
+            if (eq >= 0) put_pair(a, eq, res, 0.0, 0.0, 0.0);
+            else atomicOr(a.err, ERR_NEAR_LIST);
+        }
+    }
+}
+
 // Every pair of the flat list once: warps claim 32 consecutive pairs at a
 // time (consecutive pairs mostly share their first agent).
 template <int BODY>
 __global__ void __launch_bounds__(NTG, 4) k_pairs(StepArgs a) {
+    pdl_enter();
     constexpr unsigned FULL = 0xffffffffu;
     if (a.nl_off[a.n] > a.nl_cap) return;
     extern __shared__ unsigned char smem[];
     PairQueue *wq = reinterpret_cast<PairQueue *>(smem);
     const int lane = threadIdx.x & 31;
-    const int npairs = a.fw_off[a.n];
+    // after k_pairs_light (ThreeCircle): the first part, then the pairs the
+    // float32 pass left
+    const bool split = BODY == 1 && a.defer_list != nullptr;
+    const int nfirst = split ? a.fs_off[a.n] : a.fw_off[a.n];
+    const int npairs = split ? nfirst + a.work[1] : nfirst;
     // the next chunk's pair and partner are loaded before this chunk is
     // evaluated, so that their load latency overlaps its work
     auto claim = [&](int &s_, int &e_, int &t_) {
@@ -2231,7 +2362,8 @@ __global__ void __launch_bounds__(NTG, 4) k_pairs(StepArgs a) {
         const int k_ = chunk * 32 + lane;
         s_ = 0; e_ = 0; t_ = 0;
         if (k_ < npairs) {
-            const int2 pe = __ldg(&a.fw_pairs[k_]);
+            const int kk = k_ < nfirst ? k_ : __ldg(&a.defer_list[k_ - nfirst]);
+            const int2 pe = __ldg(&a.fw_pairs[kk]);
             s_ = pe.x;
             e_ = pe.y;
             t_ = __ldg(&a.nl_idx[e_]);
@@ -2933,6 +3065,7 @@ int variant_staged(int variant) {
 // Resident blocks of each force kernel variant (and pair kernel) on each device.
 int g_forces_blocks[64][2][N_VARIANTS];
 int g_pairs_blocks[64][2][N_PAIR_L];
+int g_light_blocks[64];
 
 int init_kernels() {
     int dev = 0, sms = 0;
@@ -2967,6 +3100,11 @@ int init_kernels() {
             if (e == cudaSuccess && dev >= 0 && dev < 64)
                 g_pairs_blocks[dev][body][l] = (nb > 0 ? nb : 1) * sms;
         }
+    if (e == cudaSuccess) {
+        int nb = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pairs_light, NTG, 0);
+        if (e == cudaSuccess && dev >= 0 && dev < 64) g_light_blocks[dev] = (nb > 0 ? nb : 1) * sms;
+    }
     return e == cudaSuccess ? 0 : (int)e;
 }
 
@@ -3012,8 +3150,14 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
         // at most one warp per 32 pairs (about 16 pairs per agent): enough blocks
         if (pro && stage_deferred && fork) cudaStreamWaitEvent(s, fork->join_stage, 0);
         if (pair_ev) cudaEventRecordWithFlags(pair_ev[0], s, captured ? cudaEventRecordExternal : 0);
-        kPairs[body]<<<std::min(nblk((long long)a.n * 16, NTG), rp), NTG, pairs_smem_bytes(body),
-                       s>>>(a);
+        if (body == 1 && a.defer_list) {
+            int rl = (dev >= 0 && dev < 64) ? g_light_blocks[dev] : 0;
+            if (rl <= 0) rl = 152;
+            k_pairs_light<<<std::min(nblk((long long)a.n * 16, NTG), rl), NTG, 0, s>>>(a);
+        }
+        // after k_pairs_light: chained to it
+        launch_k(body == 1 && a.defer_list, kPairs[body],
+                 std::min(nblk((long long)a.n * 16, NTG), rp), NTG, pairs_smem_bytes(body), s, a);
         if (pair_ev) cudaEventRecordWithFlags(pair_ev[1], s, captured ? cudaEventRecordExternal : 0);
     }
     int resident = (dev >= 0 && dev < 64) ? g_forces_blocks[dev][body][variant] : 0;
