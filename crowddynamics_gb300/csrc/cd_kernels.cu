@@ -2339,9 +2339,11 @@ __global__ void __launch_bounds__(NTG) k_pairs_light(StepArgs a) {
 }
 
 // Every pair of the flat list once: warps claim 32 consecutive pairs at a
-// time (consecutive pairs mostly share their first agent).
+// time (consecutive pairs mostly share their first agent).  Three blocks per
+// SM (156 registers, none spilled): after the float32 pass most of its pairs
+// take the float64 paths, which run faster unspilled than at four blocks.
 template <int BODY>
-__global__ void __launch_bounds__(NTG, 4) k_pairs(StepArgs a) {
+__global__ void __launch_bounds__(NTG, 3) k_pairs(StepArgs a) {
     pdl_enter();
     constexpr unsigned FULL = 0xffffffffu;
     if (a.nl_off[a.n] > a.nl_cap) return;
