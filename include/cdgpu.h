@@ -119,7 +119,9 @@ void cd_destroy(cd_ctx *ctx);
 /* Copy `n` (= total agents) packed host records of `itemsize` bytes into the
  * device.  `field_offsets` holds CD_F_COUNT byte offsets (-1 = absent);
  * float64 fields must be 4-byte aligned; the integer and bool fields
- * (CD_F_TARGET and after) may sit at any offset.  Recomputes timestep maxima. */
+ * (CD_F_TARGET and after) may sit at any offset.  Recomputes timestep maxima.
+ * Returns once the records have been read: the caller may then reuse them.
+ * The per-scenario maxima are computed behind that on the context stream. */
 int cd_upload_agents(cd_ctx *ctx, const void *records, int64_t n,
                      int64_t itemsize, const int64_t *field_offsets);
 /* Write the device state back into `n` packed host records.  Whole records
