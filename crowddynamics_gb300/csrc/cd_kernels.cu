@@ -953,7 +953,7 @@ __device__ __forceinline__ bool tc_pair_eval(const TC &A, const float4 meC, cons
     // exact float64 minimum over the candidates, first in visiting order wins
     double h_min = __longlong_as_double(0x7ff8000000000000LL);
     double sdx = 0.0, sdy = 0.0, sd = 0.0;
-    int mine_min = 0, theirs_min = 0;
+    int mine_min = 0;
     {
         int k = __ffs(seq) - 1;
         unsigned rest = seq & (seq - 1);
@@ -962,7 +962,7 @@ __device__ __forceinline__ bool tc_pair_eval(const TC &A, const float4 meC, cons
         double dx = sel3(A.x, mi) - sel3(B.x, ti), dy = sel3(A.y, mi) - sel3(B.y, ti);
         double d = cdm_hypot(dx, dy);
         h_min = d - (part_r(A, mi) + part_r(B, ti));
-        sdx = dx; sdy = dy; sd = d; mine_min = mi; theirs_min = ti;
+        sdx = dx; sdy = dy; sd = d; mine_min = mi;
         while (rest) {
             k = __ffs(rest) - 1;
             rest &= rest - 1;
@@ -972,7 +972,7 @@ __device__ __forceinline__ bool tc_pair_eval(const TC &A, const float4 meC, cons
             d = cdm_hypot(dx, dy);
             double h = d - (part_r(A, mi) + part_r(B, ti));
             if (h < h_min || isnan(h_min)) {
-                h_min = h; sdx = dx; sdy = dy; sd = d; mine_min = mi; theirs_min = ti;
+                h_min = h; sdx = dx; sdy = dy; sd = d; mine_min = mi;
             }
         }
     }
@@ -2646,7 +2646,6 @@ __global__ void k_pair_counts(StepArgs a, int *out) {
             int w = all_walls ? q : a.wall_idx[q];
             if (wall_far(me.x, me.y, me.z, a.walls_f[w])) continue;
             ++wn;
-            double fx = 0, fy = 0, tq = 0;
             if (a.body == 0) {
                 const Circ A = load_circ(a.stage, s);
                 double nx, ny;
@@ -2662,7 +2661,6 @@ __global__ void k_pair_counts(StepArgs a, int *out) {
                 }
                 wc += h_min < 0;
             }
-            (void)fx; (void)fy; (void)tq;
         }
     }
     int *o = out + (size_t)i * COUNT_COLS;
