@@ -17,6 +17,7 @@ from crowddynamics_gb300.simulation.agents import (
 from crowddynamics_gb300.simulation.agents import field_offsets as _field_offsets
 
 _OFFSETS = {}
+_OFFSET_PTRS = {}
 
 
 def field_offsets(dtype):
@@ -27,6 +28,15 @@ def field_offsets(dtype):
         off.flags.writeable = False
         _OFFSETS[dtype] = off
     return off
+
+
+def _offsets_arg(dtype):
+    """``field_offsets(dtype)`` as the C ABI's int64 pointer (made once per
+    dtype; the table it points at is kept alive by the cache)."""
+    p = _OFFSET_PTRS.get(dtype)
+    if p is None:
+        p = _OFFSET_PTRS[dtype] = N.i64ptr(field_offsets(dtype))
+    return p
 
 
 def walls_as_rows(walls):
@@ -114,17 +124,17 @@ class DeviceBatch:
             raise InvalidType('agent dtype does not match the context body type')
         if not records.flags.c_contiguous:
             raise InvalidValue('agent array must be C-contiguous')
-        off = field_offsets(records.dtype)
-        self._offsets = off
-        self._chk(self._lib.cd_upload_agents(self._ctx, N.ptr(records), len(records),
-                                             records.dtype.itemsize, N.i64ptr(off)))
+        self._offsets = field_offsets(records.dtype)
+        self._chk(self._lib.cd_upload_agents(self._ctx, records.ctypes.data, len(records),
+                                             records.dtype.itemsize,
+                                             _offsets_arg(records.dtype)))
 
     def download(self, records):
         if not records.flags.c_contiguous or not records.flags.writeable:
             raise InvalidValue('agent array must be C-contiguous and writeable')
-        off = field_offsets(records.dtype)
-        self._chk(self._lib.cd_download_agents(self._ctx, N.ptr(records), len(records),
-                                               records.dtype.itemsize, N.i64ptr(off)))
+        self._chk(self._lib.cd_download_agents(self._ctx, records.ctypes.data, len(records),
+                                               records.dtype.itemsize,
+                                               _offsets_arg(records.dtype)))
 
     def snapshot(self, slot, records, dt=None, time_tot=None):
         """Enqueue an asynchronous copy of the state (after the steps already
