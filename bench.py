@@ -434,6 +434,11 @@ def run_ours(args, ws, rank, local):
                                 'sample': '%d steps of the full %d-agent workload, C restatement '
                                           'of the reference algorithm, OpenMP over %d threads'
                                           % (steps, n, nthreads)}
+        # one thread: the reference's own functions run serially
+        el1 = cpu_sample(scen, ORC_NODES, 1, 1)
+        line['cpu_baseline']['single_thread'] = {
+            'value': n / el1, 'unit': UNIT, 'cores': 1,
+            'sample': '1 step of the full %d-agent workload on one thread' % n}
     print(json.dumps(line), flush=True)
     b.close()
     if dist is not None:
