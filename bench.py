@@ -364,6 +364,17 @@ def run_ours(args, ws, rank, local):
         m = re.search(r'^%s FP64 pipe active: ([\d.]+)' % kernel, text, re.M)
         pipe = float(m.group(1)) / 100 if m else None
 
+    # the HBM side of the roofline: the state read and written once per step
+    # and the cell list (ThreeCircle: 29 float64 read, 13 written with the
+    # shoulders; Circular: 19 and 6; cell list 24 B), against the measured copy
+    # bandwidth
+    hbm_peak = None
+    ppath = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(ppath):
+        hbm_peak = json.load(open(ppath)).get('hbm_gbs')
+    bytes_agent = (29 + 13) * 8 + 24 if scen.body == 'three_circle' else (19 + 6) * 8 + 24
+    hbm_gbs = value * bytes_agent / 1e9
+
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -383,6 +394,10 @@ def run_ours(args, ws, rank, local):
             'roofline': {'bound': 'fp64', 'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s',
                          'frac': achieved / peak, 'traffic': traffic,
                          'kernel': label, 'kernel_ms': kernel_ms,
+                         'hbm': {'bytes_per_agent_step': bytes_agent, 'achieved': hbm_gbs,
+                                 'peak': hbm_peak, 'unit': 'GB/s',
+                                 'frac': hbm_gbs / hbm_peak if hbm_peak else None,
+                                 'peak_source': 'MEASURED_PEAKS.json hbm_gbs (copy)'},
                          'flops_per_launch': kreq,
                          'peak_source': 'measured live: FP64 FMA chain kernel (2 flops per FMA)',
                          # achieved counts the float64 operations whose
