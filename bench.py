@@ -315,6 +315,7 @@ def run_ours(args, ws, rank, local):
     value = whole_job_rate(ws, n, args.steps, run_ms / 1e3)
     force_ms = kt['force_ms'] / max(kt['force_launches'], 1)
     pair_ms = kt['pair_ms'] / max(kt['pair_launches'], 1) if kt['pair_launches'] else None
+    split = b.pair_split() if pair_ms else None     # the last timed step's flat list
     counts1 = b.pair_counts()
     flops = 0.5 * (algorithmic_flops(scen, counts0) + algorithmic_flops(scen, counts1))
     flops_req = 0.5 * (algorithmic_flops_required(scen, counts0) +
@@ -393,7 +394,7 @@ def run_ours(args, ws, rank, local):
             'gpu_launches': b.kernels_per_step(nodes) * args.steps,
             'roofline': {'bound': 'fp64', 'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s',
                          'frac': achieved / peak, 'traffic': traffic,
-                         'kernel': label, 'kernel_ms': kernel_ms,
+                         'kernel': label, 'kernel_ms': kernel_ms, 'pair_split': split,
                          'hbm': {'bytes_per_agent_step': bytes_agent, 'achieved': hbm_gbs,
                                  'peak': hbm_peak, 'unit': 'GB/s',
                                  'frac': hbm_gbs / hbm_peak if hbm_peak else None,

@@ -1304,6 +1304,22 @@ int cd_pair_kernel_time(cd_ctx *c, double *ms, int64_t *launches) {
     return CD_OK;
 }
 
+int cd_pair_split(cd_ctx *c, int64_t *pairs, int64_t *first_part, int64_t *deferred) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    int v[3] = {0, 0, 0};
+    if (c->n > 0 && c->nl_cap > 0) {
+        CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+        CUDA_OR_FAIL(c, cudaMemcpy(&v[0], c->fw_off + c->n, sizeof(int), cudaMemcpyDeviceToHost));
+        CUDA_OR_FAIL(c, cudaMemcpy(&v[1], c->fs_off + c->n, sizeof(int), cudaMemcpyDeviceToHost));
+        if (c->defer_list)
+            CUDA_OR_FAIL(c, cudaMemcpy(&v[2], c->work + 1, sizeof(int), cudaMemcpyDeviceToHost));
+    }
+    if (pairs) *pairs = v[0];
+    if (first_part) *first_part = v[1];
+    if (deferred) *deferred = v[2];
+    return CD_OK;
+}
+
 int cd_kernel_time(cd_ctx *c, double *force_ms, int64_t *force_launches, double *step_ms,
                    double *run_ms, int64_t *run_steps) {
     if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");

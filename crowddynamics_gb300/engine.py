@@ -331,6 +331,13 @@ class DeviceBatch:
                     run_ms=r.value, run_steps=rn.value, pair_ms=pm.value,
                     pair_launches=pn.value)
 
+    def pair_split(self):
+        """The last pair-pipeline step's flat pair list: dict(pairs,
+        first_part, deferred) (see cd_pair_split)."""
+        v = [ctypes.c_int64() for _ in range(3)]
+        self._chk(self._lib.cd_pair_split(self._ctx, *[ctypes.byref(x) for x in v]))
+        return dict(pairs=v[0].value, first_part=v[1].value, deferred=v[2].value)
+
     def kernels_per_step(self, nodes=N.NODE_ALL):
         k = ctypes.c_int64()
         self._chk(self._lib.cd_kernels_per_step(self._ctx, int(nodes), ctypes.byref(k)))

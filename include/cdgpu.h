@@ -257,6 +257,11 @@ int cd_kernel_time(cd_ctx *ctx, double *force_ms, int64_t *force_launches,
 /* Time and launches of the pair kernel alone (pair-pipeline variants, steps
  * with agent-agent), accumulated like cd_kernel_time. */
 int cd_pair_kernel_time(cd_ctx *ctx, double *ms, int64_t *launches);
+/* The last pair-pipeline step's flat pair list: its pairs, those in its
+ * first part (guessed to need the social force) and, for ThreeCircle
+ * contexts, those the float32 pass left to the float64 pair kernel (zeros
+ * when no near lists are in use).  Waits for the context stream. */
+int cd_pair_split(cd_ctx *ctx, int64_t *pairs, int64_t *first_part, int64_t *deferred);
 /* Number of kernels one step with `nodes` launches (memsets excluded). */
 int cd_kernels_per_step(const cd_ctx *ctx, int nodes, int64_t *kernels);
 

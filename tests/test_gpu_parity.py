@@ -528,6 +528,30 @@ def test_large_field_forces(oracle, native):
     assert_vec_close(got['torque'], ref['torque'], RTOL, ATOL, 'torque')
 
 
+@pytest.mark.parametrize('speed', [0.0, 1.0, 3.0])
+def test_pair_split(oracle, native, speed):
+    """The flat pair list's split after a ThreeCircle pair-pipeline step: the
+    first part and the pairs the float32 pass deferred are within the list
+    (with all agents at rest no pair is guessed, and every interacting pair
+    has zero relative speed, which the float32 pass defers), and the step
+    matches the oracle bit for bit."""
+    scen = crowded(21, speed)
+    b, agents, _ = batch_from_scenarios([scen])
+    b.set_variant(10)
+    nodes = N.NODE_ALL & ~N.NODE_FLUCTUATION
+    b.step(nodes)
+    sp = b.pair_split()
+    got = agents.copy()
+    b.download(got)
+    b.close()
+    assert sp['pairs'] > 0
+    assert 0 <= sp['first_part'] <= sp['pairs']
+    assert 0 <= sp['deferred'] <= sp['pairs'] - sp['first_part']
+    if speed == 0.0:
+        assert sp['first_part'] == 0 and sp['deferred'] > 0
+    assert_identical(got, oracle_step(oracle, scen, nodes, exact=True)[0], 'split')
+
+
 def test_deterministic(native):
     scen = S.room()
     outs = []
