@@ -2106,38 +2106,54 @@ __global__ void __launch_bounds__(NTG) k_nl_count(StepArgs a) {
     const int r = lane & (L - 1), g0 = lane & ~(L - 1);
     const unsigned gm = GMASK << g0;
     const int s = (int)(((long long)blockIdx.x * NTG + threadIdx.x) / L);
-    if (s >= a.n) return;                                 // whole groups leave together
-    const int i = a.perm[s];
-    const ScenDev sc = a.scen[a.scen_of[i]];
-    const float4 me = a.cull[s];
-    int rb[3], re[3];
-    candidate_runs(a, sc, a.key[i], rb, re);
+    const bool valid = s < a.n;                           // whole groups
+    float4 me = make_float4(0.f, 0.f, 0.f, 0.f);
+    int rb[3] = {0, 0, 0}, re[3] = {0, 0, 0};
+    if (valid) {
+        const int i = a.perm[s];
+        const ScenDev sc = a.scen[a.scen_of[i]];
+        me = a.cull[s];
+        candidate_runs(a, sc, a.key[i], rb, re);
+    }
+    // The group's chunks, run after run: the agents of one cell have the
+    // same runs, and the warp steps through the most chunks any of its groups
+    // has, so that its ballots take all 32 lanes without divergence.
+    const int n0 = (re[0] - rb[0] + CW - 1) / CW, n1 = (re[1] - rb[1] + CW - 1) / CW;
+    const int mine = n0 + n1 + (re[2] - rb[2] + CW - 1) / CW;
+    const int most = __reduce_max_sync(0xffffffffu, mine);
     // the group's mask row is staged in shared memory and written out whole
     __shared__ unsigned srow[(NTG / L) * NL_MASK_CHUNKS];
     unsigned *row = srow + (threadIdx.x / L) * NL_MASK_CHUNKS;
     int cnt = 0, fwd = 0, soc = 0, ch = 0;
+    for (int it = 0; it < most; ++it) {
+        const bool on = it < mine;
+        // run d of chunk `it` (selects, so that the runs stay in registers)
+        const bool r0 = it < n0, r1 = !r0 && it < n0 + n1;
+        const int base = (r0 ? rb[0] : (r1 ? rb[1] : rb[2])) +
+                         (it - (r0 ? 0 : (r1 ? n0 : n0 + n1))) * CW;
+        const int end = r0 ? re[0] : (r1 ? re[1] : re[2]);
+        unsigned nb = 0, sb = 0;
 #pragma unroll
-    for (int d = 0; d < 3; ++d)
-        for (int base = rb[d]; base < re[d]; base += CW) {
-            unsigned nb = 0, sb = 0;
-#pragma unroll
-            for (int c = 0; c < C; ++c) {
-                const int t = base + c * L + r;
-                bool near = false, guess = false;
-                if (t < re[d] && t != s) {
-                    const float4 o = __ldg(&a.cull[t]);
-                    near = !pair_far(me, o);
-                    if (near && t > s) guess = social_guess(me, o);
-                }
-                nb |= ((__ballot_sync(gm, near) >> g0) & GMASK) << (c * L);
-                sb |= ((__ballot_sync(gm, guess) >> g0) & GMASK) << (c * L);
+        for (int c = 0; c < C; ++c) {
+            const int t = base + c * L + r;
+            bool near = false, guess = false;
+            if (on && t < end && t != s) {
+                const float4 o = __ldg(&a.cull[t]);
+                near = !pair_far(me, o);
+                if (near && t > s) guess = social_guess(me, o);
             }
+            nb |= ((__ballot_sync(0xffffffffu, near) >> g0) & GMASK) << (c * L);
+            sb |= ((__ballot_sync(0xffffffffu, guess) >> g0) & GMASK) << (c * L);
+        }
+        if (on) {
             if (r == 0 && ch < NL_MASK_CHUNKS) row[ch] = nb | (sb << 16);
             ++ch;
             cnt += __popc(nb);
             fwd += __popc(nb & later_bits<L>(s, base));
             soc += __popc(sb);
         }
+    }
+    if (!valid) return;
     __syncwarp(gm);
     unsigned *mrow = a.nl_mask + (size_t)s * NL_MASK_CHUNKS;
     const int nst = ch < NL_MASK_CHUNKS ? ch : NL_MASK_CHUNKS;
