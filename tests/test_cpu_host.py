@@ -29,6 +29,32 @@ def test_library_exports_every_declared_symbol(native):
     assert set(declared) == set(native.SYMBOLS)
 
 
+def test_null_context_is_rejected(native):
+    """Every entry point that takes a context answers a NULL context with
+    CD_ERR_INVALID_VALUE and a message, before touching the device (so this
+    runs without a GPU); cd_destroy(NULL) does nothing."""
+    import ctypes
+    lib = native.load()
+    text = open(os.path.join(ROOT, 'include', 'cdgpu.h')).read()
+    text = re.sub(r'/\*.*?\*/', '', text, flags=re.S)
+    sigs = re.findall(r'\bint\s+(cd_[a-z0-9_]+)\s*\(([^)]*)\)', text)
+    checked = 0
+    for name, params in sigs:
+        params = [q.strip() for q in params.split(',') if q.strip()]
+        if not params or not re.match(r'(const )?cd_ctx \*ctx$', params[0]):
+            continue
+        f = getattr(lib, name)
+        args = [None]
+        for t in f.argtypes[1:]:
+            pointer = t in (ctypes.c_void_p, ctypes.c_char_p) or issubclass(t, ctypes._Pointer)
+            args.append(None if pointer else 0)
+        assert f(*args) == 2, name
+        assert lib.cd_last_error(None), name
+        checked += 1
+    assert checked >= 25
+    lib.cd_destroy(None)
+
+
 def test_status_codes_map_to_reference_exceptions(native, monkeypatch):
     from crowddynamics_gb300 import exceptions as E
 
