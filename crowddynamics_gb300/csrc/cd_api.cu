@@ -770,16 +770,18 @@ int cd_upload_agents(cd_ctx *c, const void *records, int64_t n, int64_t itemsize
         const void *dv = (c->direct_host && cdk::records_per_block(itemsize) > 0)
                              ? device_view_of_host(records, bytes)
                              : nullptr;
+        const cdk::StateOffsets so = state_offsets(off, itemsize);
         if (dv) {
-            cdk::launch_records_in(dv, c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
+            cdk::launch_records_in(dv, c->aos, itemsize, offl, (int)n, c->body, c->col, so,
+                                   state_cols(c), c->stream);
+            CUDA_OR_FAIL(c, cudaEventRecord(c->ev_read, c->stream));
         } else {
             CUDA_OR_FAIL(c, cudaMemcpyAsync(c->aos, records, bytes, cudaMemcpyHostToDevice,
                                             c->stream));
+            CUDA_OR_FAIL(c, cudaEventRecord(c->ev_read, c->stream));
             cdk::launch_aos_to_soa(c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
+            cdk::launch_states_in(c->aos, itemsize, so, (int)n, state_cols(c), c->stream);
         }
-        CUDA_OR_FAIL(c, cudaEventRecord(c->ev_read, c->stream));
-        cdk::launch_states_in(c->aos, itemsize, state_offsets(off, itemsize), (int)n,
-                              state_cols(c), c->stream);
         c->states_dirty = false;
     }
     StepArgs a = args_of(c, 0);

@@ -242,8 +242,10 @@ void launch_soa_to_aos(char *aos, long long itemsize, const long long *off,
 // records for the fields the step does not write).  0 records per block:
 // records too large for shared memory, use the staged path.
 int records_per_block(long long itemsize);
+// launch_records_in also fills the state columns (as launch_states_in).
 void launch_records_in(const void *src, char *aos, long long itemsize, const long long *off,
-                       int n, int body, double *const *col, cudaStream_t s);
+                       int n, int body, double *const *col, const StateOffsets &so,
+                       const StateCols &sc, cudaStream_t s);
 void launch_records_out(void *dst, const char *aos, long long itemsize, const long long *off,
                         int n, int body, const double *const *col, cudaStream_t s);
 double fp64_peak_gflops();

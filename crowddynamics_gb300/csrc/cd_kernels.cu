@@ -2773,6 +2773,35 @@ __global__ void k_soa_to_aos(char *aos, long long itemsize, OffTable off, int n,
     }
 }
 
+// Integer and bool state fields of the packed records (target, active,
+// is_leader, is_follower, index_leader, familiar_exit) sit at any byte offset
+// (target at 2 in the reference dtypes, after two bools): read and written
+// byte by byte, little-endian.
+__device__ __forceinline__ long long ld_int(const char *rec, long long off, int bytes) {
+    const unsigned char *p = reinterpret_cast<const unsigned char *>(rec + off);
+    unsigned long long v = 0;
+    for (int k = 0; k < bytes; ++k) v |= (unsigned long long)p[k] << (8 * k);
+    return (long long)v;
+}
+__device__ __forceinline__ void st_int(char *rec, long long off, int bytes, long long v) {
+    unsigned char *p = reinterpret_cast<unsigned char *>(rec + off);
+    for (int k = 0; k < bytes; ++k) p[k] = (unsigned char)((unsigned long long)v >> (8 * k));
+}
+__device__ __forceinline__ int clamp_index(long long t) {
+    return (t >= 0 && t <= 0x7fffffffLL) ? (int)t : -1;
+}
+
+// One record's state fields into the state columns (row i).
+__device__ __forceinline__ void states_of_record(const char *rec, const StateOffsets &o,
+                                                 const StateCols &c, int i) {
+    c.target[i] = o.target >= 0 ? clamp_index(ld_int(rec, o.target, 8)) : -1;
+    c.active[i] = o.active >= 0 ? (ld_int(rec, o.active, 1) != 0) : 1;
+    c.leader[i] = o.leader >= 0 ? (ld_int(rec, o.leader, 1) != 0) : 0;
+    c.follower[i] = o.follower >= 0 ? (ld_int(rec, o.follower, 1) != 0) : 0;
+    c.index_leader[i] = o.index_leader >= 0 ? clamp_index(ld_int(rec, o.index_leader, 8)) : -1;
+    c.familiar_exit[i] = o.familiar_exit >= 0 ? clamp_index(ld_int(rec, o.familiar_exit, 8)) : -1;
+}
+
 // Records moved straight between host memory the device can address (pinned,
 // on this Grace-Blackwell part over the chip-to-chip link) and the columns:
 // a block takes REC_BLOCK consecutive records, copies their 32-bit words with
@@ -2784,7 +2813,7 @@ struct XferTable { int n; int word[40]; int col[40]; };   // field word offset, 
 
 __global__ void __launch_bounds__(XFER_NT)
 k_records_in(const unsigned *__restrict__ src, unsigned *__restrict__ copy, int wpr, int per_block,
-             int n, XferTable t, ColPtrs cols) {
+             int n, XferTable t, ColPtrs cols, StateOffsets so, StateCols sc) {
     extern __shared__ __align__(16) unsigned rec_sm[];
     const int i0 = blockIdx.x * per_block;
     const int nrec = min(per_block, n - i0);
@@ -2824,6 +2853,9 @@ k_records_in(const unsigned *__restrict__ src, unsigned *__restrict__ copy, int 
         const unsigned *p = rec_sm + r * wpr + t.word[k];
         cols.p[t.col[k]][i0 + r] = __hiloint2double((int)p[1], (int)p[0]);
     }
+    // the integer and bool state fields, from the same shared copy
+    for (int r = threadIdx.x; r < nrec; r += XFER_NT)
+        states_of_record(reinterpret_cast<const char *>(rec_sm + r * wpr), so, sc, i0 + r);
 }
 
 __global__ void __launch_bounds__(XFER_NT)
@@ -2863,35 +2895,11 @@ k_records_out(unsigned *__restrict__ dst, const unsigned *__restrict__ base, int
     for (int w = done + threadIdx.x; w < words; w += XFER_NT) dst[w0 + w] = rec_sm[w];
 }
 
-// Integer and bool state fields of the packed records (target, active,
-// is_leader, is_follower, index_leader, familiar_exit) sit at any byte offset
-// (target at 2 in the reference dtypes, after two bools): read and written
-// byte by byte, little-endian.
-__device__ __forceinline__ long long ld_int(const char *rec, long long off, int bytes) {
-    const unsigned char *p = reinterpret_cast<const unsigned char *>(rec + off);
-    unsigned long long v = 0;
-    for (int k = 0; k < bytes; ++k) v |= (unsigned long long)p[k] << (8 * k);
-    return (long long)v;
-}
-__device__ __forceinline__ void st_int(char *rec, long long off, int bytes, long long v) {
-    unsigned char *p = reinterpret_cast<unsigned char *>(rec + off);
-    for (int k = 0; k < bytes; ++k) p[k] = (unsigned char)((unsigned long long)v >> (8 * k));
-}
-__device__ __forceinline__ int clamp_index(long long t) {
-    return (t >= 0 && t <= 0x7fffffffLL) ? (int)t : -1;
-}
-
 __global__ void k_states_in(const char *aos, long long itemsize, StateOffsets o, int n,
                             StateCols c) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const char *rec = aos + (size_t)i * itemsize;
-    c.target[i] = o.target >= 0 ? clamp_index(ld_int(rec, o.target, 8)) : -1;
-    c.active[i] = o.active >= 0 ? (ld_int(rec, o.active, 1) != 0) : 1;
-    c.leader[i] = o.leader >= 0 ? (ld_int(rec, o.leader, 1) != 0) : 0;
-    c.follower[i] = o.follower >= 0 ? (ld_int(rec, o.follower, 1) != 0) : 0;
-    c.index_leader[i] = o.index_leader >= 0 ? clamp_index(ld_int(rec, o.index_leader, 8)) : -1;
-    c.familiar_exit[i] = o.familiar_exit >= 0 ? clamp_index(ld_int(rec, o.familiar_exit, 8)) : -1;
+    states_of_record(aos + (size_t)i * itemsize, o, c, i);
 }
 
 // The state fields the state nodes change: target, index_leader, active,
@@ -3280,14 +3288,15 @@ static XferTable xfer_table(const long long *off, int body, bool outputs_only) {
 }
 
 void launch_records_in(const void *src, char *aos, long long itemsize, const long long *off,
-                       int n, int body, double *const *col, cudaStream_t s) {
+                       int n, int body, double *const *col, const StateOffsets &so,
+                       const StateCols &sc, cudaStream_t s) {
     const int per = records_per_block(itemsize);
     if (n <= 0 || per <= 0) return;
     ColPtrs c;
     for (int k = 0; k < NCOL; ++k) c.p[k] = col[k];
     k_records_in<<<nblk(n, per), XFER_NT, (size_t)per * itemsize, s>>>(
         static_cast<const unsigned *>(src), reinterpret_cast<unsigned *>(aos), (int)(itemsize / 4),
-        per, n, xfer_table(off, body, false), c);
+        per, n, xfer_table(off, body, false), c, so, sc);
 }
 
 void launch_records_out(void *dst, const char *aos, long long itemsize, const long long *off,
