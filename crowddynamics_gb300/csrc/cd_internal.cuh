@@ -92,7 +92,8 @@ struct StepArgs {
     // near lists (compute-once pair pipeline): per cell-sorted slot, the
     // slots of its near candidates in ascending order (= visiting order)
     int *nl_cnt;                 // n + 1 counts (scan input)
-    int *nl_off;                 // n + 1 offsets; nl_off[n] = entries needed
+    int *nl_off;                 // n + 1 offsets; nl_off[n] = entries needed (k_scan_tiles
+                                 // leaves tile-relative offsets, k_nl_fill the final ones)
     int *nl_fwd;                 // per slot: first entry with a later slot
     unsigned *nl_mask;           // per slot NL_MASK_CHUNKS chunk ballots (k_nl_count -> k_nl_fill)
     int *nl_nch;                 // per slot: its candidate chunks
@@ -100,14 +101,14 @@ struct StepArgs {
     double *nl_res;              // per entry: RES_D doubles of pair results (forces only)
     unsigned char *nl_kind;      // per entry: none / zero force (+0 or -0 torque) / force
     int nl_cap;
-    int *nl_scan;                // scan scratch for n counts
+    int *nl_scan;                // scan scratch: tile totals, tile offsets, a tile counter
     int *fw_cnt, *fw_off;        // per slot: entries with a later slot (n + 1 each)
     int2 *fw_pairs;              // flat list of (slot, entry) for those entries
     int *defer_list;             // flat-list indices the float32 pair pass left to k_pairs
                                  // (nl_cap entries; ThreeCircle contexts, else null)
-    int *fw_scan;                // scan scratch
+    int *fw_scan;                // scan scratch (as nl_scan)
     int *fs_cnt, *fs_off;        // per agent: those guessed to need the social force, scan
-    int *fs_scan;                // scan scratch
+    int *fs_scan;                // scan scratch (as nl_scan)
 };
 
 // Pair-result record of a near-list entry with a force: (fx, fy, torque, -);
