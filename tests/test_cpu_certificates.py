@@ -246,6 +246,26 @@ def edge_population(n_pairs, seed):
     return a, p, q
 
 
+def near_list_far(a, p, q):
+    """pair_far: the near lists' float32 cull (torso centres' hi parts, the
+    extent bounds, 1 cm of margin)."""
+    R = precheck_records(a)
+    dx = R['xh'][p] - R['xh'][q]
+    dy = R['yh'][p] - R['yh'][q]
+    lim = (R['ext'][p] + R['ext'][q]) + (SIGHT + F(0.01))
+    return dx * dx + dy * dy > lim * lim
+
+
+def test_near_list_cull_is_sound():
+    """A pair the near lists leave out never interacts."""
+    for seed in range(2):
+        a, p, q = edge_population(500_000, 10 + seed)
+        far = near_list_far(a, p, q)
+        inter, _ = reference_classes(a, p, q)
+        assert not (far & inter).any()
+        assert far.any() and (~far).any()
+
+
 def test_float32_pair_certificates_are_sound():
     total = decided = 0
     for seed in range(4):
