@@ -283,3 +283,138 @@ def test_float32_pair_certificates_are_sound():
     # quarter of the pairs (most pairs of a real crowd are far from every
     # edge: the float32 pass defers 436 of 1.83M on the 100k field)
     assert decided > 0.15 * total, decided / total
+
+
+def root_certificates(a, p, q):
+    """The float32 time-to-collision part of tc_pair_both for the pairs
+    (p[k], q[k]): the class of the first sub-pair that may have a root
+    (0 float64 decides, 1 certainly negative, 2 certainly positive), the
+    sub-pairs queued for float64 roots before and after the pruning of roots
+    that cannot be the least positive one (bit k: sub-pair k)."""
+    R = precheck_records(a)
+    g = lambda name, idx: R[name][idx]
+    dxt = (g('xh', p) - g('xh', q)) + (g('xl', p) - g('xl', q))
+    dyt = (g('yh', p) - g('yh', q)) + (g('yl', p) - g('yl', q))
+    zero = np.zeros_like(dxt)
+    mox = [zero, g('oxl', p), g('oxr', p)]
+    moy = [zero, g('oyl', p), g('oyr', p)]
+    oox = [zero, g('oxl', q), g('oxr', q)]
+    ooy = [zero, g('oyl', q), g('oyr', q)]
+    mr = [g('rt', p), g('rs', p), g('rs', p)]
+    orr = [g('rt', q), g('rs', q), g('rs', q)]
+    vp, vq = a['velocity'][p], a['velocity'][q]
+    vxf, vyf = (vp[:, 0] - vq[:, 0]).astype(F), (vp[:, 1] - vq[:, 1]).astype(F)
+    af = vxf * vxf + vyf * vyf
+    e0s = F(1.0) + np.abs(dxt)
+    for t in (np.abs(dyt), np.abs(mox[1]), np.abs(moy[1]), np.abs(mox[2]), np.abs(moy[2]),
+              np.abs(oox[1]), np.abs(ooy[1]), np.abs(oox[2]), np.abs(ooy[2])):
+        e0s = e0s + t
+    e0 = F(1e-6) * e0s
+    re = g('ext', p) + g('ext', q)
+    xe2 = dxt * dxt + dyt * dyt
+    be = -(dxt * vxf + dyt * vyf)
+    ce = xe2 - re * re
+    mbe = (F(4.0) * e0) * (np.abs(vxf) + np.abs(vyf)) + \
+        F(1e-6) * (np.abs(dxt * vxf) + np.abs(dyt * vyf))
+    mce = (F(8.0) * e0) * ((np.abs(dxt) + np.abs(dyt)) + re) + F(1e-6) * (xe2 + re * re)
+    bbe = np.abs(be) + mbe
+    apart = (ce - mce > F(0)) & ((be + mbe <= F(0)) | (bbe * bbe < (F(0.99) * af) * (ce - mce)))
+    first = np.where(apart, 1, -1)
+    cand = np.zeros(len(p), np.int64)
+    min_hi = np.full(len(p), np.inf, F)
+    terms = []
+    for k in range(9):
+        i, j = k // 3, k % 3
+        dx = (dxt + mox[i]) - oox[j]
+        dy = (dyt + moy[i]) - ooy[j]
+        rt = mr[i] + orr[j]
+        bf = -(dx * vxf + dy * vyf)
+        x2 = dx * dx + dy * dy
+        cf = x2 - rt * rt
+        acf = af * cf
+        discf = bf * bf - acf
+        m = (F(1e-5) * af) * ((F(1.0) + x2) + rt * rt) + F(1e-6) * (bf * bf + np.abs(acf))
+        mb = (F(4.0) * e0) * (np.abs(vxf) + np.abs(vyf)) + \
+            F(1e-6) * (np.abs(dx * vxf) + np.abs(dy * vyf))
+        mc = (F(8.0) * e0) * ((np.abs(dx) + np.abs(dy)) + rt) + F(1e-6) * (x2 + rt * rt)
+        bb = (np.abs(bf) + mb) * (np.abs(bf) + mb)
+        terms.append((bf, cf, discf, m, mb, mc, bb))
+        c_k = ~apart & ~(discf < -m)
+        cand |= np.where(c_k, 1 << k, 0)
+        pos = (discf > m) & (bf > mb) & (cf > mc) & ((F(0.99) * af) * (cf - mc) > F(1e-9) * bb)
+        neg = (bf < -mb) | ((cf < -mc) & ((F(0.99) * af) * (-cf - mc) > F(1e-9) * bb))
+        cls = np.where(discf > m, np.where(neg, 1, np.where(pos, 2, 0)), 0)
+        first = np.where(c_k & (first < 0), cls, first)
+        with np.errstate(invalid='ignore', divide='ignore'):
+            hi = (cf + mc) / ((bf - mb) + np.sqrt(discf - m)) * F(1.00001)
+        min_hi = np.where(c_k & pos, np.fmin(min_hi, hi), min_hi)
+    queued = np.where(first == 1, 0, cand)
+    pruned = queued.copy()
+    several = np.array([bin(int(x)).count('1') > 1 for x in queued])
+    for k in range(9):
+        bf, cf, discf, m, mb, mc, bb = terms[k]
+        inq = ((queued >> k) & 1).astype(bool) & (first == 2) & several & (discf > m)
+        drop = (bf < -mb) | ((cf < -mc) & ((F(0.99) * af) * (-cf - mc) > F(1e-9) * bb))
+        ok = ~drop & (bf > mb) & (cf > mc) & ((F(0.99) * af) * (cf - mc) > F(1e-9) * bb)
+        with np.errstate(invalid='ignore', divide='ignore'):
+            lo = (cf - mc) / ((bf + mb) + np.sqrt(discf + m)) * F(0.99999)
+        drop = drop | (ok & (lo > min_hi))
+        pruned = np.where(inq & drop, pruned & ~(1 << k), pruned)
+    return first, queued, pruned, vxf, vyf
+
+
+def reference_roots(a, p, q):
+    """Per pair and sub-pair in visiting order: the reference's root (NaN
+    where undefined), and the index of the selected one (-1 for none)."""
+    v = a['velocity'][p] - a['velocity'][q]
+    av = v[:, 0] * v[:, 0] + v[:, 1] * v[:, 1]
+    roots = np.full((len(p), 9), np.nan)
+    tau = np.full(len(p), np.nan)
+    sel = np.full(len(p), -1)
+    for k in range(9):
+        i, j = k // 3, k % 3
+        x = a[PARTS[i]][p] - a[PARTS[j]][q]
+        r = a[RADII[i]][p] + a[RADII[j]][q]
+        b = -(x[:, 0] * v[:, 0] + x[:, 1] * v[:, 1])
+        c = (x[:, 0] * x[:, 0] + x[:, 1] * x[:, 1]) - r * r
+        with np.errstate(invalid='ignore', divide='ignore'):
+            d = np.sqrt(b * b - av * c)
+            ok = (av != 0) & ~(np.isnan(d) | (d == 0))
+            tn = (b - d) / av
+        roots[:, k] = np.where(ok, tn, np.nan)
+        take = ok & (np.isnan(tau) | ((0 < tn) & (tn < tau)))
+        tau = np.where(take, tn, tau)
+        sel = np.where(take, k, sel)
+    return roots, sel, tau
+
+
+def test_float32_root_certificates_are_sound():
+    """tc_pair_both's float32 time-to-collision certificates: every defined
+    root is queued unless the first root is certainly negative; a first root
+    classed negative or positive has that sign; and the pruning keeps the
+    root the reference selects.  With the margins and the 1e-5 bound factors
+    removed, 400,000 of these pairs give thousands of misses, wrong signs and
+    lost roots."""
+    checked = pruned_any = 0
+    for seed in range(3):
+        a, p, q = edge_population(400_000, 20 + seed)
+        inter, _ = reference_classes(a, p, q)
+        first, queued, pruned, vxf, vyf = root_certificates(a, p, q)
+        roots, sel, tau = reference_roots(a, p, q)
+        live = inter & ((np.abs(vxf) > F(1e-20)) | (np.abs(vyf) > F(1e-20)))
+        defined = ~np.isnan(roots)
+        first_root = np.array([r[np.flatnonzero(~np.isnan(r))[0]] if (~np.isnan(r)).any()
+                               else np.nan for r in roots])
+        bits = (queued[:, None] >> np.arange(9)) & 1
+        # every defined root queued, unless the first one is certainly negative
+        missed = live & (first != 1) & (defined & (bits == 0)).any(1)
+        assert not missed.any(), np.flatnonzero(missed)[:5]
+        neg_wrong = live & (first == 1) & ~(np.isnan(tau) | (tau <= 0))
+        assert not neg_wrong.any(), np.flatnonzero(neg_wrong)[:5]
+        pos_wrong = live & (first == 2) & ~(first_root > 0)
+        assert not pos_wrong.any(), np.flatnonzero(pos_wrong)[:5]
+        lost = live & (first == 2) & (sel >= 0) & (((pruned >> np.maximum(sel, 0)) & 1) == 0)
+        assert not lost.any(), np.flatnonzero(lost)[:5]
+        checked += int(live.sum())
+        pruned_any += int((live & (pruned != queued)).sum())
+    assert checked > 100_000 and pruned_any > 1000, (checked, pruned_any)
