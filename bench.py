@@ -25,7 +25,6 @@ exchange between ranks); rank 0 prints one JSON line.
 import argparse
 import json
 import os
-import re
 import statistics
 import subprocess
 import sys
@@ -75,6 +74,8 @@ def parse():
     ap.add_argument('--no-noise', action='store_true')
     ap.add_argument('--no-save', action='store_true')
     ap.add_argument('--no-states', action='store_true')
+    ap.add_argument('--detail', default=os.path.join('gpurun_out', 'bench_detail.json'),
+                    help='file for the per-leg detail the JSON line leaves out')
     return ap.parse_args()
 
 
@@ -264,7 +265,7 @@ def run_reference(args, ws, rank):
             'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic (seeded)',
             'config': config_of(scen, 'orientation+adjusting+agent_agent+agent_obstacle+integrate+reset'),
             'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': nthreads, 'kind': 'port',
-                             'sample': sample},
+                             'sample': sample, 'numba': numba_probe()},
             'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0,
                     'd2h_bytes_per_step': 0}}
     print(json.dumps(line), flush=True)
@@ -354,16 +355,14 @@ def run_ours(args, ws, rank, local):
         trials.append(whole_job_rate(ws, n, args.steps, e2e_s))
     e2e = sorted(trials)[1]
 
-    # DRAM bytes per launch of the dominant kernel(s), from the committed
-    # summary of one ncu capture of this workload
+    # DRAM bytes per launch of the dominant kernels and their FP64 pipe
+    # activity, from the committed summary of one ncu capture of this workload
     traffic = pipe = None
-    tpath = os.path.join(ROOT, 'profiles', '%s_field100k_threecircle.md' % kernel)
-    if n == 100_000 and scen.body == 'three_circle' and os.path.exists(tpath):
-        text = open(tpath).read()
-        m = re.search(r'^%s DRAM bytes per launch: (\d+)' % kernel, text, re.M)
-        traffic = int(m.group(1)) if m else None
-        m = re.search(r'^%s FP64 pipe active: ([\d.]+)' % kernel, text, re.M)
-        pipe = float(m.group(1)) / 100 if m else None
+    tpath = os.path.join(ROOT, 'profiles', 'pair_stage_field100k_threecircle.json')
+    if n == 100_000 and scen.body == 'three_circle' and kernel == 'k_pairs' and \
+            os.path.exists(tpath):
+        prof = json.load(open(tpath))
+        traffic, pipe = prof.get('dram_bytes_per_step'), prof.get('fp64_pipe_active')
 
     # the HBM side of the roofline: the state read and written once per step
     # and the cell list (ThreeCircle: 29 float64 read, 13 written with the
@@ -380,85 +379,111 @@ def run_ours(args, ws, rank, local):
         if dist is not None:
             dist.destroy_process_group()
         return
+    # The JSON line stays short (the driver keeps its tail): headline, roofline,
+    # baselines, then the batched and adjoint parts of the metric last; the
+    # per-leg detail goes to args.detail.
+    detail = {'e2e_trials': trials,
+              'e2e_timing': 'host wall clock around upload (pinned records), one graph step '
+                            'launch and download (waits, checks the step status), per step; '
+                            'median of 3 passes',
+              'roofline_work': 'achieved counts the float64 operations whose results the state '
+                               'depends on (branch-exact for the state); reference_algorithm '
+                               'counts every float64 operation the reference executes on it '
+                               '(an effective rate: float32 decides most of them exactly)',
+              'force_stage_kernels': 'k_nl_count, near scans (one launch), k_nl_fill, '
+                                     'k_pairs_light, k_pairs, k_forces_gather, k_forces_fallback '
+                                     '(exits at once unless the near lists overflowed)'}
     line = {'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': run_ms / args.steps, 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic (seeded)',
             'config': config_of(scen, 'orientation+adjusting+agent_agent+agent_obstacle+integrate+reset'),
             'e2e': {'value': e2e, 'unit': UNIT,
                     'h2d_bytes_per_step': n * agents.dtype.itemsize,
-                    'd2h_bytes_per_step': n * agents.dtype.itemsize,
-                    'trials': trials,
-                    'timing': 'host wall clock around upload (pinned records), one graph '
-                              'step launch and download (waits, checks the step status), '
-                              'per step; median of 3 passes'},
+                    'd2h_bytes_per_step': n * agents.dtype.itemsize},
             'gpu_launches': b.kernels_per_step(nodes) * args.steps,
             'roofline': {'bound': 'fp64', 'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s',
                          'frac': achieved / peak, 'traffic': traffic,
-                         'kernel': label, 'kernel_ms': kernel_ms, 'pair_split': split,
-                         'hbm': {'bytes_per_agent_step': bytes_agent, 'achieved': hbm_gbs,
-                                 'peak': hbm_peak, 'unit': 'GB/s',
-                                 'frac': hbm_gbs / hbm_peak if hbm_peak else None,
-                                 'peak_source': 'MEASURED_PEAKS.json hbm_gbs (copy)'},
-                         'flops_per_launch': kreq,
-                         'peak_source': 'measured live: FP64 FMA chain kernel (2 flops per FMA)',
-                         # achieved counts the float64 operations whose
-                         # results the state depends on (the reference's
-                         # formulas for the pairs, sub-pairs and branches that
-                         # matter; div, sqrt = 1), branch-exact for the state.
-                         # reference_algorithm counts every float64 operation
-                         # the reference itself executes on this state: an
-                         # effective rate, above the peak because the kernel
-                         # decides most of them exactly in float32.  The
-                         # hardware view is the FP64 pipe's active fraction in
-                         # the committed ncu capture.
-                         'work': 'float64 results the state depends on, branch-exact counts',
-                         'reference_algorithm': {
-                             'flops_per_launch': kflops, 'achieved': effective,
-                             'frac': effective / peak},
+                         'kernel': label, 'kernel_ms': kernel_ms, 'flops_per_launch': kreq,
+                         'peak_source': 'measured live (FP64 FMA chain, 2 flops per FMA)',
                          'fp64_pipe_active_ncu': pipe,
-                         'force_stage': {'ms': force_ms, 'flops_per_step': flops_req,
-                                         'achieved': stage_achieved,
-                                         'frac': stage_achieved / peak,
-                                         'reference_algorithm': {
-                                             'flops_per_step': flops,
-                                             'achieved': stage_effective,
-                                             'frac': stage_effective / peak},
-                                         'kernels': 'k_nl_count, near scans (one launch), '
-                                                    'k_nl_fill, k_pairs_light, k_pairs, '
-                                                    'k_forces_gather, '
-                                                    'k_forces_fallback (exits at once unless '
-                                                    'the near lists overflowed)'}},
+                         'reference_algorithm_frac': effective / peak,
+                         'hbm_frac': hbm_gbs / hbm_peak if hbm_peak else None,
+                         'force_stage_ms': force_ms, 'force_stage_frac': stage_achieved / peak},
             'clocks': clk.summary()}
-    if not args.no_batched:
-        line['batched'] = run_batched(args.steps, args.warmup, flush)
-    if not args.no_adjoint:
-        line['adjoint'] = run_adjoint()
-    if not args.no_navigation:
-        line['navigation'] = run_navigation(args.steps)
-    if not args.no_noise:
-        line['fluctuation'] = run_noise(b, agents, scen, args.steps)
-    if not args.no_save:
-        line['save'] = run_save(max(args.steps, 20))
-    if not args.no_states:
-        line['states'] = run_states(max(args.steps, 10))
+    detail['roofline'] = {'pair_split': split,
+                          'hbm': {'bytes_per_agent_step': bytes_agent, 'achieved_gbs': hbm_gbs,
+                                  'peak_gbs': hbm_peak,
+                                  'peak_source': 'MEASURED_PEAKS.json hbm_gbs (copy)'},
+                          'reference_algorithm': {'flops_per_launch': kflops,
+                                                  'achieved': effective},
+                          'force_stage': {'ms': force_ms, 'flops_per_step': flops_req,
+                                          'achieved': stage_achieved,
+                                          'reference_algorithm_flops_per_step': flops,
+                                          'reference_algorithm_achieved': stage_effective}}
     if ws == 1 and not args.no_cpu_baseline:
-        nthreads = os.cpu_count() or 1
-        steps = 2
-        el = cpu_sample(scen, ORC_NODES, steps, nthreads)
-        line['cpu_baseline'] = {'value': n * steps / el, 'unit': UNIT, 'cores': nthreads,
-                                'kind': 'port',
-                                'sample': '%d steps of the full %d-agent workload, C restatement '
-                                          'of the reference algorithm, OpenMP over %d threads'
-                                          % (steps, n, nthreads)}
-        # one thread: the reference's own functions run serially
-        el1 = cpu_sample(scen, ORC_NODES, 1, 1)
-        line['cpu_baseline']['single_thread'] = {
-            'value': n / el1, 'unit': UNIT, 'cores': 1,
-            'sample': '1 step of the full %d-agent workload on one thread' % n}
-    print(json.dumps(line), flush=True)
+        line['cpu_baseline'], detail['cpu_baseline'] = cpu_baseline(scen, n)
+    legs = {}
+    if not args.no_navigation:
+        d = run_navigation(args.steps)
+        detail['navigation'] = d
+        legs['navigation_device_over_host'] = d['device_navigation'] / d['host_navigation']
+    if not args.no_noise:
+        d = run_noise(b, agents, scen, args.steps)
+        detail['fluctuation'] = d
+        legs['device_noise'] = d['device_noise']
+    if not args.no_save:
+        d = run_save(max(args.steps, 20))
+        detail['save'] = d
+        legs['async_save_over_host_save'] = d['async_save'] / d['host_save']
+    if not args.no_states:
+        detail['states'] = run_states(max(args.steps, 10))
+    if legs:
+        line['legs'] = legs
+    if not args.no_batched:
+        line['batched'], detail['batched'] = run_batched(args.steps, args.warmup, flush)
+    if not args.no_adjoint:
+        line['adjoint'], detail['adjoint'] = run_adjoint()
+    if args.detail:
+        try:
+            os.makedirs(os.path.dirname(os.path.abspath(args.detail)), exist_ok=True)
+            with open(args.detail, 'w') as f:
+                json.dump(detail, f, indent=1)
+        except OSError:
+            pass
+    print(json.dumps(line, separators=(',', ':')), flush=True)
     b.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def numba_probe():
+    """Whether the reference's own numba path could be timed here.  It needs
+    numba and the reference's source files, which are not shipped with this
+    repository; the C port (bit-identical to the device in exact-math mode)
+    is timed instead."""
+    try:
+        import numba  # noqa: F401
+        return 'numba imports, but the reference source is not on this box'
+    except Exception as e:                        # noqa: BLE001
+        return 'unavailable on this box (import numba: %s)' % type(e).__name__
+
+
+def cpu_baseline(scen, n):
+    """The oracle's agent-parallel C port on all host cores (20 steps after
+    one warm-up step) and on one core (3 steps): the reference's algorithm
+    on the host, a baseline reported beside the device number."""
+    nthreads = os.cpu_count() or 1
+    steps, steps1 = 20, 3
+    el = cpu_sample(scen, ORC_NODES, steps, nthreads)
+    el1 = cpu_sample(scen, ORC_NODES, steps1, 1)
+    probe = numba_probe()
+    line = {'value': n * steps / el, 'unit': UNIT, 'cores': nthreads, 'kind': 'port',
+            'sample': '%d steps of the %d-agent workload, OpenMP x %d' % (steps, n, nthreads),
+            'single_thread': n * steps1 / el1, 'numba': probe}
+    detail = dict(line, sample_single_thread='%d steps on one thread' % steps1,
+                  what='C restatement of the reference algorithm (oracle/cd_oracle.c), '
+                       'bit-identical to the device in exact-math mode')
+    return line, detail
 
 
 def run_save(steps, n=2000, size=30.0):
@@ -609,8 +634,14 @@ def run_noise(b, agents, scen, steps):
 
 def run_batched(steps, warmup, flush=None):
     """Batched form: the 512-scenario mix advanced as two contexts (one per
-    body type) launched concurrently, vs. the same scenarios advanced one
-    context at a time.  Returns a dict for the JSON line."""
+    body type), both graphs launched, then one device synchronisation per
+    step; against the same scenarios as 512 single-scenario contexts (the
+    plain step run scenario by scenario): every scenario's step graph
+    launched back to back with one device synchronisation per step (the
+    fair baseline), and each scenario's step awaited before the next
+    (cd_synchronize per scenario, as a caller stepping one simulation after
+    another does).  The same number of steps in every leg, L2 flushed before
+    each.  Returns (the line's part, the detail)."""
     import torch
     from crowddynamics_gb300 import _native as N
     from crowddynamics_gb300 import autotune
@@ -619,8 +650,28 @@ def run_batched(steps, warmup, flush=None):
     nodes = N.NODE_ALL & ~N.NODE_FLUCTUATION
     mix = S.batch_mix()
     groups = [[s for s in mix if s.body == b] for b in ('circular', 'three_circle')]
-    batches = []
-    tuned = {}
+
+    def timed(ctxs, per_scenario_sync=False):
+        for c in ctxs:
+            c.run(max(warmup, 3), nodes)
+        torch.cuda.synchronize()
+        el = 0.0
+        for k in range(steps):
+            if flush is not None:
+                flush.fill_(k & 0xff)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for c in ctxs:
+                c.launch(1, nodes)
+                if per_scenario_sync:
+                    c.synchronize()
+            torch.cuda.synchronize()
+            el += time.perf_counter() - t0
+        for c in ctxs:
+            c.synchronize()                      # status of every context checked
+        return el
+
+    batches, tuned = [], {}
     for g in groups:
         b, agents, _ = batch_from_scenarios(g)
         v, times = autotune.tune(b, agents)
@@ -629,45 +680,22 @@ def run_batched(steps, warmup, flush=None):
                          {str(k): round(t, 4) for k, t in times.items()}}
         batches.append(b)
     n_total = sum(b.n_agents for b in batches)
-    for b in batches:
-        b.run(max(warmup, 3), nodes)
-    el = 0.0
-    for k in range(steps):
-        if flush is not None:
-            flush.fill_(k & 0xff)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for b in batches:
-            b.launch(1, nodes)
-        for b in batches:
-            b.synchronize()
-        el += time.perf_counter() - t0
-    batched = n_total * steps / el
+    batched = n_total * steps / timed(batches)
     for b in batches:
         b.close()
-    # the same scenarios one context at a time (each step a graph launch)
-    singles = []
-    for s in mix:
-        b, _, _ = batch_from_scenarios([s])
-        singles.append(b)
-    for b in singles:
-        b.run(2, nodes)
-    steps_single = max(2, steps // 4)
-    t0 = time.perf_counter()
-    for _ in range(steps_single):
-        for b in singles:
-            b.run(1, nodes)
-    el1 = time.perf_counter() - t0
-    one_by_one = n_total * steps_single / el1
+    singles = [batch_from_scenarios([s])[0] for s in mix]
+    back_to_back = n_total * steps / timed(singles)
+    synchronised = n_total * steps / timed(singles, per_scenario_sync=True)
     for b in singles:
         b.close()
-    return {'value': batched, 'unit': UNIT, 'scenario_by_scenario': one_by_one,
-            'speedup': batched / one_by_one, 'scenarios': len(mix), 'agents': n_total,
-            'walls': sum(len(s.walls) for s in mix), 'steps': steps,
-            'steps_scenario_by_scenario': steps_single,
-            'timing': 'host wall clock per step around both contexts\' graph launches and '
-                      'synchronisation, L2 flushed between steps',
-            'autotune': tuned}
+    line = {'value': batched, 'scenario_by_scenario': back_to_back,
+            'speedup': batched / back_to_back, 'speedup_vs_synchronised': batched / synchronised,
+            'steps': steps, 'scenarios': len(mix), 'agents': n_total}
+    detail = dict(line, unit=UNIT, scenario_by_scenario_synchronised=synchronised,
+                  walls=sum(len(s.walls) for s in mix), autotune=tuned,
+                  timing='host wall clock per step from the first launch to the device '
+                         'synchronisation, L2 flushed (256 MiB write) before each step')
+    return line, detail
 
 
 def run_adjoint(n=5000, width=80.0, height=20.0, steps=400, ckpt=20, seed=4, fd_steps=10):
@@ -740,7 +768,10 @@ def run_adjoint(n=5000, width=80.0, height=20.0, steps=400, ckpt=20, seed=4, fd_
         growth[str(t)] = float(np.abs(rollout(a, True, t)[1]).max())
     growth[str(steps)] = float(np.abs(g).max())
     b.close()
-    return {'workload': 'hallway_80x20_circular_5000_rollout400_ckpt20', 'loss': loss,
+    line = {'adjoint_over_forward': a_ms / f_only, 'gradient_over_forward': (f_ms + a_ms) / f_only,
+            'forward_ms': f_only, 'adjoint_ms': a_ms, 'worst_rel_diff': worst,
+            'fd_steps': fd_steps, 'steps': steps, 'checkpoint_every': ckpt}
+    return line, {'workload': 'hallway_80x20_circular_5000_rollout400_ckpt20', 'loss': loss,
             'forward_only_ms': f_only, 'forward_ms': f_ms, 'adjoint_ms': a_ms,
             'adjoint_over_forward': a_ms / f_only,
             'gradient_over_forward': (f_ms + a_ms) / f_only,

@@ -16,7 +16,8 @@ CSRC = os.path.join(PKG, 'csrc')
 BUILD = os.path.join(PKG, '_build')
 LIB = os.path.join(PKG, 'libcdgpu.so')
 SOURCES = ['cd_kernels.cu', 'cd_api.cu', 'cd_adjoint.cu', 'cd_states.cu']
-HEADERS = [os.path.join(CSRC, 'cd_internal.cuh'), os.path.join(CSRC, 'cd_math.h'), os.path.join(ROOT, 'include', 'cdgpu.h')]
+HEADERS = [os.path.join(CSRC, h) for h in ('cd_internal.cuh', 'cd_cull.cuh', 'cd_math.h',
+                                           'cd_noise.h')] + [os.path.join(ROOT, 'include', 'cdgpu.h')]
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 FLAGS = ['-O3', '-lineinfo', '-std=c++17', '--fmad=false', '-Xcompiler', '-fPIC,-O2',
          '-I', os.path.join(ROOT, 'include')]

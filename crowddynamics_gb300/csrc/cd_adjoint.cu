@@ -26,6 +26,7 @@
 #include <cstdint>
 #include <cmath>
 #include "cd_internal.cuh"
+#include "cd_cull.cuh"
 #include "cd_math.h"
 
 namespace cdk {
@@ -34,7 +35,6 @@ namespace {
 constexpr double SIGTH_SOC = 3.0;
 constexpr double F_SOC_MAX = 2e3;
 constexpr double TAU_MAX = 30.0;
-constexpr float CULL_MARGIN = 0.01f;
 constexpr int NT = 128;
 constexpr int RED_NT = 256;
 
@@ -50,12 +50,6 @@ __device__ __forceinline__ Circ load_circ(const double2 *__restrict__ st, int sl
     a.x = q0.x; a.y = q0.y; a.vx = q1.x; a.vy = q1.y; a.r = q2.x; a.m = q2.y;
     a.k = q3.x; a.tau0 = q3.y; a.mu = q4.x; a.kappa = q4.y; a.damp = q5.x;
     return a;
-}
-
-__device__ __forceinline__ bool pair_far(float4 me, float4 o) {
-    float dx = me.x - o.x, dy = me.y - o.y;
-    float lim = (me.z + o.z) + ((float)SIGTH_SOC + CULL_MARGIN);
-    return dx * dx + dy * dy > lim * lim;
 }
 
 // Reverse of a sum of contact forces sharing one geometry,

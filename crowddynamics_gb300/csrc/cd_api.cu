@@ -504,6 +504,9 @@ int check_device_error(cd_ctx *c, bool enqueued = false) {
         cudaStreamSynchronize(c->stream);
         if (h & cdk::ERR_NOT_FINITE)
             return fail(c, CD_ERR_NOT_FINITE, "an agent position is not finite");
+        if (h & cdk::ERR_RANGE)
+            return fail(c, CD_ERR_INVALID_VALUE,
+                        "an agent is more than 1e7 m from its scenario's grid origin");
         if (h & cdk::ERR_NEAR_LIST)
             return fail(c, CD_ERR_CUDA, "internal error: a near list lacks a pair partner");
         return fail(c, CD_ERR_INVALID_VALUE, "device reported error bits " + std::to_string(h));
@@ -878,9 +881,20 @@ int cd_set_walls(cd_ctx *c, const double *walls, int64_t n_walls) {
     if (n_walls > 0 && !walls) return fail(c, CD_ERR_INVALID_VALUE, "walls is NULL");
     c->walls_host.assign(walls, walls + 4 * n_walls);
     if (n_walls > 0) {
+        // float32 pre-check records relative to the wall's scenario grid
+        // origin (the agents' records are relative to the same origin)
+        std::vector<float4> wf((size_t)n_walls);
+        for (const cd_scenario &sc : c->scen_host)
+            for (int64_t w = sc.wall_begin; w < sc.wall_begin + sc.wall_count; ++w) {
+                const double *p = walls + 4 * w;
+                wf[w] = make_float4((float)(p[0] - sc.x0), (float)(p[1] - sc.y0),
+                                    (float)(p[2] - sc.x0), (float)(p[3] - sc.y0));
+            }
         CUDA_OR_FAIL(c, cudaMemcpyAsync(c->walls_raw, walls, sizeof(double) * 4 * n_walls,
                                         cudaMemcpyHostToDevice, c->stream));
-        cdk::launch_wall_prep(c->walls_raw, c->walls, c->walls_f, (int)n_walls, c->stream);
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(c->walls_f, wf.data(), sizeof(float4) * n_walls,
+                                        cudaMemcpyHostToDevice, c->stream));
+        cdk::launch_wall_prep(c->walls_raw, c->walls, (int)n_walls, c->stream);
     }
     c->walls_dirty = true;
     CUDA_OR_FAIL(c, cudaGetLastError());
@@ -1586,7 +1600,9 @@ constexpr size_t NA_OFF_STAGEF = NA_OFF_CULL + na_align(sizeof(float4) * NA_N);
 constexpr size_t NA_OFF_VMAX = NA_OFF_STAGEF + na_align(sizeof(float4) * 2 * NA_N);
 constexpr size_t NA_OFF_ERR = NA_OFF_VMAX + na_align(sizeof(unsigned long long));
 constexpr size_t NA_OFF_WORK = NA_OFF_ERR + na_align(sizeof(int));
-constexpr size_t NA_BYTES = NA_OFF_WORK + na_align(sizeof(int));
+// StepArgs::work holds two ints (the force kernel's work counter and the
+// float32 pair pass's deferred count)
+constexpr size_t NA_BYTES = NA_OFF_WORK + na_align(2 * sizeof(int));
 static_assert(NA_BYTES < (4u << 20), "allocation-free scratch stays below 4 MiB");
 
 __device__ __align__(256) static unsigned char g_noalloc_scratch[NA_BYTES];
@@ -1710,5 +1726,7 @@ extern "C" int cd_agent_agent_noalloc(int body_type, int64_t n, const double *co
     CUDA_OR_FAIL(nullptr, cudaMemcpyAsync(&h, a.err, sizeof(int), cudaMemcpyDeviceToHost, st));
     CUDA_OR_FAIL(nullptr, cudaStreamSynchronize(st));
     if (h & cdk::ERR_NOT_FINITE) return fail(nullptr, CD_ERR_NOT_FINITE, "an agent position is not finite");
+    if (h & cdk::ERR_RANGE)
+        return fail(nullptr, CD_ERR_INVALID_VALUE, "an agent is more than 1e7 m from the grid origin");
     return CD_OK;
 }

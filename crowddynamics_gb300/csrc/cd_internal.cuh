@@ -22,6 +22,8 @@ constexpr int WALL_D = 8;          // p0x p0y p1x p1y tx ty lw -
 
 // Device error bits (StepArgs::err).
 constexpr int ERR_NOT_FINITE = 1;
+// An agent farther than COORD_MAX (cd_cull.cuh) from its scenario's grid origin.
+constexpr int ERR_RANGE = 4;
 
 // Candidate chunks per agent whose ballots the near-list count keeps for the
 // fill (an agent with more is evaluated again by the fill).
@@ -227,8 +229,7 @@ void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s);
 void launch_scen_max(const StepArgs &a, double *v0max, double *ext, double *partial,
                      cudaStream_t s);
 int scen_max_partials(int n_scen);
-void launch_wall_prep(const double *raw, double *walls, float4 *walls_f, int nw,
-                      cudaStream_t s);
+void launch_wall_prep(const double *raw, double *walls, int nw, cudaStream_t s);
 void launch_aos_to_soa(const char *aos, long long itemsize, const long long *off,
                        int n, int body, double *const *col, cudaStream_t s);
 void launch_states_in(const char *aos, long long itemsize, const StateOffsets &o, int n,

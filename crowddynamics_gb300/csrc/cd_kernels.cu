@@ -28,6 +28,7 @@
 #include <cmath>
 #include <cuda_fp16.h>
 #include "cd_internal.cuh"
+#include "cd_cull.cuh"
 #include "cd_math.h"
 #include "cd_noise.h"
 
@@ -39,7 +40,6 @@ constexpr double SIGTH_SOC = 3.0;      // core/interactions.py:45
 constexpr double F_SOC_MAX = 2e3;      // core/motion/power_law.py:52
 constexpr double TAU_MAX = 30.0;       // core/motion/power_law.py:243
 constexpr double PI_D = 3.141592653589793;
-constexpr float CULL_MARGIN = 0.01f;   // metres, >> float32 error at 1e4 m
 
 // ---- float64 helpers restating core/vector2D.py ------------------------
 
@@ -172,17 +172,6 @@ __device__ __forceinline__ double dist_circle_line(double x, double y, double r,
     return d_iw - r;
 }
 
-// Float32 pre-check: centre-to-segment distance clearly above `reach`.
-__device__ __forceinline__ bool wall_far(float x, float y, float reach, float4 w) {
-    float dx = w.z - w.x, dy = w.w - w.y;
-    float qx = x - w.x, qy = y - w.y;
-    float dd = dx * dx + dy * dy;
-    float t = dd > 0.f ? fminf(fmaxf((qx * dx + qy * dy) / dd, 0.f), 1.f) : 0.f;
-    float rx = qx - t * dx, ry = qy - t * dy;
-    float lim = reach + CULL_MARGIN;
-    return rx * rx + ry * ry > lim * lim;       // false for NaN
-}
-
 __device__ __forceinline__ void wall_circular(const Circ &A, const double *w,
                                               double &fx, double &fy) {
     double nx, ny;
@@ -248,6 +237,9 @@ __global__ void __launch_bounds__(PREP_NT) k_prepare(StepArgs a) {
         int key = sc.cell_base;
         if (isfinite(x) && isfinite(y)) {
             key += axis_cell(x, sc.x0, sc.cell, sc.nx) * sc.ny + axis_cell(y, sc.y0, sc.cell, sc.ny);
+            // the float32 pre-checks are sound within COORD_MAX of the origin
+            if (!(fabs(x - sc.x0) <= COORD_MAX && fabs(y - sc.y0) <= COORD_MAX))
+                atomicOr(a.err, ERR_RANGE);
         } else {
             atomicOr(a.err, ERR_NOT_FINITE);
         }
@@ -639,6 +631,10 @@ __global__ void k_gather(StepArgs a, int part) {
     if (a.slot_of) { i = t; s = a.slot_of[t]; }
     else { s = t; i = a.perm[t]; }
     double *const *c = a.col;
+    // pre-check records: positions relative to the scenario's grid origin
+    // (cd_cull.cuh); the staged float64 records keep the reference's values
+    const ScenDev *sc = a.scen + __ldg(&a.scen_of[i]);
+    const double ox = __ldg(&sc->x0), oy = __ldg(&sc->y0);
     if (a.body == 0) {
         if (part != 1) {
             double2 *p = a.stage + (size_t)s * STAGE_Q_CIRC;
@@ -649,9 +645,11 @@ __global__ void k_gather(StepArgs a, int part) {
             p[4] = make_double2(c[MU][i], c[KAPPA][i]);
             p[5] = make_double2(c[DAMP][i], 0.0);
         }
-        if (part != 2)
-            a.cull[s] = make_float4((float)c[X][i], (float)c[Y][i], up_f(c[R][i]),
+        if (part != 2) {
+            const float xf = (float)(c[X][i] - ox), yf = (float)(c[Y][i] - oy);
+            a.cull[s] = make_float4(xf, yf, up_f(c[R][i]) + cull_slack(xf, yf),
                                     pack_velocity(c[VX][i], c[VY][i]));
+        }
     } else {
         double x = c[X][i], y = c[Y][i];
         if (part != 1) {
@@ -670,30 +668,23 @@ __global__ void k_gather(StepArgs a, int part) {
             p[9] = make_double2(cs, 0.0);
         }
         if (part == 2) return;
-        float xh = (float)x, yh = (float)y;
-        // position = float hi + float lo; shoulder centres relative to the torso
+        // position relative to the grid origin = float hi + float lo;
+        // shoulder centres relative to the torso
+        const double xr = x - ox, yr = y - oy;
+        const float xh = (float)xr, yh = (float)yr;
         const float oxl = (float)(c[XLS][i] - x), oyl = (float)(c[YLS][i] - y);
         const float oxr = (float)(c[XRS][i] - x), oyr = (float)(c[YRS][i] - y);
         const float rtf = (float)c[RT][i], rsf = (float)c[RS][i];
-        a.stage_f[2 * s] = make_float4((float)(x - (double)xh), (float)(y - (double)yh), rtf, rsf);
+        a.stage_f[2 * s] = make_float4((float)(xr - (double)xh), (float)(yr - (double)yh), rtf, rsf);
         a.stage_f[2 * s + 1] = make_float4(oxl, oyl, oxr, oyr);
         // extent (extent_tc) in float32 from the same offsets: its error is
         // below 1e-6 relative, the 1e-5 added makes it an upper bound, which
-        // is all the pre-check records need
+        // is all the pre-check records need; raised by the position's slack
         const float ef = fmaxf(rtf, fmaxf(sqrtf(oxl * oxl + oyl * oyl) + rsf,
                                           sqrtf(oxr * oxr + oyr * oyr) + rsf));
-        a.cull[s] = make_float4(xh, yh, ef + ef * 1e-5f + 1e-5f,
+        a.cull[s] = make_float4(xh, yh, (ef + ef * 1e-5f + 1e-5f) + cull_slack(xh, yh),
                                 pack_velocity(c[VX][i], c[VY][i]));
     }
-}
-
-// Float32 conservative pre-check: true if the pair certainly has h >= 3.
-// Symmetric in its arguments (the two extents are added first), so both
-// agents of a pair agree on it.
-__device__ __forceinline__ bool pair_far(float4 me, float4 o) {
-    float dx = me.x - o.x, dy = me.y - o.y;
-    float lim = (me.z + o.z) + ((float)SIGTH_SOC + CULL_MARGIN);
-    return dx * dx + dy * dy > lim * lim;       // false for NaN
 }
 
 // Candidate enumeration over the 3 x 3 cell neighbourhood of slot s.  The
@@ -2684,7 +2675,10 @@ __global__ void k_pair_counts(StepArgs a, int *out) {
     o[6] = ns; o[7] = nd; o[8] = nv;
 }
 
-__global__ void k_wall_prep(const double *raw, double *walls, float4 *wf, int nw) {
+// Float64 wall records (the tangent and length of distance_circle_line);
+// the float32 pre-check records are written by the host (relative to their
+// scenario's grid origin, cd_cull.cuh).
+__global__ void k_wall_prep(const double *raw, double *walls, int nw) {
     int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nw) return;
     double p0x = raw[4 * w], p0y = raw[4 * w + 1], p1x = raw[4 * w + 2], p1y = raw[4 * w + 3];
@@ -2693,7 +2687,6 @@ __global__ void k_wall_prep(const double *raw, double *walls, float4 *wf, int nw
     double *o = walls + (size_t)w * WALL_D;
     o[0] = p0x; o[1] = p0y; o[2] = p1x; o[3] = p1y;
     o[4] = dx / l_w; o[5] = dy / l_w; o[6] = l_w; o[7] = 0.0;
-    wf[w] = make_float4((float)p0x, (float)p0y, (float)p1x, (float)p1y);
 }
 
 // -- packed host records <-> columns -------------------------------------
@@ -3233,8 +3226,8 @@ void launch_scen_max(const StepArgs &a, double *v0max, double *ext, double *part
     k_scen_max_final<<<(a.n_scen + 7) / 8, 256, 0, s>>>(partial, nb, a.n_scen, v0max, ext);
 }
 int scen_max_partials(int n_scen) { return 2 * V0MAX_B * (n_scen > 0 ? n_scen : 1); }
-void launch_wall_prep(const double *raw, double *walls, float4 *wf, int nw, cudaStream_t s) {
-    if (nw > 0) k_wall_prep<<<nblk(nw, 128), 128, 0, s>>>(raw, walls, wf, nw);
+void launch_wall_prep(const double *raw, double *walls, int nw, cudaStream_t s) {
+    if (nw > 0) k_wall_prep<<<nblk(nw, 128), 128, 0, s>>>(raw, walls, nw);
 }
 void launch_aos_to_soa(const char *aos, long long itemsize, const long long *off, int n,
                        int body, double *const *col, cudaStream_t s) {

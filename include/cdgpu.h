@@ -94,7 +94,11 @@ enum {
  * [y0, y0 + ny*cell_size); an agent outside it is binned into the nearest
  * border cell, which keeps every interacting pair in adjacent cells.  The
  * reference's default cell size is sight_soc + 2 * max_agent_radius
- * (simulation/logic.py:97-116). */
+ * (simulation/logic.py:97-116).  Coordinates may be anywhere (UTM metres,
+ * say), but every agent must stay within 1e7 m of its scenario's (x0, y0) in
+ * each axis: a step that finds one farther fails with CD_ERR_INVALID_VALUE
+ * (the float32 pre-checks that skip non-interacting pairs work relative to
+ * the grid origin and are exact only within that range). */
 typedef struct {
     int64_t agent_begin, agent_count;   /* range in the batch's agent array */
     int64_t wall_begin, wall_count;     /* range in the batch's wall array  */
@@ -336,8 +340,13 @@ int cd_rollout_loss(cd_ctx *ctx, int64_t steps, const double *target,
  *
  * The first call on a device looks up the array's device address (once per
  * device, with that device current); make that first call before any stream
- * capture.  All calls share the one array: calls whose work overlaps on the
- * GPU (other host threads, or other streams) race and must not be issued. */
+ * capture.  The address is kept for the life of the process: after a
+ * cudaDeviceReset (or any teardown of the device's primary context) it is
+ * stale, and the entry point must not be called on that device again.  All
+ * calls share the one array: calls whose work overlaps on the GPU (other
+ * host threads, or other streams) race and must not be issued.  Positions
+ * farther than 1e7 m from (x0, y0) are rejected with CD_ERR_INVALID_VALUE
+ * (the step's float32 pre-checks are exact only within that range). */
 #define CD_NOALLOC_MAX_AGENTS 16384
 #define CD_NOALLOC_MAX_CELLS 16384
 enum {

@@ -16,6 +16,15 @@ motion, positions far from the origin.  A decided pair must never disagree
 with the reference.  The population is sharp enough to matter: with every
 margin of the certificates set to zero it yields about 25,000 wrong
 decisions in 500,000 pairs.
+
+The pre-check records hold positions relative to the scenario's grid origin,
+with every extent raised by 2^-21 of the position's magnitude
+(csrc/cd_cull.cuh); walls likewise, with 2^-20 of their endpoints'
+magnitudes.  The same checks run on crowds at UTM-like coordinates
+(5e5, 7e6) m, with the grid origin beside the crowd and with it at (0, 0)
+(relative coordinates near the 1e7 m bound the step enforces), and the cull
+of the earlier absolute records without the slack is shown to drop
+interacting pairs and wall contacts there.
 """
 import numpy as np
 
@@ -25,16 +34,32 @@ from crowddynamics_gb300.simulation.agents import new_agents, shoulders
 F = np.float32
 SIGHT = F(3.0)
 PRESEL_MARGIN = F(1e-4)
+CULL_MARGIN = F(0.01)
+CULL_MAG = F(2.0 ** -21)
+WALL_MAG = F(2.0 ** -20)
 NONE, ZERO, DEFER = 0, 1, 3
+UTM = (5e5, 7e6)
 
 
-def precheck_records(a):
-    """k_gather's float32 records: hi and lo parts of the torso position,
-    shoulder offsets from the torso, radii, and the extent bound."""
+def cull_slack(xh, yh):
+    """cull_slack (csrc/cd_cull.cuh)."""
+    m = np.abs(xh) + np.abs(yh)
+    return np.where(m <= F(3.0e38), m * CULL_MAG, F(0.0)).astype(F)
+
+
+def precheck_records(a, origin=(0.0, 0.0), relative=True):
+    """k_gather's float32 records: hi and lo parts of the torso position
+    relative to the grid origin, shoulder offsets from the torso, radii, and
+    the extent bound raised by the position's slack.  relative=False gives
+    the earlier records (absolute positions, no slack)."""
     x, y = a['position'][:, 0], a['position'][:, 1]
-    xh, yh = x.astype(F), y.astype(F)
+    if relative:
+        xr, yr = x - origin[0], y - origin[1]
+    else:
+        xr, yr = x, y
+    xh, yh = xr.astype(F), yr.astype(F)
     rec = dict(xh=xh, yh=yh,
-               xl=(x - xh.astype(np.float64)).astype(F), yl=(y - yh.astype(np.float64)).astype(F),
+               xl=(xr - xh.astype(np.float64)).astype(F), yl=(yr - yh.astype(np.float64)).astype(F),
                rt=a['r_t'].astype(F), rs=a['r_s'].astype(F),
                oxl=(a['position_ls'][:, 0] - x).astype(F), oyl=(a['position_ls'][:, 1] - y).astype(F),
                oxr=(a['position_rs'][:, 0] - x).astype(F), oyr=(a['position_rs'][:, 1] - y).astype(F))
@@ -42,12 +67,14 @@ def precheck_records(a):
     er = np.sqrt(rec['oxr'] * rec['oxr'] + rec['oyr'] * rec['oyr']) + rec['rs']
     ef = np.fmax(rec['rt'], np.fmax(el, er))
     rec['ext'] = (ef + ef * F(1e-5)) + F(1e-5)
+    if relative:
+        rec['ext'] = rec['ext'] + cull_slack(xh, yh)
     return rec
 
 
-def light_decisions(a, p, q):
+def light_decisions(a, p, q, origin=(0.0, 0.0)):
     """tc_pair_light for the pairs (p[k], q[k])."""
-    R = precheck_records(a)
+    R = precheck_records(a, origin)
     g = lambda name, idx: R[name][idx]
     dxt = (g('xh', p) - g('xh', q)) + (g('xl', p) - g('xl', q))
     dyt = (g('yh', p) - g('yh', q)) + (g('yl', p) - g('yl', q))
@@ -186,12 +213,12 @@ def move(a, idx, d):
         a[part][idx] += d
 
 
-def edge_population(n_pairs, seed):
+def edge_population(n_pairs, seed, center=(0.0, 0.0)):
     """Pairs (2k, 2k + 1) of ThreeCircle agents at the certificates' edges:
     the exact minimum skin distance set to within 1e-9 .. 1e-2 m of 3 or of
     0 (or anywhere in [-0.4, 3.6]); relative velocities random, head-on,
     receding, grazing the closest sub-pair within 1e-9 .. 1e-3 of its radii
-    sum, zero, or tiny; torsos up to 300 m from the origin."""
+    sum, zero, or tiny; torsos up to 300 m from `center`."""
     rng = np.random.default_rng(seed)
     n = 2 * n_pairs
     a = new_agents(n, 'three_circle')
@@ -200,7 +227,7 @@ def edge_population(n_pairs, seed):
     p, q = np.arange(0, n, 2), np.arange(1, n, 2)
     th = rng.uniform(0, 2 * np.pi, n_pairs)
     u = np.stack((np.cos(th), np.sin(th)), 1)
-    origin = rng.uniform(0, 300.0, (n_pairs, 2))
+    origin = np.asarray(center) + rng.uniform(0, 300.0, (n_pairs, 2))
     a['position'][p] = origin
     a['position'][q] = origin + (rng.uniform(-0.4, 3.6, n_pairs) + a['r_t'][p] +
                                  a['r_t'][q])[:, None] * u
@@ -246,13 +273,13 @@ def edge_population(n_pairs, seed):
     return a, p, q
 
 
-def near_list_far(a, p, q):
+def near_list_far(a, p, q, origin=(0.0, 0.0), relative=True):
     """pair_far: the near lists' float32 cull (torso centres' hi parts, the
-    extent bounds, 1 cm of margin)."""
-    R = precheck_records(a)
+    raised extent bounds, 1 cm of margin)."""
+    R = precheck_records(a, origin, relative)
     dx = R['xh'][p] - R['xh'][q]
     dy = R['yh'][p] - R['yh'][q]
-    lim = (R['ext'][p] + R['ext'][q]) + (SIGHT + F(0.01))
+    lim = (R['ext'][p] + R['ext'][q]) + (SIGHT + CULL_MARGIN)
     return dx * dx + dy * dy > lim * lim
 
 
@@ -264,6 +291,26 @@ def test_near_list_cull_is_sound():
         inter, _ = reference_classes(a, p, q)
         assert not (far & inter).any()
         assert far.any() and (~far).any()
+
+
+def test_near_list_cull_is_sound_at_utm_coordinates():
+    """Crowds at (5e5, 7e6) m: the cull stays sound with the grid origin
+    beside the crowd and with it at (0, 0), where the relative coordinates
+    reach 7e6 m (near the 1e7 m bound) and only the extent slack keeps the
+    float32 rounding (0.25 m per coordinate there) on the safe side: there
+    the slack (3.6 m per agent) keeps every pair of this population, which
+    costs time, not results.  The earlier absolute records without slack
+    drop interacting pairs here."""
+    a, p, q = edge_population(300_000, 30, center=UTM)
+    inter, _ = reference_classes(a, p, q)
+    far = near_list_far(a, p, q, (UTM[0] - 20.0, UTM[1] - 20.0))
+    assert not (far & inter).any()
+    assert far.sum() > 1000 and (~far).any()
+    for origin in ((0.0, 0.0), (-2e6, 9.9e6)):
+        far = near_list_far(a, p, q, origin)
+        assert not (far & inter).any(), origin
+    old = near_list_far(a, p, q, relative=False)
+    assert (old & inter).sum() > 1000
 
 
 def test_float32_pair_certificates_are_sound():
@@ -283,6 +330,111 @@ def test_float32_pair_certificates_are_sound():
     # quarter of the pairs (most pairs of a real crowd are far from every
     # edge: the float32 pass defers 436 of 1.83M on the 100k field)
     assert decided > 0.15 * total, decided / total
+
+
+def test_float32_pair_certificates_are_sound_at_utm_coordinates():
+    """The certificates on hi + lo positions relative to a grid origin beside
+    the crowd and 7e6 m away from it."""
+    a, p, q = edge_population(300_000, 31, center=UTM)
+    inter, force = reference_classes(a, p, q)
+    for origin in ((UTM[0] - 20.0, UTM[1] - 20.0), (0.0, 0.0)):
+        got = light_decisions(a, p, q, origin)
+        assert not ((got == NONE) & inter).any(), origin
+        assert not ((got == ZERO) & (~inter | force)).any(), origin
+        assert np.sum(got != DEFER) > 0.15 * len(p)
+
+
+def wall_far(xh, yh, reach, w):
+    """wall_far (csrc/cd_cull.cuh) in float32, w = (p0x, p0y, p1x, p1y)."""
+    dx, dy = w[:, 2] - w[:, 0], w[:, 3] - w[:, 1]
+    qx, qy = xh - w[:, 0], yh - w[:, 1]
+    dd = dx * dx + dy * dy
+    with np.errstate(invalid='ignore', divide='ignore'):
+        t = np.where(dd > F(0), np.fmin(np.fmax((qx * dx + qy * dy) / dd, F(0)), F(1)), F(0))
+    rx, ry = qx - t * dx, qy - t * dy
+    wm = (np.abs(w[:, 0]) + np.abs(w[:, 1])) + (np.abs(w[:, 2]) + np.abs(w[:, 3]))
+    lim = (reach + CULL_MARGIN) + wm * WALL_MAG
+    return rx * rx + ry * ry > lim * lim
+
+
+def wall_population(n, seed, center):
+    """ThreeCircle agents and one wall segment each (length 1-15 m, any
+    angle, up to 300 m from `center`), the torso centre's distance to the
+    segment set within 1e-7 .. 1e-1 m of the agent's extent (either side),
+    or anywhere in [0, 4] m; about a third of the closest points are the
+    segment's end points."""
+    rng = np.random.default_rng(seed)
+    a = new_agents(n, 'three_circle')
+    S._three_circle_bodies(a, rng, n)
+    a['orientation'] = rng.uniform(-np.pi, np.pi, n)
+    a['position'] = np.asarray(center) + rng.uniform(0, 300.0, (n, 2))
+    shoulders(a)
+    x = a['position']
+    ext = np.maximum(a['r_t'], np.maximum(
+        np.hypot(*(a['position_ls'] - x).T) + a['r_s'],
+        np.hypot(*(a['position_rs'] - x).T) + a['r_s']))
+    dh = rng.choice([-1.0, 1.0], n) * 10.0 ** rng.uniform(-7, -1, n)
+    dist = np.where(rng.uniform(size=n) < 0.8, ext + dh, rng.uniform(0, 4.0, n))
+    th = rng.uniform(0, 2 * np.pi, n)
+    t = np.stack((np.cos(th), np.sin(th)), 1)
+    nrm = np.stack((-t[:, 1], t[:, 0]), 1)
+    length = rng.uniform(1.0, 15.0, n)
+    # the closest point: inside the segment, or an end point (then the
+    # agent sits beyond that end, along a direction in the end's half-plane)
+    along = rng.uniform(0, 1.0, n) * length
+    end = rng.integers(0, 3, n)
+    ang = rng.uniform(-np.pi / 2, np.pi / 2, n)
+    out_dir = np.where((end == 1)[:, None], -t, t)
+    off = np.where((end == 0)[:, None], nrm * dist[:, None],
+                   (out_dir * np.cos(ang)[:, None] + nrm * np.sin(ang)[:, None]) * dist[:, None])
+    foot = np.where((end == 0)[:, None], x - off, x - off)
+    start = np.where((end == 1)[:, None], foot,
+                     np.where((end == 2)[:, None], foot - t * length[:, None],
+                              foot - t * along[:, None]))
+    walls = np.concatenate((start, start + t * length[:, None]), 1)
+    return a, walls, ext
+
+
+def segment_distance(x, w):
+    """The torso centre's distance to the segment in float64, as
+    distance_circle_line (core/distance.py:108-146) computes it with r = 0."""
+    p0, p1 = w[:, :2], w[:, 2:]
+    d = p1 - p0
+    lw = np.hypot(d[:, 0], d[:, 1])
+    t = d / lw[:, None]
+    q0, q1 = x - p0, x - p1
+    l_t = -(t * q1).sum(1) - (t * q0).sum(1)
+    nrm = np.stack((-t[:, 1], t[:, 0]), 1)
+    perp = np.abs((nrm * q0).sum(1))
+    return np.where(l_t > lw, np.hypot(*q0.T), np.where(l_t < -lw, np.hypot(*q1.T), perp))
+
+
+def test_wall_cull_is_sound():
+    """A wall segment the float32 wall cull skips is farther from the torso
+    centre than the agent's extent, so the reference finds no contact with
+    it; near the origin, at (5e5, 7e6) m with the grid origin beside the crowd
+    and at (0, 0).  The earlier absolute records without the magnitude terms
+    skip walls in contact there."""
+    for center, origins in (((0.0, 0.0), ((0.0, 0.0),)),
+                            (UTM, ((UTM[0] - 20.0, UTM[1] - 20.0), (0.0, 0.0)))):
+        a, walls, ext = wall_population(300_000, 40, center)
+        dist = segment_distance(a['position'], walls)
+        touching = dist <= ext
+        for k, origin in enumerate(origins):
+            o = np.array([origin[0], origin[1], origin[0], origin[1]])
+            R = precheck_records(a, origin)
+            far = wall_far(R['xh'], R['yh'], R['ext'], (walls - o).astype(F))
+            assert not (far & touching).any(), (center, origin)
+            if k == 0:                      # the grid origin beside the crowd
+                assert far.sum() > 1000 and (~far).any()
+    R = precheck_records(a, relative=False)
+    wf = walls.astype(F)
+    dx, dy = wf[:, 2] - wf[:, 0], wf[:, 3] - wf[:, 1]
+    qx, qy = R['xh'] - wf[:, 0], R['yh'] - wf[:, 1]
+    t = np.fmin(np.fmax((qx * dx + qy * dy) / (dx * dx + dy * dy), F(0)), F(1))
+    rx, ry = qx - t * dx, qy - t * dy
+    lim = R['ext'] + CULL_MARGIN
+    assert ((rx * rx + ry * ry > lim * lim) & touching).sum() > 1000
 
 
 def root_certificates(a, p, q):
