@@ -38,12 +38,15 @@ import types
 
 import numpy as np
 
-REFERENCE_ROOT = os.environ.get('CROWDDYNAMICS_REFERENCE', '/root/reference')
+# The reference source tree: the crowddynamics project root, named by the
+# CROWDDYNAMICS_REFERENCE environment variable (unset: the tests that need it
+# skip, and the committed fixtures stand in for it).
+REFERENCE_ROOT = os.environ.get('CROWDDYNAMICS_REFERENCE', '')
 
 
 def available():
-    return os.path.exists(os.path.join(REFERENCE_ROOT, 'crowddynamics', 'core',
-                                       'interactions.py'))
+    return bool(REFERENCE_ROOT) and os.path.exists(
+        os.path.join(REFERENCE_ROOT, 'crowddynamics', 'core', 'interactions.py'))
 
 
 class _Inert:
@@ -205,18 +208,102 @@ _FILES = [
     ('crowddynamics.core.evacuation', 'crowddynamics/core/evacuation.py'),
 ]
 
-_loaded = None
+_loaded = {}
 
 
-def load():
+def _libm_numpy():
+    """A stand-in for ``numpy`` in the reference modules that evaluates the
+    elementary functions as numba's compiled code does: on float64 scalars,
+    numba lowers ``np.exp``, ``np.sin``, ``np.cos`` and ``np.arctan2`` to the
+    C library's ``exp``, ``sin``, ``cos`` and ``atan2``, and ``np.hypot`` to
+    its ``hypot`` (numba's math implementation calls the platform function).
+    numpy's own loops for exp, hypot and arctan2 round differently from the C
+    library in a few percent of calls, which chaos amplifies to millimetres
+    over tens of steps.  Everything else is numpy itself."""
+    import ctypes
+    import ctypes.util
+    libm = ctypes.CDLL(ctypes.util.find_library('m'))
+    proxy = types.ModuleType('numpy')
+    proxy.__dict__.update(np.__dict__)
+
+    def wrap(cfn, nargs):
+        cfn.restype = ctypes.c_double
+        cfn.argtypes = [ctypes.c_double] * nargs
+        vec = np.vectorize(lambda *a: cfn(*a), otypes=[np.float64])
+
+        def f(*args):
+            if all(np.ndim(a) == 0 for a in args):
+                return np.float64(cfn(*(float(a) for a in args)))
+            return vec(*args)
+        return f
+
+    proxy.exp = wrap(libm.exp, 1)
+    proxy.sin = wrap(libm.sin, 1)
+    proxy.cos = wrap(libm.cos, 1)
+    proxy.arctan2 = wrap(libm.atan2, 2)
+    proxy.hypot = wrap(libm.hypot, 2)
+    return proxy
+
+
+def _numba_ipow(a, n):
+    """``a ** n`` for a literal integer n as numba lowers it: exponentiation
+    by squaring from 1 (so a ** 2 is exactly a * a), the reciprocal for
+    n < 0.  CPython evaluates a float ** 2 with the C library's pow, which
+    differs from a * a in about one case in a thousand."""
+    one = 1.0 if isinstance(a, (float, np.floating)) else 1
+    r, e = one, abs(n)
+    while e:
+        if e & 1:
+            r = r * a
+        e >>= 1
+        if e:
+            a = a * a
+    return one / r if n < 0 else r
+
+
+class _PowLowering(__import__('ast').NodeTransformer):
+    """Rewrites ``x ** k`` with an integer literal k into _numba_ipow(x, k)."""
+
+    def visit_BinOp(self, node):
+        import ast
+        self.generic_visit(node)
+        if isinstance(node.op, ast.Pow):
+            k = node.right
+            neg = isinstance(k, ast.UnaryOp) and isinstance(k.op, ast.USub)
+            lit = k.operand if neg else k
+            if isinstance(lit, ast.Constant) and type(lit.value) is int:
+                call = ast.Call(func=ast.Name('_numba_ipow', ast.Load()),
+                                args=[node.left, ast.Constant(-lit.value if neg else lit.value)],
+                                keywords=[])
+                return ast.copy_location(call, node)
+        return node
+
+
+def _exec_numba_semantics(mod, path):
+    """Execute a reference file in `mod` with numba's lowering of literal
+    integer powers (the source itself is read unchanged)."""
+    import ast
+    tree = ast.parse(open(path).read(), path)
+    tree = ast.fix_missing_locations(_PowLowering().visit(tree))
+    mod.__dict__['_numba_ipow'] = _numba_ipow
+    exec(compile(tree, path, 'exec'), mod.__dict__)
+
+
+def load(math='numpy'):
     """Load the reference hot-path modules; returns a namespace of them.
 
-    The stubs are installed only for the duration of the load and the
-    loaded modules keep references to them, so other imports are unaffected.
+    ``math='numpy'`` runs them as CPython executes them (numpy's elementary
+    functions, the C library's pow for ``x ** 2``); ``math='libm'`` runs them
+    with numba's scalar semantics: the C library's elementary functions (see
+    _libm_numpy) and literal integer powers as multiplications (see
+    _numba_ipow).  The stubs are installed only for
+    the duration of the load and the loaded modules keep references to them,
+    so other imports are unaffected.
     """
-    global _loaded
-    if _loaded is not None:
-        return _loaded
+    if math in _loaded:
+        return _loaded[math]
+    if math not in ('numpy', 'libm'):
+        raise ValueError(math)
     if not available():
         raise RuntimeError('reference source tree not found at ' + REFERENCE_ROOT)
     nb, tys = _make_numba()
@@ -238,6 +325,7 @@ def load():
         stubs[pkg] = p
     stubs['crowddynamics.simulation.agents'] = _make_agents_module()
     saved = {k: sys.modules.get(k) for k in list(stubs) + [n for n, _ in _FILES]}
+    np_libm = _libm_numpy() if math == 'libm' else None
     sys.modules.update(stubs)
     ns = types.SimpleNamespace()
     try:
@@ -246,7 +334,12 @@ def load():
                 name, os.path.join(REFERENCE_ROOT, rel))
             mod = importlib.util.module_from_spec(spec)
             sys.modules[name] = mod
-            spec.loader.exec_module(mod)
+            if math == 'libm':
+                _exec_numba_semantics(mod, os.path.join(REFERENCE_ROOT, rel))
+                if hasattr(mod, 'np'):
+                    mod.np = np_libm
+            else:
+                spec.loader.exec_module(mod)
             setattr(ns, name.rsplit('.', 1)[-1], mod)
             if name == 'crowddynamics.core.vector2D':
                 stubs['crowddynamics.simulation.agents'].vector2D = mod
@@ -257,8 +350,10 @@ def load():
                 sys.modules.pop(k, None)
             else:
                 sys.modules[k] = v
+    if math == 'libm':
+        ns.agents_module.np = np_libm
     ns.grid = CellGrid
-    _loaded = ns
+    _loaded[math] = ns
     return ns
 
 
@@ -328,10 +423,10 @@ def configure_grid(x0, y0, cell, nx, ny):
 def step(agents, cell_size, walls=None, noise_f=None, noise_m=None,
          dt_min=0.001, dt_max=0.01, nodes=('fluctuation', 'orientation', 'adjusting',
                                            'agent_agent', 'agent_obstacle',
-                                           'integrate', 'reset')):
+                                           'integrate', 'reset'), math='numpy'):
     """One update() of the standard tree with the reference's own functions
     (node bodies restated from simulation/logic.py:59-130,258-261)."""
-    R = load()
+    R = load(math)
     three = R.agents_module.is_model(agents, 'three_circle')
     dt = 0.0
     if 'fluctuation' in nodes and noise_f is not None:

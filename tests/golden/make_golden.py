@@ -1,15 +1,18 @@
 """Generate the golden fixtures from the reference's own hot-path code.
 
-Run in a container that has the reference source tree (path from the
-CROWDDYNAMICS_REFERENCE environment variable, default /root/reference):
+Run where the reference source tree is present, its project root named by
+the CROWDDYNAMICS_REFERENCE environment variable:
 
-    python tests/golden/make_golden.py
+    CROWDDYNAMICS_REFERENCE=<crowddynamics checkout> python tests/golden/make_golden.py [case ...]
 
 It executes the reference's numba-decorated functions as plain Python via
 ``oracle/ref_loader.py`` (numba, cell_lists and the agents module stubbed)
 on seeded inputs and stores inputs and outputs in ``tests/golden/*.npz``.
-Each case records the grid of the restated cell list it used.
+Each case records the grid of the restated cell list it used.  The
+``rollout`` case runs the reference with numba's scalar semantics (the C
+library's elementary functions, literal integer powers as products).
 """
+import hashlib
 import os
 import sys
 
@@ -257,12 +260,62 @@ def exit_cases():
          grid=np.array(scen.grid, dtype=np.float64))
 
 
+def input_digest(*arrays):
+    """sha256 of the inputs' bytes (the fixture stores it instead of the
+    inputs, which the seeded generators rebuild)."""
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+ROLLOUTS = {'hallway': (lambda: S.hallway(), 50, 7, 10),      # config 0: 400 Circular
+            'room': (lambda: S.room(), 3, 8, 3)}              # config 1: 2000 ThreeCircle
+ROLLOUT_FIELDS = ('position', 'velocity', 'force_prev', 'orientation', 'angular_velocity',
+                  'torque_prev')
+
+
+def rollout_noise(scen, steps, seed):
+    """The host-drawn fluctuation noise of every step (drawn from the state's
+    parameters, which do not change over a rollout)."""
+    rng = np.random.default_rng(seed)
+    out = [S.draw_noise(scen.agents, rng) for _ in range(steps)]
+    return [f for f, _ in out], [m for _, m in out]
+
+
+def rollout_cases():
+    """The reference's own update() on config 0 (the 400-agent Circular
+    hallway) for 50 steps and on config 1 (the 2000-agent ThreeCircle room)
+    for 3 steps, with host-drawn noise, run with numba's scalar semantics;
+    states every `every` steps."""
+    out = {}
+    for name, (make, steps, seed, every) in ROLLOUTS.items():
+        scen = make()
+        RL.configure_grid(*scen.grid)
+        nf, nm = rollout_noise(scen, steps, seed)
+        a = scen.agents.copy()
+        out[name + '_digest'] = np.array(input_digest(a, scen.walls, *nf,
+                                                      *[m for m in nm if m is not None]))
+        dts = []
+        for k in range(steps):
+            dts.append(RL.step(a, scen.cell_size, scen.walls, nf[k], nm[k], scen.dt_min,
+                               scen.dt_max, nodes=NODES_ALL, math='libm'))
+            if (k + 1) % every == 0:
+                for f in ROLLOUT_FIELDS:
+                    if f in a.dtype.names:
+                        out['%s_%s_%d' % (name, f, k + 1)] = np.ascontiguousarray(a[f])
+            print(name, k + 1, flush=True)
+        out[name + '_dt'] = np.array(dts)
+    save('rollout', **out)
+
+
 CASES = {'scenarios': lambda: (
              scenario_case('hallway_small', S.hallway(n=120, width=20.0, height=6.0, seed=3), 3,
                            21),
              scenario_case('room_small', S.room(n=150, size=12.0, seed=4), 3, 22)),
          'pairs': pair_cases, 'walls': wall_cases, 'misc': misc_cases,
-         'navigation': navigation_cases, 'herding': herding_cases, 'exit': exit_cases}
+         'navigation': navigation_cases, 'herding': herding_cases, 'exit': exit_cases,
+         'rollout': rollout_cases}
 
 
 def main():

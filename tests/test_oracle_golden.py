@@ -169,3 +169,44 @@ def test_exit_fixture_reproduces_reference():
     a['target'][mask] = targets[mask]
     a['is_follower'][mask] = False
     assert np.array_equal(a, d['after'])
+
+
+# ---- the reference's own update() at scale (tests/golden/rollout.npz) -------
+
+def _rollout_inputs(name):
+    """The seeded inputs of the rollout fixture, rebuilt and checked against
+    the digest it stores."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        'make_golden', os.path.join(GOLDEN, 'make_golden.py'))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    make, steps, seed, every = mg.ROLLOUTS[name]
+    scen = make()
+    nf, nm = mg.rollout_noise(scen, steps, seed)
+    digest = mg.input_digest(scen.agents, scen.walls, *nf, *[m for m in nm if m is not None])
+    return scen, nf, nm, steps, every, digest, mg.ROLLOUT_FIELDS
+
+
+@pytest.mark.parametrize('name', ['hallway', 'room'])
+def test_oracle_reproduces_reference_rollouts(oracle, name):
+    """The C oracle with the C library's elementary functions reproduces the
+    reference's own update(), run with numba's scalar semantics, bit for bit:
+    config 0 (400 Circular agents, two walls) over 50 steps and config 1
+    (2000 ThreeCircle agents in the 30 m room) over 3 steps, with host noise."""
+    g = load('rollout')
+    scen, nf, nm, steps, every, digest, fields = _rollout_inputs(name)
+    assert str(g[name + '_digest']) == digest, 'the seeded inputs changed'
+    grid = oracle.make_grid(*scen.grid)
+    a = scen.agents.copy()
+    for k in range(steps):
+        dt = oracle.step(a, grid, scen.walls, nf[k], nm[k], dt_min=scen.dt_min,
+                         dt_max=scen.dt_max)
+        assert dt == g[name + '_dt'][k], k
+        if (k + 1) % every == 0:
+            for f in fields:
+                if f in a.dtype.names:
+                    ref = g['%s_%s_%d' % (name, f, k + 1)]
+                    got = np.ascontiguousarray(a[f])
+                    assert np.array_equal(got.view(np.uint64), ref.view(np.uint64)), \
+                        (k + 1, f, float(np.abs(got - ref).max()))
