@@ -76,7 +76,32 @@ def parse():
     ap.add_argument('--no-states', action='store_true')
     ap.add_argument('--detail', default=os.path.join('gpurun_out', 'bench_detail.json'),
                     help='file for the per-leg detail the JSON line leaves out')
+    ap.add_argument('--profile-range', default=None,
+                    choices=('step', 'records', 'adjoint', 'states'),
+                    help='bracket one instance of that work with cudaProfilerStart/Stop '
+                         '(for ncu --profile-from-start off); no work is skipped')
     return ap.parse_args()
+
+
+class ProfileRange:
+    """cudaProfilerStart/Stop around a block when `on` (one capture range
+    for ncu --profile-from-start off), synchronised on both sides."""
+
+    def __init__(self, on):
+        self.on = bool(on)
+
+    def __enter__(self):
+        if self.on:
+            import torch
+            torch.cuda.synchronize()
+            torch.cuda.profiler.start()
+        return self
+
+    def __exit__(self, *exc):
+        if self.on:
+            import torch
+            torch.cuda.synchronize()
+            torch.cuda.profiler.stop()
 
 
 def dist_env():
@@ -308,7 +333,8 @@ def run_ours(args, ws, rank, local):
         for k in range(args.steps):
             flush.fill_(k & 0xff)
             torch.cuda.synchronize()
-            b.run(1, nodes)
+            with ProfileRange(args.profile_range == 'step' and k == args.steps - 1):
+                b.run(1, nodes)
     barrier()
     kt = b.kernel_time()
     b.set_timing(False)
@@ -344,13 +370,15 @@ def run_ours(args, ws, rank, local):
     # host wall clock: three timed passes of `steps` steps, the median kept
     # (a single pass can catch an unrelated host stall)
     trials = []
-    for _ in range(3):
+    for trial in range(3):
         barrier()
         t0 = time.perf_counter()
-        for _ in range(args.steps):
-            b.upload(rec)
-            b.launch(1, nodes)     # download waits for the step and checks its status
-            b.download(rec)
+        for k in range(args.steps):
+            with ProfileRange(args.profile_range == 'records' and trial == 2 and
+                              k == args.steps - 1):
+                b.upload(rec)
+                b.launch(1, nodes)     # download waits for the step and checks its status
+                b.download(rec)
         e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
         trials.append(whole_job_rate(ws, n, args.steps, e2e_s))
     e2e = sorted(trials)[1]
@@ -436,13 +464,13 @@ def run_ours(args, ws, rank, local):
         detail['save'] = d
         legs['async_save_over_host_save'] = d['async_save'] / d['host_save']
     if not args.no_states:
-        detail['states'] = run_states(max(args.steps, 10))
+        detail['states'] = run_states(max(args.steps, 10), profile=args.profile_range == 'states')
     if legs:
         line['legs'] = legs
     if not args.no_batched:
         line['batched'], detail['batched'] = run_batched(args.steps, args.warmup, flush)
     if not args.no_adjoint:
-        line['adjoint'], detail['adjoint'] = run_adjoint()
+        line['adjoint'], detail['adjoint'] = run_adjoint(profile=args.profile_range == 'adjoint')
     if args.detail:
         try:
             os.makedirs(os.path.dirname(os.path.abspath(args.detail)), exist_ok=True)
@@ -560,7 +588,7 @@ def run_save(steps, n=2000, size=30.0):
     return out
 
 
-def run_states(steps, n=2000, size=30.0):
+def run_states(steps, n=2000, size=30.0, profile=False):
     """The state nodes between steps on the ThreeCircle room (2000 agents,
     5 walls plus 3 interior walls): LeaderFollowerWithHerding (10% leaders,
     70% followers, 5 nearest within 10 m), InsideDomain and TargetReached;
@@ -589,7 +617,8 @@ def run_states(steps, n=2000, size=30.0):
                      ('leader_follower', lambda: b.herding(False, sight_follower=1.0)),
                      ('inside_domain', lambda: b.inside_domain(0, domain)),
                      ('target_reached', lambda: b.target_reached(0, exit_))):
-        fn()
+        with ProfileRange(profile):
+            fn()
         b.synchronize()
         t0 = time.perf_counter()
         for _ in range(steps):
@@ -698,7 +727,8 @@ def run_batched(steps, warmup, flush=None):
     return line, detail
 
 
-def run_adjoint(n=5000, width=80.0, height=20.0, steps=400, ckpt=20, seed=4, fd_steps=10):
+def run_adjoint(n=5000, width=80.0, height=20.0, steps=400, ckpt=20, seed=4, fd_steps=10,
+                profile=False):
     """Differentiable form: Circular hallway 80 m x 20 m, 5000 agents,
     400-step rollout, loss = mean squared position error against a rollout
     with hidden tau_adj ~ U(0.3, 0.7) and target speed ~ N(1.2, 0.2); the
@@ -727,6 +757,9 @@ def run_adjoint(n=5000, width=80.0, height=20.0, steps=400, ckpt=20, seed=4, fd_
         return b.rollout_loss(t, target[:t], ckpt, grads=grads)
 
     rollout(a, True)                                    # warm-up (graph capture, allocation)
+    if profile:
+        with ProfileRange(True):
+            rollout(a, True, ckpt)                      # one checkpoint segment
     fwd_only = []
     full = []
     for _ in range(3):

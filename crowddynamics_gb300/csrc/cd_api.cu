@@ -504,6 +504,9 @@ int check_device_error(cd_ctx *c, bool enqueued = false) {
         cudaStreamSynchronize(c->stream);
         if (h & cdk::ERR_NOT_FINITE)
             return fail(c, CD_ERR_NOT_FINITE, "an agent position is not finite");
+        if (h & cdk::ERR_LEADER_FOLLOWER)
+            return fail(c, CD_ERR_INVALID_VALUE,
+                        "an agent is both leader and follower (is_leader and is_follower)");
         if (h & cdk::ERR_RANGE)
             return fail(c, CD_ERR_INVALID_VALUE,
                         "an agent is more than 1e7 m from its scenario's grid origin");
@@ -913,6 +916,8 @@ int cd_herding(cd_ctx *c, int with_herding, double sight_follower, int64_t size_
         return fail(c, CD_ERR_INVALID_VALUE, "bad sight");
     const int64_t n = c->n;
     if (n == 0) return CD_OK;
+    cdk::launch_check_roles(state_cols(c), (int)n, c->err, c->stream);
+    if (int rc = check_device_error(c)) return rc;
     const int K = with_herding ? (int)size_nearest_other : 1;
     const int64_t scan = cdk::scan_scratch_ints((int)n);
     if (!c->herd) {

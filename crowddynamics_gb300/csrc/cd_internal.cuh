@@ -24,6 +24,8 @@ constexpr int WALL_D = 8;          // p0x p0y p1x p1y tx ty lw -
 constexpr int ERR_NOT_FINITE = 1;
 // An agent farther than COORD_MAX (cd_cull.cuh) from its scenario's grid origin.
 constexpr int ERR_RANGE = 4;
+// A record flagged both leader and follower (cd_herding rejects it).
+constexpr int ERR_LEADER_FOLLOWER = 8;
 
 // Candidate chunks per agent whose ballots the near-list count keeps for the
 // fill (an agent with more is evaluated again by the fill).
@@ -144,6 +146,8 @@ struct HerdArgs {
     int *tgt_before;                 // targets before the update
     double sight_f, sight_l, cos_phi, w_herd, w_lead, w_dir;
 };
+// Sets ERR_LEADER_FOLLOWER in *err if any record is both leader and follower.
+void launch_check_roles(const StateCols &st, int n, int *err, cudaStream_t s);
 void launch_herd_neighbors(const HerdArgs &h, cudaStream_t s);
 void launch_leaders(const HerdArgs &h, int *flags, int *pos, int *scan_scratch, int *list,
                     cudaStream_t s);

@@ -149,6 +149,15 @@ __global__ void __launch_bounds__(HNT) k_herd_neighbors(HerdArgs h) {
     }
 }
 
+// The reference's follower loop reads the targets of leaders it may already
+// have updated as followers (core/steering/collective_motion.py:186-216);
+// the device reads the targets from before the update, so both roles at
+// once are rejected before any state is written.
+__global__ void k_check_roles(StateCols st, int n, int *err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && st.leader[i] && st.follower[i]) atomicOr(err, ERR_LEADER_FOLLOWER);
+}
+
 __global__ void k_leader_flags(HerdArgs h, int *flags) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < h.n) flags[i] = h.st.leader[i] ? 1 : 0;
@@ -313,11 +322,18 @@ __global__ void k_exit_detection(int begin, int count, const double *x, const do
     }
 }
 
-// Crossings test (E. Haines, "Point in polygon strategies", Graphics Gems IV,
-// 1994): a horizontal ray from the point crosses the edges an odd number of
-// times.  The ring's closing edge runs from the last vertex to the first.
+// Point in polygon as the reference's nodes compute it with matplotlib's
+// Path.contains_points (simulation/logic.py:348-357,372-387): the "crossings
+// multiply" test of E. Haines (Point in Polygon Strategies, Graphics Gems IV,
+// 1994).  A ray from the point towards +x; an edge from an earlier vertex p0
+// to the next p1 is a candidate when the flags (p.y >= ty) differ, and is
+// crossed when ((p1.y - ty) * (p0.x - p1.x) >= (p1.x - tx) * (p0.y - p1.y))
+// equals p1's flag; an odd count is inside.  The path is closed (the edge from
+// the last vertex to the first is tested; a repeated first vertex only adds
+// an edge of length zero) and a point with a non-finite coordinate is outside.
 __device__ __forceinline__ bool inside_polygon(double tx, double ty, const double2 *v, int m) {
     bool inside = false;
+    if (!(isfinite(tx) && isfinite(ty)) || m < 1) return false;
     double2 p0 = v[m - 1];
     bool y0 = p0.y >= ty;
     for (int k = 0; k < m; ++k) {
@@ -371,6 +387,9 @@ inline int nblk(long long n, int nt) { return (int)((n + nt - 1) / nt); }
 void launch_herd_neighbors(const HerdArgs &h, cudaStream_t s) {
     if (h.n > 0 && h.with_herding)
         k_herd_neighbors<<<nblk((long long)h.n * 32, HNT), HNT, 0, s>>>(h);
+}
+void launch_check_roles(const StateCols &st, int n, int *err, cudaStream_t s) {
+    if (n > 0) k_check_roles<<<nblk(n, 256), 256, 0, s>>>(st, n, err);
 }
 void launch_leaders(const HerdArgs &h, int *flags, int *pos, int *scan_scratch, int *list,
                     cudaStream_t s) {

@@ -76,7 +76,7 @@ class LogicNodeBase:
         for node in pre_order(self.root):
             if node.name == item:
                 return node
-        raise KeyError('Key: "{}" not in the tree.'.format(item))
+        raise KeyError('no node named %r in this logic tree' % (item,))
 
 
 def pre_order(node):

@@ -161,7 +161,10 @@ int cd_snapshot_wait(cd_ctx *ctx, int slot);
  * `size_nearest_other` <= 16 unobstructed neighbours within `sight_follower`,
  * on a cell list of that cell size).  Reference arguments: sight_leader 20
  * (herding) or the node's sight, phi 0.45 pi, weights 0.15 (herding
- * position), 0.40 (leader position), 0.65 (leader direction). */
+ * position), 0.40 (leader position), 0.65 (leader direction).  A record
+ * that is both leader and follower is rejected with CD_ERR_INVALID_VALUE
+ * before any state changes (the reference's serial follower loop would read
+ * targets it has already updated in that case). */
 int cd_herding(cd_ctx *ctx, int with_herding, double sight_follower,
                int64_t size_nearest_other, double sight_leader, double phi,
                double w_herding, double w_leader, double w_direction);

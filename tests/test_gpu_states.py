@@ -12,7 +12,7 @@ import pytest
 from crowddynamics_gb300 import scenarios as S
 from crowddynamics_gb300.engine import DeviceBatch, walls_as_rows
 from crowddynamics_gb300.simulation import logic as L
-from crowddynamics_gb300.simulation.agents import Agents
+from crowddynamics_gb300.simulation.agents import Agents, new_agents
 from crowddynamics_gb300.simulation.field import Field
 from crowddynamics_gb300.simulation.multiagent import MultiAgentSimulation
 
@@ -66,16 +66,44 @@ def test_herding_node_in_simulation(native):
 
 
 def crossings(points, poly):
-    """Haines' crossings test in numpy (test restatement)."""
-    px, py = points[:, 0], points[:, 1]
-    inside = np.zeros(len(points), bool)
-    p0 = poly[-1]
-    for p1 in poly:
-        y0, y1 = p0[1] >= py, p1[1] >= py
-        hit = (y0 != y1) & (((p1[1] - py) * (p0[0] - p1[0]) >= (p1[0] - px) * (p0[1] - p1[1])) == y1)
-        inside ^= hit
-        p0 = p1
-    return inside
+    """matplotlib's Path(poly).contains_points(points), restated by the oracle."""
+    from oracle.pip import contains_points
+    return contains_points(points, poly)
+
+
+RINGS = {
+    'square_ccw': [(0, 0), (4, 0), (4, 4), (0, 4)],
+    'square_cw_closed': [(0, 0), (0, 4), (4, 4), (4, 0), (0, 0)],
+    'concave': [(0, 0), (8, 0), (8, 4), (5, 4), (4, 1), (3, 4), (0, 4)],
+    'triangle': [(0.5, 0.25), (7.75, 1.5), (2.25, 5.5)],
+}
+
+
+@pytest.mark.parametrize('ring', sorted(RINGS))
+def test_inside_domain_boundary_conventions(native, ring):
+    """Points on a 0.25 m lattice (every vertex and the edges' lattice points
+    among them, on the boundary bit for bit), random points and non-finite
+    positions: the device's inside flags equal the oracle's restatement of
+    matplotlib's crossings test, with its half-open edge conventions."""
+    poly = np.array(RINGS[ring], float)
+    g = np.arange(-1.0, 9.01, 0.25)
+    gx, gy = np.meshgrid(g, g, indexing='ij')
+    rng = np.random.default_rng(4)
+    pts = np.vstack([np.column_stack([gx.ravel(), gy.ravel()]), rng.uniform(-1, 9, (2000, 2)),
+                     [(np.nan, 1.0), (1.0, np.inf), (-np.inf, 2.0)]])
+    a = new_agents(len(pts), 'circular')
+    a['position'] = pts
+    a['active'] = True
+    b = DeviceBatch('circular', [dict(n_agents=len(a), n_walls=0, grid=(-1.0, -1.0, 3.7, 3, 3))])
+    b.upload(a)
+    b.inside_domain(0, poly)
+    got = a.copy()
+    b.download(got)
+    b.close()
+    want = crossings(pts, poly)
+    bad = np.flatnonzero(got['active'] != want)
+    assert bad.size == 0, pts[bad[:5]]
+    assert want.any() and (~want).any()
 
 
 def test_inside_domain_and_target_reached(native):
@@ -137,3 +165,31 @@ def test_exit_detection_matches_reference(native):
     b.close()
     assert np.array_equal(got['target'], want['target'])
     assert np.array_equal(got['is_follower'], want['is_follower'])
+
+
+def test_herding_rejects_leader_and_follower(native):
+    """A record flagged both leader and follower is rejected before any state
+    changes; the same crowd without that record runs."""
+    from crowddynamics_gb300.exceptions import InvalidValue
+    scen = S.room(n=200, size=15.0, seed=5)
+    a = scen.agents
+    rng = np.random.default_rng(2)
+    a['is_leader'] = rng.uniform(size=len(a)) < 0.1
+    a['is_follower'] = ~a['is_leader'] & (rng.uniform(size=len(a)) < 0.7)
+    a['target'] = np.where(a['is_leader'], 0, -1)
+    bad = a.copy()
+    k = int(np.flatnonzero(bad['is_leader'])[0])
+    bad['is_follower'][k] = True
+    b = DeviceBatch('three_circle', [dict(n_agents=len(a), n_walls=len(scen.walls),
+                                          grid=scen.grid)])
+    b.set_walls(scen.walls)
+    b.upload(bad)
+    with pytest.raises(InvalidValue, match='leader and follower'):
+        b.herding(True)
+    got = bad.copy()
+    b.download(got)
+    assert np.array_equal(got['target_direction'], bad['target_direction'])
+    assert np.array_equal(got['target'], bad['target'])
+    b.upload(a)
+    b.herding(True)
+    b.close()

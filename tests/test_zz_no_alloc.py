@@ -56,10 +56,48 @@ def context_forces(scen):
     return out
 
 
-@pytest.mark.parametrize('make', [S.hallway, S.room], ids=['circular', 'three_circle'])
-def test_noalloc_matches_context_path(native, make):
+def regridded(scen, bounds):
+    """The scenario on another cell grid (same agents)."""
+    return S.Scenario(scen.name, scen.agents, scen.walls, bounds, scen.cell_size)
+
+
+def field_16k():
+    """16,000 ThreeCircle agents on a 67 x 67 grid (4489 cells: the
+    multi-block cell scan; the context path runs its pair pipeline here, the
+    entry point its lane-group twin)."""
+    return S.large_field(n=16000, size=240.0, n_walls=0, seed=8)
+
+
+def hallway_max_cells():
+    """The 400-agent hallway on a grid of exactly CD_NOALLOC_MAX_CELLS cells."""
+    scen = S.hallway()
+    side = int(N.NOALLOC_MAX_CELLS ** 0.5)
+    return regridded(scen, (0.0, 0.0, side * scen.cell_size, side * scen.cell_size))
+
+
+def room_outside_grid():
+    """The room on a grid covering only its lower-left 12 m x 12 m: most
+    agents lie outside it and are binned into its border cells."""
+    scen = moving_room()
+    return regridded(scen, (0.0, 0.0, 12.0, 12.0))
+
+
+def moving_room():
+    scen = S.room()
+    scen.agents['velocity'] = np.random.default_rng(3).normal(0, 1.0, (len(scen.agents), 2))
+    return scen
+
+
+CASES = {'circular': S.hallway, 'three_circle': S.room, 'three_circle_16k': field_16k,
+         'circular_max_cells': hallway_max_cells, 'three_circle_outside_grid': room_outside_grid}
+
+
+@pytest.mark.parametrize('case', list(CASES))
+def test_noalloc_matches_context_path(native, case):
     import torch
-    scen = make()
+    scen = CASES[case]()
+    assert len(scen.agents) <= N.NOALLOC_MAX_AGENTS
+    assert scen.grid[3] * scen.grid[4] <= N.NOALLOC_MAX_CELLS
     ref = context_forces(scen)
     three = scen.body == 'three_circle'
     lib = native.load()
