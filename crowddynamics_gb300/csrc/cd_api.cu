@@ -87,7 +87,7 @@ struct cd_ctx {
     int *fw_cnt = nullptr, *fw_off = nullptr, *fw_scan = nullptr;
     int *fs_cnt = nullptr, *fs_off = nullptr, *fs_scan = nullptr;
     int2 *fw_pairs = nullptr;
-    int *defer_list = nullptr;                     // ThreeCircle: the float32 pass's leftovers
+    int *defer_list = nullptr;                     // the float32 pair pass's leftovers
     int64_t nl_cap = 0;
     bool nl_fixed = false;              // capacity set by cd_set_near_list_capacity
 
@@ -373,8 +373,7 @@ int alloc_near_lists(cd_ctx *c, int64_t cap) {
         if (int rc = dalloc(c, &c->nl_res, cap * res_d)) return rc;
         if (int rc = dalloc(c, &c->nl_kind, cap)) return rc;
         if (int rc = dalloc(c, &c->fw_pairs, cap)) return rc;
-        if (c->body == CD_BODY_THREE_CIRCLE)
-            if (int rc = dalloc(c, &c->defer_list, cap)) return rc;
+        if (int rc = dalloc(c, &c->defer_list, cap)) return rc;
     }
     c->nl_cap = cap;
     if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; c->graph_nodes = -1; }

@@ -109,7 +109,7 @@ struct StepArgs {
     int *fw_cnt, *fw_off;        // per slot: entries with a later slot (n + 1 each)
     int2 *fw_pairs;              // flat list of (slot, entry) for those entries
     int *defer_list;             // flat-list indices the float32 pair pass left to k_pairs
-                                 // (nl_cap entries; ThreeCircle contexts, else null)
+                                 // (nl_cap entries; null: no float32 pass)
     int *fw_scan;                // scan scratch (as nl_scan)
     int *fs_cnt, *fs_off;        // per agent: those guessed to need the social force, scan
     int *fs_scan;                // scan scratch (as nl_scan)

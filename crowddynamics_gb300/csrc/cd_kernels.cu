@@ -245,7 +245,6 @@ __global__ void __launch_bounds__(PREP_NT) k_prepare(StepArgs a) {
         }
         a.key[i] = key;
         atomicAdd(&a.count[key], 1);
-        l = cdm_hypot(a.col[VX][i], a.col[VY][i]);      // length(velocity)
     }
     // per-scenario max |v| (NaN and 0 ignored, like `if l > v_max`): one
     // atomic per block when its agents share a scenario (fmax is exact, so
@@ -254,7 +253,30 @@ __global__ void __launch_bounds__(PREP_NT) k_prepare(StepArgs a) {
     __shared__ double wmax[PREP_NT / 32];
     if (threadIdx.x == 0) s_block = s;
     __syncthreads();
+    const double vx = i < a.n ? a.col[VX][i] : 0.0, vy = i < a.n ? a.col[VY][i] : 0.0;
     if (__syncthreads_and(s == s_block || s < 0)) {
+        // length(velocity) = hypot(vx, vy) only where it can be the block's
+        // maximum: q = vx^2 + vy^2 is within 4 ulp of |v|^2, so a lane whose q
+        // lies 2^-40 below the block's largest q has a |v| smaller by far
+        // more than hypot's 2 ulp and cannot hold the maximum.  Non-finite q,
+        // and blocks whose largest q is tiny (squares near underflow), take
+        // hypot everywhere.
+        const double q = vx * vx + vy * vy;
+        double qm = (q > 0) ? q : 0.0;
+        for (int o = 16; o > 0; o >>= 1) {
+            const double t = __shfl_xor_sync(0xffffffffu, qm, o);
+            qm = (t > qm) ? t : qm;
+        }
+        if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = qm;
+        __syncthreads();
+        qm = wmax[0];
+#pragma unroll
+        for (int w = 1; w < PREP_NT / 32; ++w) qm = (wmax[w] > qm) ? wmax[w] : qm;
+        __syncthreads();                                // wmax is reused below
+        const double thr = !(qm >= 0x1p-900) ? 0.0
+                           : (qm <= 0x1.fffffffffffffp+1023 ? qm * (1.0 - 0x1p-40)
+                                                            : 0x1.fffffffffffffp+1022);
+        if (s >= 0 && !(q < thr)) l = cdm_hypot(vx, vy);
         double m = (l > 0) ? l : 0.0;
         for (int o = 16; o > 0; o >>= 1) {
             const double t = __shfl_xor_sync(0xffffffffu, m, o);
@@ -270,8 +292,9 @@ __global__ void __launch_bounds__(PREP_NT) k_prepare(StepArgs a) {
             }
             if (threadIdx.x == 0 && s_block >= 0 && m > 0) atomicMax(&a.vmax[s_block], ord_bits(m));
         }
-    } else if (s >= 0 && l > 0) {
-        atomicMax(&a.vmax[s], ord_bits(l));
+    } else if (s >= 0) {
+        l = cdm_hypot(vx, vy);
+        if (l > 0) atomicMax(&a.vmax[s], ord_bits(l));
     }
 }
 
@@ -646,9 +669,14 @@ __global__ void k_gather(StepArgs a, int part) {
             p[5] = make_double2(c[DAMP][i], 0.0);
         }
         if (part != 2) {
-            const float xf = (float)(c[X][i] - ox), yf = (float)(c[Y][i] - oy);
+            const double xr = c[X][i] - ox, yr = c[Y][i] - oy;
+            const float xf = (float)xr, yf = (float)yr;
             a.cull[s] = make_float4(xf, yf, up_f(c[R][i]) + cull_slack(xf, yf),
                                     pack_velocity(c[VX][i], c[VY][i]));
+            // position = float hi (cull) + float lo, and the radius, for the
+            // float32 pair pass (circ_pair_light)
+            a.stage_f[2 * s] = make_float4((float)(xr - (double)xf), (float)(yr - (double)yf),
+                                           (float)c[R][i], 0.f);
         }
     } else {
         double x = c[X][i], y = c[Y][i];
@@ -1597,6 +1625,55 @@ __device__ __forceinline__ int tc_pair_light(const StepArgs &a, int s, int t) {
     return RES_ZERO;                                     // no sub-pair has a root
 }
 
+// The float32 certificates of pair_circular_both for a pair (s, t):
+// RES_NONE where the skin distance is certainly >= 3 m, RES_ZERO where it is
+// certainly in (0, 3) and the pair certainly has no time to collision in
+// (0, 30] (no root; a negative root; or one beyond the 30 s cut-off, with
+// a c >= 1e-9 b^2 so that the float64 root's own cancellation stays below
+// 1e-6 relative), RES_DEFER otherwise (contact, the edges of 3 and 0, roots
+// near 0 or 30, a zero relative speed).  The margins are those of
+// tc_pair_light's sub-pairs: each bounds the float32 error of every input
+// (positions as hi + lo floats relative to the grid origin, radii and the
+// relative velocity rounded once) and operation many times over.
+__device__ __forceinline__ int circ_pair_light(const StepArgs &a, int s, int t) {
+    const float4 meC = __ldg(&a.cull[s]), meF = __ldg(&a.stage_f[2 * s]);
+    const float4 oC = __ldg(&a.cull[t]), oF = __ldg(&a.stage_f[2 * t]);
+    const float dx = (meC.x - oC.x) + (meF.x - oF.x);
+    const float dy = (meC.y - oC.y) + (meF.y - oF.y);
+    const float rt = meF.z + oF.z;
+    const float x2 = dx * dx + dy * dy;
+    const float h = sqrtf(x2) - rt;
+    const float dmarg = PRESEL_MARGIN + 1e-6f * (fabsf(dx) + fabsf(dy) + rt);
+    if (h - dmarg >= (float)SIGTH_SOC) return RES_NONE;
+    if (!(h + dmarg < (float)SIGTH_SOC && h - dmarg > 0.f)) return RES_DEFER;
+    // interacting without contact: a force only from a time to collision
+    // in (0, 30] (the relative velocity as pair_circular_both forms it)
+    const double2 vp = __ldg(&a.stage[(size_t)s * STAGE_Q_CIRC + 1]);
+    const double2 vq = __ldg(&a.stage[(size_t)t * STAGE_Q_CIRC + 1]);
+    const float vxf = (float)(vp.x - vq.x), vyf = (float)(vp.y - vq.y);
+    if (!(fabsf(vxf) > 1e-20f || fabsf(vyf) > 1e-20f)) return RES_DEFER;
+    const float af = vxf * vxf + vyf * vyf;
+    const float e0 = 1e-6f * (1.f + fabsf(dx) + fabsf(dy));
+    const float bf = -(dx * vxf + dy * vyf);
+    const float cf = x2 - rt * rt;
+    const float acf = af * cf;
+    const float discf = bf * bf - acf;
+    const float m = 1e-5f * af * (1.f + x2 + rt * rt) + 1e-6f * (bf * bf + fabsf(acf));
+    if (discf < -m) return RES_ZERO;                     // no root
+    if (!(discf > m)) return RES_DEFER;
+    const float mb = 4.f * e0 * (fabsf(vxf) + fabsf(vyf)) +
+                     1e-6f * (fabsf(dx * vxf) + fabsf(dy * vyf));
+    const float mc = 8.f * e0 * (fabsf(dx) + fabsf(dy) + rt) + 1e-6f * (x2 + rt * rt);
+    if (bf < -mb) return RES_ZERO;                       // tau = (b - d) / a < 0
+    const float bb = (fabsf(bf) + mb) * (fabsf(bf) + mb);
+    if (bf > mb && cf > mc && 0.99f * af * (cf - mc) > 1e-9f * bb) {
+        // tau = c / (b + d) from below
+        const float lo = (cf - mc) / ((bf + mb) + sqrtf(discf + m)) * 0.99999f;
+        if (lo > (float)TAU_MAX * 1.00001f) return RES_ZERO;
+    }
+    return RES_DEFER;
+}
+
 // Resumable candidate enumeration into the thread's list (visiting order:
 // 3 x 3 cells in (dx, dy) lexicographic order, each cell ascending).
 struct EnumState { int ck, t; };
@@ -2305,12 +2382,13 @@ __device__ __forceinline__ void put_pair(const StepArgs &a, int e, int res, doub
     a.nl_kind[e] = kind;
 }
 
-// ThreeCircle bodies: the pairs of the flat list's second part (not guessed
-// to need the social force), in float32 alone (tc_pair_light): a decided
-// pair writes the kind bytes of both its entries; the others are appended
-// to defer_list for k_pairs, which takes them after the first part.  Few
+// The pairs of the flat list's second part (not guessed to need the social
+// force), in float32 alone (tc_pair_light, circ_pair_light): a decided pair
+// writes the kind bytes of both its entries; the others are appended to
+// defer_list for k_pairs, which takes them after the first part.  Few
 // registers, so many warps per SM hide the loads.  Warps take 32
 // consecutive pairs at a time, in turn.
+template <int BODY>
 __global__ void __launch_bounds__(NTG) k_pairs_light(StepArgs a) {
     pdl_enter();
     constexpr unsigned FULL = 0xffffffffu;
@@ -2327,7 +2405,7 @@ __global__ void __launch_bounds__(NTG) k_pairs_light(StepArgs a) {
             s = pe.x;
             e = pe.y;
             t = __ldg(&a.nl_idx[e]);
-            res = tc_pair_light(a, s, t);
+            res = BODY == 1 ? tc_pair_light(a, s, t) : circ_pair_light(a, s, t);
         }
         const unsigned dm = __ballot_sync(FULL, k < npairs && res == RES_DEFER);
         if (dm) {
@@ -2357,9 +2435,8 @@ __global__ void __launch_bounds__(NTG, 3) k_pairs(StepArgs a) {
     extern __shared__ unsigned char smem[];
     PairQueue *wq = reinterpret_cast<PairQueue *>(smem);
     const int lane = threadIdx.x & 31;
-    // after k_pairs_light (ThreeCircle): the first part, then the pairs the
-    // float32 pass left
-    const bool split = BODY == 1 && a.defer_list != nullptr;
+    // after k_pairs_light: the first part, then the pairs the float32 pass left
+    const bool split = a.defer_list != nullptr;
     const int nfirst = split ? a.fs_off[a.n] : a.fw_off[a.n];
     const int npairs = split ? nfirst + a.work[1] : nfirst;
     // the next chunk's pair and partner are loaded before this chunk is
@@ -3045,6 +3122,7 @@ constexpr int N_PAIR_L = 3;
 constexpr ForcesFn kNlCount[N_PAIR_L] = {k_nl_count<4>, k_nl_count<8>, k_nl_count<16>};
 constexpr ForcesFn kNlFill[N_PAIR_L] = {k_nl_fill<4>, k_nl_fill<8>, k_nl_fill<16>};
 constexpr ForcesFn kPairs[2] = {k_pairs<0>, k_pairs<1>};
+constexpr ForcesFn kPairsLight[2] = {k_pairs_light<0>, k_pairs_light<1>};
 constexpr ForcesFn kFallback[2][N_PAIR_L] = {
     {k_forces_fallback<0, 4>, k_forces_fallback<0, 8>, k_forces_fallback<0, 16>},
     {k_forces_fallback<1, 4>, k_forces_fallback<1, 8>, k_forces_fallback<1, 16>}};
@@ -3082,7 +3160,7 @@ int variant_staged(int variant) {
 // Resident blocks of each force kernel variant (and pair kernel) on each device.
 int g_forces_blocks[64][2][N_VARIANTS];
 int g_pairs_blocks[64][2][N_PAIR_L];
-int g_light_blocks[64];
+int g_light_blocks[64][2];
 
 int init_kernels() {
     int dev = 0, sms = 0;
@@ -3117,10 +3195,11 @@ int init_kernels() {
             if (e == cudaSuccess && dev >= 0 && dev < 64)
                 g_pairs_blocks[dev][body][l] = (nb > 0 ? nb : 1) * sms;
         }
-    if (e == cudaSuccess) {
+    for (int body = 0; body < 2 && e == cudaSuccess; ++body) {
         int nb = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pairs_light, NTG, 0);
-        if (e == cudaSuccess && dev >= 0 && dev < 64) g_light_blocks[dev] = (nb > 0 ? nb : 1) * sms;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kPairsLight[body], NTG, 0);
+        if (e == cudaSuccess && dev >= 0 && dev < 64)
+            g_light_blocks[dev][body] = (nb > 0 ? nb : 1) * sms;
     }
     return e == cudaSuccess ? 0 : (int)e;
 }
@@ -3167,13 +3246,13 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
         // at most one warp per 32 pairs (about 16 pairs per agent): enough blocks
         if (pro && stage_deferred && fork) cudaStreamWaitEvent(s, fork->join_stage, 0);
         if (pair_ev) cudaEventRecordWithFlags(pair_ev[0], s, captured ? cudaEventRecordExternal : 0);
-        if (body == 1 && a.defer_list) {
-            int rl = (dev >= 0 && dev < 64) ? g_light_blocks[dev] : 0;
+        if (a.defer_list) {
+            int rl = (dev >= 0 && dev < 64) ? g_light_blocks[dev][body] : 0;
             if (rl <= 0) rl = 152;
-            k_pairs_light<<<std::min(nblk((long long)a.n * 16, NTG), rl), NTG, 0, s>>>(a);
+            kPairsLight[body]<<<std::min(nblk((long long)a.n * 16, NTG), rl), NTG, 0, s>>>(a);
         }
         // after k_pairs_light: chained to it
-        launch_k(body == 1 && a.defer_list, kPairs[body],
+        launch_k(a.defer_list != nullptr, kPairs[body],
                  std::min(nblk((long long)a.n * 16, NTG), rp), NTG, pairs_smem_bytes(body), s, a);
         if (pair_ev) cudaEventRecordWithFlags(pair_ev[1], s, captured ? cudaEventRecordExternal : 0);
     }

@@ -570,3 +570,148 @@ def test_float32_root_certificates_are_sound():
         checked += int(live.sum())
         pruned_any += int((live & (pruned != queued)).sum())
     assert checked > 100_000 and pruned_any > 1000, (checked, pruned_any)
+
+
+# ---- Circular bodies: circ_pair_light ---------------------------------------
+
+def circ_records(x, r, origin=(0.0, 0.0)):
+    """k_gather's Circular pre-check records: position hi (cull) and lo
+    (stage_f) relative to the grid origin, the radius as float32."""
+    xr, yr = x[:, 0] - origin[0], x[:, 1] - origin[1]
+    xh, yh = xr.astype(F), yr.astype(F)
+    return dict(xh=xh, yh=yh, xl=(xr - xh.astype(np.float64)).astype(F),
+                yl=(yr - yh.astype(np.float64)).astype(F), r=r.astype(F))
+
+
+def circ_light(x, v, r, p, q, origin=(0.0, 0.0), margins=True):
+    """circ_pair_light (csrc/cd_kernels.cu) in numpy float32 for the pairs
+    (p[k], q[k]); margins=False drops every margin."""
+    R = circ_records(x, r, origin)
+    k = F(1.0) if margins else F(0.0)
+    dx = (R['xh'][p] - R['xh'][q]) + (R['xl'][p] - R['xl'][q])
+    dy = (R['yh'][p] - R['yh'][q]) + (R['yl'][p] - R['yl'][q])
+    rt = R['r'][p] + R['r'][q]
+    x2 = dx * dx + dy * dy
+    h = np.sqrt(x2) - rt
+    dmarg = k * (PRESEL_MARGIN + F(1e-6) * ((np.abs(dx) + np.abs(dy)) + rt))
+    out = np.full(len(p), -1, int)
+
+    def decide(mask, value):
+        out[mask & (out < 0)] = value
+
+    decide(h - dmarg >= SIGHT, NONE)
+    decide(~((h + dmarg < SIGHT) & (h - dmarg > F(0))), DEFER)
+    vxf = (v[p, 0] - v[q, 0]).astype(F)
+    vyf = (v[p, 1] - v[q, 1]).astype(F)
+    decide(~((np.abs(vxf) > F(1e-20)) | (np.abs(vyf) > F(1e-20))), DEFER)
+    af = vxf * vxf + vyf * vyf
+    e0 = F(1e-6) * ((F(1.0) + np.abs(dx)) + np.abs(dy))
+    bf = -(dx * vxf + dy * vyf)
+    cf = x2 - rt * rt
+    acf = af * cf
+    discf = bf * bf - acf
+    m = k * ((F(1e-5) * af) * ((F(1.0) + x2) + rt * rt) + F(1e-6) * (bf * bf + np.abs(acf)))
+    decide(discf < -m, ZERO)
+    decide(~(discf > m), DEFER)
+    mb = k * ((F(4.0) * e0) * (np.abs(vxf) + np.abs(vyf)) +
+              F(1e-6) * (np.abs(dx * vxf) + np.abs(dy * vyf)))
+    mc = k * ((F(8.0) * e0) * ((np.abs(dx) + np.abs(dy)) + rt) + F(1e-6) * (x2 + rt * rt))
+    decide(bf < -mb, ZERO)
+    bb = (np.abs(bf) + mb) * (np.abs(bf) + mb)
+    ok = (bf > mb) & (cf > mc) & ((F(0.99) * af) * (cf - mc) > F(1e-9) * bb)
+    with np.errstate(invalid='ignore', divide='ignore', over='ignore'):
+        lo = (cf - mc) / ((bf + mb) + np.sqrt(discf + m)) * (F(0.99999) if margins else F(1.0))
+    decide(ok & (lo > F(30.0) * (F(1.00001) if margins else F(1.0))), ZERO)
+    decide(np.ones(len(p), bool), DEFER)
+    return out
+
+
+def circ_reference(x, v, r, p, q):
+    """(interacting, force) per pair as pair_circular_both decides in float64
+    (core/interactions.py:51-70, core/motion/power_law.py:213-259): h < 3;
+    contact, or a time to collision in (0, 30]."""
+    xx, xy = x[p, 0] - x[q, 0], x[p, 1] - x[q, 1]
+    rt = r[p] + r[q]
+    h = np.hypot(xx, xy) - rt
+    vx, vy = v[p, 0] - v[q, 0], v[p, 1] - v[q, 1]
+    a = vx * vx + vy * vy
+    b = -(xx * vx + xy * vy)
+    c = (xx * xx + xy * xy) - rt * rt
+    disc = b * b - a * c
+    with np.errstate(invalid='ignore', divide='ignore'):
+        tau = (b - np.sqrt(disc)) / a
+    social = (disc > 0) & (a != 0) & (tau > 0) & (tau <= 30.0)
+    inter = h < 3.0
+    return inter, inter & ((h < 0) | social)
+
+
+def circ_edge_population(n_pairs, seed, center=(0.0, 0.0)):
+    """Circular pairs at the certificates' edges: skin distance within
+    1e-9 .. 1e-2 m of 3 or 0 (or anywhere in [-0.3, 3.5]); relative motion
+    random, head-on, receding, grazing (discriminant near 0), parallel or
+    tiny, or head-on with the time to collision within 1e-7 .. 1e-2 of the
+    30 s cut-off (either side); torsos up to 300 m from `center`."""
+    rng = np.random.default_rng(seed)
+    n = 2 * n_pairs
+    r = rng.uniform(0.2, 0.35, n)
+    p, q = np.arange(0, n, 2), np.arange(1, n, 2)
+    x = np.zeros((n, 2))
+    x[p] = np.asarray(center) + rng.uniform(0, 300.0, (n_pairs, 2))
+    th = rng.uniform(0, 2 * np.pi, n_pairs)
+    u = np.stack((np.cos(th), np.sin(th)), 1)                  # from p towards q
+    kind = rng.integers(0, 3, n_pairs)
+    dh = rng.choice([-1.0, 1.0], n_pairs) * 10.0 ** rng.uniform(-9, -2, n_pairs)
+    h = np.where(kind == 0, 3.0 + dh, np.where(kind == 1, dh, rng.uniform(-0.3, 3.5, n_pairs)))
+    rt = r[p] + r[q]
+    x[q] = x[p] + ((rt + h)[:, None] * u)
+    motion = rng.integers(0, 7, n_pairs)
+    speed = rng.uniform(0.05, 2.0, n_pairs)[:, None]
+    rel = rng.normal(0, 1.0, (n_pairs, 2))
+    rel = np.where((motion == 1)[:, None], speed * u, rel)        # p heads for q
+    rel = np.where((motion == 2)[:, None], -speed * u, rel)       # receding
+    d = rt + h
+    s_ang = np.clip(rt / d * (1 + rng.choice([-1.0, 1.0], n_pairs) *
+                              10.0 ** rng.uniform(-9, -3, n_pairs)), -1.0, 1.0)
+    c_ang = np.sqrt(1 - s_ang * s_ang)
+    sg = rng.choice([-1.0, 1.0], n_pairs)
+    g = np.stack((u[:, 0] * c_ang - sg * u[:, 1] * s_ang, u[:, 1] * c_ang + sg * u[:, 0] * s_ang), 1)
+    rel = np.where((motion == 3)[:, None], speed * g, rel)        # grazing
+    rel = np.where((motion == 4)[:, None], 0.0, rel)
+    tiny = rng.normal(0, 1.0, (n_pairs, 2)) * (10.0 ** rng.uniform(-12, -3, n_pairs))[:, None]
+    rel = np.where((motion == 5)[:, None], tiny, rel)
+    # head-on with tau = (d - rt) / speed near 30 s
+    t30 = 30.0 * (1 + rng.choice([-1.0, 1.0], n_pairs) * 10.0 ** rng.uniform(-7, -2, n_pairs))
+    sp30 = np.maximum(h, 1e-3) / t30
+    rel = np.where((motion == 6)[:, None], sp30[:, None] * u, rel)
+    base = rng.normal(0, 1.0, (n_pairs, 2))
+    v = np.zeros((n, 2))
+    v[q] = base
+    v[p] = base + rel
+    return x, v, r, p, q
+
+
+def test_circular_float32_pair_certificates_are_sound():
+    """circ_pair_light never disagrees with the reference's float64
+    classification, near the origin and at UTM coordinates (grid origin beside
+    the crowd and at (0, 0)); without its margins the same population gives
+    wrong decisions."""
+    total = decided = 0
+    for seed, center, origins in ((50, (0.0, 0.0), ((0.0, 0.0),)),
+                                  (51, (0.0, 0.0), ((0.0, 0.0),)),
+                                  (52, UTM, ((UTM[0] - 20.0, UTM[1] - 20.0), (0.0, 0.0)))):
+        x, v, r, p, q = circ_edge_population(400_000, seed, center)
+        inter, force = circ_reference(x, v, r, p, q)
+        for origin in origins:
+            got = circ_light(x, v, r, p, q, origin)
+            assert np.all((got == NONE) | (got == ZERO) | (got == DEFER))
+            wrong_none = (got == NONE) & inter
+            wrong_zero = (got == ZERO) & (~inter | force)
+            assert not wrong_none.any(), (origin, np.flatnonzero(wrong_none)[:5])
+            assert not wrong_zero.any(), (origin, np.flatnonzero(wrong_zero)[:5])
+        total += len(p)
+        decided += int(np.sum(got != DEFER))
+        if seed == 50:
+            bare = circ_light(x, v, r, p, q, margins=False)
+            wrong = ((bare == NONE) & inter) | ((bare == ZERO) & (~inter | force))
+            assert wrong.sum() > 1000, wrong.sum()
+    assert decided > 0.15 * total, decided / total

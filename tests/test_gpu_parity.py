@@ -590,3 +590,64 @@ def test_non_finite_position_raises(native):
     with pytest.raises(InvalidValue):
         b.step(N.NODE_AGENT_AGENT, want_dt=True)
     b.close()
+
+
+def circular_edge_pairs(seed=31, n_pairs=1500, center=(0.0, 0.0)):
+    """Isolated Circular pairs from the float32 certificates' edge population
+    (tests/test_cpu_certificates.py): skin distances at 3 and 0, grazing,
+    roots near 0 and near the 30 s cut-off, parallel and tiny relative
+    speeds; each pair 15 m from the next."""
+    from crowddynamics_gb300.simulation.agents import new_agents
+    from test_cpu_certificates import circ_edge_population
+    x, v, r, p, q = circ_edge_population(n_pairs, seed)
+    side = int(np.ceil(np.sqrt(n_pairs)))
+    spacing = 15.0
+    k = np.arange(n_pairs)
+    slot = np.stack((10.0 + spacing * (k % side), 10.0 + spacing * (k // side)), 1) + \
+        np.asarray(center)
+    x = x - np.repeat(x[p], 2, axis=0) + np.repeat(slot, 2, axis=0)
+    a = new_agents(2 * n_pairs, 'circular')
+    S._circular_bodies(a, np.random.default_rng(seed), 2 * n_pairs)
+    a['radius'] = r
+    a['position'] = x
+    a['velocity'] = v
+    rows = int(np.ceil(n_pairs / side))
+    bounds = (center[0], center[1], center[0] + 20.0 + spacing * side,
+              center[1] + 20.0 + spacing * rows)
+    return S.Scenario('circular_edge_pairs', a, S.walls_array([]), bounds, 3.7)
+
+
+@pytest.mark.parametrize('variant', [9, 10, 11])
+@pytest.mark.parametrize('where', ['origin', 'utm'])
+def test_circular_certificate_edges(oracle, native, variant, where):
+    """circ_pair_light's certificates at their edges, near the origin and at
+    (5e5, 7e6) m: one full step of the pair pipeline bit for bit."""
+    scen = circular_edge_pairs(center=(0.0, 0.0) if where == 'origin' else (5e5, 7e6))
+    nodes = N.NODE_ALL & ~N.NODE_FLUCTUATION
+    got, _ = device_step(scen, nodes, variant=variant)
+    ref, _ = oracle_step(oracle, scen, nodes, exact=True)
+    assert_identical(got, ref, 'circular edge pairs')
+
+
+@pytest.mark.parametrize('case', ['ties', 'spread', 'tiny', 'huge'])
+def test_timestep_speed_maximum(oracle, native, case):
+    """The per-scenario maximum speed behind the adaptive timestep
+    (core/integrator.py:29-97): k_prepare evaluates hypot only where it can
+    hold a block's maximum.  Speeds equal up to their last bits in every
+    direction, a wide spread, squares that underflow and squares that
+    overflow: the timestep equals the oracle's bit for bit."""
+    scen = S.hallway(n=3000, width=60.0, height=40.0, seed=12)
+    n = len(scen.agents)
+    rng = np.random.default_rng(13)
+    th = rng.uniform(0, 2 * np.pi, n)
+    mag = {'ties': np.full(n, 5.0), 'spread': rng.uniform(0.0, 12.0, n),
+           'tiny': 10.0 ** rng.uniform(-170, -150, n), 'huge': 10.0 ** rng.uniform(150, 156, n)}[case]
+    scen.agents['velocity'] = np.stack((mag * np.cos(th), mag * np.sin(th)), 1)
+    dts = []
+    for variant in (7, 10):
+        b, agents, _ = batch_from_scenarios([scen])
+        b.set_variant(variant)
+        dts.append(b.step(N.NODE_INTEGRATE, want_dt=True)[0])
+        b.close()
+    want = oracle.adaptive_timestep(scen.agents.copy(), scen.dt_min, scen.dt_max)
+    assert dts[0] == want and dts[1] == want, (dts, want)
