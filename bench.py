@@ -670,20 +670,23 @@ def run_noise(b, agents, scen, steps):
 
 
 def run_batched(steps, warmup, flush=None):
-    """Batched form: the 512-scenario mix advanced as two contexts (one per
-    body type), both graphs launched, then one device synchronisation per
-    step; against the same scenarios as 512 single-scenario contexts (the
-    plain step run scenario by scenario): every scenario's step graph
-    launched back to back with one device synchronisation per step (the
+    """Batched form: the 512-scenario mix held in two contexts (one per body
+    type, each with its autotuned force-stage variant) and advanced by one
+    graph launch per step for both (cd_group_*), then one device
+    synchronisation; against the same scenarios as 512 single-scenario
+    contexts (the plain step run scenario by scenario): every scenario's step
+    graph launched back to back with one device synchronisation per step (the
     fair baseline), and each scenario's step awaited before the next
     (cd_synchronize per scenario, as a caller stepping one simulation after
-    another does).  The same number of steps in every leg, L2 flushed before
-    each.  Returns (the line's part, the detail)."""
+    another does).  The detail adds the two contexts launched separately and
+    the group with 10 steps per launch.  The same number of steps in every
+    leg, L2 flushed before each step (per launch for the 10-step group).
+    Returns (the line's part, the detail)."""
     import torch
     from crowddynamics_gb300 import _native as N
     from crowddynamics_gb300 import autotune
     from crowddynamics_gb300 import scenarios as S
-    from crowddynamics_gb300.engine import batch_from_scenarios
+    from crowddynamics_gb300.engine import DeviceGroup, batch_from_scenarios
     nodes = N.NODE_ALL & ~N.NODE_FLUCTUATION
     mix = S.batch_mix()
     groups = [[s for s in mix if s.body == b] for b in ('circular', 'three_circle')]
@@ -717,7 +720,27 @@ def run_batched(steps, warmup, flush=None):
                          {str(k): round(t, 4) for k, t in times.items()}}
         batches.append(b)
     n_total = sum(b.n_agents for b in batches)
-    batched = n_total * steps / timed(batches)
+
+    def timed_group(per_launch):
+        grp = DeviceGroup(batches, nodes, steps_per_launch=per_launch)
+        grp.launch(max(1, warmup // per_launch))
+        grp.synchronize()
+        el = 0.0
+        for k in range(steps // per_launch):
+            if flush is not None:
+                flush.fill_(k & 0xff)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            grp.launch(1)
+            torch.cuda.synchronize()
+            el += time.perf_counter() - t0
+        grp.synchronize()
+        grp.close()
+        return n_total * (steps // per_launch) * per_launch / el
+
+    batched = timed_group(1)
+    group10 = timed_group(10) if steps >= 10 else None
+    two_launches = n_total * steps / timed(batches)
     for b in batches:
         b.close()
     singles = [batch_from_scenarios([s])[0] for s in mix]
@@ -729,6 +752,7 @@ def run_batched(steps, warmup, flush=None):
             'speedup': batched / back_to_back, 'speedup_vs_synchronised': batched / synchronised,
             'steps': steps, 'scenarios': len(mix), 'agents': n_total}
     detail = dict(line, unit=UNIT, scenario_by_scenario_synchronised=synchronised,
+                  two_contexts_launched_separately=two_launches, group_10_steps_per_launch=group10,
                   walls=sum(len(s.walls) for s in mix), autotune=tuned,
                   timing='host wall clock per step from the first launch to the device '
                          'synchronisation, L2 flushed (256 MiB write) before each step')

@@ -44,6 +44,8 @@ SYMBOLS = (
     'cd_herding', 'cd_inside_domain', 'cd_target_reached', 'cd_exit_detection',
     'cd_launch',
     'cd_rollout_loss',
+    'cd_group_create', 'cd_group_launch', 'cd_group_synchronize', 'cd_group_last_error',
+    'cd_group_destroy',
 )
 
 #: Limits and column order of cd_agent_agent_noalloc.
@@ -129,6 +131,12 @@ def load(path=None):
         'cd_rollout_loss': (ctypes.c_int, [P, i64, P, i64, pd, pd, pd, pd]),
         'cd_agent_agent_noalloc': (ctypes.c_int, [ctypes.c_int, i64, P, P, P, P, ctypes.c_double,
                                                   ctypes.c_double, ctypes.c_double, i64, i64, P]),
+        'cd_group_create': (ctypes.c_int, [ctypes.POINTER(P), ctypes.POINTER(P), i64, ctypes.c_int,
+                                           i64]),
+        'cd_group_launch': (ctypes.c_int, [P, i64]),
+        'cd_group_synchronize': (ctypes.c_int, [P]),
+        'cd_group_last_error': (ctypes.c_char_p, [P]),
+        'cd_group_destroy': (None, [P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -142,7 +150,17 @@ def check(rc, ctx=None):
     """Map a CD_* status to the reference's exception hierarchy."""
     if rc == CD_OK:
         return
-    msg = load().cd_last_error(ctx).decode(errors='replace')
+    raise_status(rc, load().cd_last_error(ctx).decode(errors='replace'))
+
+
+def check_group(rc, group=None):
+    """check() for the cd_group_* calls (the group's own message)."""
+    if rc == CD_OK:
+        return
+    raise_status(rc, load().cd_group_last_error(group).decode(errors='replace'))
+
+
+def raise_status(rc, msg):
     if rc == CD_ERR_INVALID_TYPE:
         raise InvalidType(msg)
     if rc in (CD_ERR_INVALID_VALUE, CD_ERR_NOT_FINITE):

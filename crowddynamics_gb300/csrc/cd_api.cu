@@ -103,6 +103,7 @@ struct cd_ctx {
 
     cudaGraphExec_t graph = nullptr;
     int graph_nodes = -1;
+    uint64_t graph_gen = 0;        // bumped whenever a graph of this context goes stale
     int variant = 0;
 
     bool timing = false;
@@ -124,6 +125,15 @@ int fail(cd_ctx *c, int code, const std::string &m) {
     if (c) c->msg = m;
     else g_create_error = m;
     return code;
+}
+
+// Drop the step graph: buffers, variant or nodes changed (graphs built from
+// this context's steps, its own or a group's, are stale from now on).
+void drop_graph(cd_ctx *c) {
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+    c->graph_nodes = -1;
+    ++c->graph_gen;
 }
 
 #define CUDA_OR_FAIL(ctx, call)                                                       \
@@ -291,7 +301,7 @@ int bin_walls(cd_ctx *c) {
         c->wall_idx = nullptr;
         if (int rc = dalloc(c, &c->wall_idx, (int64_t)idx.size())) return rc;
         c->wall_idx_cap = (int64_t)idx.size();
-        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; c->graph_nodes = -1; }
+        drop_graph(c);
     }
     CUDA_OR_FAIL(c, cudaMemcpyAsync(c->wall_start, startv.data(), sizeof(int) * startv.size(),
                                     cudaMemcpyHostToDevice, c->stream));
@@ -376,7 +386,7 @@ int alloc_near_lists(cd_ctx *c, int64_t cap) {
         if (int rc = dalloc(c, &c->defer_list, cap)) return rc;
     }
     c->nl_cap = cap;
-    if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; c->graph_nodes = -1; }
+    drop_graph(c);
     return CD_OK;
 }
 
@@ -1122,7 +1132,7 @@ int cd_set_direction_maps(cd_ctx *c, int64_t scenario, int64_t n_targets, const 
     }
     CUDA_OR_FAIL(c, cudaMemcpy(c->scen, c->scen_dev.data(), sizeof(ScenDev) * c->nscen,
                                cudaMemcpyHostToDevice));
-    if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; c->graph_nodes = -1; }
+    drop_graph(c);
     return CD_OK;
 }
 
@@ -1130,7 +1140,7 @@ int cd_set_noise_mode(cd_ctx *c, int device, uint64_t seed, uint64_t step) {
     if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
     const bool dev = device != 0;
     if (dev != c->noise_dev || (dev && seed != c->noise_seed)) {
-        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; c->graph_nodes = -1; }
+        drop_graph(c);
     }
     c->noise_dev = dev;
     c->noise_seed = seed;
@@ -1190,7 +1200,7 @@ int ensure_graph(cd_ctx *c, int nodes) {
                     "graph steps cannot consume per-step host noise (use device noise)");
     if (int rc = prepare_step(c, nodes)) return rc;
     if (!c->graph || c->graph_nodes != nodes) {
-        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+        drop_graph(c);
         cudaGraph_t g;
         CUDA_OR_FAIL(c, cudaGetLastError());
         CUDA_OR_FAIL(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
@@ -1383,11 +1393,7 @@ int cd_set_variant(cd_ctx *c, int variant) {
     if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
     if (variant < 0 || variant >= cdk::N_VARIANTS)
         return fail(c, CD_ERR_INVALID_VALUE, "unknown variant");
-    if (variant != c->variant && c->graph) {
-        cudaGraphExecDestroy(c->graph);
-        c->graph = nullptr;
-        c->graph_nodes = -1;
-    }
+    if (variant != c->variant) drop_graph(c);
     c->variant = variant;
     return CD_OK;
 }
@@ -1575,6 +1581,171 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
     if (forward_ms) *forward_ms = f_ms;
     if (adjoint_ms) *adjoint_ms = a_ms;
     return check_device_error(c);
+}
+
+// ---- groups: several contexts' steps in one graph launch ------------------
+//
+// A group captures the steps of its contexts into one CUDA graph: each
+// context's stream joins the capture and enqueues its own `steps_per_launch`
+// steps (exactly the sequence cd_launch replays, so every result is the
+// same), then joins back.  Contexts advance independently inside the graph;
+// one cudaGraphLaunch advances them all.  The graph is rebuilt when a member
+// context's buffers, variant or walls changed (its graph generation moved).
+
+struct cd_group {
+    std::vector<cd_ctx *> ctx;
+    std::vector<uint64_t> gen;
+    std::vector<cudaEvent_t> ev_ctx;       // per member: its stream before a launch / capture join
+    cudaEvent_t ev_fork = nullptr, ev_done = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int nodes = 0;
+    int64_t k = 1;
+    int device = 0;
+    std::string msg;
+};
+
+namespace {
+
+int gfail(cd_group *g, int code, const std::string &m) {
+    if (g) g->msg = m;
+    else g_create_error = m;
+    return code;
+}
+
+#define GCUDA_OR_FAIL(g, call)                                                        \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess)                                                        \
+            return gfail((g), CD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// Host-side preparation of every member (wall bins, noise checks), then the
+// group graph if it is missing or stale.
+int group_prepare(cd_group *g) {
+    for (cd_ctx *c : g->ctx) {
+        if ((g->nodes & CD_NODE_FLUCTUATION) && !c->noise_dev)
+            return gfail(g, CD_ERR_INVALID_VALUE,
+                         "graph steps cannot consume per-step host noise (use device noise)");
+        if (int rc = prepare_step(c, g->nodes)) return gfail(g, rc, c->msg);
+    }
+    bool stale = g->exec == nullptr;
+    for (size_t i = 0; i < g->ctx.size(); ++i) stale |= g->gen[i] != g->ctx[i]->graph_gen;
+    if (!stale) return CD_OK;
+    if (g->exec) {                                  // launches of the old graph end first
+        GCUDA_OR_FAIL(g, cudaStreamSynchronize(g->stream));
+        cudaGraphExecDestroy(g->exec);
+        g->exec = nullptr;
+    }
+    GCUDA_OR_FAIL(g, cudaGetLastError());
+    GCUDA_OR_FAIL(g, cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaEventRecord(g->ev_fork, g->stream);
+    for (size_t i = 0; i < g->ctx.size() && e == cudaSuccess; ++i) {
+        cd_ctx *c = g->ctx[i];
+        e = cudaStreamWaitEvent(c->stream, g->ev_fork, 0);
+        for (int64_t k = 0; k < g->k && e == cudaSuccess; ++k) {
+            enqueue_step(c, g->nodes, false, false);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(g->ev_ctx[i], c->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(g->stream, g->ev_ctx[i], 0);
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(g->stream, &graph);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return gfail(g, CD_ERR_CUDA, std::string("group graph: ") + cudaGetErrorString(e));
+    }
+    for (size_t i = 0; i < g->ctx.size(); ++i) g->gen[i] = g->ctx[i]->graph_gen;
+    return CD_OK;
+}
+
+}  // namespace
+
+int cd_group_create(cd_group **out, cd_ctx *const *ctxs, int64_t n_ctxs, int nodes,
+                    int64_t steps_per_launch) {
+    if (!out) return gfail(nullptr, CD_ERR_INVALID_VALUE, "out is NULL");
+    *out = nullptr;
+    if (n_ctxs < 1 || !ctxs) return gfail(nullptr, CD_ERR_INVALID_VALUE, "need >= 1 context");
+    if (steps_per_launch < 1 || steps_per_launch > 1000)
+        return gfail(nullptr, CD_ERR_INVALID_VALUE, "steps_per_launch must be in [1, 1000]");
+    if (nodes & ~(CD_NODE_ALL | CD_NODE_NAVIGATION))
+        return gfail(nullptr, CD_ERR_INVALID_VALUE, "unknown node flags");
+    int dev = 0;
+    GCUDA_OR_FAIL(nullptr, cudaGetDevice(&dev));
+    for (int64_t i = 0; i < n_ctxs; ++i) {
+        if (!ctxs[i]) return gfail(nullptr, CD_ERR_INVALID_VALUE, "a context is NULL");
+        if (ctxs[i]->device != dev)
+            return gfail(nullptr, CD_ERR_INVALID_VALUE, "contexts on another device");
+        for (int64_t j = 0; j < i; ++j)
+            if (ctxs[j] == ctxs[i]) return gfail(nullptr, CD_ERR_INVALID_VALUE, "a context twice");
+    }
+    cd_group *g = new cd_group();
+    g->ctx.assign(ctxs, ctxs + n_ctxs);
+    g->gen.assign(n_ctxs, 0);
+    g->ev_ctx.assign(n_ctxs, nullptr);
+    g->nodes = nodes;
+    g->k = steps_per_launch;
+    g->device = dev;
+    bool ok = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&g->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&g->ev_done, cudaEventDisableTiming) == cudaSuccess;
+    for (auto &e : g->ev_ctx)
+        ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        cd_group_destroy(g);
+        return gfail(nullptr, CD_ERR_CUDA, "cudaStreamCreate / cudaEventCreate failed");
+    }
+    if (int rc = group_prepare(g)) {
+        const std::string m = g->msg;
+        cd_group_destroy(g);
+        return gfail(nullptr, rc, m);
+    }
+    *out = g;
+    return CD_OK;
+}
+
+void cd_group_destroy(cd_group *g) {
+    if (!g) return;
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    for (cudaEvent_t e : g->ev_ctx)
+        if (e) cudaEventDestroy(e);
+    if (g->ev_fork) cudaEventDestroy(g->ev_fork);
+    if (g->ev_done) cudaEventDestroy(g->ev_done);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+}
+
+const char *cd_group_last_error(const cd_group *g) {
+    return g ? g->msg.c_str() : g_create_error.c_str();
+}
+
+int cd_group_launch(cd_group *g, int64_t launches) {
+    if (!g) return gfail(nullptr, CD_ERR_INVALID_VALUE, "group is NULL");
+    if (launches < 0) return gfail(g, CD_ERR_INVALID_VALUE, "negative launch count");
+    if (int rc = group_prepare(g)) return rc;
+    // after each member's earlier work; each member's later work after the launch
+    for (size_t i = 0; i < g->ctx.size(); ++i) {
+        GCUDA_OR_FAIL(g, cudaEventRecord(g->ev_ctx[i], g->ctx[i]->stream));
+        GCUDA_OR_FAIL(g, cudaStreamWaitEvent(g->stream, g->ev_ctx[i], 0));
+    }
+    for (int64_t k = 0; k < launches; ++k) GCUDA_OR_FAIL(g, cudaGraphLaunch(g->exec, g->stream));
+    GCUDA_OR_FAIL(g, cudaEventRecord(g->ev_done, g->stream));
+    for (cd_ctx *c : g->ctx) GCUDA_OR_FAIL(g, cudaStreamWaitEvent(c->stream, g->ev_done, 0));
+    GCUDA_OR_FAIL(g, cudaGetLastError());
+    return CD_OK;
+}
+
+int cd_group_synchronize(cd_group *g) {
+    if (!g) return gfail(nullptr, CD_ERR_INVALID_VALUE, "group is NULL");
+    GCUDA_OR_FAIL(g, cudaStreamSynchronize(g->stream));
+    for (cd_ctx *c : g->ctx)
+        if (int rc = cd_synchronize(c)) return gfail(g, rc, c->msg);
+    return CD_OK;
 }
 
 // ---- agent-agent forces without device allocation -------------------------

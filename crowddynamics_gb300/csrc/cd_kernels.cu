@@ -246,9 +246,9 @@ __global__ void __launch_bounds__(PREP_NT) k_prepare(StepArgs a) {
         a.key[i] = key;
         atomicAdd(&a.count[key], 1);
     }
-    // per-scenario max |v| (NaN and 0 ignored, like `if l > v_max`): one
-    // atomic per block when its agents share a scenario (fmax is exact, so
-    // the order does not matter)
+    // per-scenario max |v| (NaN and 0 ignored, like `if l > v_max`): about
+    // one atomic per block when its agents share a scenario (fmax is exact,
+    // so the order does not matter)
     __shared__ int s_block;
     __shared__ double wmax[PREP_NT / 32];
     if (threadIdx.x == 0) s_block = s;
@@ -272,25 +272,13 @@ __global__ void __launch_bounds__(PREP_NT) k_prepare(StepArgs a) {
         qm = wmax[0];
 #pragma unroll
         for (int w = 1; w < PREP_NT / 32; ++w) qm = (wmax[w] > qm) ? wmax[w] : qm;
-        __syncthreads();                                // wmax is reused below
         const double thr = !(qm >= 0x1p-900) ? 0.0
                            : (qm <= 0x1.fffffffffffffp+1023 ? qm * (1.0 - 0x1p-40)
                                                             : 0x1.fffffffffffffp+1022);
-        if (s >= 0 && !(q < thr)) l = cdm_hypot(vx, vy);
-        double m = (l > 0) ? l : 0.0;
-        for (int o = 16; o > 0; o >>= 1) {
-            const double t = __shfl_xor_sync(0xffffffffu, m, o);
-            m = (t > m) ? t : m;
-        }
-        if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
-        __syncthreads();
-        if (threadIdx.x < 32) {
-            m = threadIdx.x < PREP_NT / 32 ? wmax[threadIdx.x] : 0.0;
-            for (int o = 16; o > 0; o >>= 1) {
-                const double t = __shfl_xor_sync(0xffffffffu, m, o);
-                m = (t > m) ? t : m;
-            }
-            if (threadIdx.x == 0 && s_block >= 0 && m > 0) atomicMax(&a.vmax[s_block], ord_bits(m));
+        // usually one lane per block: its hypot goes straight to the maximum
+        if (s >= 0 && !(q < thr)) {
+            l = cdm_hypot(vx, vy);
+            if (l > 0) atomicMax(&a.vmax[s], ord_bits(l));
         }
     } else if (s >= 0) {
         l = cdm_hypot(vx, vy);

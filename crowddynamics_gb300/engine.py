@@ -344,6 +344,42 @@ class DeviceBatch:
         return k.value
 
 
+class DeviceGroup:
+    """Several DeviceBatch contexts advanced by one CUDA-graph launch
+    (``cd_group_*``): ``steps_per_launch`` steps of ``nodes`` of every
+    member per launch, each member exactly as its own ``launch`` would run
+    it.  The members must stay open while the group is used."""
+
+    def __init__(self, batches, nodes=N.NODE_ALL & ~N.NODE_FLUCTUATION, steps_per_launch=1):
+        self._lib = N.load()
+        self.batches = list(batches)
+        arr = (ctypes.c_void_p * len(self.batches))(*[b._ctx for b in self.batches])
+        g = ctypes.c_void_p()
+        N.check_group(self._lib.cd_group_create(ctypes.byref(g), arr, len(self.batches),
+                                                int(nodes), int(steps_per_launch)))
+        self._g = g
+        self.steps_per_launch = int(steps_per_launch)
+
+    def launch(self, launches=1):
+        """Enqueue ``launches`` graph launches; returns without waiting."""
+        N.check_group(self._lib.cd_group_launch(self._g, int(launches)), self._g)
+
+    def synchronize(self):
+        """Wait for the launches; raise on any member's device status."""
+        N.check_group(self._lib.cd_group_synchronize(self._g), self._g)
+
+    def close(self):
+        if getattr(self, '_g', None):
+            self._lib.cd_group_destroy(self._g)
+            self._g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def batch_from_scenarios(scenarios):
     """DeviceBatch holding every scenario of ``scenarios`` (same body type),
     with the concatenated agent array and walls uploaded.  Returns

@@ -321,6 +321,28 @@ int cd_rollout_loss(cd_ctx *ctx, int64_t steps, const double *target,
                     int64_t checkpoint_every, double *loss, double *grads,
                     double *forward_ms, double *adjoint_ms);
 
+/* ---- groups: the steps of several contexts in one graph launch ---------
+ * The batched form (several contexts, e.g. one per body type, each holding
+ * many scenarios) advanced by one CUDA-graph launch: the group captures
+ * `steps_per_launch` steps of `nodes` of every member into one graph, each
+ * member's steps exactly as cd_launch runs them (results are the same as
+ * the members stepped one by one), the members advancing independently
+ * inside it.  Replaces the reference's loop of MultiAgentSimulation.update()
+ * over independent simulations (simulation/multiagent.py:51-55, one call
+ * per scenario and step).  The members must outlive the group; a launch is
+ * ordered after work already enqueued on each member and before work
+ * enqueued on them afterwards.  A member whose buffers, variant or walls
+ * change is recaptured at the next launch.  cd_group_synchronize waits for
+ * the launches and checks every member's status.  Errors: the group's
+ * message (cd_group_last_error; the creation's with a NULL group). */
+typedef struct cd_group cd_group;
+int cd_group_create(cd_group **out, cd_ctx *const *ctxs, int64_t n_ctxs, int nodes,
+                    int64_t steps_per_launch);
+int cd_group_launch(cd_group *group, int64_t launches);
+int cd_group_synchronize(cd_group *group);
+const char *cd_group_last_error(const cd_group *group);
+void cd_group_destroy(cd_group *group);
+
 /* ---- agent-agent forces without any device allocation ------------------
  * No counterpart in the reference: an extra entry point for callers that
  * cannot allocate device memory while they run -- for example a host

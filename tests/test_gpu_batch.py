@@ -80,3 +80,36 @@ def test_autotune_picks_and_caches(native, mix, tmp_path, monkeypatch):
     data = json.load(open(tmp_path / 'tune.json'))
     assert len(data) == 1
     b.close()
+
+
+@pytest.mark.parametrize('per_launch', [1, 4])
+def test_group_launch_equals_contexts_alone(native, mix, per_launch):
+    """Both body types' contexts advanced by one graph launch (cd_group_*),
+    `per_launch` steps per launch: bit-identical to each context run alone,
+    also after a member changes its variant (the group recaptures)."""
+    from crowddynamics_gb300.engine import DeviceGroup
+    bodies = ('circular', 'three_circle')
+    groups = [[s for s in mix if s.body == body] for body in bodies]
+    alone = []
+    for g in groups:
+        b, agents, _ = batch_from_scenarios(g)
+        b.run(8, NODES)
+        o = agents.copy()
+        b.download(o)
+        alone.append((o, b.time()))
+        b.close()
+    members = [batch_from_scenarios(g) for g in groups]
+    grp = DeviceGroup([m[0] for m in members], NODES, steps_per_launch=per_launch)
+    grp.launch(4 // per_launch)
+    members[1][0].set_variant(7)                   # recaptured at the next launch
+    grp.launch(4 // per_launch)
+    grp.synchronize()
+    for (b, agents, _), (ref, (dt, tt)) in zip(members, alone):
+        got = agents.copy()
+        b.download(got)
+        assert_identical(got, ref, 'group member')
+        dt_g, tt_g = b.time()
+        assert np.array_equal(dt_g, dt) and np.array_equal(tt_g, tt)
+    grp.close()
+    for b, _, _ in members:
+        b.close()
