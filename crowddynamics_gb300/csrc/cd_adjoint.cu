@@ -473,39 +473,76 @@ __global__ void k_copy_cols(ColCopy cc, int n) {
         cc.dst[k][i] = cc.src[k][i];
 }
 
-// max |v| and max v0 with their first indices (single block, index order).
+// (value, index) of a maximum: the larger value, on ties the smaller index
+// (-1 = none); NaN never wins.
+__device__ __forceinline__ void better(double &v, int &j, double v2, int j2) {
+    if (j2 >= 0 && (v2 > v || (v2 == v && (j < 0 || j2 < j)))) { v = v2; j = j2; }
+}
+
+// Per block: max |v| (positive values only) and max v0 with their first
+// indices, written to vals / idx [2 * block + {0, 1}]; k_adj_dt combines the
+// blocks.  |v| = hypot(vx, vy) only where q = vx^2 + vy^2 can hold the
+// block's maximum: q is within 4 ulp of |v|^2, so a lane 2^-40 below the
+// block's largest q has a |v| smaller by far more than hypot's 2 ulp
+// (non-finite q, and blocks whose largest q is tiny, take hypot everywhere).
 __global__ void k_adj_argmax(const double *vx, const double *vy, const double *v0, int n,
-                             double *out_vals, int *out_idx) {
-    __shared__ double bv[RED_NT], b0[RED_NT];
-    __shared__ int iv[RED_NT], i0[RED_NT];
+                             double *vals, int *idx) {
+    __shared__ double sq[RED_NT / 32], sv[RED_NT / 32], s0[RED_NT / 32];
+    __shared__ int jv_s[RED_NT / 32], j0_s[RED_NT / 32];
+    const int i = blockIdx.x * RED_NT + threadIdx.x, w = threadIdx.x >> 5;
+    const bool in = i < n;
+    const double x = in ? vx[i] : 0.0, y = in ? vy[i] : 0.0;
+    const double q = x * x + y * y;
+    double qm = (in && q > 0) ? q : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+        const double t = __shfl_xor_sync(0xffffffffu, qm, o);
+        qm = (t > qm) ? t : qm;
+    }
+    if ((threadIdx.x & 31) == 0) sq[w] = qm;
+    __syncthreads();
+    qm = sq[0];
+#pragma unroll
+    for (int k = 1; k < RED_NT / 32; ++k) qm = (sq[k] > qm) ? sq[k] : qm;
+    const double thr = !(qm >= 0x1p-900) ? 0.0
+                       : (qm <= 0x1.fffffffffffffp+1023 ? qm * (1.0 - 0x1p-40)
+                                                        : 0x1.fffffffffffffp+1022);
     double mv = 0.0, m0 = -INFINITY;
     int jv = -1, j0 = -1;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double l = cdm_hypot(vx[i], vy[i]);
+    if (in && !(q < thr)) {
+        const double l = cdm_hypot(x, y);
         if (l > mv) { mv = l; jv = i; }
-        if (v0[i] > m0) { m0 = v0[i]; j0 = i; }
     }
-    bv[threadIdx.x] = mv; iv[threadIdx.x] = jv; b0[threadIdx.x] = m0; i0[threadIdx.x] = j0;
+    if (in && v0[i] > m0) { m0 = v0[i]; j0 = i; }
+    for (int o = 16; o > 0; o >>= 1) {
+        better(mv, jv, __shfl_xor_sync(0xffffffffu, mv, o), __shfl_xor_sync(0xffffffffu, jv, o));
+        better(m0, j0, __shfl_xor_sync(0xffffffffu, m0, o), __shfl_xor_sync(0xffffffffu, j0, o));
+    }
+    if ((threadIdx.x & 31) == 0) { sv[w] = mv; jv_s[w] = jv; s0[w] = m0; j0_s[w] = j0; }
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int t = 1; t < (int)blockDim.x; ++t) {
-            if (bv[t] > mv || (bv[t] == mv && iv[t] >= 0 && iv[t] < jv)) { mv = bv[t]; jv = iv[t]; }
-            if (b0[t] > m0 || (b0[t] == m0 && i0[t] >= 0 && i0[t] < j0)) { m0 = b0[t]; j0 = i0[t]; }
+        for (int k = 1; k < RED_NT / 32; ++k) {
+            better(mv, jv, sv[k], jv_s[k]);
+            better(m0, j0, s0[k], j0_s[k]);
         }
-        out_vals[0] = mv; out_vals[1] = m0;
-        out_idx[0] = jv; out_idx[1] = j0;
+        vals[2 * blockIdx.x] = mv; vals[2 * blockIdx.x + 1] = m0;
+        idx[2 * blockIdx.x] = jv; idx[2 * blockIdx.x + 1] = j0;
     }
 }
 
 // The timestep's own gradient, when dt was not clamped:
 // dt = 1.1 V0 dt_max / Vm  ->  d/dV0 = dt / V0,  d/dVm = -dt / Vm.
 __global__ void k_adj_dt(AdjArgs q, double dt_min, double dt_max, const double *vx,
-                         const double *vy) {
+                         const double *vy, int blocks) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     const double dt = *q.dt, ldt = *q.ldt;
-    const double Vm = q.argmax_vals[0], V0 = q.argmax_vals[1];
+    // the blocks of k_adj_argmax in order: the maxima with their first indices
+    double Vm = 0.0, V0 = -INFINITY;
+    int jv = -1, j0 = -1;
+    for (int b = 0; b < blocks; ++b) {
+        better(Vm, jv, q.argmax_vals[2 * b], q.argmax_idx[2 * b]);
+        better(V0, j0, q.argmax_vals[2 * b + 1], q.argmax_idx[2 * b + 1]);
+    }
     if (!(Vm > 0) || !(dt > dt_min && dt < dt_max)) return;
-    const int jv = q.argmax_idx[0], j0 = q.argmax_idx[1];
     if (j0 >= 0) q.grad[4 * j0 + 1] += ldt * dt / V0;
     if (jv >= 0) {
         double c = ldt * (-dt / Vm) / Vm;
@@ -553,8 +590,9 @@ void launch_copy_cols(const double *const *src, double *const *dst, int ncol, in
 }
 void launch_adj_dt(const AdjArgs &q, double dt_min, double dt_max, const double *vx,
                    const double *vy, const double *v0, cudaStream_t s) {
-    k_adj_argmax<<<1, RED_NT, 0, s>>>(vx, vy, v0, q.n, q.argmax_vals, q.argmax_idx);
-    k_adj_dt<<<1, 1, 0, s>>>(q, dt_min, dt_max, vx, vy);
+    const int nb = adj_partials(q.n);
+    k_adj_argmax<<<nb, RED_NT, 0, s>>>(vx, vy, v0, q.n, q.argmax_vals, q.argmax_idx);
+    k_adj_dt<<<1, 1, 0, s>>>(q, dt_min, dt_max, vx, vy, nb);
 }
 void launch_loss(const double *x, const double *y, const double *target, int n, double *partial,
                  double *loss, double scale, cudaStream_t s) {

@@ -30,6 +30,7 @@ struct cd_ctx {
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;              // beside the near-list build
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join_stage = nullptr;
+    cudaEvent_t ev_fork_pro = nullptr;   // the prologue's fork, right after k_prepare
     cudaEvent_t ev_read = nullptr;               // an upload has read the host records
     cudaEvent_t ev_ext = nullptr;                // an upload's extents are in ext_host
     bool ext_pending = false;                    // ext_host not yet folded into extent_max
@@ -242,6 +243,7 @@ void release(cd_ctx *c) {
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_fork_pro) cudaEventDestroy(c->ev_fork_pro);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->ev_join_stage) cudaEventDestroy(c->ev_join_stage);
     if (c->ev_read) cudaEventDestroy(c->ev_read);
@@ -318,18 +320,28 @@ int bin_walls(cd_ctx *c) {
 // Cell list + staging for the current state (no forces).
 // `defer_stage`: only the pre-check records here; the force stage writes the
 // float64 staged records beside the near-list build.
-void enqueue_cells(cd_ctx *c, const StepArgs &a, bool defer_stage = false) {
+// `prologue`: fork the per-agent prologue (k_prologue) to the second stream
+// right after k_prepare (it reads the step's noise counter, which k_prepare
+// advances, and no output of the cell list), so that it runs beside the
+// latency-bound cell-list kernels.
+void enqueue_cells(cd_ctx *c, const StepArgs &a, bool defer_stage = false,
+                   bool prologue = false) {
     // count, fill and vmax are zero between cell lists (zeroed at creation,
     // then by k_rank and k_scatter once used)
     cdk::launch_prepare(a, c->stream);
+    if (prologue) {
+        cudaEventRecord(c->ev_fork_pro, c->stream);
+        cudaStreamWaitEvent(c->stream2, c->ev_fork_pro, 0);
+        cdk::launch_prologue(a, c->stream2);
+    }
     // dt is computed by the scatter kernel, launched only for agents
     const bool dt_kernel = (a.nodes & cdk::N_INTEG) && a.n == 0;
     if (dt_kernel) cdk::launch_dt(a, c->stream);
-    // each kernel of the cell list chained to the one before it
+    // each kernel of the cell list chained to the one before it (after the
+    // fork's event record, an ordinary launch)
     cdk::launch_scan(c->count, c->start, (int)c->ncells, c->scan_scratch, c->stream,
-                     a.n > 0 || dt_kernel);
-    cdk::launch_scatter(a, c->stream, true);
-    cdk::launch_gather(a, c->stream, defer_stage ? 1 : 0, true);
+                     (a.n > 0 || dt_kernel) && !prologue);
+    cdk::launch_scatter(a, c->stream, true, defer_stage ? 1 : 0);     // rank + gather
 }
 
 // One step on the context stream.  `timed`: record the step and force-kernel
@@ -340,13 +352,15 @@ void enqueue_step(cd_ctx *c, int nodes, bool timed, bool captured = false) {
     StepArgs a = args_of(c, nodes);
     // the pair pipeline writes the float64 staged records beside the near lists
     const bool defer = cdk::variant_pairs(c->variant) && c->nl_cnt;
+    // ... and runs k_prologue on the second stream from the start of the step
+    const bool early = defer && a.pro;
     if (timed) cudaEventRecord(c->evs0, c->stream);
-    enqueue_cells(c, a, defer);
+    enqueue_cells(c, a, defer, early);
     if (timed) cudaEventRecord(c->ev0, c->stream);
     if (captured) cudaEventRecordWithFlags(c->ev0, c->stream, cudaEventRecordExternal);
     const cdk::Fork fork{c->stream2, c->ev_fork, c->ev_join, c->ev_join_stage};
     cdk::launch_forces(a, c->stream, c->variant, (timed || captured) ? c->evp : nullptr, captured,
-                       &fork, defer);
+                       &fork, defer, early);
     if (timed) cudaEventRecord(c->ev1, c->stream);
     if (captured) cudaEventRecordWithFlags(c->ev1, c->stream, cudaEventRecordExternal);
     if (timed) cudaEventRecord(c->evs1, c->stream);
@@ -354,7 +368,7 @@ void enqueue_step(cd_ctx *c, int nodes, bool timed, bool captured = false) {
 
 int64_t kernels_per_step(const cd_ctx *c, int nodes) {
     if (c->n == 0) return (nodes & CD_NODE_INTEGRATE) ? 1 : 0;
-    int64_t k = 5;                                      // prepare scatter(+dt) rank gather forces
+    int64_t k = 4;                                      // prepare scatter(+dt) rank(+gather) forces
     k += cdk::scan_launches_single((int)c->ncells);
     if (cdk::variant_pairs(c->variant) && c->nl_cnt) k += 2;     // prologue, float64 staging
     if (cdk::variant_pairs(c->variant) && (nodes & CD_NODE_AGENT_AGENT) && c->nl_cnt)
@@ -633,6 +647,7 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_fork_pro, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join_stage, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_read, cudaEventDisableTiming) != cudaSuccess ||
@@ -1484,8 +1499,9 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
     double *partial = mem.get<double>(c, cdk::adj_partials((int)n), rc);
     double *scal = mem.get<double>(c, 4, rc);           // loss, ldt, saved dt, saved time
     double *adj = grads ? mem.get<double>(c, 16 * n + 4 * n, rc) : nullptr;
-    int *amax = grads ? mem.get<int>(c, 2, rc) : nullptr;
-    double *avals = grads ? mem.get<double>(c, 2, rc) : nullptr;
+    // per block of the argmax: (max |v|, max v0) and their first indices
+    int *amax = grads ? mem.get<int>(c, 2 * cdk::adj_partials((int)n), rc) : nullptr;
+    double *avals = grads ? mem.get<double>(c, 2 * cdk::adj_partials((int)n), rc) : nullptr;
     if (rc) return rc;
     cudaStream_t st = c->stream;
     CUDA_OR_FAIL(c, cudaMemcpyAsync(tgt, target, sizeof(double) * steps * 2 * n,
@@ -1893,8 +1909,7 @@ extern "C" int cd_agent_agent_noalloc(int body_type, int64_t n, const double *co
                                                        (int)nx, (int)ny);
     cdk::launch_prepare(a, st);
     cdk::launch_scan(a.count, a.start, ncells, scan, st);
-    cdk::launch_scatter(a, st);
-    cdk::launch_gather(a, st);
+    cdk::launch_scatter(a, st, false, 0);               // rank + gather
     cdk::launch_forces(a, st, cdk::default_group_variant(n));
     CUDA_OR_FAIL(nullptr, cudaGetLastError());
     int h = 0;

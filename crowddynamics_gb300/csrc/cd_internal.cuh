@@ -176,8 +176,8 @@ struct AdjArgs {
     double *lx_out, *lv_out;               // outgoing adjoints of x, v
     double *partial, *ldt;                 // dt adjoint (block partials, total)
     double *grad;                          // n x 4: tau_adj, v0, tau_0, k_soc
-    double *argmax_vals;                   // max |v|, max v0
-    int *argmax_idx;
+    double *argmax_vals;                   // per argmax block: max |v|, max v0
+    int *argmax_idx;                       // their first indices
 };
 
 int adj_partials(int n);
@@ -204,7 +204,10 @@ int near_scan_ints(int n);
 void launch_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s,
                  bool after_kernel = false);
 int scan_launches_single(int n);          // kernels launch_scan uses for n elements
-void launch_scatter(const StepArgs &a, cudaStream_t s, bool after_kernel = false);
+// Agents into cells in stable order; with gather_part >= 0 the ranking kernel
+// also writes the staged records of that part (as launch_gather).
+void launch_scatter(const StepArgs &a, cudaStream_t s, bool after_kernel = false,
+                    int gather_part = -1);
 // Staged records of the cell-sorted agents: part 0 all, 1 the float32
 // pre-check records, 2 the float64 records.
 void launch_gather(const StepArgs &a, cudaStream_t s, int part = 0, bool after_kernel = false);
@@ -220,9 +223,14 @@ int variant_staged(int variant);
 struct Fork { cudaStream_t s2; cudaEvent_t fork, join, join_stage; };
 // The agent-force stage; with `pair_ev`, events recorded around the pair
 // kernel of the pair pipeline (as external event-record nodes if `captured`).
+// `prologue_launched`: k_prologue already runs on fork->s2 (launch_prologue).
 void launch_forces(const StepArgs &a, cudaStream_t s, int variant,
                    const cudaEvent_t *pair_ev = nullptr, bool captured = false,
-                   const Fork *fork = nullptr, bool stage_deferred = false);
+                   const Fork *fork = nullptr, bool stage_deferred = false,
+                   bool prologue_launched = false);
+// The per-agent terms before agent-agent (navigation, fluctuation,
+// orientation, adjusting) and the old accelerations, into StepArgs::pro.
+void launch_prologue(const StepArgs &a, cudaStream_t s);
 // Near-list counts and their scan (nl_off) for the state staged in `a`.
 void launch_near_count(const StepArgs &a, cudaStream_t s, int variant);
 // Near lists (counts, scans, fill; 8 lanes per agent) for the state staged in `a`.

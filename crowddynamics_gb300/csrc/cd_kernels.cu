@@ -245,44 +245,33 @@ __global__ void __launch_bounds__(PREP_NT) k_prepare(StepArgs a) {
         }
         a.key[i] = key;
         atomicAdd(&a.count[key], 1);
+        l = cdm_hypot(a.col[VX][i], a.col[VY][i]);      // length(velocity)
     }
-    // per-scenario max |v| (NaN and 0 ignored, like `if l > v_max`): about
-    // one atomic per block when its agents share a scenario (fmax is exact,
-    // so the order does not matter)
+    // per-scenario max |v| (NaN and 0 ignored, like `if l > v_max`): one
+    // atomic per block when its agents share a scenario (fmax is exact, so
+    // the order does not matter)
     __shared__ int s_block;
     __shared__ double wmax[PREP_NT / 32];
     if (threadIdx.x == 0) s_block = s;
     __syncthreads();
-    const double vx = i < a.n ? a.col[VX][i] : 0.0, vy = i < a.n ? a.col[VY][i] : 0.0;
     if (__syncthreads_and(s == s_block || s < 0)) {
-        // length(velocity) = hypot(vx, vy) only where it can be the block's
-        // maximum: q = vx^2 + vy^2 is within 4 ulp of |v|^2, so a lane whose q
-        // lies 2^-40 below the block's largest q has a |v| smaller by far
-        // more than hypot's 2 ulp and cannot hold the maximum.  Non-finite q,
-        // and blocks whose largest q is tiny (squares near underflow), take
-        // hypot everywhere.
-        const double q = vx * vx + vy * vy;
-        double qm = (q > 0) ? q : 0.0;
+        double m = (l > 0) ? l : 0.0;
         for (int o = 16; o > 0; o >>= 1) {
-            const double t = __shfl_xor_sync(0xffffffffu, qm, o);
-            qm = (t > qm) ? t : qm;
+            const double t = __shfl_xor_sync(0xffffffffu, m, o);
+            m = (t > m) ? t : m;
         }
-        if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = qm;
+        if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
         __syncthreads();
-        qm = wmax[0];
-#pragma unroll
-        for (int w = 1; w < PREP_NT / 32; ++w) qm = (wmax[w] > qm) ? wmax[w] : qm;
-        const double thr = !(qm >= 0x1p-900) ? 0.0
-                           : (qm <= 0x1.fffffffffffffp+1023 ? qm * (1.0 - 0x1p-40)
-                                                            : 0x1.fffffffffffffp+1022);
-        // usually one lane per block: its hypot goes straight to the maximum
-        if (s >= 0 && !(q < thr)) {
-            l = cdm_hypot(vx, vy);
-            if (l > 0) atomicMax(&a.vmax[s], ord_bits(l));
+        if (threadIdx.x < 32) {
+            m = threadIdx.x < PREP_NT / 32 ? wmax[threadIdx.x] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) {
+                const double t = __shfl_xor_sync(0xffffffffu, m, o);
+                m = (t > m) ? t : m;
+            }
+            if (threadIdx.x == 0 && s_block >= 0 && m > 0) atomicMax(&a.vmax[s_block], ord_bits(m));
         }
-    } else if (s >= 0) {
-        l = cdm_hypot(vx, vy);
-        if (l > 0) atomicMax(&a.vmax[s], ord_bits(l));
+    } else if (s >= 0 && l > 0) {
+        atomicMax(&a.vmax[s], ord_bits(l));
     }
 }
 
@@ -583,26 +572,6 @@ __global__ void k_scatter(StepArgs a) {
     a.perm_unsorted[p] = i;
 }
 
-// Stable order inside a cell: rank = number of agents of the cell with a
-// smaller index.
-__global__ void k_rank(StepArgs a) {
-    pdl_enter();
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= a.n) return;
-    int i = a.perm_unsorted[p];
-    int c = a.key[i];
-    int b = a.start[c], e = a.start[c + 1];
-    int r = 0;
-    for (int q = b; q < e; ++q) r += (a.perm_unsorted[q] < i);
-    a.perm[b + r] = i;
-    if (a.slot_of) a.slot_of[i] = b + r;
-    // the cell's count and fill are used up: zero for the next cell list
-    if (p == b) {
-        a.count[c] = 0;
-        a.fill[c] = 0;
-    }
-}
-
 // Extent: distance from the torso centre to the farthest skin point.
 __device__ __forceinline__ double extent_tc(double x, double y, double xl, double yl,
                                             double xr, double yr, double rt, double rs) {
@@ -630,17 +599,11 @@ __device__ __forceinline__ float up_f(double v) {
     return f + fabsf(f) * 1e-6f + 1e-6f;
 }
 
-// One lane per agent where the slots are known (column reads coalesced, the
-// staged records written whole), else one lane per slot.  `part`: 0 all
+// The staged records of agent i in its cell-sorted slot s.  `part`: 0 all
 // records; 1 the float32 pre-check records only (all the near-list build
 // reads); 2 the float64 staged records only.
-__global__ void k_gather(StepArgs a, int part) {
-    pdl_enter();
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= a.n) return;
-    int s, i;
-    if (a.slot_of) { i = t; s = a.slot_of[t]; }
-    else { s = t; i = a.perm[t]; }
+__device__ __forceinline__ void gather_agent(const StepArgs &a, const int i, const int s,
+                                             const int part) {
     double *const *c = a.col;
     // pre-check records: positions relative to the scenario's grid origin
     // (cd_cull.cuh); the staged float64 records keep the reference's values
@@ -701,6 +664,41 @@ __global__ void k_gather(StepArgs a, int part) {
         a.cull[s] = make_float4(xh, yh, (ef + ef * 1e-5f + 1e-5f) + cull_slack(xh, yh),
                                 pack_velocity(c[VX][i], c[VY][i]));
     }
+}
+
+// One lane per agent where the slots are known (column reads coalesced, the
+// staged records written whole), else one lane per slot.
+__global__ void k_gather(StepArgs a, int part) {
+    pdl_enter();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.n) return;
+    int s, i;
+    if (a.slot_of) { i = t; s = a.slot_of[t]; }
+    else { s = t; i = a.perm[t]; }
+    gather_agent(a, i, s, part);
+}
+
+// Stable order inside a cell: the rank of agent i is the number of agents of
+// its cell with a smaller index.  One lane per agent (its columns read
+// coalesced); with part >= 0 it also writes the agent's staged records
+// (gather_agent) at its slot, so no separate gather runs.
+__global__ void k_rank(StepArgs a, int part) {
+    pdl_enter();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const int c = a.key[i];
+    const int b = a.start[c], e = a.start[c + 1];
+    int r = 0;
+    for (int q = b; q < e; ++q) r += (a.perm_unsorted[q] < i);
+    const int s = b + r;
+    a.perm[s] = i;
+    if (a.slot_of) a.slot_of[i] = s;
+    // the cell's count and fill are used up: zero for the next cell list
+    if (r == 0) {
+        a.count[c] = 0;
+        a.fill[c] = 0;
+    }
+    if (part >= 0) gather_agent(a, i, s, part);
 }
 
 // Candidate enumeration over the 3 x 3 cell neighbourhood of slot s.  The
@@ -3065,10 +3063,10 @@ void launch_near_scans(const StepArgs &a, cudaStream_t s) {
                     {a.nl_scan, a.fw_scan, a.fs_scan}};
     launch_k(true, k_scan_tiles, dim3(nb, 3), SCAN_NT, 0, s, S, a.n, nb);   // after the count
 }
-void launch_scatter(const StepArgs &a, cudaStream_t s, bool after_kernel) {
+void launch_scatter(const StepArgs &a, cudaStream_t s, bool after_kernel, int gather_part) {
     if (a.n <= 0) return;
     launch_k(after_kernel, k_scatter, nblk(a.n, 256), 256, 0, s, a);
-    launch_k(true, k_rank, nblk(a.n, 256), 256, 0, s, a);
+    launch_k(true, k_rank, nblk(a.n, 128), 128, 0, s, a, gather_part);
 }
 void launch_gather(const StepArgs &a, cudaStream_t s, int part, bool after_kernel) {
     if (a.n > 0) launch_k(after_kernel, k_gather, nblk(a.n, 128), 128, 0, s, a, part);
@@ -3192,8 +3190,14 @@ int init_kernels() {
     return e == cudaSuccess ? 0 : (int)e;
 }
 
+void launch_prologue(const StepArgs &a, cudaStream_t s) {
+    if (a.n <= 0) return;
+    if (a.body) k_prologue<1><<<nblk(a.n, 128), 128, 0, s>>>(a);
+    else k_prologue<0><<<nblk(a.n, 128), 128, 0, s>>>(a);
+}
+
 void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEvent_t *pair_ev,
-                   bool captured, const Fork *fork, bool stage_deferred) {
+                   bool captured, const Fork *fork, bool stage_deferred, bool prologue_launched) {
     if (a.n <= 0) return;
     if (variant < 0 || variant >= N_VARIANTS) variant = 0;
     // the pair pipeline needs the near-list buffers: otherwise its lane-group twin
@@ -3217,8 +3221,7 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
             launch_gather(a, sp, 2);
             if (fork) cudaEventRecord(fork->join_stage, fork->s2);
         }
-        if (body) k_prologue<1><<<nblk(a.n, 128), 128, 0, sp>>>(a);
-        else k_prologue<0><<<nblk(a.n, 128), 128, 0, sp>>>(a);
+        if (!prologue_launched) launch_prologue(a, sp);
         if (fork) cudaEventRecord(fork->join, fork->s2);
     } else if (stage_deferred) {
         launch_gather(a, s, 2);
