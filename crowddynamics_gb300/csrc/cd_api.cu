@@ -30,7 +30,6 @@ struct cd_ctx {
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;              // beside the near-list build
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join_stage = nullptr;
-    cudaEvent_t ev_fork_pro = nullptr;   // the prologue's fork, right after k_prepare
     cudaEvent_t ev_read = nullptr;               // an upload has read the host records
     cudaEvent_t ev_ext = nullptr;                // an upload's extents are in ext_host
     bool ext_pending = false;                    // ext_host not yet folded into extent_max
@@ -243,7 +242,6 @@ void release(cd_ctx *c) {
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
-    if (c->ev_fork_pro) cudaEventDestroy(c->ev_fork_pro);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->ev_join_stage) cudaEventDestroy(c->ev_join_stage);
     if (c->ev_read) cudaEventDestroy(c->ev_read);
@@ -320,27 +318,16 @@ int bin_walls(cd_ctx *c) {
 // Cell list + staging for the current state (no forces).
 // `defer_stage`: only the pre-check records here; the force stage writes the
 // float64 staged records beside the near-list build.
-// `prologue`: fork the per-agent prologue (k_prologue) to the second stream
-// right after k_prepare (it reads the step's noise counter, which k_prepare
-// advances, and no output of the cell list), so that it runs beside the
-// latency-bound cell-list kernels.
-void enqueue_cells(cd_ctx *c, const StepArgs &a, bool defer_stage = false,
-                   bool prologue = false) {
+void enqueue_cells(cd_ctx *c, const StepArgs &a, bool defer_stage = false) {
     // count, fill and vmax are zero between cell lists (zeroed at creation,
     // then by k_rank and k_scatter once used)
     cdk::launch_prepare(a, c->stream);
-    if (prologue) {
-        cudaEventRecord(c->ev_fork_pro, c->stream);
-        cudaStreamWaitEvent(c->stream2, c->ev_fork_pro, 0);
-        cdk::launch_prologue(a, c->stream2);
-    }
     // dt is computed by the scatter kernel, launched only for agents
     const bool dt_kernel = (a.nodes & cdk::N_INTEG) && a.n == 0;
     if (dt_kernel) cdk::launch_dt(a, c->stream);
-    // each kernel of the cell list chained to the one before it (after the
-    // fork's event record, an ordinary launch)
+    // each kernel of the cell list chained to the one before it
     cdk::launch_scan(c->count, c->start, (int)c->ncells, c->scan_scratch, c->stream,
-                     (a.n > 0 || dt_kernel) && !prologue);
+                     a.n > 0 || dt_kernel);
     cdk::launch_scatter(a, c->stream, true, defer_stage ? 1 : 0);     // rank + gather
 }
 
@@ -352,15 +339,13 @@ void enqueue_step(cd_ctx *c, int nodes, bool timed, bool captured = false) {
     StepArgs a = args_of(c, nodes);
     // the pair pipeline writes the float64 staged records beside the near lists
     const bool defer = cdk::variant_pairs(c->variant) && c->nl_cnt;
-    // ... and runs k_prologue on the second stream from the start of the step
-    const bool early = defer && a.pro;
     if (timed) cudaEventRecord(c->evs0, c->stream);
-    enqueue_cells(c, a, defer, early);
+    enqueue_cells(c, a, defer);
     if (timed) cudaEventRecord(c->ev0, c->stream);
     if (captured) cudaEventRecordWithFlags(c->ev0, c->stream, cudaEventRecordExternal);
     const cdk::Fork fork{c->stream2, c->ev_fork, c->ev_join, c->ev_join_stage};
     cdk::launch_forces(a, c->stream, c->variant, (timed || captured) ? c->evp : nullptr, captured,
-                       &fork, defer, early);
+                       &fork, defer);
     if (timed) cudaEventRecord(c->ev1, c->stream);
     if (captured) cudaEventRecordWithFlags(c->ev1, c->stream, cudaEventRecordExternal);
     if (timed) cudaEventRecord(c->evs1, c->stream);
@@ -644,10 +629,15 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     if (int e = cdk::init_kernels())
         rc = fail(c, CD_ERR_CUDA, std::string("kernel attributes: ") +
                                      cudaGetErrorString((cudaError_t)e));
-    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+    // the step's critical path runs on the context stream; the second stream
+    // (the prologue, the float64 staging) fills the SMs the critical path
+    // leaves idle: it gets the lowest priority, the context stream the highest,
+    // so that waiting blocks of the critical path are scheduled first
+    int prio_low = 0, prio_high = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+    if (cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_high) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&c->stream2, cudaStreamNonBlocking, prio_low) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_fork_pro, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join_stage, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_read, cudaEventDisableTiming) != cudaSuccess ||

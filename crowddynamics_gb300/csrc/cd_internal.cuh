@@ -223,11 +223,9 @@ int variant_staged(int variant);
 struct Fork { cudaStream_t s2; cudaEvent_t fork, join, join_stage; };
 // The agent-force stage; with `pair_ev`, events recorded around the pair
 // kernel of the pair pipeline (as external event-record nodes if `captured`).
-// `prologue_launched`: k_prologue already runs on fork->s2 (launch_prologue).
 void launch_forces(const StepArgs &a, cudaStream_t s, int variant,
                    const cudaEvent_t *pair_ev = nullptr, bool captured = false,
-                   const Fork *fork = nullptr, bool stage_deferred = false,
-                   bool prologue_launched = false);
+                   const Fork *fork = nullptr, bool stage_deferred = false);
 // The per-agent terms before agent-agent (navigation, fluctuation,
 // orientation, adjusting) and the old accelerations, into StepArgs::pro.
 void launch_prologue(const StepArgs &a, cudaStream_t s);

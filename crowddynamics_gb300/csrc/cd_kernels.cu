@@ -2510,13 +2510,11 @@ __device__ __noinline__ double tc_zero_force_torque(const StepArgs &a, int s, in
 // (k_forces_fallback, which otherwise has nothing to do), which runs it again
 // with EXACT, evaluating those signs.
 // The per-agent terms before agent-agent (navigation, fluctuation,
-// orientation, adjusting) of every agent, one lane per agent, for the gather:
-// they do not depend on the pairs, so they run beside the near-list build
-// (which leaves the float64 pipe idle).
+// orientation, adjusting) of every agent, one lane per agent, for the
+// gather: they do not depend on the pairs, so they run beside the near-list
+// build (which leaves the float64 pipe idle).
 template <int BODY>
-__global__ void __launch_bounds__(128) k_prologue(StepArgs a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
+__device__ __forceinline__ void prologue_agent(const StepArgs &a, const int i) {
     double fx, fy, tq, phi0;
     agent_prologue<BODY>(a, i, fx, fy, tq, phi0);
     double4_32a v;
@@ -2535,6 +2533,12 @@ __global__ void __launch_bounds__(128) k_prologue(StepArgs a) {
         w.w = 0.0;
         p[1] = w;
     }
+}
+
+template <int BODY>
+__global__ void __launch_bounds__(128) k_prologue(StepArgs a) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
+        prologue_agent<BODY>(a, i);
 }
 
 template <int BODY, bool EXACT>
@@ -3197,7 +3201,7 @@ void launch_prologue(const StepArgs &a, cudaStream_t s) {
 }
 
 void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEvent_t *pair_ev,
-                   bool captured, const Fork *fork, bool stage_deferred, bool prologue_launched) {
+                   bool captured, const Fork *fork, bool stage_deferred) {
     if (a.n <= 0) return;
     if (variant < 0 || variant >= N_VARIANTS) variant = 0;
     // the pair pipeline needs the near-list buffers: otherwise its lane-group twin
@@ -3221,7 +3225,7 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
             launch_gather(a, sp, 2);
             if (fork) cudaEventRecord(fork->join_stage, fork->s2);
         }
-        if (!prologue_launched) launch_prologue(a, sp);
+        launch_prologue(a, sp);
         if (fork) cudaEventRecord(fork->join, fork->s2);
     } else if (stage_deferred) {
         launch_gather(a, s, 2);
