@@ -324,11 +324,13 @@ def run_ours(args, ws, rank, local):
         if dist is not None:
             dist.barrier()
 
-    # warm-up (graph capture happens here)
-    b.run(max(args.warmup, 3), nodes)
+    # `value`: events around each step's graph launch only (no event node
+    # inside the step graph, whose kernels then stay chained to each other)
+    b.set_timing(True, kernels=False)
+    b.run(max(args.warmup, 3), nodes)          # warm-up (graph capture happens here)
     b.synchronize()
     barrier()
-    b.set_timing(True)
+    b.set_timing(True, kernels=False)
     with Clocks(local) as clk:
         for k in range(args.steps):
             flush.fill_(k & 0xff)
@@ -336,12 +338,25 @@ def run_ours(args, ws, rank, local):
             with ProfileRange(args.profile_range == 'step' and k == args.steps - 1):
                 b.run(1, nodes)
     barrier()
+    run_ms = max_over_ranks(b.kernel_time()['run_ms'], dist)
+    value = whole_job_rate(ws, n, args.steps, run_ms / 1e3)
+    # the kernels' own times: the same steps again with CUDA events inside the
+    # step graph around the force stage, the float32 pair pass and k_pairs
+    b.set_timing(True, kernels=True)
+    b.run(2, nodes)
+    b.synchronize()
+    b.set_timing(True, kernels=True)
+    for k in range(args.steps):
+        flush.fill_(k & 0xff)
+        torch.cuda.synchronize()
+        b.run(1, nodes)
     kt = b.kernel_time()
     b.set_timing(False)
-    run_ms = max_over_ranks(kt['run_ms'], dist)
-    value = whole_job_rate(ws, n, args.steps, run_ms / 1e3)
     force_ms = kt['force_ms'] / max(kt['force_launches'], 1)
     pair_ms = kt['pair_ms'] / max(kt['pair_launches'], 1) if kt['pair_launches'] else None
+    light_ms = kt['light_ms'] / max(kt['pair_launches'], 1) if kt['pair_launches'] else None
+    pairs_ms = kt['pairs_ms'] / max(kt['pair_launches'], 1) if kt['pair_launches'] else None
+    stepk_ms = kt['run_ms'] / max(kt['run_steps'], 1)
     split = b.pair_split() if pair_ms else None     # the last timed step's flat list
     counts1 = b.pair_counts()
     flops = 0.5 * (algorithmic_flops(scen, counts0) + algorithmic_flops(scen, counts1))
@@ -352,11 +367,11 @@ def run_ours(args, ws, rank, local):
     stage_achieved = flops_req / (force_ms / 1e3) / 1e12
     stage_effective = flops / (force_ms / 1e3) / 1e12
     peak = peak_gflops / 1e3
-    # the pair pipeline: its pair stage (ThreeCircle: the float32 pass
-    # k_pairs_light, then k_pairs; the pair events bracket both) dominates
+    # the pair pipeline: its pair stage (the float32 pass k_pairs_light, then
+    # k_pairs) dominates the step, and k_pairs the stage
     if pair_ms:
         kernel, kernel_ms, kflops, kreq = 'k_pairs', pair_ms, pflops, rflops
-        label = 'k_pairs_light + k_pairs'
+        label = 'k_pairs'
     else:
         kernel, kernel_ms, kflops, kreq = 'k_forces', force_ms, flops, flops_req
         label = kernel
@@ -386,15 +401,22 @@ def run_ours(args, ws, rank, local):
     # instructions) and FP64 pipe activity of the dominant kernels per step,
     # from the committed summary of one ncu capture of this workload
     traffic = pipe = executed = None
+    stage = None
     tpath = os.path.join(ROOT, 'profiles', 'pair_stage_field100k_threecircle.json')
     if n == 100_000 and scen.body == 'three_circle' and kernel == 'k_pairs' and \
             os.path.exists(tpath):
         prof = json.load(open(tpath))
-        traffic, pipe = prof.get('dram_bytes_per_step'), prof.get('fp64_pipe_active')
-        executed = prof.get('fp64_flops_per_step')
-    # achieved: the float64 work the stage executes (the float32 certificates
-    # decide the rest exactly); without a capture of this workload, the
-    # model count of the float64 results the state depends on
+        traffic = prof['dram_bytes_by_kernel']['k_pairs']
+        pipe = prof['fp64_pipe_active_by_kernel']['k_pairs']
+        executed = prof['fp64_flops_by_kernel']['k_pairs']
+        stage = {'kernels': 'k_pairs_light + k_pairs', 'ms': pair_ms, 'light_ms': light_ms,
+                 'flops': prof['fp64_flops_per_step'], 'traffic': prof['dram_bytes_per_step'],
+                 'fp64_pipe_active_ncu': prof['fp64_pipe_active'],
+                 'frac': prof['fp64_flops_per_step'] / (pair_ms / 1e3) / 1e12 / (peak_gflops / 1e3)}
+        kernel_ms = pairs_ms
+    # achieved: the float64 work the kernel executes (the float32 certificates
+    # decide the rest exactly); without a capture of this workload, the model
+    # count of the float64 results the state depends on over the whole stage
     work = executed if executed else kreq
     achieved = work / (kernel_ms / 1e3) / 1e12
 
@@ -441,10 +463,12 @@ def run_ours(args, ws, rank, local):
                          'work': 'float64 flops executed per step (ncu DADD+DMUL+2*DFMA)'
                                  if executed else 'model count of float64 results',
                          'peak_source': 'measured live (FP64 FMA chain, 2 flops per FMA)',
-                         'fp64_pipe_active_ncu': pipe, 'model_flops_per_launch': kreq,
+                         'fp64_pipe_active_ncu': pipe, 'pair_stage': stage,
+                         'model_flops_per_stage': kreq,
                          'reference_algorithm_frac': effective / peak,
                          'hbm_frac': hbm_gbs / hbm_peak if hbm_peak else None,
-                         'force_stage_ms': force_ms, 'force_stage_frac': stage_achieved / peak},
+                         'force_stage_ms': force_ms, 'force_stage_frac': stage_achieved / peak,
+                         'step_ms_with_kernel_events': stepk_ms},
             'clocks': clk.summary()}
     detail['roofline'] = {'pair_split': split,
                           'hbm': {'bytes_per_agent_step': bytes_agent, 'achieved_gbs': hbm_gbs,

@@ -39,7 +39,7 @@ SYMBOLS = (
     'cd_synchronize', 'cd_get_time', 'cd_get_cell_list', 'cd_pair_counts',
     'cd_sizes', 'cd_set_timing', 'cd_kernel_time', 'cd_kernels_per_step',
     'cd_measure_fp64_peak', 'cd_agent_agent_noalloc', 'cd_variant_count',
-    'cd_variant_shape', 'cd_set_variant', 'cd_set_near_list_capacity', 'cd_pair_kernel_time', 'cd_pair_split',
+    'cd_variant_shape', 'cd_set_variant', 'cd_set_near_list_capacity', 'cd_pair_kernel_time', 'cd_pair_kernel_times', 'cd_pair_split',
     'cd_set_direction_maps', 'cd_set_noise_mode', 'cd_set_direct_host_access', 'cd_snapshot_agents', 'cd_snapshot_wait',
     'cd_herding', 'cd_inside_domain', 'cd_target_reached', 'cd_exit_detection',
     'cd_launch',
@@ -114,6 +114,7 @@ def load(path=None):
         'cd_set_variant': (ctypes.c_int, [P, ctypes.c_int]),
         'cd_set_near_list_capacity': (ctypes.c_int, [P, i64]),
         'cd_pair_kernel_time': (ctypes.c_int, [P, pd, pi64]),
+        'cd_pair_kernel_times': (ctypes.c_int, [P, pd, pd, pi64]),
         'cd_pair_split': (ctypes.c_int, [P, pi64, pi64, pi64]),
         'cd_set_noise_mode': (ctypes.c_int, [P, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64]),
         'cd_set_direct_host_access': (ctypes.c_int, [P, ctypes.c_int]),

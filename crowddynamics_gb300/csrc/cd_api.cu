@@ -106,12 +106,13 @@ struct cd_ctx {
     uint64_t graph_gen = 0;        // bumped whenever a graph of this context goes stale
     int variant = 0;
 
-    bool timing = false;
+    int timing = 0;                // 0 off; 1 run, step and kernel events; 2 run events only
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs0 = nullptr, evs1 = nullptr;
     cudaEvent_t evr0 = nullptr, evr1 = nullptr;
-    cudaEvent_t evp[2] = {nullptr, nullptr};     // around the pair kernel
+    cudaEvent_t evp[3] = {nullptr, nullptr, nullptr};   // pair stage: start, after the
+                                                         // float32 pass, end
     cudaEvent_t evsnap[CD_SNAPSHOT_SLOTS] = {};  // completion of asynchronous snapshots
-    double pair_ms = 0;
+    double pair_ms = 0, light_ms = 0;
     int64_t pair_launches = 0;
     double force_ms = 0, step_ms = 0, run_ms = 0;
     int64_t launches = 0, run_steps = 0;
@@ -235,6 +236,7 @@ void release(cd_ctx *c) {
     if (c->evr1) cudaEventDestroy(c->evr1);
     if (c->evp[0]) cudaEventDestroy(c->evp[0]);
     if (c->evp[1]) cudaEventDestroy(c->evp[1]);
+    if (c->evp[2]) cudaEventDestroy(c->evp[2]);
     for (cudaEvent_t e : c->evsnap)
         if (e) cudaEventDestroy(e);
     if (c->ext_host) cudaFreeHost(c->ext_host);
@@ -333,21 +335,24 @@ void enqueue_cells(cd_ctx *c, const StepArgs &a, bool defer_stage = false) {
 
 // One step on the context stream.  `timed`: record the step and force-kernel
 // events (cd_step).  `captured`: the sequence is being captured into a graph;
-// the force-kernel events are then recorded as external event-record nodes
-// (a plain cudaEventRecord under capture only marks a capture dependency).
+// with kernel timing (mode 1) the force-stage and pair events are then
+// recorded as external event-record nodes (a plain cudaEventRecord under
+// capture only marks a capture dependency); otherwise the graph holds none,
+// so that every kernel of the step stays chained to the one before it.
 void enqueue_step(cd_ctx *c, int nodes, bool timed, bool captured = false) {
     StepArgs a = args_of(c, nodes);
+    const bool kev = captured && c->timing == 1;
     // the pair pipeline writes the float64 staged records beside the near lists
     const bool defer = cdk::variant_pairs(c->variant) && c->nl_cnt;
     if (timed) cudaEventRecord(c->evs0, c->stream);
     enqueue_cells(c, a, defer);
     if (timed) cudaEventRecord(c->ev0, c->stream);
-    if (captured) cudaEventRecordWithFlags(c->ev0, c->stream, cudaEventRecordExternal);
+    if (kev) cudaEventRecordWithFlags(c->ev0, c->stream, cudaEventRecordExternal);
     const cdk::Fork fork{c->stream2, c->ev_fork, c->ev_join, c->ev_join_stage};
-    cdk::launch_forces(a, c->stream, c->variant, (timed || captured) ? c->evp : nullptr, captured,
+    cdk::launch_forces(a, c->stream, c->variant, (timed || kev) ? c->evp : nullptr, captured,
                        &fork, defer);
     if (timed) cudaEventRecord(c->ev1, c->stream);
-    if (captured) cudaEventRecordWithFlags(c->ev1, c->stream, cudaEventRecordExternal);
+    if (kev) cudaEventRecordWithFlags(c->ev1, c->stream, cudaEventRecordExternal);
     if (timed) cudaEventRecord(c->evs1, c->stream);
 }
 
@@ -419,10 +424,12 @@ int ensure_near_lists(cd_ctx *c, int nodes) {
 // Pair-kernel time of the step just timed (pair pipeline with agent-agent).
 void add_pair_time(cd_ctx *c, int nodes) {
     if (!cdk::variant_pairs(c->variant) || !(nodes & CD_NODE_AGENT_AGENT) || c->n == 0) return;
-    float pms = 0;
-    if (cudaEventElapsedTime(&pms, c->evp[0], c->evp[1]) == cudaSuccess) {
+    float pms = 0, lms = 0;
+    if (cudaEventElapsedTime(&pms, c->evp[0], c->evp[2]) == cudaSuccess) {
         c->pair_ms += pms;
         c->pair_launches += 1;
+        if (c->defer_list && cudaEventElapsedTime(&lms, c->evp[0], c->evp[1]) == cudaSuccess)
+            c->light_ms += lms;
     }
 }
 
@@ -719,6 +726,7 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
         cudaEventCreate(&c->evr1);
         cudaEventCreate(&c->evp[0]);
         cudaEventCreate(&c->evp[1]);
+        cudaEventCreate(&c->evp[2]);
         for (cudaEvent_t &e : c->evsnap) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
         cudaError_t e = cudaDeviceSynchronize();
         if (e != cudaSuccess) rc = fail(c, CD_ERR_CUDA, cudaGetErrorString(e));
@@ -1177,7 +1185,7 @@ int cd_step(cd_ctx *c, int nodes, double *dt) {
     if (int rc = prepare_step(c, nodes)) return rc;
     if ((nodes & CD_NODE_FLUCTUATION) && !c->noise_dev && !c->noise_pending)
         return fail(c, CD_ERR_INVALID_VALUE, "cd_set_noise must precede a step with fluctuation");
-    enqueue_step(c, nodes, c->timing);
+    enqueue_step(c, nodes, c->timing != 0);
     if ((nodes & CD_NODE_FLUCTUATION) && !c->noise_dev) c->noise_pending = false;
     CUDA_OR_FAIL(c, cudaGetLastError());
     if (c->timing) {
@@ -1245,7 +1253,7 @@ int cd_run(cd_ctx *c, int nodes, int64_t steps) {
         cudaEventElapsedTime(&ms, c->evr0, c->evr1);
         c->run_ms += ms;
         c->run_steps += steps;
-        if (steps == 1) {      // the graph's own events bracket its force kernel
+        if (steps == 1 && c->timing == 1) {   // the graph's own events bracket its force stage
             float fms = 0;
             cudaEventElapsedTime(&fms, c->ev0, c->ev1);
             c->force_ms += fms;
@@ -1326,8 +1334,11 @@ int cd_sizes(const cd_ctx *c, int64_t *n_agents, int64_t *n_walls, int64_t *n_ce
 
 int cd_set_timing(cd_ctx *c, int enable) {
     if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
-    c->timing = enable != 0;
-    c->force_ms = c->step_ms = c->run_ms = c->pair_ms = 0;
+    if (enable < 0 || enable > 2) return fail(c, CD_ERR_INVALID_VALUE, "timing mode must be 0, 1 or 2");
+    // the step graph holds kernel events only in mode 1
+    if ((enable == 1) != (c->timing == 1)) drop_graph(c);
+    c->timing = enable;
+    c->force_ms = c->step_ms = c->run_ms = c->pair_ms = c->light_ms = 0;
     c->launches = c->run_steps = c->pair_launches = 0;
     return CD_OK;
 }
@@ -1335,6 +1346,14 @@ int cd_set_timing(cd_ctx *c, int enable) {
 int cd_pair_kernel_time(cd_ctx *c, double *ms, int64_t *launches) {
     if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
     if (ms) *ms = c->pair_ms;
+    if (launches) *launches = c->pair_launches;
+    return CD_OK;
+}
+
+int cd_pair_kernel_times(cd_ctx *c, double *light_ms, double *pairs_ms, int64_t *launches) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (light_ms) *light_ms = c->light_ms;
+    if (pairs_ms) *pairs_ms = c->pair_ms - c->light_ms;
     if (launches) *launches = c->pair_launches;
     return CD_OK;
 }

@@ -221,8 +221,9 @@ int variant_staged(int variant);
 // A second stream for work that runs beside the near-list build (fork after
 // the work already on the main stream, join before the gather).
 struct Fork { cudaStream_t s2; cudaEvent_t fork, join, join_stage; };
-// The agent-force stage; with `pair_ev`, events recorded around the pair
-// kernel of the pair pipeline (as external event-record nodes if `captured`).
+// The agent-force stage; with `pair_ev` (3 events), events recorded before
+// the pair stage, after its float32 pass and after it (as external
+// event-record nodes if `captured`).
 void launch_forces(const StepArgs &a, cudaStream_t s, int variant,
                    const cudaEvent_t *pair_ev = nullptr, bool captured = false,
                    const Fork *fork = nullptr, bool stage_deferred = false);

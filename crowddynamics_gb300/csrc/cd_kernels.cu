@@ -3245,11 +3245,13 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
             int rl = (dev >= 0 && dev < 64) ? g_light_blocks[dev][body] : 0;
             if (rl <= 0) rl = 152;
             kPairsLight[body]<<<std::min(nblk((long long)a.n * 16, NTG), rl), NTG, 0, s>>>(a);
+            if (pair_ev)            // the float32 pass's end (timing only)
+                cudaEventRecordWithFlags(pair_ev[1], s, captured ? cudaEventRecordExternal : 0);
         }
-        // after k_pairs_light: chained to it
-        launch_k(a.defer_list != nullptr, kPairs[body],
+        // after k_pairs_light: chained to it (unless an event sits between)
+        launch_k(a.defer_list != nullptr && !pair_ev, kPairs[body],
                  std::min(nblk((long long)a.n * 16, NTG), rp), NTG, pairs_smem_bytes(body), s, a);
-        if (pair_ev) cudaEventRecordWithFlags(pair_ev[1], s, captured ? cudaEventRecordExternal : 0);
+        if (pair_ev) cudaEventRecordWithFlags(pair_ev[2], s, captured ? cudaEventRecordExternal : 0);
     }
     int resident = (dev >= 0 && dev < 64) ? g_forces_blocks[dev][body][variant] : 0;
     if (resident <= 0) resident = 152;

@@ -315,21 +315,28 @@ class DeviceBatch:
         self._chk(self._lib.cd_pair_counts(self._ctx, N.i64ptr(c)))
         return c
 
-    def set_timing(self, enable=True):
-        self._chk(self._lib.cd_set_timing(self._ctx, int(bool(enable))))
+    def set_timing(self, enable=True, kernels=True):
+        """CUDA-event timing; ``kernels=False`` times whole runs only, with no
+        event node inside the step graph (see cd_set_timing)."""
+        mode = 0 if not enable else (1 if kernels else 2)
+        self._chk(self._lib.cd_set_timing(self._ctx, mode))
 
     def kernel_time(self):
         """dict(force_ms, force_launches, step_ms, run_ms, run_steps, pair_ms,
-        pair_launches) since the last set_timing."""
+        pair_launches, light_ms, pairs_ms) since the last set_timing (pair_ms:
+        the pair stage; light_ms, pairs_ms: its float32 pass and k_pairs)."""
         f, s, r = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         n, rn = ctypes.c_int64(), ctypes.c_int64()
         self._chk(self._lib.cd_kernel_time(self._ctx, ctypes.byref(f), ctypes.byref(n),
                                            ctypes.byref(s), ctypes.byref(r), ctypes.byref(rn)))
         pm, pn = ctypes.c_double(), ctypes.c_int64()
         self._chk(self._lib.cd_pair_kernel_time(self._ctx, ctypes.byref(pm), ctypes.byref(pn)))
+        lm, km = ctypes.c_double(), ctypes.c_double()
+        self._chk(self._lib.cd_pair_kernel_times(self._ctx, ctypes.byref(lm), ctypes.byref(km),
+                                                 None))
         return dict(force_ms=f.value, force_launches=n.value, step_ms=s.value,
                     run_ms=r.value, run_steps=rn.value, pair_ms=pm.value,
-                    pair_launches=pn.value)
+                    pair_launches=pn.value, light_ms=lm.value, pairs_ms=km.value)
 
     def pair_split(self):
         """The last pair-pipeline step's flat pair list: dict(pairs,

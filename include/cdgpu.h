@@ -257,13 +257,22 @@ int cd_sizes(const cd_ctx *ctx, int64_t *n_agents, int64_t *n_walls,
  * around the whole step and around the agent-force kernel, and cd_run
  * around its graph launches; cd_kernel_time returns the accumulated
  * milliseconds since the last cd_set_timing: force kernel (and its launch
- * count), whole cd_step steps, and cd_run steps (and their count). */
+ * count), whole cd_step steps, and cd_run steps (and their count).
+ * `enable`: 0 off; 1 all of these, the step graph then holding event nodes
+ * around the force stage and the pair stage (one-step cd_run calls accumulate
+ * them); 2 cd_step's events and cd_run's around its launches only, the step
+ * graph holding no event node (the kernels of a step stay chained to each
+ * other, as with timing off). */
 int cd_set_timing(cd_ctx *ctx, int enable);
 int cd_kernel_time(cd_ctx *ctx, double *force_ms, int64_t *force_launches,
                    double *step_ms, double *run_ms, int64_t *run_steps);
-/* Time and launches of the pair kernel alone (pair-pipeline variants, steps
- * with agent-agent), accumulated like cd_kernel_time. */
+/* Time and launches of the pair stage (the float32 pair pass and the pair
+ * kernel; pair-pipeline variants, steps with agent-agent), accumulated like
+ * cd_kernel_time (timing mode 1). */
 int cd_pair_kernel_time(cd_ctx *ctx, double *ms, int64_t *launches);
+/* The same split into the float32 pair pass (k_pairs_light) and the float64
+ * pair kernel (k_pairs); light_ms is 0 without a float32 pass. */
+int cd_pair_kernel_times(cd_ctx *ctx, double *light_ms, double *pairs_ms, int64_t *launches);
 /* The last pair-pipeline step's flat pair list: its pairs, those in its
  * first part (guessed to need the social force) and, for ThreeCircle
  * contexts, those the float32 pass left to the float64 pair kernel (zeros
