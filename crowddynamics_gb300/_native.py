@@ -187,7 +187,8 @@ def dptr(a):
 
 def variants():
     """[(threads_per_block, staged_per_thread, lanes_per_agent, pair_pipeline)]
-    of the force-kernel variants."""
+    of the force-kernel variants (pair_pipeline 0: per-agent kernels, 1: the
+    pair pipeline, 2: the pair pipeline with a separate force pass)."""
     L = load()
     n = ctypes.c_int()
     check(L.cd_variant_count(ctypes.byref(n)))

@@ -409,10 +409,15 @@ __device__ __forceinline__ void put_adj(double *res, int e, double gx, double gy
     p[2] = make_double2(gk, gt0);
 }
 
+// The flat list's first part (pairs guessed to need the social force), then
+// the pairs of the second part that the float32 pass could not certify to be
+// without a force; that pass wrote the others' zero records.
 __global__ void __launch_bounds__(NT) k_adj_pairs(StepArgs a, AdjArgs q) {
     if (a.nl_off[a.n] > a.nl_cap) return;
-    const int npairs = a.fw_off[a.n];
-    for (int k = blockIdx.x * NT + threadIdx.x; k < npairs; k += gridDim.x * NT) {
+    const int nfirst = a.fs_off[a.n];
+    const int npairs = nfirst + a.work[1];
+    for (int kk = blockIdx.x * NT + threadIdx.x; kk < npairs; kk += gridDim.x * NT) {
+        const int k = kk < nfirst ? kk : a.defer_list[kk - nfirst];
         const int2 pe = __ldg(&a.fw_pairs[k]);
         const int s = pe.x, e = pe.y;
         const int t = __ldg(&a.nl_idx[e]);
@@ -428,34 +433,57 @@ __global__ void __launch_bounds__(NT) k_adj_pairs(StepArgs a, AdjArgs q) {
     }
 }
 
+// L lanes per agent: lane r adds entries r, r + L, ... of the agent's list
+// and walls r, r + L, ...; the lanes' sums meet in a fixed butterfly, so the
+// result is deterministic.  One lane per agent left 5000 agents with one warp
+// per SM, each lane walking about a hundred 48-byte entries in turn.
+template <int L>
 __global__ void __launch_bounds__(NT) k_adj_gather(StepArgs a, AdjArgs q) {
     if (a.nl_off[a.n] > a.nl_cap) return;               // k_adj_forces' step
-    const int s = blockIdx.x * NT + threadIdx.x;
-    if (s >= a.n) return;
-    const int i = a.perm[s];
+    const int r = threadIdx.x & (L - 1);
+    const int s = (int)(((long long)blockIdx.x * NT + threadIdx.x) / L);
+    const bool valid = s < a.n;
     PairGrad G{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    const int o1 = a.nl_off[s + 1];
-    for (int e = a.nl_off[s]; e < o1; ++e) {
-        const double2 *p = reinterpret_cast<const double2 *>(a.nl_res + (size_t)e * ADJ_RES_D);
-        const double2 x = p[0], v = p[1], kt = p[2];
-        G.gxx += x.x; G.gxy += x.y;
-        G.gvx += v.x; G.gvy += v.y;
-        G.gk += kt.x; G.gt0 += kt.y;
-    }
-    const double uxi = q.lF[2 * i], uyi = q.lF[2 * i + 1];
-    const ScenDev sc = a.scen[a.scen_of[i]];
-    if (sc.wall_count > 0) {
-        const float4 me = a.cull[s];
-        const int my_cell = a.key[i];
-        const Circ A = load_circ(a.stage, s);
-        const bool all_walls = me.z > (float)sc.wall_reach;
-        const int wb = all_walls ? sc.wall_begin : __ldg(&a.wall_start[my_cell]);
-        const int we = all_walls ? sc.wall_begin + sc.wall_count : __ldg(&a.wall_start[my_cell + 1]);
-        for (int qw = wb; qw < we; ++qw) {
-            const int w = all_walls ? qw : __ldg(&a.wall_idx[qw]);
-            wall_circ_vjp(A, a.walls + (size_t)w * WALL_D, uxi, uyi, G.gxx, G.gxy, G.gvx, G.gvy);
+    int i = 0;
+    double uxi = 0.0, uyi = 0.0;
+    if (valid) {
+        i = a.perm[s];
+        const int o1 = a.nl_off[s + 1];
+        for (int e = a.nl_off[s] + r; e < o1; e += L) {
+            const double2 *p = reinterpret_cast<const double2 *>(a.nl_res + (size_t)e * ADJ_RES_D);
+            const double2 x = p[0], v = p[1], kt = p[2];
+            G.gxx += x.x; G.gxy += x.y;
+            G.gvx += v.x; G.gvy += v.y;
+            G.gk += kt.x; G.gt0 += kt.y;
+        }
+        uxi = q.lF[2 * i];
+        uyi = q.lF[2 * i + 1];
+        const ScenDev sc = a.scen[a.scen_of[i]];
+        if (sc.wall_count > 0) {
+            const float4 me = a.cull[s];
+            const int my_cell = a.key[i];
+            const Circ A = load_circ(a.stage, s);
+            const bool all_walls = me.z > (float)sc.wall_reach;
+            const int wb = all_walls ? sc.wall_begin : __ldg(&a.wall_start[my_cell]);
+            const int we = all_walls ? sc.wall_begin + sc.wall_count
+                                     : __ldg(&a.wall_start[my_cell + 1]);
+            for (int qw = wb + r; qw < we; qw += L) {
+                const int w = all_walls ? qw : __ldg(&a.wall_idx[qw]);
+                wall_circ_vjp(A, a.walls + (size_t)w * WALL_D, uxi, uyi, G.gxx, G.gxy, G.gvx,
+                              G.gvy);
+            }
         }
     }
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) {
+        G.gxx += __shfl_xor_sync(0xffffffffu, G.gxx, o);
+        G.gxy += __shfl_xor_sync(0xffffffffu, G.gxy, o);
+        G.gvx += __shfl_xor_sync(0xffffffffu, G.gvx, o);
+        G.gvy += __shfl_xor_sync(0xffffffffu, G.gvy, o);
+        G.gk += __shfl_xor_sync(0xffffffffu, G.gk, o);
+        G.gt0 += __shfl_xor_sync(0xffffffffu, G.gt0, o);
+    }
+    if (!valid || r != 0) return;
     adj_finish(a, q, i, uxi, uyi, G);
 }
 
@@ -567,8 +595,11 @@ void launch_adj_forces(const StepArgs &a, const AdjArgs &q, cudaStream_t s) {
     const long long n = a.n;
     const int over = a.nl_cnt != nullptr;     // pair pipeline first, this as its fallback
     if (over) {
+        launch_adj_light(a, s);
         k_adj_pairs<<<nblk(n * 16, NT), NT, 0, s>>>(a, q);
-        k_adj_gather<<<nblk(n, NT), NT, 0, s>>>(a, q);
+        // lanes per agent: enough warps to fill the SMs at small agent counts
+        if (n < 20000) k_adj_gather<16><<<nblk(n * 16, NT), NT, 0, s>>>(a, q);
+        else k_adj_gather<4><<<nblk(n * 4, NT), NT, 0, s>>>(a, q);
     }
     // lanes per agent: enough warps to fill the SMs at small agent counts
     if (n < 20000) k_adj_forces<16><<<nblk(n * 16, NT), NT, 0, s>>>(a, q, over);

@@ -88,6 +88,7 @@ struct cd_ctx {
     int *fs_cnt = nullptr, *fs_off = nullptr, *fs_scan = nullptr;
     int2 *fw_pairs = nullptr;
     int *defer_list = nullptr;                     // the float32 pair pass's leftovers
+    double2 *pair_jobs = nullptr;                  // k_pairs -> k_pair_forces
     int64_t nl_cap = 0;
     bool nl_fixed = false;              // capacity set by cd_set_near_list_capacity
 
@@ -198,6 +199,7 @@ StepArgs args_of(cd_ctx *c, int nodes) {
     a.fw_off = c->fw_off;
     a.fw_pairs = c->fw_pairs;
     a.defer_list = c->defer_list;
+    a.pair_jobs = c->pair_jobs;
     a.fw_scan = c->fw_scan;
     a.fs_cnt = c->fs_cnt;
     a.fs_off = c->fs_off;
@@ -222,7 +224,7 @@ void release(cd_ctx *c) {
                     c->noise_f, c->noise_m, c->vmax, c->v0max, c->dt, c->time_tot,
                     c->err, c->work, c->diag, c->aos, c->nl_cnt, c->nl_off, c->nl_fwd,
                     c->nl_scan, c->nl_idx, c->nl_res, c->nl_kind, c->fw_cnt, c->fw_off, c->fw_scan,
-                    c->fw_pairs, c->defer_list, c->ext, c->max_partial, c->tgt, c->navmap, c->rng_step,
+                    c->fw_pairs, c->defer_list, c->pair_jobs, c->ext, c->max_partial, c->tgt, c->navmap, c->rng_step,
                     c->states, c->herd, c->scen_h, c->counters, c->reached, c->polys,
                     c->poly_off, c->fs_cnt, c->fs_off, c->fs_scan, c->nl_mask, c->nl_nch,
                     c->fix_count, c->fix_list, c->slot_of, c->pro};
@@ -362,7 +364,8 @@ int64_t kernels_per_step(const cd_ctx *c, int nodes) {
     k += cdk::scan_launches_single((int)c->ncells);
     if (cdk::variant_pairs(c->variant) && c->nl_cnt) k += 2;     // prologue, float64 staging
     if (cdk::variant_pairs(c->variant) && (nodes & CD_NODE_AGENT_AGENT) && c->nl_cnt)
-        k += 5 + (c->defer_list ? 1 : 0);         // count, scans, fill, (float32 pass,) pairs, fallback
+        k += 5 + (c->defer_list ? 1 : 0) +        // count, scans, fill, (float32 pass,) pairs,
+             (cdk::variant_split(c->variant) ? 1 : 0);    // (force pass,) fallback
     return k;
 }
 
@@ -375,7 +378,9 @@ int alloc_near_lists(cd_ctx *c, int64_t cap) {
     if (c->nl_kind) cudaFree(c->nl_kind);
     if (c->fw_pairs) cudaFree(c->fw_pairs);
     if (c->defer_list) cudaFree(c->defer_list);
+    if (c->pair_jobs) cudaFree(c->pair_jobs);
     c->defer_list = nullptr;
+    c->pair_jobs = nullptr;
     c->nl_idx = nullptr;
     c->nl_res = nullptr;
     c->nl_kind = nullptr;
@@ -388,6 +393,8 @@ int alloc_near_lists(cd_ctx *c, int64_t cap) {
         if (int rc = dalloc(c, &c->nl_kind, cap)) return rc;
         if (int rc = dalloc(c, &c->fw_pairs, cap)) return rc;
         if (int rc = dalloc(c, &c->defer_list, cap)) return rc;
+        const int64_t job_q = c->body == CD_BODY_CIRCULAR ? cdk::JOB_Q_CIRC : cdk::JOB_Q_TC;
+        if (int rc = dalloc(c, &c->pair_jobs, (cap / 2 + 1) * job_q)) return rc;
     }
     c->nl_cap = cap;
     drop_graph(c);
@@ -604,7 +611,7 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     cd_ctx *c = new cd_ctx();
     c->body = body_type;
     c->n = n;
-    c->variant = cdk::default_variant(n);
+    c->variant = cdk::default_variant(n, body_type == CD_BODY_CIRCULAR ? 0 : 1);
     c->nw = nw;
     c->ncells = ncells;
     c->nscen = (int)n_scenarios;
@@ -686,7 +693,7 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->dt, n_scenarios));
     step(dalloc(c, &c->time_tot, n_scenarios));
     step(dalloc(c, &c->err, 1));
-    step(dalloc(c, &c->work, 2));
+    step(dalloc(c, &c->work, 4));
     step(dalloc(c, &c->diag, (int64_t)CD_COUNT_COLS * n));
     step(dalloc(c, &c->nl_cnt, n + 1));
     step(dalloc(c, &c->nl_off, n + 1));
@@ -1919,7 +1926,7 @@ extern "C" int cd_agent_agent_noalloc(int body_type, int64_t n, const double *co
     cdk::launch_prepare(a, st);
     cdk::launch_scan(a.count, a.start, ncells, scan, st);
     cdk::launch_scatter(a, st, false, 0);               // rank + gather
-    cdk::launch_forces(a, st, cdk::default_group_variant(n));
+    cdk::launch_forces(a, st, cdk::default_group_variant(n, a.body ? 1 : 0));
     CUDA_OR_FAIL(nullptr, cudaGetLastError());
     int h = 0;
     CUDA_OR_FAIL(nullptr, cudaMemcpyAsync(&h, a.err, sizeof(int), cudaMemcpyDeviceToHost, st));

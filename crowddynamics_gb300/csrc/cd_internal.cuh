@@ -110,6 +110,8 @@ struct StepArgs {
     int2 *fw_pairs;              // flat list of (slot, entry) for those entries
     int *defer_list;             // flat-list indices the float32 pair pass left to k_pairs
                                  // (nl_cap entries; null: no float32 pass)
+    double2 *pair_jobs;          // the pairs k_pairs found to have a force, for k_pair_forces
+                                 // (nl_cap / 2 + 1 records of JOB_Q_TC / JOB_Q_CIRC double2)
     int *fw_scan;                // scan scratch (as nl_scan)
     int *fs_cnt, *fs_off;        // per agent: those guessed to need the social force, scan
     int *fs_scan;                // scan scratch (as nl_scan)
@@ -119,6 +121,10 @@ struct StepArgs {
 // the adjoint's records (Circular contexts) hold ADJ_RES_D doubles.
 constexpr int RES_D = 4;
 constexpr int ADJ_RES_D = 6;
+// Force-pass job records (double2 each): ThreeCircle (s, t, e, eq), (tau, b),
+// (d, h), (dx, dy), (|d|, flags); Circular (s, t, e, eq), (|x|, sqrt D), (tau, flags).
+constexpr int JOB_Q_TC = 5;
+constexpr int JOB_Q_CIRC = 3;
 // Device error bit: a pair partner's near list lacked the pair.
 constexpr int ERR_NEAR_LIST = 2;
 
@@ -211,11 +217,12 @@ void launch_scatter(const StepArgs &a, cudaStream_t s, bool after_kernel = false
 // Staged records of the cell-sorted agents: part 0 all, 1 the float32
 // pre-check records, 2 the float64 records.
 void launch_gather(const StepArgs &a, cudaStream_t s, int part = 0, bool after_kernel = false);
-constexpr int N_VARIANTS = 12;      // launch variants of the force kernel
+constexpr int N_VARIANTS = 15;      // launch variants of the force kernel
 bool variant_pairs(int variant);
+bool variant_split(int variant);     // the pair pipeline with the separate force pass
 int variant_lanes(int variant);
-int default_variant(long long n_agents);
-int default_group_variant(long long n_agents);
+int default_variant(long long n_agents, int body);
+int default_group_variant(long long n_agents, int body);
 int variant_threads(int variant);
 int variant_staged(int variant);
 // A second stream for work that runs beside the near-list build (fork after
@@ -234,6 +241,10 @@ void launch_prologue(const StepArgs &a, cudaStream_t s);
 void launch_near_count(const StepArgs &a, cudaStream_t s, int variant);
 // Near lists (counts, scans, fill; 8 lanes per agent) for the state staged in `a`.
 void launch_near_lists(const StepArgs &a, cudaStream_t s);
+// The float32 pass of the Circular reverse step over the flat list's second
+// part: zero adjoint records for the pairs without a force, the rest
+// appended to the deferred list for k_adj_pairs.
+void launch_adj_light(const StepArgs &a, cudaStream_t s);
 void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s);
 // Per-scenario max target_velocity and (if `ext`) max agent extent;
 // `partial` holds scen_max_partials(n_scen) doubles.

@@ -828,10 +828,15 @@ constexpr int RES_DEFER = 3;                // tc_pair_light: float64 needed
 // comes out exactly as pair_circular_eval computes it from that side (Q's
 // relative position, velocity, tau gradient and normal are exact negations
 // of P's), sharing the distance, the time-to-collision and its gradient.
-__device__ __forceinline__ int pair_circular_both(const Circ &A, const Circ &B, double &FPx,
-                                                  double &FPy, double &FQx, double &FQy) {
-    FPx = 0.0; FPy = 0.0; FQx = 0.0; FQy = 0.0;
-    bool forced = false;
+// Two passes: circ_pair_decide returns RES_NONE, RES_ZERO or RES_FORCE with
+// the distance, sqrt(D) and tau in a CircJob; circ_pair_force computes both
+// forces from it.
+struct CircJob {
+    double d, dd, tau;          // |x_P - x_Q|, sqrt of the discriminant, time to collision
+    bool social, contact;
+};
+
+__device__ __forceinline__ int circ_pair_decide(const Circ &A, const Circ &B, CircJob &J) {
     double xx = A.x - B.x, xy = A.y - B.y;
     double d = cdm_hypot(xx, xy);
     double r_tot = A.r + B.r;
@@ -842,29 +847,52 @@ __device__ __forceinline__ int pair_circular_both(const Circ &A, const Circ &B, 
     double b = -(xx * vrx + xy * vry);
     double c = (xx * xx + xy * xy) - r_tot * r_tot;
     double disc = b * b - a * c;
+    J.d = d;
+    J.dd = 0.0;
+    J.tau = 0.0;
+    J.social = false;
+    J.contact = h < 0;
     if (disc > 0 && a != 0) {
         double dd = sqrt(disc);
         double tau = (b - dd) / a;
         if (!(tau <= 0 || tau > TAU_MAX)) {
-            forced = true;
-            double gx = (vrx - (vrx * b + xx * a) / dd) / a;
-            double gy = (vry - (vry * b + xy * a) / dd) / a;
-            double cmp = (-A.m) * A.k, cmq = (-B.m) * B.k;
-            double two_t = 2.0 / tau, tt = tau * tau;       // shared terms of magnitude()
-            double magp = (two_t + 1.0 / A.tau0) * cdm_exp(-tau / A.tau0) / tt;
-            // magnitude() depends on (tau, tau_0) only: equal tau_0, equal value
-            double magq = B.tau0 == A.tau0 ? magp
-                                           : (two_t + 1.0 / B.tau0) * cdm_exp(-tau / B.tau0) / tt;
-            FPx = (cmp * gx) * magp;
-            FPy = (cmp * gy) * magp;
-            truncate2(FPx, FPy, F_SOC_MAX);
-            FQx = (cmq * (-gx)) * magq;
-            FQy = (cmq * (-gy)) * magq;
-            truncate2(FQx, FQy, F_SOC_MAX);
+            J.social = true;
+            J.dd = dd;
+            J.tau = tau;
         }
     }
+    return (J.social || J.contact) ? RES_FORCE : RES_ZERO;
+}
+
+__device__ __forceinline__ void circ_pair_force(const Circ &A, const Circ &B, const CircJob &J,
+                                                double &FPx, double &FPy, double &FQx,
+                                                double &FQy) {
+    FPx = 0.0; FPy = 0.0; FQx = 0.0; FQy = 0.0;
+    double xx = A.x - B.x, xy = A.y - B.y;
+    double d = J.d;
+    double r_tot = A.r + B.r;
+    double h = d - r_tot;
+    double vrx = A.vx - B.vx, vry = A.vy - B.vy;
+    if (J.social) {
+        double a = vrx * vrx + vry * vry;
+        double b = -(xx * vrx + xy * vry);
+        double dd = J.dd, tau = J.tau;
+        double gx = (vrx - (vrx * b + xx * a) / dd) / a;
+        double gy = (vry - (vry * b + xy * a) / dd) / a;
+        double cmp = (-A.m) * A.k, cmq = (-B.m) * B.k;
+        double two_t = 2.0 / tau, tt = tau * tau;       // shared terms of magnitude()
+        double magp = (two_t + 1.0 / A.tau0) * cdm_exp(-tau / A.tau0) / tt;
+        // magnitude() depends on (tau, tau_0) only: equal tau_0, equal value
+        double magq = B.tau0 == A.tau0 ? magp
+                                       : (two_t + 1.0 / B.tau0) * cdm_exp(-tau / B.tau0) / tt;
+        FPx = (cmp * gx) * magp;
+        FPy = (cmp * gy) * magp;
+        truncate2(FPx, FPy, F_SOC_MAX);
+        FQx = (cmq * (-gx)) * magq;
+        FQy = (cmq * (-gy)) * magq;
+        truncate2(FQx, FQy, F_SOC_MAX);
+    }
     if (h < 0) {
-        forced = true;
         double nx = 0.0, ny = 0.0, mx = 0.0, my = 0.0;
         if (d != 0.0) { nx = xx / d; ny = xy / d; mx = -nx; my = -ny; }   // (-x)/d == -(x/d)
         double cx, cy;
@@ -875,7 +903,6 @@ __device__ __forceinline__ int pair_circular_both(const Circ &A, const Circ &B, 
         FQx = FQx + cx;
         FQy = FQy + cy;
     }
-    return forced ? RES_FORCE : RES_ZERO;
 }
 
 // Per-warp queue for the square root and division of the defined sub-circle
@@ -891,7 +918,7 @@ struct WarpQueue {
 constexpr float PRESEL_MARGIN = 1e-4f;   // metres (float32 error of h is ~1e-6 m)
 
 
-// Per-warp queue of tc_pair_both: the sub-circle pairs that may have a
+// Per-warp queue of tc_pair_decide: the sub-circle pairs that may have a
 // time-to-collision (9 slots per lane) and each lane's pair geometry.
 constexpr int GEO_D = 19;   // P parts x[3] y[3], Q parts x[3] y[3], P rt rs, Q rt rs, vr, a
 struct PairQueue {
@@ -1196,17 +1223,24 @@ __device__ __forceinline__ void tc_moment_arms(const TC &A, const TC &B, const T
 }
 
 // Both sides of a ThreeCircle pair (interactions.py:73-101,
-// power_law.py:264-363) with P = A first and Q = the pair partner: the
-// distance search, the time-to-collision selection and the tau gradient are
-// computed once; each side's force, contact and torque come out exactly as
-// tc_pair_eval computes them from that side.  Warp collective like
-// tc_pair_eval (all 32 lanes call it).  Returns RES_NONE, RES_ZERO (no
-// force: forces +0, torques signed zeros left to the gather) or RES_FORCE.
-__device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const float4 meF0,
-                                             const float4 meF1, const StepArgs &a, bool act,
-                                             int t, PairQueue &q, int lane, double &FPx,
-                                             double &FPy, double &TP, double &FQx, double &FQy,
-                                             double &TQ) {
+// power_law.py:264-363) with P = A first and Q = the pair partner, in two
+// passes.  tc_pair_decide computes the distance search and the
+// time-to-collision selection once (warp collective like tc_pair_eval: all 32
+// lanes call it) and returns RES_NONE, RES_ZERO (no force: forces +0, torques
+// signed zeros left to the gather) or RES_FORCE with what the force needs in
+// a TcJob; tc_pair_force then computes each side's force, contact and torque
+// exactly as tc_pair_eval computes them from that side.  k_pairs decides,
+// k_pair_forces evaluates the jobs with every lane busy.
+struct TcJob {
+    double tau, b_min, d_min;   // selected time to collision and its root's b, sqrt(D)
+    TcDist D;                   // the exact minimum sub-pair
+    int k_sel;                  // selected sub-pair (3 * P part + Q part)
+    bool social, contact;
+};
+
+__device__ __forceinline__ int tc_pair_decide(const TC &A, const float4 meC, const float4 meF0,
+                                               const float4 meF1, const StepArgs &a, bool act,
+                                               int t, PairQueue &q, int lane, TcJob &J) {
     constexpr unsigned wmask = 0xffffffffu;
     constexpr int nlanes = 32;
     // Q's staged record is loaded only where a float64 path needs it
@@ -1477,11 +1511,37 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
         }
         __syncwarp(wmask);
     }
-    FPx = 0.0; FPy = 0.0; FQx = 0.0; FQy = 0.0;
     const bool social = soc && candmask && !(isnan(tau) || tau <= 0);
-    if (social) {
-        need_b();
-        const int mi = k_sel / 3, ti = k_sel % 3;
+    // No force on either side: forces (+0, +0), and each side's torque
+    // r x (+0, +0) a signed zero that the gather needs only when the agent's
+    // running torque is -0 (the agent is then redone with exact signs)
+    if (!(social || contact)) return inter ? RES_ZERO : RES_NONE;
+    need_b();
+    if (!have_d) {
+        if (!have_pre) pre = tc_presel(dxt, dyt, mox, moy, oox, ooy, mr, orr, act);
+        D = tc_distance_exact(A, B, pre.seq);
+    }
+    J.tau = tau;
+    J.b_min = b_min;
+    J.d_min = d_min;
+    J.D = D;
+    J.k_sel = k_sel;
+    J.social = social;
+    J.contact = contact;
+    return RES_FORCE;
+}
+
+// The forces and torques of a pair tc_pair_decide found to have a force.
+// The relative velocity and a = |v|^2 are formed as tc_pair_decide forms them.
+__device__ __forceinline__ void tc_pair_force(const TC &A, const TC &B, const TcJob &J,
+                                              double &FPx, double &FPy, double &TP, double &FQx,
+                                              double &FQy, double &TQ) {
+    const double vrx = A.vx - B.vx, vry = A.vy - B.vy;
+    FPx = 0.0; FPy = 0.0; FQx = 0.0; FQy = 0.0;
+    if (J.social) {
+        const double av = vrx * vrx + vry * vry;
+        const double tau = J.tau, b_min = J.b_min, d_min = J.d_min;
+        const int mi = J.k_sel / 3, ti = J.k_sel % 3;
         double o1x, o1y, o2x, o2y;
         r_off_part(A, mi, o1x, o1y);
         r_off_part(B, ti, o2x, o2y);
@@ -1502,20 +1562,10 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
         FQy = (cmq * (-gy)) * magq;
         truncate2(FQx, FQy, F_SOC_MAX);
     }
-    TP = 0.0;
-    TQ = 0.0;
-    // No force on either side: forces (+0, +0), and each side's torque
-    // r x (+0, +0) a signed zero that the gather needs only when the agent's
-    // running torque is -0 (the agent is then redone with exact signs)
-    if (!(social || contact)) return inter ? RES_ZERO : RES_NONE;
-    need_b();
-    if (!have_d) {
-        if (!have_pre) pre = tc_presel(dxt, dyt, mox, moy, oox, ooy, mr, orr, act);
-        D = tc_distance_exact(A, B, pre.seq);
-    }
     double npx, npy, nqx, nqy, rpx, rpy, rqx, rqy;
-    tc_moment_arms(A, B, D, npx, npy, nqx, nqy, rpx, rpy, rqx, rqy);
-    if (contact) {
+    tc_moment_arms(A, B, J.D, npx, npy, nqx, nqy, rpx, rpy, rqx, rqy);
+    if (J.contact) {
+        const double h_min = J.D.h;
         double cx, cy;
         force_contact(h_min, npx, npy, vrx, vry, A.mu, A.kappa, A.damp, cx, cy);
         FPx = FPx + cx;
@@ -1526,13 +1576,12 @@ __device__ __forceinline__ int tc_pair_both(const TC &A, const float4 meC, const
     }
     TP = rpx * FPy - rpy * FPx;
     TQ = rqx * FQy - rqy * FQx;
-    return RES_FORCE;
 }
 
-// The float32 part of tc_pair_both alone, for a pair (s, t): RES_NONE or
+// The float32 part of tc_pair_decide alone, for a pair (s, t): RES_NONE or
 // RES_ZERO where its certificates decide the pair (no contact, no positive
 // time to collision; the same tests and margins, so the same decision), and
-// RES_DEFER where tc_pair_both would need float64 (the exact distance, the
+// RES_DEFER where tc_pair_decide would need float64 (the exact distance, the
 // roots, a zero relative speed).  Reads 96 bytes of pre-check records and
 // the two velocities; holds no float64 geometry.
 __device__ __forceinline__ int tc_pair_light(const StepArgs &a, int s, int t) {
@@ -1566,7 +1615,7 @@ __device__ __forceinline__ int tc_pair_light(const StepArgs &a, int s, int t) {
         if (!near_cert) return RES_NONE;
     }
     // interacting without contact: a force only from a positive time to
-    // collision (the relative velocity as tc_pair_both forms it)
+    // collision (the relative velocity as tc_pair_decide forms it)
     const double2 vp = __ldg(&a.stage[(size_t)s * STAGE_Q_TC + 3]);
     const double2 vq = __ldg(&a.stage[(size_t)t * STAGE_Q_TC + 3]);
     const float vxf = (float)(vp.x - vq.x), vyf = (float)(vp.y - vq.y);
@@ -1611,7 +1660,7 @@ __device__ __forceinline__ int tc_pair_light(const StepArgs &a, int s, int t) {
     return RES_ZERO;                                     // no sub-pair has a root
 }
 
-// The float32 certificates of pair_circular_both for a pair (s, t):
+// The float32 certificates of circ_pair_decide for a pair (s, t):
 // RES_NONE where the skin distance is certainly >= 3 m, RES_ZERO where it is
 // certainly in (0, 3) and the pair certainly has no time to collision in
 // (0, 30] (no root; a negative root; or one beyond the 30 s cut-off, with
@@ -1633,7 +1682,7 @@ __device__ __forceinline__ int circ_pair_light(const StepArgs &a, int s, int t) 
     if (h - dmarg >= (float)SIGTH_SOC) return RES_NONE;
     if (!(h + dmarg < (float)SIGTH_SOC && h - dmarg > 0.f)) return RES_DEFER;
     // interacting without contact: a force only from a time to collision
-    // in (0, 30] (the relative velocity as pair_circular_both forms it)
+    // in (0, 30] (the relative velocity as circ_pair_decide forms it)
     const double2 vp = __ldg(&a.stage[(size_t)s * STAGE_Q_CIRC + 1]);
     const double2 vq = __ldg(&a.stage[(size_t)t * STAGE_Q_CIRC + 1]);
     const float vxf = (float)(vp.x - vq.x), vyf = (float)(vp.y - vq.y);
@@ -2223,9 +2272,11 @@ __global__ void __launch_bounds__(NTG) k_nl_count(StepArgs a) {
 template <int L>
 __global__ void __launch_bounds__(NTG) k_nl_fill(StepArgs a) {
     pdl_enter();
-    if (blockIdx.x == 0 && threadIdx.x == 0) {     // k_pairs' work counter, pairs deferred
-        a.work[0] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {     // k_pairs' work counter, pairs deferred,
+        a.work[0] = 0;                              // jobs of the force pass
         a.work[1] = 0;
+        a.work[2] = 0;
+        a.work[3] = 0;
     }
     if (a.nl_off[a.n] > a.nl_cap) return;                 // over capacity: fallback
     constexpr unsigned GMASK = (1u << L) - 1u;
@@ -2368,13 +2419,23 @@ __device__ __forceinline__ void put_pair(const StepArgs &a, int e, int res, doub
     a.nl_kind[e] = kind;
 }
 
+// An adjoint record of zeros: the reverse of a pair without a force (no
+// contact, no time to collision in (0, 30]) adds nothing to either side.
+__device__ __forceinline__ void put_adj_zero(const StepArgs &a, int e) {
+    double2 *p = reinterpret_cast<double2 *>(a.nl_res + (size_t)e * ADJ_RES_D);
+    const double2 z = make_double2(0.0, 0.0);
+    p[0] = z;
+    p[1] = z;
+    p[2] = z;
+}
+
 // The pairs of the flat list's second part (not guessed to need the social
 // force), in float32 alone (tc_pair_light, circ_pair_light): a decided pair
-// writes the kind bytes of both its entries; the others are appended to
-// defer_list for k_pairs, which takes them after the first part.  Few
-// registers, so many warps per SM hide the loads.  Warps take 32
-// consecutive pairs at a time, in turn.
-template <int BODY>
+// writes the kind bytes of both its entries (ADJ: zero adjoint records); the
+// others are appended to defer_list for k_pairs (ADJ: k_adj_pairs), which
+// takes them after the first part.  Few registers, so many warps per SM hide
+// the loads.  Warps take 32 consecutive pairs at a time, in turn.
+template <int BODY, bool ADJ = false>
 __global__ void __launch_bounds__(NTG) k_pairs_light(StepArgs a) {
     pdl_enter();
     constexpr unsigned FULL = 0xffffffffu;
@@ -2401,20 +2462,93 @@ __global__ void __launch_bounds__(NTG) k_pairs_light(StepArgs a) {
             if ((dm >> lane) & 1u) a.defer_list[d0 + __popc(dm & ((1u << lane) - 1u))] = k;
         }
         if (k < npairs && res != RES_DEFER) {
-            put_pair(a, e, res, 0.0, 0.0, 0.0);
             const int eq = partner_entry(a, t, s);
-            if (eq >= 0) put_pair(a, eq, res, 0.0, 0.0, 0.0);
-            else atomicOr(a.err, ERR_NEAR_LIST);
+            if (ADJ) {
+                put_adj_zero(a, e);
+                if (eq >= 0) put_adj_zero(a, eq);
+            } else {
+                put_pair(a, e, res, 0.0, 0.0, 0.0);
+                if (eq >= 0) put_pair(a, eq, res, 0.0, 0.0, 0.0);
+            }
+            if (eq < 0) atomicOr(a.err, ERR_NEAR_LIST);
         }
     }
 }
 
+// Job records of the force pass (JOB_Q_TC / JOB_Q_CIRC double2 each).  Jobs
+// without contact fill the buffer from the front (count work[2]), jobs with
+// contact from the back (count work[3]), so that the force pass's warps take
+// one kind at a time: contact is rare, and mixed in it would make nearly
+// every warp run the contact arithmetic with a few lanes.
+__device__ __forceinline__ int job_cap(const StepArgs &a) { return a.nl_cap / 2 + 1; }
+__device__ __forceinline__ int job_record(const StepArgs &a, int j, int n_front) {
+    return j < n_front ? j : job_cap(a) - 1 - (j - n_front);
+}
+
+__device__ __forceinline__ void put_job(const StepArgs &a, int j, int s, int t, int e, int eq,
+                                        const TcJob &J) {
+    double2 *p = a.pair_jobs + (size_t)j * JOB_Q_TC;
+    *reinterpret_cast<int4 *>(p) = make_int4(s, t, e, eq);
+    const long long f = (long long)J.social | ((long long)J.contact << 1) |
+                        ((long long)J.k_sel << 2) | ((long long)J.D.pp << 6) |
+                        ((long long)J.D.qp << 8);
+    p[1] = make_double2(J.tau, J.b_min);
+    p[2] = make_double2(J.d_min, J.D.h);
+    p[3] = make_double2(J.D.sdx, J.D.sdy);
+    p[4] = make_double2(J.D.sd, __longlong_as_double(f));
+}
+
+__device__ __forceinline__ int4 get_job(const StepArgs &a, int j, TcJob &J) {
+    const double2 *p = a.pair_jobs + (size_t)j * JOB_Q_TC;
+    const int4 h = __ldg(reinterpret_cast<const int4 *>(p));
+    const double2 q1 = __ldg(p + 1), q2 = __ldg(p + 2), q3 = __ldg(p + 3), q4 = __ldg(p + 4);
+    const long long f = __double_as_longlong(q4.y);
+    J.tau = q1.x;
+    J.b_min = q1.y;
+    J.d_min = q2.x;
+    J.D.h = q2.y;
+    J.D.sdx = q3.x;
+    J.D.sdy = q3.y;
+    J.D.sd = q4.x;
+    J.social = (f & 1) != 0;
+    J.contact = (f & 2) != 0;
+    J.k_sel = (int)((f >> 2) & 15);
+    J.D.pp = (int)((f >> 6) & 3);
+    J.D.qp = (int)((f >> 8) & 3);
+    return h;
+}
+
+__device__ __forceinline__ void put_job(const StepArgs &a, int j, int s, int t, int e, int eq,
+                                        const CircJob &J) {
+    double2 *p = a.pair_jobs + (size_t)j * JOB_Q_CIRC;
+    *reinterpret_cast<int4 *>(p) = make_int4(s, t, e, eq);
+    p[1] = make_double2(J.d, J.dd);
+    p[2] = make_double2(J.tau, __longlong_as_double((long long)J.social |
+                                                    ((long long)J.contact << 1)));
+}
+
+__device__ __forceinline__ int4 get_job(const StepArgs &a, int j, CircJob &J) {
+    const double2 *p = a.pair_jobs + (size_t)j * JOB_Q_CIRC;
+    const int4 h = __ldg(reinterpret_cast<const int4 *>(p));
+    const double2 q1 = __ldg(p + 1), q2 = __ldg(p + 2);
+    J.d = q1.x;
+    J.dd = q1.y;
+    J.tau = q2.x;
+    const long long f = __double_as_longlong(q2.y);
+    J.social = (f & 1) != 0;
+    J.contact = (f & 2) != 0;
+    return h;
+}
+
 // Every pair of the flat list once: warps claim 32 consecutive pairs at a
-// time (consecutive pairs mostly share their first agent).  Three blocks per
-// SM (156 registers, none spilled): after the float32 pass most of its pairs
-// take the float64 paths, which run faster unspilled than at four blocks.
-template <int BODY>
-__global__ void __launch_bounds__(NTG, 3) k_pairs(StepArgs a) {
+// time (consecutive pairs mostly share their first agent) and decide them.
+// A pair without a force writes the kind bytes of both its entries.  A pair
+// with a force: its forces at once (SPLIT false), or a job of k_pair_forces
+// (SPLIT true), which evaluates the jobs with its own register budget and
+// with the contact jobs apart.  Which is faster depends on the workload
+// (the launch variants hold both).
+template <int BODY, bool SPLIT>
+__global__ void __launch_bounds__(NTG, (BODY == 0 && SPLIT) ? 6 : 3) k_pairs(StepArgs a) {
     pdl_enter();
     constexpr unsigned FULL = 0xffffffffu;
     if (a.nl_off[a.n] > a.nl_cap) return;
@@ -2449,12 +2583,15 @@ __global__ void __launch_bounds__(NTG, 3) k_pairs(StepArgs a) {
         const int k = nk, s = ns, e = ne, t = nt;
         const bool act = k < npairs;
         nk = claim(ns, ne, nt);
-        double fpx = 0.0, fpy = 0.0, tp = 0.0, fqx = 0.0, fqy = 0.0, tq = 0.0;
         int kind = RES_NONE;
+        TcJob tj;
+        CircJob cj;
+        bool contact = false;
         if (BODY == 0) {
-            if (act)
-                kind = pair_circular_both(load_circ(a.stage, s), load_circ(a.stage, t), fpx, fpy,
-                                          fqx, fqy);
+            if (act) {
+                kind = circ_pair_decide(load_circ(a.stage, s), load_circ(a.stage, t), cj);
+                contact = kind == RES_FORCE && cj.contact;
+            }
         } else {
             TC At;
             float4 me = make_float4(0.f, 0.f, 0.f, 0.f), meF0 = me, meF1 = me;
@@ -2466,20 +2603,82 @@ __global__ void __launch_bounds__(NTG, 3) k_pairs(StepArgs a) {
             } else {
                 At = load_tc(a.stage, 0);
             }
-            kind = tc_pair_both(At, me, meF0, meF1, a, act, t, wq[threadIdx.x >> 5], lane, fpx,
-                                fpy, tp, fqx, fqy, tq);
+            kind = tc_pair_decide(At, me, meF0, meF1, a, act, t, wq[threadIdx.x >> 5], lane, tj);
+            contact = kind == RES_FORCE && tj.contact;
         }
+        int eq = -1;
         if (act) {
-            put_pair(a, e, kind, fpx, fpy, tp);
-            const int eq = partner_entry(a, t, s);
-            if (eq >= 0) put_pair(a, eq, kind, fqx, fqy, tq);
-            else atomicOr(a.err, ERR_NEAR_LIST);
+            eq = partner_entry(a, t, s);
+            if (eq < 0) atomicOr(a.err, ERR_NEAR_LIST);
+            if (kind != RES_FORCE) {
+                put_pair(a, e, kind, 0.0, 0.0, 0.0);
+                if (eq >= 0) put_pair(a, eq, kind, 0.0, 0.0, 0.0);
+            } else if (!SPLIT) {
+                double fpx, fpy, tp = 0.0, fqx, fqy, tq = 0.0;
+                if (BODY == 0)
+                    circ_pair_force(load_circ(a.stage, s), load_circ(a.stage, t), cj, fpx, fpy,
+                                    fqx, fqy);
+                else
+                    tc_pair_force(load_tc(a.stage, s), load_tc(a.stage, t), tj, fpx, fpy, tp, fqx,
+                                  fqy, tq);
+                put_pair(a, e, RES_FORCE, fpx, fpy, tp);
+                if (eq >= 0) put_pair(a, eq, RES_FORCE, fqx, fqy, tq);
+            }
+        }
+        if (SPLIT) {
+            // jobs in warp order: without contact at the front, with it at the back
+            const unsigned jm = __ballot_sync(FULL, act && kind == RES_FORCE && !contact);
+            const unsigned cm = __ballot_sync(FULL, act && kind == RES_FORCE && contact);
+            if (jm | cm) {
+                int j0 = 0, c0 = 0;
+                if (lane == 0) {
+                    if (jm) j0 = atomicAdd(a.work + 2, __popc(jm));
+                    if (cm) c0 = atomicAdd(a.work + 3, __popc(cm));
+                }
+                j0 = __shfl_sync(FULL, j0, 0);
+                c0 = __shfl_sync(FULL, c0, 0);
+                const unsigned below = (1u << lane) - 1u;
+                int rec = -1;
+                if ((jm >> lane) & 1u) rec = j0 + __popc(jm & below);
+                if ((cm >> lane) & 1u) rec = job_cap(a) - 1 - (c0 + __popc(cm & below));
+                if (rec >= 0) {
+                    if (BODY == 0) put_job(a, rec, s, t, e, eq, cj);
+                    else put_job(a, rec, s, t, e, eq, tj);
+                }
+            }
         }
     }
 }
 
+// The force pass: one lane per job of k_pairs, both sides' forces (and
+// torques) into the pair's two entries; the jobs without contact first.
+template <int BODY>
+__global__ void __launch_bounds__(NTG, 5) k_pair_forces(StepArgs a) {
+    pdl_enter();
+    if (a.nl_off[a.n] > a.nl_cap) return;
+    const int n_front = a.work[2], njobs = n_front + a.work[3];
+    for (int j = blockIdx.x * NTG + threadIdx.x; j < njobs; j += gridDim.x * NTG) {
+        const int rec = job_record(a, j, n_front);
+        double fpx, fpy, tp = 0.0, fqx, fqy, tq = 0.0;
+        int4 h;
+        if (BODY == 0) {
+            CircJob J;
+            h = get_job(a, rec, J);
+            circ_pair_force(load_circ(a.stage, h.x), load_circ(a.stage, h.y), J, fpx, fpy, fqx,
+                            fqy);
+        } else {
+            TcJob J;
+            h = get_job(a, rec, J);
+            tc_pair_force(load_tc(a.stage, h.x), load_tc(a.stage, h.y), J, fpx, fpy, tp, fqx, fqy,
+                          tq);
+        }
+        put_pair(a, h.z, RES_FORCE, fpx, fpy, tp);
+        if (h.w >= 0) put_pair(a, h.w, RES_FORCE, fqx, fqy, tq);
+    }
+}
+
 // Torque of slot s's side of the interacting pair (s, t) that exerts no
-// force: r x (+0, +0) with the exact moment arm r, as tc_pair_both computes
+// force: r x (+0, +0) with the exact moment arm r, as tc_pair_force computes
 // it for a pair with a force (the same distance search and arms).
 __device__ __noinline__ double tc_zero_force_torque(const StepArgs &a, int s, int t) {
     const int p = s < t ? s : t, q = s < t ? t : s;
@@ -3075,18 +3274,18 @@ void launch_scatter(const StepArgs &a, cudaStream_t s, bool after_kernel, int ga
 void launch_gather(const StepArgs &a, cudaStream_t s, int part, bool after_kernel) {
     if (a.n > 0) launch_k(after_kernel, k_gather, nblk(a.n, 128), 128, 0, s, a, part);
 }
-// Launch variants of the force kernel: (threads per block, staged candidates
-// per thread).
 // Force-kernel launch variants: the per-thread kernel (k_forces, lanes = 1)
 // with NT threads per block and CAP candidates staged per thread per pass,
 // the lane-group kernel (k_forces_group) with L lanes per agent, and the
-// compute-once pair pipeline (pairs = 1: near lists, k_pairs, gather) with
-// L lanes per agent.
+// compute-once pair pipeline (near lists, k_pairs, gather) with L lanes per
+// agent in the list build, its forces computed in k_pairs (pairs = 1) or in
+// the separate force pass k_pair_forces (pairs = 2).
 struct Variant { int nt, cap, lanes, pairs; };
 constexpr Variant kVariants[N_VARIANTS] = {
     {128, 64, 1, 0}, {64, 64, 1, 0}, {128, 32, 1, 0}, {64, 32, 1, 0}, {256, 32, 1, 0},
     {NTG, 0, 4, 0},  {NTG, 0, 8, 0}, {NTG, 0, 16, 0}, {NTG, 0, 32, 0},
-    {NTG, 0, 4, 1},  {NTG, 0, 8, 1}, {NTG, 0, 16, 1}};
+    {NTG, 0, 4, 1},  {NTG, 0, 8, 1}, {NTG, 0, 16, 1},
+    {NTG, 0, 4, 2},  {NTG, 0, 8, 2}, {NTG, 0, 16, 2}};
 
 size_t forces_smem_bytes(int body, int variant) {
     const Variant v = kVariants[variant];
@@ -3102,39 +3301,64 @@ typedef void (*ForcesFn)(StepArgs);
 constexpr ForcesFn kForces[2][N_VARIANTS] = {
     {k_forces<0, 128, 64>, k_forces<0, 64, 64>, k_forces<0, 128, 32>, k_forces<0, 64, 32>,
      k_forces<0, 256, 32>, k_forces_group<0, 4>, k_forces_group<0, 8>, k_forces_group<0, 16>,
-     k_forces_group<0, 32>, k_forces_gather<0>, k_forces_gather<0>, k_forces_gather<0>},
+     k_forces_group<0, 32>, k_forces_gather<0>, k_forces_gather<0>, k_forces_gather<0>,
+     k_forces_gather<0>, k_forces_gather<0>, k_forces_gather<0>},
     {k_forces<1, 128, 64>, k_forces<1, 64, 64>, k_forces<1, 128, 32>, k_forces<1, 64, 32>,
      k_forces<1, 256, 32>, k_forces_group<1, 4>, k_forces_group<1, 8>, k_forces_group<1, 16>,
-     k_forces_group<1, 32>, k_forces_gather<1>, k_forces_gather<1>, k_forces_gather<1>}};
+     k_forces_group<1, 32>, k_forces_gather<1>, k_forces_gather<1>, k_forces_gather<1>,
+     k_forces_gather<1>, k_forces_gather<1>, k_forces_gather<1>}};
 
 // Near-list and pair kernels of the pair-pipeline variants (by lanes 4, 8, 16).
 constexpr int N_PAIR_L = 3;
 constexpr ForcesFn kNlCount[N_PAIR_L] = {k_nl_count<4>, k_nl_count<8>, k_nl_count<16>};
 constexpr ForcesFn kNlFill[N_PAIR_L] = {k_nl_fill<4>, k_nl_fill<8>, k_nl_fill<16>};
-constexpr ForcesFn kPairs[2] = {k_pairs<0>, k_pairs<1>};
+constexpr ForcesFn kPairs[2][2] = {{k_pairs<0, false>, k_pairs<0, true>},
+                                    {k_pairs<1, false>, k_pairs<1, true>}};
+constexpr ForcesFn kPairForces[2] = {k_pair_forces<0>, k_pair_forces<1>};
 constexpr ForcesFn kPairsLight[2] = {k_pairs_light<0>, k_pairs_light<1>};
 constexpr ForcesFn kFallback[2][N_PAIR_L] = {
     {k_forces_fallback<0, 4>, k_forces_fallback<0, 8>, k_forces_fallback<0, 16>},
     {k_forces_fallback<1, 4>, k_forces_fallback<1, 8>, k_forces_fallback<1, 16>}};
 inline int pair_l_index(int lanes) { return lanes == 4 ? 0 : (lanes == 8 ? 1 : 2); }
+// The lane-group variant with a pair-pipeline variant's lanes (4, 8, 16).
+inline int group_twin(int variant) { return 5 + pair_l_index(kVariants[variant].lanes); }
 
 bool variant_pairs(int variant) {
     return variant >= 0 && variant < N_VARIANTS && kVariants[variant].pairs != 0;
 }
 
-// Variant a new context starts with: lanes per agent such that the warps
-// cover the SMs several times over, and the pair pipeline from 8k agents
-// (measured on hallway, room and field workloads of 400 to 100k agents).
-int default_variant(long long n) {
-    if (n < 1000) return 8;          // lane groups, 32 lanes per agent
-    if (n < 8000) return 7;          // lane groups, 16
-    return 10;                       // pair pipeline (8 lanes per agent in the list build)
+// Variant a new context starts with, from its agent count and body type
+// (autotune.py refines it per workload).  Measured whole steps (ms) on GB300,
+// lane groups of 16 / 32 against the pair pipeline with 16 / 8 list-build
+// lanes and forces in k_pairs: Circular hallways of 400 agents 0.054 / 0.045
+// against 0.065 / 0.067, 2000 agents 0.153 / 0.162 against 0.140 / 0.146,
+// 5000 agents 0.276 / 0.312 against 0.176 / 0.182, 20000 agents 0.99 / 1.16
+// against 0.294 / 0.295; the 2000-agent ThreeCircle room 0.237 / 0.247
+// against 0.147 / 0.152.  Near the crossing it depends on the density: lane
+// groups of 32 against the pipeline with 16 lanes, 1000 agents 0.062 against
+// 0.079 (hallway, 1.3 per m^2) and 0.146 against 0.144 (room, 2.2 per m^2),
+// 1300-1400 agents 0.075 against 0.079 and 0.201 against 0.147.  The force
+// pass (variants 12-14 against 9-11, 4 / 8 / 16 list-build lanes): Circular
+// 100k agents 0.347 / 0.340 / 0.369 against 0.351 / 0.344 / 0.373, 20k
+// 0.302 / 0.270 / 0.270 against 0.330 / 0.298 / 0.298, 5000 0.180 / 0.163 /
+// 0.157 against 0.201 / 0.181 / 0.176; ThreeCircle 100k field 0.337 / 0.340 /
+// 0.366 against 0.333 / 0.335 / 0.362, 2000-agent room 0.164 / 0.150 / 0.145
+// against 0.165 / 0.151 / 0.147, 4000 agents in contact 0.185 / 0.171 /
+// 0.166 against 0.172 / 0.157 / 0.153.
+int default_variant(long long n, int body) {
+    if (n < 1200) return 8;                  // lane groups, 32 lanes per agent
+    if (body == 0) return n < 16000 ? 14 : 13;   // Circular: the separate force pass
+    return n < 16000 ? 11 : 9;               // ThreeCircle: forces in k_pairs
 }
 
 // The same without the pair pipeline (contexts without near-list memory).
-int default_group_variant(long long n) {
-    const int v = default_variant(n);
-    return kVariants[v].pairs ? v - 4 : v;
+int default_group_variant(long long n, int body) {
+    const int v = default_variant(n, body);
+    return kVariants[v].pairs ? group_twin(v) : v;
+}
+
+bool variant_split(int variant) {
+    return variant >= 0 && variant < N_VARIANTS && kVariants[variant].pairs == 2;
 }
 
 int variant_lanes(int variant) {
@@ -3149,8 +3373,9 @@ int variant_staged(int variant) {
 
 // Resident blocks of each force kernel variant (and pair kernel) on each device.
 int g_forces_blocks[64][2][N_VARIANTS];
-int g_pairs_blocks[64][2][N_PAIR_L];
+int g_pairs_blocks[64][2][2];             // [device][body][split]
 int g_light_blocks[64][2];
+int g_job_blocks[64][2];
 
 int init_kernels() {
     int dev = 0, sms = 0;
@@ -3169,27 +3394,33 @@ int init_kernels() {
                 g_forces_blocks[dev][body][v] = (nb > 0 ? nb : 1) * sms;
         }
     for (int body = 0; body < 2 && e == cudaSuccess; ++body)
-        for (int l = 0; l < N_PAIR_L && e == cudaSuccess; ++l) {
+        for (int l = 0; l < N_PAIR_L && e == cudaSuccess; ++l)
             // the fallback kernel shares the lane-group variant's shared memory
             e = cudaFuncSetAttribute(kFallback[body][l],
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)forces_smem_bytes(body, 5 + l));
-            if (e == cudaSuccess)
-                e = cudaFuncSetAttribute(kPairs[body],
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)pairs_smem_bytes(body));
+    for (int body = 0; body < 2 && e == cudaSuccess; ++body)
+        for (int sp = 0; sp < 2 && e == cudaSuccess; ++sp) {
+            e = cudaFuncSetAttribute(kPairs[body][sp],
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)pairs_smem_bytes(body));
             int nb = 0;
             if (e == cudaSuccess)
-                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kPairs[body], NTG,
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kPairs[body][sp], NTG,
                                                                   pairs_smem_bytes(body));
             if (e == cudaSuccess && dev >= 0 && dev < 64)
-                g_pairs_blocks[dev][body][l] = (nb > 0 ? nb : 1) * sms;
+                g_pairs_blocks[dev][body][sp] = (nb > 0 ? nb : 1) * sms;
         }
     for (int body = 0; body < 2 && e == cudaSuccess; ++body) {
         int nb = 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kPairsLight[body], NTG, 0);
         if (e == cudaSuccess && dev >= 0 && dev < 64)
             g_light_blocks[dev][body] = (nb > 0 ? nb : 1) * sms;
+        nb = 0;
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kPairForces[body], NTG, 0);
+        if (e == cudaSuccess && dev >= 0 && dev < 64)
+            g_job_blocks[dev][body] = (nb > 0 ? nb : 1) * sms;
     }
     return e == cudaSuccess ? 0 : (int)e;
 }
@@ -3205,7 +3436,7 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
     if (a.n <= 0) return;
     if (variant < 0 || variant >= N_VARIANTS) variant = 0;
     // the pair pipeline needs the near-list buffers: otherwise its lane-group twin
-    if (kVariants[variant].pairs && !a.nl_cnt) variant -= 4;
+    if (kVariants[variant].pairs && !a.nl_cnt) variant = group_twin(variant);
     const Variant v = kVariants[variant];
     int dev = 0;
     cudaGetDevice(&dev);
@@ -3236,7 +3467,8 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
         kNlCount[l]<<<nb, NTG, 0, s>>>(a);
         launch_near_scans(a, s);
         launch_k(true, kNlFill[l], nb, NTG, 0, s, a);
-        int rp = (dev >= 0 && dev < 64) ? g_pairs_blocks[dev][body][l] : 0;
+        const int sp = v.pairs == 2 ? 1 : 0;
+        int rp = (dev >= 0 && dev < 64) ? g_pairs_blocks[dev][body][sp] : 0;
         if (rp <= 0) rp = 152;
         // at most one warp per 32 pairs (about 16 pairs per agent): enough blocks
         if (pro && stage_deferred && fork) cudaStreamWaitEvent(s, fork->join_stage, 0);
@@ -3249,8 +3481,15 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
                 cudaEventRecordWithFlags(pair_ev[1], s, captured ? cudaEventRecordExternal : 0);
         }
         // after k_pairs_light: chained to it (unless an event sits between)
-        launch_k(a.defer_list != nullptr && !pair_ev, kPairs[body],
+        launch_k(a.defer_list != nullptr && !pair_ev, kPairs[body][sp],
                  std::min(nblk((long long)a.n * 16, NTG), rp), NTG, pairs_smem_bytes(body), s, a);
+        if (sp) {
+            // the force pass over the jobs (their count is known on the device only)
+            int rj = (dev >= 0 && dev < 64) ? g_job_blocks[dev][body] : 0;
+            if (rj <= 0) rj = 152;
+            launch_k(true, kPairForces[body], std::min(nblk((long long)a.n * 16, NTG), rj), NTG,
+                     0, s, a);
+        }
         if (pair_ev) cudaEventRecordWithFlags(pair_ev[2], s, captured ? cudaEventRecordExternal : 0);
     }
     int resident = (dev >= 0 && dev < 64) ? g_forces_blocks[dev][body][variant] : 0;
@@ -3266,7 +3505,7 @@ void launch_forces(const StepArgs &a, cudaStream_t s, int variant, const cudaEve
     if (pro && fork) cudaStreamWaitEvent(s, fork->join, 0);
     kForces[body][variant]<<<blocks, nt, forces_smem_bytes(body, variant), s>>>(a);
     if (v.pairs && (a.nodes & N_AGENT)) {
-        const int gv = variant - 4;                       // the lane-group twin
+        const int gv = group_twin(variant);
         int rg = (dev >= 0 && dev < 64) ? g_forces_blocks[dev][body][gv] : 0;
         if (rg <= 0) rg = 152;
         launch_k(true, kFallback[body][pair_l_index(v.lanes)],
@@ -3288,6 +3527,10 @@ void launch_near_lists(const StepArgs &a, cudaStream_t s) {
     kNlCount[1]<<<nb, NTG, 0, s>>>(a);
     launch_near_scans(a, s);
     launch_k(true, kNlFill[1], nb, NTG, 0, s, a);
+}
+void launch_adj_light(const StepArgs &a, cudaStream_t s) {
+    if (a.n <= 0 || !a.nl_cnt || a.body != 0) return;
+    k_pairs_light<0, true><<<nblk((long long)a.n * 16, NTG), NTG, 0, s>>>(a);
 }
 
 void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s) {

@@ -271,7 +271,8 @@ int cd_kernel_time(cd_ctx *ctx, double *force_ms, int64_t *force_launches,
  * cd_kernel_time (timing mode 1). */
 int cd_pair_kernel_time(cd_ctx *ctx, double *ms, int64_t *launches);
 /* The same split into the float32 pair pass (k_pairs_light) and the float64
- * pair kernel (k_pairs); light_ms is 0 without a float32 pass. */
+ * pair kernels (k_pairs, and k_pair_forces for pair_pipeline 2); light_ms is
+ * 0 without a float32 pass. */
 int cd_pair_kernel_times(cd_ctx *ctx, double *light_ms, double *pairs_ms, int64_t *launches);
 /* The last pair-pipeline step's flat pair list: its pairs, those in its
  * first part (guessed to need the social force) and, for ThreeCircle
@@ -284,9 +285,10 @@ int cd_kernels_per_step(const cd_ctx *ctx, int nodes, int64_t *kernels);
 /* Launch variants of the agent-force kernel: threads per block, candidates
  * staged per thread per pass (lanes_per_agent == 1: one lane per agent) or
  * lanes that share one agent (lanes_per_agent > 1, staged_per_thread 0), and
- * whether the variant is the compute-once pair pipeline (pair_pipeline 1:
- * every unordered pair evaluated once into per-agent near lists, then summed
- * per agent in visiting order; the lists' device memory is allocated on
+ * whether the variant is the compute-once pair pipeline (pair_pipeline 1 or
+ * 2: every unordered pair evaluated once into per-agent near lists, then
+ * summed per agent in visiting order; 2 computes the forces of the pairs
+ * that have one in a separate pass; the lists' device memory is allocated on
  * first use and grown after a step that needed more, that step falling back
  * to the lane-group kernel).  Every variant gives bit-identical results;
  * only the speed differs, so an autotuner may pick one per context (the

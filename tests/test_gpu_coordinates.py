@@ -48,7 +48,7 @@ CASES = {
 
 
 @pytest.mark.parametrize('name', sorted(CASES))
-@pytest.mark.parametrize('variant', range(12))
+@pytest.mark.parametrize('variant', range(15))
 def test_utm_full_step_every_variant(oracle, native, name, variant):
     scen = CASES[name]()
     noise = S.draw_noise(scen.agents, np.random.default_rng(21))

@@ -129,12 +129,13 @@ def test_full_step(oracle, native, name):
 
 
 @pytest.mark.parametrize('name', sorted(SCENARIOS))
-@pytest.mark.parametrize('variant', range(12))
+@pytest.mark.parametrize('variant', range(15))
 def test_full_step_every_variant(oracle, native, name, variant):
     """Each force-kernel launch variant (one lane per agent, 4 to 32 lanes
-    sharing an agent, or the compute-once pair pipeline) reproduces the
-    oracle's step bit for bit."""
-    assert len(N.variants()) == 12
+    sharing an agent, or the compute-once pair pipeline with its forces in
+    the pair kernel or in a separate force pass) reproduces the oracle's step
+    bit for bit."""
+    assert len(N.variants()) == 15
     scen = SCENARIOS[name]()
     noise = S.draw_noise(scen.agents, np.random.default_rng(12))
     got, dt_g = device_step(scen, N.NODE_ALL, noise, variant=variant)
@@ -442,7 +443,7 @@ def edge_pairs(seed=17):
     return S.Scenario('edge_pairs', a, S.walls_array([]), bounds, 3.6)
 
 
-@pytest.mark.parametrize('variant', [9, 10, 11])
+@pytest.mark.parametrize('variant', [9, 10, 11, 12, 14])
 def test_certificate_edges(oracle, native, variant):
     """The pair kernel's float32 certificates (distance bounds, pre-selection,
     no time to collision) at their edges: one full step bit for bit."""
@@ -485,11 +486,14 @@ def crowded(seed, speed=1.0):
     return scen
 
 
+@pytest.mark.parametrize('variant', [10, 13])
 @pytest.mark.parametrize('case', [('room', 1, 0.1), ('room', 2, 1.0), ('room', 3, 3.0),
                                   ('crowded', 4, 0.3), ('crowded', 5, 1.0), ('crowded', 6, 2.5)])
-def test_pair_pipeline_random_sweep(oracle, native, case):
+def test_pair_pipeline_random_sweep(oracle, native, case, variant):
     """Random states for the pair pipeline's float32 decisions: moving rooms at
-    several speed scales and dense, overlapping fields; three steps bit for bit."""
+    several speed scales and dense, overlapping fields (contacts: the force
+    pass's jobs with contact apart from the others); three steps bit for bit,
+    with the forces in the pair kernel and in the separate force pass."""
     kind, seed, speed = case
     if kind == 'room':
         scen = S.room(n=1500, size=25.0, seed=seed)
@@ -499,7 +503,7 @@ def test_pair_pipeline_random_sweep(oracle, native, case):
         scen = crowded(seed, speed)
     nodes = N.NODE_ALL & ~N.NODE_FLUCTUATION
     b, agents, _ = batch_from_scenarios([scen])
-    b.set_variant(10)
+    b.set_variant(variant)
     b.run(3, nodes)
     got = agents.copy()
     b.download(got)
@@ -617,7 +621,7 @@ def circular_edge_pairs(seed=31, n_pairs=1500, center=(0.0, 0.0)):
     return S.Scenario('circular_edge_pairs', a, S.walls_array([]), bounds, 3.7)
 
 
-@pytest.mark.parametrize('variant', [9, 10, 11])
+@pytest.mark.parametrize('variant', [9, 10, 11, 12, 14])
 @pytest.mark.parametrize('where', ['origin', 'utm'])
 def test_circular_certificate_edges(oracle, native, variant, where):
     """circ_pair_light's certificates at their edges, near the origin and at
