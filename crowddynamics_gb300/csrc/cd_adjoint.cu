@@ -94,6 +94,8 @@ __device__ __forceinline__ void contact_vjp(double xx, double xy, double d0, dou
 // Seed of the untruncated force from the seed u of truncate(F, 2000 N)
 // (vector2D.py:166-187): u itself, or (s)(I - f f^T) u above the limit.
 __device__ __forceinline__ void truncate_vjp(double Fx, double Fy, double &ux, double &uy) {
+    // certainly below the limit (as truncate2 decides it): the identity
+    if (Fx * Fx + Fy * Fy < 0.99 * (F_SOC_MAX * F_SOC_MAX)) return;
     const double L = cdm_hypot(Fx, Fy);
     if (L > F_SOC_MAX) {
         const double iL = 1.0 / L;

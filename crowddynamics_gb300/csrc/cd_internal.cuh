@@ -15,9 +15,9 @@ enum Col {
 };
 
 // Staged neighbour records (cell-sorted order), in double2 units.
-constexpr int STAGE_Q_CIRC = 6;    // (x,y)(vx,vy)(r,m)(k,tau0)(mu,kappa)(damp,-)
+constexpr int STAGE_Q_CIRC = 6;    // (x,y)(vx,vy)(r,m)(k,tau0)(mu,kappa)(damp,1/tau0)
 constexpr int STAGE_Q_TC = 10;     // (x,y)(xls,yls)(xrs,yrs)(vx,vy)(rt,rs)
-                                   // (rts,m)(k,tau0)(mu,kappa)(damp,sin)(cos,-)
+                                   // (rts,m)(k,tau0)(mu,kappa)(damp,sin)(cos,1/tau0)
 constexpr int WALL_D = 8;          // p0x p0y p1x p1y tx ty lw -
 
 // Device error bits (StepArgs::err).

@@ -66,8 +66,13 @@ __device__ __forceinline__ double np_sign(double x) {
     return x > 0 ? 1.0 : (x < 0 ? -1.0 : x);
 }
 
-// truncate, core/vector2D.py:166-187
+// truncate, core/vector2D.py:166-187.  A vector whose float64 squared
+// length is below 0.99 l^2 is certainly shorter than l (the sum of two
+// rounded squares is within 3 units in the last place of |v|^2), so the
+// exact test would leave it as it is: it is returned without the hypot.
+// NaN, infinite and overflowing squares take the exact test.
 __device__ __forceinline__ void truncate2(double &vx, double &vy, double l) {
+    if (vx * vx + vy * vy < 0.99 * (l * l)) return;
     double vlen = cdm_hypot(vx, vy);
     if (vlen > l) {
         double s = l / vlen;
@@ -76,9 +81,10 @@ __device__ __forceinline__ void truncate2(double &vx, double &vy, double l) {
     }
 }
 
-// magnitude, core/motion/power_law.py:83-102
-__device__ __forceinline__ double magnitude(double tau, double tau_0) {
-    return (2.0 / tau + 1.0 / tau_0) * cdm_exp(-tau / tau_0) / (tau * tau);
+// magnitude, core/motion/power_law.py:83-102, with 1 / tau_0 (itau_0) the
+// staged records' IEEE quotient: the same value, divided once per agent
+__device__ __forceinline__ double magnitude(double tau, double tau_0, double itau_0) {
+    return (2.0 / tau + itau_0) * cdm_exp(-tau / tau_0) / (tau * tau);
 }
 
 // force_contact, core/motion/contact.py:12-48; t = rotate270(n) = (n.y, -n.x)
@@ -108,12 +114,12 @@ __device__ __forceinline__ int axis_cell(double v, double v0, double cell, int n
 // ---- staged agent records ----------------------------------------------
 
 struct Circ {
-    double x, y, vx, vy, r, m, k, tau0, mu, kappa, damp;
+    double x, y, vx, vy, r, m, k, tau0, mu, kappa, damp, itau0;   // itau0 = 1.0 / tau0
 };
 
 struct TC {
     double x[3], y[3];          // torso, left shoulder, right shoulder
-    double vx, vy, rt, rs, rts, m, k, tau0, mu, kappa, damp, sn, cs;
+    double vx, vy, rt, rs, rts, m, k, tau0, mu, kappa, damp, sn, cs, itau0;   // itau0 = 1 / tau0
 };
 
 // Register-friendly selection of part k (0 torso, 1 left, 2 right).
@@ -127,7 +133,7 @@ __device__ __forceinline__ Circ load_circ(const double2 *__restrict__ st, int sl
             q4 = __ldg(p + 4), q5 = __ldg(p + 5);
     Circ a;
     a.x = q0.x; a.y = q0.y; a.vx = q1.x; a.vy = q1.y; a.r = q2.x; a.m = q2.y;
-    a.k = q3.x; a.tau0 = q3.y; a.mu = q4.x; a.kappa = q4.y; a.damp = q5.x;
+    a.k = q3.x; a.tau0 = q3.y; a.mu = q4.x; a.kappa = q4.y; a.damp = q5.x; a.itau0 = q5.y;
     return a;
 }
 
@@ -141,6 +147,7 @@ __device__ __forceinline__ TC load_tc(const double2 *__restrict__ st, int slot) 
     a.vx = q3.x; a.vy = q3.y; a.rt = q4.x; a.rs = q4.y; a.rts = q5.x; a.m = q5.y;
     a.k = q6.x; a.tau0 = q6.y; a.mu = q7.x; a.kappa = q7.y; a.damp = q8.x; a.sn = q8.y;
     a.cs = q9.x;
+    a.itau0 = q9.y;
     return a;
 }
 
@@ -617,7 +624,7 @@ __device__ __forceinline__ void gather_agent(const StepArgs &a, const int i, con
             p[2] = make_double2(c[R][i], c[MASS][i]);
             p[3] = make_double2(c[K_SOC][i], c[TAU0][i]);
             p[4] = make_double2(c[MU][i], c[KAPPA][i]);
-            p[5] = make_double2(c[DAMP][i], 0.0);
+            p[5] = make_double2(c[DAMP][i], 1.0 / c[TAU0][i]);
         }
         if (part != 2) {
             const double xr = c[X][i] - ox, yr = c[Y][i] - oy;
@@ -644,7 +651,7 @@ __device__ __forceinline__ void gather_agent(const StepArgs &a, const int i, con
             double sn, cs;
             cdm_sincos(c[PHI][i], &sn, &cs);
             p[8] = make_double2(c[DAMP][i], sn);
-            p[9] = make_double2(cs, 0.0);
+            p[9] = make_double2(cs, 1.0 / c[TAU0][i]);
         }
         if (part == 2) return;
         // position relative to the grid origin = float hi + float lo;
@@ -792,7 +799,7 @@ __device__ __forceinline__ bool pair_circular_eval(const Circ &A, const Circ &B,
             double gx = (vrx - (vrx * b + xx * a) / dd) / a;
             double gy = (vry - (vry * b + xy * a) / dd) / a;
             double cm = (-A.m) * A.k;
-            double mag = magnitude(tau, A.tau0);
+            double mag = magnitude(tau, A.tau0, A.itau0);
             Fx = (cm * gx) * mag;
             Fy = (cm * gy) * mag;
             truncate2(Fx, Fy, F_SOC_MAX);
@@ -881,10 +888,10 @@ __device__ __forceinline__ void circ_pair_force(const Circ &A, const Circ &B, co
         double gy = (vry - (vry * b + xy * a) / dd) / a;
         double cmp = (-A.m) * A.k, cmq = (-B.m) * B.k;
         double two_t = 2.0 / tau, tt = tau * tau;       // shared terms of magnitude()
-        double magp = (two_t + 1.0 / A.tau0) * cdm_exp(-tau / A.tau0) / tt;
+        double magp = (two_t + A.itau0) * cdm_exp(-tau / A.tau0) / tt;
         // magnitude() depends on (tau, tau_0) only: equal tau_0, equal value
         double magq = B.tau0 == A.tau0 ? magp
-                                       : (two_t + 1.0 / B.tau0) * cdm_exp(-tau / B.tau0) / tt;
+                                       : (two_t + B.itau0) * cdm_exp(-tau / B.tau0) / tt;
         FPx = (cmp * gx) * magp;
         FPy = (cmp * gy) * magp;
         truncate2(FPx, FPy, F_SOC_MAX);
@@ -1103,7 +1110,7 @@ __device__ __forceinline__ bool tc_pair_eval(const TC &A, const float4 meC, cons
         double gx = (vrx - (av * (xr + 2 * ox) + b_min * vrx) / d_min) / av;
         double gy = (vry - (av * (yr + 2 * oy) + b_min * vry) / d_min) / av;
         double cm = (-A.m) * A.k;
-        double mag = magnitude(tau, A.tau0);
+        double mag = magnitude(tau, A.tau0, A.itau0);
         Fx = (cm * gx) * mag;
         Fy = (cm * gy) * mag;
         truncate2(Fx, Fy, F_SOC_MAX);
@@ -1551,10 +1558,10 @@ __device__ __forceinline__ void tc_pair_force(const TC &A, const TC &B, const Tc
         double gy = (vry - (av * (yr + 2 * oy) + b_min * vry) / d_min) / av;
         double cmp = (-A.m) * A.k, cmq = (-B.m) * B.k;
         double two_t = 2.0 / tau, tt = tau * tau;            // shared terms of magnitude()
-        double magp = (two_t + 1.0 / A.tau0) * cdm_exp(-tau / A.tau0) / tt;
+        double magp = (two_t + A.itau0) * cdm_exp(-tau / A.tau0) / tt;
         // magnitude() depends on (tau, tau_0) only: equal tau_0, equal value
         double magq = B.tau0 == A.tau0 ? magp
-                                       : (two_t + 1.0 / B.tau0) * cdm_exp(-tau / B.tau0) / tt;
+                                       : (two_t + B.itau0) * cdm_exp(-tau / B.tau0) / tt;
         FPx = (cmp * gx) * magp;
         FPy = (cmp * gy) * magp;
         truncate2(FPx, FPy, F_SOC_MAX);
