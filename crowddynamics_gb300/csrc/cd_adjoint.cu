@@ -42,6 +42,30 @@ struct Circ {
     double x, y, vx, vy, r, m, k, tau0, mu, kappa, damp;
 };
 
+// Last-block-done: every block has written its partial (made visible by the
+// fence) before it counts itself; the block that counts last returns true
+// and resets the counter for the next kernel.
+__device__ __forceinline__ bool last_block(int *blocks_done) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        last = atomicAdd(blocks_done, 1) == (int)gridDim.x - 1;
+        if (last) *blocks_done = 0;
+    }
+    __syncthreads();
+    return last;
+}
+
+// Sum of nb partials by warp 0 in a fixed order (lane-strided sums, then a
+// butterfly): deterministic for a given nb; every lane of warp 0 holds it.
+__device__ __forceinline__ double ordered_sum(const double *partial, int nb) {
+    double s = 0.0;
+    for (int k = threadIdx.x; k < nb; k += 32) s += __ldcg(partial + k);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    return s;
+}
+
 __device__ __forceinline__ Circ load_circ(const double2 *__restrict__ st, int slot) {
     const double2 *p = st + (size_t)slot * STAGE_Q_CIRC;
     double2 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2), q3 = __ldg(p + 3),
@@ -262,20 +286,19 @@ __global__ void k_adj_seed(AdjArgs q) {
         __syncthreads();
     }
     if (threadIdx.x == 0) q.partial[blockIdx.x] = red[0];
+    // the last block: the dt adjoint, the partials summed in a fixed order
+    if (last_block(q.blocks_done) && threadIdx.x < 32) {
+        const double t = ordered_sum(q.partial, gridDim.x);
+        if (threadIdx.x == 0) *q.ldt = t;
+    }
 }
 
-// Sum of block partials in index order (one thread: deterministic).
-__global__ void k_adj_sum(const double *partial, int nb, double *out, double scale, int accumulate) {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    double s = 0.0;
-    for (int k = 0; k < nb; ++k) s += partial[k];
-    if (accumulate) *out += s * scale;
-    else *out = s * scale;
-}
-
-// Loss partials: sum_i |x_i - target_i|^2 per block.
-__global__ void k_loss_partial(const double *x, const double *y, const double *target, int n,
-                               double *partial) {
+// loss += scale * sum_i |x_i - target_i|^2: per block partials, summed by
+// the last block in a fixed order; block 0 also copies the step's dt.
+__global__ void k_loss(const double *x, const double *y, const double *target, int n,
+                       double *partial, double *loss, double scale, int *blocks_done,
+                       const double *dt_src, double *dt_dst) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && dt_dst) *dt_dst = *dt_src;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     double s = 0.0;
     if (i < n) {
@@ -290,6 +313,10 @@ __global__ void k_loss_partial(const double *x, const double *y, const double *t
         __syncthreads();
     }
     if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+    if (last_block(blocks_done) && threadIdx.x < 32) {
+        const double t = ordered_sum(partial, gridDim.x);
+        if (threadIdx.x == 0) *loss += t * scale;
+    }
 }
 
 // lx += scale * 2 (x - target)
@@ -509,14 +536,44 @@ __device__ __forceinline__ void better(double &v, int &j, double v2, int j2) {
     if (j2 >= 0 && (v2 > v || (v2 == v && (j < 0 || j2 < j)))) { v = v2; j = j2; }
 }
 
+// The timestep's own gradient, when dt was not clamped:
+// dt = 1.1 V0 dt_max / Vm  ->  d/dV0 = dt / V0,  d/dVm = -dt / Vm.
+// Warp 0 of k_adj_argmax's last block: the blocks' maxima combined (the
+// largest value, on ties the first index: the same whatever the order).
+__device__ __forceinline__ void adj_dt(const AdjArgs &q, double dt_min, double dt_max,
+                                       const double *vx, const double *vy) {
+    const int lane = threadIdx.x & 31;
+    double Vm = 0.0, V0 = -INFINITY;
+    int jv = -1, j0 = -1;
+    for (int b = lane; b < (int)gridDim.x; b += 32) {
+        better(Vm, jv, __ldcg(q.argmax_vals + 2 * b), __ldcg(q.argmax_idx + 2 * b));
+        better(V0, j0, __ldcg(q.argmax_vals + 2 * b + 1), __ldcg(q.argmax_idx + 2 * b + 1));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        better(Vm, jv, __shfl_xor_sync(0xffffffffu, Vm, o), __shfl_xor_sync(0xffffffffu, jv, o));
+        better(V0, j0, __shfl_xor_sync(0xffffffffu, V0, o), __shfl_xor_sync(0xffffffffu, j0, o));
+    }
+    if (lane != 0) return;
+    const double dt = *q.dt, ldt = *q.ldt;
+    if (!(Vm > 0) || !(dt > dt_min && dt < dt_max)) return;
+    if (j0 >= 0) q.grad[4 * j0 + 1] += ldt * dt / V0;
+    if (jv >= 0) {
+        double c = ldt * (-dt / Vm) / Vm;
+        q.lv_out[2 * jv] += c * vx[jv];
+        q.lv_out[2 * jv + 1] += c * vy[jv];
+    }
+}
+
 // Per block: max |v| (positive values only) and max v0 with their first
-// indices, written to vals / idx [2 * block + {0, 1}]; k_adj_dt combines the
-// blocks.  |v| = hypot(vx, vy) only where q = vx^2 + vy^2 can hold the
+// indices, written to vals / idx [2 * block + {0, 1}]; the last block
+// combines the blocks (adj_dt).  |v| = hypot(vx, vy) only where q = vx^2 + vy^2 can hold the
 // block's maximum: q is within 4 ulp of |v|^2, so a lane 2^-40 below the
 // block's largest q has a |v| smaller by far more than hypot's 2 ulp
 // (non-finite q, and blocks whose largest q is tiny, take hypot everywhere).
-__global__ void k_adj_argmax(const double *vx, const double *vy, const double *v0, int n,
-                             double *vals, int *idx) {
+__global__ void k_adj_argmax(AdjArgs aq, double dt_min, double dt_max, const double *vx,
+                             const double *vy, const double *v0, int n) {
+    double *vals = aq.argmax_vals;
+    int *idx = aq.argmax_idx;
     __shared__ double sq[RED_NT / 32], sv[RED_NT / 32], s0[RED_NT / 32];
     __shared__ int jv_s[RED_NT / 32], j0_s[RED_NT / 32];
     const int i = blockIdx.x * RED_NT + threadIdx.x, w = threadIdx.x >> 5;
@@ -557,28 +614,7 @@ __global__ void k_adj_argmax(const double *vx, const double *vy, const double *v
         vals[2 * blockIdx.x] = mv; vals[2 * blockIdx.x + 1] = m0;
         idx[2 * blockIdx.x] = jv; idx[2 * blockIdx.x + 1] = j0;
     }
-}
-
-// The timestep's own gradient, when dt was not clamped:
-// dt = 1.1 V0 dt_max / Vm  ->  d/dV0 = dt / V0,  d/dVm = -dt / Vm.
-__global__ void k_adj_dt(AdjArgs q, double dt_min, double dt_max, const double *vx,
-                         const double *vy, int blocks) {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    const double dt = *q.dt, ldt = *q.ldt;
-    // the blocks of k_adj_argmax in order: the maxima with their first indices
-    double Vm = 0.0, V0 = -INFINITY;
-    int jv = -1, j0 = -1;
-    for (int b = 0; b < blocks; ++b) {
-        better(Vm, jv, q.argmax_vals[2 * b], q.argmax_idx[2 * b]);
-        better(V0, j0, q.argmax_vals[2 * b + 1], q.argmax_idx[2 * b + 1]);
-    }
-    if (!(Vm > 0) || !(dt > dt_min && dt < dt_max)) return;
-    if (j0 >= 0) q.grad[4 * j0 + 1] += ldt * dt / V0;
-    if (jv >= 0) {
-        double c = ldt * (-dt / Vm) / Vm;
-        q.lv_out[2 * jv] += c * vx[jv];
-        q.lv_out[2 * jv + 1] += c * vy[jv];
-    }
+    if (last_block(aq.blocks_done) && threadIdx.x < 32) adj_dt(aq, dt_min, dt_max, vx, vy);
 }
 
 inline int nblk(long long n, int nt) { return (int)((n + nt - 1) / nt); }
@@ -588,9 +624,7 @@ inline int nblk(long long n, int nt) { return (int)((n + nt - 1) / nt); }
 int adj_partials(int n) { return nblk(n, RED_NT) > 0 ? nblk(n, RED_NT) : 1; }
 
 void launch_adj_seed(const AdjArgs &q, cudaStream_t s) {
-    int nb = adj_partials(q.n);
-    k_adj_seed<<<nb, RED_NT, 0, s>>>(q);
-    k_adj_sum<<<1, 1, 0, s>>>(q.partial, nb, q.ldt, 1.0, 0);
+    k_adj_seed<<<adj_partials(q.n), RED_NT, 0, s>>>(q);
 }
 void launch_adj_forces(const StepArgs &a, const AdjArgs &q, cudaStream_t s) {
     if (a.n <= 0) return;
@@ -623,15 +657,13 @@ void launch_copy_cols(const double *const *src, double *const *dst, int ncol, in
 }
 void launch_adj_dt(const AdjArgs &q, double dt_min, double dt_max, const double *vx,
                    const double *vy, const double *v0, cudaStream_t s) {
-    const int nb = adj_partials(q.n);
-    k_adj_argmax<<<nb, RED_NT, 0, s>>>(vx, vy, v0, q.n, q.argmax_vals, q.argmax_idx);
-    k_adj_dt<<<1, 1, 0, s>>>(q, dt_min, dt_max, vx, vy, nb);
+    k_adj_argmax<<<adj_partials(q.n), RED_NT, 0, s>>>(q, dt_min, dt_max, vx, vy, v0, q.n);
 }
 void launch_loss(const double *x, const double *y, const double *target, int n, double *partial,
-                 double *loss, double scale, cudaStream_t s) {
-    int nb = adj_partials(n);
-    k_loss_partial<<<nb, RED_NT, 0, s>>>(x, y, target, n, partial);
-    k_adj_sum<<<1, 1, 0, s>>>(partial, nb, loss, scale, 1);
+                 double *loss, double scale, int *blocks_done, const double *dt_src,
+                 double *dt_dst, cudaStream_t s) {
+    k_loss<<<adj_partials(n), RED_NT, 0, s>>>(x, y, target, n, partial, loss, scale, blocks_done,
+                                              dt_src, dt_dst);
 }
 void launch_loss_grad(const double *x, const double *y, const double *target, int n,
                       double scale, double *lx, cudaStream_t s) {

@@ -1514,6 +1514,7 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
     double *dts = mem.get<double>(c, steps, rc);
     double *partial = mem.get<double>(c, cdk::adj_partials((int)n), rc);
     double *scal = mem.get<double>(c, 4, rc);           // loss, ldt, saved dt, saved time
+    int *blocks_done = mem.get<int>(c, 1, rc);          // the reductions' last-block counter
     double *adj = grads ? mem.get<double>(c, 16 * n + 4 * n, rc) : nullptr;
     // per block of the argmax: (max |v|, max v0) and their first indices
     int *amax = grads ? mem.get<int>(c, 2 * cdk::adj_partials((int)n), rc) : nullptr;
@@ -1523,6 +1524,7 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
     CUDA_OR_FAIL(c, cudaMemcpyAsync(tgt, target, sizeof(double) * steps * 2 * n,
                                     cudaMemcpyHostToDevice, st));
     CUDA_OR_FAIL(c, cudaMemsetAsync(scal, 0, sizeof(double) * 4, st));
+    CUDA_OR_FAIL(c, cudaMemsetAsync(blocks_done, 0, sizeof(int), st));
     const double scale = 1.0 / ((double)steps * (double)std::max<int64_t>(n, 1));
     cudaEvent_t e0, e1, e2;
     cudaEventCreate(&e0);
@@ -1534,9 +1536,9 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
         if (t % ckpt == 0)
             if ((rc = copy_state(c, ck + (size_t)(t / ckpt) * snap, true))) break;
         CUDA_OR_FAIL(c, cudaGraphLaunch(c->graph, st));
-        CUDA_OR_FAIL(c, cudaMemcpyAsync(dts + t, c->dt, sizeof(double), cudaMemcpyDeviceToDevice, st));
+        // the loss term of the step, and its dt kept for the reverse pass
         cdk::launch_loss(c->col[cdk::X], c->col[cdk::Y], tgt + (size_t)t * 2 * n, (int)n, partial,
-                         scal, scale, st);
+                         scal, scale, blocks_done, c->dt, dts + t, st);
     }
     if (rc) return rc;
     if ((rc = copy_state(c, fin, true))) return rc;
@@ -1583,6 +1585,7 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
                 q.grad = g;
                 q.argmax_vals = avals;
                 q.argmax_idx = amax;
+                q.blocks_done = blocks_done;
                 cdk::launch_adj_seed(q, st);
                 cdk::launch_adj_forces(a, q, st);
                 cdk::launch_adj_dt(q, sc.dt_min, sc.dt_max, c->col[cdk::VX], c->col[cdk::VY],

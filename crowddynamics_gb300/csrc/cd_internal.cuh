@@ -184,6 +184,7 @@ struct AdjArgs {
     double *grad;                          // n x 4: tau_adj, v0, tau_0, k_soc
     double *argmax_vals;                   // per argmax block: max |v|, max v0
     int *argmax_idx;                       // their first indices
+    int *blocks_done;                      // last-block counter (zero between kernels)
 };
 
 int adj_partials(int n);
@@ -191,8 +192,11 @@ void launch_adj_seed(const AdjArgs &q, cudaStream_t s);
 void launch_adj_forces(const StepArgs &a, const AdjArgs &q, cudaStream_t s);
 void launch_adj_dt(const AdjArgs &q, double dt_min, double dt_max, const double *vx,
                    const double *vy, const double *v0, cudaStream_t s);
+// loss += scale * sum |x - target|^2 (block partials summed by the last
+// block in a fixed order); also copies the step's dt (dt_src) to dt_dst.
 void launch_loss(const double *x, const double *y, const double *target, int n,
-                 double *partial, double *loss, double scale, cudaStream_t s);
+                 double *partial, double *loss, double scale, int *blocks_done,
+                 const double *dt_src, double *dt_dst, cudaStream_t s);
 void launch_loss_grad(const double *x, const double *y, const double *target, int n,
                       double scale, double *lx, cudaStream_t s);
 void launch_copy_cols(const double *const *src, double *const *dst, int ncol, int n,
