@@ -146,13 +146,15 @@ def test_full_step_every_variant(oracle, native, name, variant):
 
 @pytest.mark.parametrize('name', sorted(SCENARIOS))
 @pytest.mark.parametrize('capacity', [0, 10])
-def test_pair_pipeline_over_capacity(oracle, native, name, capacity):
+@pytest.mark.parametrize('variant', [10, 13])
+def test_pair_pipeline_over_capacity(oracle, native, name, capacity, variant):
     """A pair-pipeline step whose near lists exceed the (fixed) capacity runs
-    the lane-group kernel instead, with the same bit-exact results."""
+    the lane-group kernel instead, with the same bit-exact results (with the
+    forces in the pair kernel and with the force pass)."""
     scen = SCENARIOS[name]()
     noise = S.draw_noise(scen.agents, np.random.default_rng(13))
     b, agents, _ = batch_from_scenarios([scen])
-    b.set_variant(10)
+    b.set_variant(variant)
     b.set_near_list_capacity(capacity)
     b.set_noise(*noise)
     dt = b.step(N.NODE_ALL, want_dt=True)
