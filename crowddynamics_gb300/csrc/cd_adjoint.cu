@@ -257,6 +257,7 @@ __device__ void wall_circ_vjp(const Circ &A, const double *w, double ux, double 
 }
 
 __global__ void k_adj_seed(AdjArgs q) {
+    pdl_enter();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     double s = 0.0;
     if (i < q.n) {
@@ -322,6 +323,7 @@ __global__ void k_loss(const double *x, const double *y, const double *target, i
 // lx += scale * 2 (x - target)
 __global__ void k_loss_grad(const double *x, const double *y, const double *target, int n,
                             double scale, double *lx) {
+    pdl_enter();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     lx[2 * i] += scale * 2.0 * (x[i] - target[2 * i]);
@@ -356,6 +358,7 @@ __device__ __forceinline__ void adj_finish(const StepArgs &a, const AdjArgs &q, 
 // partial sums meet in a fixed butterfly, so the result is deterministic.
 template <int L>
 __global__ void __launch_bounds__(NT) k_adj_forces(StepArgs a, AdjArgs q, int only_if_over) {
+    pdl_enter();
     // as the pair pipeline's fallback: only for a step whose near lists did not fit
     if (only_if_over && !(a.nl_off[a.n] > a.nl_cap)) return;
     const int r = threadIdx.x & (L - 1);
@@ -430,18 +433,22 @@ __device__ __forceinline__ int partner_entry(const StepArgs &a, int t, int s) {
     return (lo < end && __ldg(&a.nl_idx[lo]) == s) ? lo : -1;
 }
 
-__device__ __forceinline__ void put_adj(double *res, int e, double gx, double gy, double gvx,
-                                        double gvy, double gk, double gt0) {
-    double2 *p = reinterpret_cast<double2 *>(res + (size_t)e * ADJ_RES_D);
+// An entry's adjoint record, marked present (kind 1; the float32 pass marks
+// the entries of the pairs it certifies to have no force empty, kind 0).
+__device__ __forceinline__ void put_adj(const StepArgs &a, int e, double gx, double gy,
+                                        double gvx, double gvy, double gk, double gt0) {
+    double2 *p = reinterpret_cast<double2 *>(a.nl_res + (size_t)e * ADJ_RES_D);
     p[0] = make_double2(gx, gy);
     p[1] = make_double2(gvx, gvy);
     p[2] = make_double2(gk, gt0);
+    a.nl_kind[e] = 1;
 }
 
 // The flat list's first part (pairs guessed to need the social force), then
 // the pairs of the second part that the float32 pass could not certify to be
-// without a force; that pass wrote the others' zero records.
+// without a force; that pass marked the others' entries empty.
 __global__ void __launch_bounds__(NT) k_adj_pairs(StepArgs a, AdjArgs q) {
+    pdl_enter();
     if (a.nl_off[a.n] > a.nl_cap) return;
     const int nfirst = a.fs_off[a.n];
     const int npairs = nfirst + a.work[1];
@@ -455,19 +462,21 @@ __global__ void __launch_bounds__(NT) k_adj_pairs(StepArgs a, AdjArgs q) {
         double gkj = 0.0, gt0j = 0.0;
         pair_vjp_both(load_circ(a.stage, s), load_circ(a.stage, t), q.lF[2 * i], q.lF[2 * i + 1],
                       q.lF[2 * j], q.lF[2 * j + 1], G, &gkj, &gt0j);
-        put_adj(a.nl_res, e, G.gxx, G.gxy, G.gvx, G.gvy, G.gk, G.gt0);
+        put_adj(a, e, G.gxx, G.gxy, G.gvx, G.gvy, G.gk, G.gt0);
         const int eq = partner_entry(a, t, s);
-        if (eq >= 0) put_adj(a.nl_res, eq, -G.gxx, -G.gxy, -G.gvx, -G.gvy, gkj, gt0j);
+        if (eq >= 0) put_adj(a, eq, -G.gxx, -G.gxy, -G.gvx, -G.gvy, gkj, gt0j);
         else atomicOr(a.err, ERR_NEAR_LIST);
     }
 }
 
 // L lanes per agent: lane r adds entries r, r + L, ... of the agent's list
+// (those marked present)
 // and walls r, r + L, ...; the lanes' sums meet in a fixed butterfly, so the
 // result is deterministic.  One lane per agent left 5000 agents with one warp
 // per SM, each lane walking about a hundred 48-byte entries in turn.
 template <int L>
 __global__ void __launch_bounds__(NT) k_adj_gather(StepArgs a, AdjArgs q) {
+    pdl_enter();
     if (a.nl_off[a.n] > a.nl_cap) return;               // k_adj_forces' step
     const int r = threadIdx.x & (L - 1);
     const int s = (int)(((long long)blockIdx.x * NT + threadIdx.x) / L);
@@ -479,6 +488,7 @@ __global__ void __launch_bounds__(NT) k_adj_gather(StepArgs a, AdjArgs q) {
         i = a.perm[s];
         const int o1 = a.nl_off[s + 1];
         for (int e = a.nl_off[s] + r; e < o1; e += L) {
+            if (!a.nl_kind[e]) continue;                    // a pair without a force
             const double2 *p = reinterpret_cast<const double2 *>(a.nl_res + (size_t)e * ADJ_RES_D);
             const double2 x = p[0], v = p[1], kt = p[2];
             G.gxx += x.x; G.gxy += x.y;
@@ -524,6 +534,7 @@ struct ColCopy {
 };
 
 __global__ void k_copy_cols(ColCopy cc, int n) {
+    pdl_enter();
     const int k = blockIdx.y;
     if (k >= cc.ncol) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -572,6 +583,7 @@ __device__ __forceinline__ void adj_dt(const AdjArgs &q, double dt_min, double d
 // (non-finite q, and blocks whose largest q is tiny, take hypot everywhere).
 __global__ void k_adj_argmax(AdjArgs aq, double dt_min, double dt_max, const double *vx,
                              const double *vy, const double *v0, int n) {
+    pdl_enter();
     double *vals = aq.argmax_vals;
     int *idx = aq.argmax_idx;
     __shared__ double sq[RED_NT / 32], sv[RED_NT / 32], s0[RED_NT / 32];
@@ -624,7 +636,7 @@ inline int nblk(long long n, int nt) { return (int)((n + nt - 1) / nt); }
 int adj_partials(int n) { return nblk(n, RED_NT) > 0 ? nblk(n, RED_NT) : 1; }
 
 void launch_adj_seed(const AdjArgs &q, cudaStream_t s) {
-    k_adj_seed<<<adj_partials(q.n), RED_NT, 0, s>>>(q);
+    launch_k(true, k_adj_seed, adj_partials(q.n), RED_NT, 0, s, q);
 }
 void launch_adj_forces(const StepArgs &a, const AdjArgs &q, cudaStream_t s) {
     if (a.n <= 0) return;
@@ -632,18 +644,18 @@ void launch_adj_forces(const StepArgs &a, const AdjArgs &q, cudaStream_t s) {
     const int over = a.nl_cnt != nullptr;     // pair pipeline first, this as its fallback
     if (over) {
         launch_adj_light(a, s);
-        k_adj_pairs<<<nblk(n * 16, NT), NT, 0, s>>>(a, q);
+        launch_k(true, k_adj_pairs, nblk(n * 16, NT), NT, 0, s, a, q);
         // lanes per agent: enough warps to fill the SMs at small agent counts
-        if (n < 20000) k_adj_gather<16><<<nblk(n * 16, NT), NT, 0, s>>>(a, q);
-        else k_adj_gather<4><<<nblk(n * 4, NT), NT, 0, s>>>(a, q);
+        if (n < 20000) launch_k(true, k_adj_gather<16>, nblk(n * 16, NT), NT, 0, s, a, q);
+        else launch_k(true, k_adj_gather<4>, nblk(n * 4, NT), NT, 0, s, a, q);
     }
     // lanes per agent: enough warps to fill the SMs at small agent counts
-    if (n < 20000) k_adj_forces<16><<<nblk(n * 16, NT), NT, 0, s>>>(a, q, over);
-    else if (n < 80000) k_adj_forces<8><<<nblk(n * 8, NT), NT, 0, s>>>(a, q, over);
-    else k_adj_forces<4><<<nblk(n * 4, NT), NT, 0, s>>>(a, q, over);
+    if (n < 20000) launch_k(over, k_adj_forces<16>, nblk(n * 16, NT), NT, 0, s, a, q, over);
+    else if (n < 80000) launch_k(over, k_adj_forces<8>, nblk(n * 8, NT), NT, 0, s, a, q, over);
+    else launch_k(over, k_adj_forces<4>, nblk(n * 4, NT), NT, 0, s, a, q, over);
 }
 void launch_copy_cols(const double *const *src, double *const *dst, int ncol, int n,
-                      cudaStream_t s) {
+                      cudaStream_t s, bool dep) {
     if (n <= 0 || ncol <= 0) return;
     ColCopy cc;
     for (int k = 0; k < 8; ++k) {
@@ -653,11 +665,12 @@ void launch_copy_cols(const double *const *src, double *const *dst, int ncol, in
     cc.ncol = ncol < 8 ? ncol : 8;
     int nb = nblk(n, 256);
     if (nb > 1024) nb = 1024;
-    k_copy_cols<<<dim3(nb, cc.ncol), 256, 0, s>>>(cc, n);
+    launch_k(dep, k_copy_cols, dim3(nb, cc.ncol), 256, 0, s, cc, n);
 }
 void launch_adj_dt(const AdjArgs &q, double dt_min, double dt_max, const double *vx,
                    const double *vy, const double *v0, cudaStream_t s) {
-    k_adj_argmax<<<adj_partials(q.n), RED_NT, 0, s>>>(q, dt_min, dt_max, vx, vy, v0, q.n);
+    launch_k(true, k_adj_argmax, adj_partials(q.n), RED_NT, 0, s, q, dt_min, dt_max, vx, vy, v0,
+             q.n);
 }
 void launch_loss(const double *x, const double *y, const double *target, int n, double *partial,
                  double *loss, double scale, int *blocks_done, const double *dt_src,
@@ -666,8 +679,8 @@ void launch_loss(const double *x, const double *y, const double *target, int n, 
                                               dt_src, dt_dst);
 }
 void launch_loss_grad(const double *x, const double *y, const double *target, int n,
-                      double scale, double *lx, cudaStream_t s) {
-    if (n > 0) k_loss_grad<<<nblk(n, RED_NT), RED_NT, 0, s>>>(x, y, target, n, scale, lx);
+                      double scale, double *lx, cudaStream_t s, bool dep) {
+    if (n > 0) launch_k(dep, k_loss_grad, nblk(n, RED_NT), RED_NT, 0, s, x, y, target, n, scale, lx);
 }
 
 }  // namespace cdk

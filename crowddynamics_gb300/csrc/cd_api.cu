@@ -107,6 +107,7 @@ struct cd_ctx {
     uint64_t graph_gen = 0;        // bumped whenever a graph of this context goes stale
     int variant = 0;
 
+    cd_ctx *shadow = nullptr;      // the adjoint's recomputation context (made on first use)
     int timing = 0;                // 0 off; 1 run, step and kernel events; 2 run events only
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs0 = nullptr, evs1 = nullptr;
     cudaEvent_t evr0 = nullptr, evr1 = nullptr;
@@ -217,6 +218,8 @@ int dalloc(cd_ctx *c, T **p, int64_t count) {
 }
 
 void release(cd_ctx *c) {
+    if (c->shadow) cd_destroy(c->shadow);
+    c->shadow = nullptr;
     if (c->graph) cudaGraphExecDestroy(c->graph);
     void *ptrs[] = {c->colbuf, c->scen_of, c->scen, c->key, c->count, c->fill, c->start,
                     c->perm_unsorted, c->perm, c->scan_scratch, c->stage, c->cull, c->stage_f,
@@ -1457,7 +1460,7 @@ constexpr int SNAP_COLS = 8;
 constexpr int kSnapCol[SNAP_COLS] = {cdk::X,   cdk::Y,   cdk::VX, cdk::VY,
                                      cdk::FPX, cdk::FPY, cdk::FX, cdk::FY};
 
-int copy_state(cd_ctx *c, double *snap, bool save) {
+int copy_state(cd_ctx *c, double *snap, bool save, bool dep = false) {
     const double *src[SNAP_COLS];
     double *dst[SNAP_COLS];
     for (int k = 0; k < SNAP_COLS; ++k) {
@@ -1465,7 +1468,7 @@ int copy_state(cd_ctx *c, double *snap, bool save) {
         src[k] = save ? col : buf;
         dst[k] = save ? buf : col;
     }
-    cdk::launch_copy_cols(src, dst, SNAP_COLS, (int)c->n, c->stream);
+    cdk::launch_copy_cols(src, dst, SNAP_COLS, (int)c->n, c->stream, dep);
     return CD_OK;
 }
 
@@ -1479,6 +1482,41 @@ struct DevBuf {
         return static_cast<T *>(p);
     }
 };
+
+// The adjoint's recomputation context: a copy of `c` (scenarios, walls,
+// agent records, launch variant) with its own buffers, stream and step graph,
+// so that the forward steps of one checkpoint segment are recomputed on its
+// stream while `c` runs the reverse pass of the segment after it.  Made on
+// first use; before each rollout its walls, wall bins and variant follow c's
+// (the same bins, so its steps are bit-identical to c's), and the rollout
+// copies c's columns, timestep maxima and agent states into it.
+int sync_shadow(cd_ctx *c, int nodes) {
+    cd_ctx *b = c->shadow;
+    if (!b) {
+        if (cd_create(&b, c->body, c->nscen, c->scen_host.data()) != CD_OK)
+            return fail(c, CD_ERR_CUDA,
+                        std::string("recomputation context: ") + cd_last_error(nullptr));
+        c->shadow = b;
+        std::vector<char> rec((size_t)(c->n * c->itemsize));
+        if (int rc = cd_download_agents(c, rec.data(), c->n, c->itemsize, c->off)) return rc;
+        if (cd_upload_agents(b, rec.data(), c->n, c->itemsize, c->off) != CD_OK)
+            return fail(c, CD_ERR_CUDA, std::string("recomputation context: ") + cd_last_error(b));
+    }
+    if (c->nw > 0 && b->walls_host != c->walls_host)
+        if (cd_set_walls(b, c->walls_host.data(), c->nw) != CD_OK)
+            return fail(c, CD_ERR_CUDA, std::string("recomputation context: ") + cd_last_error(b));
+    if (int rc = absorb_extent(c)) return rc;
+    if (int rc = absorb_extent(b)) return fail(c, rc, cd_last_error(b));
+    if (b->extent_max != c->extent_max) {
+        b->extent_max = c->extent_max;
+        b->walls_dirty = true;
+    }
+    if (b->variant != c->variant && cd_set_variant(b, c->variant) != CD_OK)
+        return fail(c, CD_ERR_CUDA, std::string("recomputation context: ") + cd_last_error(b));
+    if (ensure_graph(b, nodes) != CD_OK)
+        return fail(c, CD_ERR_CUDA, std::string("recomputation context: ") + cd_last_error(b));
+    return CD_OK;
+}
 
 }  // namespace
 
@@ -1503,13 +1541,16 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
     if (grads)                                      // near-list entries for the reverse pass
         if (int rc = size_near_lists(c)) return rc;  // (before the graph: sizing drops it)
     if (int rc = ensure_graph(c, nodes)) return rc;
+    if (grads)
+        if (int rc = sync_shadow(c, nodes)) return rc;
     const int64_t nseg = (steps + ckpt - 1) / ckpt;
     const size_t snap = (size_t)SNAP_COLS * (size_t)std::max<int64_t>(n, 1);
     int rc = CD_OK;
     DevBuf mem;
     double *tgt = mem.get<double>(c, steps * 2 * n, rc);
     double *ck = mem.get<double>(c, nseg * snap, rc);
-    double *seg = grads ? mem.get<double>(c, (ckpt + 1) * snap, rc) : nullptr;
+    // two segment buffers: one being recomputed, one being reversed
+    double *segbuf = grads ? mem.get<double>(c, 2 * (ckpt + 1) * snap, rc) : nullptr;
     double *fin = mem.get<double>(c, snap, rc);
     double *dts = mem.get<double>(c, steps, rc);
     double *partial = mem.get<double>(c, cdk::adj_partials((int)n), rc);
@@ -1552,18 +1593,56 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
         CUDA_OR_FAIL(c, cudaMemsetAsync(adj, 0, sizeof(double) * (16 * n + 4 * n), st));
         const int fnodes = CD_NODE_ADJUSTING | CD_NODE_AGENT_AGENT | CD_NODE_AGENT_OBSTACLE;
         const cd_scenario &sc = c->scen_host[0];
+        // The recomputation context takes this rollout's parameters and agent
+        // states; each checkpoint segment's forward steps are recomputed on
+        // its stream into one of two segment buffers while this stream
+        // reverses the segment after it from the other buffer.
+        cd_ctx *b = c->shadow;
+        const int64_t npad = std::max<int64_t>(n, 1);
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(b->colbuf, c->colbuf, sizeof(double) * npad * cdk::NCOL,
+                                        cudaMemcpyDeviceToDevice, st));
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(b->v0max, c->v0max, sizeof(double) * c->nscen,
+                                        cudaMemcpyDeviceToDevice, st));
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(b->states, c->states, sizeof(int) * 5 * npad,
+                                        cudaMemcpyDeviceToDevice, st));
+        cudaEvent_t ev_sync, ev_rec[2], ev_rev[2];
+        cudaEventCreateWithFlags(&ev_sync, cudaEventDisableTiming);
+        for (int k = 0; k < 2; ++k) {
+            cudaEventCreateWithFlags(&ev_rec[k], cudaEventDisableTiming);
+            cudaEventCreateWithFlags(&ev_rev[k], cudaEventDisableTiming);
+        }
+        CUDA_OR_FAIL(c, cudaEventRecord(ev_sync, st));
+        CUDA_OR_FAIL(c, cudaStreamWaitEvent(b->stream, ev_sync, 0));
+        auto seg_of = [&](int64_t sgi) { return segbuf + (size_t)(sgi & 1) * (ckpt + 1) * snap; };
+        auto recompute = [&](int64_t sgi) -> int {
+            const int64_t t0 = sgi * ckpt, t1 = std::min<int64_t>(t0 + ckpt, steps);
+            double *seg = seg_of(sgi);
+            if (int e = copy_state(b, ck + (size_t)sgi * snap, false)) return e;
+            for (int64_t t = t0; t < t1; ++t) {
+                if (int e = copy_state(b, seg + (size_t)(t - t0) * snap, true)) return e;
+                CUDA_OR_FAIL(c, cudaGraphLaunch(b->graph, b->stream));
+            }
+            if (int e = copy_state(b, seg + (size_t)(t1 - t0) * snap, true)) return e;
+            CUDA_OR_FAIL(c, cudaEventRecord(ev_rec[sgi & 1], b->stream));
+            return CD_OK;
+        };
+        rc = recompute(nseg - 1);
         for (int64_t sgi = nseg - 1; sgi >= 0 && rc == CD_OK; --sgi) {
             const int64_t t0 = sgi * ckpt, t1 = std::min<int64_t>(t0 + ckpt, steps);
-            if ((rc = copy_state(c, ck + (size_t)sgi * snap, false))) break;
-            for (int64_t t = t0; t < t1; ++t) {            // recompute the segment
-                if ((rc = copy_state(c, seg + (size_t)(t - t0) * snap, true))) break;
-                CUDA_OR_FAIL(c, cudaGraphLaunch(c->graph, st));
+            double *seg = seg_of(sgi);
+            CUDA_OR_FAIL(c, cudaStreamWaitEvent(st, ev_rec[sgi & 1], 0));
+            if (sgi > 0) {
+                // the buffer of segment sgi - 1 held segment sgi + 1: reversed by now
+                if (sgi + 1 < nseg) CUDA_OR_FAIL(c, cudaStreamWaitEvent(b->stream, ev_rev[(sgi + 1) & 1], 0));
+                if ((rc = recompute(sgi - 1))) break;
             }
-            if (rc || (rc = copy_state(c, seg + (size_t)(t1 - t0) * snap, true))) break;
             for (int64_t t = t1 - 1; t >= t0; --t) {
                 const double *after = seg + (size_t)(t + 1 - t0) * snap;
-                cdk::launch_loss_grad(after, after + n, tgt + (size_t)t * 2 * n, (int)n, scale, lx, st);
-                if ((rc = copy_state(c, seg + (size_t)(t - t0) * snap, false))) break;
+                // the segment's first reverse step follows a wait on the other stream
+                cdk::launch_loss_grad(after, after + n, tgt + (size_t)t * 2 * n, (int)n, scale, lx,
+                                      st, t != t1 - 1);
+                // after k_loss_grad: chained to it
+                if ((rc = copy_state(c, seg + (size_t)(t - t0) * snap, false, true))) break;
                 StepArgs a = args_of(c, fnodes);
                 enqueue_cells(c, a);                        // cell list of the state before step t
                 cdk::launch_near_lists(a, st);              // and its near lists
@@ -1594,15 +1673,25 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
                 std::swap(lv, lv2);
                 std::swap(lfp, lfp2);
             }
+            if (rc == CD_OK) CUDA_OR_FAIL(c, cudaEventRecord(ev_rev[sgi & 1], st));
+        }
+        if (rc == CD_OK)
+            CUDA_OR_FAIL(c, cudaMemcpyAsync(grads, g, sizeof(double) * 4 * n,
+                                            cudaMemcpyDeviceToHost, st));
+        cudaStreamSynchronize(b->stream);
+        cudaEventDestroy(ev_sync);
+        for (int k = 0; k < 2; ++k) {
+            cudaEventDestroy(ev_rec[k]);
+            cudaEventDestroy(ev_rev[k]);
         }
         if (rc) return rc;
-        CUDA_OR_FAIL(c, cudaMemcpyAsync(grads, g, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st));
+        if (check_device_error(b) != CD_OK)
+            return fail(c, CD_ERR_CUDA, std::string("recomputation context: ") + cd_last_error(b));
     }
     cudaEventRecord(e2, st);
     // leave the context in the rollout's final state
     if ((rc = copy_state(c, fin, false))) return rc;
     CUDA_OR_FAIL(c, cudaMemcpyAsync(c->dt, scal + 2, sizeof(double), cudaMemcpyDeviceToDevice, st));
-    // recomputed steps advanced time_tot a second time: restore the forward's value
     CUDA_OR_FAIL(c, cudaMemcpyAsync(c->time_tot, scal + 3, sizeof(double), cudaMemcpyDeviceToDevice, st));
     CUDA_OR_FAIL(c, cudaMemcpyAsync(loss, scal, sizeof(double), cudaMemcpyDeviceToHost, st));
     CUDA_OR_FAIL(c, cudaGetLastError());

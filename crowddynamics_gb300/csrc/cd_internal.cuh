@@ -198,9 +198,43 @@ void launch_loss(const double *x, const double *y, const double *target, int n,
                  double *partial, double *loss, double scale, int *blocks_done,
                  const double *dt_src, double *dt_dst, cudaStream_t s);
 void launch_loss_grad(const double *x, const double *y, const double *target, int n,
-                      double scale, double *lx, cudaStream_t s);
+                      double scale, double *lx, cudaStream_t s, bool dep = true);
+// `dep`: launched as the programmatic dependent of the kernel before it.
 void launch_copy_cols(const double *const *src, double *const *dst, int ncol, int n,
-                      cudaStream_t s);
+                      cudaStream_t s, bool dep = false);
+
+// Programmatic dependent launch: a kernel launched by launch_k(true, ...)
+// may start while the kernel before it on the stream finishes; it begins
+// with pdl_enter, which waits for that kernel (its memory visible) and lets
+// the next dependent start in turn.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Launch of kernel `k` on `s`.  `dep`: as the programmatic dependent of the
+// kernel launched just before it on `s` (every such kernel starts with
+// pdl_enter), so that its launch overlaps that kernel's last blocks.
+template <typename... P, typename... A>
+inline void launch_k(bool dep, void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+              A... args) {
+    if (!dep) {
+        k<<<grid, block, smem, s>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 
 // Launchers (cd_kernels.cu)
 void launch_prepare(const StepArgs &a, cudaStream_t s);
@@ -246,7 +280,7 @@ void launch_near_count(const StepArgs &a, cudaStream_t s, int variant);
 // Near lists (counts, scans, fill; 8 lanes per agent) for the state staged in `a`.
 void launch_near_lists(const StepArgs &a, cudaStream_t s);
 // The float32 pass of the Circular reverse step over the flat list's second
-// part: zero adjoint records for the pairs without a force, the rest
+// part: the entries of the pairs without a force marked empty, the rest
 // appended to the deferred list for k_adj_pairs.
 void launch_adj_light(const StepArgs &a, cudaStream_t s);
 void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s);

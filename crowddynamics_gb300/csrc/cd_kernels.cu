@@ -222,10 +222,6 @@ __device__ __forceinline__ void wall_three_circle(const TC &A, const double *w,
 // and its memory is visible (returns at once after an ordinary launch), then
 // allow the next kernel's blocks to be scheduled beside this one's last
 // blocks (they wait here in turn).
-__device__ __forceinline__ void pdl_enter() {
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
 
 constexpr int PREP_NT = 256;                     // k_prepare's block size
 
@@ -2426,19 +2422,14 @@ __device__ __forceinline__ void put_pair(const StepArgs &a, int e, int res, doub
     a.nl_kind[e] = kind;
 }
 
-// An adjoint record of zeros: the reverse of a pair without a force (no
-// contact, no time to collision in (0, 30]) adds nothing to either side.
-__device__ __forceinline__ void put_adj_zero(const StepArgs &a, int e) {
-    double2 *p = reinterpret_cast<double2 *>(a.nl_res + (size_t)e * ADJ_RES_D);
-    const double2 z = make_double2(0.0, 0.0);
-    p[0] = z;
-    p[1] = z;
-    p[2] = z;
-}
+// The reverse of a pair without a force (no contact, no time to collision
+// in (0, 30]) adds nothing to either side: its entries are marked empty
+// (kind 0) and k_adj_gather skips them.
+__device__ __forceinline__ void put_adj_zero(const StepArgs &a, int e) { a.nl_kind[e] = 0; }
 
 // The pairs of the flat list's second part (not guessed to need the social
 // force), in float32 alone (tc_pair_light, circ_pair_light): a decided pair
-// writes the kind bytes of both its entries (ADJ: zero adjoint records); the
+// writes the kind bytes of both its entries (ADJ: marks them empty); the
 // others are appended to defer_list for k_pairs (ADJ: k_adj_pairs), which
 // takes them after the first part.  Few registers, so many warps per SM hide
 // the loads.  Warps take 32 consecutive pairs at a time, in turn.
@@ -3192,29 +3183,6 @@ __global__ void k_fp64_fma(double *out, int iters, double b, double c) {
 
 inline int nblk(long long n, int nt) { return (int)((n + nt - 1) / nt); }
 
-// Launch of kernel `k` on `s`.  `dep`: as the programmatic dependent of the
-// kernel launched just before it on `s` (every such kernel starts with
-// pdl_enter), so that its launch overlaps that kernel's last blocks.
-template <typename... P, typename... A>
-void launch_k(bool dep, void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
-              A... args) {
-    if (!dep) {
-        k<<<grid, block, smem, s>>>(args...);
-        return;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, k, args...);
-}
-
 }  // namespace
 
 void launch_prepare(const StepArgs &a, cudaStream_t s) {
@@ -3537,7 +3505,7 @@ void launch_near_lists(const StepArgs &a, cudaStream_t s) {
 }
 void launch_adj_light(const StepArgs &a, cudaStream_t s) {
     if (a.n <= 0 || !a.nl_cnt || a.body != 0) return;
-    k_pairs_light<0, true><<<nblk((long long)a.n * 16, NTG), NTG, 0, s>>>(a);
+    launch_k(true, k_pairs_light<0, true>, nblk((long long)a.n * 16, NTG), NTG, 0, s, a);
 }
 
 void launch_pair_counts(const StepArgs &a, int *counts, cudaStream_t s) {
