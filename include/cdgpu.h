@@ -327,7 +327,10 @@ int cd_measure_fp64_peak(double *gflops);
  * Replaces nothing in the reference (which has no gradients); the forward
  * part is the same step as cd_step.  `forward_ms` / `adjoint_ms` (may be
  * NULL) receive the device time of the forward rollout and of the reverse
- * sweep (recomputation included). */
+ * sweep (recomputation included).  The first call with `grads` makes a second
+ * context inside this one (the same scenarios, walls and agents, its own
+ * device buffers and stream), on which each segment is recomputed while the
+ * reverse step runs the segment after it; cd_destroy releases it. */
 int cd_rollout_loss(cd_ctx *ctx, int64_t steps, const double *target,
                     int64_t checkpoint_every, double *loss, double *grads,
                     double *forward_ms, double *adjoint_ms);
