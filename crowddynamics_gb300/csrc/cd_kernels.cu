@@ -1663,6 +1663,49 @@ __device__ __forceinline__ int tc_pair_light(const StepArgs &a, int s, int t) {
     return RES_ZERO;                                     // no sub-pair has a root
 }
 
+// The first stages of tc_pair_light, which decide most pairs (the distance
+// bounds, then the enclosing circles apart for t > 0): its result, or
+// RES_SLOW where tc_pair_light goes on to the pre-selection or to the
+// sub-pair roots (the same tests on the same values, so the same decisions).
+constexpr int RES_SLOW = 4;
+__device__ __forceinline__ int tc_pair_light_quick(const StepArgs &a, int s, int t) {
+    const float4 meC = __ldg(&a.cull[s]), meF0 = __ldg(&a.stage_f[2 * s]),
+                 meF1 = __ldg(&a.stage_f[2 * s + 1]);
+    const float4 oC = __ldg(&a.cull[t]), oF0 = __ldg(&a.stage_f[2 * t]),
+                 oF1 = __ldg(&a.stage_f[2 * t + 1]);
+    const float dxt = (meC.x - oC.x) + (meF0.x - oF0.x);
+    const float dyt = (meC.y - oC.y) + (meF0.y - oF0.y);
+    const float mox1 = meF1.x, moy1 = meF1.y, mox2 = meF1.z, moy2 = meF1.w;
+    const float oox1 = oF1.x, ooy1 = oF1.y, oox2 = oF1.z, ooy2 = oF1.w;
+    const float xe2 = dxt * dxt + dyt * dyt;
+    const float xe = sqrtf(xe2);
+    const float re = meC.z + oC.z;
+    const float dmarg = PRESEL_MARGIN +
+                        1e-6f * (fabsf(dxt) + fabsf(dyt) + fabsf(mox1) + fabsf(moy1) +
+                                 fabsf(mox2) + fabsf(moy2) + fabsf(oox1) + fabsf(ooy1) +
+                                 fabsf(oox2) + fabsf(ooy2) + meF0.z + meF0.w + oF0.z + oF0.w);
+    const float h_lo = xe - re, h_hi = xe - (meF0.z + oF0.z);
+    if (h_lo - dmarg >= (float)SIGTH_SOC) return RES_NONE;
+    if (!(h_hi + dmarg < (float)SIGTH_SOC && h_lo - dmarg > 0.f)) return RES_SLOW;
+    const double2 vp = __ldg(&a.stage[(size_t)s * STAGE_Q_TC + 3]);
+    const double2 vq = __ldg(&a.stage[(size_t)t * STAGE_Q_TC + 3]);
+    const float vxf = (float)(vp.x - vq.x), vyf = (float)(vp.y - vq.y);
+    if (!(fabsf(vxf) > 1e-20f || fabsf(vyf) > 1e-20f)) return RES_DEFER;
+    const float af = vxf * vxf + vyf * vyf;
+    const float e0 = 1e-6f * (1.f + fabsf(dxt) + fabsf(dyt) + fabsf(mox1) + fabsf(moy1) +
+                              fabsf(mox2) + fabsf(moy2) + fabsf(oox1) + fabsf(ooy1) +
+                              fabsf(oox2) + fabsf(ooy2));
+    const float be = -(dxt * vxf + dyt * vyf);
+    const float ce = xe2 - re * re;
+    const float mbe = 4.f * e0 * (fabsf(vxf) + fabsf(vyf)) +
+                      1e-6f * (fabsf(dxt * vxf) + fabsf(dyt * vyf));
+    const float mce = 8.f * e0 * (fabsf(dxt) + fabsf(dyt) + re) + 1e-6f * (xe2 + re * re);
+    const float bbe = fabsf(be) + mbe;
+    if (ce - mce > 0.f && (be + mbe <= 0.f || bbe * bbe < 0.99f * af * (ce - mce)))
+        return RES_ZERO;
+    return RES_SLOW;
+}
+
 // The float32 certificates of circ_pair_decide for a pair (s, t):
 // RES_NONE where the skin distance is certainly >= 3 m, RES_ZERO where it is
 // certainly in (0, 3) and the pair certainly has no time to collision in
@@ -2441,25 +2484,21 @@ __global__ void __launch_bounds__(NTG) k_pairs_light(StepArgs a) {
     const int lane = threadIdx.x & 31;
     const int k0 = a.fs_off[a.n], npairs = a.fw_off[a.n];
     const int warps = gridDim.x * (NTG / 32);
-    for (int base = k0 + (blockIdx.x * (NTG / 32) + (threadIdx.x >> 5)) * 32; base < npairs;
-         base += warps * 32) {
-        const int k = base + lane;
-        int res = RES_NONE, s = 0, e = 0, t = 0;
-        if (k < npairs) {
-            const int2 pe = __ldg(&a.fw_pairs[k]);
-            s = pe.x;
-            e = pe.y;
-            t = __ldg(&a.nl_idx[e]);
-            res = BODY == 1 ? tc_pair_light(a, s, t) : circ_pair_light(a, s, t);
-        }
-        const unsigned dm = __ballot_sync(FULL, k < npairs && res == RES_DEFER);
+    // ThreeCircle: the few pairs that need the pre-selection or the sub-pair
+    // roots wait in a per-warp queue and are evaluated 32 at a time, so that
+    // the warps do not run those stages for one lane each
+    __shared__ int slow_q[NTG / 32][64];
+    int *sq = slow_q[threadIdx.x >> 5];
+    int nq = 0;                                            // warp-uniform
+    auto finish = [&](int k, int s, int e, int t, int res, bool on) {
+        const unsigned dm = __ballot_sync(FULL, on && res == RES_DEFER);
         if (dm) {
             int d0 = 0;
             if (lane == 0) d0 = atomicAdd(a.work + 1, __popc(dm));
             d0 = __shfl_sync(FULL, d0, 0);
             if ((dm >> lane) & 1u) a.defer_list[d0 + __popc(dm & ((1u << lane) - 1u))] = k;
         }
-        if (k < npairs && res != RES_DEFER) {
+        if (on && res != RES_DEFER) {
             const int eq = partner_entry(a, t, s);
             if (ADJ) {
                 put_adj_zero(a, e);
@@ -2470,7 +2509,52 @@ __global__ void __launch_bounds__(NTG) k_pairs_light(StepArgs a) {
             }
             if (eq < 0) atomicOr(a.err, ERR_NEAR_LIST);
         }
+    };
+    // the queue's first `count` pairs, one per lane, through all of tc_pair_light
+    auto drain = [&](int count) {
+        const bool on = lane < count;
+        int k = 0, s = 0, e = 0, t = 0, res = RES_NONE;
+        if (on) {
+            k = sq[lane];
+            const int2 pe = __ldg(&a.fw_pairs[k]);
+            s = pe.x;
+            e = pe.y;
+            t = __ldg(&a.nl_idx[e]);
+            res = tc_pair_light(a, s, t);
+        }
+        __syncwarp(FULL);
+        finish(k, s, e, t, res, on);
+    };
+    for (int base = k0 + (blockIdx.x * (NTG / 32) + (threadIdx.x >> 5)) * 32; base < npairs;
+         base += warps * 32) {
+        const int k = base + lane;
+        int res = RES_NONE, s = 0, e = 0, t = 0;
+        if (k < npairs) {
+            const int2 pe = __ldg(&a.fw_pairs[k]);
+            s = pe.x;
+            e = pe.y;
+            t = __ldg(&a.nl_idx[e]);
+            res = BODY == 1 ? tc_pair_light_quick(a, s, t) : circ_pair_light(a, s, t);
+        }
+        if (BODY == 1) {
+            const unsigned sm = __ballot_sync(FULL, k < npairs && res == RES_SLOW);
+            if ((sm >> lane) & 1u) sq[nq + __popc(sm & ((1u << lane) - 1u))] = k;
+            nq += __popc(sm);
+            __syncwarp(FULL);
+        }
+        finish(k, s, e, t, res, k < npairs && res != RES_SLOW);
+        if (BODY == 1 && nq >= 32) {
+            drain(32);
+            // the rest moves to the front
+            const int rest = nq - 32;
+            const int v = lane < rest ? sq[32 + lane] : 0;
+            __syncwarp(FULL);
+            if (lane < rest) sq[lane] = v;
+            __syncwarp(FULL);
+            nq = rest;
+        }
     }
+    if (BODY == 1 && nq > 0) drain(nq);
 }
 
 // Job records of the force pass (JOB_Q_TC / JOB_Q_CIRC double2 each).  Jobs
