@@ -2417,7 +2417,10 @@ __global__ void __launch_bounds__(NTG) k_nl_fill(StepArgs a) {
 // The part is scanned 32 entries at a time with eight independent 16-byte
 // loads from a 4-aligned start (one memory round trip for most lists);
 // entries outside the part are ignored.  Near the end of the allocation a
-// binary search replaces the wide loads.
+// binary search replaces the wide loads.  k_pairs, bound by float64 latency,
+// gains from the single round trip; the float32 pass, bound by instruction
+// issue, takes the binary search (partner_entry_search: about a fifth of the
+// instructions, 57 -> 45 us per step at 100k ThreeCircle agents).
 __device__ __forceinline__ int partner_entry(const StepArgs &a, int t, int s) {
     int lo = __ldg(&a.nl_off[t]), hi = __ldg(&a.nl_fwd[t]);
     const int end = hi;
@@ -2438,6 +2441,18 @@ __device__ __forceinline__ int partner_entry(const StepArgs &a, int t, int s) {
         if (found >= 0) return found;
         lo = base + 32 > lo ? base + 32 : lo;
     }
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&a.nl_idx[mid]) < s) lo = mid + 1;
+        else hi = mid;
+    }
+    return (lo < end && __ldg(&a.nl_idx[lo]) == s) ? lo : -1;
+}
+
+// The same by binary search over the part (slots ascending).
+__device__ __forceinline__ int partner_entry_search(const StepArgs &a, int t, int s) {
+    int lo = __ldg(&a.nl_off[t]), hi = __ldg(&a.nl_fwd[t]);
+    const int end = hi;
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
         if (__ldg(&a.nl_idx[mid]) < s) lo = mid + 1;
@@ -2499,7 +2514,7 @@ __global__ void __launch_bounds__(NTG) k_pairs_light(StepArgs a) {
             if ((dm >> lane) & 1u) a.defer_list[d0 + __popc(dm & ((1u << lane) - 1u))] = k;
         }
         if (on && res != RES_DEFER) {
-            const int eq = partner_entry(a, t, s);
+            const int eq = partner_entry_search(a, t, s);
             if (ADJ) {
                 put_adj_zero(a, e);
                 if (eq >= 0) put_adj_zero(a, eq);
