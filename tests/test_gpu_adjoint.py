@@ -209,3 +209,23 @@ def test_adjoint_over_capacity_fallback(native):
     assert got[0] == ref[0]                      # the forward is unchanged
     scale = np.abs(ref[1]).max(0)
     assert np.all(np.abs(got[1] - ref[1]) <= 1e-10 * scale)
+
+
+def test_second_rollout_after_new_agents(native):
+    """The rollout's recomputation context takes the agents of each call: a
+    second rollout on the same context after a new upload (other tau_adj and
+    target speeds) gives the loss and gradients of a fresh context, bit for
+    bit."""
+    scen, a, target = _case('dense')
+    b, _ = _device(scen, a)
+    b.rollout_loss(STEPS, target, CKPT)                 # makes the recomputation context
+    a2 = a.copy()
+    rng = np.random.default_rng(11)
+    a2['tau_adj'] = rng.uniform(0.3, 0.7, len(a2))
+    a2['target_velocity'] = rng.normal(1.2, 0.2, len(a2))
+    b.upload(a2)
+    got = b.rollout_loss(STEPS, target, CKPT)
+    b.close()
+    ref = _loss(scen, a2, target)
+    assert got[0] == ref[0]
+    assert np.array_equal(got[1], ref[1])
