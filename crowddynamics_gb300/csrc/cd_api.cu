@@ -1496,11 +1496,15 @@ int sync_shadow(cd_ctx *c, int nodes) {
         if (cd_create(&b, c->body, c->nscen, c->scen_host.data()) != CD_OK)
             return fail(c, CD_ERR_CUDA,
                         std::string("recomputation context: ") + cd_last_error(nullptr));
-        c->shadow = b;
         std::vector<char> rec((size_t)(c->n * c->itemsize));
-        if (int rc = cd_download_agents(c, rec.data(), c->n, c->itemsize, c->off)) return rc;
-        if (cd_upload_agents(b, rec.data(), c->n, c->itemsize, c->off) != CD_OK)
-            return fail(c, CD_ERR_CUDA, std::string("recomputation context: ") + cd_last_error(b));
+        int rc = cd_download_agents(c, rec.data(), c->n, c->itemsize, c->off);
+        if (rc == CD_OK && cd_upload_agents(b, rec.data(), c->n, c->itemsize, c->off) != CD_OK)
+            rc = fail(c, CD_ERR_CUDA, std::string("recomputation context: ") + cd_last_error(b));
+        if (rc != CD_OK) {                      // no half-made context is kept
+            cd_destroy(b);
+            return rc;
+        }
+        c->shadow = b;
     }
     if (c->nw > 0 && b->walls_host != c->walls_host)
         if (cd_set_walls(b, c->walls_host.data(), c->nw) != CD_OK)
