@@ -2231,8 +2231,11 @@ __device__ __forceinline__ bool social_guess(float4 me, float4 o) {
 // candidate base + j) in the agent's mask row; k_nl_fill then places the
 // entries from the masks alone.  An agent with more chunks than a row holds is
 // evaluated again by the fill.
+// Chunks of 16 candidates for every lane count: the per-chunk work (the run
+// and its bounds, the counts, the row word) is spread over more candidates
+// (4 lanes x 4 against 4 x 2: the step 0.320 -> 0.315 ms at 100k agents).
 template <int L> struct NlChunk {
-    static constexpr int C = L <= 8 ? 2 : 1;          // candidates per lane and chunk
+    static constexpr int C = L == 4 ? 4 : (L <= 8 ? 2 : 1);   // candidates per lane and chunk
     static constexpr int CW = C * L;                   // candidates per chunk, <= 16
     static constexpr unsigned CMASK = (1u << CW) - 1u;
 };
