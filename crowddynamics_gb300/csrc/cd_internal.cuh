@@ -216,8 +216,8 @@ __device__ __forceinline__ void pdl_enter() {
 // kernel launched just before it on `s` (every such kernel starts with
 // pdl_enter), so that its launch overlaps that kernel's last blocks.
 template <typename... P, typename... A>
-inline void launch_k(bool dep, void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
-              A... args) {
+inline void launch_k(bool dep, void (*k)(P...), dim3 grid, dim3 block, size_t smem,
+                     cudaStream_t s, A... args) {
     if (!dep) {
         k<<<grid, block, smem, s>>>(args...);
         return;
@@ -234,7 +234,6 @@ inline void launch_k(bool dep, void (*k)(P...), dim3 grid, dim3 block, size_t sm
     cfg.numAttrs = 1;
     cudaLaunchKernelEx(&cfg, k, args...);
 }
-
 
 // Launchers (cd_kernels.cu)
 void launch_prepare(const StepArgs &a, cudaStream_t s);
