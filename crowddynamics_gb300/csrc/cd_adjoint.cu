@@ -23,6 +23,7 @@
 // Branches are differentiated where they are taken (a sub-gradient at the
 // contact onset h = 0, the social cut-offs h = 3 and tau = 30, the 2000 N
 // truncation and the dt clamp).
+#include <algorithm>
 #include <cstdint>
 #include <cmath>
 #include "cd_internal.cuh"
@@ -541,6 +542,33 @@ __global__ void k_copy_cols(ColCopy cc, int n) {
         cc.dst[k][i] = cc.src[k][i];
 }
 
+// Copies of up to 16 device buffers in one launch (byte counts multiples of 4;
+// 16-byte words where a buffer's size and both addresses allow).
+struct BufCopy {
+    const void *src[16];
+    void *dst[16];
+    long long bytes[16];
+    int nbuf;
+};
+
+__global__ void k_copy_bufs(BufCopy bc) {
+    const int k = blockIdx.y;
+    if (k >= bc.nbuf) return;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long done = 0;
+    if ((((uintptr_t)bc.src[k] | (uintptr_t)bc.dst[k]) & 15) == 0) {
+        const uint4 *s4 = static_cast<const uint4 *>(bc.src[k]);
+        uint4 *d4 = static_cast<uint4 *>(bc.dst[k]);
+        const long long n4 = bc.bytes[k] / 16;
+        for (long long w = t0; w < n4; w += stride) d4[w] = s4[w];
+        done = n4 * 16;
+    }
+    const unsigned *s1 = static_cast<const unsigned *>(bc.src[k]);
+    unsigned *d1 = static_cast<unsigned *>(bc.dst[k]);
+    for (long long w = done / 4 + t0; w < bc.bytes[k] / 4; w += stride) d1[w] = s1[w];
+}
+
 // (value, index) of a maximum: the larger value, on ties the smaller index
 // (-1 = none); NaN never wins.
 __device__ __forceinline__ void better(double &v, int &j, double v2, int j2) {
@@ -666,6 +694,22 @@ void launch_copy_cols(const double *const *src, double *const *dst, int ncol, in
     int nb = nblk(n, 256);
     if (nb > 1024) nb = 1024;
     launch_k(dep, k_copy_cols, dim3(nb, cc.ncol), 256, 0, s, cc, n);
+}
+void launch_copy_bufs(const void *const *src, void *const *dst, const long long *bytes, int nbuf,
+                      cudaStream_t s) {
+    if (nbuf <= 0) return;
+    BufCopy bc;
+    long long most = 0;
+    for (int k = 0; k < 16; ++k) {
+        bc.src[k] = k < nbuf ? src[k] : nullptr;
+        bc.dst[k] = k < nbuf ? dst[k] : nullptr;
+        bc.bytes[k] = k < nbuf ? bytes[k] : 0;
+        if (k < nbuf) most = std::max(most, bytes[k]);
+    }
+    bc.nbuf = nbuf < 16 ? nbuf : 16;
+    int nb = (int)std::min<long long>((most / 16 + 255) / 256, 512);
+    if (nb < 1) nb = 1;
+    k_copy_bufs<<<dim3(nb, bc.nbuf), 256, 0, s>>>(bc);
 }
 void launch_adj_dt(const AdjArgs &q, double dt_min, double dt_max, const double *vx,
                    const double *vy, const double *v0, cudaStream_t s) {

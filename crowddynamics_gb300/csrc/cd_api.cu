@@ -1483,6 +1483,60 @@ struct DevBuf {
     }
 };
 
+// The step structures a reverse step reads (cell list, staged records, near
+// lists, flat pair list) as the recomputation context builds them for the
+// state before each step of a segment: kept per step, the reverse pass takes
+// them instead of building them again.
+enum { SN_KEY, SN_PERM, SN_START, SN_STAGE, SN_CULL, SN_STAGEF, SN_NLOFF, SN_NLFWD, SN_FWOFF,
+       SN_FSOFF, SN_NLIDX, SN_FWPAIRS, SN_COUNT };
+struct StepSnapLayout {
+    long long off[SN_COUNT], bytes[SN_COUNT], total;
+};
+
+StepSnapLayout snap_layout(const cd_ctx *b) {
+    const long long n = std::max<int64_t>(b->n, 1), cells = b->ncells + 1, cap = b->nl_cap;
+    const long long sq = b->body == CD_BODY_CIRCULAR ? cdk::STAGE_Q_CIRC : cdk::STAGE_Q_TC;
+    // (fw_pairs: at most cap / 2 pairs of two ints)
+    const long long bytes[SN_COUNT] = {4 * n,       4 * n,       4 * cells,   16 * sq * n,
+                                       16 * n,      32 * n,      4 * (n + 1), 4 * n,
+                                       4 * (n + 1), 4 * (n + 1), 4 * cap,     4 * cap};
+    StepSnapLayout L;
+    long long o = 0;
+    for (int k = 0; k < SN_COUNT; ++k) {
+        L.off[k] = o;
+        L.bytes[k] = bytes[k];
+        o += (bytes[k] + 255) / 256 * 256;
+    }
+    L.total = o;
+    return L;
+}
+
+void snap_step(const cd_ctx *b, const StepSnapLayout &L, char *dst) {
+    const void *src[SN_COUNT] = {b->key,    b->perm,   b->start,  b->stage,  b->cull,   b->stage_f,
+                                 b->nl_off, b->nl_fwd, b->fw_off, b->fs_off, b->nl_idx, b->fw_pairs};
+    void *to[SN_COUNT];
+    for (int k = 0; k < SN_COUNT; ++k) to[k] = dst + L.off[k];
+    cdk::launch_copy_bufs(src, to, L.bytes, SN_COUNT, b->stream);
+}
+
+// The reverse step's structures from a snapshot (c's own buffers for what it
+// writes: entry records and kinds, the deferred list, the work counters).
+void snap_args(StepArgs &a, const StepSnapLayout &L, char *sp, int64_t cap) {
+    a.key = reinterpret_cast<int *>(sp + L.off[SN_KEY]);
+    a.perm = reinterpret_cast<int *>(sp + L.off[SN_PERM]);
+    a.start = reinterpret_cast<int *>(sp + L.off[SN_START]);
+    a.stage = reinterpret_cast<double2 *>(sp + L.off[SN_STAGE]);
+    a.cull = reinterpret_cast<float4 *>(sp + L.off[SN_CULL]);
+    a.stage_f = reinterpret_cast<float4 *>(sp + L.off[SN_STAGEF]);
+    a.nl_off = reinterpret_cast<int *>(sp + L.off[SN_NLOFF]);
+    a.nl_fwd = reinterpret_cast<int *>(sp + L.off[SN_NLFWD]);
+    a.fw_off = reinterpret_cast<int *>(sp + L.off[SN_FWOFF]);
+    a.fs_off = reinterpret_cast<int *>(sp + L.off[SN_FSOFF]);
+    a.nl_idx = reinterpret_cast<int *>(sp + L.off[SN_NLIDX]);
+    a.fw_pairs = reinterpret_cast<int2 *>(sp + L.off[SN_FWPAIRS]);
+    a.nl_cap = (int)cap;
+}
+
 // The adjoint's recomputation context: a copy of `c` (scenarios, walls,
 // agent records, launch variant) with its own buffers, stream and step graph,
 // so that the forward steps of one checkpoint segment are recomputed on its
@@ -1555,6 +1609,14 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
     double *ck = mem.get<double>(c, nseg * snap, rc);
     // two segment buffers: one being recomputed, one being reversed
     double *segbuf = grads ? mem.get<double>(c, 2 * (ckpt + 1) * snap, rc) : nullptr;
+    // and, where the recomputation builds near lists, each step's structures
+    // (up to 8 GiB; beyond, the reverse pass builds them itself)
+    const cd_ctx *shadow = grads ? c->shadow : nullptr;
+    const bool keep_steps = shadow && shadow->nl_cap > 0 && cdk::variant_pairs(shadow->variant) &&
+                            c->nl_cnt && c->nl_cap > 0;
+    const StepSnapLayout snl = keep_steps ? snap_layout(shadow) : StepSnapLayout{};
+    const bool use_snaps = keep_steps && 2 * ckpt * snl.total <= (8LL << 30);
+    char *snapbuf = use_snaps ? mem.get<char>(c, 2 * ckpt * snl.total, rc) : nullptr;
     double *fin = mem.get<double>(c, snap, rc);
     double *dts = mem.get<double>(c, steps, rc);
     double *partial = mem.get<double>(c, cdk::adj_partials((int)n), rc);
@@ -1625,6 +1687,8 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
             for (int64_t t = t0; t < t1; ++t) {
                 if (int e = copy_state(b, seg + (size_t)(t - t0) * snap, true)) return e;
                 CUDA_OR_FAIL(c, cudaGraphLaunch(b->graph, b->stream));
+                if (use_snaps)
+                    snap_step(b, snl, snapbuf + ((size_t)(sgi & 1) * ckpt + (t - t0)) * snl.total);
             }
             if (int e = copy_state(b, seg + (size_t)(t1 - t0) * snap, true)) return e;
             CUDA_OR_FAIL(c, cudaEventRecord(ev_rec[sgi & 1], b->stream));
@@ -1648,8 +1712,15 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
                 // after k_loss_grad: chained to it
                 if ((rc = copy_state(c, seg + (size_t)(t - t0) * snap, false, true))) break;
                 StepArgs a = args_of(c, fnodes);
-                enqueue_cells(c, a);                        // cell list of the state before step t
-                cdk::launch_near_lists(a, st);              // and its near lists
+                if (use_snaps) {
+                    // the recomputation's cell list and near lists of the state before step t
+                    snap_args(a, snl, snapbuf + ((size_t)(sgi & 1) * ckpt + (t - t0)) * snl.total,
+                              std::min<int64_t>(c->nl_cap, shadow->nl_cap));
+                    CUDA_OR_FAIL(c, cudaMemsetAsync(c->work, 0, 4 * sizeof(int), st));
+                } else {
+                    enqueue_cells(c, a);                    // cell list of the state before step t
+                    cdk::launch_near_lists(a, st);          // and its near lists
+                }
                 cdk::AdjArgs q;
                 q.n = (int)n;
                 q.dt = dts + t;

@@ -199,6 +199,9 @@ void launch_loss(const double *x, const double *y, const double *target, int n,
                  const double *dt_src, double *dt_dst, cudaStream_t s);
 void launch_loss_grad(const double *x, const double *y, const double *target, int n,
                       double scale, double *lx, cudaStream_t s, bool dep = true);
+// Up to 16 device-to-device copies in one launch (byte counts multiples of 4).
+void launch_copy_bufs(const void *const *src, void *const *dst, const long long *bytes, int nbuf,
+                      cudaStream_t s);
 // `dep`: launched as the programmatic dependent of the kernel before it.
 void launch_copy_cols(const double *const *src, double *const *dst, int ncol, int n,
                       cudaStream_t s, bool dep = false);

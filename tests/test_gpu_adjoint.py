@@ -42,26 +42,33 @@ def _case(kind, seed=3):
     return scen, a.copy(), target
 
 
-def _device(scen, agents):
+def _device(scen, agents, variant=None):
+    """A context for the scenario; `variant` 14 (the pair pipeline with the
+    force pass) instead of the small-scenario default makes the rollout's
+    recomputation context keep each step's cell list and near lists for the
+    reverse pass."""
     b, _, walls = batch_from_scenarios([scen])
+    if variant is not None:
+        b.set_variant(variant)
     b.upload(agents)
     return b, walls
 
 
-def _loss(scen, agents, target, ckpt=CKPT, grads=True):
-    b, _ = _device(scen, agents)
+def _loss(scen, agents, target, ckpt=CKPT, grads=True, variant=None):
+    b, _ = _device(scen, agents, variant)
     try:
         return b.rollout_loss(STEPS, target, ckpt, grads=grads)
     finally:
         b.close()
 
 
+@pytest.mark.parametrize('variant', [None, 14])
 @pytest.mark.parametrize('kind', ['sparse', 'dense'])
-def test_adjoint_matches_torch_autograd(native, kind):
+def test_adjoint_matches_torch_autograd(native, kind, variant):
     from oracle import torch_circular as TC
     from crowddynamics_gb300.adjoint import PARAMS
     scen, a, target = _case(kind)
-    b, walls = _device(scen, a)
+    b, walls = _device(scen, a, variant)
     loss, g, fms, ams = b.rollout_loss(STEPS, target, CKPT)
     b.close()
     p = [torch.tensor(np.ascontiguousarray(a[k]), dtype=torch.float64, requires_grad=True)
@@ -123,15 +130,22 @@ def test_adjoint_matches_central_differences(native, kind):
         check(e, '%s of agent %d' % (name, i))
 
 
-def test_checkpoint_interval_does_not_change_result(native):
+@pytest.mark.parametrize('variant', [None, 14])
+def test_checkpoint_interval_does_not_change_result(native, variant):
     scen, a, target = _case('sparse')
-    ref = _loss(scen, a, target, ckpt=CKPT)
+    ref = _loss(scen, a, target, ckpt=CKPT, variant=variant)
     for ckpt in (1, 4, STEPS, 100):
-        got = _loss(scen, a, target, ckpt=ckpt)
+        got = _loss(scen, a, target, ckpt=ckpt, variant=variant)
         assert got[0] == ref[0], ckpt
         assert np.array_equal(got[1], ref[1]), ckpt
-    again = _loss(scen, a, target, ckpt=CKPT)
+    again = _loss(scen, a, target, ckpt=CKPT, variant=variant)
     assert np.array_equal(again[1], ref[1])                 # deterministic
+    if variant is not None:
+        # the same gradient as the small-scenario default's (lane groups in
+        # the forward, the reverse building its own near lists)
+        other = _loss(scen, a, target, ckpt=CKPT)
+        assert other[0] == ref[0]
+        assert np.array_equal(other[1], ref[1])
 
 
 @pytest.mark.parametrize('kind', ['sparse', 'dense'])
