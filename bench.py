@@ -390,9 +390,9 @@ def run_ours(args, ws, rank, local):
         for k in range(args.steps):
             with ProfileRange(args.profile_range == 'records' and trial == 2 and
                               k == args.steps - 1):
-                b.upload(rec)
-                b.launch(1, nodes)     # download waits for the step and checks its status
-                b.download(rec)
+                # upload, one graph step and download in one call (the host
+                # waits once, for the download, which checks the step status)
+                b.step_records(rec, 1, nodes)
         e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
         trials.append(whole_job_rate(ws, n, args.steps, e2e_s))
     e2e = sorted(trials)[1]
@@ -439,8 +439,9 @@ def run_ours(args, ws, rank, local):
     # baselines, then the batched and adjoint parts of the metric last; the
     # per-leg detail goes to args.detail.
     detail = {'e2e_trials': trials,
-              'e2e_timing': 'host wall clock around upload (pinned records), one graph step '
-                            'launch and download (waits, checks the step status), per step; '
+              'e2e_timing': 'host wall clock around cd_step_records per step: upload of the '
+                            'pinned records, one graph step and download, enqueued together '
+                            '(the call waits for the download and checks the step status); '
                             'median of 3 passes',
               'roofline_work': 'achieved counts the float64 operations whose results the state '
                                'depends on (branch-exact for the state); reference_algorithm '

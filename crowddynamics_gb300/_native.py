@@ -35,7 +35,7 @@ SNAPSHOT_SLOTS = 8
 #: Exported entry points (every function declared in include/cdgpu.h).
 SYMBOLS = (
     'cd_last_error', 'cd_create', 'cd_destroy', 'cd_upload_agents',
-    'cd_download_agents', 'cd_set_walls', 'cd_set_noise', 'cd_step', 'cd_run',
+    'cd_download_agents', 'cd_step_records', 'cd_set_walls', 'cd_set_noise', 'cd_step', 'cd_run',
     'cd_synchronize', 'cd_get_time', 'cd_get_cell_list', 'cd_pair_counts',
     'cd_sizes', 'cd_set_timing', 'cd_kernel_time', 'cd_kernels_per_step',
     'cd_measure_fp64_peak', 'cd_agent_agent_noalloc', 'cd_variant_count',
@@ -96,6 +96,7 @@ def load(path=None):
         'cd_destroy': (None, [P]),
         'cd_upload_agents': (ctypes.c_int, [P, P, i64, i64, pi64]),
         'cd_download_agents': (ctypes.c_int, [P, P, i64, i64, pi64]),
+        'cd_step_records': (ctypes.c_int, [P, P, i64, i64, pi64, ctypes.c_int, i64]),
         'cd_set_walls': (ctypes.c_int, [P, P, i64]),
         'cd_set_noise': (ctypes.c_int, [P, P, P]),
         'cd_step': (ctypes.c_int, [P, ctypes.c_int, pd]),

@@ -759,8 +759,21 @@ void cd_destroy(cd_ctx *ctx) {
     delete ctx;
 }
 
+namespace {
+int upload_records(cd_ctx *c, const void *records, int64_t n, int64_t itemsize,
+                   const int64_t *off, bool wait_read);
+}
+
 int cd_upload_agents(cd_ctx *c, const void *records, int64_t n, int64_t itemsize,
                      const int64_t *off) {
+    return upload_records(c, records, n, itemsize, off, true);
+}
+
+namespace {
+// `wait_read`: return once the records have been read (cd_upload_agents);
+// cd_step_records does not wait, since it returns only after the download.
+int upload_records(cd_ctx *c, const void *records, int64_t n, int64_t itemsize,
+                   const int64_t *off, bool wait_read) {
     if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
     if (n != c->n) return fail(c, CD_ERR_INVALID_VALUE, "agent count differs from the context");
     if (itemsize <= 0 || !off || (n > 0 && !records))
@@ -832,12 +845,13 @@ int cd_upload_agents(cd_ctx *c, const void *records, int64_t n, int64_t itemsize
     c->have_records = true;
     // The caller may reuse `records` once this returns: wait for the read of
     // them, not for the extent reduction behind it.
-    if (n > 0) CUDA_OR_FAIL(c, cudaEventSynchronize(c->ev_read));
+    if (n > 0 && wait_read) CUDA_OR_FAIL(c, cudaEventSynchronize(c->ev_read));
     // Wall bins depend on the agents' extent: the first upload sizes them.
     if (c->extent_max.empty())
         if (int rc = absorb_extent(c)) return rc;
     return CD_OK;
 }
+}  // namespace
 
 int cd_download_agents(cd_ctx *c, void *records, int64_t n, int64_t itemsize, const int64_t *off) {
     if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
@@ -865,6 +879,17 @@ int cd_download_agents(cd_ctx *c, void *records, int64_t n, int64_t itemsize, co
     if (int rc = enqueue_status(c)) return rc;
     CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
     return check_device_error(c, true);
+}
+
+int cd_step_records(cd_ctx *c, void *records, int64_t n, int64_t itemsize, const int64_t *off,
+                    int nodes, int64_t steps) {
+    if (!c) return fail(nullptr, CD_ERR_INVALID_VALUE, "ctx is NULL");
+    if (steps < 0) return fail(c, CD_ERR_INVALID_VALUE, "negative step count");
+    // everything enqueued at once: the records are read, stepped and written
+    // back without the host waiting in between
+    if (int rc = upload_records(c, records, n, itemsize, off, false)) return rc;
+    if (int rc = cd_launch(c, nodes, steps)) return rc;
+    return cd_download_agents(c, records, n, itemsize, off);
 }
 
 int cd_set_direct_host_access(cd_ctx *c, int enable) {

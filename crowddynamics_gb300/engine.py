@@ -136,6 +136,19 @@ class DeviceBatch:
                                                records.dtype.itemsize,
                                                _offsets_arg(records.dtype)))
 
+    def step_records(self, records, steps=1, nodes=N.NODE_ALL & ~N.NODE_FLUCTUATION):
+        """``steps`` steps of the host ``records`` in place: upload, graph
+        steps and download in one call (cd_step_records), the drop-in form of
+        the reference's update() on a host array."""
+        if body_type_of(records) != self.body_code:
+            raise InvalidType('agent dtype does not match the context body type')
+        if not records.flags.c_contiguous or not records.flags.writeable:
+            raise InvalidValue('agent array must be C-contiguous and writeable')
+        self._offsets = field_offsets(records.dtype)
+        self._chk(self._lib.cd_step_records(self._ctx, records.ctypes.data, len(records),
+                                            records.dtype.itemsize, _offsets_arg(records.dtype),
+                                            int(nodes), int(steps)))
+
     def snapshot(self, slot, records, dt=None, time_tot=None):
         """Enqueue an asynchronous copy of the state (after the steps already
         enqueued) into ``records`` and the per-scenario ``dt`` / ``time_tot``

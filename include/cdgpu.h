@@ -133,6 +133,12 @@ int cd_upload_agents(cd_ctx *ctx, const void *records, int64_t n,
  * last cd_upload_agents. */
 int cd_download_agents(cd_ctx *ctx, void *records, int64_t n, int64_t itemsize,
                        const int64_t *field_offsets);
+/* `steps` graph steps of the host records in place: cd_upload_agents,
+ * cd_launch and cd_download_agents in one call, enqueued together (the host
+ * does not wait between them; the records must not be touched until it
+ * returns).  The drop-in form of the reference's update() on a host array. */
+int cd_step_records(cd_ctx *ctx, void *records, int64_t n, int64_t itemsize,
+                    const int64_t *field_offsets, int nodes, int64_t steps);
 /* Host records in pinned (page-locked, device-mapped) memory are read and
  * written by the device directly, copy and transpose in one kernel pass;
  * other host memory goes through a staged copy.  Both give the same bytes.

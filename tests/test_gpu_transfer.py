@@ -104,3 +104,25 @@ def test_direct_upload_round_trip(native):
     b.close()
     assert back.tobytes() == scen.agents.tobytes()
     del keep, keep2
+
+
+@pytest.mark.parametrize('pinned', [True, False])
+def test_step_records_matches_upload_run_download(native, pinned):
+    """cd_step_records (upload, graph steps and download in one call, the
+    host not waiting in between) gives the records of cd_upload_agents,
+    cd_run and cd_download_agents, byte for byte, over three calls."""
+    scen = S.room(n=1500, seed=12)
+    recs = scen.agents.copy()
+    if pinned:
+        recs, keep = pinned_like(recs)
+    b1, _, _ = batch_from_scenarios([scen])
+    b2, _, _ = batch_from_scenarios([scen])
+    ref = scen.agents.copy()
+    for _ in range(3):
+        b1.step_records(recs, 2, NODES)
+        b2.upload(ref)
+        b2.run(2, NODES)
+        b2.download(ref)
+        assert recs.tobytes() == ref.tobytes()
+    b1.close()
+    b2.close()
