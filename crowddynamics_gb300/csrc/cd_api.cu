@@ -393,7 +393,8 @@ int alloc_near_lists(cd_ctx *c, int64_t cap) {
     if (cap > 0) {
         if (int rc = dalloc(c, &c->nl_idx, cap)) return rc;
         if (int rc = dalloc(c, &c->nl_res, cap * res_d)) return rc;
-        if (int rc = dalloc(c, &c->nl_kind, cap)) return rc;
+        // 16 bytes past the last entry: the gather reads the kinds in 4-byte words
+        if (int rc = dalloc(c, &c->nl_kind, cap + 16)) return rc;
         if (int rc = dalloc(c, &c->fw_pairs, cap)) return rc;
         if (int rc = dalloc(c, &c->defer_list, cap)) return rc;
         const int64_t job_q = c->body == CD_BODY_CIRCULAR ? cdk::JOB_Q_CIRC : cdk::JOB_Q_TC;

@@ -2840,8 +2840,95 @@ __global__ void __launch_bounds__(128) k_prologue(StepArgs a) {
         prologue_agent<BODY>(a, i);
 }
 
+// Bytes j of a 4-byte word of kinds with lo <= j < hi (0xff each).
+__device__ __forceinline__ unsigned byte_keep(int lo, int hi) {
+    unsigned m = 0xffffffffu;
+    if (lo > 0) m = m << (8 * lo);                   // lo <= 3: the word holds entry lo
+    if (hi < 4) m &= 0xffffffffu >> (8 * (4 - hi));  // hi >= 1: the word holds entry hi - 1
+    return m;
+}
+
+// Adds agent s's near-list results to (fx, fy, tq) in list order, the lanes
+// of `lanes` (every lane of the warp running an agent) together.  Each lane
+// walks its kind bytes four at a time (the next word loaded while one is
+// read) to its next force entry with integer work alone, so that the float64
+// adds run once per force entry of the lane with the most, not once per entry
+// of any lane.  Entries without a force between two forces act once: each
+// turns a -0 force component into +0 (what adding +0 does), which is
+// idempotent, and the torque they would need the exact sign of is the same
+// for all of them.  Returns false when the torque is -0 at such an entry (the
+// agent is left to the exact pass).  The kinds array has 16 bytes of padding,
+// so the word holding the last entry is inside it.
+template <int BODY>
+__device__ __forceinline__ bool add_entries(const StepArgs &a, const int s, const unsigned lanes,
+                                            double &fx, double &fy, double &tq) {
+    constexpr long long NEG_ZERO = (long long)0x8000000000000000ULL;
+    const double4_32a *res = reinterpret_cast<const double4_32a *>(a.nl_res);
+    const unsigned *kw = reinterpret_cast<const unsigned *>(a.nl_kind);
+    const int o0 = a.nl_off[s], o1 = a.nl_off[s + 1];
+    int w = o0 >> 2;
+    const int wend = (o1 + 3) >> 2;                  // words holding entries o0 .. o1 - 1
+    unsigned fm = 0, zm = 0, nk = 0;                 // force / zero bytes left in word w
+    if (w < wend) {
+        const unsigned k = __ldg(kw + w);
+        if (w + 1 < wend) nk = __ldg(kw + w + 1);
+        const unsigned keep = byte_keep(o0 - 4 * w, o1 - 4 * w);
+        fm = __vcmpeq4(k, 0x03030303u) & keep;      // KIND_FORCE
+        zm = __vcmpeq4(k, 0x01010101u) & keep;      // KIND_ZERO
+    }
+    bool ok = true;
+    for (;;) {
+        int e = -1;                                  // the lane's next force entry
+        for (;;) {
+            if (fm) {
+                const int b = __ffs(fm) - 1;         // its byte's lowest bit
+                const unsigned thru = ((1u << b) - 1u) | (0xffu << b);
+                if (zm & ((1u << b) - 1u)) {         // entries without a force before it
+                    if (__double_as_longlong(fx) == NEG_ZERO) fx = 0.0;
+                    if (__double_as_longlong(fy) == NEG_ZERO) fy = 0.0;
+                    if (BODY == 1 && __double_as_longlong(tq) == NEG_ZERO) {
+                        ok = false;
+                        fm = zm = 0;
+                        w = wend;
+                        break;
+                    }
+                }
+                fm &= ~thru;
+                zm &= ~thru;
+                e = 4 * w + (b >> 3);
+                break;
+            }
+            if (zm) {
+                if (__double_as_longlong(fx) == NEG_ZERO) fx = 0.0;
+                if (__double_as_longlong(fy) == NEG_ZERO) fy = 0.0;
+                zm = 0;
+                if (BODY == 1 && __double_as_longlong(tq) == NEG_ZERO) {
+                    ok = false;
+                    fm = 0;
+                    w = wend;
+                    break;
+                }
+            }
+            if (++w >= wend) break;
+            const unsigned k = nk;
+            if (w + 1 < wend) nk = __ldg(kw + w + 1);
+            const unsigned keep = byte_keep(o0 - 4 * w, o1 - 4 * w);
+            fm = __vcmpeq4(k, 0x03030303u) & keep;
+            zm = __vcmpeq4(k, 0x01010101u) & keep;
+        }
+        if (!__any_sync(lanes, e >= 0)) return ok;
+        if (e >= 0) {
+            const double4_32a v = res[e];
+            fx = fx + v.x;
+            fy = fy + v.y;
+            if (BODY == 1) tq = tq + v.z;
+        }
+    }
+}
+
 template <int BODY, bool EXACT>
-__device__ __forceinline__ void gather_agent(const StepArgs &a, const int s, const int i) {
+__device__ __forceinline__ void gather_agent(const StepArgs &a, const int s, const int i,
+                                             const unsigned lanes = 0u) {
     const int sid = a.scen_of[i];
     const ScenDev sc = a.scen[sid];
     const float4 me = a.cull[s];
@@ -2853,7 +2940,12 @@ __device__ __forceinline__ void gather_agent(const StepArgs &a, const int s, con
     } else {
         agent_prologue<BODY>(a, i, fx, fy, tq, phi0);
     }
-    if (a.nodes & N_AGENT) {
+    if (!EXACT && (a.nodes & N_AGENT)) {
+        if (!add_entries<BODY>(a, s, lanes, fx, fy, tq)) {
+            a.fix_list[atomicAdd(a.fix_count, 1)] = s;
+            return;
+        }
+    } else if (a.nodes & N_AGENT) {
         const double4_32a *res = reinterpret_cast<const double4_32a *>(a.nl_res);
         const int o1 = a.nl_off[s + 1];
         constexpr long long NEG_ZERO = (long long)0x8000000000000000ULL;
@@ -2893,7 +2985,9 @@ __global__ void __launch_bounds__(GATHER_NT, 24) k_forces_gather(StepArgs a) {
     // (launched in one-warp blocks: the float64 epilogue spreads evenly
     // over the SMs)
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < a.n) gather_agent<BODY, false>(a, s, a.perm[s]);
+    const int left = a.n - blockIdx.x * blockDim.x;       // agents from this warp's first
+    const unsigned lanes = left >= 32 ? 0xffffffffu : (1u << left) - 1u;
+    if (s < a.n) gather_agent<BODY, false>(a, s, a.perm[s], lanes);
 }
 
 // The lane-group kernel, for a step whose near lists exceeded the capacity.
