@@ -2000,9 +2000,9 @@ constexpr size_t NA_OFF_STAGEF = NA_OFF_CULL + na_align(sizeof(float4) * NA_N);
 constexpr size_t NA_OFF_VMAX = NA_OFF_STAGEF + na_align(sizeof(float4) * 2 * NA_N);
 constexpr size_t NA_OFF_ERR = NA_OFF_VMAX + na_align(sizeof(unsigned long long));
 constexpr size_t NA_OFF_WORK = NA_OFF_ERR + na_align(sizeof(int));
-// StepArgs::work holds two ints (the force kernel's work counter and the
-// float32 pair pass's deferred count)
-constexpr size_t NA_BYTES = NA_OFF_WORK + na_align(2 * sizeof(int));
+// StepArgs::work holds four ints (the force kernel's work counter, the
+// float32 pair pass's deferred count, the force pass's two job counts)
+constexpr size_t NA_BYTES = NA_OFF_WORK + na_align(4 * sizeof(int));
 static_assert(NA_BYTES < (4u << 20), "allocation-free scratch stays below 4 MiB");
 
 __device__ __align__(256) static unsigned char g_noalloc_scratch[NA_BYTES];

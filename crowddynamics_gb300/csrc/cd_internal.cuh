@@ -88,7 +88,8 @@ struct StepArgs {
     double *dt, *time_tot;       // per scenario
     int *err;
     int *work;                   // [0] force-kernel work counter (zeroed per launch),
-                                 // [1] pairs the float32 pair pass left to k_pairs
+                                 // [1] pairs the float32 pair pass left to k_pairs,
+                                 // [2] / [3] force-pass jobs without / with contact
     int *fix_count, *fix_list;   // agents the gather leaves to k_forces_fallback
     int *slot_of;                // per agent: its cell-sorted slot (k_rank)
     double *pro;                 // per agent PRO_D doubles: prologue fx, fy, torque, phi0;
