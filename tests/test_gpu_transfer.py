@@ -126,3 +126,15 @@ def test_step_records_matches_upload_run_download(native, pinned):
         assert recs.tobytes() == ref.tobytes()
     b1.close()
     b2.close()
+
+
+def test_step_records_without_steps_round_trips(native):
+    """cd_step_records with no steps uploads and downloads the records:
+    they come back byte for byte."""
+    scen = S.hallway(n=700, seed=21)
+    recs, keep = pinned_like(scen.agents)
+    before = recs.tobytes()
+    b, _, _ = batch_from_scenarios([scen])
+    b.step_records(recs, 0, NODES)
+    assert recs.tobytes() == before
+    b.close()
