@@ -73,6 +73,10 @@ struct cd_ctx {
     double *v0max = nullptr, *dt = nullptr, *time_tot = nullptr;
     double *ext = nullptr, *max_partial = nullptr;      // per-scenario max extent, scratch
     double *ext_host = nullptr;                        // pinned copy of ext
+    // the direct upload's per-scenario maxima: two order keys per scenario
+    // and the kernel's block counter, zero between uploads
+    unsigned long long *max_key = nullptr;
+    int *max_done = nullptr;
     int *status_host = nullptr;                        // pinned: error word, near-list need
     int *err = nullptr, *work = nullptr;
     int *diag = nullptr;
@@ -245,6 +249,8 @@ void release(cd_ctx *c) {
     for (cudaEvent_t e : c->evsnap)
         if (e) cudaEventDestroy(e);
     if (c->ext_host) cudaFreeHost(c->ext_host);
+    if (c->max_key) cudaFree(c->max_key);
+    if (c->max_done) cudaFree(c->max_done);
     if (c->status_host) cudaFreeHost(c->status_host);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->stream2) cudaStreamDestroy(c->stream2);
@@ -689,6 +695,11 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->vmax, n_scenarios));
     step(dalloc(c, &c->v0max, n_scenarios));
     step(dalloc(c, &c->ext, n_scenarios));
+    step(dalloc(c, &c->max_key, 2 * (int64_t)n_scenarios));
+    step(dalloc(c, &c->max_done, 1));
+    if (rc == CD_OK && (cudaMemset(c->max_key, 0, sizeof(unsigned long long) * 2 * std::max<int64_t>(n_scenarios, 1)) != cudaSuccess ||
+                        cudaMemset(c->max_done, 0, sizeof(int)) != cudaSuccess))
+        rc = fail(c, CD_ERR_CUDA, "cudaMemset failed");
     step(dalloc(c, &c->max_partial, cdk::scen_max_partials((int)n_scenarios)));
     if (rc == CD_OK && cudaMallocHost((void **)&c->ext_host, sizeof(double) * n_scenarios) != cudaSuccess)
         rc = fail(c, CD_ERR_CUDA, "cudaMallocHost failed");
@@ -816,6 +827,7 @@ int upload_records(cd_ctx *c, const void *records, int64_t n, int64_t itemsize,
     }
     c->itemsize = itemsize;
     std::memcpy(c->off, off, sizeof(int64_t) * CD_F_COUNT);
+    bool maxima_done = false;
     if (n > 0) {
         long long offl[CD_F_COUNT];
         for (int k = 0; k < CD_F_COUNT; ++k) offl[k] = off[k];
@@ -824,9 +836,13 @@ int upload_records(cd_ctx *c, const void *records, int64_t n, int64_t itemsize,
                              : nullptr;
         const cdk::StateOffsets so = state_offsets(off, itemsize);
         if (dv) {
+            // the per-scenario maxima in the same pass
+            const cdk::ScenMax mx{c->max_key, c->max_done, c->scen_of, c->v0max, c->ext,
+                                  (int)c->nscen, c->body == CD_BODY_CIRCULAR ? 0 : 1};
             cdk::launch_records_in(dv, c->aos, itemsize, offl, (int)n, c->body, c->col, so,
-                                   state_cols(c), c->stream);
+                                   state_cols(c), c->stream, mx);
             CUDA_OR_FAIL(c, cudaEventRecord(c->ev_read, c->stream));
+            maxima_done = true;
         } else {
             CUDA_OR_FAIL(c, cudaMemcpyAsync(c->aos, records, bytes, cudaMemcpyHostToDevice,
                                             c->stream));
@@ -836,8 +852,10 @@ int upload_records(cd_ctx *c, const void *records, int64_t n, int64_t itemsize,
         }
         c->states_dirty = false;
     }
-    StepArgs a = args_of(c, 0);
-    cdk::launch_scen_max(a, c->v0max, c->ext, c->max_partial, c->stream);
+    if (!maxima_done) {
+        StepArgs a = args_of(c, 0);
+        cdk::launch_scen_max(a, c->v0max, c->ext, c->max_partial, c->stream);
+    }
     CUDA_OR_FAIL(c, cudaMemcpyAsync(c->ext_host, c->ext, sizeof(double) * c->nscen,
                                     cudaMemcpyDeviceToHost, c->stream));
     CUDA_OR_FAIL(c, cudaEventRecord(c->ev_ext, c->stream));

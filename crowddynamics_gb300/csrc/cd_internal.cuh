@@ -307,10 +307,21 @@ void launch_soa_to_aos(char *aos, long long itemsize, const long long *off,
 // records for the fields the step does not write).  0 records per block:
 // records too large for shared memory, use the staged path.
 int records_per_block(long long itemsize);
+// The per-scenario maxima an upload leaves (launch_scen_max's results),
+// reduced by launch_records_in in its own pass when `key` is set: `key` holds
+// two order keys per scenario (zero between uploads), `blocks_done` one
+// counter (zero between uploads).
+struct ScenMax {
+    unsigned long long *key;
+    int *blocks_done;
+    const int *scen_of;
+    double *v0max, *ext;
+    int n_scen, body;
+};
 // launch_records_in also fills the state columns (as launch_states_in).
 void launch_records_in(const void *src, char *aos, long long itemsize, const long long *off,
                        int n, int body, double *const *col, const StateOffsets &so,
-                       const StateCols &sc, cudaStream_t s);
+                       const StateCols &sc, cudaStream_t s, const ScenMax &mx);
 void launch_records_out(void *dst, const char *aos, long long itemsize, const long long *off,
                         int n, int body, const double *const *col, cudaStream_t s);
 double fp64_peak_gflops();

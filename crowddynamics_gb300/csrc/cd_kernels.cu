@@ -314,12 +314,14 @@ __device__ __forceinline__ double extent_tc(double x, double y, double xl, doubl
 
 // Wall-binning extent of an agent: ThreeCircle also counts r_ts + r_s, the
 // shoulders' reach at any orientation.
-__device__ __forceinline__ double agent_extent(const StepArgs &a, int i) {
-    double *const *c = a.col;
-    if (a.body == 0) return c[R][i];
+__device__ __forceinline__ double extent_of(double *const *c, int body, int i) {
+    if (body == 0) return c[R][i];
     const double e = extent_tc(c[X][i], c[Y][i], c[XLS][i], c[YLS][i], c[XRS][i], c[YRS][i],
                                c[RT][i], c[RS][i]);
     return fmax(e, c[RTS][i] + c[RS][i]);
+}
+__device__ __forceinline__ double agent_extent(const StepArgs &a, int i) {
+    return extent_of(a.col, a.body, i);
 }
 
 __global__ void k_scen_max_partial(StepArgs a, double *partial) {
@@ -3264,9 +3266,30 @@ __device__ __forceinline__ void states_of_record(const char *rec, const StateOff
 constexpr int XFER_NT = 256;
 struct XferTable { int n; int word[40]; int col[40]; };   // field word offset, column
 
+// A float64 as a key whose unsigned order is the numbers' order (-inf lowest,
+// +inf highest, -0 below +0); 0 is no number, ~0 a NaN.
+__device__ __forceinline__ unsigned long long order_key(double v) {
+    if (isnan(v)) return ~0ull;
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double key_value(unsigned long long k, double none) {
+    if (k == 0ull) return none;
+    if (k == ~0ull) return __longlong_as_double(0x7ff8000000000000LL);
+    return __longlong_as_double((long long)((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k));
+}
+
+__device__ __forceinline__ unsigned long long shfl_max64(unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xffffffffu, v, o);
+        v = t > v ? t : v;
+    }
+    return v;
+}
+
 __global__ void __launch_bounds__(XFER_NT)
 k_records_in(const unsigned *__restrict__ src, unsigned *__restrict__ copy, int wpr, int per_block,
-             int n, XferTable t, ColPtrs cols, StateOffsets so, StateCols sc) {
+             int n, XferTable t, ColPtrs cols, StateOffsets so, StateCols sc, ScenMax mx) {
     extern __shared__ __align__(16) unsigned rec_sm[];
     const int i0 = blockIdx.x * per_block;
     const int nrec = min(per_block, n - i0);
@@ -3309,6 +3332,70 @@ k_records_in(const unsigned *__restrict__ src, unsigned *__restrict__ copy, int 
     // the integer and bool state fields, from the same shared copy
     for (int r = threadIdx.x; r < nrec; r += XFER_NT)
         states_of_record(reinterpret_cast<const char *>(rec_sm + r * wpr), so, sc, i0 + r);
+    if (!mx.key) return;
+    // Per scenario: the largest target speed (a NaN wins) and the largest
+    // finite extent, as order keys reduced per block (a max is exact in any
+    // order), then one atomic per block and scenario; the last block to
+    // finish writes them out as numbers and clears the keys for the next
+    // upload.  The kernel waits on the host link: this work is hidden.
+    __syncthreads();                                   // the block's columns are written
+    __shared__ unsigned long long kv[XFER_NT / 32], ke[XFER_NT / 32];
+    __shared__ int ks[XFER_NT / 32], last;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned long long v = 0ull, e = 0ull;
+    int sid = -1;
+    if (threadIdx.x < nrec) {
+        const int i = i0 + threadIdx.x;
+        sid = mx.scen_of[i];
+        v = order_key(cols.p[V0][i]);
+        const double x = extent_of(cols.p, mx.body, i);
+        e = isfinite(x) ? order_key(x) : 0ull;
+    }
+    const int s0 = __shfl_sync(0xffffffffu, sid, 0);
+    if (__all_sync(0xffffffffu, sid == s0 || sid < 0)) {
+        v = shfl_max64(v);
+        e = shfl_max64(e);
+        if (lane == 0) { kv[w] = v; ke[w] = e; ks[w] = s0; }
+    } else {
+        if (sid >= 0) {
+            atomicMax(&mx.key[2 * sid], v);
+            atomicMax(&mx.key[2 * sid + 1], e);
+        }
+        if (lane == 0) ks[w] = -1;
+    }
+    __threadfence();                                   // these atomics before the count below
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int nw = (nrec + 31) / 32;
+        int cur = -1;
+        unsigned long long cv = 0ull, ce = 0ull;
+        for (int k = 0; k < nw; ++k) {                 // runs of warps of one scenario
+            if (ks[k] != cur && cur >= 0) {
+                atomicMax(&mx.key[2 * cur], cv);
+                atomicMax(&mx.key[2 * cur + 1], ce);
+                cv = 0ull; ce = 0ull;
+            }
+            cur = ks[k];
+            if (cur >= 0) { cv = kv[k] > cv ? kv[k] : cv; ce = ke[k] > ce ? ke[k] : ce; }
+        }
+        if (cur >= 0) {
+            atomicMax(&mx.key[2 * cur], cv);
+            atomicMax(&mx.key[2 * cur + 1], ce);
+        }
+        __threadfence();
+        last = atomicAdd(mx.blocks_done, 1) == (int)gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int k = threadIdx.x; k < mx.n_scen; k += XFER_NT) {
+        const unsigned long long kvk = atomicExch(&mx.key[2 * k], 0ull);
+        const unsigned long long kek = atomicExch(&mx.key[2 * k + 1], 0ull);
+        mx.v0max[k] = key_value(kvk, -INFINITY);
+        const double ek = key_value(kek, 0.0);
+        mx.ext[k] = ek > 0.0 ? ek : 0.0;
+    }
+    if (threadIdx.x == 0) *mx.blocks_done = 0;
 }
 
 __global__ void __launch_bounds__(XFER_NT)
@@ -3772,14 +3859,14 @@ static XferTable xfer_table(const long long *off, int body, bool outputs_only) {
 
 void launch_records_in(const void *src, char *aos, long long itemsize, const long long *off,
                        int n, int body, double *const *col, const StateOffsets &so,
-                       const StateCols &sc, cudaStream_t s) {
+                       const StateCols &sc, cudaStream_t s, const ScenMax &mx) {
     const int per = records_per_block(itemsize);
     if (n <= 0 || per <= 0) return;
     ColPtrs c;
     for (int k = 0; k < NCOL; ++k) c.p[k] = col[k];
     k_records_in<<<nblk(n, per), XFER_NT, (size_t)per * itemsize, s>>>(
         static_cast<const unsigned *>(src), reinterpret_cast<unsigned *>(aos), (int)(itemsize / 4),
-        per, n, xfer_table(off, body, false), c, so, sc);
+        per, n, xfer_table(off, body, false), c, so, sc, mx);
 }
 
 void launch_records_out(void *dst, const char *aos, long long itemsize, const long long *off,

@@ -138,3 +138,35 @@ def test_step_records_without_steps_round_trips(native):
     b.step_records(recs, 0, NODES)
     assert recs.tobytes() == before
     b.close()
+
+
+def test_direct_upload_maxima_across_scenarios(native):
+    """The direct upload reduces each scenario's largest target speed and
+    extent in its own pass (per block of records, blocks that straddle
+    scenarios included); the steps after it match those after a staged
+    upload byte for byte, dt and time included."""
+    sizes = [37, 64, 5, 129, 200, 1, 77, 300, 63, 65]
+    scens = [S.hallway(n=n, seed=30 + k) for k, n in enumerate(sizes)]
+    for k, sc in enumerate(scens):                 # distinct maxima per scenario
+        sc.agents['target_velocity'] *= 1.0 + 0.1 * k
+    bd, agents, _ = batch_from_scenarios(scens)
+    bs, _, _ = batch_from_scenarios(scens)
+    pinned, keep = pinned_like(agents)
+    bd.set_direct_host_access(True)
+    bs.set_direct_host_access(False)
+    for _ in range(2):                             # the second upload reuses the keys
+        c_upload(bd, pinned)
+        c_upload(bs, agents.copy())
+        bd.run(3, NODES)
+        bs.run(3, NODES)
+        od, os_ = np.zeros_like(agents), np.zeros_like(agents)
+        bd.download(od)
+        bs.download(os_)
+        assert od.tobytes() == os_.tobytes()
+        for x, y in zip(bd.time(), bs.time()):
+            assert x.tobytes() == y.tobytes()
+        pinned[:] = od
+        agents = od.copy()
+    bd.close()
+    bs.close()
+    del keep
