@@ -78,6 +78,9 @@ struct cd_ctx {
     unsigned long long *max_key = nullptr;
     int *max_done = nullptr;
     int *status_host = nullptr;                        // pinned: error word, near-list need
+    // device views of ext_host and status_host (null: copied by the stream)
+    double *ext_host_dev = nullptr;
+    int *status_host_dev = nullptr;
     int *err = nullptr, *work = nullptr;
     int *diag = nullptr;
     // near lists of the compute-once pair pipeline (entries allocated on use)
@@ -705,6 +708,16 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
         rc = fail(c, CD_ERR_CUDA, "cudaMallocHost failed");
     if (rc == CD_OK && cudaMallocHost((void **)&c->status_host, sizeof(int) * 2) != cudaSuccess)
         rc = fail(c, CD_ERR_CUDA, "cudaMallocHost failed");
+    if (rc == CD_OK) {
+        // the transfer kernels write these two directly where the device can
+        // address them; otherwise small copies on the stream do
+        if (cudaHostGetDevicePointer((void **)&c->ext_host_dev, c->ext_host, 0) != cudaSuccess ||
+            cudaHostGetDevicePointer((void **)&c->status_host_dev, c->status_host, 0) != cudaSuccess) {
+            c->ext_host_dev = nullptr;
+            c->status_host_dev = nullptr;
+            cudaGetLastError();
+        }
+    }
     step(dalloc(c, &c->dt, n_scenarios));
     step(dalloc(c, &c->time_tot, n_scenarios));
     step(dalloc(c, &c->err, 1));
@@ -837,7 +850,8 @@ int upload_records(cd_ctx *c, const void *records, int64_t n, int64_t itemsize,
         const cdk::StateOffsets so = state_offsets(off, itemsize);
         if (dv) {
             // the per-scenario maxima in the same pass
-            const cdk::ScenMax mx{c->max_key, c->max_done, c->scen_of, c->v0max, c->ext,
+            const cdk::ScenMax mx{c->max_key,    c->max_done,  c->scen_of,
+                                  c->v0max,      c->ext,       c->ext_host_dev,
                                   (int)c->nscen, c->body == CD_BODY_CIRCULAR ? 0 : 1};
             cdk::launch_records_in(dv, c->aos, itemsize, offl, (int)n, c->body, c->col, so,
                                    state_cols(c), c->stream, mx);
@@ -856,8 +870,9 @@ int upload_records(cd_ctx *c, const void *records, int64_t n, int64_t itemsize,
         StepArgs a = args_of(c, 0);
         cdk::launch_scen_max(a, c->v0max, c->ext, c->max_partial, c->stream);
     }
-    CUDA_OR_FAIL(c, cudaMemcpyAsync(c->ext_host, c->ext, sizeof(double) * c->nscen,
-                                    cudaMemcpyDeviceToHost, c->stream));
+    if (!maxima_done || !c->ext_host_dev)   // else the upload kernel wrote ext_host itself
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(c->ext_host, c->ext, sizeof(double) * c->nscen,
+                                        cudaMemcpyDeviceToHost, c->stream));
     CUDA_OR_FAIL(c, cudaEventRecord(c->ev_ext, c->stream));
     CUDA_OR_FAIL(c, cudaGetLastError());
     c->ext_pending = true;
@@ -888,14 +903,20 @@ int cd_download_agents(cd_ctx *c, void *records, int64_t n, int64_t itemsize, co
                    ? const_cast<void *>(device_view_of_host(records, n * itemsize))
                    : nullptr;
     if (dv) {
-        cdk::launch_records_out(dv, c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
+        // the download kernel also copies the status into status_host
+        const cdk::StepStatus st{c->err, (c->nl_cap > 0 && c->n > 0) ? c->nl_off + c->n : nullptr,
+                                 c->status_host_dev};
+        cdk::launch_records_out(dv, c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream,
+                                st);
+        if (!c->status_host_dev)
+            if (int rc = enqueue_status(c)) return rc;
     } else {
         cdk::launch_soa_to_aos(c->aos, itemsize, offl, (int)n, c->body, c->col, c->stream);
         CUDA_OR_FAIL(c, cudaMemcpyAsync(records, c->aos, n * itemsize, cudaMemcpyDeviceToHost,
                                         c->stream));
+        if (int rc = enqueue_status(c)) return rc;
     }
     CUDA_OR_FAIL(c, cudaGetLastError());
-    if (int rc = enqueue_status(c)) return rc;
     CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
     return check_device_error(c, true);
 }

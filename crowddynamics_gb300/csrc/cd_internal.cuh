@@ -316,14 +316,23 @@ struct ScenMax {
     int *blocks_done;
     const int *scen_of;
     double *v0max, *ext;
+    double *ext_host;            // page-locked copy of ext, written by the kernel too
     int n_scen, body;
+};
+// What the host reads after a download (the step status and the entries the
+// last near-list build needed), written into page-locked memory by
+// launch_records_out itself.
+struct StepStatus {
+    const int *err, *need;       // need: nl_off + n, or null without near lists
+    int *host;                   // [0] err, [1] need (0 without near lists)
 };
 // launch_records_in also fills the state columns (as launch_states_in).
 void launch_records_in(const void *src, char *aos, long long itemsize, const long long *off,
                        int n, int body, double *const *col, const StateOffsets &so,
                        const StateCols &sc, cudaStream_t s, const ScenMax &mx);
 void launch_records_out(void *dst, const char *aos, long long itemsize, const long long *off,
-                        int n, int body, const double *const *col, cudaStream_t s);
+                        int n, int body, const double *const *col, cudaStream_t s,
+                        const StepStatus &st);
 double fp64_peak_gflops();
 // Shared-memory bytes of the force kernel (dynamic) and one-time attributes.
 size_t forces_smem_bytes(int body, int variant);

@@ -3394,14 +3394,20 @@ k_records_in(const unsigned *__restrict__ src, unsigned *__restrict__ copy, int 
         mx.v0max[k] = key_value(kvk, -INFINITY);
         const double ek = key_value(kek, 0.0);
         mx.ext[k] = ek > 0.0 ? ek : 0.0;
+        if (mx.ext_host) mx.ext_host[k] = ek > 0.0 ? ek : 0.0;
     }
     if (threadIdx.x == 0) *mx.blocks_done = 0;
 }
 
 __global__ void __launch_bounds__(XFER_NT)
 k_records_out(unsigned *__restrict__ dst, const unsigned *__restrict__ base, int wpr,
-              int per_block, int n, XferTable t, ColPtrs cols) {
+              int per_block, int n, XferTable t, ColPtrs cols, StepStatus st) {
     extern __shared__ __align__(16) unsigned rec_sm[];
+    // the status the host reads once the download is complete
+    if (st.host && blockIdx.x == 0 && threadIdx.x == 0) {
+        st.host[0] = *st.err;
+        st.host[1] = st.need ? *st.need : 0;
+    }
     const int i0 = blockIdx.x * per_block;
     const int nrec = min(per_block, n - i0);
     const size_t w0 = (size_t)i0 * wpr;
@@ -3870,14 +3876,15 @@ void launch_records_in(const void *src, char *aos, long long itemsize, const lon
 }
 
 void launch_records_out(void *dst, const char *aos, long long itemsize, const long long *off,
-                        int n, int body, const double *const *col, cudaStream_t s) {
+                        int n, int body, const double *const *col, cudaStream_t s,
+                        const StepStatus &st) {
     const int per = records_per_block(itemsize);
     if (n <= 0 || per <= 0) return;
     ColPtrs c;
     for (int k = 0; k < NCOL; ++k) c.p[k] = const_cast<double *>(col[k]);
     k_records_out<<<nblk(n, per), XFER_NT, (size_t)per * itemsize, s>>>(
         static_cast<unsigned *>(dst), reinterpret_cast<const unsigned *>(aos), (int)(itemsize / 4),
-        per, n, xfer_table(off, body, true), c);
+        per, n, xfer_table(off, body, true), c, st);
 }
 
 double fp64_peak_gflops() {
