@@ -125,7 +125,8 @@ void cd_destroy(cd_ctx *ctx);
  * float64 fields must be 4-byte aligned; the integer and bool fields
  * (CD_F_TARGET and after) may sit at any offset.  Recomputes timestep maxima.
  * Returns once the records have been read: the caller may then reuse them.
- * The per-scenario maxima are computed behind that on the context stream. */
+ * The per-scenario maxima are computed on the context stream: by the same
+ * pass that reads page-locked records, else behind the staged copy. */
 int cd_upload_agents(cd_ctx *ctx, const void *records, int64_t n,
                      int64_t itemsize, const int64_t *field_offsets);
 /* Write the device state back into `n` packed host records.  Whole records
