@@ -700,8 +700,9 @@ int cd_create(cd_ctx **out, int body_type, int64_t n_scenarios, const cd_scenari
     step(dalloc(c, &c->ext, n_scenarios));
     step(dalloc(c, &c->max_key, 2 * (int64_t)n_scenarios));
     step(dalloc(c, &c->max_done, 1));
-    if (rc == CD_OK && (cudaMemset(c->max_key, 0, sizeof(unsigned long long) * 2 * std::max<int64_t>(n_scenarios, 1)) != cudaSuccess ||
-                        cudaMemset(c->max_done, 0, sizeof(int)) != cudaSuccess))
+    if (rc == CD_OK &&
+        (cudaMemset(c->max_key, 0, sizeof(unsigned long long) * 2 * n_scenarios) != cudaSuccess ||
+         cudaMemset(c->max_done, 0, sizeof(int)) != cudaSuccess))
         rc = fail(c, CD_ERR_CUDA, "cudaMemset failed");
     step(dalloc(c, &c->max_partial, cdk::scen_max_partials((int)n_scenarios)));
     if (rc == CD_OK && cudaMallocHost((void **)&c->ext_host, sizeof(double) * n_scenarios) != cudaSuccess)
