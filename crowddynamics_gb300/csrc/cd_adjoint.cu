@@ -474,7 +474,11 @@ __global__ void __launch_bounds__(NT) k_adj_pairs(StepArgs a, AdjArgs q) {
 // (those marked present)
 // and walls r, r + L, ...; the lanes' sums meet in a fixed butterfly, so the
 // result is deterministic.  One lane per agent left 5000 agents with one warp
-// per SM, each lane walking about a hundred 48-byte entries in turn.
+// per SM, each lane walking about a hundred 48-byte entries in turn.  Each
+// lane steps over its empty entries with integer work alone and the warp's
+// lanes add their next present entries together, so that the six float64
+// adds run once per present entry of the lane with the most, not at every
+// entry where any lane has one (each lane keeps its own order).
 template <int L>
 __global__ void __launch_bounds__(NT) k_adj_gather(StepArgs a, AdjArgs q) {
     pdl_enter();
@@ -485,17 +489,26 @@ __global__ void __launch_bounds__(NT) k_adj_gather(StepArgs a, AdjArgs q) {
     PairGrad G{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     int i = 0;
     double uxi = 0.0, uyi = 0.0;
+    int e = 0, o1 = 0;
     if (valid) {
-        i = a.perm[s];
-        const int o1 = a.nl_off[s + 1];
-        for (int e = a.nl_off[s] + r; e < o1; e += L) {
-            if (!a.nl_kind[e]) continue;                    // a pair without a force
+        e = a.nl_off[s] + r;
+        o1 = a.nl_off[s + 1];
+    }
+    for (;;) {
+        while (e < o1 && !a.nl_kind[e]) e += L;         // pairs without a force
+        const bool has = e < o1;
+        if (!__any_sync(0xffffffffu, has)) break;
+        if (has) {
             const double2 *p = reinterpret_cast<const double2 *>(a.nl_res + (size_t)e * ADJ_RES_D);
             const double2 x = p[0], v = p[1], kt = p[2];
             G.gxx += x.x; G.gxy += x.y;
             G.gvx += v.x; G.gvy += v.y;
             G.gk += kt.x; G.gt0 += kt.y;
+            e += L;
         }
+    }
+    if (valid) {
+        i = a.perm[s];
         uxi = q.lF[2 * i];
         uyi = q.lF[2 * i + 1];
         const ScenDev sc = a.scen[a.scen_of[i]];
