@@ -265,6 +265,12 @@ __global__ void k_adj_seed(AdjArgs q) {
         const double dt = *q.dt;
         const double m = q.mass[i];
         double lxx = q.lx[2 * i], lxy = q.lx[2 * i + 1];
+        if (q.gtarget) {                   // the step's loss term: lx += scale 2 (x' - target)
+            lxx += q.gscale * 2.0 * (q.gx[i] - q.gtarget[2 * i]);
+            lxy += q.gscale * 2.0 * (q.gy[i] - q.gtarget[2 * i + 1]);
+            q.lx_rw[2 * i] = lxx;
+            q.lx_rw[2 * i + 1] = lxy;
+        }
         double lvtx = q.lv[2 * i] + lxx * dt, lvty = q.lv[2 * i + 1] + lxy * dt;
         double c1 = dt / (2.0 * m), c2 = dt * dt / (2.0 * m);
         double Fx = q.fx[i], Fy = q.fy[i];
@@ -319,16 +325,6 @@ __global__ void k_loss(const double *x, const double *y, const double *target, i
         const double t = ordered_sum(partial, gridDim.x);
         if (threadIdx.x == 0) *loss += t * scale;
     }
-}
-
-// lx += scale * 2 (x - target)
-__global__ void k_loss_grad(const double *x, const double *y, const double *target, int n,
-                            double scale, double *lx) {
-    pdl_enter();
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    lx[2 * i] += scale * 2.0 * (x[i] - target[2 * i]);
-    lx[2 * i + 1] += scale * 2.0 * (y[i] - target[2 * i + 1]);
 }
 
 // Adjusting term (F = (m / tau_adj) (v0 e0 - v)) and the agent's outputs.
@@ -735,9 +731,4 @@ void launch_loss(const double *x, const double *y, const double *target, int n, 
     k_loss<<<adj_partials(n), RED_NT, 0, s>>>(x, y, target, n, partial, loss, scale, blocks_done,
                                               dt_src, dt_dst);
 }
-void launch_loss_grad(const double *x, const double *y, const double *target, int n,
-                      double scale, double *lx, cudaStream_t s, bool dep) {
-    if (n > 0) launch_k(dep, k_loss_grad, nblk(n, RED_NT), RED_NT, 0, s, x, y, target, n, scale, lx);
-}
-
 }  // namespace cdk

@@ -1772,11 +1772,9 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
             }
             for (int64_t t = t1 - 1; t >= t0; --t) {
                 const double *after = seg + (size_t)(t + 1 - t0) * snap;
-                // the segment's first reverse step follows a wait on the other stream
-                cdk::launch_loss_grad(after, after + n, tgt + (size_t)t * 2 * n, (int)n, scale, lx,
-                                      st, t != t1 - 1);
-                // after k_loss_grad: chained to it
-                if ((rc = copy_state(c, seg + (size_t)(t - t0) * snap, false, true))) break;
+                // chained to the reverse step before it; the segment's first
+                // reverse step follows a wait on the other stream
+                if ((rc = copy_state(c, seg + (size_t)(t - t0) * snap, false, t != t1 - 1))) break;
                 StepArgs a = args_of(c, fnodes);
                 if (use_snaps) {
                     // the recomputation's cell list and near lists of the state before step t
@@ -1798,6 +1796,11 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
                 q.fpx = c->col[cdk::FPX];
                 q.fpy = c->col[cdk::FPY];
                 q.lx = lx; q.lv = lv; q.lfp = lfp;
+                q.gx = after;                               // the step's loss term
+                q.gy = after + n;
+                q.gtarget = tgt + (size_t)t * 2 * n;
+                q.gscale = scale;
+                q.lx_rw = lx;
                 q.lF = lF; q.lvt = lvt; q.lfp_out = lfp2;
                 q.lx_out = lx2; q.lv_out = lv2;
                 q.partial = partial;

@@ -179,6 +179,11 @@ struct AdjArgs {
     const double *vnx, *vny;               // velocity after the step
     const double *fpx, *fpy;               // force_prev before the step
     const double *lx, *lv, *lfp;           // incoming adjoints of x', v', fp'
+    // this step's loss term, added to the incoming x' adjoint by k_adj_seed
+    // (lx += scale 2 (x' - target), written back to lx_rw = lx); gtarget null: none
+    const double *gx, *gy, *gtarget;       // positions after the step, their target
+    double gscale;
+    double *lx_rw;
     double *lF, *lvt, *lfp_out;            // adjoint of F, of v' incl. x', of fp
     double *lx_out, *lv_out;               // outgoing adjoints of x, v
     double *partial, *ldt;                 // dt adjoint (block partials, total)
@@ -198,8 +203,6 @@ void launch_adj_dt(const AdjArgs &q, double dt_min, double dt_max, const double 
 void launch_loss(const double *x, const double *y, const double *target, int n,
                  double *partial, double *loss, double scale, int *blocks_done,
                  const double *dt_src, double *dt_dst, cudaStream_t s);
-void launch_loss_grad(const double *x, const double *y, const double *target, int n,
-                      double scale, double *lx, cudaStream_t s, bool dep = true);
 // Up to 16 device-to-device copies in one launch (byte counts multiples of 4).
 void launch_copy_bufs(const void *const *src, void *const *dst, const long long *bytes, int nbuf,
                       cudaStream_t s);
