@@ -260,6 +260,12 @@ __device__ void wall_circ_vjp(const Circ &A, const double *w, double ux, double 
 __global__ void k_adj_seed(AdjArgs q) {
     pdl_enter();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0 && q.work_zero) {           // the reverse pair kernels' counters
+        q.work_zero[0] = 0;
+        q.work_zero[1] = 0;
+        q.work_zero[2] = 0;
+        q.work_zero[3] = 0;
+    }
     double s = 0.0;
     if (i < q.n) {
         const double dt = *q.dt;

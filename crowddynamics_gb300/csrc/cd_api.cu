@@ -1780,7 +1780,7 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
                     // the recomputation's cell list and near lists of the state before step t
                     snap_args(a, snl, snapbuf + ((size_t)(sgi & 1) * ckpt + (t - t0)) * snl.total,
                               std::min<int64_t>(c->nl_cap, shadow->nl_cap));
-                    CUDA_OR_FAIL(c, cudaMemsetAsync(c->work, 0, 4 * sizeof(int), st));
+                    // the work counters are zeroed by k_adj_seed (k_nl_fill does not run)
                 } else {
                     enqueue_cells(c, a);                    // cell list of the state before step t
                     cdk::launch_near_lists(a, st);          // and its near lists
@@ -1801,6 +1801,7 @@ extern "C" int cd_rollout_loss(cd_ctx *c, int64_t steps, const double *target, i
                 q.gtarget = tgt + (size_t)t * 2 * n;
                 q.gscale = scale;
                 q.lx_rw = lx;
+                q.work_zero = use_snaps ? c->work : nullptr;
                 q.lF = lF; q.lvt = lvt; q.lfp_out = lfp2;
                 q.lx_out = lx2; q.lv_out = lv2;
                 q.partial = partial;

@@ -184,6 +184,7 @@ struct AdjArgs {
     const double *gx, *gy, *gtarget;       // positions after the step, their target
     double gscale;
     double *lx_rw;
+    int *work_zero;                        // StepArgs::work, zeroed by k_adj_seed (null: not)
     double *lF, *lvt, *lfp_out;            // adjoint of F, of v' incl. x', of fp
     double *lx_out, *lv_out;               // outgoing adjoints of x, v
     double *partial, *ldt;                 // dt adjoint (block partials, total)
